@@ -1,0 +1,344 @@
+"""Benchmark: compartment-steps/s of the batched uneven HH cable population.
+
+Workload (config 2): 16,384 HH cables with odd compartment counts U[51, 401]
+(3.70 M compartments), float32 state, extracellular point-source stimulation
+(cathodic 0.1 ms pulse), dt 0.005 ms for 10 ms = 2000 timesteps.  One bench
+"step" is one full 2000-timestep run of the whole population: a single
+persistent launch of dgb_cable_run.
+
+Usage:  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line.  ``value`` is timed with CUDA events on the launching
+stream with inputs resident in HBM; ``e2e`` is the same metric through the
+public API from pinned host buffers (state + prepared workspace in, spike
+results + final voltages out, copies inside the timed region).  The reference
+arm (``--impl reference``) times the CPU restatement of the reference's
+PyTorch CPU cable solver (oracle port) on all host cores on a bounded sample.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "compartment-steps/s"
+ALG_BYTES_PER_COMP_STEP = 48  # unfused per-step traffic of one float32 compartment-step
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(n_sample: int, steps: int, threads: int | None = None):
+    """Oracle port of the reference CPU cable update on a config-2 subsample."""
+    import torch
+
+    import oracle
+    from dendra_gb300.workloads import cable_population_c2
+
+    rng = np.random.default_rng(99)
+    subset = np.sort(rng.choice(16384, n_sample, replace=False))
+    pop = cable_population_c2(dtype=torch.float32, device="cpu", subset=subset)
+    p = pop.problem_dict()
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
+    oracle.cable_run(p, steps)
+    dt = time.perf_counter() - t0
+    return pop.N * steps / dt, pop.N, dt, oracle.num_threads()
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    n_sample = args.sample
+    steps = 2000
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(max(8, n_sample // 8), 50)
+    last = None
+    for _ in range(args.steps):
+        v, n_comp, secs, cores = cpu_baseline(n_sample, steps)
+        vals.append(v)
+        last = (n_comp, secs, cores)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": last[1] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "c2-uneven-hh-cables-extracellular", "n_cables": 16384,
+                   "k_range": [51, 401], "dt_ms": 0.005, "timesteps": steps,
+                   "sample_cables": n_sample},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": last[2], "kind": "port",
+                         "sample": f"{n_sample} of 16384 cables ({last[0]} compartments) x "
+                                   f"{steps} timesteps, float32, per bench step"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--sample", type=int, default=512, help="CPU baseline cables")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = _dist()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    import torch
+
+    import dendra_gb300
+    from dendra_gb300.workloads import C2_STEPS, cable_population_c2
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    dendra_gb300.load()
+
+    # each rank owns an independent shard of cables (weak scaling, no collective)
+    pop = cable_population_c2(dtype=torch.float32, device=dev, seed=2024 + rank)
+    comp_steps = pop.N * C2_STEPS
+    v0, m0, h0, n0 = (t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
+
+    def reset():
+        pop.v.copy_(v0)
+        pop.m.copy_(m0)
+        pop.h.copy_(h0)
+        pop.n.copy_(n0)
+        pop.step_index = 0
+
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+
+    def one(spk=False):
+        reset()
+        return pop.run(C2_STEPS, spk_idx=0 if spk else None)
+
+    for _ in range(max(3, args.warmup)):
+        one()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    times = []
+    with ClockSampler(local) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            reset()
+            flush.fill_(1.0)  # evict L2 between timed steps (outside the events)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            pop.run(C2_STEPS)
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        barrier()
+    ms = float(np.mean(times))
+    if pg is not None:
+        t = torch.tensor([ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+        n = torch.tensor([comp_steps], dtype=torch.float64, device=dev)
+        pg.all_reduce(n)
+        total_units = float(n.item())
+    else:
+        total_units = float(comp_steps)
+    value = total_units / (ms * 1e-3)
+
+    # ---- end-to-end through the public API from pinned host buffers ----
+    host_in = {k: v.detach().cpu().pin_memory() for k, v in pop._dev.items()}
+    host_state = {k: t.cpu().pin_memory() for k, t in (("v", v0), ("m", m0), ("h", h0), ("n", n0))}
+    h2d = sum(t.numel() * t.element_size() for t in host_in.values())
+    h2d += sum(t.numel() * t.element_size() for t in host_state.values())
+    out_v = torch.empty(pop.N, dtype=pop.dtype).pin_memory()
+    out_cnt = torch.empty(pop.B, dtype=torch.int32).pin_memory()
+    out_first = torch.empty(pop.B, dtype=torch.int32).pin_memory()
+    d2h = sum(t.numel() * t.element_size() for t in (out_v, out_cnt, out_first))
+
+    def e2e_step():
+        for k, t in host_in.items():
+            pop._dev[k].copy_(t, non_blocking=True)
+        for k, t in host_state.items():
+            getattr(pop, k).copy_(t, non_blocking=True)
+        pop.step_index = 0
+        res = pop.run(C2_STEPS, spk_idx=0)
+        out_v.copy_(pop.v, non_blocking=True)
+        out_cnt.copy_(res.spk_count, non_blocking=True)
+        out_first.copy_(res.spk_first, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if pg is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = total_units / (e2e_ms * 1e-3)
+    n_spiking = int((out_cnt > 0).sum())
+
+    # ---- the plain per-step path (assemble + solve/update per timestep) ----
+    plain = None
+    if not args.no_plain:
+        reset()
+        bands = torch.empty((4, pop.N), dtype=pop.dtype, device=dev)
+        for _ in range(3):
+            pop.step_plain(bands)
+        reset()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        n_plain = 200
+        e0.record(st)
+        for _ in range(n_plain):
+            pop.step_plain(bands)
+        e1.record(st)
+        e1.synchronize()
+        pms = e0.elapsed_time(e1) / n_plain
+        plain = {"value": pop.N / (pms * 1e-3), "unit": METRIC, "ms_per_timestep": pms,
+                 "timesteps_timed": n_plain,
+                 "what": "dgb_cable_assemble + dgb_cable_solve_update per timestep (2 launches)"}
+
+    peak, peak_kind = _peaks()
+    achieved = ALG_BYTES_PER_COMP_STEP * comp_steps / (ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c2-uneven-hh-cables-extracellular", "n_cables": 16384 * world,
+                   "compartments_per_rank": pop.N, "k_range": [51, 401], "dt_ms": 0.005,
+                   "timesteps": C2_STEPS, "state_dtype": "float32",
+                   "l2": "flushed between timed steps (256 MiB write, outside the events)",
+                   "launch": "one persistent dgb_cable_run launch per step"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": (f"achieved = {ALG_BYTES_PER_COMP_STEP} algorithmic B per "
+                              f"compartment-step of the unfused update x {comp_steps} "
+                              f"compartment-steps / launch time; peak {peak_kind} copy "
+                              "bandwidth; the persistent kernel keeps state on chip")},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+        "gpu_launches": args.steps,
+        "clocks": clocks.summary(),
+        "cables_spiking": n_spiking,
+    }
+    if plain is not None:
+        line["plain_gpu"] = plain
+        line["speedup_vs_plain_gpu"] = value / plain["value"]
+        line["gpu_launches"] += 0  # plain path runs outside the timed region
+    if rank == 0 and not args.no_cpu:
+        v, n_comp, secs, cores = cpu_baseline(args.sample, 200)
+        line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
+                                "sample": f"{args.sample} of 16384 cables ({n_comp} "
+                                          f"compartments) x 200 timesteps, float32"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

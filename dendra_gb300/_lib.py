@@ -1,0 +1,119 @@
+"""ctypes binding of the C ABI in ``include/dendra_gb300.h``.
+
+The library is the only compute path: if it cannot be built or loaded the
+import of a kernel-facing function raises, there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+F32 = 0
+F64 = 1
+THOMAS = 0
+PCR = 1
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_INT = ctypes.c_int
+
+
+class DgbError(RuntimeError):
+    """A dendra_gb300 C-ABI call returned an error code."""
+
+
+class CableArgs(ctypes.Structure):
+    """Mirror of ``dgb_cable_args`` (field order and types must match)."""
+
+    _fields_ = [
+        ("dtype", _I32), ("n_cables", _I32), ("n_steps", _I32), ("rec_every", _I32),
+        ("cable_ptr", _P), ("order", _P),
+        ("v", _P), ("m", _P), ("h", _P), ("n", _P),
+        ("g_right", _P), ("g_left", _P), ("scale", _P), ("cm_inv", _P), ("field", _P),
+        ("gnabar", _P), ("gkbar", _P), ("gl", _P), ("el", _P),
+        ("ena", _D), ("ek", _D), ("q10", _D), ("dt_ms", _D), ("dt_s", _D), ("t0_ms", _D),
+        ("step0", _I64),
+        ("ve_amp", _P), ("ve_delay", _P), ("ve_pw", _P),
+        ("in_idx", _P), ("in_amp", _P), ("in_delay", _P), ("in_pw", _P),
+        ("rec_idx", _P), ("trace", _P),
+        ("spk_idx", _P), ("spk_thr", _D), ("spk_below", _P), ("spk_count", _P),
+        ("spk_first", _P),
+        ("max_k", _I32), ("lanes", _I32), ("n_comp", _I64),
+        ("comp_cable", _P), ("scratch", _P),
+    ]
+
+
+# name -> (restype, argtypes); every symbol declared in include/dendra_gb300.h
+SIGNATURES = {
+    "dgb_version": (ctypes.c_char_p, []),
+    "dgb_last_error": (ctypes.c_char_p, []),
+    "dgb_cable_args_size": (ctypes.c_size_t, []),
+    "dgb_tridiag_solve": (_INT, [_INT, _INT, _I64, _I64, _P, _P, _P, _P, _P, _P]),
+    "dgb_tridiag_solve_lanes": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _I32, _P]),
+    "dgb_tridiag_solve_transpose": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P]),
+    "dgb_cable_run": (_INT, [ctypes.POINTER(CableArgs), _P]),
+    "dgb_cable_assemble": (_INT, [ctypes.POINTER(CableArgs), _I32, _P, _P, _P, _P, _P]),
+    "dgb_cable_solve_update": (_INT, [ctypes.POINTER(CableArgs), _P, _P, _P, _P, _P]),
+}
+
+
+def _declare(L):
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def path() -> str:
+    return _build.LIB
+
+
+def load():
+    """Build (if stale) and load the CUDA library; raise if that fails."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            try:
+                so = _build.build()
+            except Exception as exc:  # no silent fallback: the kernels are the product
+                raise DgbError(f"dendra_gb300 CUDA library could not be built: {exc}") from exc
+            if not os.path.exists(so):
+                raise DgbError(f"dendra_gb300 CUDA library missing at {so}")
+            L = ctypes.CDLL(so)
+            _declare(L)
+            _lib = L
+    return _lib
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        msg = load().dgb_last_error().decode(errors="replace")
+        kind = {-1: ValueError, -4: ValueError}.get(rc)
+        if kind is not None:
+            raise kind(f"{what}: {msg}")
+        raise DgbError(f"{what} failed (code {rc}): {msg}")
+
+
+def stream_ptr(device=None) -> int:
+    import torch
+
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def dtype_code(dtype) -> int:
+    import torch
+
+    if dtype == torch.float32:
+        return F32
+    if dtype == torch.float64:
+        return F64
+    raise TypeError("dendra_gb300 kernels support only float32 and float64")

@@ -1,0 +1,33 @@
+// Library-wide C-ABI helpers: version, last error, device properties.
+#include <stdarg.h>
+
+#include "common.cuh"
+
+namespace dgb {
+
+static thread_local char g_last_error[512] = {0};
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+  va_end(ap);
+}
+
+void clear_error() { g_last_error[0] = 0; }
+
+int device_sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
+  return n > 0 ? n : 1;
+}
+
+}  // namespace dgb
+
+extern "C" const char* dgb_version(void) { return "dendra_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" const char* dgb_last_error(void) { return dgb::g_last_error; }
+
+// Size of dgb_cable_args as compiled, so bindings can check their mirror.
+extern "C" size_t dgb_cable_args_size(void) { return sizeof(dgb_cable_args); }

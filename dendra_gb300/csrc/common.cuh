@@ -1,0 +1,189 @@
+// Shared device/host helpers for the dendra_gb300 kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "../../include/dendra_gb300.h"
+
+namespace dgb {
+
+// ---------------------------------------------------------------------------
+// Host-side error reporting (thread-local last error message).
+// ---------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+void clear_error();
+
+#define DGB_REQUIRE(cond, ...)        \
+  do {                                \
+    if (!(cond)) {                    \
+      ::dgb::set_error(__VA_ARGS__);  \
+      return DGB_EINVAL;              \
+    }                                 \
+  } while (0)
+
+#define DGB_CUDA_CHECK(expr)                                                   \
+  do {                                                                         \
+    cudaError_t _e = (expr);                                                   \
+    if (_e != cudaSuccess) {                                                   \
+      ::dgb::set_error("%s failed: %s", #expr, cudaGetErrorString(_e));        \
+      return DGB_ECUDA;                                                        \
+    }                                                                          \
+  } while (0)
+
+#define DGB_LAUNCH_CHECK()                                                     \
+  do {                                                                         \
+    cudaError_t _e = cudaGetLastError();                                       \
+    if (_e != cudaSuccess) {                                                   \
+      ::dgb::set_error("kernel launch failed: %s (%s:%d)",                     \
+                       cudaGetErrorString(_e), __FILE__, __LINE__);            \
+      return DGB_ECUDA;                                                        \
+    }                                                                          \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int device_sm_count();
+
+// ---------------------------------------------------------------------------
+// dtype-specific HH arithmetic.  Branch thresholds and polynomial degrees
+// follow the reference per dtype:
+//   vtrap/exprelr  dendra/models/mechanisms/ops.py:13-125
+//   phi1           dendra/models/mechanisms/_cnexp.py:46-93
+//   rates          dendra/models/mod/HH.py:24-40
+//   cnexp step     dendra/models/mechanisms/_cnexp.py:96-132
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Math;
+
+template <>
+struct Math<float> {
+  static __device__ __forceinline__ float ex(float x) { return expf(x); }
+  static __device__ __forceinline__ float fabs_(float x) { return fabsf(x); }
+  static constexpr float kVtrapLocal = 1.0f;
+  static __device__ __forceinline__ float even_series(float q) {
+    float q2 = q * q;
+    float value = q2 * (float)(-691.0 / 1307674368000.0) + (float)(1.0 / 47900160.0);
+    value = value * q2 - (float)(1.0 / 1209600.0);
+    value = value * q2 + (float)(1.0 / 30240.0);
+    value = value * q2 - (float)(1.0 / 720.0);
+    value = value * q2 + (float)(1.0 / 12.0);
+    return value;
+  }
+  static __device__ __forceinline__ float phi1(float z) {
+    float value = z * (float)(1.0 / 3628800.0) + (float)(1.0 / 362880.0);
+    value = value * z + (float)(1.0 / 40320.0);
+    value = value * z + (float)(1.0 / 5040.0);
+    value = value * z + (float)(1.0 / 720.0);
+    value = value * z + (float)(1.0 / 120.0);
+    value = value * z + (float)(1.0 / 24.0);
+    value = value * z + (float)(1.0 / 6.0);
+    value = value * z + 0.5f;
+    value = value * z + 1.0f;
+    return value;
+  }
+};
+
+template <>
+struct Math<double> {
+  static __device__ __forceinline__ double ex(double x) { return exp(x); }
+  static __device__ __forceinline__ double fabs_(double x) { return fabs(x); }
+  static constexpr double kVtrapLocal = 0.5;
+  static __device__ __forceinline__ double even_series(double q) {
+    double q2 = q * q;
+    double value = q2 * (43867.0 / 5109094217170944000.0) - 3617.0 / 10670622842880000.0;
+    value = value * q2 + 1.0 / 74724249600.0;
+    value = value * q2 - 691.0 / 1307674368000.0;
+    value = value * q2 + 1.0 / 47900160.0;
+    value = value * q2 - 1.0 / 1209600.0;
+    value = value * q2 + 1.0 / 30240.0;
+    value = value * q2 - 1.0 / 720.0;
+    value = value * q2 + 1.0 / 12.0;
+    return value;
+  }
+  static __device__ __forceinline__ double phi1(double z) {
+    double value = z * (1.0 / 355687428096000.0) + 1.0 / 20922789888000.0;
+    value = value * z + 1.0 / 1307674368000.0;
+    value = value * z + 1.0 / 87178291200.0;
+    value = value * z + 1.0 / 6227020800.0;
+    value = value * z + 1.0 / 479001600.0;
+    value = value * z + 1.0 / 39916800.0;
+    value = value * z + 1.0 / 3628800.0;
+    value = value * z + 1.0 / 362880.0;
+    value = value * z + 1.0 / 40320.0;
+    value = value * z + 1.0 / 5040.0;
+    value = value * z + 1.0 / 720.0;
+    value = value * z + 1.0 / 120.0;
+    value = value * z + 1.0 / 24.0;
+    value = value * z + 1.0 / 6.0;
+    value = value * z + 0.5;
+    value = value * z + 1.0;
+    return value;
+  }
+};
+
+// x / (exp(x/y) - 1) with the local Bernoulli branch.
+template <typename T>
+__device__ __forceinline__ T vtrap(T x, T y) {
+  T q = x / y;
+  if (Math<T>::fabs_(q) <= Math<T>::kVtrapLocal) {
+    T even = Math<T>::even_series(q);
+    return (y - x / T(2)) + x * (q * even);
+  }
+  return x / (Math<T>::ex(q) - T(1));
+}
+
+// Exact affine step of x' = a - b x over dt.
+template <typename T>
+__device__ __forceinline__ T cnexp_step(T x, T a, T b, T dt) {
+  T rate = a - b * x;
+  T coef = -b;
+  T z = coef * dt;
+  if (Math<T>::fabs_(z) <= T(0.5)) {
+    return x + dt * rate * Math<T>::phi1(z);
+  }
+  T eq = -a / coef;
+  return eq + (x - eq) * Math<T>::ex(z);
+}
+
+// Rate constants am1 = 0.1, ah1 = 0.07, an1 = 0.01: the reference keeps its
+// mechanism GLOBALs as float32 values even in float64 models, so these are the
+// float32-rounded values in both precisions (am2 = 4, ah2 = 1, an2 = 0.125 are
+// exact either way).
+// Advance m, h, n by one cnexp step using the rates at voltage v.
+template <typename T>
+__device__ __forceinline__ void hh_gates(T v, T q10, T dt, T& m, T& h, T& n) {
+  T alpha_m = T(0.1f) * vtrap<T>(-(v + T(40)), T(10));
+  T beta_m = T(4.0) * Math<T>::ex(-(v + T(65)) / T(18));
+  T alpha_h = T(0.07f) * Math<T>::ex(-(v + T(65)) / T(20));
+  T beta_h = T(1.0) / (Math<T>::ex(-(v + T(35)) / T(10)) + T(1));
+  T alpha_n = T(0.01f) * vtrap<T>(-(v + T(55)), T(10));
+  T beta_n = T(0.125) * Math<T>::ex(-(v + T(65)) / T(80));
+  m = cnexp_step<T>(m, q10 * alpha_m, q10 * (alpha_m + beta_m), dt);
+  h = cnexp_step<T>(h, q10 * alpha_h, q10 * (alpha_h + beta_h), dt);
+  n = cnexp_step<T>(n, q10 * alpha_n, q10 * (alpha_n + beta_n), dt);
+}
+
+// HH affine membrane terms (HH.py:109-116): G = gl + gna + gk, J = gl el + gna ena + gk ek.
+template <typename T>
+__device__ __forceinline__ void hh_affine(T m, T h, T n, T gnabar, T gkbar, T gl, T el,
+                                          T ena, T ek, T& G, T& J) {
+  T m3 = m * m * m;
+  T n2 = n * n;
+  T gna = gnabar * m3 * h;
+  T gk = gkbar * (n2 * n2);
+  G = gl + gna + gk;
+  J = gl * el + gna * ena + gk * ek;
+}
+
+// Rectangular pulse amp on [delay, delay + pw).
+template <typename T>
+__device__ __forceinline__ T rect_pulse(T t, T amp, T delay, T pw) {
+  T stop = delay + pw;
+  return (t >= delay && t < stop) ? amp : T(0);
+}
+
+}  // namespace dgb

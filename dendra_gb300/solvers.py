@@ -1,0 +1,140 @@
+"""Solver callables with the reference's signatures, backed by sm_103a kernels.
+
+Drop-ins for the solver objects ``_bwd_euler_ub._select_solver`` installs as
+``self._solve`` (dendra/models/integrators/implicit.py:364-440):
+
+* :func:`thomas_solve_cuda_t` — replaces triton/t_kernel_thomas.py:218-232
+* :func:`pcr_solve_cuda_t`    — replaces triton/pcr_kernel_thomas.py:199-226
+
+Both take ``a (B,K-1), b (B,K), c (B,K-1), d (B,K)`` CUDA tensors of one float
+dtype and return a fresh ``x (B,K)``.  Gradients follow the reference's
+``ThomasSolve.backward`` (t_kernel_thomas.py:147-189): one transpose solve
+``A^T y = grad_x`` on the kernel, then ``grad_b = -y x``,
+``grad_a = -y[:,1:] x[:,:-1]``, ``grad_c = -y[:,:-1] x[:,1:]``.
+Argument checks raise the reference's exception types and messages
+(triton/_contracts.py:87-159).
+"""
+
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+
+_FLOAT_DTYPES = (torch.float32, torch.float64)
+
+
+def _validate_float_group(named):
+    first_name, first = named[0]
+    if first.device.type != "cuda":
+        raise ValueError("Triton solver inputs must be CUDA tensors")
+    if first.dtype not in _FLOAT_DTYPES:
+        raise TypeError("Triton solvers support only float32 and float64")
+    for name, tensor in named[1:]:
+        if tensor.device != first.device:
+            raise ValueError(
+                f"{name} must be on the same device as {first_name}; "
+                f"got {tensor.device} and {first.device}"
+            )
+        if tensor.dtype != first.dtype:
+            raise ValueError(
+                f"{name} must have the same dtype as {first_name}; "
+                f"got {tensor.dtype} and {first.dtype}"
+            )
+
+
+def validate_tridiagonal(a, b, c, d):
+    """Shape/dtype/device contract of a batched scalar tridiagonal solve."""
+    named = (("a", a), ("b", b), ("c", c), ("d", d))
+    for name, t in named:
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{name} must be a torch.Tensor")
+    if b.ndim != 2:
+        raise ValueError(f"b must have shape (B, K), got {tuple(b.shape)}")
+    batch, size = map(int, b.shape)
+    if batch < 1 or size < 1:
+        raise ValueError("B and K must both be >= 1")
+    band = (batch, size - 1)
+    if tuple(a.shape) != band:
+        raise ValueError(f"a must have shape {band}, got {tuple(a.shape)}")
+    if tuple(c.shape) != band:
+        raise ValueError(f"c must have shape {band}, got {tuple(c.shape)}")
+    if tuple(d.shape) != (batch, size):
+        raise ValueError(f"d must have shape {(batch, size)}, got {tuple(d.shape)}")
+    _validate_float_group(named)
+    return batch, size
+
+
+def _solve(a, b, c, d, method, lanes=0):
+    B, K = b.shape
+    a, b, c, d = (t.contiguous() for t in (a, b, c, d))
+    x = torch.empty_like(d)
+    L = _lib.load()
+    with torch.cuda.device(d.device):
+        st = _lib.stream_ptr(d.device)
+        if lanes:
+            rc = L.dgb_tridiag_solve_lanes(_lib.dtype_code(d.dtype), B, K, a.data_ptr(),
+                                           b.data_ptr(), c.data_ptr(), d.data_ptr(),
+                                           x.data_ptr(), int(lanes), st)
+        else:
+            rc = L.dgb_tridiag_solve(_lib.dtype_code(d.dtype), method, B, K, a.data_ptr(),
+                                     b.data_ptr(), c.data_ptr(), d.data_ptr(), x.data_ptr(), st)
+    _lib.check(rc, "dgb_tridiag_solve")
+    return x
+
+
+def _solve_transpose(a, b, c, g):
+    B, K = b.shape
+    a, b, c, g = (t.contiguous() for t in (a, b, c, g))
+    y = torch.empty_like(g)
+    L = _lib.load()
+    with torch.cuda.device(g.device):
+        rc = L.dgb_tridiag_solve_transpose(_lib.dtype_code(g.dtype), B, K, a.data_ptr(),
+                                           b.data_ptr(), c.data_ptr(), g.data_ptr(),
+                                           y.data_ptr(), _lib.stream_ptr(g.device))
+    _lib.check(rc, "dgb_tridiag_solve_transpose")
+    return y
+
+
+class _TridiagSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, a, b, c, d, method):
+        x = _solve(a, b, c, d, method)
+        ctx.save_for_backward(a, b, c, x)
+        return x
+
+    @staticmethod
+    def backward(ctx, grad_x):
+        a, b, c, x = ctx.saved_tensors
+        need = ctx.needs_input_grad
+        if not any(need[:4]):
+            return None, None, None, None, None
+        y = _solve_transpose(a, b, c, grad_x)
+        grad_a = -y[:, 1:] * x[:, :-1] if need[0] else None
+        grad_b = -y * x if need[1] else None
+        grad_c = -y[:, :-1] * x[:, 1:] if need[2] else None
+        grad_d = y if need[3] else None
+        return grad_a, grad_b, grad_c, grad_d, None
+
+
+def thomas_solve_cuda_t(a, b, c, d):
+    """Batched tridiagonal solve (drop-in for the reference's Triton Thomas)."""
+    validate_tridiagonal(a, b, c, d)
+    return _TridiagSolve.apply(a, b, c, d, _lib.THOMAS)
+
+
+def pcr_solve_cuda_t(a, b, c, d):
+    """Batched tridiagonal solve (drop-in for the reference's Triton PCR)."""
+    validate_tridiagonal(a, b, c, d)
+    return _TridiagSolve.apply(a, b, c, d, _lib.PCR)
+
+
+def tridiag_solve_lanes(a, b, c, d, lanes: int):
+    """Forward-only solve with an explicit lanes-per-system split (autotuner)."""
+    validate_tridiagonal(a, b, c, d)
+    return _solve(a, b, c, d, _lib.THOMAS, lanes=lanes)
+
+
+# The increment-RHS contract is granted to these solver identities only
+# (mirrors _BWD_EULER_INCREMENT_SOLVERS, integrators/implicit.py:59-82).
+INCREMENT_SOLVERS = (thomas_solve_cuda_t, pcr_solve_cuda_t)

@@ -1,0 +1,216 @@
+"""ctypes bindings of the C oracle — TEST INFRASTRUCTURE ONLY.
+
+Builds ``oracle.c`` with gcc into ``oracle/_build/liboracle.so`` on first use
+(the build is plain C with OpenMP; no reference sources are compiled).
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_SO = os.path.join(_BUILD, "liboracle.so")
+_SRC = [os.path.join(_HERE, "oracle.c"), os.path.join(_HERE, "oracle_impl.h")]
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library if it is missing or stale."""
+    os.makedirs(_BUILD, exist_ok=True)
+    stale = not os.path.exists(_SO) or any(
+        os.path.getmtime(s) > os.path.getmtime(_SO) for s in _SRC
+    )
+    if force or stale:
+        tmp = _SO + f".tmp{os.getpid()}"
+        cmd = [
+            "gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+            "-fno-fast-math", "-o", tmp, _SRC[0], "-lm",
+        ]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, _SO)
+    return _SO
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            _lib = ctypes.CDLL(build())
+            _declare(_lib)
+    return _lib
+
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_D = ctypes.c_double
+
+
+def _declare(L):
+    for sfx, real in (("_f64", ctypes.c_double), ("_f32", ctypes.c_float)):
+        getattr(L, "orc_vtrap" + sfx).restype = real
+        getattr(L, "orc_vtrap" + sfx).argtypes = [real, real]
+        getattr(L, "orc_phi1" + sfx).restype = real
+        getattr(L, "orc_phi1" + sfx).argtypes = [real]
+        getattr(L, "orc_cnexp" + sfx).restype = real
+        getattr(L, "orc_cnexp" + sfx).argtypes = [real, real, real, real]
+        getattr(L, "orc_hh_rates" + sfx).argtypes = [real, real, _P]
+        getattr(L, "orc_hh_steady" + sfx).argtypes = [real, _P]
+        getattr(L, "orc_thomas_batched" + sfx).argtypes = [_I64, _I64, _P, _P, _P, _P, _P]
+        getattr(L, "orc_pcr" + sfx).argtypes = [_I64, _P, _P, _P, _P, _P]
+        getattr(L, "orc_dhs_solve_batched" + sfx).argtypes = [
+            _I64, _I64, _P, _P, _P, _P, _P, _P, _I32, _P]
+        getattr(L, "orc_cable_run" + sfx).argtypes = (
+            [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
+            + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P]
+        )
+    L.orc_num_threads.restype = ctypes.c_int
+
+
+def _sfx(dtype) -> str:
+    dtype = np.dtype(dtype)
+    if dtype == np.float64:
+        return "_f64"
+    if dtype == np.float32:
+        return "_f32"
+    raise TypeError(f"oracle supports float32/float64, got {dtype}")
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def num_threads() -> int:
+    return int(lib().orc_num_threads())
+
+
+def vtrap(x, y, dtype=np.float64):
+    f = getattr(lib(), "orc_vtrap" + _sfx(dtype))
+    return np.array([f(float(a), float(b)) for a, b in np.broadcast(x, y)], dtype=dtype)
+
+
+def phi1(z, dtype=np.float64):
+    f = getattr(lib(), "orc_phi1" + _sfx(dtype))
+    return np.array([f(float(a)) for a in np.ravel(z)], dtype=dtype)
+
+
+def hh_rates(v, q10=1.0, dtype=np.float64):
+    """Return (len(v), 6) rates m_a, m_b, h_a, h_b, n_a, n_b."""
+    f = getattr(lib(), "orc_hh_rates" + _sfx(dtype))
+    v = np.ravel(np.asarray(v, dtype=dtype))
+    out = np.empty((v.size, 6), dtype=dtype)
+    for i, vi in enumerate(v):
+        f(float(vi), float(q10), out[i].ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+def hh_steady(v, dtype=np.float64):
+    f = getattr(lib(), "orc_hh_steady" + _sfx(dtype))
+    v = np.ravel(np.asarray(v, dtype=dtype))
+    out = np.empty((v.size, 3), dtype=dtype)
+    for i, vi in enumerate(v):
+        f(float(vi), out[i].ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+def cnexp(x, a, b, dt, dtype=np.float64):
+    f = getattr(lib(), "orc_cnexp" + _sfx(dtype))
+    return np.array(
+        [f(float(xi), float(ai), float(bi), float(dt)) for xi, ai, bi in np.broadcast(x, a, b)],
+        dtype=dtype,
+    )
+
+
+def thomas(a, b, c, d):
+    """Batched functional Thomas (reference pcr_solve_t) on (B,K) arrays."""
+    dtype = b.dtype
+    a, b, c, d = (np.ascontiguousarray(t, dtype=dtype) for t in (a, b, c, d))
+    B, K = b.shape
+    x = np.empty_like(d)
+    getattr(lib(), "orc_thomas_batched" + _sfx(dtype))(
+        B, K, _ptr(a), _ptr(b), _ptr(c), _ptr(d), _ptr(x))
+    return x
+
+
+def pcr(a, b, c, d):
+    """Batched PCR (reference pcr_solve_parallel_t) on (B,K) arrays."""
+    dtype = b.dtype
+    a, b, c, d = (np.ascontiguousarray(t, dtype=dtype) for t in (a, b, c, d))
+    B, K = b.shape
+    x = np.empty_like(d)
+    f = getattr(lib(), "orc_pcr" + _sfx(dtype))
+    for i in range(B):
+        f(K, _ptr(a[i]), _ptr(b[i]), _ptr(c[i]), _ptr(d[i]), _ptr(x[i]))
+    return x
+
+
+def dhs_solve(d, a, b, parent, order, layer_ptr):
+    """Sequential DHS solve of (B,K) systems in solver order."""
+    dtype = d.dtype
+    d, a, b = (np.ascontiguousarray(t, dtype=dtype) for t in (d, a, b))
+    parent = np.ascontiguousarray(parent, dtype=np.int32)
+    order = np.ascontiguousarray(order, dtype=np.int32)
+    layer_ptr = np.ascontiguousarray(layer_ptr, dtype=np.int32)
+    B, K = d.shape
+    x = np.zeros_like(d)
+    getattr(lib(), "orc_dhs_solve_batched" + _sfx(dtype))(
+        B, K, _ptr(d), _ptr(a), _ptr(b), _ptr(parent), _ptr(order), _ptr(layer_ptr),
+        int(layer_ptr.size - 1), _ptr(x))
+    return x
+
+
+def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0):
+    """Run the HH cable update on a packed problem dict (see dendra_gb300.cable).
+
+    ``p`` holds numpy arrays: cable_ptr, v, m, h, n (modified in place),
+    g_right, g_left, scale, cm_inv, field (or None), gnabar, gkbar, gl, el,
+    ve_amp/ve_delay/ve_pw (or None), in_idx/in_amp/in_delay/in_pw (or None),
+    rec_idx, spk_idx, and scalars ena, ek, q10, dt_ms, dt_s, spk_thr.
+    Returns (trace, spk_count, spk_first, spk_below).
+    """
+    dtype = p["v"].dtype
+    sfx = _sfx(dtype)
+    B = int(p["cable_ptr"].size - 1)
+    n_rec = 1 + n_steps // rec_every
+    trace = np.full((B, n_rec), np.nan, dtype=dtype)
+    spk_below = p.get("spk_below")
+    if spk_below is None:
+        spk_below = np.ones(B, dtype=np.int32)
+    spk_count = np.zeros(B, dtype=np.int32)
+    spk_first = np.full(B, -1, dtype=np.int32)
+
+    def arr(name, dt=dtype):
+        x = p.get(name)
+        if x is None:
+            return None
+        y = np.ascontiguousarray(x, dtype=dt)
+        return y
+
+    keep = {k: arr(k) for k in ("g_right", "g_left", "scale", "cm_inv", "field", "gnabar",
+                                  "gkbar", "gl", "el", "ve_amp", "ve_delay", "ve_pw",
+                                  "in_amp", "in_delay", "in_pw")}
+    for k in ("in_idx", "rec_idx", "spk_idx"):
+        keep[k] = arr(k, np.int32)
+    cable_ptr = np.ascontiguousarray(p["cable_ptr"], dtype=np.int64)
+    getattr(lib(), "orc_cable_run" + sfx)(
+        B, int(n_steps), int(rec_every), _ptr(cable_ptr),
+        _ptr(p["v"]), _ptr(p["m"]), _ptr(p["h"]), _ptr(p["n"]),
+        _ptr(keep["g_right"]), _ptr(keep["g_left"]), _ptr(keep["scale"]),
+        _ptr(keep["cm_inv"]), _ptr(keep["field"]), _ptr(keep["gnabar"]),
+        _ptr(keep["gkbar"]), _ptr(keep["gl"]), _ptr(keep["el"]),
+        float(p["ena"]), float(p["ek"]), float(p["q10"]), float(p["dt_ms"]),
+        float(p["dt_s"]), float(t0_ms),
+        _ptr(keep["ve_amp"]), _ptr(keep["ve_delay"]), _ptr(keep["ve_pw"]),
+        _ptr(keep["in_idx"]), _ptr(keep["in_amp"]), _ptr(keep["in_delay"]),
+        _ptr(keep["in_pw"]), _ptr(keep["rec_idx"]), _ptr(trace),
+        _ptr(keep["spk_idx"]), float(p.get("spk_thr", 0.0)), _ptr(spk_below),
+        _ptr(spk_count), _ptr(spk_first),
+    )
+    return trace, spk_count, spk_first, spk_below

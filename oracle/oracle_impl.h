@@ -1,0 +1,406 @@
+/*
+ * CPU oracle for the Dendra cable update — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference algorithms, used by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the checker
+ * and CPU timing baseline.  It is never part of the product path.
+ *
+ * This file is included twice by oracle.c, once with REAL=double (suffix
+ * _f64) and once with REAL=float (suffix _f32), so that both precisions
+ * follow the reference's dtype-specific branches exactly.  It is compiled
+ * with -ffp-contract=off so each operation rounds like the reference's
+ * elementwise PyTorch kernels.
+ *
+ * Reference files (Dendra v0.30.1, paths relative to its source tree):
+ *   rates   dendra/models/mod/HH.py:24-40, dendra/models/mechanisms/ops.py:13-125
+ *   cnexp   dendra/models/mechanisms/_cnexp.py:46-132 (via ode.py:51-73)
+ *   current dendra/models/mod/HH.py:109-116
+ *   update  dendra/models/integrators/implicit.py:484-522 and :569-664
+ *   thomas  dendra/models/integrators/tridiag/pcr.py:125-183
+ *   pcr     dendra/models/integrators/tridiag/pcr.py:4-96
+ *   dhs     dendra/models/integrators/triton/dhs_kernel.py:14-112
+ *   pulse   dendra/models/stim/waveform/implementations.py:551-558,
+ *           dendra/models/stim/waveform/_gates.py:50-65
+ *   spikes  dendra/models/_threshold_callbacks.py:50-53
+ */
+
+#define CAT_(a, b) a##b
+#define CAT(a, b) CAT_(a, b)
+#define F(name) CAT(name, SFX)
+
+/* Reciprocal-exprel even series (ops.py:13-44). */
+static REAL F(even_series)(REAL q) {
+  REAL q2 = q * q;
+  REAL value;
+  if (IS_F64) {
+    value = q2 * (REAL)(43867.0 / 5109094217170944000.0) - (REAL)(3617.0 / 10670622842880000.0);
+    value = value * q2 + (REAL)(1.0 / 74724249600.0);
+    value = value * q2 - (REAL)(691.0 / 1307674368000.0);
+    value = value * q2 + (REAL)(1.0 / 47900160.0);
+  } else {
+    value = q2 * (REAL)(-691.0 / 1307674368000.0) + (REAL)(1.0 / 47900160.0);
+  }
+  value = value * q2 - (REAL)(1.0 / 1209600.0);
+  value = value * q2 + (REAL)(1.0 / 30240.0);
+  value = value * q2 - (REAL)(1.0 / 720.0);
+  value = value * q2 + (REAL)(1.0 / 12.0);
+  return value;
+}
+
+/* vtrap(x, y) = x / (exp(x/y) - 1) with the local Bernoulli branch (ops.py:47-112). */
+REAL F(orc_vtrap)(REAL x, REAL y) {
+  REAL q = x / y;
+  REAL thr = IS_F64 ? (REAL)0.5 : (REAL)1.0;
+  if (FABS(q) <= thr) {
+    REAL even = F(even_series)(q);
+    return (y - x / (REAL)2) + x * (q * even);
+  }
+  return x / (EXP(q) - (REAL)1);
+}
+
+/* expm1(z)/z by Horner Taylor series for |z| <= 0.5 (_cnexp.py:46-93). */
+REAL F(orc_phi1)(REAL z) {
+  REAL value;
+  if (IS_F64) {
+    value = z * (REAL)(1.0 / 355687428096000.0) + (REAL)(1.0 / 20922789888000.0);
+    value = value * z + (REAL)(1.0 / 1307674368000.0);
+    value = value * z + (REAL)(1.0 / 87178291200.0);
+    value = value * z + (REAL)(1.0 / 6227020800.0);
+    value = value * z + (REAL)(1.0 / 479001600.0);
+    value = value * z + (REAL)(1.0 / 39916800.0);
+    value = value * z + (REAL)(1.0 / 3628800.0);
+    value = value * z + (REAL)(1.0 / 362880.0);
+  } else {
+    value = z * (REAL)(1.0 / 3628800.0) + (REAL)(1.0 / 362880.0);
+  }
+  value = value * z + (REAL)(1.0 / 40320.0);
+  value = value * z + (REAL)(1.0 / 5040.0);
+  value = value * z + (REAL)(1.0 / 720.0);
+  value = value * z + (REAL)(1.0 / 120.0);
+  value = value * z + (REAL)(1.0 / 24.0);
+  value = value * z + (REAL)(1.0 / 6.0);
+  value = value * z + (REAL)(1.0 / 2.0);
+  value = value * z + (REAL)1;
+  return value;
+}
+
+/* Rate constants am1=0.1, ah1=0.07, an1=0.01 are held by the reference as
+   float32 values even in a float64 model (its GLOBAL buffers are created in
+   float32 and widened), so the oracle uses the float32-rounded values. */
+#define AM1 ((REAL)0.1f)
+#define AH1 ((REAL)0.07f)
+#define AN1 ((REAL)0.01f)
+
+/* HH rate pairs (source a, decay b) for m, h, n at voltage v (HH.py:24-40). */
+void F(orc_hh_rates)(REAL v, REAL q10, REAL* out6) {
+  REAL alpha_m = AM1 * F(orc_vtrap)(-(v + (REAL)40), (REAL)10);
+  REAL beta_m = (REAL)4.0 * EXP(-(v + (REAL)65) / (REAL)18);
+  REAL alpha_h = AH1 * EXP(-(v + (REAL)65) / (REAL)20);
+  REAL beta_h = (REAL)1.0 / (EXP(-(v + (REAL)35) / (REAL)10) + (REAL)1);
+  REAL alpha_n = AN1 * F(orc_vtrap)(-(v + (REAL)55), (REAL)10);
+  REAL beta_n = (REAL)0.125 * EXP(-(v + (REAL)65) / (REAL)80);
+  out6[0] = q10 * alpha_m;
+  out6[1] = q10 * (alpha_m + beta_m);
+  out6[2] = q10 * alpha_h;
+  out6[3] = q10 * (alpha_h + beta_h);
+  out6[4] = q10 * alpha_n;
+  out6[5] = q10 * (alpha_n + beta_n);
+}
+
+/* Steady-state gates at v (HH.py:42-56). */
+void F(orc_hh_steady)(REAL v, REAL* mhn) {
+  REAL alpha_m = AM1 * F(orc_vtrap)(-(v + (REAL)40), (REAL)10);
+  REAL beta_m = (REAL)4.0 * EXP(-(v + (REAL)65) / (REAL)18);
+  REAL alpha_h = AH1 * EXP(-(v + (REAL)65) / (REAL)20);
+  REAL beta_h = (REAL)1.0 / (EXP(-(v + (REAL)35) / (REAL)10) + (REAL)1);
+  REAL alpha_n = AN1 * F(orc_vtrap)(-(v + (REAL)55), (REAL)10);
+  REAL beta_n = (REAL)0.125 * EXP(-(v + (REAL)65) / (REAL)80);
+  mhn[0] = alpha_m / (alpha_m + beta_m);
+  mhn[1] = alpha_h / (alpha_h + beta_h);
+  mhn[2] = alpha_n / (alpha_n + beta_n);
+}
+
+/* cnexp exact affine step of x' = a - b x over dt (_cnexp.py:96-132). */
+REAL F(orc_cnexp)(REAL x, REAL a, REAL b, REAL dt) {
+  REAL rate = a - b * x;
+  REAL coef = -b;
+  REAL z = coef * dt;
+  if (FABS(z) <= (REAL)0.5) {
+    return x + dt * rate * F(orc_phi1)(z);
+  }
+  REAL eq = -a / coef;
+  return eq + (x - eq) * EXP(z);
+}
+
+/* Functional Thomas solve of one system (pcr.py:125-183).  a,c: K-1; b,d,x: K. */
+void F(orc_thomas)(int64_t K, const REAL* a, const REAL* b, const REAL* c,
+                   const REAL* d, REAL* x, REAL* work) {
+  if (K == 1) {
+    x[0] = d[0] / b[0];
+    return;
+  }
+  REAL* cp = work;
+  REAL* dp = work + K;
+  REAL denom0 = b[0];
+  cp[0] = c[0] / denom0;
+  dp[0] = d[0] / denom0;
+  for (int64_t i = 1; i < K; ++i) {
+    REAL denom = b[i] - a[i - 1] * cp[i - 1];
+    if (i < K - 1) cp[i] = c[i] / denom;
+    dp[i] = (d[i] - a[i - 1] * dp[i - 1]) / denom;
+  }
+  x[K - 1] = dp[K - 1];
+  for (int64_t i = K - 2; i >= 0; --i) x[i] = dp[i] - cp[i] * x[i + 1];
+}
+
+/* Batched Thomas over B row-major systems. */
+void F(orc_thomas_batched)(int64_t B, int64_t K, const REAL* a, const REAL* b,
+                           const REAL* c, const REAL* d, REAL* x) {
+#pragma omp parallel
+  {
+    REAL* work = (REAL*)malloc(sizeof(REAL) * 2 * (size_t)(K > 0 ? K : 1));
+#pragma omp for schedule(static)
+    for (int64_t i = 0; i < B; ++i) {
+      F(orc_thomas)(K, a + i * (K - 1), b + i * K, c + i * (K - 1), d + i * K,
+                    x + i * K, work);
+    }
+    free(work);
+  }
+}
+
+/* Parallel cyclic reduction with zero-padded shifted bands (pcr.py:4-96). */
+void F(orc_pcr)(int64_t K, const REAL* a_in, const REAL* b_in, const REAL* c_in,
+                const REAL* d_in, REAL* x) {
+  if (K == 1) {
+    x[0] = d_in[0] / b_in[0];
+    return;
+  }
+  REAL* buf = (REAL*)malloc(sizeof(REAL) * 8 * (size_t)K);
+  REAL *a = buf, *b = buf + K, *c = buf + 2 * K, *d = buf + 3 * K;
+  REAL *an = buf + 4 * K, *bn = buf + 5 * K, *cn = buf + 6 * K, *dn = buf + 7 * K;
+  a[0] = 0;
+  for (int64_t i = 1; i < K; ++i) a[i] = a_in[i - 1];
+  for (int64_t i = 0; i < K - 1; ++i) c[i] = c_in[i];
+  c[K - 1] = 0;
+  for (int64_t i = 0; i < K; ++i) {
+    b[i] = b_in[i];
+    d[i] = d_in[i];
+  }
+  for (int64_t s = 1; s < K; s <<= 1) {
+    for (int64_t i = 0; i < K; ++i) {
+      REAL alpha = (i >= s) ? -a[i] / b[i - s] : (REAL)0;
+      REAL beta = (i + s < K) ? -c[i] / b[i + s] : (REAL)0;
+      REAL a_left = (i >= s) ? a[i - s] : (REAL)0;
+      REAL c_left = (i >= s) ? c[i - s] : (REAL)0;
+      REAL d_left = (i >= s) ? d[i - s] : (REAL)0;
+      REAL a_right = (i + s < K) ? a[i + s] : (REAL)0;
+      REAL c_right = (i + s < K) ? c[i + s] : (REAL)0;
+      REAL d_right = (i + s < K) ? d[i + s] : (REAL)0;
+      an[i] = alpha * a_left;
+      bn[i] = b[i] + alpha * c_left + beta * a_right;
+      cn[i] = beta * c_right;
+      dn[i] = d[i] + alpha * d_left + beta * d_right;
+    }
+    REAL* t;
+    t = a; a = an; an = t;
+    t = b; b = bn; bn = t;
+    t = c; c = cn; cn = t;
+    t = d; d = dn; dn = t;
+  }
+  for (int64_t i = 0; i < K; ++i) x[i] = d[i] / b[i];
+  free(buf);
+}
+
+/* Rectangular pulse gate on [delay, delay+pw) at time t (_gates.py:50-65). */
+static REAL F(rect)(REAL t, REAL amp, REAL delay, REAL pw) {
+  REAL stop = delay + pw;
+  return (t >= delay && t < stop) ? amp : (REAL)0;
+}
+
+/*
+ * Multi-step backward-Euler HH cable run (the per-step update of
+ * implicit.py:569-664 after the gate advance of integrators/core.py:769-834),
+ * all cables packed by cable_ptr.  Arguments mirror dgb_cable_args.
+ */
+void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
+                      const int64_t* cable_ptr, REAL* v, REAL* m, REAL* h, REAL* n,
+                      const REAL* g_right, const REAL* g_left, const REAL* scale,
+                      const REAL* cm_inv, const REAL* field, const REAL* gnabar,
+                      const REAL* gkbar, const REAL* gl, const REAL* el, double ena_d,
+                      double ek_d, double q10_d, double dt_ms_d, double dt_s_d,
+                      double t0_ms, const REAL* ve_amp, const REAL* ve_delay,
+                      const REAL* ve_pw, const int32_t* in_idx, const REAL* in_amp,
+                      const REAL* in_delay, const REAL* in_pw, const int32_t* rec_idx,
+                      REAL* trace, const int32_t* spk_idx, double spk_thr_d,
+                      int32_t* spk_below, int32_t* spk_count, int32_t* spk_first) {
+  const REAL ena = (REAL)ena_d, ek = (REAL)ek_d, q10 = (REAL)q10_d;
+  const REAL dt = (REAL)dt_ms_d, dt_s = (REAL)dt_s_d, thr = (REAL)spk_thr_d;
+  const int64_t n_rec = 1 + (int64_t)n_steps / (rec_every > 0 ? rec_every : 1);
+  int64_t kmax = 1;
+  for (int32_t c = 0; c < n_cables; ++c) {
+    int64_t K = cable_ptr[c + 1] - cable_ptr[c];
+    if (K > kmax) kmax = K;
+  }
+#pragma omp parallel
+  {
+    REAL* w = (REAL*)malloc(sizeof(REAL) * 10 * (size_t)kmax);
+#pragma omp for schedule(dynamic, 1)
+    for (int32_t c = 0; c < n_cables; ++c) {
+      const int64_t o = cable_ptr[c];
+      const int64_t K = cable_ptr[c + 1] - o;
+      REAL* vv = v + o;
+      REAL *mm = m + o, *hh = h + o, *nn = n + o;
+      REAL* lower = w;
+      REAL* mainv = w + kmax;
+      REAL* upper = w + 2 * kmax;
+      REAL* rhs = w + 3 * kmax;
+      REAL* x = w + 4 * kmax;
+      REAL* fn = w + 5 * kmax;
+      REAL* G = w + 6 * kmax;
+      REAL* ve = w + 7 * kmax;
+      REAL* work = w + 8 * kmax;
+      const int32_t ri = rec_idx ? rec_idx[c] : -1;
+      const int32_t si = spk_idx ? spk_idx[c] : -1;
+      if (trace && ri >= 0) trace[(int64_t)c * n_rec] = vv[ri];
+      for (int32_t s = 0; s < n_steps; ++s) {
+        /* stimulus time of this step: binary64 grid cast to the state dtype */
+        const REAL t = (REAL)(t0_ms + (double)s * dt_ms_d);
+        REAL ve_i = (REAL)0;
+        const int use_ve = field && ve_amp;
+        if (use_ve) {
+          REAL I = F(rect)(t, ve_amp[c], ve_delay[c], ve_pw[c]);
+          for (int64_t i = 0; i < K; ++i) ve[i] = field[o + i] * I;
+        }
+        (void)ve_i;
+        for (int64_t i = 0; i < K; ++i) {
+          REAL vi = vv[i];
+          REAL r[6];
+          F(orc_hh_rates)(vi, q10, r);
+          mm[i] = F(orc_cnexp)(mm[i], r[0], r[1], dt);
+          hh[i] = F(orc_cnexp)(hh[i], r[2], r[3], dt);
+          nn[i] = F(orc_cnexp)(nn[i], r[4], r[5], dt);
+          REAL m3 = mm[i] * mm[i] * mm[i];
+          REAL n4 = (nn[i] * nn[i]) * (nn[i] * nn[i]);
+          REAL gna = gnabar[o + i] * m3 * hh[i];
+          REAL gk = gkbar[o + i] * n4;
+          REAL Gi = gl[o + i] + gna + gk;
+          REAL Ji = gl[o + i] * el[o + i] + gna * ena + gk * ek;
+          G[i] = Gi;
+          fn[i] = (Ji - Gi * vi) * scale[o + i];
+        }
+        if (K > 1) {
+          for (int64_t i = 0; i < K; ++i) {
+            REAL ax = (REAL)0;
+            if (i == 0) {
+              ax = g_right[o] * (vv[1] - vv[0]);
+            } else if (i == K - 1) {
+              ax = -(g_left[o + i] * (vv[i] - vv[i - 1]));
+            } else {
+              ax = g_right[o + i] * (vv[i + 1] - vv[i]) - g_left[o + i] * (vv[i] - vv[i - 1]);
+            }
+            fn[i] = fn[i] + ax;
+          }
+          if (use_ve) {
+            for (int64_t i = 0; i < K; ++i) {
+              REAL ex;
+              if (i == 0) {
+                ex = g_right[o] * (ve[1] - ve[0]);
+              } else if (i == K - 1) {
+                ex = -(g_left[o + i] * (ve[i] - ve[i - 1]));
+              } else {
+                ex = g_right[o + i] * (ve[i + 1] - ve[i]) - g_left[o + i] * (ve[i] - ve[i - 1]);
+              }
+              fn[i] = fn[i] + ex;
+            }
+          }
+        }
+        if (in_idx && in_amp && in_idx[c] >= 0) {
+          int32_t ii = in_idx[c];
+          REAL I = F(rect)(t, in_amp[c], in_delay[c], in_pw[c]);
+          for (int64_t i = 0; i < K; ++i) {
+            REAL inj = (i == ii) ? I : (REAL)0;
+            fn[i] = fn[i] + inj * cm_inv[o + i];
+          }
+        }
+        for (int64_t i = 0; i < K; ++i) {
+          REAL diag_base = -g_right[o + i] + -g_left[o + i];
+          rhs[i] = dt_s * fn[i];
+          mainv[i] = (REAL)1 - dt_s * (diag_base - G[i] * scale[o + i]);
+          if (i < K - 1) upper[i] = -dt_s * g_right[o + i];
+          if (i > 0) lower[i - 1] = -dt_s * g_left[o + i];
+        }
+        if (K == 1) {
+          x[0] = rhs[0] / mainv[0];
+        } else {
+          F(orc_thomas)(K, lower, mainv, upper, rhs, x, work);
+        }
+        for (int64_t i = 0; i < K; ++i) vv[i] = vv[i] + x[i];
+        if (si >= 0) {
+          int above = vv[si] >= thr;
+          if (above && spk_below[c]) {
+            if (spk_count[c] == 0) spk_first[c] = s + 1;
+            spk_count[c] += 1;
+          }
+          spk_below[c] = !above;
+        }
+        if (trace && ri >= 0 && ((s + 1) % rec_every) == 0)
+          trace[(int64_t)c * n_rec + (s + 1) / rec_every] = vv[ri];
+      }
+    }
+    free(w);
+  }
+}
+
+/*
+ * Sequential DHS/Hines solve of one tree in solver order: layers
+ * layer_ptr[0..L] list nodes deepest first; parent[] uses the same indices
+ * (dhs_kernel.py:45-112, executed one node at a time).
+ */
+void F(orc_dhs_solve)(int64_t K, const REAL* d_in, const REAL* a, const REAL* b_in,
+                      const int32_t* parent, const int32_t* order,
+                      const int32_t* layer_ptr, int32_t n_layers, REAL* x) {
+  REAL* D = (REAL*)malloc(sizeof(REAL) * 2 * (size_t)K);
+  REAL* Bv = D + K;
+  for (int64_t i = 0; i < K; ++i) {
+    D[i] = d_in[i];
+    Bv[i] = b_in[i];
+  }
+  for (int32_t l = 0; l < n_layers; ++l) {
+    for (int32_t o = layer_ptr[l]; o < layer_ptr[l + 1]; ++o) {
+      int32_t i = order[o];
+      REAL g = a[i];
+      REAL old_d = D[i];
+      REAL di = old_d + g;
+      D[i] = di;
+      int32_t p = parent[i];
+      if (p >= 0) {
+        REAL fac = -g * ((REAL)1 / di);
+        D[p] = D[p] + (-fac * old_d);
+        Bv[p] = Bv[p] + (-fac * Bv[i]);
+      }
+    }
+  }
+  for (int32_t l = n_layers - 1; l >= 0; --l) {
+    for (int32_t o = layer_ptr[l]; o < layer_ptr[l + 1]; ++o) {
+      int32_t i = order[o];
+      int32_t p = parent[i];
+      REAL vp = p >= 0 ? x[p] : (REAL)0;
+      x[i] = (Bv[i] + a[i] * vp) / D[i];
+    }
+  }
+  free(D);
+}
+
+void F(orc_dhs_solve_batched)(int64_t B, int64_t K, const REAL* d, const REAL* a,
+                              const REAL* b, const int32_t* parent, const int32_t* order,
+                              const int32_t* layer_ptr, int32_t n_layers, REAL* x) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < B; ++i)
+    F(orc_dhs_solve)(K, d + i * K, a + i * K, b + i * K, parent, order, layer_ptr,
+                     n_layers, x + i * K);
+}
+
+#undef AM1
+#undef AH1
+#undef AN1
+#undef F

@@ -1,0 +1,77 @@
+"""Shared builders of the golden and synthetic test cases."""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from dendra_gb300.cable import CablePopulation
+
+
+def golden_cable_population(g, dtype, device="cpu"):
+    """The reference's config-1-geometry run recorded in hh_cable_*.npz."""
+    B, K = int(g["B"]), int(g["K"])
+    pop = CablePopulation([K] * B, float(g["diam"]), float(g["dx"]), rhoa=float(g["rhoa"]),
+                          celsius=float(g["celsius"]), v_init=float(g["v_init"]),
+                          dtype=dtype, device=device)
+    pop.inject(int(g["comp"]), torch.as_tensor(g["amp_ma"]), float(g["delay"]), float(g["pw"]))
+    return pop.initialize(float(g["dt"]))
+
+
+def golden_extra_population(g, dtype, device="cpu"):
+    """The reference's extracellular run recorded in hh_extra_*.npz."""
+    B, K = int(g["B"]), int(g["K"])
+    pop = CablePopulation([K] * B, torch.as_tensor(g["diam"]), float(g["dx"]),
+                          rhoa=float(g["rhoa"]), celsius=float(g["celsius"]),
+                          v_init=float(g["v_init"]), dtype=dtype, device=device)
+    field = torch.as_tensor(g["field_times_amp"]).reshape(-1)
+    pop.set_extracellular(field, 1.0, float(g["delay"]), float(g["pw"]))
+    return pop.initialize(float(g["dt"]))
+
+
+def oracle_traces(pop, steps, comps, spk_idx=None):
+    """Run the oracle from pop's current state once per recorded compartment.
+
+    Returns (traces (steps+1, B, len(comps)), final problem dict, spikes).
+    """
+    import oracle
+
+    out = []
+    final = None
+    spikes = None
+    for c in comps:
+        p = pop.problem_dict()
+        p["rec_idx"] = np.full(pop.B, int(c), dtype=np.int32)
+        if spk_idx is not None:
+            p["spk_idx"] = np.full(pop.B, int(spk_idx), dtype=np.int32)
+        tr, cnt, first, _ = oracle.cable_run(p, steps)
+        out.append(tr)
+        final = p
+        spikes = (cnt, first)
+    return np.stack(out, axis=-1).transpose(1, 0, 2), final, spikes
+
+
+def synthetic_population(seed, n_cables, kmin, kmax, dtype, device, *, extra=True, intra=False,
+                         dt=0.005):
+    """A C2-style ragged population: odd K uniform in [kmin, kmax], diam U[0.5,4],
+    length U[500,5000] um (dx = L/K), point source at U[0.5,3] mm with a cathodic
+    0.1 ms pulse of U[0.1,2] mA starting at t=0."""
+    rng = np.random.default_rng(seed)
+    ks = 2 * rng.integers((kmin - 1) // 2, (kmax - 1) // 2 + 1, n_cables) + 1
+    ks = np.clip(ks, kmin, kmax)
+    diam = rng.uniform(0.5, 4.0, n_cables)
+    length = rng.uniform(500.0, 5000.0, n_cables)
+    dx = length / ks
+    pop = CablePopulation(ks.tolist(), torch.as_tensor(diam), torch.as_tensor(dx), rhoa=100.0,
+                          celsius=6.3, v_init=-65.0, dtype=dtype, device=device)
+    if extra:
+        dist = rng.uniform(500.0, 3000.0, n_cables)
+        amp = -rng.uniform(0.1, 2.0, n_cables)
+        x = pop.positions()
+        cab = np.repeat(np.arange(n_cables), ks)
+        r_um = torch.sqrt(x ** 2 + torch.as_tensor(dist[cab]) ** 2)
+        field = (1.0 / 0.3 * 100.0) / (4 * torch.pi * r_um * 1e-4)
+        pop.set_extracellular(field, torch.as_tensor(amp), 0.0, 0.1)
+    if intra:
+        pop.inject(0, torch.as_tensor(rng.uniform(0.05, 0.5, n_cables) * 1e-6), 0.5, 1.0)
+    return pop.initialize(dt)

@@ -1,0 +1,285 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference.
+
+The reference (Dendra v0.30.1) is a Python package; this script imports it
+from its source tree with the small stub/shim set in ``refshim/`` (empty
+pandas/natsort/h5py/dask/matplotlib stand-ins and three torch.library
+compatibility shims) and records its outputs on seeded inputs:
+
+  hh_cable_{f64,f32}.npz   Unmyelinated + hh + bwd_euler_ub + somatic mono_rect
+                           (config-1 geometry: diam 1 um, L 1000 um, dx 10 um)
+  hh_extra_{f64,f32}.npz   Unmyelinated + hh with extra=(point field, mono_rect)
+  tridiag.npz              pcr_solve_t / pcr_solve_parallel_t on random systems
+  rates.npz                exprelr, _bounded_phi1, _linear_exact_step, HH rates
+  dhs.npz                  build_morphology / build_dhs_layers plans and the
+                           dense-matrix solve of the reference's DHS parity test
+  events.npz               dense_fixed_delay_transition ring sequence, Exp2Syn
+                           factor and the NetCon delay-rounding known answers
+
+Usage (in a container that holds the reference source):
+
+    PYTHONPATH=<dendra-src>:tests/golden/refshim python tests/golden/make_golden.py
+
+The fixtures are committed; tests never import the reference.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _ref():
+    import dendra as dn  # noqa: F401
+
+    return dn
+
+
+def hh_cable(dtype, tag):
+    dn = _ref()
+    from dendra.models.mod import hh
+
+    B, steps, dt = 3, 800, 0.025
+    g = torch.Generator().manual_seed(1234)
+    amp_na = 0.05 + 0.45 * torch.rand(B, generator=g, dtype=torch.float64)
+    amp_na[0] = 0.5  # at least one cable spikes
+    amp_na[2] = 0.02  # and one stays subthreshold
+    with dn.ctx(JIT=0):
+        # rhoa must be given to the constructor: the workspace reads the
+        # constructor value (an in-place edit of model.rhoa is not picked up)
+        model = dn.Unmyelinated([1.0] * B, L=1000.0, dx=10.0, celsius=6.3, v_init=-65.0,
+                                dtype=dtype, integrator=dn.bwd_euler_ub(), rhoa=100.0)
+        model.insert(hh)
+        amp_ma = (amp_na * 1e-6).to(dtype).reshape(B, 1)
+        model[..., 0].inject(dn.mono_rect(amp=amp_ma, delay=5.0, pw=1.0))
+        model.initialize()
+        m0 = model.mech.hh.m.detach().clone()
+        rec = dn.Recorder(("v",))
+        model.run(dt=dt, duration=steps * dt, callbacks=[rec])
+        v = torch.stack([x.reshape(B, -1) for x in rec.rec["v"]]).to(torch.float64)
+    K = v.shape[-1]
+    out = dict(
+        B=B, K=K, steps=steps, dt=dt, diam=1.0, dx=10.0, rhoa=100.0, celsius=6.3,
+        v_init=-65.0, amp_ma=(amp_na * 1e-6).numpy(), delay=5.0, pw=1.0, comp=0,
+        v_trace=v.numpy(),  # (steps+1, B, K)
+        m0=m0.reshape(B, -1).double().numpy(),
+        v_final=model.v.reshape(B, -1).double().numpy(),
+        m_final=model.mech.hh.m.reshape(B, -1).double().numpy(),
+        h_final=model.mech.hh.h.reshape(B, -1).double().numpy(),
+        n_final=model.mech.hh.n.reshape(B, -1).double().numpy(),
+    )
+    keep = [0, K // 4, K // 2, 3 * K // 4, K - 1]
+    out["trace_comps"] = np.array(keep)
+    out["v_trace"] = out["v_trace"][:, :, keep]
+    np.savez_compressed(os.path.join(HERE, f"hh_cable_{tag}.npz"), **out)
+    print("hh_cable", tag, "K", K, "max v", float(v.max()))
+
+
+def hh_extra(dtype, tag):
+    dn = _ref()
+    from dendra.models.mod import hh
+
+    B, steps, dt = 3, 600, 0.005
+    diam = [1.0, 2.0, 4.0]
+    dist_um = torch.tensor([500.0, 200.0, 300.0], dtype=torch.float64)
+    amp = torch.tensor([-1.0, -4.0, -8.0], dtype=torch.float64)  # cathodic, mA
+    with dn.ctx(JIT=0):
+        model = dn.Unmyelinated(diam, L=500.0, dx=10.0, celsius=6.3, v_init=-65.0,
+                                dtype=dtype, integrator=dn.bwd_euler_ub(), rhoa=100.0)
+        model.insert(hh)
+        model.initialize()
+        K = model.v.shape[-1]
+        x = torch.linspace(-(K - 1) * 10.0 / 2, (K - 1) * 10.0 / 2, K, dtype=torch.float64)
+        rhoe = 1.0 / 0.3 * 100.0  # sigma 0.3 S/m -> 333.33 ohm cm
+        r = torch.sqrt(x[None, :] ** 2 + dist_um[:, None] ** 2) * 1e-4
+        field = rhoe / (4 * torch.pi * r)  # mV/mA, (B, K)
+        spatial = (field * amp[:, None]).to(dtype)
+        rec = dn.Recorder(("v",))
+        model.run(dt=dt, duration=steps * dt, callbacks=[rec],
+                  extra=(spatial, dn.mono_rect(amp=1.0, delay=1.0, pw=0.1)))
+        v = torch.stack([t.reshape(B, -1) for t in rec.rec["v"]]).to(torch.float64)
+    out = dict(B=B, K=K, steps=steps, dt=dt, diam=np.array(diam), dx=10.0, rhoa=100.0,
+               celsius=6.3, v_init=-65.0, field_times_amp=spatial.double().numpy(),
+               delay=1.0, pw=0.1, v_trace=v.numpy(),
+               v_final=model.v.reshape(B, -1).double().numpy())
+    keep = [0, K // 4, K // 2, 3 * K // 4, K - 1]
+    out["trace_comps"] = np.array(keep)
+    out["v_trace"] = out["v_trace"][:, :, keep]
+    np.savez_compressed(os.path.join(HERE, f"hh_extra_{tag}.npz"), **out)
+    print("hh_extra", tag, "K", K, "max v", float(v.max()))
+
+
+def tridiag():
+    _ref()
+    from dendra.models.integrators.tridiag.pcr import pcr_solve_parallel_t, pcr_solve_t
+
+    out = {}
+    g = torch.Generator().manual_seed(7)
+    for K in (1, 2, 3, 7, 33, 101, 401):
+        B = 6
+        a = -torch.rand(B, K - 1, generator=g, dtype=torch.float64)
+        c = -torch.rand(B, K - 1, generator=g, dtype=torch.float64)
+        b = 2.5 + torch.rand(B, K, generator=g, dtype=torch.float64)
+        d = torch.randn(B, K, generator=g, dtype=torch.float64)
+        for tag, dt in (("f64", torch.float64), ("f32", torch.float32)):
+            args = [t.to(dt) for t in (a, b, c, d)]
+            out[f"K{K}_{tag}_thomas"] = pcr_solve_t(*args).numpy()
+            out[f"K{K}_{tag}_pcr"] = pcr_solve_parallel_t(*args).numpy()
+        out[f"K{K}_a"], out[f"K{K}_b"], out[f"K{K}_c"], out[f"K{K}_d"] = (
+            t.numpy() for t in (a, b, c, d))
+    np.savez_compressed(os.path.join(HERE, "tridiag.npz"), **out)
+    print("tridiag", len(out))
+
+
+def rates():
+    _ref()
+    from dendra.models.mechanisms._cnexp import _bounded_phi1, _linear_exact_step
+    from dendra.models.mechanisms.ops import exprelr
+
+    out = {}
+    v = torch.linspace(-120.0, 60.0, 1801, dtype=torch.float64)
+    v = torch.cat([v, torch.tensor([-40.0, -55.0, -40.0 + 1e-7, -55.0 - 3e-6])])
+    for tag, dt in (("f64", torch.float64), ("f32", torch.float32)):
+        vv = v.to(dt)
+        ten = torch.full_like(vv, 10.0)
+        # GLOBAL rate constants as the reference holds them (float32 values)
+        am = float(np.float32(0.1)) * exprelr(-(vv + 40), ten)
+        bm = 4.0 * torch.exp(-(vv + 65) / 18)
+        ah = float(np.float32(0.07)) * torch.exp(-(vv + 65) / 20)
+        bh = 1.0 / (torch.exp(-(vv + 35) / 10) + 1)
+        an = float(np.float32(0.01)) * exprelr(-(vv + 55), ten)
+        bn = 0.125 * torch.exp(-(vv + 65) / 80)
+        out[f"v_{tag}"] = vv.numpy()
+        out[f"rates_{tag}"] = torch.stack([am, am + bm, ah, ah + bh, an, an + bn], -1).numpy()
+        z = torch.linspace(-0.5, 0.5, 201, dtype=dt)
+        out[f"z_{tag}"] = z.numpy()
+        out[f"phi1_{tag}"] = _bounded_phi1(z).numpy()
+        # cnexp on a grid of (x, a, b) including both branches
+        gx = torch.Generator().manual_seed(3)
+        x = torch.rand(500, generator=gx, dtype=torch.float64).to(dt)
+        bcoef = (10.0 ** (torch.rand(500, generator=gx, dtype=torch.float64) * 5 - 3)).to(dt)
+        acoef = (bcoef.double() * torch.rand(500, generator=gx, dtype=torch.float64)).to(dt)
+        dtt = torch.tensor(0.025, dtype=dt)
+        out[f"cnexp_in_{tag}"] = torch.stack([x, acoef, bcoef], -1).numpy()
+        out[f"cnexp_out_{tag}"] = _linear_exact_step(x, acoef - bcoef * x, acoef, -bcoef,
+                                                     dtt).numpy()
+    np.savez_compressed(os.path.join(HERE, "rates.npz"), **out)
+    print("rates")
+
+
+def dhs():
+    _ref()
+    from dendra.models.integrators.tree import build_dhs_layers, build_morphology
+
+    out = {}
+    parent = [-1, 0, 0, 1, 1, 2, 5]
+    out["parity_parent"] = np.array(parent)
+    for threads in (1, 8, 32):
+        _, _, depth = build_morphology(parent)
+        order, layer_ptr = build_dhs_layers(depth, threads)
+        out[f"parity_order_t{threads}"] = order.numpy()
+        out[f"parity_layer_ptr_t{threads}"] = layer_ptr.numpy()
+    # a random tree (parents before children)
+    rng = np.random.default_rng(11)
+    K = 300
+    par = [-1] + [int(rng.integers(max(0, i - 20), i)) for i in range(1, K)]
+    _, _, depth = build_morphology(par)
+    order, layer_ptr = build_dhs_layers(depth, 32)
+    out["rand_parent"] = np.array(par)
+    out["rand_depth"] = depth.numpy()
+    out["rand_order_t32"] = order.numpy()
+    out["rand_layer_ptr_t32"] = layer_ptr.numpy()
+
+    def dense(par, d_mem, a_geom, rhs):
+        matrix = torch.diag_embed(d_mem + a_geom)
+        for child, p in enumerate(par):
+            if p < 0:
+                continue
+            edge = a_geom[:, child]
+            matrix[:, p, p] += edge
+            matrix[:, child, p] -= edge
+            matrix[:, p, child] -= edge
+        return torch.linalg.solve(matrix, rhs.unsqueeze(-1)).squeeze(-1)
+
+    batch, size = 5, len(parent)
+    d_mem = torch.linspace(1.3, 2.6, batch * size, dtype=torch.float64).reshape(batch, size)
+    a_geom = torch.linspace(0.015, 0.095, batch * size, dtype=torch.float64).reshape(batch, size)
+    a_geom[:, 0] = 0.0
+    rhs = torch.linspace(-1.7, 2.1, batch * size, dtype=torch.float64).reshape(batch, size)
+    out["parity_d"], out["parity_a"], out["parity_b"] = d_mem.numpy(), a_geom.numpy(), rhs.numpy()
+    out["parity_x"] = dense(parent, d_mem, a_geom, rhs).numpy()
+    g = torch.Generator().manual_seed(5)
+    d_r = 1.0 + torch.rand(4, K, generator=g, dtype=torch.float64)
+    a_r = 0.5 * torch.rand(4, K, generator=g, dtype=torch.float64)
+    a_r[:, 0] = 0
+    b_r = torch.randn(4, K, generator=g, dtype=torch.float64)
+    out["rand_d"], out["rand_a"], out["rand_b"] = d_r.numpy(), a_r.numpy(), b_r.numpy()
+    out["rand_x"] = dense(par, d_r, a_r, b_r).numpy()
+    np.savez_compressed(os.path.join(HERE, "dhs.npz"), **out)
+    print("dhs")
+
+
+def events():
+    _ref()
+    from dendra.models.mod.EXP2SYN import exp2syn  # noqa: F401
+    from dendra.models.networks._event_delivery import dense_due, dense_fixed_delay_transition
+
+    out = {}
+    rng = np.random.default_rng(21)
+    n_conn, width, depth, steps = 64, 16, 9, 30
+    post = rng.integers(0, width, n_conn)
+    delay = rng.integers(1, depth, n_conn)
+    weight = rng.lognormal(-7, 0.5, n_conn)
+    gates = (rng.random((steps, n_conn)) < 0.2).astype(np.float64)
+    queue = torch.zeros(depth, width, dtype=torch.float64)
+    slot = torch.zeros(1, dtype=torch.long)
+    gstep = torch.zeros(1, dtype=torch.long)
+    delivered = []
+    for s in range(steps):
+        due = dense_due(queue, slot).payload.clone()
+        delivered.append(due.numpy())
+        queue, slot, gstep, _ = dense_fixed_delay_transition(
+            queue, slot, gstep, torch.as_tensor(weight), torch.as_tensor(gates[s]),
+            post_idx=torch.as_tensor(post), delay_steps=torch.as_tensor(delay),
+            depth=depth, width=width)
+    out.update(post=post, delay=delay, weight=weight, gates=gates, depth=depth, width=width,
+               delivered=np.stack(delivered), final_queue=queue.numpy(),
+               final_slot=int(slot.item()))
+    # NetCon delay rounding known answers (tests/networks/test_event_delivery_contract.py:103-116)
+    ratios = np.array([0.49, 0.5, 0.51, 1.49, 1.5, 1.51, 2.5, 3.5])
+    out["round_ratios"] = ratios
+    out["round_delay_steps"] = np.array([0, 0, 1, 1, 2, 2, 2, 4])
+    out["round_inference_steps"] = np.array([1, 1, 1, 1, 2, 2, 2, 4])
+    # Exp2Syn normalisation factor (EXP2SYN.py:112-144) for a grid of taus
+    tau1 = torch.tensor([0.5, 0.1, 1.0, 2.0, 4.999, 5.0], dtype=torch.float64)
+    tau2 = torch.tensor([5.0, 10.0, 3.0, 2.0, 5.0, 5.0], dtype=torch.float64)
+    from types import SimpleNamespace
+
+    fake = SimpleNamespace(DE={"A": SimpleNamespace(tau1=tau1), "B": SimpleNamespace(tau2=tau2)})
+    derived = exp2syn.derive_buffers(fake)
+    out["exp2syn_tau1"], out["exp2syn_tau2"] = tau1.numpy(), tau2.numpy()
+    out["exp2syn_factor"] = derived["factor"].numpy()
+    np.savez_compressed(os.path.join(HERE, "events.npz"), **out)
+    print("events")
+
+
+if __name__ == "__main__":
+    what = sys.argv[1:] or ["rates", "tridiag", "dhs", "events", "cable", "extra"]
+    if "rates" in what:
+        rates()
+    if "tridiag" in what:
+        tridiag()
+    if "dhs" in what:
+        dhs()
+    if "events" in what:
+        events()
+    if "cable" in what:
+        hh_cable(torch.float64, "f64")
+        hh_cable(torch.float32, "f32")
+    if "extra" in what:
+        hh_extra(torch.float64, "f64")
+        hh_extra(torch.float32, "f32")

@@ -1,0 +1,130 @@
+"""Persistent and per-step HH cable runs on the GPU against the reference and the oracle."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from tests._cases import (
+    golden_cable_population,
+    golden_extra_population,
+    oracle_traces,
+    synthetic_population,
+)
+
+pytestmark = pytest.mark.gpu
+
+# float32 state against the float64 judge: the benchmark spec's bound of 1e-3 mV,
+# widened for spiking traces by the reference's own float32-vs-float64 error
+F32_MV = 1e-3
+
+
+def _spike_steps(trace, thr=0.0):
+    above = trace >= thr
+    return [list(np.nonzero(above[1:, b] & ~above[:-1, b])[0] + 1) for b in range(trace.shape[1])]
+
+
+def _gpu_traces(make, g, dtype, cuda, comps):
+    out = []
+    for c in comps:
+        pop = make(g, dtype, cuda)
+        res = pop.run(int(g["steps"]), rec_idx=int(c))
+        out.append(res.trace.double().cpu().numpy())
+    return np.stack(out, axis=-1).transpose(1, 0, 2), pop
+
+
+@pytest.mark.parametrize("which", ["cable", "extra"])
+def test_float64_run_matches_reference(cuda, golden, which):
+    g = golden(f"hh_{which}_f64.npz")
+    make = golden_cable_population if which == "cable" else golden_extra_population
+    tr, pop = _gpu_traces(make, g, torch.float64, cuda, g["trace_comps"])
+    ref = g["v_trace"]
+    assert np.abs(tr - ref).max() < 1e-7
+    for c in range(ref.shape[2]):
+        assert _spike_steps(tr[:, :, c]) == _spike_steps(ref[:, :, c])
+    np.testing.assert_allclose(pop.v.cpu().numpy().reshape(ref.shape[1], -1), g["v_final"],
+                               rtol=0, atol=1e-7)
+
+
+@pytest.mark.parametrize("which", ["cable", "extra"])
+def test_float32_run_within_tolerance_of_float64_judge(cuda, golden, which):
+    g64 = golden(f"hh_{which}_f64.npz")
+    g32 = golden(f"hh_{which}_f32.npz")
+    make = golden_cable_population if which == "cable" else golden_extra_population
+    tr, _ = _gpu_traces(make, g32, torch.float32, cuda, g32["trace_comps"])
+    ref64 = g64["v_trace"]
+    ref_own = np.abs(g32["v_trace"] - ref64).max()  # the reference's own float32 error
+    err = np.abs(tr - ref64).max()
+    print(f"{which}: gpu f32 vs f64 judge {err:.3e} mV; reference f32 {ref_own:.3e} mV")
+    assert err <= max(F32_MV, 2.0 * ref_own)
+    for c in range(ref64.shape[2]):
+        assert _spike_steps(tr[:, :, c]) == _spike_steps(ref64[:, :, c])
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_ragged_population_matches_oracle(cuda, dtype):
+    """Every chunk size: K from 1 to 512 in one launch, extracellular + intra drive."""
+    ks = [1, 2, 3, 17, 31, 32, 33, 63, 64, 65, 97, 128, 129, 200, 255, 256, 257, 301, 384,
+          401, 416, 417, 448, 480, 481, 511, 512]
+    from dendra_gb300.cable import CablePopulation
+
+    rng = np.random.default_rng(5)
+    pop = CablePopulation(ks, torch.as_tensor(rng.uniform(0.5, 4.0, len(ks))),
+                          torch.as_tensor(rng.uniform(5.0, 20.0, len(ks))), dtype=dtype,
+                          device=cuda)
+    x = pop.positions()
+    cab = np.repeat(np.arange(len(ks)), ks)
+    dist = torch.as_tensor(rng.uniform(300.0, 1000.0, len(ks))[cab])
+    pop.set_extracellular(333.33 / (4 * np.pi * torch.sqrt(x ** 2 + dist ** 2) * 1e-4),
+                          torch.as_tensor(-rng.uniform(0.5, 3.0, len(ks))), 0.05, 0.1)
+    pop.inject(torch.as_tensor([k // 2 for k in ks]),
+               torch.as_tensor(rng.uniform(0.1, 1.0, len(ks)) * 1e-6), 0.2, 0.5)
+    pop.initialize(0.005)
+    p64 = pop.problem_dict()
+    p64 = {k: (v.astype(np.float64) if isinstance(v, np.ndarray) and v.dtype.kind == "f" else v)
+           for k, v in p64.items()}
+    steps = 300
+    rec = np.array([k - 1 for k in ks], dtype=np.int32)
+    p64["rec_idx"] = rec
+    p64["spk_idx"] = rec
+    tr_ref, cnt_ref, first_ref, _ = oracle.cable_run(p64, steps)
+    res = pop.run(steps, rec_idx=torch.as_tensor(rec), spk_idx=torch.as_tensor(rec))
+    tr = res.trace.double().cpu().numpy()
+    tol = 1e-8 if dtype == torch.float64 else 5e-2
+    err = np.abs(tr - tr_ref).max()
+    print("ragged", dtype, err)
+    assert err < tol
+    np.testing.assert_array_equal(res.spk_count.cpu().numpy(), cnt_ref)
+    np.testing.assert_array_equal(res.spk_first.cpu().numpy(), first_ref)
+    np.testing.assert_allclose(pop.v.double().cpu().numpy(), p64["v"], atol=tol, rtol=0)
+
+
+def test_plain_per_step_path_matches_persistent_run(cuda):
+    pops = [synthetic_population(9, 64, 51, 401, torch.float64, cuda) for _ in range(2)]
+    steps = 60
+    pops[0].run(steps)
+    bands = None
+    for _ in range(steps):
+        bands = pops[1].step_plain(bands)
+    for name in ("v", "m", "h", "n"):
+        np.testing.assert_allclose(getattr(pops[0], name).cpu().numpy(),
+                                   getattr(pops[1], name).cpu().numpy(), rtol=1e-12, atol=1e-10)
+
+
+def test_split_runs_continue_exactly(cuda):
+    """Two half-length runs equal one full run (time and pulse phase carried)."""
+    a = synthetic_population(4, 32, 51, 201, torch.float32, cuda, intra=True)
+    b = synthetic_population(4, 32, 51, 201, torch.float32, cuda, intra=True)
+    a.run(400)
+    b.run(200)
+    b.run(200)
+    torch.testing.assert_close(a.v, b.v, rtol=0, atol=0)
+
+
+def test_spike_detection_counts_rising_edges(cuda, golden):
+    g = golden("hh_cable_f64.npz")
+    pop = golden_cable_population(g, torch.float64, cuda)
+    res = pop.run(int(g["steps"]), spk_idx=0)
+    ref = _spike_steps(g["v_trace"][:, :, 0])
+    np.testing.assert_array_equal(res.spk_count.cpu().numpy(), [len(s) for s in ref])
+    np.testing.assert_array_equal(res.spk_first.cpu().numpy(), [s[0] if s else -1 for s in ref])

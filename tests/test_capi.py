@@ -1,0 +1,67 @@
+"""The C-ABI library builds, loads and exports every declared symbol (CPU only)."""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+import dendra_gb300
+from dendra_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))
+           if f.endswith(".h")]
+
+
+def _declared():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(dgb_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert "dgb_tridiag_solve" in names and "dgb_cable_run" in names
+
+
+def test_library_exports_every_declared_symbol():
+    L = dendra_gb300.load()
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.path()], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\b(dgb_\w+)\b", out))
+    missing = [n for n in _declared() if n not in exported]
+    assert not missing, missing
+    for n in _declared():
+        assert hasattr(L, n)
+    # every declared function has a ctypes signature in the binding
+    assert set(_declared()) <= set(_lib.SIGNATURES)
+
+
+def test_cable_args_mirror_matches_c_layout():
+    L = dendra_gb300.load()
+    assert L.dgb_cable_args_size() == ctypes.sizeof(_lib.CableArgs)
+
+
+def test_library_has_no_torch_dependency():
+    out = subprocess.run(["readelf", "-d", _lib.path()], capture_output=True, text=True,
+                         check=True).stdout
+    assert "torch" not in out and "c10" not in out
+
+
+def test_argument_errors_are_reported_without_touching_a_device():
+    L = dendra_gb300.load()
+    rc = L.dgb_tridiag_solve(7, 0, 1, 4, None, None, None, None, None, None)
+    assert rc == -1
+    assert b"dtype" in L.dgb_last_error()
+    rc = L.dgb_tridiag_solve(0, 0, 1, 0, None, None, None, None, None, None)
+    assert rc == -1 and b"K >= 1" in L.dgb_last_error()
+    args = _lib.CableArgs()
+    args.dtype = 3
+    assert L.dgb_cable_run(ctypes.byref(args), None) == -1
+    with pytest.raises(ValueError):
+        _lib.check(-1, "probe")
