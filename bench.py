@@ -169,6 +169,10 @@ def main():
     ap.add_argument("--sample", type=int, default=512, help="CPU baseline cables")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cables", type=int, default=16384,
+                    help="cables per rank (a smaller case for profiling)")
+    ap.add_argument("--timesteps", type=int, default=0, help="timesteps per run (default 2000)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.impl == "reference":
@@ -190,8 +194,10 @@ def main():
     dendra_gb300.load()
 
     # each rank owns an independent shard of cables (weak scaling, no collective)
-    pop = cable_population_c2(dtype=torch.float32, device=dev, seed=2024 + rank)
-    comp_steps = pop.N * C2_STEPS
+    n_ts = args.timesteps or C2_STEPS
+    pop = cable_population_c2(n_cables=args.cables, dtype=torch.float32, device=dev,
+                              seed=2024 + rank)
+    comp_steps = pop.N * n_ts
     v0, m0, h0, n0 = (t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
 
     def reset():
@@ -206,11 +212,12 @@ def main():
 
     def one(spk=False):
         reset()
-        return pop.run(C2_STEPS, spk_idx=0 if spk else None)
+        return pop.run(n_ts, spk_idx=0 if spk else None)
 
     for _ in range(max(3, args.warmup)):
         one()
     torch.cuda.synchronize()
+    pop.check_status()
 
     def barrier():
         if pg is not None:
@@ -226,7 +233,7 @@ def main():
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
-            pop.run(C2_STEPS)
+            pop.run(n_ts)
             e1.record(st)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
@@ -260,19 +267,21 @@ def main():
         for k, t in host_state.items():
             getattr(pop, k).copy_(t, non_blocking=True)
         pop.step_index = 0
-        res = pop.run(C2_STEPS, spk_idx=0)
+        res = pop.run(n_ts, spk_idx=0)
         out_v.copy_(pop.v, non_blocking=True)
         out_cnt.copy_(res.spk_count, non_blocking=True)
         out_first.copy_(res.spk_first, non_blocking=True)
 
-    e2e_step()
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    e2e_ms = float("nan")
+    if not args.no_e2e:
         e2e_step()
-    torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     if pg is not None:
         t = torch.tensor([e2e_ms], device=dev)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
@@ -308,9 +317,9 @@ def main():
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "c2-uneven-hh-cables-extracellular", "n_cables": 16384 * world,
+        "config": {"workload": "c2-uneven-hh-cables-extracellular", "n_cables": args.cables * world,
                    "compartments_per_rank": pop.N, "k_range": [51, 401], "dt_ms": 0.005,
-                   "timesteps": C2_STEPS, "state_dtype": "float32",
+                   "timesteps": n_ts, "state_dtype": "float32",
                    "l2": "flushed between timed steps (256 MiB write, outside the events)",
                    "launch": "one persistent dgb_cable_run launch per step"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -321,7 +330,7 @@ def main():
                               "bandwidth; the persistent kernel keeps state on chip")},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * (1 if args.no_e2e else 2),
         "clocks": clocks.summary(),
         "cables_spiking": n_spiking,
     }

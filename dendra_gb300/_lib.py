@@ -19,6 +19,7 @@ F32 = 0
 F64 = 1
 THOMAS = 0
 PCR = 1
+CABLE_UNIFORM_CHANNELS = 1
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -47,7 +48,7 @@ class CableArgs(ctypes.Structure):
         ("rec_idx", _P), ("trace", _P),
         ("spk_idx", _P), ("spk_thr", _D), ("spk_below", _P), ("spk_count", _P),
         ("spk_first", _P),
-        ("max_k", _I32), ("lanes", _I32), ("n_comp", _I64),
+        ("max_k", _I32), ("flags", _I32), ("n_comp", _I64),
         ("comp_cable", _P), ("scratch", _P),
     ]
 

@@ -118,8 +118,8 @@ class CablePopulation:
         n_comp = [int(k) for k in n_comp]
         if not n_comp:
             raise ValueError("a population needs at least one cable")
-        if min(n_comp) < 1 or max(n_comp) > 512:
-            raise ValueError("compartments per cable must be in [1, 512]")
+        if min(n_comp) < 1 or max(n_comp) > 1024:
+            raise ValueError("compartments per cable must be in [1, 1024]")
         if dtype not in (torch.float32, torch.float64):
             raise TypeError("state dtype must be float32 or float64")
         self.dtype = dtype
@@ -235,11 +235,21 @@ class CablePopulation:
         if self.intra is not None:
             d["in_idx"], d["in_amp"], d["in_delay"], d["in_pw"] = (x.to(dev) for x in self.intra)
         self._dev = d
+        self.uniform_channels = self._channels_uniform()
         self.v = v.to(dev)
         self.m, self.h, self.n = m.to(dev), h.to(dev), n.to(dev)
         self.t = 0.0
         self.step_index = 0
         return self
+
+    def _channels_uniform(self):
+        """True when gnabar, gkbar, gl, el are constant inside every cable."""
+        cab = torch.as_tensor(np.repeat(np.arange(self.B), self.n_comp))
+        same_cable = cab[1:] == cab[:-1]
+        for t in self._chan.values():
+            if bool(((t[1:] != t[:-1]) & same_cable).any()):
+                return False
+        return True
 
     def _args(self, n_steps=0, rec_every=1, rec_idx=None, trace=None, spk=None, spk_thr=0.0):
         d = self._dev
@@ -269,7 +279,7 @@ class CablePopulation:
             a.spk_idx, a.spk_below, a.spk_count, a.spk_first = (t.data_ptr() for t in spk)
             a.spk_thr = float(spk_thr)
         a.max_k = max(self.n_comp)
-        a.lanes = 0
+        a.flags = _lib.CABLE_UNIFORM_CHANNELS if self.uniform_channels else 0
         a.n_comp = self.N
         a.comp_cable = d["comp_cable"].data_ptr()
         a.scratch = d["scratch"].data_ptr()
@@ -287,6 +297,12 @@ class CablePopulation:
         if self.dt is None:
             raise RuntimeError("Model must be initialized before running.")
         dev = self.device
+        kk = torch.as_tensor(self.n_comp, dtype=torch.int32)
+        for name, idx in (("rec_idx", rec_idx), ("spk_idx", spk_idx)):
+            if idx is not None:
+                ii = torch.as_tensor(idx, dtype=torch.int32).expand(self.B).cpu()
+                if bool(((ii < -1) | (ii >= kk)).any()):
+                    raise ValueError(f"{name} out of range for some cable")
         trace = rec = None
         if rec_idx is not None:
             rec = torch.as_tensor(rec_idx, dtype=torch.int32).expand(self.B).contiguous().to(dev)
@@ -306,6 +322,12 @@ class CablePopulation:
         self.t = self.t + int(n_steps) * self.dt
         self.step_index += int(n_steps)
         return RunResult(trace, spk[2] if spk else None, spk[3] if spk else None)
+
+    def check_status(self):
+        """Raise if the last persistent run flagged a cable it could not advance."""
+        err = int(self._dev["scratch"][1].item())
+        if err:
+            raise RuntimeError(f"dgb_cable_run reported error bits {err:#x}")
 
     def step_plain(self, bands=None):
         """One step through the unfused assemble + solve/update kernels."""

@@ -1,18 +1,6 @@
 // C-ABI entry points of the unbranched HH cable kernels; the kernels live in
-// cable_impl.cuh and are compiled per dtype in cable_f32.cu / cable_f64.cu.
-#define DGB_CASE_F32(CHV)
-#include "cable_impl.cuh"
-
-namespace dgb {
-template <typename T>
-int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st);
-template <typename T>
-int cable_assemble_t(const dgb_cable_args* args, int32_t step, void* lower, void* mainv,
-                     void* upper, void* rhs, cudaStream_t st);
-template <typename T>
-int cable_solve_update_t(const dgb_cable_args* args, const void* lower, const void* mainv,
-                         const void* upper, const void* rhs, cudaStream_t st);
-}  // namespace dgb
+// cable_impl.cuh and are compiled per dtype in cable_f32.cu / cable_f64.cu only.
+#include "cable_decl.cuh"
 
 using namespace dgb;
 
@@ -27,6 +15,7 @@ extern "C" int dgb_cable_run(const dgb_cable_args* args, void* stream) {
   DGB_REQUIRE(kmax >= 1 && kmax <= 32 * kCableMaxCH,
               "max compartments per cable (max_k) must be in [1, %d], got %lld",
               32 * kCableMaxCH, (long long)kmax);
+  // shared memory is sized for the largest chunk (rows per lane) of any cable
   const int ch_max = (int)((kmax + 31) / 32);
   cudaStream_t st = as_stream(stream);
   if (args->dtype == DGB_F32) return cable_run_t<float>(args, ch_max, st);
@@ -57,9 +46,9 @@ extern "C" int dgb_cable_solve_update(const dgb_cable_args* args, const void* lo
   DGB_REQUIRE(lower && main_diag && upper && rhs, "band inputs must be non-null");
   if (args->n_cables == 0) return DGB_OK;
   const int64_t kmax = args->max_k;
-  DGB_REQUIRE(kmax >= 1 && kmax <= 32 * kCableMaxCH,
+  DGB_REQUIRE(kmax >= 1 && kmax <= 32 * kSolveUpdateMaxCH,
               "max compartments per cable (max_k) must be in [1, %d], got %lld",
-              32 * kCableMaxCH, (long long)kmax);
+              32 * kSolveUpdateMaxCH, (long long)kmax);
   cudaStream_t st = as_stream(stream);
   if (args->dtype == DGB_F32)
     return cable_solve_update_t<float>(args, lower, main_diag, upper, rhs, st);

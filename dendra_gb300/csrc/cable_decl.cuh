@@ -1,0 +1,43 @@
+// Declarations shared by the cable C-ABI translation unit and the per-dtype
+// kernel translation units (cable_f32.cu, cable_f64.cu).  Kernel templates
+// live in cable_impl.cuh and are compiled only by the per-dtype units, so each
+// kernel has exactly one definition in the library.
+#pragma once
+
+#include "common.cuh"
+
+namespace dgb {
+
+constexpr int kCableMaxCH = 32;        // persistent run: K <= 1024
+constexpr int kSolveUpdateMaxCH = 16;  // plain per-step solve: K <= 512
+
+template <typename T>
+int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st);
+template <typename T>
+int cable_assemble_t(const dgb_cable_args* args, int32_t step, void* lower, void* mainv,
+                     void* upper, void* rhs, cudaStream_t st);
+template <typename T>
+int cable_solve_update_t(const dgb_cable_args* args, const void* lower, const void* mainv,
+                         const void* upper, const void* rhs, cudaStream_t st);
+
+inline int validate_cable_args(const dgb_cable_args* a) {
+  DGB_REQUIRE(a != nullptr, "args must be non-null");
+  DGB_REQUIRE(a->dtype == DGB_F32 || a->dtype == DGB_F64, "dtype must be DGB_F32 or DGB_F64");
+  DGB_REQUIRE(a->n_cables >= 0 && a->n_steps >= 0, "n_cables and n_steps must be >= 0");
+  DGB_REQUIRE(a->cable_ptr && a->v && a->m && a->h && a->n, "cable_ptr and v/m/h/n are required");
+  DGB_REQUIRE(a->g_right && a->g_left && a->scale && a->cm_inv,
+              "g_right, g_left, scale and cm_inv are required");
+  DGB_REQUIRE(a->gnabar && a->gkbar && a->gl && a->el, "gnabar, gkbar, gl and el are required");
+  DGB_REQUIRE(!a->in_idx || (a->in_amp && a->in_delay && a->in_pw),
+              "in_idx requires in_amp, in_delay and in_pw");
+  DGB_REQUIRE(!a->ve_amp || (a->field && a->ve_delay && a->ve_pw),
+              "ve_amp requires field, ve_delay and ve_pw");
+  DGB_REQUIRE(!a->spk_idx || (a->spk_below && a->spk_count && a->spk_first),
+              "spk_idx requires spk_below, spk_count and spk_first");
+  DGB_REQUIRE(!a->trace || a->rec_idx, "trace requires rec_idx");
+  DGB_REQUIRE(a->rec_every >= 1, "rec_every must be >= 1");
+  DGB_REQUIRE((a->flags & ~DGB_CABLE_UNIFORM_CHANNELS) == 0, "unknown flags %d", a->flags);
+  return DGB_OK;
+}
+
+}  // namespace dgb

@@ -27,6 +27,7 @@
   DGB_CASE_F32(3) DGB_CASE_F32(5) DGB_CASE_F32(6) DGB_CASE_F32(7) DGB_CASE_F32(9) \
   DGB_CASE_F32(10) DGB_CASE_F32(11) DGB_CASE_F32(12) DGB_CASE_F32(13)             \
   DGB_CASE_F32(14) DGB_CASE_F32(15)
+#include "cable_decl.cuh"
 #include "chunk_solve.cuh"
 
 namespace dgb {
@@ -102,55 +103,85 @@ static CableArgsT<T> typed(const dgb_cable_args* a) {
   return t;
 }
 
-// Per-warp shared-memory coefficient block: kNConst planes of [CH][32].
-constexpr int kNConst = 8;
-enum { Q_GR = 0, Q_GL, Q_SCALE, Q_FIELD, Q_GNA, Q_GK, Q_GLK, Q_EL };
+// error bits of scratch[1]
+constexpr int kErrChunk = 1;
 
-template <typename T, int CH>
-__device__ __forceinline__ T& sm(T* base, int q, int j, int lane) {
-  return base[(q * CH + j) * 32 + lane];
+// Shared-memory planes of one warp (one cable).  Plane q holds row j of lane r
+// at [(q * ch + j) * 32 + r]: the 32 lanes touch 32 consecutive words, so
+// every access is bank-conflict free for any chunk size ch.
+enum {
+  P_V = 0, P_M, P_H, P_N,   // state
+  P_AP, P_CP, P_DP,         // chunk-elimination coefficients a', c', d'
+  P_GR, P_GL, P_SC,         // workspace: g_right, g_left, scale
+  P_FLD,                    // extracellular lead field (runs with ve only)
+  P_GNA, P_GK, P_GLK, P_EL  // per-compartment channels (non-uniform cables only)
+};
+
+struct PlaneLayout {
+  int n_planes;
+  bool field, chan;
+};
+
+__host__ __device__ inline PlaneLayout plane_layout(bool field, bool chan) {
+  // planes past P_SC are packed: field first (if any), then channels
+  PlaneLayout L;
+  L.field = field;
+  L.chan = chan;
+  L.n_planes = P_SC + 1 + (field ? 1 : 0) + (chan ? 4 : 0);
+  return L;
 }
 
-// Select element j_sel of a register array without dynamic indexing.
-template <typename T, int CH>
-__device__ __forceinline__ T pick(const T (&x)[CH], int j_sel) {
-  T out = x[0];
-#pragma unroll
-  for (int j = 1; j < CH; ++j)
-    if (j == j_sel) out = x[j];
-  return out;
-}
+template <typename T>
+struct Planes {
+  T* base;
+  int ch;
+  int q_fld, q_gna;
+  __device__ __forceinline__ T& at(int q, int j, int r) const {
+    return base[(q * ch + j) * 32 + r];
+  }
+};
 
-template <typename T, int CH>
-__device__ __noinline__ void run_cable(const CableArgsT<T>& A, int cable, T* smw) {
-  const int lane = threadIdx.x & 31;
+// One cable, all steps, one warp.  ch = rows per lane (runtime), rows of lane
+// r are i = r*ch + j.  Rows with i >= K are identity rows with zero
+// coefficients and zero state.
+template <typename T>
+__device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
+                          const PlaneLayout& lay, bool chan_uniform) {
+  const int r = threadIdx.x & 31;
   const int64_t off = A.cable_ptr[cable];
   const int K = (int)(A.cable_ptr[cable + 1] - off);
-  const bool use_ve = A.field != nullptr && A.ve_amp != nullptr;
-  const T* fieldp = A.field;
+  Planes<T> P{smw, ch, P_SC + 1, P_SC + 1 + (lay.field ? 1 : 0)};
+  const bool use_ve = lay.field;
 
-  T v[CH], m[CH], h[CH], n[CH];
-#pragma unroll
-  for (int j = 0; j < CH; ++j) {
-    const int i = lane * CH + j;
+  for (int j = 0; j < ch; ++j) {
+    const int i = r * ch + j;
     const bool in = i < K;
     const int64_t g = off + i;
-    v[j] = in ? A.v[g] : T(0);
-    m[j] = in ? A.m[g] : T(0);
-    h[j] = in ? A.h[g] : T(0);
-    n[j] = in ? A.n[g] : T(0);
-    sm<T, CH>(smw, Q_GR, j, lane) = in ? A.g_right[g] : T(0);
-    sm<T, CH>(smw, Q_GL, j, lane) = in ? A.g_left[g] : T(0);
-    sm<T, CH>(smw, Q_SCALE, j, lane) = in ? A.scale[g] : T(0);
-    sm<T, CH>(smw, Q_FIELD, j, lane) = (in && use_ve) ? fieldp[g] : T(0);
-    sm<T, CH>(smw, Q_GNA, j, lane) = in ? A.gnabar[g] : T(0);
-    sm<T, CH>(smw, Q_GK, j, lane) = in ? A.gkbar[g] : T(0);
-    sm<T, CH>(smw, Q_GLK, j, lane) = in ? A.gl[g] : T(0);
-    sm<T, CH>(smw, Q_EL, j, lane) = in ? A.el[g] : T(0);
+    P.at(P_V, j, r) = in ? A.v[g] : T(0);
+    P.at(P_M, j, r) = in ? A.m[g] : T(0);
+    P.at(P_H, j, r) = in ? A.h[g] : T(0);
+    P.at(P_N, j, r) = in ? A.n[g] : T(0);
+    P.at(P_GR, j, r) = in ? A.g_right[g] : T(0);
+    P.at(P_GL, j, r) = in ? A.g_left[g] : T(0);
+    P.at(P_SC, j, r) = in ? A.scale[g] : T(0);
+    if (use_ve) P.at(P.q_fld, j, r) = in ? A.field[g] : T(0);
+    if (lay.chan) {
+      P.at(P.q_gna + 0, j, r) = in ? A.gnabar[g] : T(0);
+      P.at(P.q_gna + 1, j, r) = in ? A.gkbar[g] : T(0);
+      P.at(P.q_gna + 2, j, r) = in ? A.gl[g] : T(0);
+      P.at(P.q_gna + 3, j, r) = in ? A.el[g] : T(0);
+    }
+  }
+  // uniform channels: the cable's values, identical on every compartment
+  T gna_c = T(0), gk_c = T(0), gl_c = T(0), el_c = T(0);
+  if (chan_uniform) {
+    gna_c = A.gnabar[off];
+    gk_c = A.gkbar[off];
+    gl_c = A.gl[off];
+    el_c = A.el[off];
   }
   __syncwarp();
 
-  // Per-cable scalars.
   T ve_amp = T(0), ve_delay = T(0), ve_pw = T(0);
   if (use_ve) {
     ve_amp = A.ve_amp[cable];
@@ -165,97 +196,187 @@ __device__ __noinline__ void run_cable(const CableArgsT<T>& A, int cable, T* smw
     in_pw = A.in_pw[cable];
     in_cm = A.cm_inv[off + in_i];
   }
-  const int in_lane = in_i >= 0 ? in_i / CH : -1, in_j = in_i >= 0 ? in_i % CH : -1;
   const int rec_i = (A.rec_idx && A.trace) ? A.rec_idx[cable] : -1;
-  const int rec_lane = rec_i >= 0 ? rec_i / CH : -1, rec_j = rec_i >= 0 ? rec_i % CH : -1;
   const int spk_i = A.spk_idx ? A.spk_idx[cable] : -1;
-  const int spk_lane = spk_i >= 0 ? spk_i / CH : -1, spk_j = spk_i >= 0 ? spk_i % CH : -1;
   int below = 1, count = 0, first = -1;
-  if (spk_i >= 0 && lane == spk_lane) {
+  if (spk_i >= 0 && r == spk_i / ch) {
     below = A.spk_below[cable];
     count = A.spk_count[cable];
     first = A.spk_first[cable];
   }
-  if (rec_i >= 0 && lane == rec_lane) A.trace[(int64_t)cable * A.n_rec] = pick<T, CH>(v, rec_j);
+  if (rec_i >= 0 && r == rec_i / ch) A.trace[(int64_t)cable * A.n_rec] = P.at(P_V, rec_i % ch, r);
 
   const T dt = A.dt, dt_s = A.dt_s, q10 = A.q10, ena = A.ena, ek = A.ek;
+  const int last = ch - 1;
   for (int s = 0; s < A.n_steps; ++s) {
     const T t = (T)(A.t0_ms + (double)(A.step0 + s) * A.dt_ms_d);
     const T Ive = use_ve ? rect_pulse<T>(t, ve_amp, ve_delay, ve_pw) : T(0);
     const T Iin = (in_i >= 0) ? rect_pulse<T>(t, in_amp, in_delay, in_pw) : T(0);
-    // halo voltages from the neighbouring lanes
-    T v_lo = shfl_up<T>(v[CH - 1], 1, 32);
-    T v_hi = shfl_down<T>(v[0], 1, 32);
-    T a[CH], b[CH], c[CH], d[CH];
-#pragma unroll
-    for (int j = 0; j < CH; ++j) {
-      const T vj = v[j];
-      hh_gates<T>(vj, q10, dt, m[j], h[j], n[j]);
+    const bool ve_on = Ive != T(0);  // per cable: warp-uniform
+
+    // ---- phase A: gates, membrane frame, row assembly fused with the
+    //      forward sweep of the chunk elimination (chunk_solve.cuh, step 1)
+    T As = T(0), Bs = T(1), Cs = T(0), Ds = T(0);
+    T ap = T(0), cp = T(0), dp = T(0);
+    T v_prev = (r > 0) ? P.at(P_V, last, r - 1) : T(0);
+    T vj = P.at(P_V, 0, r);
+    T f_prev = T(0), fj = T(0);
+    if (ve_on) {
+      f_prev = (r > 0) ? P.at(P.q_fld, last, r - 1) : T(0);
+      fj = P.at(P.q_fld, 0, r);
+    }
+    for (int j = 0; j < ch; ++j) {
+      const T v_next = (j < last) ? P.at(P_V, j + 1, r) : ((r < 31) ? P.at(P_V, 0, r + 1) : T(0));
+      T m = P.at(P_M, j, r), h = P.at(P_H, j, r), n = P.at(P_N, j, r);
+      hh_gates<T>(vj, q10, dt, m, h, n);
+      P.at(P_M, j, r) = m;
+      P.at(P_H, j, r) = h;
+      P.at(P_N, j, r) = n;
       T G, J;
-      hh_affine<T>(m[j], h[j], n[j], sm<T, CH>(smw, Q_GNA, j, lane),
-                   sm<T, CH>(smw, Q_GK, j, lane), sm<T, CH>(smw, Q_GLK, j, lane),
-                   sm<T, CH>(smw, Q_EL, j, lane), ena, ek, G, J);
-      const T scl = sm<T, CH>(smw, Q_SCALE, j, lane);
-      const T gr = sm<T, CH>(smw, Q_GR, j, lane);
-      const T glf = sm<T, CH>(smw, Q_GL, j, lane);
-      const T vl = (j == 0) ? v_lo : v[j - 1];
-      const T vr = (j == CH - 1) ? v_hi : v[j + 1];
-      T fn = (J - G * vj) * scl;
-      fn = fn + (gr * (vr - vj) - glf * (vj - vl));
-      d[j] = fn;
-      b[j] = T(1) - dt_s * ((-gr + -glf) - G * scl);
-      a[j] = -dt_s * glf;
-      c[j] = -dt_s * gr;
-    }
-    if (Ive != T(0)) {  // warp-uniform: the pulse is per cable
-      T ve[CH];
-#pragma unroll
-      for (int j = 0; j < CH; ++j) ve[j] = sm<T, CH>(smw, Q_FIELD, j, lane) * Ive;
-      T ve_lo = shfl_up<T>(ve[CH - 1], 1, 32);
-      T ve_hi = shfl_down<T>(ve[0], 1, 32);
-#pragma unroll
-      for (int j = 0; j < CH; ++j) {
-        const T gr = sm<T, CH>(smw, Q_GR, j, lane);
-        const T glf = sm<T, CH>(smw, Q_GL, j, lane);
-        const T el_ = (j == 0) ? ve_lo : ve[j - 1];
-        const T er_ = (j == CH - 1) ? ve_hi : ve[j + 1];
-        d[j] = d[j] + (gr * (er_ - ve[j]) - glf * (ve[j] - el_));
+      if (lay.chan) {
+        hh_affine<T>(m, h, n, P.at(P.q_gna, j, r), P.at(P.q_gna + 1, j, r),
+                     P.at(P.q_gna + 2, j, r), P.at(P.q_gna + 3, j, r), ena, ek, G, J);
+      } else {
+        hh_affine<T>(m, h, n, gna_c, gk_c, gl_c, el_c, ena, ek, G, J);
       }
+      const T scl = P.at(P_SC, j, r);
+      const T gr = P.at(P_GR, j, r);
+      const T glf = P.at(P_GL, j, r);
+      // row i couples to i-1 through glf and to i+1 through gr; at a cable
+      // end (or past it) that coefficient is exactly zero
+      T fn = (J - G * vj) * scl;
+      fn = fn + (gr * (v_next - vj) - glf * (vj - v_prev));
+      if (ve_on) {
+        const T f_next = (j < last) ? P.at(P.q_fld, j + 1, r)
+                                    : ((r < 31) ? P.at(P.q_fld, 0, r + 1) : T(0));
+        const T ve_l = f_prev * Ive, ve_c = fj * Ive, ve_r = f_next * Ive;
+        fn = fn + (gr * (ve_r - ve_c) - glf * (ve_c - ve_l));
+        f_prev = fj;
+        fj = f_next;
+      }
+      if (r * ch + j == in_i) fn = fn + Iin * in_cm;
+      const T b = T(1) - dt_s * ((-gr + -glf) - G * scl);
+      const T a = -dt_s * glf;
+      const T c = -dt_s * gr;
+      const T d = dt_s * fn;
+      if (j == 0) {
+        As = a;
+        Bs = b;
+        Cs = c;
+        Ds = d;
+      } else if (j == 1) {
+        const T rinv = T(1) / b;
+        ap = a * rinv;
+        cp = c * rinv;
+        dp = d * rinv;
+      } else {
+        const T rinv = T(1) / (b - a * cp);
+        ap = -a * ap * rinv;
+        dp = (d - a * dp) * rinv;
+        cp = c * rinv;
+      }
+      if (j >= 1) {
+        P.at(P_AP, j, r) = ap;
+        P.at(P_CP, j, r) = cp;
+        P.at(P_DP, j, r) = dp;
+      }
+      v_prev = vj;
+      vj = v_next;
     }
-    if (Iin != T(0) && lane == in_lane) {
-#pragma unroll
-      for (int j = 0; j < CH; ++j)
-        if (j == in_j) d[j] = d[j] + Iin * in_cm;
+    // ---- phase B: backward sweep (rows ch-3 .. 1) and the reduced row
+    T al, be, ga, de, Ae = ap, Ce = cp, De = dp;
+    if (ch == 1) {
+      al = As;
+      be = Bs;
+      ga = Cs;
+      de = Ds;
+    } else {
+      T a2 = ap, c2 = cp, d2 = dp;  // row ch-2 after the loop below
+      if (ch >= 3) {
+        a2 = P.at(P_AP, ch - 2, r);
+        c2 = P.at(P_CP, ch - 2, r);
+        d2 = P.at(P_DP, ch - 2, r);
+        for (int j = ch - 3; j >= 1; --j) {
+          const T cj = P.at(P_CP, j, r);
+          d2 = P.at(P_DP, j, r) - cj * d2;
+          a2 = P.at(P_AP, j, r) - cj * a2;
+          c2 = -cj * c2;
+          P.at(P_AP, j, r) = a2;
+          P.at(P_CP, j, r) = c2;
+          P.at(P_DP, j, r) = d2;
+        }
+      }
+      T Bs2 = Bs, Cs2 = Cs, Ds2 = Ds;
+      if (ch >= 3) {
+        Bs2 = Bs - Cs * a2;
+        Cs2 = -Cs * c2;
+        Ds2 = Ds - Cs * d2;
+      }
+      T Ae_l = shfl_up<T>(Ae, 1, 32), Ce_l = shfl_up<T>(Ce, 1, 32), De_l = shfl_up<T>(De, 1, 32);
+      if (r == 0) {
+        Ae_l = T(0);
+        Ce_l = T(0);
+        De_l = T(0);
+      }
+      al = -As * Ae_l;
+      be = Bs2 - As * Ce_l - Cs2 * Ae;
+      ga = -Cs2 * Ce;
+      de = Ds2 - As * De_l - Cs2 * De;
     }
+    // ---- phase C: PCR across the 32 lanes, then back-substitution
 #pragma unroll
-    for (int j = 0; j < CH; ++j) d[j] = dt_s * d[j];
-    chunk_solve<T, CH, 32>(a, b, c, d, lane);
-#pragma unroll
-    for (int j = 0; j < CH; ++j) v[j] = v[j] + d[j];
-    if (spk_i >= 0 && lane == spk_lane) {
-      const T vs = pick<T, CH>(v, spk_j);
-      const int above = vs >= A.spk_thr;
+    for (int sh = 1; sh < 32; sh <<= 1) {
+      T al_l = shfl_up<T>(al, sh, 32), be_l = shfl_up<T>(be, sh, 32);
+      T ga_l = shfl_up<T>(ga, sh, 32), de_l = shfl_up<T>(de, sh, 32);
+      T al_r = shfl_down<T>(al, sh, 32), be_r = shfl_down<T>(be, sh, 32);
+      T ga_r = shfl_down<T>(ga, sh, 32), de_r = shfl_down<T>(de, sh, 32);
+      const bool hl = r >= sh;
+      const bool hr = r + sh < 32;
+      T k1 = hl ? al / be_l : T(0);
+      T k2 = hr ? ga / be_r : T(0);
+      T al_n = hl ? -k1 * al_l : T(0);
+      T ga_n = hr ? -k2 * ga_r : T(0);
+      be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
+      de = de - (hl ? k1 * de_l : T(0)) - (hr ? k2 * de_r : T(0));
+      al = al_n;
+      ga = ga_n;
+    }
+    const T xs = de / be;
+    T xe = xs;
+    if (ch > 1) {
+      T xs_next = shfl_down<T>(xs, 1, 32);
+      if (r == 31) xs_next = T(0);
+      xe = De - Ae * xs - Ce * xs_next;
+    }
+    __syncwarp();  // every lane has read its neighbours' v for this step
+    P.at(P_V, 0, r) = P.at(P_V, 0, r) + xs;
+    for (int j = 1; j < last; ++j)
+      P.at(P_V, j, r) = P.at(P_V, j, r) + (P.at(P_DP, j, r) - P.at(P_AP, j, r) * xs -
+                                           P.at(P_CP, j, r) * xe);
+    if (ch > 1) P.at(P_V, last, r) = P.at(P_V, last, r) + xe;
+    if (spk_i >= 0 && r == spk_i / ch) {
+      const int above = P.at(P_V, spk_i % ch, r) >= A.spk_thr;
       if (above && below) {
         if (count == 0) first = s + 1;
         count += 1;
       }
       below = !above;
     }
-    if (rec_i >= 0 && lane == rec_lane && ((s + 1) % A.rec_every) == 0)
-      A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = pick<T, CH>(v, rec_j);
+    if (rec_i >= 0 && r == rec_i / ch && ((s + 1) % A.rec_every) == 0)
+      A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = P.at(P_V, rec_i % ch, r);
+    __syncwarp();  // new v visible to the neighbouring lanes
   }
-#pragma unroll
-  for (int j = 0; j < CH; ++j) {
-    const int i = lane * CH + j;
+  for (int j = 0; j < ch; ++j) {
+    const int i = r * ch + j;
     if (i < K) {
       const int64_t g = off + i;
-      A.v[g] = v[j];
-      A.m[g] = m[j];
-      A.h[g] = h[j];
-      A.n[g] = n[j];
+      A.v[g] = P.at(P_V, j, r);
+      A.m[g] = P.at(P_M, j, r);
+      A.h[g] = P.at(P_H, j, r);
+      A.n[g] = P.at(P_N, j, r);
     }
   }
-  if (spk_i >= 0 && lane == spk_lane) {
+  if (spk_i >= 0 && r == spk_i / ch) {
     A.spk_below[cable] = below;
     A.spk_count[cable] = count;
     A.spk_first[cable] = first;
@@ -263,10 +384,39 @@ __device__ __noinline__ void run_cable(const CableArgsT<T>& A, int cable, T* smw
   __syncwarp();
 }
 
-constexpr int kCableMaxCH = 16;  // K <= 512
+constexpr int kCableWarps = 4;  // default warps (cables in flight) per block
 
-// float64 runs (small, latency-bound populations) use fewer chunk
-// instantiations; rows past the cable end are identity rows.
+template <typename T>
+__global__ void __launch_bounds__(kCableWarps * 32) cable_run_kernel(CableArgsT<T> A, int ch_max,
+                                                                     PlaneLayout lay,
+                                                                     int chan_uniform) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5;
+  T* smw = reinterpret_cast<T*>(smem_raw) + (size_t)warp * lay.n_planes * ch_max * 32;
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(A.counter, 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= A.n_cables) break;
+    const int cable = A.order ? A.order[idx] : idx;
+    const int K = (int)(A.cable_ptr[cable + 1] - A.cable_ptr[cable]);
+    const int ch = (K + 31) / 32;
+    if (ch > ch_max) {  // the host sized shared memory for smaller cables: flag, never skip silently
+      if (lane == 0) atomicOr(A.counter + 1, kErrChunk);
+      continue;
+    }
+    run_cable<T>(A, cable, smw, ch, lay, chan_uniform != 0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Plain per-step path.
+// ---------------------------------------------------------------------------
+
+// Chunk sizes compiled for the register-resident per-step solve: all of
+// 1..16 in float32; float64 rounds up to 1, 2, 4, 8, 16 (extra rows are
+// identity rows).
 template <typename T>
 __device__ __forceinline__ int chunk_round(int ch) {
   if constexpr (sizeof(T) == 8) {
@@ -276,34 +426,6 @@ __device__ __forceinline__ int chunk_round(int ch) {
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(128) cable_run_kernel(CableArgsT<T> A, int ch_max) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* smw = reinterpret_cast<T*>(smem_raw) + (size_t)(threadIdx.x >> 5) * kNConst * ch_max * 32;
-  const int lane = threadIdx.x & 31;
-  for (;;) {
-    int idx = 0;
-    if (lane == 0) idx = atomicAdd(A.counter, 1);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
-    if (idx >= A.n_cables) break;
-    const int cable = A.order ? A.order[idx] : idx;
-    const int K = (int)(A.cable_ptr[cable + 1] - A.cable_ptr[cable]);
-    const int ch = chunk_round<T>((K + 31) / 32);
-    switch (ch) {
-#define DGB_CASE(CHV)                  \
-  case CHV:                            \
-    run_cable<T, CHV>(A, cable, smw);  \
-    break;
-      DGB_CHUNK_CASES(T)
-#undef DGB_CASE
-      default:
-        break;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Plain per-step path.
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void cable_assemble_kernel(CableArgsT<T> A, const int32_t* __restrict__ comp_cable,
@@ -401,44 +523,33 @@ __global__ void __launch_bounds__(128) cable_solve_update_kernel(CableArgsT<T> A
   }
 }
 
-inline int validate_cable_args(const dgb_cable_args* a) {
-  DGB_REQUIRE(a != nullptr, "args must be non-null");
-  DGB_REQUIRE(a->dtype == DGB_F32 || a->dtype == DGB_F64, "dtype must be DGB_F32 or DGB_F64");
-  DGB_REQUIRE(a->n_cables >= 0 && a->n_steps >= 0, "n_cables and n_steps must be >= 0");
-  DGB_REQUIRE(a->cable_ptr && a->v && a->m && a->h && a->n, "cable_ptr and v/m/h/n are required");
-  DGB_REQUIRE(a->g_right && a->g_left && a->scale && a->cm_inv,
-              "g_right, g_left, scale and cm_inv are required");
-  DGB_REQUIRE(a->gnabar && a->gkbar && a->gl && a->el, "gnabar, gkbar, gl and el are required");
-  DGB_REQUIRE(!a->in_idx || (a->in_amp && a->in_delay && a->in_pw),
-              "in_idx requires in_amp, in_delay and in_pw");
-  DGB_REQUIRE(!a->ve_amp || (a->field && a->ve_delay && a->ve_pw),
-              "ve_amp requires field, ve_delay and ve_pw");
-  DGB_REQUIRE(!a->spk_idx || (a->spk_below && a->spk_count && a->spk_first),
-              "spk_idx requires spk_below, spk_count and spk_first");
-  DGB_REQUIRE(!a->trace || a->rec_idx, "trace requires rec_idx");
-  DGB_REQUIRE(a->rec_every >= 1, "rec_every must be >= 1");
-  DGB_REQUIRE(a->lanes == 0, "lanes is reserved and must be 0");
-  return DGB_OK;
-}
-
 template <typename T>
 int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st) {
   CableArgsT<T> A = typed<T>(args);
-  const int threads = 128;
-  const size_t smem = (size_t)(threads / 32) * kNConst * ch_max * 32 * sizeof(T);
+  const bool field = args->field != nullptr && args->ve_amp != nullptr;
+  const bool chan_uniform = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) != 0;
+  const PlaneLayout lay = plane_layout(field, !chan_uniform);
+  // one warp per cable in flight; long cables get fewer warps per block so
+  // the block's planes fit the 227 KB shared-memory limit
+  const size_t per_warp = (size_t)lay.n_planes * ch_max * 32 * sizeof(T);
+  int wpb = kCableWarps;
+  while (wpb > 1 && (size_t)wpb * per_warp > 227 * 1024) wpb >>= 1;
+  DGB_REQUIRE((size_t)wpb * per_warp <= 227 * 1024,
+              "cable too long for shared memory (%zu bytes per cable)", per_warp);
+  const int threads = wpb * 32;
+  const size_t smem = (size_t)wpb * per_warp;
   DGB_CUDA_CHECK(cudaFuncSetAttribute(cable_run_kernel<T>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cable_run_kernel<T>,
                                                                threads, smem));
   if (per_sm < 1) per_sm = 1;
-  const int warps_needed = A.n_cables;
   int blocks = device_sm_count() * per_sm;
-  const int blocks_needed = (warps_needed + 3) / 4;
+  const int blocks_needed = (A.n_cables + wpb - 1) / wpb;
   if (blocks > blocks_needed) blocks = blocks_needed;
   if (blocks < 1) blocks = 1;
-  DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, sizeof(int32_t), st));
-  cable_run_kernel<T><<<blocks, threads, smem, st>>>(A, ch_max);
+  DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, 2 * sizeof(int32_t), st));
+  cable_run_kernel<T><<<blocks, threads, smem, st>>>(A, ch_max, lay, chan_uniform ? 1 : 0);
   DGB_LAUNCH_CHECK();
   return DGB_OK;
 }

@@ -88,19 +88,31 @@ __device__ __forceinline__ void chunk_solve(T (&a)[CH], T (&b)[CH], T (&c)[CH], 
       Ds = d[0] - c[0] * d[1];
     }
   }
-  // Eliminate the x_e unknowns: one row per lane in x_s.
-  T Ae_l = shfl_up<T>(Ae, 1, P);
-  T Ce_l = shfl_up<T>(Ce, 1, P);
-  T De_l = shfl_up<T>(De, 1, P);
-  if (r == 0) {
-    Ae_l = T(0);
-    Ce_l = T(0);
-    De_l = T(0);
+  T al, be, ga, de;
+  if constexpr (CH == 1) {
+    // one row per lane: it already couples only the neighbouring lanes' rows
+    al = As;
+    be = Bs;
+    ga = Cs;
+    de = Ds;
+    (void)Ae;
+    (void)Ce;
+    (void)De;
+  } else {
+    // Eliminate the x_e unknowns: one row per lane in x_s.
+    T Ae_l = shfl_up<T>(Ae, 1, P);
+    T Ce_l = shfl_up<T>(Ce, 1, P);
+    T De_l = shfl_up<T>(De, 1, P);
+    if (r == 0) {
+      Ae_l = T(0);
+      Ce_l = T(0);
+      De_l = T(0);
+    }
+    al = -As * Ae_l;
+    be = Bs - As * Ce_l - Cs * Ae;
+    ga = -Cs * Ce;
+    de = Ds - As * De_l - Cs * De;
   }
-  T al = -As * Ae_l;
-  T be = Bs - As * Ce_l - Cs * Ae;
-  T ga = -Cs * Ce;
-  T de = Ds - As * De_l - Cs * De;
   // Parallel cyclic reduction across the P lanes.
 #pragma unroll
   for (int s = 1; s < P; s <<= 1) {

@@ -146,14 +146,19 @@ typedef struct dgb_cable_args {
   int32_t* spk_count;
   int32_t* spk_first;
   /* sizes known to the host: largest cable and total compartments */
-  int32_t max_k;       /* max over cables of K (<= 512) */
-  int32_t lanes;       /* reserved, must be 0 */
+  int32_t max_k;       /* max over cables of K */
+  int32_t flags;       /* DGB_CABLE_* bits */
   int64_t n_comp;      /* cable_ptr[n_cables] */
   /* cable index of every compartment, int32[n_comp] (assembly kernel only) */
   const int32_t* comp_cable;
-  /* scratch: one int32 work counter, device (dgb_cable_run only) */
+  /* scratch, int32[2] on the device (dgb_cable_run only): [0] work counter,
+     [1] error bits after the run (0 = every cable advanced) */
   int32_t* scratch;
 } dgb_cable_args;
+
+/* dgb_cable_args.flags: gnabar, gkbar, gl and el are constant within each
+   cable (the kernel then reads them once per cable) */
+#define DGB_CABLE_UNIFORM_CHANNELS 1
 
 /*
  * Run n_steps backward-Euler + cnexp steps of every cable in one persistent

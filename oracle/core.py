@@ -69,7 +69,7 @@ def _declare(L):
             _I64, _I64, _P, _P, _P, _P, _P, _P, _I32, _P]
         getattr(L, "orc_cable_run" + sfx).argtypes = (
             [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
-            + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P]
+            + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P, _I32]
         )
     L.orc_num_threads.restype = ctypes.c_int
 
@@ -166,13 +166,16 @@ def dhs_solve(d, a, b, parent, order, layer_ptr):
     return x
 
 
-def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0):
+def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
+              gate_f32: bool = False):
     """Run the HH cable update on a packed problem dict (see dendra_gb300.cable).
 
     ``p`` holds numpy arrays: cable_ptr, v, m, h, n (modified in place),
     g_right, g_left, scale, cm_inv, field (or None), gnabar, gkbar, gl, el,
     ve_amp/ve_delay/ve_pw (or None), in_idx/in_amp/in_delay/in_pw (or None),
     rec_idx, spk_idx, and scalars ena, ek, q10, dt_ms, dt_s, spk_thr.
+    ``gate_f32`` evaluates the pulse gates on a float32 time grid (how a
+    float32 model sees its pulses) while the arithmetic stays in p's dtype.
     Returns (trace, spk_count, spk_first, spk_below).
     """
     dtype = p["v"].dtype
@@ -211,6 +214,6 @@ def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0):
         _ptr(keep["in_idx"]), _ptr(keep["in_amp"]), _ptr(keep["in_delay"]),
         _ptr(keep["in_pw"]), _ptr(keep["rec_idx"]), _ptr(trace),
         _ptr(keep["spk_idx"]), float(p.get("spk_thr", 0.0)), _ptr(spk_below),
-        _ptr(spk_count), _ptr(spk_first),
+        _ptr(spk_count), _ptr(spk_first), int(bool(gate_f32)),
     )
     return trace, spk_count, spk_first, spk_below

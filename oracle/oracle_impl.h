@@ -211,8 +211,17 @@ void F(orc_pcr)(int64_t K, const REAL* a_in, const REAL* b_in, const REAL* c_in,
   free(buf);
 }
 
-/* Rectangular pulse gate on [delay, delay+pw) at time t (_gates.py:50-65). */
-static REAL F(rect)(REAL t, REAL amp, REAL delay, REAL pw) {
+/* Rectangular pulse gate on [delay, delay+pw) at time t (_gates.py:50-65).
+   The reference forms the time grid and delay+pw in the state dtype, so a
+   float64 judge of a float32 run evaluates the gate in float32 (gate_f32). */
+static REAL F(rect)(double t0_ms, int32_t s, double dt_ms, REAL amp, REAL delay, REAL pw,
+                    int32_t gate_f32) {
+  if (gate_f32) {
+    float t = (float)(t0_ms + (double)s * dt_ms);
+    float d = (float)delay, stop = (float)delay + (float)pw;
+    return (t >= d && t < stop) ? amp : (REAL)0;
+  }
+  REAL t = (REAL)(t0_ms + (double)s * dt_ms);
   REAL stop = delay + pw;
   return (t >= delay && t < stop) ? amp : (REAL)0;
 }
@@ -232,7 +241,8 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
                       const REAL* ve_pw, const int32_t* in_idx, const REAL* in_amp,
                       const REAL* in_delay, const REAL* in_pw, const int32_t* rec_idx,
                       REAL* trace, const int32_t* spk_idx, double spk_thr_d,
-                      int32_t* spk_below, int32_t* spk_count, int32_t* spk_first) {
+                      int32_t* spk_below, int32_t* spk_count, int32_t* spk_first,
+                      int32_t gate_f32) {
   const REAL ena = (REAL)ena_d, ek = (REAL)ek_d, q10 = (REAL)q10_d;
   const REAL dt = (REAL)dt_ms_d, dt_s = (REAL)dt_s_d, thr = (REAL)spk_thr_d;
   const int64_t n_rec = 1 + (int64_t)n_steps / (rec_every > 0 ? rec_every : 1);
@@ -264,11 +274,10 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
       if (trace && ri >= 0) trace[(int64_t)c * n_rec] = vv[ri];
       for (int32_t s = 0; s < n_steps; ++s) {
         /* stimulus time of this step: binary64 grid cast to the state dtype */
-        const REAL t = (REAL)(t0_ms + (double)s * dt_ms_d);
         REAL ve_i = (REAL)0;
         const int use_ve = field && ve_amp;
         if (use_ve) {
-          REAL I = F(rect)(t, ve_amp[c], ve_delay[c], ve_pw[c]);
+          REAL I = F(rect)(t0_ms, s, dt_ms_d, ve_amp[c], ve_delay[c], ve_pw[c], gate_f32);
           for (int64_t i = 0; i < K; ++i) ve[i] = field[o + i] * I;
         }
         (void)ve_i;
@@ -316,7 +325,7 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
         }
         if (in_idx && in_amp && in_idx[c] >= 0) {
           int32_t ii = in_idx[c];
-          REAL I = F(rect)(t, in_amp[c], in_delay[c], in_pw[c]);
+          REAL I = F(rect)(t0_ms, s, dt_ms_d, in_amp[c], in_delay[c], in_pw[c], gate_f32);
           for (int64_t i = 0; i < K; ++i) {
             REAL inj = (i == ii) ? I : (REAL)0;
             fn[i] = fn[i] + inj * cm_inv[o + i];

@@ -29,9 +29,17 @@ def golden_extra_population(g, dtype, device="cpu"):
     return pop.initialize(float(g["dt"]))
 
 
-def oracle_traces(pop, steps, comps, spk_idx=None):
+def as_f64(p):
+    """Widen a problem dict's float arrays to float64 (the float64 judge of a run)."""
+    return {k: (v.astype(np.float64) if isinstance(v, np.ndarray) and v.dtype.kind == "f" else v)
+            for k, v in p.items()}
+
+
+def oracle_traces(pop, steps, comps, spk_idx=None, judge64=False):
     """Run the oracle from pop's current state once per recorded compartment.
 
+    judge64: run in float64 on the population's (float32) inputs, with the
+    pulse gates on the float32 time grid the population itself sees.
     Returns (traces (steps+1, B, len(comps)), final problem dict, spikes).
     """
     import oracle
@@ -39,12 +47,15 @@ def oracle_traces(pop, steps, comps, spk_idx=None):
     out = []
     final = None
     spikes = None
+    gate_f32 = judge64 and pop.dtype == torch.float32
     for c in comps:
         p = pop.problem_dict()
+        if judge64:
+            p = as_f64(p)
         p["rec_idx"] = np.full(pop.B, int(c), dtype=np.int32)
         if spk_idx is not None:
             p["spk_idx"] = np.full(pop.B, int(spk_idx), dtype=np.int32)
-        tr, cnt, first, _ = oracle.cable_run(p, steps)
+        tr, cnt, first, _ = oracle.cable_run(p, steps, gate_f32=gate_f32)
         out.append(tr)
         final = p
         spikes = (cnt, first)

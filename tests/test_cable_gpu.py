@@ -6,6 +6,7 @@ import torch
 
 import oracle
 from tests._cases import (
+    as_f64,
     golden_cable_population,
     golden_extra_population,
     oracle_traces,
@@ -48,24 +49,31 @@ def test_float64_run_matches_reference(cuda, golden, which):
 
 @pytest.mark.parametrize("which", ["cable", "extra"])
 def test_float32_run_within_tolerance_of_float64_judge(cuda, golden, which):
-    g64 = golden(f"hh_{which}_f64.npz")
+    """float32 GPU run vs the float64 oracle on the same inputs and pulse grid.
+
+    The reference's own float32 run is held to the same judge; its error sets
+    the scale next to the 1e-3 mV bound.  Spike steps must equal those of the
+    reference's float32 run exactly.
+    """
     g32 = golden(f"hh_{which}_f32.npz")
     make = golden_cable_population if which == "cable" else golden_extra_population
     tr, _ = _gpu_traces(make, g32, torch.float32, cuda, g32["trace_comps"])
-    ref64 = g64["v_trace"]
-    ref_own = np.abs(g32["v_trace"] - ref64).max()  # the reference's own float32 error
-    err = np.abs(tr - ref64).max()
-    print(f"{which}: gpu f32 vs f64 judge {err:.3e} mV; reference f32 {ref_own:.3e} mV")
+    judge, _, _ = oracle_traces(make(g32, torch.float32), int(g32["steps"]), g32["trace_comps"],
+                                judge64=True)
+    ref_own = np.abs(g32["v_trace"] - judge).max()
+    err = np.abs(tr - judge).max()
+    print(f"{which}: gpu f32 vs f64 judge {err:.3e} mV; reference f32 vs judge {ref_own:.3e} mV")
     assert err <= max(F32_MV, 2.0 * ref_own)
-    for c in range(ref64.shape[2]):
-        assert _spike_steps(tr[:, :, c]) == _spike_steps(ref64[:, :, c])
+    for c in range(judge.shape[2]):
+        assert _spike_steps(tr[:, :, c]) == _spike_steps(g32["v_trace"][:, :, c])
+        assert _spike_steps(tr[:, :, c]) == _spike_steps(judge[:, :, c])
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_ragged_population_matches_oracle(cuda, dtype):
-    """Every chunk size: K from 1 to 512 in one launch, extracellular + intra drive."""
+    """Every chunk size: K from 1 to 1024 in one launch, extracellular + intra drive."""
     ks = [1, 2, 3, 17, 31, 32, 33, 63, 64, 65, 97, 128, 129, 200, 255, 256, 257, 301, 384,
-          401, 416, 417, 448, 480, 481, 511, 512]
+          401, 416, 417, 448, 480, 481, 511, 512, 777, 1024]
     from dendra_gb300.cable import CablePopulation
 
     rng = np.random.default_rng(5)
@@ -80,16 +88,17 @@ def test_ragged_population_matches_oracle(cuda, dtype):
     pop.inject(torch.as_tensor([k // 2 for k in ks]),
                torch.as_tensor(rng.uniform(0.1, 1.0, len(ks)) * 1e-6), 0.2, 0.5)
     pop.initialize(0.005)
-    p64 = pop.problem_dict()
-    p64 = {k: (v.astype(np.float64) if isinstance(v, np.ndarray) and v.dtype.kind == "f" else v)
-           for k, v in p64.items()}
+    p64 = as_f64(pop.problem_dict())
     steps = 300
     rec = np.array([k - 1 for k in ks], dtype=np.int32)
     p64["rec_idx"] = rec
     p64["spk_idx"] = rec
-    tr_ref, cnt_ref, first_ref, _ = oracle.cable_run(p64, steps)
+    tr_ref, cnt_ref, first_ref, _ = oracle.cable_run(p64, steps,
+                                                     gate_f32=dtype == torch.float32)
     res = pop.run(steps, rec_idx=torch.as_tensor(rec), spk_idx=torch.as_tensor(rec))
+    pop.check_status()
     tr = res.trace.double().cpu().numpy()
+    assert np.isfinite(tr).all()
     tol = 1e-8 if dtype == torch.float64 else 5e-2
     err = np.abs(tr - tr_ref).max()
     print("ragged", dtype, err)
