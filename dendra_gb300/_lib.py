@@ -20,6 +20,8 @@ F64 = 1
 THOMAS = 0
 PCR = 1
 CABLE_UNIFORM_CHANNELS = 1
+CABLE_UNIFORM_GEOMETRY = 2
+CABLE_FAST_MATH = 4
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32

@@ -114,7 +114,8 @@ class CablePopulation:
     """
 
     def __init__(self, n_comp, diam, dx, *, rhoa=100.0, cm=1.0, celsius=6.3, v_init=-65.0,
-                 dtype=torch.float32, device="cuda", hh=None):
+                 dtype=torch.float32, device="cuda", hh=None, fast_math=False,
+                 compress_uniform=True):
         n_comp = [int(k) for k in n_comp]
         if not n_comp:
             raise ValueError("a population needs at least one cable")
@@ -140,6 +141,10 @@ class CablePopulation:
         self.ena = float(hh["ena"])
         self.ek = float(hh["ek"])
         self._chan = {k: self._per_comp(hh[k]) for k in ("gnabar", "gkbar", "gl", "el")}
+        if fast_math and dtype != torch.float32:
+            raise ValueError("fast_math applies to float32 state only")
+        self.fast_math = bool(fast_math)
+        self.compress_uniform = bool(compress_uniform)
         self.field = None
         self.ve = None
         self.intra = None
@@ -235,7 +240,8 @@ class CablePopulation:
         if self.intra is not None:
             d["in_idx"], d["in_amp"], d["in_delay"], d["in_pw"] = (x.to(dev) for x in self.intra)
         self._dev = d
-        self.uniform_channels = self._channels_uniform()
+        self.uniform_channels = self.compress_uniform and self._channels_uniform()
+        self.uniform_geometry = self.compress_uniform and self._geometry_uniform(ws)
         self.v = v.to(dev)
         self.m, self.h, self.n = m.to(dev), h.to(dev), n.to(dev)
         self.t = 0.0
@@ -249,6 +255,22 @@ class CablePopulation:
         for t in self._chan.values():
             if bool(((t[1:] != t[:-1]) & same_cable).any()):
                 return False
+        return True
+
+    def _geometry_uniform(self, ws):
+        """True when g_right / g_left (interior edges) and scale are constant per cable."""
+        cab = torch.as_tensor(np.repeat(np.arange(self.B), self.n_comp))
+        same = cab[1:] == cab[:-1]
+        gr, gl, sc = ws["g_right"], ws["g_left"], ws["scale"]
+        # g_right on compartments i < K-1 and g_left on i > 0 are the interior edges
+        gr_in = gr[:-1][same]
+        gl_in = gl[1:][same]
+        cab_edges = cab[:-1][same]
+        for t in (gr_in, gl_in):
+            if t.numel() > 1 and bool(((t[1:] != t[:-1]) & (cab_edges[1:] == cab_edges[:-1])).any()):
+                return False
+        if bool(((sc[1:] != sc[:-1]) & same).any()):
+            return False
         return True
 
     def _args(self, n_steps=0, rec_every=1, rec_idx=None, trace=None, spk=None, spk_thr=0.0):
@@ -279,7 +301,9 @@ class CablePopulation:
             a.spk_idx, a.spk_below, a.spk_count, a.spk_first = (t.data_ptr() for t in spk)
             a.spk_thr = float(spk_thr)
         a.max_k = max(self.n_comp)
-        a.flags = _lib.CABLE_UNIFORM_CHANNELS if self.uniform_channels else 0
+        a.flags = ((_lib.CABLE_UNIFORM_CHANNELS if self.uniform_channels else 0)
+                   | (_lib.CABLE_UNIFORM_GEOMETRY if self.uniform_geometry else 0)
+                   | (_lib.CABLE_FAST_MATH if self.fast_math else 0))
         a.n_comp = self.N
         a.comp_cable = d["comp_cable"].data_ptr()
         a.scratch = d["scratch"].data_ptr()

@@ -36,7 +36,11 @@ inline int validate_cable_args(const dgb_cable_args* a) {
               "spk_idx requires spk_below, spk_count and spk_first");
   DGB_REQUIRE(!a->trace || a->rec_idx, "trace requires rec_idx");
   DGB_REQUIRE(a->rec_every >= 1, "rec_every must be >= 1");
-  DGB_REQUIRE((a->flags & ~DGB_CABLE_UNIFORM_CHANNELS) == 0, "unknown flags %d", a->flags);
+  DGB_REQUIRE((a->flags & ~(DGB_CABLE_UNIFORM_CHANNELS | DGB_CABLE_UNIFORM_GEOMETRY |
+                             DGB_CABLE_FAST_MATH)) == 0,
+              "unknown flags %d", a->flags);
+  DGB_REQUIRE(!(a->flags & DGB_CABLE_FAST_MATH) || a->dtype == DGB_F32,
+              "DGB_CABLE_FAST_MATH applies to float32 state only");
   return DGB_OK;
 }
 

@@ -108,26 +108,27 @@ constexpr int kErrChunk = 1;
 
 // Shared-memory planes of one warp (one cable).  Plane q holds row j of lane r
 // at [(q * ch + j) * 32 + r]: the 32 lanes touch 32 consecutive words, so
-// every access is bank-conflict free for any chunk size ch.
-enum {
-  P_V = 0, P_M, P_H, P_N,   // state
-  P_AP, P_CP, P_DP,         // chunk-elimination coefficients a', c', d'
-  P_GR, P_GL, P_SC,         // workspace: g_right, g_left, scale
-  P_FLD,                    // extracellular lead field (runs with ve only)
-  P_GNA, P_GK, P_GLK, P_EL  // per-compartment channels (non-uniform cables only)
-};
+// every access is bank-conflict free for any chunk size ch.  Planes 0..6 are
+// always present; the rest only when a coefficient varies along the cable.
+enum { P_V = 0, P_M, P_H, P_N, P_AP, P_CP, P_DP, P_FIXED };
 
 struct PlaneLayout {
   int n_planes;
-  bool field, chan;
+  int q_geo;   // g_right, g_left, scale planes (-1: uniform per cable)
+  int q_fld;   // extracellular lead field (-1: no ve)
+  int q_chan;  // gnabar, gkbar, gl, el planes (-1: uniform per cable)
 };
 
-__host__ __device__ inline PlaneLayout plane_layout(bool field, bool chan) {
-  // planes past P_SC are packed: field first (if any), then channels
+__host__ __device__ inline PlaneLayout plane_layout(bool geo_planes, bool field, bool chan_planes) {
   PlaneLayout L;
-  L.field = field;
-  L.chan = chan;
-  L.n_planes = P_SC + 1 + (field ? 1 : 0) + (chan ? 4 : 0);
+  int q = P_FIXED;
+  L.q_geo = geo_planes ? q : -1;
+  q += geo_planes ? 3 : 0;
+  L.q_fld = field ? q : -1;
+  q += field ? 1 : 0;
+  L.q_chan = chan_planes ? q : -1;
+  q += chan_planes ? 4 : 0;
+  L.n_planes = q;
   return L;
 }
 
@@ -135,23 +136,33 @@ template <typename T>
 struct Planes {
   T* base;
   int ch;
-  int q_fld, q_gna;
   __device__ __forceinline__ T& at(int q, int j, int r) const {
     return base[(q * ch + j) * 32 + r];
   }
 };
 
+// Division policy: exact IEEE division, or the approximate reciprocal in the
+// float32 fast-math variant.
+template <typename T, bool FAST>
+__device__ __forceinline__ T dv(T a, T b) {
+  if constexpr (FAST) {
+    return __fdividef(a, b);
+  } else {
+    return a / b;
+  }
+}
+
 // One cable, all steps, one warp.  ch = rows per lane (runtime), rows of lane
 // r are i = r*ch + j.  Rows with i >= K are identity rows with zero
 // coefficients and zero state.
-template <typename T>
+template <typename T, bool FAST>
 __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
-                          const PlaneLayout& lay, bool chan_uniform) {
+                          const PlaneLayout& lay) {
   const int r = threadIdx.x & 31;
   const int64_t off = A.cable_ptr[cable];
   const int K = (int)(A.cable_ptr[cable + 1] - off);
-  Planes<T> P{smw, ch, P_SC + 1, P_SC + 1 + (lay.field ? 1 : 0)};
-  const bool use_ve = lay.field;
+  Planes<T> P{smw, ch};
+  const bool use_ve = lay.q_fld >= 0;
 
   for (int j = 0; j < ch; ++j) {
     const int i = r * ch + j;
@@ -161,24 +172,33 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
     P.at(P_M, j, r) = in ? A.m[g] : T(0);
     P.at(P_H, j, r) = in ? A.h[g] : T(0);
     P.at(P_N, j, r) = in ? A.n[g] : T(0);
-    P.at(P_GR, j, r) = in ? A.g_right[g] : T(0);
-    P.at(P_GL, j, r) = in ? A.g_left[g] : T(0);
-    P.at(P_SC, j, r) = in ? A.scale[g] : T(0);
-    if (use_ve) P.at(P.q_fld, j, r) = in ? A.field[g] : T(0);
-    if (lay.chan) {
-      P.at(P.q_gna + 0, j, r) = in ? A.gnabar[g] : T(0);
-      P.at(P.q_gna + 1, j, r) = in ? A.gkbar[g] : T(0);
-      P.at(P.q_gna + 2, j, r) = in ? A.gl[g] : T(0);
-      P.at(P.q_gna + 3, j, r) = in ? A.el[g] : T(0);
+    if (lay.q_geo >= 0) {
+      P.at(lay.q_geo + 0, j, r) = in ? A.g_right[g] : T(0);
+      P.at(lay.q_geo + 1, j, r) = in ? A.g_left[g] : T(0);
+      P.at(lay.q_geo + 2, j, r) = in ? A.scale[g] : T(0);
+    }
+    if (use_ve) P.at(lay.q_fld, j, r) = in ? A.field[g] : T(0);
+    if (lay.q_chan >= 0) {
+      P.at(lay.q_chan + 0, j, r) = in ? A.gnabar[g] : T(0);
+      P.at(lay.q_chan + 1, j, r) = in ? A.gkbar[g] : T(0);
+      P.at(lay.q_chan + 2, j, r) = in ? A.gl[g] : T(0);
+      P.at(lay.q_chan + 3, j, r) = in ? A.el[g] : T(0);
     }
   }
-  // uniform channels: the cable's values, identical on every compartment
+  // uniform coefficients: the cable's values, identical on every compartment
+  // (interior edges for g_right / g_left), so reading them once is exact
   T gna_c = T(0), gk_c = T(0), gl_c = T(0), el_c = T(0);
-  if (chan_uniform) {
+  if (lay.q_chan < 0) {
     gna_c = A.gnabar[off];
     gk_c = A.gkbar[off];
     gl_c = A.gl[off];
     el_c = A.el[off];
+  }
+  T gr_c = T(0), glf_c = T(0), sc_c = T(0);
+  if (lay.q_geo < 0) {
+    gr_c = K > 1 ? A.g_right[off] : T(0);
+    glf_c = K > 1 ? A.g_left[off + 1] : T(0);
+    sc_c = A.scale[off];
   }
   __syncwarp();
 
@@ -222,33 +242,45 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
     T vj = P.at(P_V, 0, r);
     T f_prev = T(0), fj = T(0);
     if (ve_on) {
-      f_prev = (r > 0) ? P.at(P.q_fld, last, r - 1) : T(0);
-      fj = P.at(P.q_fld, 0, r);
+      f_prev = (r > 0) ? P.at(lay.q_fld, last, r - 1) : T(0);
+      fj = P.at(lay.q_fld, 0, r);
     }
     for (int j = 0; j < ch; ++j) {
       const T v_next = (j < last) ? P.at(P_V, j + 1, r) : ((r < 31) ? P.at(P_V, 0, r + 1) : T(0));
       T m = P.at(P_M, j, r), h = P.at(P_H, j, r), n = P.at(P_N, j, r);
-      hh_gates<T>(vj, q10, dt, m, h, n);
+      if constexpr (FAST) {
+        hh_gates_fast(vj, q10, dt, m, h, n);
+      } else {
+        hh_gates<T>(vj, q10, dt, m, h, n);
+      }
       P.at(P_M, j, r) = m;
       P.at(P_H, j, r) = h;
       P.at(P_N, j, r) = n;
       T G, J;
-      if (lay.chan) {
-        hh_affine<T>(m, h, n, P.at(P.q_gna, j, r), P.at(P.q_gna + 1, j, r),
-                     P.at(P.q_gna + 2, j, r), P.at(P.q_gna + 3, j, r), ena, ek, G, J);
+      if (lay.q_chan >= 0) {
+        hh_affine<T>(m, h, n, P.at(lay.q_chan, j, r), P.at(lay.q_chan + 1, j, r),
+                     P.at(lay.q_chan + 2, j, r), P.at(lay.q_chan + 3, j, r), ena, ek, G, J);
       } else {
         hh_affine<T>(m, h, n, gna_c, gk_c, gl_c, el_c, ena, ek, G, J);
       }
-      const T scl = P.at(P_SC, j, r);
-      const T gr = P.at(P_GR, j, r);
-      const T glf = P.at(P_GL, j, r);
+      T scl, gr, glf;
+      if (lay.q_geo >= 0) {
+        gr = P.at(lay.q_geo, j, r);
+        glf = P.at(lay.q_geo + 1, j, r);
+        scl = P.at(lay.q_geo + 2, j, r);
+      } else {
+        const int i = r * ch + j;
+        gr = i < K - 1 ? gr_c : T(0);
+        glf = (i >= 1 && i < K) ? glf_c : T(0);
+        scl = i < K ? sc_c : T(0);
+      }
       // row i couples to i-1 through glf and to i+1 through gr; at a cable
       // end (or past it) that coefficient is exactly zero
       T fn = (J - G * vj) * scl;
       fn = fn + (gr * (v_next - vj) - glf * (vj - v_prev));
       if (ve_on) {
-        const T f_next = (j < last) ? P.at(P.q_fld, j + 1, r)
-                                    : ((r < 31) ? P.at(P.q_fld, 0, r + 1) : T(0));
+        const T f_next = (j < last) ? P.at(lay.q_fld, j + 1, r)
+                                    : ((r < 31) ? P.at(lay.q_fld, 0, r + 1) : T(0));
         const T ve_l = f_prev * Ive, ve_c = fj * Ive, ve_r = f_next * Ive;
         fn = fn + (gr * (ve_r - ve_c) - glf * (ve_c - ve_l));
         f_prev = fj;
@@ -265,12 +297,12 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
         Cs = c;
         Ds = d;
       } else if (j == 1) {
-        const T rinv = T(1) / b;
+        const T rinv = dv<T, FAST>(T(1), b);
         ap = a * rinv;
         cp = c * rinv;
         dp = d * rinv;
       } else {
-        const T rinv = T(1) / (b - a * cp);
+        const T rinv = dv<T, FAST>(T(1), b - a * cp);
         ap = -a * ap * rinv;
         dp = (d - a * dp) * rinv;
         cp = c * rinv;
@@ -332,8 +364,8 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
       T ga_r = shfl_down<T>(ga, sh, 32), de_r = shfl_down<T>(de, sh, 32);
       const bool hl = r >= sh;
       const bool hr = r + sh < 32;
-      T k1 = hl ? al / be_l : T(0);
-      T k2 = hr ? ga / be_r : T(0);
+      T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
+      T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
       T al_n = hl ? -k1 * al_l : T(0);
       T ga_n = hr ? -k2 * ga_r : T(0);
       be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
@@ -341,7 +373,7 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
       al = al_n;
       ga = ga_n;
     }
-    const T xs = de / be;
+    const T xs = dv<T, FAST>(de, be);
     T xe = xs;
     if (ch > 1) {
       T xs_next = shfl_down<T>(xs, 1, 32);
@@ -386,10 +418,9 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
 
 constexpr int kCableWarps = 4;  // default warps (cables in flight) per block
 
-template <typename T>
+template <typename T, bool FAST>
 __global__ void __launch_bounds__(kCableWarps * 32) cable_run_kernel(CableArgsT<T> A, int ch_max,
-                                                                     PlaneLayout lay,
-                                                                     int chan_uniform) {
+                                                                     PlaneLayout lay) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5;
   T* smw = reinterpret_cast<T*>(smem_raw) + (size_t)warp * lay.n_planes * ch_max * 32;
@@ -406,7 +437,7 @@ __global__ void __launch_bounds__(kCableWarps * 32) cable_run_kernel(CableArgsT<
       if (lane == 0) atomicOr(A.counter + 1, kErrChunk);
       continue;
     }
-    run_cable<T>(A, cable, smw, ch, lay, chan_uniform != 0);
+    run_cable<T, FAST>(A, cable, smw, ch, lay);
   }
 }
 
@@ -523,12 +554,9 @@ __global__ void __launch_bounds__(128) cable_solve_update_kernel(CableArgsT<T> A
   }
 }
 
-template <typename T>
-int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st) {
-  CableArgsT<T> A = typed<T>(args);
-  const bool field = args->field != nullptr && args->ve_amp != nullptr;
-  const bool chan_uniform = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) != 0;
-  const PlaneLayout lay = plane_layout(field, !chan_uniform);
+template <typename T, bool FAST>
+static int launch_cable_run(CableArgsT<T> A, int ch_max, const PlaneLayout& lay,
+                            cudaStream_t st) {
   // one warp per cable in flight; long cables get fewer warps per block so
   // the block's planes fit the 227 KB shared-memory limit
   const size_t per_warp = (size_t)lay.n_planes * ch_max * 32 * sizeof(T);
@@ -538,20 +566,33 @@ int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st) {
               "cable too long for shared memory (%zu bytes per cable)", per_warp);
   const int threads = wpb * 32;
   const size_t smem = (size_t)wpb * per_warp;
-  DGB_CUDA_CHECK(cudaFuncSetAttribute(cable_run_kernel<T>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto kern = cable_run_kernel<T, FAST>;
+  DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
   int per_sm = 0;
-  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cable_run_kernel<T>,
-                                                               threads, smem));
+  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
   if (per_sm < 1) per_sm = 1;
   int blocks = device_sm_count() * per_sm;
   const int blocks_needed = (A.n_cables + wpb - 1) / wpb;
   if (blocks > blocks_needed) blocks = blocks_needed;
   if (blocks < 1) blocks = 1;
   DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, 2 * sizeof(int32_t), st));
-  cable_run_kernel<T><<<blocks, threads, smem, st>>>(A, ch_max, lay, chan_uniform ? 1 : 0);
+  kern<<<blocks, threads, smem, st>>>(A, ch_max, lay);
   DGB_LAUNCH_CHECK();
   return DGB_OK;
+}
+
+template <typename T>
+int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st) {
+  CableArgsT<T> A = typed<T>(args);
+  const bool field = args->field != nullptr && args->ve_amp != nullptr;
+  const bool chan_planes = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) == 0;
+  const bool geo_planes = (args->flags & DGB_CABLE_UNIFORM_GEOMETRY) == 0;
+  const PlaneLayout lay = plane_layout(geo_planes, field, chan_planes);
+  if constexpr (sizeof(T) == 4) {
+    if (args->flags & DGB_CABLE_FAST_MATH) return launch_cable_run<T, true>(A, ch_max, lay, st);
+  }
+  return launch_cable_run<T, false>(A, ch_max, lay, st);
 }
 
 template <typename T>

@@ -167,6 +167,59 @@ __device__ __forceinline__ void hh_gates(T v, T q10, T dt, T& m, T& h, T& n) {
   n = cnexp_step<T>(n, q10 * alpha_n, q10 * (alpha_n + beta_n), dt);
 }
 
+// ---------------------------------------------------------------------------
+// float32 fast-math variant of the gate advance (opt-in, DGB_CABLE_FAST_MATH).
+// Same formulas and branch rules as hh_gates, evaluated with fewer
+// instructions:
+//   * constant divisors become multiplications by the rounded reciprocal;
+//   * the remaining divisions use the approximate reciprocal (__fdividef);
+//   * three exponentials instead of six, by exact identities:
+//       exp(-(v+35)/10) = exp(-(v+40)/10) * e^{0.5}
+//       exp(-(v+55)/10) = exp(-(v+40)/10) * e^{-1.5}
+//       exp(-(v+65)/20) = (exp(-(v+65)/80))^4
+// Each substitution changes a result by a few float32 ulps; the tests hold
+// the resulting voltages to the same 1e-3 mV float64 bound as the exact path.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float vtrap_fast(float x, float q, float e) {
+  // x / (exp(q) - 1) with q = x / 10 and e = exp(q) supplied by the caller
+  if (fabsf(q) <= 1.0f) {
+    const float even = Math<float>::even_series(q);
+    return (10.0f - x * 0.5f) + x * (q * even);
+  }
+  return __fdividef(x, e - 1.0f);
+}
+
+__device__ __forceinline__ float cnexp_fast(float x, float a, float b, float dt) {
+  const float rate = a - b * x;
+  const float z = -b * dt;
+  if (fabsf(z) <= 0.5f) return x + dt * rate * Math<float>::phi1(z);
+  const float eq = __fdividef(a, b);
+  return eq + (x - eq) * expf(z);
+}
+
+__device__ __forceinline__ void hh_gates_fast(float v, float q10, float dt, float& m, float& h,
+                                              float& n) {
+  const float xm = -(v + 40.0f), xn = -(v + 55.0f);
+  const float qm = xm * 0.1f, qn = xn * 0.1f;
+  const float e10 = expf(qm);               // exp(-(v+40)/10)
+  const float e_n = e10 * 0.22313016014843f;  // exp(-(v+55)/10) = e10 * e^{-1.5}
+  const float e_h = e10 * 1.6487212707001282f; // exp(-(v+35)/10) = e10 * e^{0.5}
+  const float u = -(v + 65.0f);
+  const float e18 = expf(u * (1.0f / 18.0f));
+  const float e80 = expf(u * (1.0f / 80.0f));
+  const float e80_2 = e80 * e80;
+  const float e20 = e80_2 * e80_2;
+  const float alpha_m = 0.1f * vtrap_fast(xm, qm, e10);
+  const float beta_m = 4.0f * e18;
+  const float alpha_h = 0.07f * e20;
+  const float beta_h = __fdividef(1.0f, e_h + 1.0f);
+  const float alpha_n = 0.01f * vtrap_fast(xn, qn, e_n);
+  const float beta_n = 0.125f * e80;
+  m = cnexp_fast(m, q10 * alpha_m, q10 * (alpha_m + beta_m), dt);
+  h = cnexp_fast(h, q10 * alpha_h, q10 * (alpha_h + beta_h), dt);
+  n = cnexp_fast(n, q10 * alpha_n, q10 * (alpha_n + beta_n), dt);
+}
+
 // HH affine membrane terms (HH.py:109-116): G = gl + gna + gk, J = gl el + gna ena + gk ek.
 template <typename T>
 __device__ __forceinline__ void hh_affine(T m, T h, T n, T gnabar, T gkbar, T gl, T el,

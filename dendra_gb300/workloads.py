@@ -38,14 +38,15 @@ def c2_spec(n_cables=16384, seed=2024, kmin=51, kmax=401):
 
 
 def cable_population_c2(n_cables=16384, seed=2024, dtype=torch.float32, device="cuda",
-                        subset=None):
+                        subset=None, fast_math=False):
     """Config-2 population (optionally only the cables listed in ``subset``)."""
     s = c2_spec(n_cables, seed)
     idx = np.arange(n_cables) if subset is None else np.asarray(subset)
     ks = s["ks"][idx]
     dx = s["length"][idx] / ks
     pop = CablePopulation(ks.tolist(), torch.as_tensor(s["diam"][idx]), torch.as_tensor(dx),
-                          rhoa=100.0, celsius=6.3, v_init=-65.0, dtype=dtype, device=device)
+                          rhoa=100.0, celsius=6.3, v_init=-65.0, dtype=dtype, device=device,
+                          fast_math=fast_math)
     x = pop.positions()
     cab = np.repeat(np.arange(len(idx)), ks)
     r_cm = torch.sqrt(x ** 2 + torch.as_tensor(s["dist"][idx][cab]) ** 2) * 1e-4

@@ -156,9 +156,17 @@ typedef struct dgb_cable_args {
   int32_t* scratch;
 } dgb_cable_args;
 
-/* dgb_cable_args.flags: gnabar, gkbar, gl and el are constant within each
-   cable (the kernel then reads them once per cable) */
+/* dgb_cable_args.flags bits.
+   UNIFORM_CHANNELS: gnabar, gkbar, gl, el are constant within each cable.
+   UNIFORM_GEOMETRY: g_right (all but the last compartment), g_left (all but
+     the first) and scale are constant within each cable.
+   The kernel then reads those values once per cable (exactly the same values).
+   FAST_MATH (float32 only): approximate reciprocals and shared exponentials in
+     the gate advance and the solve; the results stay within the float32
+     tolerance of the exact path (1e-3 mV against a float64 run). */
 #define DGB_CABLE_UNIFORM_CHANNELS 1
+#define DGB_CABLE_UNIFORM_GEOMETRY 2
+#define DGB_CABLE_FAST_MATH 4
 
 /*
  * Run n_steps backward-Euler + cnexp steps of every cable in one persistent

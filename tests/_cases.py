@@ -8,22 +8,22 @@ import torch
 from dendra_gb300.cable import CablePopulation
 
 
-def golden_cable_population(g, dtype, device="cpu"):
+def golden_cable_population(g, dtype, device="cpu", **kw):
     """The reference's config-1-geometry run recorded in hh_cable_*.npz."""
     B, K = int(g["B"]), int(g["K"])
     pop = CablePopulation([K] * B, float(g["diam"]), float(g["dx"]), rhoa=float(g["rhoa"]),
                           celsius=float(g["celsius"]), v_init=float(g["v_init"]),
-                          dtype=dtype, device=device)
+                          dtype=dtype, device=device, **kw)
     pop.inject(int(g["comp"]), torch.as_tensor(g["amp_ma"]), float(g["delay"]), float(g["pw"]))
     return pop.initialize(float(g["dt"]))
 
 
-def golden_extra_population(g, dtype, device="cpu"):
+def golden_extra_population(g, dtype, device="cpu", **kw):
     """The reference's extracellular run recorded in hh_extra_*.npz."""
     B, K = int(g["B"]), int(g["K"])
     pop = CablePopulation([K] * B, torch.as_tensor(g["diam"]), float(g["dx"]),
                           rhoa=float(g["rhoa"]), celsius=float(g["celsius"]),
-                          v_init=float(g["v_init"]), dtype=dtype, device=device)
+                          v_init=float(g["v_init"]), dtype=dtype, device=device, **kw)
     field = torch.as_tensor(g["field_times_amp"]).reshape(-1)
     pop.set_extracellular(field, 1.0, float(g["delay"]), float(g["pw"]))
     return pop.initialize(float(g["dt"]))
@@ -63,7 +63,7 @@ def oracle_traces(pop, steps, comps, spk_idx=None, judge64=False):
 
 
 def synthetic_population(seed, n_cables, kmin, kmax, dtype, device, *, extra=True, intra=False,
-                         dt=0.005):
+                         dt=0.005, **kw):
     """A C2-style ragged population: odd K uniform in [kmin, kmax], diam U[0.5,4],
     length U[500,5000] um (dx = L/K), point source at U[0.5,3] mm with a cathodic
     0.1 ms pulse of U[0.1,2] mA starting at t=0."""
@@ -74,7 +74,7 @@ def synthetic_population(seed, n_cables, kmin, kmax, dtype, device, *, extra=Tru
     length = rng.uniform(500.0, 5000.0, n_cables)
     dx = length / ks
     pop = CablePopulation(ks.tolist(), torch.as_tensor(diam), torch.as_tensor(dx), rhoa=100.0,
-                          celsius=6.3, v_init=-65.0, dtype=dtype, device=device)
+                          celsius=6.3, v_init=-65.0, dtype=dtype, device=device, **kw)
     if extra:
         dist = rng.uniform(500.0, 3000.0, n_cables)
         amp = -rng.uniform(0.1, 2.0, n_cables)

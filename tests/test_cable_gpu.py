@@ -25,10 +25,10 @@ def _spike_steps(trace, thr=0.0):
     return [list(np.nonzero(above[1:, b] & ~above[:-1, b])[0] + 1) for b in range(trace.shape[1])]
 
 
-def _gpu_traces(make, g, dtype, cuda, comps):
+def _gpu_traces(make, g, dtype, cuda, comps, **kw):
     out = []
     for c in comps:
-        pop = make(g, dtype, cuda)
+        pop = make(g, dtype, cuda, **kw)
         res = pop.run(int(g["steps"]), rec_idx=int(c))
         out.append(res.trace.double().cpu().numpy())
     return np.stack(out, axis=-1).transpose(1, 0, 2), pop
@@ -47,8 +47,9 @@ def test_float64_run_matches_reference(cuda, golden, which):
                                rtol=0, atol=1e-7)
 
 
+@pytest.mark.parametrize("fast_math", [False, True])
 @pytest.mark.parametrize("which", ["cable", "extra"])
-def test_float32_run_within_tolerance_of_float64_judge(cuda, golden, which):
+def test_float32_run_within_tolerance_of_float64_judge(cuda, golden, which, fast_math):
     """float32 GPU run vs the float64 oracle on the same inputs and pulse grid.
 
     The reference's own float32 run is held to the same judge; its error sets
@@ -57,12 +58,13 @@ def test_float32_run_within_tolerance_of_float64_judge(cuda, golden, which):
     """
     g32 = golden(f"hh_{which}_f32.npz")
     make = golden_cable_population if which == "cable" else golden_extra_population
-    tr, _ = _gpu_traces(make, g32, torch.float32, cuda, g32["trace_comps"])
+    tr, _ = _gpu_traces(make, g32, torch.float32, cuda, g32["trace_comps"], fast_math=fast_math)
     judge, _, _ = oracle_traces(make(g32, torch.float32), int(g32["steps"]), g32["trace_comps"],
                                 judge64=True)
     ref_own = np.abs(g32["v_trace"] - judge).max()
     err = np.abs(tr - judge).max()
-    print(f"{which}: gpu f32 vs f64 judge {err:.3e} mV; reference f32 vs judge {ref_own:.3e} mV")
+    print(f"{which} fast={fast_math}: gpu f32 vs f64 judge {err:.3e} mV; "
+          f"reference f32 vs judge {ref_own:.3e} mV")
     assert err <= max(F32_MV, 2.0 * ref_own)
     for c in range(judge.shape[2]):
         assert _spike_steps(tr[:, :, c]) == _spike_steps(g32["v_trace"][:, :, c])
@@ -137,3 +139,35 @@ def test_spike_detection_counts_rising_edges(cuda, golden):
     ref = _spike_steps(g["v_trace"][:, :, 0])
     np.testing.assert_array_equal(res.spk_count.cpu().numpy(), [len(s) for s in ref])
     np.testing.assert_array_equal(res.spk_first.cpu().numpy(), [s[0] if s else -1 for s in ref])
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_uniform_coefficient_compression_is_exact(cuda, dtype):
+    """Per-cable uniform geometry/channels read once give bit-identical runs."""
+    a = synthetic_population(13, 96, 1, 700, dtype, cuda, intra=True)
+    b = synthetic_population(13, 96, 1, 700, dtype, cuda, intra=True, compress_uniform=False)
+    assert a.uniform_geometry and a.uniform_channels
+    assert not b.uniform_geometry and not b.uniform_channels
+    ra = a.run(300, rec_idx=0, spk_idx=0)
+    rb = b.run(300, rec_idx=0, spk_idx=0)
+    for name in ("v", "m", "h", "n"):
+        torch.testing.assert_close(getattr(a, name), getattr(b, name), rtol=0, atol=0)
+    torch.testing.assert_close(ra.trace, rb.trace, rtol=0, atol=0)
+
+
+def test_fast_math_on_config2_sample_within_tolerance(cuda):
+    """float32 fast math vs the float64 judge on a config-2 subsample (2000 steps)."""
+    from dendra_gb300.workloads import cable_population_c2
+
+    sub = np.arange(0, 16384, 128)
+    pop = cable_population_c2(device=cuda, subset=sub, fast_math=True)
+    p64 = as_f64(pop.problem_dict())
+    p64["rec_idx"] = np.zeros(pop.B, dtype=np.int32)
+    p64["spk_idx"] = np.zeros(pop.B, dtype=np.int32)
+    tr_ref, cnt_ref, first_ref, _ = oracle.cable_run(p64, 2000, gate_f32=True)
+    res = pop.run(2000, rec_idx=0, spk_idx=0)
+    err = np.abs(res.trace.double().cpu().numpy() - tr_ref).max()
+    print("c2 sample fast-math vs f64 judge", err)
+    assert err <= F32_MV
+    np.testing.assert_array_equal(res.spk_count.cpu().numpy(), cnt_ref)
+    np.testing.assert_array_equal(res.spk_first.cpu().numpy(), first_ref)
