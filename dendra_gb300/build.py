@@ -24,6 +24,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# extra nvcc flags for experiments (e.g. DGB_NVCC_EXTRA="-fmad=false")
+NVCC_FLAGS += os.environ.get("DGB_NVCC_EXTRA", "").split()
 
 
 def _nvcc() -> str:

@@ -276,18 +276,20 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
       }
       // row i couples to i-1 through glf and to i+1 through gr; at a cable
       // end (or past it) that coefficient is exactly zero
-      T fn = (J - G * vj) * scl;
-      fn = fn + (gr * (v_next - vj) - glf * (vj - v_prev));
+      T fn = (J - mul_rn(G, vj)) * scl;
+      fn = fn + (mul_rn(gr, v_next - vj) - mul_rn(glf, vj - v_prev));
       if (ve_on) {
         const T f_next = (j < last) ? P.at(lay.q_fld, j + 1, r)
                                     : ((r < 31) ? P.at(lay.q_fld, 0, r + 1) : T(0));
-        const T ve_l = f_prev * Ive, ve_c = fj * Ive, ve_r = f_next * Ive;
-        fn = fn + (gr * (ve_r - ve_c) - glf * (ve_c - ve_l));
+        // ve values are rounded before they are differenced, as the reference
+        // materialises its ve tape; a fused field*I - ve would skip that rounding
+        const T ve_l = mul_rn(f_prev, Ive), ve_c = mul_rn(fj, Ive), ve_r = mul_rn(f_next, Ive);
+        fn = fn + (mul_rn(gr, ve_r - ve_c) - mul_rn(glf, ve_c - ve_l));
         f_prev = fj;
         fj = f_next;
       }
       if (r * ch + j == in_i) fn = fn + Iin * in_cm;
-      const T b = T(1) - dt_s * ((-gr + -glf) - G * scl);
+      const T b = T(1) - dt_s * ((-gr + -glf) - mul_rn(G, scl));
       const T a = -dt_s * glf;
       const T c = -dt_s * gr;
       const T d = dt_s * fn;
@@ -483,15 +485,15 @@ __global__ void cable_assemble_kernel(CableArgsT<T> A, const int32_t* __restrict
   const T glf = A.g_left[g];
   const T vl = i > 0 ? A.v[g - 1] : vj;
   const T vr = i < K - 1 ? A.v[g + 1] : vj;
-  T fn = (J - G * vj) * scl;
-  fn = fn + (gr * (vr - vj) - glf * (vj - vl));
+  T fn = (J - mul_rn(G, vj)) * scl;
+  fn = fn + (mul_rn(gr, vr - vj) - mul_rn(glf, vj - vl));
   if (A.field && A.ve_amp) {
     const T I = rect_pulse<T>(t, A.ve_amp[cable], A.ve_delay[cable], A.ve_pw[cable]);
     if (I != T(0)) {
-      const T ve = A.field[g] * I;
-      const T vel = i > 0 ? A.field[g - 1] * I : ve;
-      const T ver = i < K - 1 ? A.field[g + 1] * I : ve;
-      fn = fn + (gr * (ver - ve) - glf * (ve - vel));
+      const T ve = mul_rn(A.field[g], I);
+      const T vel = i > 0 ? mul_rn(A.field[g - 1], I) : ve;
+      const T ver = i < K - 1 ? mul_rn(A.field[g + 1], I) : ve;
+      fn = fn + (mul_rn(gr, ver - ve) - mul_rn(glf, ve - vel));
     }
   }
   if (A.in_idx && A.in_idx[cable] == (int)i) {
@@ -499,7 +501,7 @@ __global__ void cable_assemble_kernel(CableArgsT<T> A, const int32_t* __restrict
     if (I != T(0)) fn = fn + I * A.cm_inv[g];
   }
   rhs[g] = A.dt_s * fn;
-  mainv[g] = T(1) - A.dt_s * ((-gr + -glf) - G * scl);
+  mainv[g] = T(1) - A.dt_s * ((-gr + -glf) - mul_rn(G, scl));
   lower[g] = -A.dt_s * glf;
   upper[g] = -A.dt_s * gr;
 }

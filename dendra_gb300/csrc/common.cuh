@@ -220,6 +220,15 @@ __device__ __forceinline__ void hh_gates_fast(float v, float q10, float dt, floa
   n = cnexp_fast(n, q10 * alpha_n, q10 * (alpha_n + beta_n), dt);
 }
 
+// Rounded product that the compiler may not fuse into an FMA.  Used where the
+// reference rounds a product before a cancelling add: the extracellular
+// voltages field*I (large, then differenced between neighbours), the axial
+// coupling g_r (v_r - v) - g_l (v - v_l), the membrane source J - G v and J's
+// reversal terms.  A fused product there rounds differently from the
+// reference, and spike upstrokes amplify the difference.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
 // HH affine membrane terms (HH.py:109-116): G = gl + gna + gk, J = gl el + gna ena + gk ek.
 template <typename T>
 __device__ __forceinline__ void hh_affine(T m, T h, T n, T gnabar, T gkbar, T gl, T el,
@@ -229,7 +238,7 @@ __device__ __forceinline__ void hh_affine(T m, T h, T n, T gnabar, T gkbar, T gl
   T gna = gnabar * m3 * h;
   T gk = gkbar * (n2 * n2);
   G = gl + gna + gk;
-  J = gl * el + gna * ena + gk * ek;
+  J = mul_rn(gl, el) + mul_rn(gna, ena) + mul_rn(gk, ek);
 }
 
 // Rectangular pulse amp on [delay, delay + pw).
