@@ -66,6 +66,7 @@ SIGNATURES = {
     "dgb_cable_run": (_INT, [ctypes.POINTER(CableArgs), _P]),
     "dgb_cable_assemble": (_INT, [ctypes.POINTER(CableArgs), _I32, _P, _P, _P, _P, _P]),
     "dgb_cable_solve_update": (_INT, [ctypes.POINTER(CableArgs), _P, _P, _P, _P, _P]),
+    "dgb_cable_step_static": (_INT, [ctypes.POINTER(CableArgs), _I32, _P]),
 }
 
 

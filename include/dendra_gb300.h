@@ -197,6 +197,23 @@ int dgb_cable_solve_update(const dgb_cable_args* args, const void* lower,
                            const void* main_diag, const void* upper,
                            const void* rhs, void* stream);
 
+/*
+ * Allocation-free unfused step: dgb_cable_assemble + dgb_cable_solve_update
+ * with their band scratch in a 4 MiB array compiled into the library
+ * (at most 262,144 float32 or 131,072 float64 compartments; larger
+ * populations return DGB_ERANGE).  No counterpart in the reference: it
+ * serves callers that cannot allocate device memory on their call path
+ * (hosts that preallocate all GPU memory up front, plugins running while
+ * another runtime owns the allocator).  The caller passes inputs and
+ * outputs as for dgb_cable_assemble (comp_cable required; scratch unused).
+ * The first call on a device looks up the array's device address (with that
+ * device current) and should come before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU race and must be
+ * serialised by the caller (one stream, or events between them).  Nothing in
+ * the array needs clearing; each call writes the bands before reading them.
+ */
+int dgb_cable_step_static(const dgb_cable_args* args, int32_t step, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
