@@ -67,6 +67,13 @@ SIGNATURES = {
     "dgb_cable_assemble": (_INT, [ctypes.POINTER(CableArgs), _I32, _P, _P, _P, _P, _P]),
     "dgb_cable_solve_update": (_INT, [ctypes.POINTER(CableArgs), _P, _P, _P, _P, _P]),
     "dgb_cable_step_static": (_INT, [ctypes.POINTER(CableArgs), _I32, _P]),
+    "dgb_dhs_solve": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P, _P]),
+    "dgb_dhs_solve_forest": (_INT, [_INT, _P, _P, _P, _P, _P, _P]),
+    "dgb_detect_spikes": (_INT, [_INT, _P, _P, _I64, _D, _P, _P, _P]),
+    "dgb_pack_source_spikes": (_INT, [_P, _I64, _P, _I64, _P, _P]),
+    "dgb_build_delivery": (_INT, [_INT, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64,
+                                  _P]),
+    "dgb_ring_enqueue": (_INT, [_INT, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
 }
 
 

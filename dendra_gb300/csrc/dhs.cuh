@@ -1,0 +1,72 @@
+// Deterministic DHS / Hines elimination of one tree by one warp.
+//
+// Row i of the tree system (nodes in solver order, parent p(i), axial
+// conductance g_i to the parent, g_root = 0 acts as extra diagonal):
+//   (d_i + g_i + sum_{c child of i} g_c) x_i - g_i x_p(i) - sum_c g_c x_c = b_i
+// Elimination leaves -> root by depth layers (layer_ptr over order, deepest
+// layer first), back substitution root -> leaves.  The reference kernel
+// (triton/dhs_kernel.py:14-112) pushes each child's Schur contribution into
+// its parent with floating-point atomics; here every node pulls its
+// children's contributions in a fixed child order, so results are
+// deterministic and need no atomics:
+//   D_i = d_i + sum_c (g_c / (D_c + g_c)) D_c,  B_i = b_i + sum_c (g_c / (D_c + g_c)) B_c
+//   x_i = (B_i + g_i x_p(i)) / (D_i + g_i)
+// D and B live in shared memory (2 K values per tree); x overwrites B.
+#pragma once
+
+#include "common.cuh"
+
+namespace dgb {
+
+struct TreeTopo {
+  const int32_t* parent;     // [K] local parent (-1 at the root)
+  const int32_t* order;      // [K] nodes, deepest layer first
+  const int32_t* layer_ptr;  // [L+1] layer boundaries in order
+  const int32_t* child_ptr;  // [K+1] children CSR
+  const int32_t* child_idx;  // [K-1]
+  int32_t K, L;
+};
+
+// sD, sB: shared arrays of K values holding d and b on entry; g: global
+// axial conductances of this tree.  On return sB holds x.
+template <typename T>
+__device__ __forceinline__ void dhs_eliminate(const TreeTopo& t, const T* __restrict__ g, T* sD,
+                                              T* sB, int lane) {
+  for (int l = 0; l < t.L; ++l) {
+    const int lo = t.layer_ptr[l], hi = t.layer_ptr[l + 1];
+    for (int o = lo + lane; o < hi; o += 32) {
+      const int i = t.order[o];
+      T D = sD[i], Bv = sB[i];
+      const int c0 = t.child_ptr[i], c1 = t.child_ptr[i + 1];
+      for (int k = c0; k < c1; ++k) {
+        const int c = t.child_idx[k];
+        const T gc = g[c];
+        const T Dc = sD[c];
+        const T f = gc * (T(1) / (Dc + gc));
+        D = D + f * Dc;
+        Bv = Bv + f * sB[c];
+      }
+      sD[i] = D;
+      sB[i] = Bv;
+    }
+    __syncwarp();
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dhs_substitute(const TreeTopo& t, const T* __restrict__ g, T* sD,
+                                               T* sB, int lane) {
+  for (int l = t.L - 1; l >= 0; --l) {
+    const int lo = t.layer_ptr[l], hi = t.layer_ptr[l + 1];
+    for (int o = lo + lane; o < hi; o += 32) {
+      const int i = t.order[o];
+      const int p = t.parent[i];
+      const T gi = g[i];
+      const T xp = p >= 0 ? sB[p] : T(0);
+      sB[i] = (sB[i] + gi * xp) / (sD[i] + gi);
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace dgb

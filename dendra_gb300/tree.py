@@ -1,0 +1,295 @@
+"""Tree (DHS/Hines) solves on the GB300 kernels.
+
+Host-side topology planning restates the reference's helpers:
+
+* :func:`build_morphology`  — integrators/tree.py:414-474 (parent, children, BFS depth)
+* :func:`build_dhs_layers`  — integrators/tree.py:615-673 (depth buckets deepest
+  first, chunked by ``threads``)
+
+and adds the children CSR the deterministic kernel pulls from.  Solves:
+
+* :func:`dhs_solve_cuda` — reference signature (triton/dhs_kernel.py:634-651),
+  B trees sharing one topology, with the reference's gradients
+  (DHSSolvePacked.backward, dhs_kernel.py:546-598: the system is symmetric, so
+  the adjoint is the same solve).
+* :class:`ForestPlan` / :func:`dhs_solve_forest` — trees of different
+  topologies packed into one launch (the role of dhs_solve_multi_cuda,
+  triton/dhs_kernel_multi.py:831-888).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from collections import deque
+
+import numpy as np
+import torch
+
+from . import _lib
+from .solvers import _validate_float_group
+
+_INDEX_DTYPES = (torch.int32, torch.int64)
+
+
+def build_morphology(parent_idx):
+    """Return (parent int32[K], children lists, depth int32[K]) of a rooted tree."""
+    K = len(parent_idx)
+    if K == 0:
+        raise ValueError("parent_idx must contain at least one node")
+    roots = [i for i, p in enumerate(parent_idx) if p == -1]
+    if len(roots) != 1:
+        raise ValueError(f"parent_idx must contain exactly one root; found {len(roots)}")
+    children = [[] for _ in range(K)]
+    for i, p in enumerate(parent_idx):
+        if p == -1:
+            continue
+        if isinstance(p, bool) or not isinstance(p, (int, np.integer)):
+            raise TypeError(f"parent index at node {i} must be an integer; got {p!r}")
+        if p < 0 or p >= K:
+            raise ValueError(f"parent index at node {i} must be in [0, {K - 1}]; got {p}")
+        if p == i:
+            raise ValueError(f"node {i} cannot be its own parent")
+        children[p].append(i)
+    depth = np.zeros(K, dtype=np.int32)
+    q = deque([roots[0]])
+    visited = set()
+    while q:
+        u = q.popleft()
+        if u in visited:
+            raise ValueError("parent_idx contains a cycle")
+        visited.add(u)
+        for c in children[u]:
+            depth[c] = depth[u] + 1
+            q.append(c)
+    if len(visited) != K:
+        raise ValueError("parent_idx contains a cycle or nodes unreachable from the root")
+    return torch.as_tensor(np.asarray(parent_idx, dtype=np.int32)), children, torch.as_tensor(depth)
+
+
+def validate_threads(threads):
+    if isinstance(threads, bool) or not isinstance(threads, int):
+        raise TypeError("threads must be a positive integer that divides 32")
+    if threads <= 0 or threads > 32:
+        raise ValueError("threads must be in [1, 32]")
+    if 32 % threads != 0:
+        raise ValueError("threads must divide 32 (warp size)")
+    return threads
+
+
+def build_dhs_layers(depth, k_threads):
+    """Elimination order (deepest depth first) and layer boundaries (chunks <= k_threads)."""
+    k_threads = validate_threads(k_threads)
+    depth = np.asarray(torch.as_tensor(depth).cpu().numpy())
+    if depth.ndim != 1 or depth.size == 0:
+        raise ValueError("depth must be a non-empty one-dimensional integer tensor")
+    if (depth < 0).any():
+        raise ValueError("depth values must be nonnegative")
+    bins = [[] for _ in range(int(depth.max()) + 1)]
+    for i, d in enumerate(depth):
+        bins[int(d)].append(i)
+    order, layer_ptr = [], [0]
+    for d in range(len(bins) - 1, -1, -1):
+        bucket = bins[d]
+        for s in range(0, len(bucket), k_threads):
+            order.extend(bucket[s:s + k_threads])
+            layer_ptr.append(len(order))
+    return (torch.as_tensor(order, dtype=torch.int32),
+            torch.as_tensor(layer_ptr, dtype=torch.int32))
+
+
+def children_csr(parent):
+    """Children of every node, increasing index order: (child_ptr[K+1], child_idx[max(K-1,1)])."""
+    parent = np.asarray(parent, dtype=np.int64)
+    K = parent.size
+    nonroot = np.nonzero(parent >= 0)[0]
+    counts = np.bincount(parent[nonroot], minlength=K)
+    ptr = np.zeros(K + 1, dtype=np.int32)
+    ptr[1:] = np.cumsum(counts)
+    idx = nonroot[np.argsort(parent[nonroot], kind="stable")].astype(np.int32)
+    if idx.size == 0:
+        idx = np.zeros(1, dtype=np.int32)
+    return ptr, idx
+
+
+def validate_tree(d_mem, a_geom, b, parent_idx, order, layer_ptr, threads):
+    """Shape/dtype/device contract of the scalar tree solve (triton/_contracts.py:199-229)."""
+    data = (("d_mem", d_mem), ("a_geom", a_geom), ("b", b))
+    topo = (("parent_idx", parent_idx), ("order", order), ("layer_ptr", layer_ptr))
+    for name, t in data + topo:
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{name} must be a torch.Tensor")
+    if d_mem.ndim != 2:
+        raise ValueError(f"d_mem must have shape (B, K), got {tuple(d_mem.shape)}")
+    batch, size = map(int, d_mem.shape)
+    if batch < 1 or size < 1:
+        raise ValueError("B and K must both be >= 1")
+    if tuple(a_geom.shape) != (batch, size) or tuple(b.shape) != (batch, size):
+        raise ValueError("d_mem, a_geom, and b must have identical (B, K) shapes")
+    _validate_float_group(data)
+    for name, t in topo:
+        if t.ndim != 1:
+            raise ValueError(f"{name} must be 1-D")
+        if t.dtype not in _INDEX_DTYPES:
+            raise TypeError(f"{name} must have dtype int32 or int64")
+        if t.device != d_mem.device:
+            raise ValueError(f"{name} must be on device {d_mem.device}; got {t.device}")
+    if parent_idx.numel() != size or order.numel() != size:
+        raise ValueError("parent_idx and order must each contain K entries")
+    if layer_ptr.numel() < 2:
+        raise ValueError("layer_ptr must contain at least two entries")
+    return batch, size, validate_threads(threads)
+
+
+_topo_cache: dict = {}
+
+
+def _device_topology(parent_idx, order, layer_ptr):
+    """int32 device copies of the plan plus the children CSR, cached per tensor version."""
+    key = tuple((t.data_ptr(), t._version, t.numel(), str(t.device))
+                for t in (parent_idx, order, layer_ptr))
+    hit = _topo_cache.get(key)
+    if hit is not None:
+        return hit
+    dev = parent_idx.device
+    parent_np = parent_idx.detach().cpu().numpy().astype(np.int64)
+    cptr, cidx = children_csr(parent_np)
+    topo = tuple(torch.as_tensor(x, dtype=torch.int32, device=dev).contiguous() for x in (
+        parent_np, order.detach().cpu().numpy(), layer_ptr.detach().cpu().numpy(), cptr, cidx))
+    if len(_topo_cache) > 64:
+        _topo_cache.clear()
+    _topo_cache[key] = topo
+    return topo
+
+
+def _solve(d, a, b, topo):
+    parent, order, layer_ptr, cptr, cidx = topo
+    B, K = d.shape
+    d, a, b = (t.contiguous() for t in (d, a, b))
+    x = torch.empty_like(b)
+    with torch.cuda.device(d.device):
+        rc = _lib.load().dgb_dhs_solve(
+            _lib.dtype_code(d.dtype), B, K, d.data_ptr(), a.data_ptr(), b.data_ptr(),
+            parent.data_ptr(), order.data_ptr(), layer_ptr.data_ptr(), layer_ptr.numel() - 1,
+            cptr.data_ptr(), cidx.data_ptr(), x.data_ptr(), _lib.stream_ptr(d.device))
+    _lib.check(rc, "dgb_dhs_solve")
+    return x
+
+
+class _DHSSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, d_mem, a_geom, b, topo):
+        x = _solve(d_mem, a_geom, b, topo)
+        ctx.topo = topo
+        ctx.save_for_backward(d_mem, a_geom, x)
+        return x
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        d_mem, a_geom, V = ctx.saved_tensors
+        g = _solve(d_mem, a_geom, grad_out.contiguous(), ctx.topo)  # symmetric system
+        parent_idx = ctx.topo[0].long()
+        parent = parent_idx.clamp_min(0)
+        Vp = V.index_select(1, parent)
+        gp = g.index_select(1, parent)
+        root = (parent_idx < 0).view(1, -1)
+        grad_a = torch.where(root, -(g * V), -((g - gp) * (V - Vp)))
+        return -(g * V), grad_a, g, None
+
+
+def dhs_solve_cuda(d_mem, a_geom, b, parent_idx, order, layer_ptr, threads=32):
+    """Batched tree solve, drop-in for the reference's dhs_solve_cuda.
+
+    All (B, K) tensors are in the solver order that ``order``/``layer_ptr``
+    index; ``threads`` is validated like the reference (it sets the layer
+    chunking there; this kernel always runs one warp per tree).
+    """
+    validate_tree(d_mem, a_geom, b, parent_idx, order, layer_ptr, threads)
+    topo = _device_topology(parent_idx, order, layer_ptr)
+    return _DHSSolve.apply(d_mem, a_geom, b, topo)
+
+
+class DgbForest(ctypes.Structure):
+    _fields_ = [
+        ("n_trees", ctypes.c_int32), ("max_k", ctypes.c_int32),
+        ("node_ptr", ctypes.c_void_p), ("plan_of", ctypes.c_void_p),
+        ("plan_node_ptr", ctypes.c_void_p), ("plan_layer_off", ctypes.c_void_p),
+        ("parent", ctypes.c_void_p), ("order", ctypes.c_void_p), ("layer_ptr", ctypes.c_void_p),
+        ("child_ptr", ctypes.c_void_p), ("child_idx", ctypes.c_void_p),
+    ]
+
+
+class ForestPlan:
+    """Packed plans of many trees (one topology plan per distinct tree).
+
+    ``parents``: list of parent arrays (local indices, -1 at the root), one per
+    tree; trees may share a plan by passing ``plan_of``.
+    """
+
+    def __init__(self, parents, device="cuda", threads=32, plan_of=None):
+        self.n_plans = len(parents)
+        node_counts = [len(p) for p in parents]
+        plan_node_ptr = np.zeros(self.n_plans + 1, dtype=np.int64)
+        plan_node_ptr[1:] = np.cumsum(node_counts)
+        par, orders, layers, cptrs, cidxs, layer_off = [], [], [], [], [], [0]
+        for p in parents:
+            p = [int(v) for v in p]
+            _, _, depth = build_morphology(p)
+            order, layer_ptr = build_dhs_layers(depth, threads)
+            cptr, cidx = children_csr(p)
+            par.append(np.asarray(p, dtype=np.int32))
+            orders.append(order.numpy())
+            layers.append(layer_ptr.numpy())
+            layer_off.append(layer_off[-1] + layer_ptr.numel())
+            cptrs.append(cptr)
+            cidxs.append(cidx[: max(len(p) - 1, 0)])
+        if plan_of is None:
+            plan_of_np = np.arange(self.n_plans, dtype=np.int32)
+        else:
+            plan_of_np = np.asarray(plan_of, dtype=np.int32)
+        tree_k = np.asarray(node_counts, dtype=np.int64)[plan_of_np]
+        node_ptr = np.zeros(plan_of_np.size + 1, dtype=np.int64)
+        node_ptr[1:] = np.cumsum(tree_k)
+        dev = torch.device(device)
+
+        def t(x, dt):
+            return torch.as_tensor(np.concatenate(x) if isinstance(x, list) else x,
+                                   dtype=dt, device=dev).contiguous()
+
+        cidx_all = np.concatenate(cidxs) if sum(c.size for c in cidxs) else np.zeros(1, np.int32)
+        self.tensors = dict(
+            node_ptr=t(node_ptr, torch.int64), plan_of=t(plan_of_np, torch.int32),
+            plan_node_ptr=t(plan_node_ptr, torch.int64),
+            plan_layer_off=t(np.asarray(layer_off, dtype=np.int64), torch.int64),
+            parent=t(par, torch.int32), order=t(orders, torch.int32),
+            layer_ptr=t(layers, torch.int32), child_ptr=t(cptrs, torch.int32),
+            child_idx=torch.as_tensor(cidx_all, dtype=torch.int32, device=dev).contiguous(),
+        )
+        self.n_trees = int(plan_of_np.size)
+        self.n_nodes = int(node_ptr[-1])
+        self.max_k = int(tree_k.max()) if tree_k.size else 1
+        self.node_ptr = node_ptr
+        self.device = dev
+
+    def struct(self):
+        f = DgbForest()
+        f.n_trees = self.n_trees
+        f.max_k = self.max_k
+        for k, v in self.tensors.items():
+            setattr(f, k, v.data_ptr())
+        return f
+
+
+def dhs_solve_forest(d, a, b, plan: ForestPlan):
+    """Solve packed heterogeneous trees: d, a, b are (n_nodes,) packed by tree."""
+    if not (d.shape == a.shape == b.shape == (plan.n_nodes,)):
+        raise ValueError(f"d, a, b must have shape ({plan.n_nodes},)")
+    _validate_float_group((("d", d), ("a", a), ("b", b)))
+    d, a, b = (t.contiguous() for t in (d, a, b))
+    x = torch.empty_like(b)
+    f = plan.struct()
+    with torch.cuda.device(d.device):
+        rc = _lib.load().dgb_dhs_solve_forest(_lib.dtype_code(d.dtype), ctypes.byref(f),
+                                              d.data_ptr(), a.data_ptr(), b.data_ptr(),
+                                              x.data_ptr(), _lib.stream_ptr(d.device))
+    _lib.check(rc, "dgb_dhs_solve_forest")
+    return x

@@ -21,6 +21,13 @@
  *                             population: models/core.py:4555-4628 driving
  *                             integrators/core.py:769-834 and
  *                             integrators/implicit.py:569-664
+ *   dgb_dhs_solve             dhs_solve_cuda, triton/dhs_kernel.py:634-651
+ *   dgb_dhs_solve_forest      dhs_solve_multi_cuda, triton/dhs_kernel_multi.py:831-888
+ *   dgb_detect_spikes         threshold_transition, networks/spiking.py:43-73
+ *   dgb_pack_source_spikes    pack_source_spikes, networks/netcon_bitpack_kernel.cpp:145-149
+ *   dgb_build_delivery        build_delivery, networks/netcon_bitpack_kernel.cpp:145-149
+ *   dgb_ring_enqueue          dense_fixed_delay_transition enqueue,
+ *                             networks/_event_delivery.py:61-199
  *   dgb_cable_assemble        the eager per-step assembly of the same update
  *                             (mechanism advance + membrane frame + RHS),
  *                             integrators/core.py:769-834, implicit.py:569-646
@@ -196,6 +203,93 @@ int dgb_cable_assemble(const dgb_cable_args* args, int32_t step,
 int dgb_cable_solve_update(const dgb_cable_args* args, const void* lower,
                            const void* main_diag, const void* upper,
                            const void* rhs, void* stream);
+
+/*
+ * Tree (DHS/Hines) solve of B trees sharing one topology of K nodes, in the
+ * solver order of the reference's plan (build_dhs_layers):
+ *   d: (B, K) membrane diagonal, a: (B, K) axial conductance of each node to
+ *   its parent (a[:, root] acts as extra diagonal), b: (B, K) right-hand
+ *   side, x: (B, K) solution.  parent: (K) int32, -1 at the root; order: (K)
+ *   nodes deepest layer first; layer_ptr: (n_layers + 1) layer boundaries in
+ *   order; child_ptr (K + 1) / child_idx (K - 1): children of each node (CSR).
+ * One warp per tree; deterministic (children summed in child_idx order, no
+ * floating-point atomics).  Replaces dhs_solve_cuda
+ * (dendra/models/integrators/triton/dhs_kernel.py:634-651).
+ */
+int dgb_dhs_solve(int dtype, int64_t B, int64_t K, const void* d, const void* a,
+                  const void* b, const int32_t* parent, const int32_t* order,
+                  const int32_t* layer_ptr, int32_t n_layers,
+                  const int32_t* child_ptr, const int32_t* child_idx, void* x,
+                  void* stream);
+
+/* Trees of different topologies solved in one launch (packed forest). */
+typedef struct dgb_forest {
+  int32_t n_trees;
+  int32_t max_k;                /* largest tree, in nodes */
+  const int64_t* node_ptr;      /* [n_trees+1] tree t's d/a/b/x entries */
+  const int32_t* plan_of;       /* [n_trees] topology plan of tree t; NULL: plan t */
+  const int64_t* plan_node_ptr; /* [n_plans+1] plan p's nodes in parent/order/child_idx;
+                                   its child_ptr (K_p+1 entries) starts at
+                                   plan_node_ptr[p] + p */
+  const int64_t* plan_layer_off;/* [n_plans+1] plan p's layer_ptr entries (L_p+1) */
+  const int32_t* parent;        /* local node indices, per plan */
+  const int32_t* order;
+  const int32_t* layer_ptr;
+  const int32_t* child_ptr;
+  const int32_t* child_idx;
+} dgb_forest;
+
+/*
+ * Heterogeneous trees (different sizes and topologies) in one launch, values
+ * packed by node_ptr.  Replaces dhs_solve_multi_cuda
+ * (dendra/models/integrators/triton/dhs_kernel_multi.py:831-888).
+ */
+int dgb_dhs_solve_forest(int dtype, const dgb_forest* forest, const void* d,
+                         const void* a, const void* b, void* x, void* stream);
+
+/*
+ * Rising-edge spike detection (threshold_transition): for each source s,
+ * spikes[s] = v[comp[s]] >= thr and below[s]; then below[s] = !(v >= thr).
+ * comp may be NULL (v indexed by s).  below/spikes are uint8 (0/1).
+ */
+int dgb_detect_spikes(int dtype, const void* v, const int64_t* comp, int64_t n,
+                      double thr, uint8_t* below, uint8_t* spikes, void* stream);
+
+/*
+ * Pack a uint8 source-spike vector into row current_time_step[0] of a bit
+ * history of [depth][n_words] int64 words, 63 sources per word (bit 63 unused).
+ * One warp per word (ballots), no atomics.
+ */
+int dgb_pack_source_spikes(const uint8_t* source_spikes, int64_t n_source,
+                           int64_t* packed_history, int64_t n_words,
+                           const int64_t* current_time_step, void* stream);
+
+/*
+ * Delayed delivery from the bit history: for every connection e whose source
+ * bit is set in row (step - delay_steps[e]) mod max_delay_steps, add
+ * weight[e] to delivery_out[p] of its target p.  Connections are given in CSR
+ * order by target (post_ptr, n_post + 1 entries); each target's events are
+ * added one after another in connection order by one thread: deterministic,
+ * no floating-point atomics.
+ */
+int dgb_build_delivery(int dtype, const int64_t* packed_history,
+                       const int64_t* current_time_step, const int64_t* delay_steps,
+                       const int64_t* conn_word_idx, const int64_t* conn_bit_mask,
+                       const int64_t* post_ptr, int64_t n_post, const void* weight,
+                       void* delivery_out, int64_t n_conn, int64_t max_delay_steps,
+                       int64_t n_words, void* stream);
+
+/*
+ * Dense delay-ring enqueue: ring is [depth][width]; for each target p (CSR
+ * post_ptr over connections sorted by target, column post_col[p] or p) and
+ * each of its connections e with gate[pre[e]] set:
+ *   ring[(slot[0] + delay_steps[e]) % depth][col] += weight[e]
+ * in connection order, one thread per target.
+ */
+int dgb_ring_enqueue(int dtype, void* ring, int64_t depth, int64_t width,
+                     const int64_t* slot, const int64_t* post_ptr, int64_t n_post,
+                     const int64_t* post_col, const int64_t* pre, const uint8_t* gate,
+                     const int64_t* delay_steps, const void* weight, void* stream);
 
 /*
  * Allocation-free unfused step: dgb_cable_assemble + dgb_cable_solve_update
