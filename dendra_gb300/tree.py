@@ -241,7 +241,10 @@ class ForestPlan:
             layers.append(layer_ptr.numpy())
             layer_off.append(layer_off[-1] + layer_ptr.numel())
             cptrs.append(cptr)
-            cidxs.append(cidx[: max(len(p) - 1, 0)])
+            # K_p entries per plan (K_p - 1 children + one unused) so that plan
+            # p's block starts at plan_node_ptr[p], like parent and order
+            cidxs.append(np.concatenate([cidx[: max(len(p) - 1, 0)],
+                                         np.zeros(1, dtype=np.int32)]))
         if plan_of is None:
             plan_of_np = np.arange(self.n_plans, dtype=np.int32)
         else:
@@ -255,7 +258,8 @@ class ForestPlan:
             return torch.as_tensor(np.concatenate(x) if isinstance(x, list) else x,
                                    dtype=dt, device=dev).contiguous()
 
-        cidx_all = np.concatenate(cidxs) if sum(c.size for c in cidxs) else np.zeros(1, np.int32)
+        cidx_all = np.concatenate(cidxs)
+        assert cidx_all.size == plan_node_ptr[-1]
         self.tensors = dict(
             node_ptr=t(node_ptr, torch.int64), plan_of=t(plan_of_np, torch.int32),
             plan_node_ptr=t(plan_node_ptr, torch.int64),

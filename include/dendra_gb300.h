@@ -228,9 +228,10 @@ typedef struct dgb_forest {
   int32_t max_k;                /* largest tree, in nodes */
   const int64_t* node_ptr;      /* [n_trees+1] tree t's d/a/b/x entries */
   const int32_t* plan_of;       /* [n_trees] topology plan of tree t; NULL: plan t */
-  const int64_t* plan_node_ptr; /* [n_plans+1] plan p's nodes in parent/order/child_idx;
-                                   its child_ptr (K_p+1 entries) starts at
-                                   plan_node_ptr[p] + p */
+  const int64_t* plan_node_ptr; /* [n_plans+1] plan p's K_p entries of parent, order
+                                   and child_idx (K_p - 1 children, one unused)
+                                   start at plan_node_ptr[p]; its child_ptr
+                                   (K_p + 1 entries) starts at plan_node_ptr[p] + p */
   const int64_t* plan_layer_off;/* [n_plans+1] plan p's layer_ptr entries (L_p+1) */
   const int32_t* parent;        /* local node indices, per plan */
   const int32_t* order;
