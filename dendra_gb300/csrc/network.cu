@@ -1,0 +1,335 @@
+// Spiking network of branched cells: window-persistent tree update and
+// deterministic event enqueue (sm_103a).
+//
+// dgb_net_window advances every cell by W consecutive steps in one launch.
+// Because every connection delay is at least W steps (the network's minimum
+// delay), no event emitted inside the window is due inside it, so cells are
+// independent for the whole window.  One warp owns one cell; per step, in the
+// reference's phase order (networks/net.py:214-240, netcon.py:5183-5205):
+//   1. deliver today's ring row into the cell's Exp2Syn states
+//      (A += w*factor, B += w*factor; mod/EXP2SYN.py:154-156) and clear it,
+//      plus the pre-generated background (NetStim) events;
+//   2. rising-edge detection at the soma on v from the previous step
+//      (networks/spiking.py:7-10); spikes are recorded in a 64-bit window mask;
+//   3. state advance: A, B exact decay, soma HH gates by cnexp at v_old;
+//   4. tree system (integrators/tree.py:1202-1357): f = (J - G v) area, axial
+//      flows between child and parent, main = cm/dt + G area; DHS solve
+//      (dhs.cuh); v += dv.
+// dgb_net_enqueue then scatters the window's spikes into the delay ring,
+// one thread per target synapse, in connection then step order.
+#include "dhs.cuh"
+
+namespace dgb {
+
+template <typename T>
+struct NetArgsT {
+  int32_t n_cells, n_steps;
+  int64_t step0, depth, slot0, n_syn;
+  // forest
+  const int64_t* node_ptr;
+  const int32_t* plan_of;
+  const int64_t* plan_node_ptr;
+  const int64_t* plan_layer_off;
+  const int32_t *parent, *order, *layer_ptr, *child_ptr, *child_idx;
+  // per node
+  T* v;
+  const T *area, *cm_dt, *a_geom, *gl, *el;
+  // soma HH, per cell
+  T *m, *h, *n;
+  T gnabar, gkbar, ena, ek, q10, dt, thr;
+  // synapses
+  const int64_t* syn_ptr;       // [n_cells+1]
+  const int32_t* node_syn_ptr;  // [N + n_cells]: per cell K+1 entries (local synapse ranges per node)
+  T *syn_A, *syn_B;
+  const T *syn_factor, *syn_decay_A, *syn_decay_B;
+  T e_syn;
+  T* ring;                      // [depth][n_syn]
+  // background events
+  const unsigned long long* bg_bits;  // [steps][bg_words]
+  int64_t bg_words;
+  int32_t bg_syn;               // local synapse receiving background events
+  T bg_weight;
+  // spikes
+  uint8_t* below;
+  unsigned long long* spike_bits;  // [n_cells] for this window
+  int32_t* spike_count;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  T* sV = reinterpret_cast<T*>(smem_raw) + (size_t)warp * 3 * kmax;
+  T* sD = sV + kmax;
+  T* sB = sD + kmax;
+  for (int cell = blockIdx.x * wpb + warp; cell < A.n_cells; cell += gridDim.x * wpb) {
+    const int64_t base = A.node_ptr[cell];
+    const int K = (int)(A.node_ptr[cell + 1] - base);
+    const int plan = A.plan_of ? A.plan_of[cell] : cell;
+    TreeTopo t;
+    {
+      const int64_t pn = A.plan_node_ptr[plan], pl = A.plan_layer_off[plan];
+      t.parent = A.parent + pn;
+      t.order = A.order + pn;
+      t.layer_ptr = A.layer_ptr + pl;
+      t.child_ptr = A.child_ptr + pn + plan;
+      t.child_idx = A.child_idx + pn;
+      t.K = K;
+      t.L = (int)(A.plan_layer_off[plan + 1] - pl - 1);
+    }
+    const int32_t* nsp = A.node_syn_ptr + base + cell;  // K+1 entries
+    const int64_t s0 = A.syn_ptr[cell];
+    const int S = (int)(A.syn_ptr[cell + 1] - s0);
+    const T* area = A.area + base;
+    const T* cmdt = A.cm_dt + base;
+    const T* ag = A.a_geom + base;
+    const T* gl = A.gl + base;
+    const T* el = A.el + base;
+    for (int i = lane; i < K; i += 32) sV[i] = A.v[base + i];
+    T m = T(0), h = T(0), nn = T(0);
+    int below = 1, count = 0;
+    if (lane == 0) {
+      m = A.m[cell];
+      h = A.h[cell];
+      nn = A.n[cell];
+      below = A.below[cell];
+      count = A.spike_count[cell];
+    }
+    unsigned long long bits = 0ull;
+    __syncwarp();
+    for (int s = 0; s < A.n_steps; ++s) {
+      const int64_t g = A.step0 + s;
+      const int64_t slot = (A.slot0 + s) % A.depth;
+      T* row = A.ring + slot * A.n_syn + s0;
+      // 1. deliver today's events (and clear the row)
+      const bool bg = A.bg_bits && ((A.bg_bits[g * A.bg_words + (cell >> 6)] >> (cell & 63)) & 1ull);
+      for (int k = lane; k < S; k += 32) {
+        T w = row[k];
+        if (w != T(0)) {
+          row[k] = T(0);
+        }
+        if (bg && k == A.bg_syn) w = w + A.bg_weight;
+        if (w != T(0)) {
+          const T inc = w * A.syn_factor[s0 + k];
+          A.syn_A[s0 + k] = A.syn_A[s0 + k] + inc;
+          A.syn_B[s0 + k] = A.syn_B[s0 + k] + inc;
+        }
+      }
+      // 2. rising edge at the soma on the previous step's v
+      if (lane == 0) {
+        const bool above = sV[0] >= A.thr;
+        if (above && below) {
+          bits |= 1ull << s;
+          count += 1;
+        }
+        below = above ? 0 : 1;
+      }
+      // 3. state advance: synapse decay, soma gates at v_old
+      for (int k = lane; k < S; k += 32) {
+        A.syn_A[s0 + k] = A.syn_A[s0 + k] * A.syn_decay_A[s0 + k];
+        A.syn_B[s0 + k] = A.syn_B[s0 + k] * A.syn_decay_B[s0 + k];
+      }
+      if (lane == 0) hh_gates<T>(sV[0], A.q10, A.dt, m, h, nn);
+      __syncwarp();
+      // 4. assemble the tree system into sD (main) and sB (rhs)
+      for (int i = lane; i < K; i += 32) {
+        const T vi = sV[i];
+        T G, J;
+        if (i == 0) {
+          hh_affine<T>(m, h, nn, A.gnabar, A.gkbar, gl[0], el[0], A.ena, A.ek, G, J);
+        } else {
+          G = gl[i];
+          J = mul_rn(gl[i], el[i]);
+        }
+        const T ar = area[i];
+        for (int k = nsp[i]; k < nsp[i + 1]; ++k) {
+          // Exp2Syn: g = B - A (uS) -> density g / (1e6 area) (S/cm^2)
+          const T gs = (A.syn_B[s0 + k] - A.syn_A[s0 + k]) / (T(1e6) * ar);
+          G = G + gs;
+          J = J + mul_rn(gs, A.e_syn);
+        }
+        T f = (J - mul_rn(G, vi)) * ar;
+        const int p = t.parent[i];
+        if (p >= 0) f = f - mul_rn(ag[i], vi - sV[p]);
+        for (int k = t.child_ptr[i]; k < t.child_ptr[i + 1]; ++k) {
+          const int c = t.child_idx[k];
+          f = f + mul_rn(ag[c], sV[c] - vi);
+        }
+        sB[i] = f;
+        sD[i] = cmdt[i] + mul_rn(G, ar);
+      }
+      __syncwarp();
+      dhs_eliminate<T>(t, ag, sD, sB, lane);
+      dhs_substitute<T>(t, ag, sD, sB, lane);
+      for (int i = lane; i < K; i += 32) sV[i] = sV[i] + sB[i];
+      __syncwarp();
+    }
+    for (int i = lane; i < K; i += 32) A.v[base + i] = sV[i];
+    if (lane == 0) {
+      A.m[cell] = m;
+      A.h[cell] = h;
+      A.n[cell] = nn;
+      A.below[cell] = (uint8_t)below;
+      A.spike_count[cell] = count;
+      A.spike_bits[cell] = bits;
+    }
+    __syncwarp();
+  }
+}
+
+// ring[(slot0 + s + delay[e]) % depth][t] += weight[e] for every connection e
+// of target t whose source spiked at window step s.
+template <typename T>
+__global__ void net_enqueue_kernel(T* __restrict__ ring, int64_t depth, int64_t n_syn,
+                                   int64_t slot0, const int64_t* __restrict__ post_ptr,
+                                   int64_t n_post, const int64_t* __restrict__ post_col,
+                                   const int64_t* __restrict__ pre,
+                                   const int64_t* __restrict__ delay, const T* __restrict__ weight,
+                                   const unsigned long long* __restrict__ spike_bits) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_post) return;
+  const int64_t col = post_col ? post_col[p] : p;
+  for (int64_t e = post_ptr[p]; e < post_ptr[p + 1]; ++e) {
+    unsigned long long bits = spike_bits[pre[e]];
+    while (bits) {
+      const int s = __ffsll((long long)bits) - 1;
+      bits &= bits - 1;
+      const int64_t r = (slot0 + s + delay[e]) % depth;
+      T* cell = ring + r * n_syn + col;
+      *cell = *cell + weight[e];
+    }
+  }
+}
+
+template <typename T>
+static NetArgsT<T> net_typed(const dgb_net_args* a) {
+  NetArgsT<T> t;
+  t.n_cells = a->n_cells;
+  t.n_steps = a->n_steps;
+  t.step0 = a->step0;
+  t.depth = a->depth;
+  t.slot0 = a->slot0;
+  t.n_syn = a->n_syn;
+  t.node_ptr = a->forest.node_ptr;
+  t.plan_of = a->forest.plan_of;
+  t.plan_node_ptr = a->forest.plan_node_ptr;
+  t.plan_layer_off = a->forest.plan_layer_off;
+  t.parent = a->forest.parent;
+  t.order = a->forest.order;
+  t.layer_ptr = a->forest.layer_ptr;
+  t.child_ptr = a->forest.child_ptr;
+  t.child_idx = a->forest.child_idx;
+  t.v = (T*)a->v;
+  t.area = (const T*)a->area;
+  t.cm_dt = (const T*)a->cm_dt;
+  t.a_geom = (const T*)a->a_geom;
+  t.gl = (const T*)a->gl;
+  t.el = (const T*)a->el;
+  t.m = (T*)a->m;
+  t.h = (T*)a->h;
+  t.n = (T*)a->n;
+  t.gnabar = (T)a->gnabar;
+  t.gkbar = (T)a->gkbar;
+  t.ena = (T)a->ena;
+  t.ek = (T)a->ek;
+  t.q10 = (T)a->q10;
+  t.dt = (T)a->dt_ms;
+  t.thr = (T)a->spk_thr;
+  t.syn_ptr = a->syn_ptr;
+  t.node_syn_ptr = a->node_syn_ptr;
+  t.syn_A = (T*)a->syn_A;
+  t.syn_B = (T*)a->syn_B;
+  t.syn_factor = (const T*)a->syn_factor;
+  t.syn_decay_A = (const T*)a->syn_decay_A;
+  t.syn_decay_B = (const T*)a->syn_decay_B;
+  t.e_syn = (T)a->e_syn;
+  t.ring = (T*)a->ring;
+  t.bg_bits = (const unsigned long long*)a->bg_bits;
+  t.bg_words = a->bg_words;
+  t.bg_syn = a->bg_syn;
+  t.bg_weight = (T)a->bg_weight;
+  t.below = a->below;
+  t.spike_bits = (unsigned long long*)a->spike_bits;
+  t.spike_count = a->spike_count;
+  return t;
+}
+
+template <typename T>
+static int net_window_t(const dgb_net_args* a, cudaStream_t st) {
+  const int kmax = a->forest.max_k;
+  const size_t per_warp = (size_t)3 * kmax * sizeof(T);
+  int wpb = 4;
+  while (wpb > 1 && wpb * per_warp > 227 * 1024) wpb >>= 1;
+  if (wpb * per_warp > 227 * 1024) {
+    set_error("cell of %d compartments too large for shared memory", kmax);
+    return DGB_ERANGE;
+  }
+  const size_t smem = wpb * per_warp;
+  DGB_CUDA_CHECK(cudaFuncSetAttribute(net_window_kernel<T>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, net_window_kernel<T>,
+                                                               wpb * 32, smem));
+  if (per_sm < 1) per_sm = 1;
+  int blocks = device_sm_count() * per_sm;
+  const int need = (a->n_cells + wpb - 1) / wpb;
+  if (blocks > need) blocks = need;
+  net_window_kernel<T><<<blocks, wpb * 32, smem, st>>>(net_typed<T>(a), kmax);
+  DGB_LAUNCH_CHECK();
+  return DGB_OK;
+}
+
+}  // namespace dgb
+
+using namespace dgb;
+
+extern "C" int dgb_net_window(const dgb_net_args* a, void* stream) {
+  clear_error();
+  DGB_REQUIRE(a != nullptr, "args must be non-null");
+  DGB_REQUIRE(a->dtype == DGB_F32 || a->dtype == DGB_F64, "dtype must be DGB_F32 or DGB_F64");
+  DGB_REQUIRE(a->n_steps >= 0 && a->n_steps <= 64, "window length must be in [0, 64]");
+  DGB_REQUIRE(a->depth >= 1 && a->slot0 >= 0 && a->slot0 < a->depth, "bad ring depth/slot");
+  DGB_REQUIRE(a->n_cells >= 0, "n_cells must be >= 0");
+  if (a->n_cells == 0) return DGB_OK;
+  DGB_REQUIRE(a->forest.node_ptr && a->forest.plan_node_ptr && a->forest.plan_layer_off &&
+                  a->forest.parent && a->forest.order && a->forest.layer_ptr &&
+                  a->forest.child_ptr && a->forest.child_idx,
+              "forest arrays must be non-null");
+  DGB_REQUIRE(a->v && a->area && a->cm_dt && a->a_geom && a->gl && a->el && a->m && a->h && a->n,
+              "per-node and soma arrays must be non-null");
+  DGB_REQUIRE(a->syn_ptr && a->node_syn_ptr && a->syn_A && a->syn_B && a->syn_factor &&
+                  a->syn_decay_A && a->syn_decay_B && a->ring,
+              "synapse arrays and ring must be non-null");
+  DGB_REQUIRE(a->below && a->spike_bits && a->spike_count, "spike outputs must be non-null");
+  DGB_REQUIRE(a->forest.max_k >= 1, "cells must have at least one compartment");
+  cudaStream_t st = as_stream(stream);
+  if (a->dtype == DGB_F32) return net_window_t<float>(a, st);
+  return net_window_t<double>(a, st);
+}
+
+extern "C" int dgb_net_enqueue(int dtype, void* ring, int64_t depth, int64_t n_syn, int64_t slot0,
+                               const int64_t* post_ptr, int64_t n_post, const int64_t* post_col,
+                               const int64_t* pre, const int64_t* delay_steps,
+                               const void* weight, const uint64_t* spike_bits, void* stream) {
+  clear_error();
+  DGB_REQUIRE(dtype == DGB_F32 || dtype == DGB_F64, "dtype must be DGB_F32 or DGB_F64");
+  DGB_REQUIRE(depth >= 1 && slot0 >= 0 && n_post >= 0 && n_syn >= 0, "bad sizes");
+  if (n_post == 0) return DGB_OK;
+  DGB_REQUIRE(ring && post_ptr && pre && delay_steps && weight && spike_bits,
+              "pointers must be non-null");
+  const int th = 256;
+  const unsigned blocks = (unsigned)((n_post + th - 1) / th);
+  cudaStream_t st = as_stream(stream);
+  const auto* bits = (const unsigned long long*)spike_bits;
+  if (dtype == DGB_F32)
+    net_enqueue_kernel<float><<<blocks, th, 0, st>>>((float*)ring, depth, n_syn, slot0, post_ptr,
+                                                     n_post, post_col, pre, delay_steps,
+                                                     (const float*)weight, bits);
+  else
+    net_enqueue_kernel<double><<<blocks, th, 0, st>>>((double*)ring, depth, n_syn, slot0, post_ptr,
+                                                      n_post, post_col, pre, delay_steps,
+                                                      (const double*)weight, bits);
+  DGB_LAUNCH_CHECK();
+  return DGB_OK;
+}

@@ -28,6 +28,10 @@
  *   dgb_build_delivery        build_delivery, networks/netcon_bitpack_kernel.cpp:145-149
  *   dgb_ring_enqueue          dense_fixed_delay_transition enqueue,
  *                             networks/_event_delivery.py:61-199
+ *   dgb_net_window            Network.run step loop, networks/net.py:214-240 with
+ *                             NetCon.advance (netcon.py:5183-5205) and
+ *                             _dhs._step (integrators/tree.py:1202-1357)
+ *   dgb_net_enqueue           NetCon enqueue, networks/_event_delivery.py:61-105
  *   dgb_cable_assemble        the eager per-step assembly of the same update
  *                             (mechanism advance + membrane frame + RHS),
  *                             integrators/core.py:769-834, implicit.py:569-646
@@ -247,6 +251,73 @@ typedef struct dgb_forest {
  */
 int dgb_dhs_solve_forest(int dtype, const dgb_forest* forest, const void* d,
                          const void* a, const void* b, void* x, void* stream);
+
+/* One window of a network of branched HH-soma cells (see dgb_net_window). */
+typedef struct dgb_net_args {
+  int32_t dtype;
+  int32_t n_cells;
+  int32_t n_steps;      /* window length W <= 64, at most the minimum delay */
+  int32_t bg_syn;       /* local synapse index receiving background events */
+  int64_t step0;        /* global index of the window's first step */
+  int64_t depth;        /* delay-ring depth (rows) */
+  int64_t slot0;        /* ring row due at step0 */
+  int64_t n_syn;        /* total synapses = ring width */
+  dgb_forest forest;    /* the cells' trees (node-packed), plan arrays on the device */
+  /* per compartment (node-packed): v in/out, area (cm^2), cm/dt (S), axial
+     conductance to the parent (S, 0 at the root), leak/passive g (S/cm^2) and
+     reversal (mV) */
+  void* v;
+  const void* area;
+  const void* cm_dt;
+  const void* a_geom;
+  const void* gl;
+  const void* el;
+  /* soma (node 0 of each cell) HH gates, per cell, in/out */
+  void* m;
+  void* h;
+  void* n;
+  double gnabar, gkbar, ena, ek, q10, dt_ms, spk_thr;
+  /* Exp2Syn synapses: cell c owns [syn_ptr[c], syn_ptr[c+1]); node_syn_ptr has
+     K_c + 1 entries per cell (at node_ptr[c] + c) giving each node's local
+     synapse range (synapses sorted by node) */
+  const int64_t* syn_ptr;
+  const int32_t* node_syn_ptr;
+  void* syn_A;
+  void* syn_B;
+  const void* syn_factor;
+  const void* syn_decay_A;  /* exp(-dt / tau1_effective) */
+  const void* syn_decay_B;  /* exp(-dt / tau2) */
+  double e_syn;
+  void* ring;               /* [depth][n_syn], rows cleared as they are delivered */
+  /* background events: bit (step, cell) of [steps][bg_words] uint64 words */
+  const uint64_t* bg_bits;
+  int64_t bg_words;
+  double bg_weight;
+  /* spikes: latch in/out, window spike mask out (bit s = step step0+s), count in/out */
+  uint8_t* below;
+  uint64_t* spike_bits;
+  int32_t* spike_count;
+} dgb_net_args;
+
+/*
+ * Advance every cell by n_steps steps in one launch: deliver due events into
+ * Exp2Syn states, detect soma spikes, advance synapses and soma gates,
+ * assemble and solve each cell's tree system (deterministic DHS), update v.
+ * Replaces the per-step Network.run loop (networks/net.py:214-240) over
+ * NetCon.advance (netcon.py:5183-5205) and _dhs._step (integrators/tree.py:1202-1357).
+ */
+int dgb_net_window(const dgb_net_args* args, void* stream);
+
+/*
+ * Enqueue a window's spikes: for every target synapse p (CSR post_ptr over
+ * connections sorted by target; ring column post_col[p] or p) and each of its
+ * connections e: for each window step s whose bit is set in
+ * spike_bits[pre[e]], ring[(slot0 + s + delay_steps[e]) % depth][col] += weight[e].
+ */
+int dgb_net_enqueue(int dtype, void* ring, int64_t depth, int64_t n_syn, int64_t slot0,
+                    const int64_t* post_ptr, int64_t n_post, const int64_t* post_col,
+                    const int64_t* pre, const int64_t* delay_steps, const void* weight,
+                    const uint64_t* spike_bits, void* stream);
 
 /*
  * Rising-edge spike detection (threshold_transition): for each source s,

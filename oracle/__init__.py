@@ -30,5 +30,6 @@ from .core import (  # noqa: F401
     pcr,
     cable_run,
     dhs_solve,
+    net_run,
     num_threads,
 )

@@ -71,6 +71,10 @@ def _declare(L):
             [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
             + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P, _I32]
         )
+        getattr(L, "orc_net_run" + sfx).argtypes = (
+            [_I32, _I32, _I64, _I64, _P, _I64] + [_P] * 9 + [_P] * 9 + [_D] * 7
+            + [_P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _I64, _I32, _D, _I64, _P, _P, _P, _P, _P,
+               _P, _P])
     L.orc_num_threads.restype = ctypes.c_int
 
 
@@ -217,3 +221,48 @@ def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
         _ptr(spk_count), _ptr(spk_first), int(bool(gate_f32)),
     )
     return trace, spk_count, spk_first, spk_below
+
+
+def net_run(pd: dict, n_steps: int):
+    """Run the network oracle on a TreeNetwork.problem_dict (arrays updated in place).
+
+    Returns the spike raster (n_steps, n_cells) uint8.
+    """
+    dtype = pd["v"].dtype
+    sfx = _sfx(dtype)
+    P = pd["plan"]
+    nodes, syn, conn, prm = pd["nodes"], pd["syn"], pd["conn"], pd["params"]
+    c = lambda x, dt=None: np.ascontiguousarray(x if dt is None else np.asarray(x, dtype=dt))
+    keep = dict(
+        node_ptr=c(P["node_ptr"], np.int64), plan_of=c(P["plan_of"], np.int32),
+        plan_node_ptr=c(P["plan_node_ptr"], np.int64), plan_layer_off=c(P["plan_layer_off"], np.int64),
+        parent=c(P["parent"], np.int32), order=c(P["order"], np.int32),
+        layer_ptr=c(P["layer_ptr"], np.int32), child_ptr=c(P["child_ptr"], np.int32),
+        child_idx=c(P["child_idx"], np.int32),
+        area=c(nodes["area"], dtype), cm_dt=c(nodes["cm_dt"], dtype), a_geom=c(nodes["a_geom"], dtype),
+        gl=c(nodes["gl"], dtype), el=c(nodes["el"], dtype),
+        syn_ptr=c(pd["syn_ptr"], np.int64), node_syn_ptr=c(pd["node_syn_ptr"], np.int32),
+        factor=c(syn["factor"], dtype), decay_A=c(syn["decay_A"], dtype),
+        decay_B=c(syn["decay_B"], dtype),
+        bg=None if pd["bg_bits"] is None else c(pd["bg_bits"], np.uint64),
+        pre=c(conn["pre"], np.int64), post=c(conn["post"], np.int64),
+        delay=c(conn["delay"], np.int64), weight=c(conn["weight"], dtype))
+    slot = np.array([pd["slot"]], dtype=np.int64)
+    raster = np.zeros((n_steps, pd["n_cells"]), dtype=np.uint8)
+    getattr(lib(), "orc_net_run" + sfx)(
+        int(pd["n_cells"]), int(n_steps), int(pd["step"]), int(pd["depth"]), _ptr(slot),
+        int(pd["n_syn"]), _ptr(keep["node_ptr"]), _ptr(keep["plan_of"]), _ptr(keep["plan_node_ptr"]),
+        _ptr(keep["plan_layer_off"]), _ptr(keep["parent"]), _ptr(keep["order"]),
+        _ptr(keep["layer_ptr"]), _ptr(keep["child_ptr"]), _ptr(keep["child_idx"]),
+        _ptr(pd["v"]), _ptr(keep["area"]), _ptr(keep["cm_dt"]), _ptr(keep["a_geom"]),
+        _ptr(keep["gl"]), _ptr(keep["el"]), _ptr(pd["m"]), _ptr(pd["h"]), _ptr(pd["n"]),
+        float(prm["gnabar"]), float(prm["gkbar"]), float(prm["ena"]), float(prm["ek"]),
+        float(prm["q10"]), float(prm["dt_ms"]), float(prm["spk_thr"]),
+        _ptr(keep["syn_ptr"]), _ptr(keep["node_syn_ptr"]), _ptr(pd["A"]), _ptr(pd["B"]),
+        _ptr(keep["factor"]), _ptr(keep["decay_A"]), _ptr(keep["decay_B"]), float(prm["e_syn"]),
+        _ptr(pd["ring"]), _ptr(keep["bg"]), int(pd["bg_words"]), int(pd["bg_syn"]),
+        float(pd["bg_weight"]), int(keep["pre"].size), _ptr(keep["pre"]), _ptr(keep["post"]),
+        _ptr(keep["delay"]), _ptr(keep["weight"]), _ptr(pd["below"]), _ptr(pd["spike_count"]),
+        _ptr(raster))
+    pd["slot"] = int(slot[0])
+    return raster

@@ -409,6 +409,135 @@ void F(orc_dhs_solve_batched)(int64_t B, int64_t K, const REAL* d, const REAL* a
                      n_layers, x + i * K);
 }
 
+
+/*
+ * Network of branched cells, one step at a time (networks/net.py:214-240,
+ * netcon.py:5183-5205, integrators/tree.py:1202-1357):
+ *   deliver ring row slot into Exp2Syn A, B (A += w factor, B += w factor) and
+ *   clear it; background event adds bg_weight to synapse bg_syn; detect the
+ *   soma rising edge on v; enqueue weight at (slot + delay) % depth for every
+ *   connection of a spiking source (connection order); decay A, B; soma HH
+ *   gates; assemble f = (J - G v) area - axial flows, main = cm/dt + G area;
+ *   sequential DHS solve; v += dv.  Arrays follow dgb_net_args (host memory).
+ */
+void F(orc_net_run)(int32_t n_cells, int32_t n_steps, int64_t step0, int64_t depth,
+                    int64_t* slot_io, int64_t n_syn, const int64_t* node_ptr,
+                    const int32_t* plan_of, const int64_t* plan_node_ptr,
+                    const int64_t* plan_layer_off, const int32_t* parent, const int32_t* order,
+                    const int32_t* layer_ptr, const int32_t* child_ptr, const int32_t* child_idx,
+                    REAL* v, const REAL* area, const REAL* cm_dt, const REAL* a_geom,
+                    const REAL* gl, const REAL* el, REAL* m, REAL* h, REAL* n, double gnabar_d,
+                    double gkbar_d, double ena_d, double ek_d, double q10_d, double dt_d,
+                    double thr_d, const int64_t* syn_ptr, const int32_t* node_syn_ptr,
+                    REAL* syn_A, REAL* syn_B, const REAL* syn_factor, const REAL* decay_A,
+                    const REAL* decay_B, double e_syn_d, REAL* ring, const uint64_t* bg_bits,
+                    int64_t bg_words, int32_t bg_syn, double bg_weight_d, int64_t n_conn,
+                    const int64_t* conn_pre, const int64_t* conn_post, const int64_t* conn_delay,
+                    const REAL* conn_weight, uint8_t* below, int32_t* spike_count,
+                    uint8_t* raster /* [n_steps][n_cells] or NULL */) {
+  const REAL gnabar = (REAL)gnabar_d, gkbar = (REAL)gkbar_d, ena = (REAL)ena_d, ek = (REAL)ek_d;
+  const REAL q10 = (REAL)q10_d, dt = (REAL)dt_d, thr = (REAL)thr_d, e_syn = (REAL)e_syn_d;
+  const REAL bg_weight = (REAL)bg_weight_d;
+  int64_t kmax = 1;
+  for (int32_t c = 0; c < n_cells; ++c)
+    if (node_ptr[c + 1] - node_ptr[c] > kmax) kmax = node_ptr[c + 1] - node_ptr[c];
+  REAL* main_ = (REAL*)malloc(sizeof(REAL) * 3 * (size_t)kmax);
+  REAL* rhs = main_ + kmax;
+  REAL* x = rhs + kmax;
+  uint8_t* spiked = (uint8_t*)malloc((size_t)(n_cells > 0 ? n_cells : 1));
+  int64_t slot = *slot_io;
+  for (int32_t s = 0; s < n_steps; ++s) {
+    const int64_t g = step0 + s;
+    REAL* row = ring + slot * n_syn;
+    /* 1. deliver */
+    for (int32_t c = 0; c < n_cells; ++c) {
+      const int bg = bg_bits && ((bg_bits[g * bg_words + (c >> 6)] >> (c & 63)) & 1ull);
+      for (int64_t k = syn_ptr[c]; k < syn_ptr[c + 1]; ++k) {
+        REAL w = row[k];
+        row[k] = (REAL)0;
+        if (bg && k - syn_ptr[c] == bg_syn) w = w + bg_weight;
+        if (w != (REAL)0) {
+          REAL inc = w * syn_factor[k];
+          syn_A[k] = syn_A[k] + inc;
+          syn_B[k] = syn_B[k] + inc;
+        }
+      }
+    }
+    /* 2. detect on the previous step's soma v, enqueue in connection order */
+    for (int32_t c = 0; c < n_cells; ++c) {
+      int above = v[node_ptr[c]] >= thr;
+      spiked[c] = (uint8_t)(above && below[c]);
+      below[c] = (uint8_t)!above;
+      if (spiked[c]) spike_count[c] += 1;
+      if (raster) raster[(int64_t)s * n_cells + c] = spiked[c];
+    }
+    for (int64_t e = 0; e < n_conn; ++e) {
+      if (!spiked[conn_pre[e]]) continue;
+      int64_t r = (slot + conn_delay[e]) % depth;
+      ring[r * n_syn + conn_post[e]] = ring[r * n_syn + conn_post[e]] + conn_weight[e];
+    }
+    /* 3-4. advance and solve every cell */
+    for (int32_t c = 0; c < n_cells; ++c) {
+      const int64_t base = node_ptr[c];
+      const int32_t K = (int32_t)(node_ptr[c + 1] - base);
+      const int32_t p = plan_of ? plan_of[c] : c;
+      const int64_t pn = plan_node_ptr[p], pl = plan_layer_off[p];
+      const int32_t* par = parent + pn;
+      const int32_t* cptr = child_ptr + pn + p;
+      const int32_t* cidx = child_idx + pn;
+      const int32_t* nsp = node_syn_ptr + base + c;
+      const int64_t s0 = syn_ptr[c];
+      for (int64_t k = syn_ptr[c]; k < syn_ptr[c + 1]; ++k) {
+        syn_A[k] = syn_A[k] * decay_A[k];
+        syn_B[k] = syn_B[k] * decay_B[k];
+      }
+      {
+        REAL r6[6];
+        F(orc_hh_rates)(v[base], q10, r6);
+        m[c] = F(orc_cnexp)(m[c], r6[0], r6[1], dt);
+        h[c] = F(orc_cnexp)(h[c], r6[2], r6[3], dt);
+        n[c] = F(orc_cnexp)(n[c], r6[4], r6[5], dt);
+      }
+      for (int32_t i = 0; i < K; ++i) {
+        const REAL vi = v[base + i];
+        REAL G, J;
+        if (i == 0) {
+          REAL m3 = m[c] * m[c] * m[c];
+          REAL n2 = n[c] * n[c];
+          REAL gna = gnabar * m3 * h[c];
+          REAL gk = gkbar * (n2 * n2);
+          G = gl[base] + gna + gk;
+          J = gl[base] * el[base] + gna * ena + gk * ek;
+        } else {
+          G = gl[base + i];
+          J = gl[base + i] * el[base + i];
+        }
+        const REAL ar = area[base + i];
+        for (int32_t k = nsp[i]; k < nsp[i + 1]; ++k) {
+          REAL gs = (syn_B[s0 + k] - syn_A[s0 + k]) / ((REAL)1e6 * ar);
+          G = G + gs;
+          J = J + gs * e_syn;
+        }
+        REAL f = (J - G * vi) * ar;
+        if (par[i] >= 0) f = f - a_geom[base + i] * (vi - v[base + par[i]]);
+        for (int32_t k = cptr[i]; k < cptr[i + 1]; ++k) {
+          int32_t ch = cidx[k];
+          f = f + a_geom[base + ch] * (v[base + ch] - vi);
+        }
+        rhs[i] = f;
+        main_[i] = cm_dt[base + i] + G * ar;
+      }
+      F(orc_dhs_solve)(K, main_, a_geom + base, rhs, par, order + pn, layer_ptr + pl,
+                       (int32_t)(plan_layer_off[p + 1] - pl - 1), x);
+      for (int32_t i = 0; i < K; ++i) v[base + i] = v[base + i] + x[i];
+    }
+    slot = (slot + 1) % depth;
+  }
+  *slot_io = slot;
+  free(main_);
+  free(spiked);
+}
+
 #undef AM1
 #undef AH1
 #undef AN1

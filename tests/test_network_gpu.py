@@ -1,0 +1,65 @@
+"""Branched-cell spiking network on the GPU against the float64 network oracle."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from dendra_gb300.network import random_network
+
+pytestmark = pytest.mark.gpu
+
+
+def _raster(bits, window):
+    b = bits.cpu().numpy().view(np.uint64)
+    n_win, n_cells = b.shape
+    out = np.zeros((n_win * window, n_cells), dtype=np.uint8)
+    for s in range(window):
+        out[s::window] = ((b >> np.uint64(s)) & np.uint64(1)).astype(np.uint8)
+    return out
+
+
+def _judge(dtype, seed, **kw):
+    net, n_steps = random_network(16, k_range=(30, 400), syn_per_cell=12, seed=seed, dtype=dtype,
+                                  device="cpu", t_stop_ms=60.0, **kw)
+    pd = net.problem_dict(n_steps)
+    if dtype == torch.float32:  # float64 judge on the float32 network's inputs
+        for grp in ("nodes", "syn"):
+            pd[grp] = {k: v.astype(np.float64) for k, v in pd[grp].items()}
+        for k in ("v", "m", "h", "n", "A", "B", "ring"):
+            pd[k] = pd[k].astype(np.float64)
+    raster = oracle.net_run(pd, n_steps)
+    return pd, raster, n_steps
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("seed", [3, 8])
+def test_network_matches_oracle(cuda, dtype, seed):
+    kw = dict(bg_weight=0.05)
+    pd, ref_raster, n_steps = _judge(dtype, seed, **kw)
+    net, _ = random_network(16, k_range=(30, 400), syn_per_cell=12, seed=seed, dtype=dtype,
+                            device=cuda, t_stop_ms=60.0, **kw)
+    bits = net.run(n_steps)
+    raster = _raster(bits, net.window)
+    assert ref_raster.sum() > 0  # the case has spikes
+    # spike routing: which cell fires at which step, exactly
+    np.testing.assert_array_equal(raster, ref_raster)
+    np.testing.assert_array_equal(net.spike_count.cpu().numpy(), pd["spike_count"])
+    v = net.v.double().cpu().numpy()
+    tol = 1e-9 if dtype == torch.float64 else 2e-3
+    assert np.abs(v - pd["v"]).max() < tol
+    np.testing.assert_allclose(net.B.double().cpu().numpy(), pd["B"], rtol=1e-6 if dtype ==
+                               torch.float32 else 1e-12, atol=1e-12)
+    assert int(net.slot) == pd["slot"]
+
+
+def test_network_window_split_is_exact(cuda):
+    """One long run equals the same steps in several calls (ring and slot carried)."""
+    a, n = random_network(8, k_range=(30, 200), syn_per_cell=6, seed=5, dtype=torch.float64,
+                          device=cuda, t_stop_ms=40.0, bg_weight=0.05)
+    b, _ = random_network(8, k_range=(30, 200), syn_per_cell=6, seed=5, dtype=torch.float64,
+                          device=cuda, t_stop_ms=40.0, bg_weight=0.05)
+    ra = _raster(a.run(n), a.window)
+    rb = np.concatenate([_raster(b.run(n // 2), b.window), _raster(b.run(n // 2), b.window)])
+    np.testing.assert_array_equal(ra, rb)
+    torch.testing.assert_close(a.v, b.v, rtol=0, atol=0)
