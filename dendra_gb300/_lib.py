@@ -74,6 +74,9 @@ SIGNATURES = {
     "dgb_build_delivery": (_INT, [_INT, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64,
                                   _P]),
     "dgb_ring_enqueue": (_INT, [_INT, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
+    "dgb_net_window": (_INT, [_P, _P]),
+    "dgb_net_enqueue": (_INT, [_INT, _P, _I64, _I64, _I64, _P, _I64, _P, _P, _P, _P, _P, _P]),
+    "dgb_net_args_size": (ctypes.c_size_t, []),
 }
 
 

@@ -31,3 +31,6 @@ extern "C" const char* dgb_last_error(void) { return dgb::g_last_error; }
 
 // Size of dgb_cable_args as compiled, so bindings can check their mirror.
 extern "C" size_t dgb_cable_args_size(void) { return sizeof(dgb_cable_args); }
+
+// Size of dgb_net_args as compiled, for foreign mirrors of the struct.
+extern "C" size_t dgb_net_args_size(void) { return sizeof(dgb_net_args); }

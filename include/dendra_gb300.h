@@ -299,6 +299,9 @@ typedef struct dgb_net_args {
   int32_t* spike_count;
 } dgb_net_args;
 
+/* sizeof(dgb_net_args) as compiled (for foreign-language mirrors). */
+size_t dgb_net_args_size(void);
+
 /*
  * Advance every cell by n_steps steps in one launch: deliver due events into
  * Exp2Syn states, detect soma spikes, advance synapses and soma gates,

@@ -47,6 +47,13 @@ def test_cable_args_mirror_matches_c_layout():
     assert L.dgb_cable_args_size() == ctypes.sizeof(_lib.CableArgs)
 
 
+def test_net_args_mirror_matches_c_layout():
+    from dendra_gb300.network import NetArgs
+
+    L = dendra_gb300.load()
+    assert L.dgb_net_args_size() == ctypes.sizeof(NetArgs)
+
+
 def test_library_has_no_torch_dependency():
     out = subprocess.run(["readelf", "-d", _lib.path()], capture_output=True, text=True,
                          check=True).stdout
