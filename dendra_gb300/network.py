@@ -239,21 +239,46 @@ class TreeNetwork:
         self.slot = 0
 
     def run(self, n_steps):
-        """Advance n_steps (a multiple of the window); returns the spike raster
-        as a (n_windows, n_cells) uint64 tensor of window spike masks."""
+        """Advance n_steps; returns the spike raster as a (n_steps, n_cells) uint8 tensor.
+
+        Steps run in windows of at most ``self.window`` (the smallest delay);
+        each window is one dgb_net_window launch plus one dgb_net_enqueue."""
         W = self.window
-        if n_steps % W:
-            raise ValueError(f"n_steps must be a multiple of the window ({W})")
-        n_win = n_steps // W
+        n_steps = int(n_steps)
+        windows = [W] * (n_steps // W) + ([n_steps % W] if n_steps % W else [])
         bits_np, words = self._bg_bits(self.step + n_steps)
         bg = torch.as_tensor(bits_np.view(np.int64), device=self.device)
-        raster = torch.zeros(n_win, self.n_cells, dtype=torch.int64, device=self.device)
+        masks = torch.zeros(len(windows), self.n_cells, dtype=torch.int64, device=self.device)
         L = _lib.load()
         st = _lib.stream_ptr(self.device)
+        a = self._args()
+        a.bg_bits = bg.data_ptr() if self.bg_steps is not None else None
+        a.bg_words = words
+        d = self.d
+        for w, wl in enumerate(windows):
+            a.n_steps = wl
+            a.step0 = self.step
+            a.slot0 = self.slot
+            a.spike_bits = masks[w].data_ptr()
+            with torch.cuda.device(self.device):
+                rc = L.dgb_net_window(ctypes.byref(a), st)
+                _lib.check(rc, "dgb_net_window")
+                rc = L.dgb_net_enqueue(a.dtype, self.ring.data_ptr(), self.depth, self.n_syn,
+                                       self.slot, d["csr_ptr"].data_ptr(), self.n_syn, None,
+                                       d["csr_pre"].data_ptr(), d["csr_delay"].data_ptr(),
+                                       d["csr_weight"].data_ptr(), masks[w].data_ptr(), st)
+                _lib.check(rc, "dgb_net_enqueue")
+            self.step += wl
+            self.slot = (self.slot + wl) % self.depth
+        shifts = torch.arange(W, device=self.device, dtype=torch.int64)
+        rows = ((masks[:, None, :] >> shifts[None, :, None]) & 1).to(torch.uint8)
+        return rows.reshape(-1, self.n_cells)[:n_steps] if n_steps % W == 0 else \
+            torch.cat([rows[i, :wl] for i, wl in enumerate(windows)])
+
+    def _args(self):
         a = NetArgs()
         a.dtype = _lib.dtype_code(self.dtype)
         a.n_cells = self.n_cells
-        a.n_steps = W
         a.bg_syn = int(self.bg_syn_sorted[0])
         a.depth = self.depth
         a.n_syn = self.n_syn
@@ -272,26 +297,10 @@ class TreeNetwork:
         a.syn_decay_A = d["syn_decay_A"].data_ptr()
         a.syn_decay_B = d["syn_decay_B"].data_ptr()
         a.ring = self.ring.data_ptr()
-        a.bg_bits = bg.data_ptr() if self.bg_steps is not None else None
-        a.bg_words = words
         a.bg_weight = self.bg_weight
         a.below = self.below.data_ptr()
         a.spike_count = self.spike_count.data_ptr()
-        for w in range(n_win):
-            a.step0 = self.step
-            a.slot0 = self.slot
-            a.spike_bits = raster[w].data_ptr()
-            with torch.cuda.device(self.device):
-                rc = L.dgb_net_window(ctypes.byref(a), st)
-                _lib.check(rc, "dgb_net_window")
-                rc = L.dgb_net_enqueue(a.dtype, self.ring.data_ptr(), self.depth, self.n_syn,
-                                       self.slot, d["csr_ptr"].data_ptr(), self.n_syn, None,
-                                       d["csr_pre"].data_ptr(), d["csr_delay"].data_ptr(),
-                                       d["csr_weight"].data_ptr(), raster[w].data_ptr(), st)
-                _lib.check(rc, "dgb_net_enqueue")
-            self.step += W
-            self.slot = (self.slot + W) % self.depth
-        return raster
+        return a
 
     # -- oracle interchange ----------------------------------------------
     def problem_dict(self, n_steps):
