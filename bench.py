@@ -160,6 +160,90 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+C3_BYTES_PER_COMP_STEP = 24  # unfused tree step: v r/w 8 B + main/rhs/axial/parent 16 B
+
+
+def bench_c3(args, world, rank, local):
+    """Config 3: 4,096 branched cells (200-2,000 compartments, HH soma, passive
+    dendrites), 100 Exp2Syn inputs each from random cells (409,600 NetCons,
+    lognormal(-7, 0.5) uS, delays U[1, 5] ms), 5 Hz Poisson background, float32,
+    dt 0.025 ms for 200 ms (8,000 steps).  One bench step = the whole run."""
+    import torch
+
+    import oracle
+    from dendra_gb300.network import random_network
+
+    n_cells = min(args.cables, 4096) if args.cables != 16384 else 4096
+    t_stop = (args.timesteps or 8000) * 0.025
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals = []
+        for _ in range(args.steps):
+            net, n = random_network(64, seed=3, dtype=torch.float32, device="cpu",
+                                    t_stop_ms=t_stop)
+            pd = net.problem_dict(n)
+            t0 = time.perf_counter()
+            oracle.net_run(pd, n)
+            dt = time.perf_counter() - t0
+            vals.append(net.N * n / dt)
+        v = float(np.median(vals))
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": "c3-branched-network", "sample_cells": 64},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": f"64-cell network, {n} steps"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    net, n = random_network(n_cells, seed=2024 + rank, dtype=torch.float32, device=dev,
+                            t_stop_ms=t_stop)
+    comp_steps = net.N * n
+    st = torch.cuda.current_stream(dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(max(3, args.warmup)):
+        net.reset()
+        net.run(n)
+    torch.cuda.synchronize()
+    times, spikes = [], 0
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            net.reset()
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            r = net.run(n)
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            spikes = int(r.sum())
+    ms = float(np.mean(times))
+    value = comp_steps * world / (ms * 1e-3)
+    peak, peak_kind = _peaks()
+    achieved = C3_BYTES_PER_COMP_STEP * comp_steps / (ms * 1e-3) / 1e9
+    windows = -(-n // net.window)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "c3-branched-network", "n_cells": n_cells,
+                   "compartments": net.N, "synapses": net.n_syn, "timesteps": n,
+                   "window_steps": net.window, "l2": "flushed between timed steps"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": f"{C3_BYTES_PER_COMP_STEP} algorithmic B per compartment-step of the "
+                             f"unfused tree step; peak {peak_kind}"},
+        "gpu_launches": args.steps * windows * 2, "spikes_per_run": spikes,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -172,11 +256,15 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
+                    help="c2: uneven cable population (default); c3: branched-cell network")
     ap.add_argument("--cables", type=int, default=16384,
                     help="cables per rank (a smaller case for profiling)")
     ap.add_argument("--timesteps", type=int, default=0, help="timesteps per run (default 2000)")
     args = ap.parse_args()
     world, rank, local = _dist()
+    if args.workload == "c3":
+        return bench_c3(args, world, rank, local)
     if args.impl == "reference":
         return run_reference(args, world, rank)
 
