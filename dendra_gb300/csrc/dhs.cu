@@ -69,8 +69,8 @@ __global__ void __launch_bounds__(128) dhs_forest_kernel(ForestArgsT F, const T*
       sB[i] = b[base + i];
     }
     __syncwarp();
-    dhs_eliminate<T>(t, g + base, sD, sB, lane);
-    dhs_substitute<T>(t, g + base, sD, sB, lane);
+    dhs_eliminate<T, int32_t>(t, g + base, sD, sB, lane);
+    dhs_substitute<T, int32_t>(t, g + base, sD, sB, lane);
     for (int i = lane; i < K; i += 32) x[base + i] = sB[i];
     __syncwarp();
   }

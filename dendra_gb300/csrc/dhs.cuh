@@ -18,20 +18,25 @@
 
 namespace dgb {
 
-struct TreeTopo {
-  const int32_t* parent;     // [K] local parent (-1 at the root)
-  const int32_t* order;      // [K] nodes, deepest layer first
-  const int32_t* layer_ptr;  // [L+1] layer boundaries in order
-  const int32_t* child_ptr;  // [K+1] children CSR
-  const int32_t* child_idx;  // [K-1]
+template <typename I>
+struct TreeTopoT {
+  const I* parent;     // [K] local parent (root: -1 for int32, 0xFFFF for uint16)
+  const I* order;      // [K] nodes, deepest layer first
+  const I* layer_ptr;  // [L+1] layer boundaries in order
+  const I* child_ptr;  // [K+1] children CSR
+  const I* child_idx;  // [K-1]
   int32_t K, L;
 };
+using TreeTopo = TreeTopoT<int32_t>;
 
-// sD, sB: shared arrays of K values holding d and b on entry; g: global
-// axial conductances of this tree.  On return sB holds x.
-template <typename T>
-__device__ __forceinline__ void dhs_eliminate(const TreeTopo& t, const T* __restrict__ g, T* sD,
-                                              T* sB, int lane) {
+__device__ __forceinline__ bool has_parent(int32_t p) { return p >= 0; }
+__device__ __forceinline__ bool has_parent(uint16_t p) { return p != 0xFFFFu; }
+
+// sD, sB: shared arrays of K values holding d and b on entry; g: axial
+// conductances of this tree (global or shared).  On return sB holds x.
+template <typename T, typename I>
+__device__ __forceinline__ void dhs_eliminate(const TreeTopoT<I>& t, const T* g, T* sD, T* sB,
+                                              int lane) {
   for (int l = 0; l < t.L; ++l) {
     const int lo = t.layer_ptr[l], hi = t.layer_ptr[l + 1];
     for (int o = lo + lane; o < hi; o += 32) {
@@ -53,16 +58,16 @@ __device__ __forceinline__ void dhs_eliminate(const TreeTopo& t, const T* __rest
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void dhs_substitute(const TreeTopo& t, const T* __restrict__ g, T* sD,
-                                               T* sB, int lane) {
+template <typename T, typename I>
+__device__ __forceinline__ void dhs_substitute(const TreeTopoT<I>& t, const T* g, T* sD, T* sB,
+                                               int lane) {
   for (int l = t.L - 1; l >= 0; --l) {
     const int lo = t.layer_ptr[l], hi = t.layer_ptr[l + 1];
     for (int o = lo + lane; o < hi; o += 32) {
       const int i = t.order[o];
-      const int p = t.parent[i];
+      const I p = t.parent[i];
       const T gi = g[i];
-      const T xp = p >= 0 ? sB[p] : T(0);
+      const T xp = has_parent(p) ? sB[p] : T(0);
       sB[i] = (sB[i] + gi * xp) / (sD[i] + gi);
     }
     __syncwarp();

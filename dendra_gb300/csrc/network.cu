@@ -55,38 +55,58 @@ struct NetArgsT {
   int32_t* spike_count;
 };
 
+// Shared memory of one warp (one cell): values sV, sD, sB, sG (axial
+// conductance) of kmax entries in T, then the cell's plan as 16-bit indices
+// (order, parent, child_ptr, child_idx, layer_ptr), staged once per window so
+// that the per-layer index chains of the DHS sweeps stay on chip.
+template <typename T>
+__host__ __device__ inline size_t net_warp_smem(int kmax) {
+  const size_t vals = (size_t)4 * kmax * sizeof(T);
+  const size_t idx = (size_t)2 * (5 * (size_t)kmax + 2);
+  return (vals + idx + 15) & ~(size_t)15;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
-  T* sV = reinterpret_cast<T*>(smem_raw) + (size_t)warp * 3 * kmax;
+  unsigned char* wbase = smem_raw + (size_t)warp * net_warp_smem<T>(kmax);
+  T* sV = reinterpret_cast<T*>(wbase);
   T* sD = sV + kmax;
   T* sB = sD + kmax;
+  T* sG = sB + kmax;
+  uint16_t* sOrder = reinterpret_cast<uint16_t*>(sG + kmax);
+  uint16_t* sParent = sOrder + kmax;
+  uint16_t* sCptr = sParent + kmax;
+  uint16_t* sCidx = sCptr + kmax + 1;
+  uint16_t* sLptr = sCidx + kmax;
   for (int cell = blockIdx.x * wpb + warp; cell < A.n_cells; cell += gridDim.x * wpb) {
     const int64_t base = A.node_ptr[cell];
     const int K = (int)(A.node_ptr[cell + 1] - base);
     const int plan = A.plan_of ? A.plan_of[cell] : cell;
-    TreeTopo t;
-    {
-      const int64_t pn = A.plan_node_ptr[plan], pl = A.plan_layer_off[plan];
-      t.parent = A.parent + pn;
-      t.order = A.order + pn;
-      t.layer_ptr = A.layer_ptr + pl;
-      t.child_ptr = A.child_ptr + pn + plan;
-      t.child_idx = A.child_idx + pn;
-      t.K = K;
-      t.L = (int)(A.plan_layer_off[plan + 1] - pl - 1);
+    const int64_t pn = A.plan_node_ptr[plan], pl = A.plan_layer_off[plan];
+    const int L = (int)(A.plan_layer_off[plan + 1] - pl - 1);
+    // stage the plan (16-bit) and the axial conductances
+    for (int i = lane; i < K; i += 32) {
+      sOrder[i] = (uint16_t)A.order[pn + i];
+      const int32_t p = A.parent[pn + i];
+      sParent[i] = p >= 0 ? (uint16_t)p : (uint16_t)0xFFFFu;
+      sCptr[i] = (uint16_t)A.child_ptr[pn + plan + i];
+      sCidx[i] = (uint16_t)A.child_idx[pn + i];
+      sG[i] = A.a_geom[base + i];
+      sV[i] = A.v[base + i];
     }
+    if (lane == 0) sCptr[K] = (uint16_t)A.child_ptr[pn + plan + K];
+    for (int l = lane; l <= L; l += 32) sLptr[l] = (uint16_t)A.layer_ptr[pl + l];
+    TreeTopoT<uint16_t> t{sParent, sOrder, sLptr, sCptr, sCidx, K, L};
     const int32_t* nsp = A.node_syn_ptr + base + cell;  // K+1 entries
     const int64_t s0 = A.syn_ptr[cell];
     const int S = (int)(A.syn_ptr[cell + 1] - s0);
     const T* area = A.area + base;
     const T* cmdt = A.cm_dt + base;
-    const T* ag = A.a_geom + base;
     const T* gl = A.gl + base;
     const T* el = A.el + base;
-    for (int i = lane; i < K; i += 32) sV[i] = A.v[base + i];
     T m = T(0), h = T(0), nn = T(0);
     int below = 1, count = 0;
     if (lane == 0) {
@@ -150,18 +170,18 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
           J = J + mul_rn(gs, A.e_syn);
         }
         T f = (J - mul_rn(G, vi)) * ar;
-        const int p = t.parent[i];
-        if (p >= 0) f = f - mul_rn(ag[i], vi - sV[p]);
-        for (int k = t.child_ptr[i]; k < t.child_ptr[i + 1]; ++k) {
-          const int c = t.child_idx[k];
-          f = f + mul_rn(ag[c], sV[c] - vi);
+        const uint16_t p = sParent[i];
+        if (has_parent(p)) f = f - mul_rn(sG[i], vi - sV[p]);
+        for (int k = sCptr[i]; k < sCptr[i + 1]; ++k) {
+          const int c = sCidx[k];
+          f = f + mul_rn(sG[c], sV[c] - vi);
         }
         sB[i] = f;
         sD[i] = cmdt[i] + mul_rn(G, ar);
       }
       __syncwarp();
-      dhs_eliminate<T>(t, ag, sD, sB, lane);
-      dhs_substitute<T>(t, ag, sD, sB, lane);
+      dhs_eliminate<T, uint16_t>(t, sG, sD, sB, lane);
+      dhs_substitute<T, uint16_t>(t, sG, sD, sB, lane);
       for (int i = lane; i < K; i += 32) sV[i] = sV[i] + sB[i];
       __syncwarp();
     }
@@ -258,7 +278,11 @@ static NetArgsT<T> net_typed(const dgb_net_args* a) {
 template <typename T>
 static int net_window_t(const dgb_net_args* a, cudaStream_t st) {
   const int kmax = a->forest.max_k;
-  const size_t per_warp = (size_t)3 * kmax * sizeof(T);
+  if (kmax > 65534) {
+    set_error("cells of more than 65,534 compartments are not supported (got %d)", kmax);
+    return DGB_ERANGE;
+  }
+  const size_t per_warp = net_warp_smem<T>(kmax);
   int wpb = 4;
   while (wpb > 1 && wpb * per_warp > 227 * 1024) wpb >>= 1;
   if (wpb * per_warp > 227 * 1024) {
