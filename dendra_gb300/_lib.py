@@ -22,6 +22,7 @@ PCR = 1
 CABLE_UNIFORM_CHANNELS = 1
 CABLE_UNIFORM_GEOMETRY = 2
 CABLE_FAST_MATH = 4
+CABLE_STOP_ON_SPIKE = 8
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
@@ -49,7 +50,7 @@ class CableArgs(ctypes.Structure):
         ("in_idx", _P), ("in_amp", _P), ("in_delay", _P), ("in_pw", _P),
         ("rec_idx", _P), ("trace", _P),
         ("spk_idx", _P), ("spk_thr", _D), ("spk_below", _P), ("spk_count", _P),
-        ("spk_first", _P),
+        ("spk_first", _P), ("spk_idx2", _P), ("spk_below2", _P),
         ("max_k", _I32), ("flags", _I32), ("n_comp", _I64),
         ("comp_cable", _P), ("scratch", _P),
     ]

@@ -104,8 +104,10 @@ class CablePopulation:
     diam, dx : float or sequence
         Per-cable diameter (um) and compartment length (um), or per-compartment
         packed arrays of length ``sum(n_comp)``.
-    rhoa, cm : float
-        Axial resistivity (ohm cm) and specific capacitance (uF/cm^2).
+    rhoa : float
+        Axial resistivity (ohm cm).
+    cm : float or sequence
+        Specific capacitance (uF/cm^2), scalar or per compartment.
     celsius, v_init : float
     dtype : torch.float32 or torch.float64
     hh : dict, optional
@@ -134,8 +136,8 @@ class CablePopulation:
         self.celsius = float(celsius)
         self.v_init = float(v_init)
         self.rhoa = rhoa
-        self.cm = cm
         self._diam = self._per_comp(diam)
+        self.cm = self._per_comp(cm)
         self._dx = self._per_comp(dx)
         hh = {**HH_DEFAULTS, **(hh or {})}
         self.ena = float(hh["ena"])
@@ -310,19 +312,23 @@ class CablePopulation:
         return a
 
     def run(self, n_steps, *, rec_idx=None, rec_every=1, spk_idx=None, spk_thr=0.0,
-            spk_state=None):
+            spk_state=None, spk_idx2=None, stop_on_spike=False, cables=None):
         """Advance every cable by n_steps in one persistent launch.
 
         rec_idx / spk_idx: per-cable local compartment (int, sequence or
         tensor; -1 disables).  Returns a RunResult with the trace
         (B, 1 + n_steps//rec_every), spike counts and first crossing steps
-        (1-based step index within this call, -1 if none).
+        (1-based step index within this call, -1 if none).  spk_idx2: an
+        optional second detection compartment (an edge at either counts).
+        stop_on_spike: a cable stops after the step of its first spike.
+        cables: optional int32 device tensor of the cables to advance (others
+        are left untouched).
         """
         if self.dt is None:
             raise RuntimeError("Model must be initialized before running.")
         dev = self.device
         kk = torch.as_tensor(self.n_comp, dtype=torch.int32)
-        for name, idx in (("rec_idx", rec_idx), ("spk_idx", spk_idx)):
+        for name, idx in (("rec_idx", rec_idx), ("spk_idx", spk_idx), ("spk_idx2", spk_idx2)):
             if idx is not None:
                 ii = torch.as_tensor(idx, dtype=torch.int32).expand(self.B).cpu()
                 if bool(((ii < -1) | (ii >= kk)).any()):
@@ -340,6 +346,16 @@ class CablePopulation:
             spk = (si, below, torch.zeros(self.B, dtype=torch.int32, device=dev),
                    torch.full((self.B,), -1, dtype=torch.int32, device=dev))
         args = self._args(n_steps, rec_every, rec, trace, spk, spk_thr)
+        if spk_idx2 is not None:
+            si2 = torch.as_tensor(spk_idx2, dtype=torch.int32).expand(self.B).contiguous().to(dev)
+            b2 = torch.ones(self.B, dtype=torch.int32, device=dev)
+            self._keep = (si2, b2)
+            args.spk_idx2, args.spk_below2 = si2.data_ptr(), b2.data_ptr()
+        if stop_on_spike:
+            args.flags |= _lib.CABLE_STOP_ON_SPIKE
+        if cables is not None:
+            args.order = cables.data_ptr()
+            args.n_cables = int(cables.numel())
         with torch.cuda.device(dev):
             rc = _lib.load().dgb_cable_run(args, _lib.stream_ptr(dev))
         _lib.check(rc, "dgb_cable_run")

@@ -35,9 +35,11 @@ inline int validate_cable_args(const dgb_cable_args* a) {
   DGB_REQUIRE(!a->spk_idx || (a->spk_below && a->spk_count && a->spk_first),
               "spk_idx requires spk_below, spk_count and spk_first");
   DGB_REQUIRE(!a->trace || a->rec_idx, "trace requires rec_idx");
+  DGB_REQUIRE(!a->spk_idx2 || (a->spk_idx && a->spk_below2),
+              "spk_idx2 requires spk_idx and spk_below2");
   DGB_REQUIRE(a->rec_every >= 1, "rec_every must be >= 1");
   DGB_REQUIRE((a->flags & ~(DGB_CABLE_UNIFORM_CHANNELS | DGB_CABLE_UNIFORM_GEOMETRY |
-                             DGB_CABLE_FAST_MATH)) == 0,
+                             DGB_CABLE_FAST_MATH | DGB_CABLE_STOP_ON_SPIKE)) == 0,
               "unknown flags %d", a->flags);
   DGB_REQUIRE(!(a->flags & DGB_CABLE_FAST_MATH) || a->dtype == DGB_F32,
               "DGB_CABLE_FAST_MATH applies to float32 state only");

@@ -52,6 +52,9 @@ struct CableArgsT {
   const int32_t* spk_idx;
   T spk_thr;
   int32_t *spk_below, *spk_count, *spk_first;
+  const int32_t* spk_idx2;
+  int32_t* spk_below2;
+  int stop_on_spike;
   int32_t* counter;
 };
 
@@ -99,6 +102,9 @@ static CableArgsT<T> typed(const dgb_cable_args* a) {
   t.spk_below = a->spk_below;
   t.spk_count = a->spk_count;
   t.spk_first = a->spk_first;
+  t.spk_idx2 = a->spk_idx2;
+  t.spk_below2 = a->spk_below2;
+  t.stop_on_spike = (a->flags & DGB_CABLE_STOP_ON_SPIKE) ? 1 : 0;
   t.counter = a->scratch;
   return t;
 }
@@ -218,12 +224,16 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
   }
   const int rec_i = (A.rec_idx && A.trace) ? A.rec_idx[cable] : -1;
   const int spk_i = A.spk_idx ? A.spk_idx[cable] : -1;
-  int below = 1, count = 0, first = -1;
-  if (spk_i >= 0 && r == spk_i / ch) {
-    below = A.spk_below[cable];
+  const int spk_i2 = A.spk_idx2 ? A.spk_idx2[cable] : -1;
+  // the count and first step live in lane 0; each detection compartment keeps
+  // its latch in the lane that owns it
+  int below = 1, below2 = 1, count = 0, first = -1;
+  if (spk_i >= 0 && r == 0) {
     count = A.spk_count[cable];
     first = A.spk_first[cable];
   }
+  if (spk_i >= 0 && r == spk_i / ch) below = A.spk_below[cable];
+  if (spk_i2 >= 0 && r == spk_i2 / ch) below2 = A.spk_below2[cable];
   if (rec_i >= 0 && r == rec_i / ch) A.trace[(int64_t)cable * A.n_rec] = P.at(P_V, rec_i % ch, r);
 
   const T dt = A.dt, dt_s = A.dt_s, q10 = A.q10, ena = A.ena, ek = A.ek;
@@ -388,13 +398,30 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
       P.at(P_V, j, r) = P.at(P_V, j, r) + (P.at(P_DP, j, r) - P.at(P_AP, j, r) * xs -
                                            P.at(P_CP, j, r) * xe);
     if (ch > 1) P.at(P_V, last, r) = P.at(P_V, last, r) + xe;
-    if (spk_i >= 0 && r == spk_i / ch) {
-      const int above = P.at(P_V, spk_i % ch, r) >= A.spk_thr;
-      if (above && below) {
+    if (spk_i >= 0) {
+      int edge = 0;
+      if (r == spk_i / ch) {
+        const int above = P.at(P_V, spk_i % ch, r) >= A.spk_thr;
+        edge = above && below;
+        below = !above;
+      }
+      int edge2 = 0;
+      if (spk_i2 >= 0 && r == spk_i2 / ch) {
+        const int above = P.at(P_V, spk_i2 % ch, r) >= A.spk_thr;
+        edge2 = above && below2;
+        below2 = !above;
+      }
+      const unsigned fired = __ballot_sync(0xffffffffu, edge || edge2);
+      if (fired && r == 0) {
         if (count == 0) first = s + 1;
         count += 1;
       }
-      below = !above;
+      if (A.stop_on_spike && fired) {
+        if (rec_i >= 0 && r == rec_i / ch && ((s + 1) % A.rec_every) == 0)
+          A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = P.at(P_V, rec_i % ch, r);
+        __syncwarp();
+        break;
+      }
     }
     if (rec_i >= 0 && r == rec_i / ch && ((s + 1) % A.rec_every) == 0)
       A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = P.at(P_V, rec_i % ch, r);
@@ -410,11 +437,12 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
       A.n[g] = P.at(P_N, j, r);
     }
   }
-  if (spk_i >= 0 && r == spk_i / ch) {
-    A.spk_below[cable] = below;
+  if (spk_i >= 0 && r == 0) {
     A.spk_count[cable] = count;
     A.spk_first[cable] = first;
   }
+  if (spk_i >= 0 && r == spk_i / ch) A.spk_below[cable] = below;
+  if (spk_i2 >= 0 && r == spk_i2 / ch) A.spk_below2[cable] = below2;
   __syncwarp();
 }
 

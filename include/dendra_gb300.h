@@ -156,6 +156,10 @@ typedef struct dgb_cable_args {
   int32_t* spk_below;
   int32_t* spk_count;
   int32_t* spk_first;
+  /* optional second detection compartment per cable (-1: none) and its latch;
+     a rising edge at either compartment counts */
+  const int32_t* spk_idx2;
+  int32_t* spk_below2;
   /* sizes known to the host: largest cable and total compartments */
   int32_t max_k;       /* max over cables of K */
   int32_t flags;       /* DGB_CABLE_* bits */
@@ -178,6 +182,10 @@ typedef struct dgb_cable_args {
 #define DGB_CABLE_UNIFORM_CHANNELS 1
 #define DGB_CABLE_UNIFORM_GEOMETRY 2
 #define DGB_CABLE_FAST_MATH 4
+/* STOP_ON_SPIKE: a cable stops at the end of the step in which its first
+   spike is counted (its state then holds that step; the trace is complete up
+   to it).  For threshold trials, which only need to know whether a fibre fires. */
+#define DGB_CABLE_STOP_ON_SPIKE 8
 
 /*
  * Run n_steps backward-Euler + cnexp steps of every cable in one persistent

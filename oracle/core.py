@@ -69,7 +69,7 @@ def _declare(L):
             _I64, _I64, _P, _P, _P, _P, _P, _P, _I32, _P]
         getattr(L, "orc_cable_run" + sfx).argtypes = (
             [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
-            + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P, _I32]
+            + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P, _I32, _P, _P]
         )
         getattr(L, "orc_net_run" + sfx).argtypes = (
             [_I32, _I32, _I64, _I64, _P, _I64] + [_P] * 9 + [_P] * 9 + [_D] * 7
@@ -203,8 +203,9 @@ def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
     keep = {k: arr(k) for k in ("g_right", "g_left", "scale", "cm_inv", "field", "gnabar",
                                   "gkbar", "gl", "el", "ve_amp", "ve_delay", "ve_pw",
                                   "in_amp", "in_delay", "in_pw")}
-    for k in ("in_idx", "rec_idx", "spk_idx"):
+    for k in ("in_idx", "rec_idx", "spk_idx", "spk_idx2"):
         keep[k] = arr(k, np.int32)
+    spk_below2 = np.ones(B, dtype=np.int32)
     cable_ptr = np.ascontiguousarray(p["cable_ptr"], dtype=np.int64)
     getattr(lib(), "orc_cable_run" + sfx)(
         B, int(n_steps), int(rec_every), _ptr(cable_ptr),
@@ -218,7 +219,8 @@ def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
         _ptr(keep["in_idx"]), _ptr(keep["in_amp"]), _ptr(keep["in_delay"]),
         _ptr(keep["in_pw"]), _ptr(keep["rec_idx"]), _ptr(trace),
         _ptr(keep["spk_idx"]), float(p.get("spk_thr", 0.0)), _ptr(spk_below),
-        _ptr(spk_count), _ptr(spk_first), int(bool(gate_f32)),
+        _ptr(spk_count), _ptr(spk_first), int(bool(gate_f32)), _ptr(keep["spk_idx2"]),
+        _ptr(spk_below2),
     )
     return trace, spk_count, spk_first, spk_below
 

@@ -242,7 +242,7 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
                       const REAL* in_delay, const REAL* in_pw, const int32_t* rec_idx,
                       REAL* trace, const int32_t* spk_idx, double spk_thr_d,
                       int32_t* spk_below, int32_t* spk_count, int32_t* spk_first,
-                      int32_t gate_f32) {
+                      int32_t gate_f32, const int32_t* spk_idx2, int32_t* spk_below2) {
   const REAL ena = (REAL)ena_d, ek = (REAL)ek_d, q10 = (REAL)q10_d;
   const REAL dt = (REAL)dt_ms_d, dt_s = (REAL)dt_s_d, thr = (REAL)spk_thr_d;
   const int64_t n_rec = 1 + (int64_t)n_steps / (rec_every > 0 ? rec_every : 1);
@@ -271,6 +271,7 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
       REAL* work = w + 8 * kmax;
       const int32_t ri = rec_idx ? rec_idx[c] : -1;
       const int32_t si = spk_idx ? spk_idx[c] : -1;
+      const int32_t si2 = spk_idx2 ? spk_idx2[c] : -1;
       if (trace && ri >= 0) trace[(int64_t)c * n_rec] = vv[ri];
       for (int32_t s = 0; s < n_steps; ++s) {
         /* stimulus time of this step: binary64 grid cast to the state dtype */
@@ -345,12 +346,19 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
         }
         for (int64_t i = 0; i < K; ++i) vv[i] = vv[i] + x[i];
         if (si >= 0) {
+          /* a rising edge at either detection compartment counts once */
           int above = vv[si] >= thr;
-          if (above && spk_below[c]) {
+          int edge = above && spk_below[c];
+          spk_below[c] = !above;
+          if (si2 >= 0) {
+            int above2 = vv[si2] >= thr;
+            edge = edge || (above2 && spk_below2[c]);
+            spk_below2[c] = !above2;
+          }
+          if (edge) {
             if (spk_count[c] == 0) spk_first[c] = s + 1;
             spk_count[c] += 1;
           }
-          spk_below[c] = !above;
         }
         if (trace && ri >= 0 && ((s + 1) % rec_every) == 0)
           trace[(int64_t)c * n_rec + (s + 1) / rec_every] = vv[ri];

@@ -86,3 +86,50 @@ def synthetic_population(seed, n_cables, kmin, kmax, dtype, device, *, extra=Tru
     if intra:
         pop.inject(0, torch.as_tensor(rng.uniform(0.05, 0.5, n_cables) * 1e-6), 0.5, 1.0)
     return pop.initialize(dt)
+
+
+def oracle_thresholds(pop, lb, ub, n_steps, rtol=0.01, max_fix=10, max_tries=25, up=2.0,
+                      spk=(60, 192)):
+    """Reference bisection rules with every trial run by the float64 oracle."""
+    import oracle
+
+    base = as_f64(pop.problem_dict())
+    B = pop.B
+    lb = np.array(lb, dtype=np.float64) * np.ones(B)
+    ub = np.array(ub, dtype=np.float64) * np.ones(B)
+
+    def fired(amp):
+        p = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in base.items()}
+        p["ve_amp"] = -amp
+        p["spk_idx"] = np.full(B, spk[0], dtype=np.int32)
+        p["spk_idx2"] = np.full(B, spk[1], dtype=np.int32)
+        _, cnt, _, _ = oracle.cable_run(p, n_steps, gate_f32=pop.dtype == torch.float32)
+        return cnt > 0
+
+    ignore = np.zeros(B, dtype=bool)
+    tries = 0
+    while True:
+        act = fired(ub) | ignore
+        if act.all():
+            break
+        if tries >= max_fix:
+            ignore |= ~act
+            ub[~act] = 1.0
+            lb[~act] = 1.0
+            break
+        ub = np.where(~act, ub * up, ub)
+        tries += 1
+    assert not (fired(lb) & ~ignore).any()
+    msk = ((ub - lb) / ub >= rtol) & ~ignore
+    tries = 0
+    while msk.any() and tries < max_tries:
+        stim = (ub + lb) / 2
+        f = fired(stim)
+        ub = np.where(msk & f, stim, ub)
+        lb = np.where(msk & ~f, stim, lb)
+        msk = ((ub - lb) / ub >= rtol) & ~ignore
+        tries += 1
+    ignore |= msk
+    ub[ignore] = np.nan
+    lb[ignore] = np.nan
+    return ub, lb
