@@ -78,6 +78,12 @@ SIGNATURES = {
     "dgb_net_window": (_INT, [_P, _P]),
     "dgb_net_enqueue": (_INT, [_INT, _P, _I64, _I64, _I64, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "dgb_net_args_size": (ctypes.c_size_t, []),
+    "dgb_mlp_gemm": (_INT, [_I32, _I32, _I32, _P, _I64, _I64, _P, _I64, _I64, _P, _I32, _P, _P,
+                            _P, _P]),
+    "dgb_colsum": (_INT, [_I32, _I32, _P, _P, _P]),
+    "dgb_adam": (_INT, [_I64, _I32, _I32, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float,
+                        ctypes.c_float, ctypes.c_float, _I32, _P, _P, _P]),
+    "dgb_mse_grad": (_INT, [_I64, _P, _P, ctypes.c_float, _P, _P, _P]),
 }
 
 

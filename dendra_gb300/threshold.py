@@ -33,6 +33,10 @@ NODE_LEN_UM = 1.0
 K_FIBRE = N_NODES + (N_NODES - 1) * SEG_PER_INTERNODE  # 241
 MYELIN_CM = 0.005  # uF/cm^2
 MYELIN_G = 5.0e-6  # S/cm^2
+# nodal HH channel densities relative to the HH defaults: nodes of Ranvier
+# carry far denser Na/K channels than a squid axon, and a 1 um node with the
+# plain HH densities cannot drive a 1.6 mm myelinated internode
+NODE_DENSITY_SCALE = 10.0
 
 
 def node_compartment(n):
@@ -48,7 +52,8 @@ def fibre_params(n, seed=0):
                 offset=rng.uniform(0.0, 1.0, n), pw=rng.uniform(0.05, 1.0, n))
 
 
-def fibre_population(p, dtype=torch.float32, device="cuda", dt=0.005, **kw):
+def fibre_population(p, dtype=torch.float32, device="cuda", dt=0.005,
+                     node_density_scale=NODE_DENSITY_SCALE, **kw):
     """Myelinated-fibre-like cables: 21 HH nodes (1 um long) and 20 passive
     internodes of 11 compartments (internode length 100 D), diameter D
     everywhere; point source at distance ``dist`` from the fibre axis, axially
@@ -70,7 +75,9 @@ def fibre_population(p, dtype=torch.float32, device="cuda", dt=0.005, **kw):
     field = RHOE_OHM_CM / (4 * np.pi * r_cm)
     # internodes: a myelin sheath of ~100 lamellae, cm 0.005 uF/cm^2 and leak
     # 5e-6 S/cm^2 (the bare membrane's 1 uF/cm^2 and pas 0.001 S/cm^2 / 200)
-    hh = {k: np.where(is_node, HH_DEFAULTS[k], v) for k, v in
+    scale = {"gnabar": node_density_scale, "gkbar": node_density_scale,
+             "gl": node_density_scale, "el": 1.0}
+    hh = {k: np.where(is_node, float(np.float32(HH_DEFAULTS[k] * scale[k])), v) for k, v in
           (("gnabar", 0.0), ("gkbar", 0.0), ("gl", MYELIN_G), ("el", -70.0))}
     hh = {k: np.tile(v, B) for k, v in hh.items()}
     hh.update(ena=HH_DEFAULTS["ena"], ek=HH_DEFAULTS["ek"])

@@ -374,6 +374,38 @@ int dgb_ring_enqueue(int dtype, void* ring, int64_t depth, int64_t width,
                      const int64_t* post_col, const int64_t* pre, const uint8_t* gate,
                      const int64_t* delay_steps, const void* weight, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Threshold-proposal MLP (BF16 tensor cores, FP32 accumulation).  No
+ * counterpart in the reference (it has no learned component).
+ * ------------------------------------------------------------------------- */
+#define DGB_EPI_PLAIN 0     /* out32 = A B */
+#define DGB_EPI_BIAS 1      /* out32 = A B + bias */
+#define DGB_EPI_BIAS_GELU 2 /* out32 = z = A B + bias; out16 = bf16(gelu(z)) */
+#define DGB_EPI_GELU_GRAD 3 /* out16 (and out32 if given) = (A B) * gelu'(aux) */
+
+/*
+ * C[M,N] = A[M,K] B[K,N] with bf16 operands addressed by element strides
+ * (A[m,k] at A + m*sam + k*sak, B[k,n] at B + k*sbk + n*sbn), fp32
+ * accumulation on mma.sync m16n8k16, and the epilogue above; outputs are
+ * row-major [M][N] (out16 bf16, out32 / bias / aux fp32).
+ */
+int dgb_mlp_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak,
+                 const void* B, int64_t sbk, int64_t sbn, const float* bias, int32_t epi,
+                 const float* aux, float* out32, void* out16, void* stream);
+
+/* out[n] = sum over m of x[m][n] (fp32, fixed order). */
+int dgb_colsum(int32_t M, int32_t N, const float* x, float* out, void* stream);
+
+/* Adam step (bias-corrected, step >= 1) on fp32 weights w[n]; refreshes the
+   bf16 copies w16 ([K][N], same layout) and wt16 ([N][K]) when non-null. */
+int dgb_adam(int64_t n, int32_t N, int32_t K, float* w, const float* grad, float* m1, float* m2,
+             float lr, float b1, float b2, float eps, int32_t step, void* w16, void* wt16,
+             void* stream);
+
+/* dy = scale * (y - target) (fp32 and/or bf16 outputs). */
+int dgb_mse_grad(int64_t n, const float* y, const float* target, float scale, float* dy32,
+                 void* dy16, void* stream);
+
 /*
  * Allocation-free unfused step: dgb_cable_assemble + dgb_cable_solve_update
  * with their band scratch in a 4 MiB array compiled into the library

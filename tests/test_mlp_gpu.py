@@ -1,0 +1,79 @@
+"""BF16 tensor-core MLP kernels against a float64 CPU oracle of the same network."""
+
+import numpy as np
+import pytest
+import torch
+from scipy.special import erf
+
+from dendra_gb300.mlp import BF16MLP
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16(x):
+    """Round float64/float32 values to bfloat16 (nearest even), returned as float64."""
+    return torch.as_tensor(np.asarray(x, dtype=np.float32)).to(torch.bfloat16).double().numpy()
+
+
+def gelu(z):
+    return 0.5 * z * (1 + erf(z / np.sqrt(2)))
+
+
+def gelu_grad(z):
+    return 0.5 * (1 + erf(z / np.sqrt(2))) + z * np.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+
+
+def oracle_forward_backward(W16, b, x16, dy16):
+    """float64 restatement with the kernels' bf16 roundings of activations and gradients."""
+    hs, zs = [x16], []
+    h = x16
+    L = len(W16)
+    for li in range(L):
+        z = h @ W16[li] + b[li]
+        zs.append(z)
+        if li < L - 1:
+            h = bf16(gelu(z))
+            hs.append(h)
+    dW, db = [None] * L, [None] * L
+    dz = dy16
+    for li in range(L - 1, -1, -1):
+        dW[li] = hs[li].T @ dz
+        db[li] = dz.sum(0)
+        if li > 0:
+            dz = bf16((dz @ W16[li].T) * gelu_grad(zs[li - 1]))
+    return zs[-1], dW, db
+
+
+def test_forward_and_gradients_match_oracle(cuda):
+    mlp = BF16MLP(device=cuda, seed=1)
+    rng = np.random.default_rng(0)
+    M = 300  # not a multiple of the 64-row tile
+    x = torch.as_tensor(rng.standard_normal((M, 4)), dtype=torch.float32)
+    x16 = x.to(torch.bfloat16).to(cuda)
+    y, acts, zs = mlp.forward(x16, keep=True)
+    dy = torch.as_tensor(rng.standard_normal((M, 1)) * 0.1, dtype=torch.float32)
+    dy16 = dy.to(torch.bfloat16).to(cuda)
+    dW, db = mlp.backward(dy16, acts, zs)
+    W16 = [w.double().cpu().numpy() for w in mlp.W16]
+    b = [v.double().cpu().numpy() for v in mlp.b]
+    y_ref, dW_ref, db_ref = oracle_forward_backward(W16, b, x16.double().cpu().numpy(),
+                                                    dy16.double().cpu().numpy())
+    np.testing.assert_allclose(y.double().cpu().numpy(), y_ref, rtol=2e-3, atol=2e-3)
+    for li in range(len(W16)):
+        scale = np.abs(dW_ref[li]).max()
+        assert np.abs(dW[li].double().cpu().numpy() - dW_ref[li]).max() <= 3e-2 * scale, li
+        np.testing.assert_allclose(db[li].double().cpu().numpy(), db_ref[li], rtol=3e-2,
+                                   atol=3e-2 * np.abs(db_ref[li]).max())
+
+
+def test_training_fits_a_smooth_function(cuda):
+    """A few epochs on y = f(x) reduce the loss by an order of magnitude."""
+    rng = np.random.default_rng(2)
+    X = torch.as_tensor(rng.uniform(-1, 1, (16384, 4)), dtype=torch.float32)
+    y = torch.sin(2 * X[:, 0]) + X[:, 1] * X[:, 2] - 0.5 * X[:, 3] ** 2
+    mlp = BF16MLP(device=cuda, seed=3)
+    losses = mlp.train(X, y, epochs=12, batch=1024, lr=2e-3)
+    assert losses[-1] < 0.1 * losses[0]
+    pred = mlp.predict(X[:2048])
+    err = (pred.cpu() - y[:2048]).abs().mean()
+    assert float(err) < 0.08
