@@ -119,8 +119,8 @@ class BF16MLP:
             _lib.check(rc, "dgb_adam")
 
     def standardize_fit(self, X, y):
-        self.x_mean = X.mean(0)
-        self.x_std = X.std(0).clamp_min(1e-6)
+        self.x_mean = X.mean(0).to(self.device)
+        self.x_std = X.std(0).clamp_min(1e-6).to(self.device)
         self.y_mean = float(y.mean())
         self.y_std = float(y.std().clamp_min(1e-6))
 
