@@ -184,3 +184,26 @@ class Thresholder:
 def horizon_steps(pw_max_ms, dt=0.005, extra_ms=4.0):
     """Trial horizon: the longest pulse plus 4 ms, in steps."""
     return int(np.ceil((float(pw_max_ms) + extra_ms) / dt))
+
+
+def learned_thresholds(th: Thresholder, pred_ma, margin, n_steps, max_lb_fix=10):
+    """Thresholds from a proposed bracket, confirmed by the same bisection.
+
+    The bracket is ``pred * exp(-margin) .. pred * exp(margin)``.  Lanes whose
+    lower end fires are moved down (halved) until it does not; the upper end
+    goes through the Thresholder's bound fixing (doubling) as usual.  The
+    bisection then narrows every lane to the tolerance, so the result satisfies
+    exactly the same acceptance rule as plain bisection.  Returns (ub, lb).
+    """
+    pred = torch.as_tensor(pred_ma, dtype=torch.float64, device=th.pop.device)
+    lb = pred * float(np.exp(-margin))
+    ub = pred * float(np.exp(margin))
+    lanes = torch.ones(th.B, dtype=torch.bool, device=th.pop.device)
+    for _ in range(max_lb_fix):
+        bad = th.check_active(lb, lanes, n_steps)
+        if not bool(bad.any()):
+            break
+        ub = torch.where(bad, lb, ub)  # a firing lower end is a valid upper end
+        lb = torch.where(bad, lb * 0.5, lb)
+        lanes = bad
+    return th.calculate_thresholds(n_steps, lb=lb, ub=ub)
