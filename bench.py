@@ -244,6 +244,109 @@ def bench_c3(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+MLP_FLOP_PER_SAMPLE = 2 * (4 * 256 + 256 * 256 + 256 * 256 + 256 * 1)
+
+
+def bench_c5(args, world, rank, local):
+    """Config 5: thresholds/s of the learned bracket + confirming bisection vs
+    plain bisection, 65,536 myelinated-fibre-like cables (241 compartments),
+    rtol 1%, dt 0.005 ms, horizon = longest pulse + 4 ms.  The MLP (4 -> 256 ->
+    256 -> 256 -> 1, GELU, BF16) is trained on ``--train`` plain-bisection
+    thresholds first.  One bench step = one batch of thresholds."""
+    import torch
+
+    from dendra_gb300.mlp import BF16MLP, MLP_FLOPS_NOTE, fibre_features
+    from dendra_gb300.threshold import (Thresholder, fibre_params, fibre_population,
+                                        horizon_steps, learned_thresholds)
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    batch = min(args.cables, 65536) if args.cables != 16384 else 65536
+
+    def plain(p):
+        pop = fibre_population(p, device=dev)
+        th = Thresholder(pop, lb=0.0, ub=0.1, rtol=0.01)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ub, lb = th.calculate_thresholds(horizon_steps(p["pw"].max()))
+        torch.cuda.synchronize()
+        return ub, lb, time.perf_counter() - t0, th
+
+    # training data from the plain solver
+    t0 = time.perf_counter()
+    X, Y = [], []
+    for i, s0 in enumerate(range(0, args.train, 65536)):
+        n = min(65536, args.train - s0)
+        p = fibre_params(n, seed=1000 + i)
+        ub, _, _, _ = plain(p)
+        ok = torch.isfinite(ub).cpu()
+        X.append(fibre_features(p)[ok])
+        Y.append(torch.log(ub.cpu()[ok]).float())
+    X, Y = torch.cat(X), torch.cat(Y)
+    gen_s = time.perf_counter() - t0
+    mlp = BF16MLP(device=dev, seed=0)
+    t0 = time.perf_counter()
+    n_val = min(8192, X.shape[0] // 10)
+    mlp.train(X[n_val:], Y[n_val:], epochs=30, batch=2048, lr=2e-3)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    err = (mlp.predict(X[:n_val]).cpu().double() - Y[:n_val].double()).abs()
+    margin = float(torch.quantile(err, 0.95))
+
+    plain_t, learned_t = [], []
+    agree = 0.0
+    for step in range(args.warmup + args.steps):
+        p = fibre_params(batch, seed=7 + step)
+        pub, plb, tp, thp = plain(p)
+        pop = fibre_population(p, device=dev)
+        th = Thresholder(pop, lb=0.0, ub=0.1, rtol=0.01)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pred = torch.exp(mlp.predict(fibre_features(p)).double())
+        lub, llb = learned_thresholds(th, pred, margin, horizon_steps(p["pw"].max()))
+        torch.cuda.synchronize()
+        tl = time.perf_counter() - t0
+        if step >= args.warmup:
+            plain_t.append(tp)
+            learned_t.append(tl)
+            fin = torch.isfinite(pub) & torch.isfinite(lub)
+            agree = float(((llb <= pub) & (plb <= lub))[fin].float().mean())
+    value = batch / float(np.mean(learned_t))
+    plain_v = batch / float(np.mean(plain_t))
+    # MLP inference roofline on the tensor pipe
+    feats = fibre_features(fibre_params(batch, seed=99))
+    for _ in range(3):
+        mlp.predict(feats)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    xin = mlp._inputs(feats.to(dev))
+    e0.record()
+    for _ in range(10):
+        mlp.forward(xin)
+    e1.record()
+    e1.synchronize()
+    mlp_ms = e0.elapsed_time(e1) / 10
+    flops = MLP_FLOP_PER_SAMPLE * batch / (mlp_ms * 1e-3) / 1e12
+    peak = 1927.7
+    line = {
+        "metric": "thresholds/s", "value": value, "unit": "thresholds/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(learned_t)) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "c5-learned-threshold", "batch": batch, "rtol": 0.01,
+                   "training_thresholds": int(X.shape[0]), "dt_ms": 0.005,
+                   "horizon": "longest pulse + 4 ms"},
+        "plain_bisection": {"value": plain_v, "unit": "thresholds/s"},
+        "speedup_vs_plain_bisection": value / plain_v,
+        "mlp": {"median_abs_log_err": float(err.median()), "margin": margin,
+                "bracket_agreement": agree, "train_s": train_s, "data_generation_s": gen_s,
+                "inference_ms": mlp_ms},
+        "roofline": {"bound": "tensor", "achieved": flops, "peak": peak, "unit": "TFLOP/s",
+                     "frac": flops / peak, "traffic": None, "note": MLP_FLOPS_NOTE},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -256,8 +359,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3"],
-                    help="c2: uneven cable population (default); c3: branched-cell network")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
+                    help="c2: uneven cable population (default); c3: branched-cell network; "
+                         "c5: learned threshold proposal vs plain bisection")
+    ap.add_argument("--train", type=int, default=200000, help="c5 training thresholds")
     ap.add_argument("--cables", type=int, default=16384,
                     help="cables per rank (a smaller case for profiling)")
     ap.add_argument("--timesteps", type=int, default=0, help="timesteps per run (default 2000)")
@@ -265,6 +370,8 @@ def main():
     world, rank, local = _dist()
     if args.workload == "c3":
         return bench_c3(args, world, rank, local)
+    if args.workload == "c5":
+        return bench_c5(args, world, rank, local)
     if args.impl == "reference":
         return run_reference(args, world, rank)
 
