@@ -144,8 +144,11 @@ class Thresholder:
             return aw >= self.atol
         return rw >= self.rtol
 
-    def calculate_thresholds(self, n_steps, lb=None, ub=None):
-        """Return (ub, lb) with NaN for ignored lanes; n_steps = horizon in steps."""
+    def calculate_thresholds(self, n_steps, lb=None, ub=None, lb_verified=False):
+        """Return (ub, lb) with NaN for ignored lanes; n_steps = horizon in steps.
+
+        lb_verified: the caller has already run the lower bounds and none fired,
+        so the lower-bound trial is not repeated."""
         lb = (self.lb_initial if lb is None else lb).clone()
         ub = (self.ub_initial if ub is None else ub).clone()
         ignore = torch.zeros(self.B, dtype=torch.bool, device=self.pop.device)
@@ -163,7 +166,10 @@ class Thresholder:
                 break
             ub = torch.where(~active, ub * self.fix_bound_up, ub)
             tries += 1
-        act_lb = self.check_active(lb, ~ignore, n_steps) & ~ignore
+        if not lb_verified:
+            act_lb = self.check_active(lb, ~ignore, n_steps) & ~ignore
+        else:
+            act_lb = torch.zeros_like(ignore)
         if bool(act_lb.any()):
             raise RuntimeError("Some lower bounds are active. Cannot proceed with bisection.")
         msk = self._tolerance_open(lb, ub) & ~ignore
@@ -206,4 +212,6 @@ def learned_thresholds(th: Thresholder, pred_ma, margin, n_steps, max_lb_fix=10)
         ub = torch.where(bad, lb, ub)  # a firing lower end is a valid upper end
         lb = torch.where(bad, lb * 0.5, lb)
         lanes = bad
-    return th.calculate_thresholds(n_steps, lb=lb, ub=ub)
+    # lower ends of lanes whose upper end fails get replaced by a verified
+    # inactive value inside bound fixing (ub only grows), so they stay valid
+    return th.calculate_thresholds(n_steps, lb=lb, ub=ub, lb_verified=True)
