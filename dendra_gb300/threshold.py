@@ -205,13 +205,15 @@ def learned_thresholds(th: Thresholder, pred_ma, margin, n_steps, max_lb_fix=10)
     lb = pred * float(np.exp(-margin))
     ub = pred * float(np.exp(margin))
     lanes = torch.ones(th.B, dtype=torch.bool, device=th.pop.device)
+    verified = False
     for _ in range(max_lb_fix):
         bad = th.check_active(lb, lanes, n_steps)
         if not bool(bad.any()):
+            verified = True
             break
         ub = torch.where(bad, lb, ub)  # a firing lower end is a valid upper end
         lb = torch.where(bad, lb * 0.5, lb)
         lanes = bad
     # lower ends of lanes whose upper end fails get replaced by a verified
     # inactive value inside bound fixing (ub only grows), so they stay valid
-    return th.calculate_thresholds(n_steps, lb=lb, ub=ub, lb_verified=True)
+    return th.calculate_thresholds(n_steps, lb=lb, ub=ub, lb_verified=verified)
