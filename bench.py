@@ -244,6 +244,188 @@ def bench_c3(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+# adjoint launch, per compartment-step: tape read (v, m, h, n) 16 B + adjoint
+# state read and write 32 B (the unfused reverse step's traffic)
+C4_ADJ_BYTES_PER_COMP_STEP = 48
+
+
+def _c4_cpu(n_sample, n_steps, seed=4):
+    """Oracle forward + reverse sweep of the config-4 fit on a sample of cables.
+
+    Returns (seconds, compartment-steps, threads)."""
+    import torch
+
+    import oracle
+    from dendra_gb300.workloads import c4_spec, cable_population_c4
+
+    pop, spec = cable_population_c4(n_sample, seed=seed, dtype=torch.float32, device="cpu")
+    p = pop.problem_dict()
+    p["rec_idx"] = np.zeros(pop.B, dtype=np.int32)
+    rng = np.random.default_rng(0)
+    tg = rng.standard_normal((pop.B, n_steps + 1)).astype(np.float32) * 1e-3
+    t0 = time.perf_counter()
+    oracle.cable_grad(p, n_steps, tg)
+    return time.perf_counter() - t0, pop.N * n_steps, oracle.num_threads()
+
+
+def bench_c4(args, world, rank, local):
+    """Config 4: seconds per gradient iteration (forward with checkpoints every
+    500 steps + checkpointed recompute + adjoint) of an MSE fit of somatic
+    traces, 1,024 HH cables x 201 compartments, float32, dt 0.025 ms,
+    20,000 steps; gradients w.r.t. per-cable gnabar, gkbar, gl and Ra."""
+    import torch
+
+    from dendra_gb300.adjoint import CableGradient, cable_traces
+    from dendra_gb300.workloads import C4_CHECKPOINT, C4_STEPS, cable_population_c4
+
+    n_cables = min(args.cables, 1024) if args.cables != 16384 else 1024
+    n_ts = args.timesteps or C4_STEPS
+    full_units = n_cables * 201 * n_ts
+    sample, sample_steps = 64, 2000
+    cfg = {"workload": "c4-adjoint-hh-fit", "n_cables": n_cables * world, "K": 201,
+           "dt_ms": 0.025, "timesteps": n_ts, "checkpoint_every": C4_CHECKPOINT,
+           "params": "per-cable gnabar, gkbar, gl, Ra", "loss": "MSE of somatic traces"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        secs = []
+        for _ in range(args.steps):
+            dt, units, cores = _c4_cpu(sample, sample_steps)
+            secs.append(dt * full_units / units)
+        v = float(np.median(secs))
+        print(json.dumps({
+            "impl": "reference", "metric": "grad s/iter", "value": v, "unit": "s/iter",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "s/iter", "cores": cores, "kind": "port",
+                             "sample": f"{sample} cables x {sample_steps} steps forward + reverse, "
+                                       "scaled to the full workload by compartment-steps"},
+            "e2e": {"value": v, "unit": "s/iter", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pop, spec = cable_population_c4(n_cables, seed=4 + rank, device=dev)
+    run = CableGradient(pop, n_ts, rec_idx=0, checkpoint_every=C4_CHECKPOINT)
+    names = ("gnabar", "gkbar", "gl", "ra")
+    hidden = [torch.as_tensor(spec["hidden"][k], dtype=torch.float32, device=dev) for k in names]
+    guess = [torch.as_tensor(spec["guess"][k], dtype=torch.float32, device=dev) for k in names]
+    run.set_params(*hidden)
+    target = run.forward().clone()
+    n_seg = -(-n_ts // C4_CHECKPOINT)
+
+    def grad_step(params, tgt):
+        prm = [t.detach().requires_grad_() for t in params]
+        trace = cable_traces(run, *prm)
+        loss = ((trace - tgt) ** 2).mean()
+        loss.backward()
+        return loss, [t.grad for t in prm]
+
+    for _ in range(max(3, args.warmup)):
+        grad_step(guess, target)
+    torch.cuda.synchronize()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    times = []
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            loss, grads = grad_step(guess, target)
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    # the dominant kernel alone: one segment's adjoint launch, timed with events
+    seg_k = n_seg - 1
+    step0, steps = run._segments()[seg_k]
+    work = tuple(c.clone() for c in run.checkpoints[seg_k])
+    import ctypes
+
+    from dendra_gb300 import _lib
+    L = _lib.load()
+    args_f = run._args(steps, step0, work)
+    _lib.check(L.dgb_cable_run_taped(args_f, run._tape.data_ptr(), _lib.stream_ptr(dev)),
+               "dgb_cable_run_taped")
+    adj = _lib.CableAdjointArgs()
+    bufs = [torch.zeros(pop.N, device=dev) for _ in range(8)]
+    gt = torch.zeros((pop.B, n_ts + 1), device=dev)
+    adj.tape, adj.trace_grad, adj.trace_len = run._tape.data_ptr(), gt.data_ptr(), n_ts + 1
+    (adj.lam_v, adj.lam_m, adj.lam_h, adj.lam_n, adj.grad_gnabar, adj.grad_gkbar, adj.grad_gl,
+     adj.grad_axial) = (b.data_ptr() for b in bufs)
+    adj_ms = []
+    for i in range(6):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        _lib.check(L.dgb_cable_adjoint(args_f, ctypes.byref(adj), _lib.stream_ptr(dev)),
+                   "dgb_cable_adjoint")
+        e1.record(st)
+        e1.synchronize()
+        if i >= 2:
+            adj_ms.append(e0.elapsed_time(e1))
+    adj_ms = float(np.mean(adj_ms))
+    peak, peak_kind = _peaks()
+    achieved = C4_ADJ_BYTES_PER_COMP_STEP * pop.N * steps / (adj_ms * 1e-3) / 1e9
+
+    # ---- end to end: parameters and targets from pinned host memory, loss and
+    # gradients back to the host, every iteration
+    h_params = [t.cpu().pin_memory() for t in guess]
+    h_target = target.cpu().pin_memory()
+    d_params = [torch.empty_like(t) for t in guess]
+    d_target = torch.empty_like(target)
+    h_out = torch.empty(1 + 4 * pop.B, dtype=torch.float32).pin_memory()
+    h2d = sum(t.numel() * 4 for t in h_params) + h_target.numel() * 4
+    d2h = h_out.numel() * 4
+
+    def e2e_step():
+        for d, h in zip(d_params, h_params):
+            d.copy_(h, non_blocking=True)
+        d_target.copy_(h_target, non_blocking=True)
+        loss, grads = grad_step(d_params, d_target)
+        out = torch.cat([loss.reshape(1)] + [g.float() for g in grads])
+        h_out.copy_(out, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    line = {
+        "metric": "grad s/iter", "value": ms * 1e-3, "unit": "s/iter", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {**cfg, "l2": "flushed between timed steps"},
+        "compartment_steps_per_s": 3 * full_units / (ms * 1e-3),
+        "loss": float(loss), "grad_norms": [float(g.norm()) for g in grads],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "cable_adjoint_kernel", "kernel_ms": adj_ms,
+                     "note": f"{C4_ADJ_BYTES_PER_COMP_STEP} algorithmic B per compartment-step "
+                             f"(tape read + adjoint state r/w) x {pop.N * steps} per launch; "
+                             f"on-chip bound in practice; peak {peak_kind}"},
+        "e2e": {"value": e2e_s, "unit": "s/iter", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps * 3 * n_seg,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        dt, units, cores = _c4_cpu(32, 1000)
+        line["cpu_baseline"] = {"value": dt * full_units / units, "unit": "s/iter",
+                                "cores": cores, "kind": "port",
+                                "sample": "32 cables x 1000 steps forward + reverse (oracle), "
+                                          "scaled to the full workload by compartment-steps"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 MLP_FLOP_PER_SAMPLE = 2 * (4 * 256 + 256 * 256 + 256 * 256 + 256 * 1)
 
 
@@ -359,8 +541,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
                     help="c2: uneven cable population (default); c3: branched-cell network; "
+                         "c4: adjoint gradient of a trace fit; "
                          "c5: learned threshold proposal vs plain bisection")
     ap.add_argument("--train", type=int, default=200000, help="c5 training thresholds")
     ap.add_argument("--cables", type=int, default=16384,
@@ -370,6 +553,8 @@ def main():
     world, rank, local = _dist()
     if args.workload == "c3":
         return bench_c3(args, world, rank, local)
+    if args.workload == "c4":
+        return bench_c4(args, world, rank, local)
     if args.workload == "c5":
         return bench_c5(args, world, rank, local)
     if args.impl == "reference":

@@ -56,6 +56,16 @@ class CableArgs(ctypes.Structure):
     ]
 
 
+class CableAdjointArgs(ctypes.Structure):
+    """Mirror of ``dgb_cable_adjoint_args``."""
+
+    _fields_ = [
+        ("tape", _P), ("trace_grad", _P), ("trace_len", _I64),
+        ("lam_v", _P), ("lam_m", _P), ("lam_h", _P), ("lam_n", _P),
+        ("grad_gnabar", _P), ("grad_gkbar", _P), ("grad_gl", _P), ("grad_axial", _P),
+    ]
+
+
 # name -> (restype, argtypes); every symbol declared in include/dendra_gb300.h
 SIGNATURES = {
     "dgb_version": (ctypes.c_char_p, []),
@@ -68,6 +78,9 @@ SIGNATURES = {
     "dgb_cable_assemble": (_INT, [ctypes.POINTER(CableArgs), _I32, _P, _P, _P, _P, _P]),
     "dgb_cable_solve_update": (_INT, [ctypes.POINTER(CableArgs), _P, _P, _P, _P, _P]),
     "dgb_cable_step_static": (_INT, [ctypes.POINTER(CableArgs), _I32, _P]),
+    "dgb_cable_run_taped": (_INT, [ctypes.POINTER(CableArgs), _P, _P]),
+    "dgb_cable_adjoint": (_INT, [ctypes.POINTER(CableArgs), ctypes.POINTER(CableAdjointArgs), _P]),
+    "dgb_cable_adjoint_args_size": (ctypes.c_size_t, []),
     "dgb_dhs_solve": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P, _P]),
     "dgb_dhs_solve_forest": (_INT, [_INT, _P, _P, _P, _P, _P, _P]),
     "dgb_detect_spikes": (_INT, [_INT, _P, _P, _I64, _D, _P, _P, _P]),

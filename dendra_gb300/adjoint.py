@@ -1,0 +1,196 @@
+"""Gradients of recorded cable traces through the hand-written adjoint kernels.
+
+The reference differentiates a cable run with torch autograd through every
+step of its eager update (integrators/implicit.py:569-664, the cnexp gate
+step mechanisms/_cnexp.py:96-132, the HH rates mod/HH.py:24-40 and current
+:109-116) and, on the GPU, the transpose solve of ThomasSolve.backward
+(triton/t_kernel_thomas.py:147-189).  Here the same gradient comes from two
+kernels per segment of ``checkpoint_every`` steps:
+
+* ``dgb_cable_run_taped`` recomputes the segment from its checkpoint and
+  writes the state tape (v, m, h, n after every step);
+* ``dgb_cable_adjoint`` walks the segment backwards: transposed chunked
+  tridiagonal solve, reverse of the membrane assembly and of the gate advance,
+  accumulating dLoss/d(gnabar, gkbar, gl) per compartment and the axial term.
+
+The forward pass keeps only the checkpoints (state every ``checkpoint_every``
+steps) and the recorded trace.  ``cable_traces`` wraps both passes in a
+``torch.autograd.Function`` whose inputs are per-cable gnabar, gkbar, gl and
+Ra (the parameters config 4 fits) and whose output is the somatic trace.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .cable import CablePopulation
+
+
+class CableGradient:
+    """Checkpointed forward and adjoint of a recorded trace of ``pop``.
+
+    pop: an initialized CablePopulation (its state is the initial state of
+    every forward; it is not modified).  rec_idx: local compartment recorded
+    per cable (int or per-cable sequence).  The trace has one sample per step,
+    (B, n_steps + 1), sample 0 being the initial state.
+    """
+
+    def __init__(self, pop: CablePopulation, n_steps: int, rec_idx=0, checkpoint_every=500):
+        if pop.dt is None:
+            raise RuntimeError("Model must be initialized before running.")
+        if pop.fast_math:
+            raise ValueError("gradients use the exact update; build the population without "
+                             "fast_math")
+        if n_steps < 1 or checkpoint_every < 1:
+            raise ValueError("n_steps and checkpoint_every must be >= 1")
+        self.pop = pop
+        self.n_steps = int(n_steps)
+        self.seg = int(min(checkpoint_every, n_steps))
+        dev = pop.device
+        kk = torch.as_tensor(pop.n_comp, dtype=torch.int32)
+        rec = torch.as_tensor(rec_idx, dtype=torch.int32).expand(pop.B).contiguous()
+        if bool(((rec < 0) | (rec >= kk)).any()):
+            raise ValueError("rec_idx out of range for some cable")
+        self.rec = rec.to(dev)
+        self.state0 = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
+        self.counts = torch.as_tensor(pop.n_comp, device=dev)
+        self.comp_cable = pop._dev["comp_cable"].long()
+        self.base_axial = (pop._dev["g_right"].clone(), pop._dev["g_left"].clone())
+        first = torch.as_tensor(pop.cable_ptr_np[:-1], device=dev)
+        self.rhoa0 = pop.rhoa.to(dev, torch.float64)[first]
+        self.ra = self.rhoa0.clone()
+        self.checkpoints = []
+        self._tape = None
+
+    # -- parameters -------------------------------------------------------
+    def set_params(self, gnabar=None, gkbar=None, gl=None, ra=None):
+        """Per-cable values (B,) of the fitted parameters (None keeps the current)."""
+        d = self.pop._dev
+        for name, val in (("gnabar", gnabar), ("gkbar", gkbar), ("gl", gl)):
+            if val is not None:
+                d[name] = self._per_cable(val).to(self.pop.dtype)
+        if ra is not None:
+            ra = torch.as_tensor(ra, device=self.pop.device).to(torch.float64).reshape(-1)
+            if ra.numel() != self.pop.B or bool((ra <= 0).any()):
+                raise ValueError("ra must hold one positive value per cable")
+            self.ra = ra.clone()
+            kappa = (self.rhoa0 / ra)[self.comp_cable]
+            gr0, gl0 = self.base_axial
+            same = bool((ra == self.rhoa0).all())
+            d["g_right"] = gr0.clone() if same else (gr0.double() * kappa).to(self.pop.dtype)
+            d["g_left"] = gl0.clone() if same else (gl0.double() * kappa).to(self.pop.dtype)
+
+    def _per_cable(self, val):
+        val = torch.as_tensor(val, device=self.pop.device).reshape(-1)
+        if val.numel() != self.pop.B:
+            raise ValueError(f"expected {self.pop.B} per-cable values")
+        return torch.repeat_interleave(val, self.counts)
+
+    # -- passes -----------------------------------------------------------
+    def _args(self, steps, step0, state, trace=None):
+        a = self.pop._args(steps, 1)
+        a.rec_idx = self.rec.data_ptr()
+        a.trace = None if trace is None else trace.data_ptr()
+        a.v, a.m, a.h, a.n = (t.data_ptr() for t in state)
+        a.step0 = int(step0)
+        return a
+
+    def _segments(self):
+        return [(k * self.seg, min(self.seg, self.n_steps - k * self.seg))
+                for k in range((self.n_steps + self.seg - 1) // self.seg)]
+
+    def forward(self):
+        """Run all steps, keep the checkpoints, return the trace (B, n_steps + 1)."""
+        pop = self.pop
+        dev = pop.device
+        L = _lib.load()
+        state = tuple(t.clone() for t in self.state0)
+        trace = torch.empty((pop.B, self.n_steps + 1), dtype=pop.dtype, device=dev)
+        seg_trace = torch.empty((pop.B, self.seg + 1), dtype=pop.dtype, device=dev)
+        self.checkpoints = []
+        with torch.cuda.device(dev):
+            for step0, steps in self._segments():
+                self.checkpoints.append(tuple(t.clone() for t in state))
+                buf = seg_trace[:, :steps + 1]
+                if steps != self.seg:
+                    buf = torch.empty((pop.B, steps + 1), dtype=pop.dtype, device=dev)
+                args = self._args(steps, step0, state, buf)
+                # the taped kernel without a tape: the checkpoints lie on the
+                # trajectory the recompute reproduces bit for bit
+                _lib.check(L.dgb_cable_run_taped(args, None, _lib.stream_ptr(dev)),
+                           "dgb_cable_run_taped")
+                trace[:, step0:step0 + steps + 1] = buf
+        return trace
+
+    def backward(self, grad_trace):
+        """Per-cable gradients {gnabar, gkbar, gl, ra} for dLoss/dtrace (B, n_steps + 1)."""
+        if not self.checkpoints:
+            raise RuntimeError("backward() needs a forward() first")
+        pop = self.pop
+        dev = pop.device
+        N, B = pop.N, pop.B
+        gt = grad_trace.to(device=dev, dtype=pop.dtype).contiguous()
+        if tuple(gt.shape) != (B, self.n_steps + 1):
+            raise ValueError(f"grad_trace must be ({B}, {self.n_steps + 1})")
+        if self._tape is None or self._tape.dtype != pop.dtype:
+            self._tape = torch.empty((self.seg + 1, 4, N), dtype=pop.dtype, device=dev)
+        lam = torch.zeros((4, N), dtype=pop.dtype, device=dev)
+        gcomp = torch.zeros((3, N), dtype=pop.dtype, device=dev)
+        gax = torch.zeros(N, dtype=pop.dtype, device=dev)
+        work = tuple(torch.empty_like(t) for t in self.state0)
+        adj = _lib.CableAdjointArgs()
+        adj.tape = self._tape.data_ptr()
+        adj.trace_grad = gt.data_ptr()
+        adj.trace_len = self.n_steps + 1
+        adj.lam_v, adj.lam_m, adj.lam_h, adj.lam_n = (lam[i].data_ptr() for i in range(4))
+        adj.grad_gnabar, adj.grad_gkbar, adj.grad_gl = (gcomp[i].data_ptr() for i in range(3))
+        adj.grad_axial = gax.data_ptr()
+        L = _lib.load()
+        st = _lib.stream_ptr(dev)
+        with torch.cuda.device(dev):
+            for k, (step0, steps) in reversed(list(enumerate(self._segments()))):
+                for w, c in zip(work, self.checkpoints[k]):
+                    w.copy_(c)
+                args = self._args(steps, step0, work)
+                _lib.check(L.dgb_cable_run_taped(args, self._tape.data_ptr(), st),
+                           "dgb_cable_run_taped")
+                _lib.check(L.dgb_cable_adjoint(args, ctypes.byref(adj), st), "dgb_cable_adjoint")
+        # per-compartment results, kept for inspection: adjoint of the initial
+        # state (v, m, h, n), dLoss/d(gnabar, gkbar, gl) and the axial term
+        self.lam0, self.grad_comp, self.grad_axial = lam, gcomp, gax
+        per = self._per_cable_sum(torch.cat([gcomp, gax[None]]))
+        return {"gnabar": per[0], "gkbar": per[1], "gl": per[2], "ra": -per[3] / self.ra}
+
+    def _per_cable_sum(self, x):
+        """Deterministic float64 sums of (R, N) per-compartment rows over each cable."""
+        x = x.double()
+        ks = self.pop.n_comp
+        if min(ks) == max(ks):
+            return x.reshape(x.shape[0], self.pop.B, ks[0]).sum(dim=2)
+        cs = torch.nn.functional.pad(torch.cumsum(x, dim=1), (1, 0))
+        ptr = torch.as_tensor(self.pop.cable_ptr_np, device=x.device)
+        return cs[:, ptr[1:]] - cs[:, ptr[:-1]]
+
+
+class _TraceFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, gnabar, gkbar, gl, ra, runner):
+        runner.set_params(gnabar.detach(), gkbar.detach(), gl.detach(), ra.detach())
+        ctx.runner = runner
+        ctx.dtypes = tuple(t.dtype for t in (gnabar, gkbar, gl, ra))
+        return runner.forward()
+
+    @staticmethod
+    def backward(ctx, grad_trace):
+        g = ctx.runner.backward(grad_trace)
+        out = tuple(g[k].to(dt) for k, dt in zip(("gnabar", "gkbar", "gl", "ra"), ctx.dtypes))
+        return (*out, None)
+
+
+def cable_traces(runner: CableGradient, gnabar, gkbar, gl, ra):
+    """Recorded traces (B, n_steps + 1) as a differentiable function of the
+    per-cable gnabar, gkbar, gl (S/cm^2) and Ra (ohm cm)."""
+    return _TraceFunction.apply(gnabar, gkbar, gl, ra, runner)

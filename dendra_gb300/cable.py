@@ -104,8 +104,8 @@ class CablePopulation:
     diam, dx : float or sequence
         Per-cable diameter (um) and compartment length (um), or per-compartment
         packed arrays of length ``sum(n_comp)``.
-    rhoa : float
-        Axial resistivity (ohm cm).
+    rhoa : float or sequence
+        Axial resistivity (ohm cm): scalar, per cable or per compartment.
     cm : float or sequence
         Specific capacitance (uF/cm^2), scalar or per compartment.
     celsius, v_init : float
@@ -135,8 +135,8 @@ class CablePopulation:
         self.cable_ptr_np = ptr
         self.celsius = float(celsius)
         self.v_init = float(v_init)
-        self.rhoa = rhoa
         self._diam = self._per_comp(diam)
+        self.rhoa = self._per_comp(rhoa)
         self.cm = self._per_comp(cm)
         self._dx = self._per_comp(dx)
         hh = {**HH_DEFAULTS, **(hh or {})}
@@ -184,13 +184,12 @@ class CablePopulation:
         """
         dt_s = dt_seconds(dt, self.dtype)
         cm = torch.as_tensor(self.cm, dtype=self.dtype)
-        rhoa = torch.as_tensor(self.rhoa, dtype=self.dtype)
         diam, dx = self._diam, self._dx
         area = membrane_area(diam, dx)
         capacitance = 1.0e-6 * (cm * torch.ones_like(area)) * area
         cm_inv = capacitance.reciprocal()
         scale = area * cm_inv
-        g_edge = cylindrical_edge_conductance(diam, dx, rhoa * torch.ones_like(diam))
+        g_edge = cylindrical_edge_conductance(diam, dx, self.rhoa)
         cab = torch.as_tensor(np.repeat(np.arange(self.B), self.n_comp))
         inner = cab[1:] == cab[:-1]  # edge (i, i+1) lies inside one cable
         zero = torch.zeros_like(g_edge)

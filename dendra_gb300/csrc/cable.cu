@@ -54,3 +54,50 @@ extern "C" int dgb_cable_solve_update(const dgb_cable_args* args, const void* lo
     return cable_solve_update_t<float>(args, lower, main_diag, upper, rhs, st);
   return cable_solve_update_t<double>(args, lower, main_diag, upper, rhs, st);
 }
+
+static int validate_taped(const dgb_cable_args* args) {
+  DGB_REQUIRE(args->scratch != nullptr, "scratch (2 x int32, device) is required");
+  DGB_REQUIRE(args->n_comp >= 0, "n_comp must be the total compartment count");
+  DGB_REQUIRE((args->flags & (DGB_CABLE_STOP_ON_SPIKE | DGB_CABLE_FAST_MATH)) == 0,
+              "the taped run and the adjoint use the exact update without early stop "
+              "(DGB_CABLE_STOP_ON_SPIKE and DGB_CABLE_FAST_MATH are not accepted)");
+  const int64_t kmax = args->max_k;
+  DGB_REQUIRE(kmax >= 1 && kmax <= 32 * kCableMaxCH,
+              "max compartments per cable (max_k) must be in [1, %d], got %lld",
+              32 * kCableMaxCH, (long long)kmax);
+  return DGB_OK;
+}
+
+extern "C" int dgb_cable_run_taped(const dgb_cable_args* args, void* tape, void* stream) {
+  clear_error();
+  int rc = validate_cable_args(args);
+  if (rc) return rc;
+  rc = validate_taped(args);
+  if (rc) return rc;
+  if (args->n_cables == 0) return DGB_OK;
+  const int ch_max = (args->max_k + 31) / 32;
+  cudaStream_t st = as_stream(stream);
+  if (args->dtype == DGB_F32) return cable_run_taped_t<float>(args, tape, ch_max, st);
+  return cable_run_taped_t<double>(args, tape, ch_max, st);
+}
+
+extern "C" int dgb_cable_adjoint(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj,
+                                 void* stream) {
+  clear_error();
+  int rc = validate_cable_args(args);
+  if (rc) return rc;
+  rc = validate_taped(args);
+  if (rc) return rc;
+  DGB_REQUIRE(adj != nullptr && adj->tape != nullptr, "adjoint args with a tape are required");
+  DGB_REQUIRE(adj->lam_v && adj->lam_m && adj->lam_h && adj->lam_n,
+              "lam_v, lam_m, lam_h and lam_n are required");
+  DGB_REQUIRE(adj->grad_gnabar && adj->grad_gkbar && adj->grad_gl && adj->grad_axial,
+              "grad_gnabar, grad_gkbar, grad_gl and grad_axial are required");
+  DGB_REQUIRE(!adj->trace_grad || (args->rec_idx && adj->trace_len >= 0),
+              "trace_grad requires rec_idx and trace_len >= 0");
+  if (args->n_cables == 0) return DGB_OK;
+  const int ch_max = (args->max_k + 31) / 32;
+  cudaStream_t st = as_stream(stream);
+  if (args->dtype == DGB_F32) return cable_adjoint_t<float>(args, adj, ch_max, st);
+  return cable_adjoint_t<double>(args, adj, ch_max, st);
+}

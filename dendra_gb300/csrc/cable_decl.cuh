@@ -14,6 +14,11 @@ constexpr int kSolveUpdateMaxCH = 16;  // plain per-step solve: K <= 512
 template <typename T>
 int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st);
 template <typename T>
+int cable_run_taped_t(const dgb_cable_args* args, void* tape, int ch_max, cudaStream_t st);
+template <typename T>
+int cable_adjoint_t(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj, int ch_max,
+                    cudaStream_t st);
+template <typename T>
 int cable_assemble_t(const dgb_cable_args* args, int32_t step, void* lower, void* mainv,
                      void* upper, void* rhs, cudaStream_t st);
 template <typename T>

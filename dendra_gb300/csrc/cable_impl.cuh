@@ -27,141 +27,15 @@
   DGB_CASE_F32(3) DGB_CASE_F32(5) DGB_CASE_F32(6) DGB_CASE_F32(7) DGB_CASE_F32(9) \
   DGB_CASE_F32(10) DGB_CASE_F32(11) DGB_CASE_F32(12) DGB_CASE_F32(13)             \
   DGB_CASE_F32(14) DGB_CASE_F32(15)
-#include "cable_decl.cuh"
+#include "cable_common.cuh"
 #include "chunk_solve.cuh"
 
 namespace dgb {
 
-template <typename T>
-struct CableArgsT {
-  int n_cables, n_steps, rec_every;
-  const int64_t* cable_ptr;
-  const int32_t* order;
-  T *v, *m, *h, *n;
-  const T *g_right, *g_left, *scale, *cm_inv, *field;
-  const T *gnabar, *gkbar, *gl, *el;
-  T ena, ek, q10, dt, dt_s;
-  double dt_ms_d, t0_ms;
-  int64_t step0;
-  const T *ve_amp, *ve_delay, *ve_pw;
-  const int32_t* in_idx;
-  const T *in_amp, *in_delay, *in_pw;
-  const int32_t* rec_idx;
-  T* trace;
-  int64_t n_rec;
-  const int32_t* spk_idx;
-  T spk_thr;
-  int32_t *spk_below, *spk_count, *spk_first;
-  const int32_t* spk_idx2;
-  int32_t* spk_below2;
-  int stop_on_spike;
-  int32_t* counter;
-};
-
-template <typename T>
-static CableArgsT<T> typed(const dgb_cable_args* a) {
-  CableArgsT<T> t;
-  t.n_cables = a->n_cables;
-  t.n_steps = a->n_steps;
-  t.rec_every = a->rec_every > 0 ? a->rec_every : 1;
-  t.cable_ptr = a->cable_ptr;
-  t.order = a->order;
-  t.v = (T*)a->v;
-  t.m = (T*)a->m;
-  t.h = (T*)a->h;
-  t.n = (T*)a->n;
-  t.g_right = (const T*)a->g_right;
-  t.g_left = (const T*)a->g_left;
-  t.scale = (const T*)a->scale;
-  t.cm_inv = (const T*)a->cm_inv;
-  t.field = (const T*)a->field;
-  t.gnabar = (const T*)a->gnabar;
-  t.gkbar = (const T*)a->gkbar;
-  t.gl = (const T*)a->gl;
-  t.el = (const T*)a->el;
-  t.ena = (T)a->ena;
-  t.ek = (T)a->ek;
-  t.q10 = (T)a->q10;
-  t.dt = (T)a->dt_ms;
-  t.dt_s = (T)a->dt_s;
-  t.dt_ms_d = a->dt_ms;
-  t.t0_ms = a->t0_ms;
-  t.step0 = a->step0;
-  t.ve_amp = (const T*)a->ve_amp;
-  t.ve_delay = (const T*)a->ve_delay;
-  t.ve_pw = (const T*)a->ve_pw;
-  t.in_idx = a->in_idx;
-  t.in_amp = (const T*)a->in_amp;
-  t.in_delay = (const T*)a->in_delay;
-  t.in_pw = (const T*)a->in_pw;
-  t.rec_idx = a->rec_idx;
-  t.trace = (T*)a->trace;
-  t.n_rec = 1 + (int64_t)a->n_steps / t.rec_every;
-  t.spk_idx = a->spk_idx;
-  t.spk_thr = (T)a->spk_thr;
-  t.spk_below = a->spk_below;
-  t.spk_count = a->spk_count;
-  t.spk_first = a->spk_first;
-  t.spk_idx2 = a->spk_idx2;
-  t.spk_below2 = a->spk_below2;
-  t.stop_on_spike = (a->flags & DGB_CABLE_STOP_ON_SPIKE) ? 1 : 0;
-  t.counter = a->scratch;
-  return t;
-}
-
-// error bits of scratch[1]
-constexpr int kErrChunk = 1;
-
-// Shared-memory planes of one warp (one cable).  Plane q holds row j of lane r
-// at [(q * ch + j) * 32 + r]: the 32 lanes touch 32 consecutive words, so
-// every access is bank-conflict free for any chunk size ch.  Planes 0..6 are
-// always present; the rest only when a coefficient varies along the cable.
-enum { P_V = 0, P_M, P_H, P_N, P_AP, P_CP, P_DP, P_FIXED };
-
-struct PlaneLayout {
-  int n_planes;
-  int q_geo;   // g_right, g_left, scale planes (-1: uniform per cable)
-  int q_fld;   // extracellular lead field (-1: no ve)
-  int q_chan;  // gnabar, gkbar, gl, el planes (-1: uniform per cable)
-};
-
-__host__ __device__ inline PlaneLayout plane_layout(bool geo_planes, bool field, bool chan_planes) {
-  PlaneLayout L;
-  int q = P_FIXED;
-  L.q_geo = geo_planes ? q : -1;
-  q += geo_planes ? 3 : 0;
-  L.q_fld = field ? q : -1;
-  q += field ? 1 : 0;
-  L.q_chan = chan_planes ? q : -1;
-  q += chan_planes ? 4 : 0;
-  L.n_planes = q;
-  return L;
-}
-
-template <typename T>
-struct Planes {
-  T* base;
-  int ch;
-  __device__ __forceinline__ T& at(int q, int j, int r) const {
-    return base[(q * ch + j) * 32 + r];
-  }
-};
-
-// Division policy: exact IEEE division, or the approximate reciprocal in the
-// float32 fast-math variant.
-template <typename T, bool FAST>
-__device__ __forceinline__ T dv(T a, T b) {
-  if constexpr (FAST) {
-    return __fdividef(a, b);
-  } else {
-    return a / b;
-  }
-}
-
 // One cable, all steps, one warp.  ch = rows per lane (runtime), rows of lane
 // r are i = r*ch + j.  Rows with i >= K are identity rows with zero
 // coefficients and zero state.
-template <typename T, bool FAST>
+template <typename T, bool FAST, bool TAPE>
 __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
                           const PlaneLayout& lay) {
   const int r = threadIdx.x & 31;
@@ -235,6 +109,12 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
   if (spk_i >= 0 && r == spk_i / ch) below = A.spk_below[cable];
   if (spk_i2 >= 0 && r == spk_i2 / ch) below2 = A.spk_below2[cable];
   if (rec_i >= 0 && r == rec_i / ch) A.trace[(int64_t)cable * A.n_rec] = P.at(P_V, rec_i % ch, r);
+  if constexpr (TAPE) {
+    if (A.tape) {
+      tape_store<T>(P, K, ch, P_V, P_M, P_H, P_N, A.tape + off, A.n_comp);
+      __syncwarp();
+    }
+  }
 
   const T dt = A.dt, dt_s = A.dt_s, q10 = A.q10, ena = A.ena, ek = A.ek;
   const int last = ch - 1;
@@ -426,6 +306,13 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
     if (rec_i >= 0 && r == rec_i / ch && ((s + 1) % A.rec_every) == 0)
       A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = P.at(P_V, rec_i % ch, r);
     __syncwarp();  // new v visible to the neighbouring lanes
+    if constexpr (TAPE) {
+      if (A.tape) {
+        tape_store<T>(P, K, ch, P_V, P_M, P_H, P_N,
+                      A.tape + (int64_t)(s + 1) * 4 * A.n_comp + off, A.n_comp);
+        __syncwarp();  // the next step rewrites rows other lanes just read
+      }
+    }
   }
   for (int j = 0; j < ch; ++j) {
     const int i = r * ch + j;
@@ -446,9 +333,7 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
   __syncwarp();
 }
 
-constexpr int kCableWarps = 4;  // default warps (cables in flight) per block
-
-template <typename T, bool FAST>
+template <typename T, bool FAST, bool TAPE>
 __global__ void __launch_bounds__(kCableWarps * 32) cable_run_kernel(CableArgsT<T> A, int ch_max,
                                                                      PlaneLayout lay) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -467,7 +352,7 @@ __global__ void __launch_bounds__(kCableWarps * 32) cable_run_kernel(CableArgsT<
       if (lane == 0) atomicOr(A.counter + 1, kErrChunk);
       continue;
     }
-    run_cable<T, FAST>(A, cable, smw, ch, lay);
+    run_cable<T, FAST, TAPE>(A, cable, smw, ch, lay);
   }
 }
 
@@ -584,7 +469,7 @@ __global__ void __launch_bounds__(128) cable_solve_update_kernel(CableArgsT<T> A
   }
 }
 
-template <typename T, bool FAST>
+template <typename T, bool FAST, bool TAPE = false>
 static int launch_cable_run(CableArgsT<T> A, int ch_max, const PlaneLayout& lay,
                             cudaStream_t st) {
   // one warp per cable in flight; long cables get fewer warps per block so
@@ -596,7 +481,7 @@ static int launch_cable_run(CableArgsT<T> A, int ch_max, const PlaneLayout& lay,
               "cable too long for shared memory (%zu bytes per cable)", per_warp);
   const int threads = wpb * 32;
   const size_t smem = (size_t)wpb * per_warp;
-  auto kern = cable_run_kernel<T, FAST>;
+  auto kern = cable_run_kernel<T, FAST, TAPE>;
   DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   int per_sm = 0;
@@ -626,6 +511,17 @@ int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st) {
 }
 
 template <typename T>
+int cable_run_taped_t(const dgb_cable_args* args, void* tape, int ch_max, cudaStream_t st) {
+  CableArgsT<T> A = typed<T>(args);
+  A.tape = (T*)tape;
+  const bool field = args->field != nullptr && args->ve_amp != nullptr;
+  const bool chan_planes = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) == 0;
+  const bool geo_planes = (args->flags & DGB_CABLE_UNIFORM_GEOMETRY) == 0;
+  return launch_cable_run<T, false, true>(A, ch_max, plane_layout(geo_planes, field, chan_planes),
+                                         st);
+}
+
+template <typename T>
 int cable_assemble_t(const dgb_cable_args* args, int32_t step, void* lower, void* mainv,
                      void* upper, void* rhs, cudaStream_t st) {
   const int64_t N = args->n_comp;
@@ -652,6 +548,7 @@ int cable_solve_update_t(const dgb_cable_args* args, const void* lower, const vo
 
 #define DGB_INSTANTIATE_CABLE(T)                                                         \
   template int cable_run_t<T>(const dgb_cable_args*, int, cudaStream_t);               \
+  template int cable_run_taped_t<T>(const dgb_cable_args*, void*, int, cudaStream_t);   \
   template int cable_assemble_t<T>(const dgb_cable_args*, int32_t, void*, void*, void*, \
                                    void*, cudaStream_t);                               \
   template int cable_solve_update_t<T>(const dgb_cable_args*, const void*, const void*, \

@@ -34,3 +34,6 @@ extern "C" size_t dgb_cable_args_size(void) { return sizeof(dgb_cable_args); }
 
 // Size of dgb_net_args as compiled, for foreign mirrors of the struct.
 extern "C" size_t dgb_net_args_size(void) { return sizeof(dgb_net_args); }
+
+// Size of dgb_cable_adjoint_args as compiled, for foreign mirrors of the struct.
+extern "C" size_t dgb_cable_adjoint_args_size(void) { return sizeof(dgb_cable_adjoint_args); }

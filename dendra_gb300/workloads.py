@@ -11,6 +11,13 @@ float32; each cable sees a point source in a homogeneous medium
 centre, delivering a cathodic 0.1 ms pulse of U[0.1, 2] mA at t = 0;
 dt 0.005 ms for 10 ms (2000 steps).
 
+``cable_population_c4``: 1,024 HH cables of 201 compartments (Unmyelinated,
+L = 2010 um, dx = 10 um -> K = 201, diam 1 um), float32, dt 0.025 ms for
+20,000 steps (500 ms); a somatic step current of U[0.1, 0.4] nA from 5 ms to
+485 ms drives repetitive firing.  ``c4_spec`` also draws the hidden per-cable
+gnabar, gkbar, gl and Ra (defaults x U[0.7, 1.3]) whose somatic traces are the
+fit targets; the initial guesses are the defaults.
+
 No public dataset is involved; the generators stand in for the reference's
 configurations with the stated distributions.
 """
@@ -20,7 +27,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from .cable import CablePopulation
+from .cable import HH_DEFAULTS, CablePopulation, unmyelinated_K
 
 RHOE_OHM_CM = 1.0 / 0.3 * 100.0  # sigma = 0.3 S/m
 
@@ -68,3 +75,27 @@ def cable_population_c1(seed=1, dtype=torch.float64, device="cuda", n_cables=64)
 
 
 C1_STEPS = 2000
+
+
+C4_STEPS = 20000
+C4_CHECKPOINT = 500
+
+
+def c4_spec(n_cables=1024, seed=4):
+    rng = np.random.default_rng(seed)
+    amp_na = rng.uniform(0.1, 0.4, n_cables)
+    defaults = dict(gnabar=HH_DEFAULTS["gnabar"], gkbar=HH_DEFAULTS["gkbar"],
+                    gl=HH_DEFAULTS["gl"], ra=100.0)
+    hidden = {k: v * rng.uniform(0.7, 1.3, n_cables) for k, v in defaults.items()}
+    guess = {k: np.full(n_cables, v) for k, v in defaults.items()}
+    return dict(K=unmyelinated_K(2010.0, 10.0), amp_ma=amp_na * 1e-6, delay=5.0, pw=480.0,
+                hidden=hidden, guess=guess)
+
+
+def cable_population_c4(n_cables=1024, seed=4, dtype=torch.float32, device="cuda"):
+    """Config-4 population at the default parameters (the guesses)."""
+    s = c4_spec(n_cables, seed)
+    pop = CablePopulation([s["K"]] * n_cables, 1.0, 10.0, rhoa=100.0, celsius=6.3,
+                          v_init=-65.0, dtype=dtype, device=device)
+    pop.inject(0, torch.as_tensor(s["amp_ma"]), s["delay"], s["pw"])
+    return pop.initialize(0.025), s

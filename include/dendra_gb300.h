@@ -32,6 +32,10 @@
  *                             NetCon.advance (netcon.py:5183-5205) and
  *                             _dhs._step (integrators/tree.py:1202-1357)
  *   dgb_net_enqueue           NetCon enqueue, networks/_event_delivery.py:61-105
+ *   dgb_cable_run_taped /     reverse mode of the same update: the gradient the
+ *   dgb_cable_adjoint         reference takes by torch autograd through
+ *                             integrators/implicit.py:569-664 (transpose solve of
+ *                             ThomasSolve.backward, t_kernel_thomas.py:147-189)
  *   dgb_cable_assemble        the eager per-step assembly of the same update
  *                             (mechanism advance + membrane frame + RHS),
  *                             integrators/core.py:769-834, implicit.py:569-646
@@ -215,6 +219,65 @@ int dgb_cable_assemble(const dgb_cable_args* args, int32_t step,
 int dgb_cable_solve_update(const dgb_cable_args* args, const void* lower,
                            const void* main_diag, const void* upper,
                            const void* rhs, void* stream);
+
+/*
+ * dgb_cable_run that also writes the state tape of the run, for the adjoint:
+ *   tape: (n_steps + 1, 4, n_comp) in the state dtype; tape[k][q][g] is
+ *   state q (0 v, 1 m, 2 h, 3 n) of compartment g after k steps of this call.
+ * n_comp must be set; DGB_CABLE_STOP_ON_SPIKE and DGB_CABLE_FAST_MATH are
+ * rejected (the adjoint differentiates the exact update).  This is the
+ * recompute pass of checkpoint-and-recompute: run it from a checkpoint over
+ * one segment, then dgb_cable_adjoint over the same segment.  tape = NULL
+ * runs the same kernel without writing a tape: checkpoints taken that way lie
+ * on bitwise the same trajectory as the taped recompute.
+ */
+int dgb_cable_run_taped(const dgb_cable_args* args, void* tape, void* stream);
+
+/*
+ * Adjoint of one segment of dgb_cable_run.  The reference obtains these
+ * gradients by torch autograd through the step (integrators/implicit.py:569-664,
+ * mechanisms/_cnexp.py:96-132, mod/HH.py:24-40,109-116) and the transpose
+ * solve of ThomasSolve.backward (triton/t_kernel_thomas.py:147-189).
+ */
+typedef struct dgb_cable_adjoint_args {
+  const void* tape;       /* the segment's tape from dgb_cable_run_taped */
+  const void* trace_grad; /* [n_cables][trace_len]: dLoss/dtrace, trace sample k
+                             recorded after global step k*rec_every; NULL: none */
+  int64_t trace_len;
+  /* adjoint state per compartment: in, the adjoint of the state after the
+     segment; out, the adjoint of the state before it */
+  void* lam_v;
+  void* lam_m;
+  void* lam_h;
+  void* lam_n;
+  /* accumulated (+=) per compartment: dLoss/dgnabar, dLoss/dgkbar, dLoss/dgl */
+  void* grad_gnabar;
+  void* grad_gkbar;
+  void* grad_gl;
+  /* accumulated (+=) per compartment: lam_g * g for both axial bands
+     (g_right, g_left) of the compartment's row, i.e. dLoss/dkappa_i for
+     g -> kappa_i g.  The bands scale as 1/Ra, so for one Ra per cable
+     dLoss/dRa = -(sum over the cable's compartments of grad_axial) / Ra.
+     Every accumulator is carried through the segment in the same order as one
+     uninterrupted reverse sweep, so results do not depend on the segment
+     length. */
+  void* grad_axial;
+} dgb_cable_adjoint_args;
+
+/*
+ * Walk one segment backwards: args describes the forward segment (same
+ * population, stimulus, rec_idx, rec_every, step0 and n_steps as the taped run;
+ * v/m/h/n are not read).  One warp per cable; the transposed tridiagonal
+ * system is solved with the same chunked elimination as the forward.
+ * Exact (non-fast) float32 or float64 arithmetic; the cable size limit is set
+ * by shared memory (float32: K <= 1024; float64: K <= 896 with every optional
+ * plane present).
+ */
+int dgb_cable_adjoint(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj,
+                      void* stream);
+
+/* sizeof(dgb_cable_adjoint_args) as compiled (for foreign-language mirrors). */
+size_t dgb_cable_adjoint_args_size(void);
 
 /*
  * Tree (DHS/Hines) solve of B trees sharing one topology of K nodes, in the

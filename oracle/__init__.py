@@ -11,7 +11,9 @@ reference implementation itself (``tests/golden/make_golden.py``), and
 
 Layers:
   * ``oracle.c`` / ``oracle_impl.h``  float64 and float32 C restatements of the
-    HH rates, cnexp, the backward-Euler cable update, Thomas, PCR and DHS.
+    HH rates, cnexp, the backward-Euler cable update, Thomas, PCR and DHS,
+    and the reverse mode of the cable update (``cable_grad``: full state
+    tape, transposed Thomas solve, gate partials on the forward's branches).
   * ``events.py``  numpy restatement of NetCon delay rounding, the dense delay
     ring and bit-packed delivery (integer/index work).
   * ``trees.py``   numpy restatement of the tree topology plan and the DHS
@@ -29,6 +31,7 @@ from .core import (  # noqa: F401
     thomas,
     pcr,
     cable_run,
+    cable_grad,
     dhs_solve,
     net_run,
     num_threads,

@@ -71,6 +71,10 @@ def _declare(L):
             [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
             + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P, _I32, _P, _P]
         )
+        getattr(L, "orc_cable_grad" + sfx).argtypes = (
+            [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
+            + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _I32] + [_P] * 8
+        )
         getattr(L, "orc_net_run" + sfx).argtypes = (
             [_I32, _I32, _I64, _I64, _P, _I64] + [_P] * 9 + [_P] * 9 + [_D] * 7
             + [_P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _I64, _I32, _D, _I64, _P, _P, _P, _P, _P,
@@ -223,6 +227,53 @@ def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
         _ptr(spk_below2),
     )
     return trace, spk_count, spk_first, spk_below
+
+
+def cable_grad(p: dict, n_steps: int, trace_grad, rec_every: int = 1, t0_ms: float = 0.0,
+               gate_f32: bool = False):
+    """Reverse mode of ``cable_run`` for a trace functional.
+
+    ``trace_grad`` (B, 1 + n_steps // rec_every) is dLoss/dtrace for the trace
+    ``cable_run`` records from the same state.  Returns a dict with lam_v,
+    lam_m, lam_h, lam_n (adjoint of the initial state), g_gnabar, g_gkbar,
+    g_gl and g_axial (per compartment; g_axial is lam_g * g over the axial
+    bands, so dLoss/dRa of a cable = -sum of its g_axial / Ra).  ``p``'s state arrays end at
+    the final state, as after ``cable_run``.
+    """
+    dtype = p["v"].dtype
+    sfx = _sfx(dtype)
+    B = int(p["cable_ptr"].size - 1)
+    N = int(p["v"].size)
+
+    def arr(name, dt=dtype):
+        x = p.get(name)
+        return None if x is None else np.ascontiguousarray(x, dtype=dt)
+
+    keep = {k: arr(k) for k in ("g_right", "g_left", "scale", "cm_inv", "field", "gnabar",
+                                  "gkbar", "gl", "el", "ve_amp", "ve_delay", "ve_pw",
+                                  "in_amp", "in_delay", "in_pw")}
+    for k in ("in_idx", "rec_idx"):
+        keep[k] = arr(k, np.int32)
+    tg = np.ascontiguousarray(trace_grad, dtype=dtype)
+    assert tg.shape == (B, 1 + n_steps // rec_every)
+    out = {k: np.zeros(N, dtype=dtype) for k in ("lam_v", "lam_m", "lam_h", "lam_n", "g_gnabar",
+                                                  "g_gkbar", "g_gl", "g_axial")}
+    cable_ptr = np.ascontiguousarray(p["cable_ptr"], dtype=np.int64)
+    getattr(lib(), "orc_cable_grad" + sfx)(
+        B, int(n_steps), int(rec_every), _ptr(cable_ptr),
+        _ptr(p["v"]), _ptr(p["m"]), _ptr(p["h"]), _ptr(p["n"]),
+        _ptr(keep["g_right"]), _ptr(keep["g_left"]), _ptr(keep["scale"]),
+        _ptr(keep["cm_inv"]), _ptr(keep["field"]), _ptr(keep["gnabar"]),
+        _ptr(keep["gkbar"]), _ptr(keep["gl"]), _ptr(keep["el"]),
+        float(p["ena"]), float(p["ek"]), float(p["q10"]), float(p["dt_ms"]),
+        float(p["dt_s"]), float(t0_ms),
+        _ptr(keep["ve_amp"]), _ptr(keep["ve_delay"]), _ptr(keep["ve_pw"]),
+        _ptr(keep["in_idx"]), _ptr(keep["in_amp"]), _ptr(keep["in_delay"]),
+        _ptr(keep["in_pw"]), _ptr(keep["rec_idx"]), _ptr(tg), int(bool(gate_f32)),
+        *(_ptr(out[k]) for k in ("lam_v", "lam_m", "lam_h", "lam_n", "g_gnabar", "g_gkbar",
+                                  "g_gl", "g_axial")),
+    )
+    return out
 
 
 def net_run(pd: dict, n_steps: int):

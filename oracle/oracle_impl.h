@@ -226,10 +226,121 @@ static REAL F(rect)(double t0_ms, int32_t s, double dt_ms, REAL amp, REAL delay,
   return (t >= delay && t < stop) ? amp : (REAL)0;
 }
 
+/* Read-only description of a packed cable problem (mirrors dgb_cable_args). */
+typedef struct {
+  const int64_t* cable_ptr;
+  const REAL *g_right, *g_left, *scale, *cm_inv, *field;
+  const REAL *gnabar, *gkbar, *gl, *el;
+  REAL ena, ek, q10, dt, dt_s;
+  double dt_ms_d, t0_ms;
+  const REAL *ve_amp, *ve_delay, *ve_pw;
+  const int32_t* in_idx;
+  const REAL *in_amp, *in_delay, *in_pw;
+  int32_t gate_f32;
+} F(cable_prob);
+
+/* One backward-Euler step of cable c (the update of implicit.py:569-664 after
+   the gate advance of integrators/core.py:769-834).  w: 10*kmax workspace. */
+static void F(cable_step)(const F(cable_prob)* P, int32_t c, int32_t s, REAL* vv, REAL* mm,
+                          REAL* hh, REAL* nn, REAL* w, int64_t kmax) {
+  const int64_t o = P->cable_ptr[c];
+  const int64_t K = P->cable_ptr[c + 1] - o;
+  const REAL *g_right = P->g_right, *g_left = P->g_left, *scale = P->scale;
+  REAL* lower = w;
+  REAL* mainv = w + kmax;
+  REAL* upper = w + 2 * kmax;
+  REAL* rhs = w + 3 * kmax;
+  REAL* x = w + 4 * kmax;
+  REAL* fn = w + 5 * kmax;
+  REAL* G = w + 6 * kmax;
+  REAL* ve = w + 7 * kmax;
+  REAL* work = w + 8 * kmax;
+  const REAL dt = P->dt, dt_s = P->dt_s;
+  /* stimulus time of this step: binary64 grid cast to the state dtype */
+  const int use_ve = P->field && P->ve_amp;
+  if (use_ve) {
+    REAL I = F(rect)(P->t0_ms, s, P->dt_ms_d, P->ve_amp[c], P->ve_delay[c], P->ve_pw[c],
+                     P->gate_f32);
+    for (int64_t i = 0; i < K; ++i) ve[i] = P->field[o + i] * I;
+  }
+  for (int64_t i = 0; i < K; ++i) {
+    REAL vi = vv[i];
+    REAL r[6];
+    F(orc_hh_rates)(vi, P->q10, r);
+    mm[i] = F(orc_cnexp)(mm[i], r[0], r[1], dt);
+    hh[i] = F(orc_cnexp)(hh[i], r[2], r[3], dt);
+    nn[i] = F(orc_cnexp)(nn[i], r[4], r[5], dt);
+    REAL m3 = mm[i] * mm[i] * mm[i];
+    REAL n4 = (nn[i] * nn[i]) * (nn[i] * nn[i]);
+    REAL gna = P->gnabar[o + i] * m3 * hh[i];
+    REAL gk = P->gkbar[o + i] * n4;
+    REAL Gi = P->gl[o + i] + gna + gk;
+    REAL Ji = P->gl[o + i] * P->el[o + i] + gna * P->ena + gk * P->ek;
+    G[i] = Gi;
+    fn[i] = (Ji - Gi * vi) * scale[o + i];
+  }
+  if (K > 1) {
+    for (int64_t i = 0; i < K; ++i) {
+      REAL ax = (REAL)0;
+      if (i == 0) {
+        ax = g_right[o] * (vv[1] - vv[0]);
+      } else if (i == K - 1) {
+        ax = -(g_left[o + i] * (vv[i] - vv[i - 1]));
+      } else {
+        ax = g_right[o + i] * (vv[i + 1] - vv[i]) - g_left[o + i] * (vv[i] - vv[i - 1]);
+      }
+      fn[i] = fn[i] + ax;
+    }
+    if (use_ve) {
+      for (int64_t i = 0; i < K; ++i) {
+        REAL ex;
+        if (i == 0) {
+          ex = g_right[o] * (ve[1] - ve[0]);
+        } else if (i == K - 1) {
+          ex = -(g_left[o + i] * (ve[i] - ve[i - 1]));
+        } else {
+          ex = g_right[o + i] * (ve[i + 1] - ve[i]) - g_left[o + i] * (ve[i] - ve[i - 1]);
+        }
+        fn[i] = fn[i] + ex;
+      }
+    }
+  }
+  if (P->in_idx && P->in_amp && P->in_idx[c] >= 0) {
+    int32_t ii = P->in_idx[c];
+    REAL I = F(rect)(P->t0_ms, s, P->dt_ms_d, P->in_amp[c], P->in_delay[c], P->in_pw[c],
+                     P->gate_f32);
+    for (int64_t i = 0; i < K; ++i) {
+      REAL inj = (i == ii) ? I : (REAL)0;
+      fn[i] = fn[i] + inj * P->cm_inv[o + i];
+    }
+  }
+  for (int64_t i = 0; i < K; ++i) {
+    REAL diag_base = -g_right[o + i] + -g_left[o + i];
+    rhs[i] = dt_s * fn[i];
+    mainv[i] = (REAL)1 - dt_s * (diag_base - G[i] * scale[o + i]);
+    if (i < K - 1) upper[i] = -dt_s * g_right[o + i];
+    if (i > 0) lower[i - 1] = -dt_s * g_left[o + i];
+  }
+  if (K == 1) {
+    x[0] = rhs[0] / mainv[0];
+  } else {
+    F(orc_thomas)(K, lower, mainv, upper, rhs, x, work);
+  }
+  for (int64_t i = 0; i < K; ++i) vv[i] = vv[i] + x[i];
+}
+
+static int64_t F(max_cable)(int32_t n_cables, const int64_t* cable_ptr) {
+  int64_t kmax = 1;
+  for (int32_t c = 0; c < n_cables; ++c) {
+    int64_t K = cable_ptr[c + 1] - cable_ptr[c];
+    if (K > kmax) kmax = K;
+  }
+  return kmax;
+}
+
 /*
- * Multi-step backward-Euler HH cable run (the per-step update of
- * implicit.py:569-664 after the gate advance of integrators/core.py:769-834),
- * all cables packed by cable_ptr.  Arguments mirror dgb_cable_args.
+ * Multi-step backward-Euler HH cable run, all cables packed by cable_ptr.
+ * Arguments mirror dgb_cable_args.
  */
 void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
                       const int64_t* cable_ptr, REAL* v, REAL* m, REAL* h, REAL* n,
@@ -243,108 +354,27 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
                       REAL* trace, const int32_t* spk_idx, double spk_thr_d,
                       int32_t* spk_below, int32_t* spk_count, int32_t* spk_first,
                       int32_t gate_f32, const int32_t* spk_idx2, int32_t* spk_below2) {
-  const REAL ena = (REAL)ena_d, ek = (REAL)ek_d, q10 = (REAL)q10_d;
-  const REAL dt = (REAL)dt_ms_d, dt_s = (REAL)dt_s_d, thr = (REAL)spk_thr_d;
+  const F(cable_prob) P = {cable_ptr, g_right, g_left, scale, cm_inv, field, gnabar, gkbar, gl,
+                           el, (REAL)ena_d, (REAL)ek_d, (REAL)q10_d, (REAL)dt_ms_d,
+                           (REAL)dt_s_d, dt_ms_d, t0_ms, ve_amp, ve_delay, ve_pw, in_idx,
+                           in_amp, in_delay, in_pw, gate_f32};
+  const REAL thr = (REAL)spk_thr_d;
   const int64_t n_rec = 1 + (int64_t)n_steps / (rec_every > 0 ? rec_every : 1);
-  int64_t kmax = 1;
-  for (int32_t c = 0; c < n_cables; ++c) {
-    int64_t K = cable_ptr[c + 1] - cable_ptr[c];
-    if (K > kmax) kmax = K;
-  }
+  const int64_t kmax = F(max_cable)(n_cables, cable_ptr);
 #pragma omp parallel
   {
     REAL* w = (REAL*)malloc(sizeof(REAL) * 10 * (size_t)kmax);
 #pragma omp for schedule(dynamic, 1)
     for (int32_t c = 0; c < n_cables; ++c) {
       const int64_t o = cable_ptr[c];
-      const int64_t K = cable_ptr[c + 1] - o;
       REAL* vv = v + o;
       REAL *mm = m + o, *hh = h + o, *nn = n + o;
-      REAL* lower = w;
-      REAL* mainv = w + kmax;
-      REAL* upper = w + 2 * kmax;
-      REAL* rhs = w + 3 * kmax;
-      REAL* x = w + 4 * kmax;
-      REAL* fn = w + 5 * kmax;
-      REAL* G = w + 6 * kmax;
-      REAL* ve = w + 7 * kmax;
-      REAL* work = w + 8 * kmax;
       const int32_t ri = rec_idx ? rec_idx[c] : -1;
       const int32_t si = spk_idx ? spk_idx[c] : -1;
       const int32_t si2 = spk_idx2 ? spk_idx2[c] : -1;
       if (trace && ri >= 0) trace[(int64_t)c * n_rec] = vv[ri];
       for (int32_t s = 0; s < n_steps; ++s) {
-        /* stimulus time of this step: binary64 grid cast to the state dtype */
-        REAL ve_i = (REAL)0;
-        const int use_ve = field && ve_amp;
-        if (use_ve) {
-          REAL I = F(rect)(t0_ms, s, dt_ms_d, ve_amp[c], ve_delay[c], ve_pw[c], gate_f32);
-          for (int64_t i = 0; i < K; ++i) ve[i] = field[o + i] * I;
-        }
-        (void)ve_i;
-        for (int64_t i = 0; i < K; ++i) {
-          REAL vi = vv[i];
-          REAL r[6];
-          F(orc_hh_rates)(vi, q10, r);
-          mm[i] = F(orc_cnexp)(mm[i], r[0], r[1], dt);
-          hh[i] = F(orc_cnexp)(hh[i], r[2], r[3], dt);
-          nn[i] = F(orc_cnexp)(nn[i], r[4], r[5], dt);
-          REAL m3 = mm[i] * mm[i] * mm[i];
-          REAL n4 = (nn[i] * nn[i]) * (nn[i] * nn[i]);
-          REAL gna = gnabar[o + i] * m3 * hh[i];
-          REAL gk = gkbar[o + i] * n4;
-          REAL Gi = gl[o + i] + gna + gk;
-          REAL Ji = gl[o + i] * el[o + i] + gna * ena + gk * ek;
-          G[i] = Gi;
-          fn[i] = (Ji - Gi * vi) * scale[o + i];
-        }
-        if (K > 1) {
-          for (int64_t i = 0; i < K; ++i) {
-            REAL ax = (REAL)0;
-            if (i == 0) {
-              ax = g_right[o] * (vv[1] - vv[0]);
-            } else if (i == K - 1) {
-              ax = -(g_left[o + i] * (vv[i] - vv[i - 1]));
-            } else {
-              ax = g_right[o + i] * (vv[i + 1] - vv[i]) - g_left[o + i] * (vv[i] - vv[i - 1]);
-            }
-            fn[i] = fn[i] + ax;
-          }
-          if (use_ve) {
-            for (int64_t i = 0; i < K; ++i) {
-              REAL ex;
-              if (i == 0) {
-                ex = g_right[o] * (ve[1] - ve[0]);
-              } else if (i == K - 1) {
-                ex = -(g_left[o + i] * (ve[i] - ve[i - 1]));
-              } else {
-                ex = g_right[o + i] * (ve[i + 1] - ve[i]) - g_left[o + i] * (ve[i] - ve[i - 1]);
-              }
-              fn[i] = fn[i] + ex;
-            }
-          }
-        }
-        if (in_idx && in_amp && in_idx[c] >= 0) {
-          int32_t ii = in_idx[c];
-          REAL I = F(rect)(t0_ms, s, dt_ms_d, in_amp[c], in_delay[c], in_pw[c], gate_f32);
-          for (int64_t i = 0; i < K; ++i) {
-            REAL inj = (i == ii) ? I : (REAL)0;
-            fn[i] = fn[i] + inj * cm_inv[o + i];
-          }
-        }
-        for (int64_t i = 0; i < K; ++i) {
-          REAL diag_base = -g_right[o + i] + -g_left[o + i];
-          rhs[i] = dt_s * fn[i];
-          mainv[i] = (REAL)1 - dt_s * (diag_base - G[i] * scale[o + i]);
-          if (i < K - 1) upper[i] = -dt_s * g_right[o + i];
-          if (i > 0) lower[i - 1] = -dt_s * g_left[o + i];
-        }
-        if (K == 1) {
-          x[0] = rhs[0] / mainv[0];
-        } else {
-          F(orc_thomas)(K, lower, mainv, upper, rhs, x, work);
-        }
-        for (int64_t i = 0; i < K; ++i) vv[i] = vv[i] + x[i];
+        F(cable_step)(&P, c, s, vv, mm, hh, nn, w, kmax);
         if (si >= 0) {
           /* a rising edge at either detection compartment counts once */
           int above = vv[si] >= thr;
@@ -364,6 +394,234 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
           trace[(int64_t)c * n_rec + (s + 1) / rec_every] = vv[ri];
       }
     }
+    free(w);
+  }
+}
+
+/* ---- reverse mode -------------------------------------------------------
+ * Derivatives of the gate advance on the branch the forward takes (the same
+ * branch tests as orc_vtrap, orc_phi1 and orc_cnexp).  The reference obtains
+ * them by torch autograd through those operations. */
+
+/* d/du of the even series (u = q^2). */
+static REAL F(even_series_du)(REAL q) {
+  REAL u = q * q;
+  REAL value;
+  if (IS_F64) {
+    value = u * (REAL)(8.0 * 43867.0 / 5109094217170944000.0)
+            - (REAL)(7.0 * 3617.0 / 10670622842880000.0);
+    value = value * u + (REAL)(6.0 / 74724249600.0);
+    value = value * u - (REAL)(5.0 * 691.0 / 1307674368000.0);
+    value = value * u + (REAL)(4.0 / 47900160.0);
+  } else {
+    value = u * (REAL)(-5.0 * 691.0 / 1307674368000.0) + (REAL)(4.0 / 47900160.0);
+  }
+  value = value * u - (REAL)(3.0 / 1209600.0);
+  value = value * u + (REAL)(2.0 / 30240.0);
+  value = value * u - (REAL)(1.0 / 720.0);
+  return value;
+}
+
+static REAL F(vtrap_dx)(REAL x, REAL y) {
+  REAL q = x / y;
+  REAL thr = IS_F64 ? (REAL)0.5 : (REAL)1.0;
+  if (FABS(q) <= thr) {
+    REAL u = q * q;
+    return (REAL)-0.5 + (REAL)2 * q * F(even_series)(q) + (REAL)2 * q * u * F(even_series_du)(q);
+  }
+  REAL e = EXP(q);
+  REAL em1 = e - (REAL)1;
+  return (em1 - x * e / y) / (em1 * em1);
+}
+
+/* d/dz of the phi1 Taylor polynomial: sum_k k z^(k-1) / (k+1)!. */
+static REAL F(phi1_dz)(REAL z) {
+  const int N = IS_F64 ? 16 : 9;
+  double inv[18];
+  inv[0] = 1.0;
+  for (int k = 1; k <= 17; ++k) inv[k] = inv[k - 1] / (double)k; /* 1/k! */
+  REAL value = (REAL)(N * inv[N + 1]);
+  for (int k = N - 1; k >= 1; --k) value = value * z + (REAL)(k * inv[k + 1]);
+  return value;
+}
+
+/* x' = cnexp(x, a, b, dt) with dx'/dx, dx'/da, dx'/db. */
+static REAL F(cnexp_d)(REAL x, REAL a, REAL b, REAL dt, REAL* dx, REAL* da, REAL* db) {
+  REAL rate = a - b * x;
+  REAL coef = -b;
+  REAL z = coef * dt;
+  if (FABS(z) <= (REAL)0.5) {
+    REAL ph = F(orc_phi1)(z);
+    *dx = (REAL)1 - dt * b * ph;
+    *da = dt * ph;
+    *db = dt * (-x) * ph - dt * rate * F(phi1_dz)(z) * dt;
+    return x + dt * rate * ph;
+  }
+  REAL E = EXP(z);
+  REAL eq = -a / coef;
+  *dx = E;
+  *da = ((REAL)1 - E) / b;
+  *db = -(a / (b * b)) * ((REAL)1 - E) - (x - eq) * E * dt;
+  return eq + (x - eq) * E;
+}
+
+/* Gate advance at v with partials d(new)/d(old) (dg[0..2]) and d(new)/dv (dg[3..5]). */
+static void F(gates_d)(REAL v, REAL q10, REAL dt, REAL* mhn, REAL* dg) {
+  REAL xm = -(v + (REAL)40), xn = -(v + (REAL)55);
+  REAL alpha_m = AM1 * F(orc_vtrap)(xm, (REAL)10);
+  REAL beta_m = (REAL)4.0 * EXP(-(v + (REAL)65) / (REAL)18);
+  REAL alpha_h = AH1 * EXP(-(v + (REAL)65) / (REAL)20);
+  REAL eh = EXP(-(v + (REAL)35) / (REAL)10);
+  REAL beta_h = (REAL)1.0 / (eh + (REAL)1);
+  REAL alpha_n = AN1 * F(orc_vtrap)(xn, (REAL)10);
+  REAL beta_n = (REAL)0.125 * EXP(-(v + (REAL)65) / (REAL)80);
+  REAL d_am = -AM1 * F(vtrap_dx)(xm, (REAL)10), d_bm = -beta_m / (REAL)18;
+  REAL d_ah = -alpha_h / (REAL)20, d_bh = eh / ((REAL)10 * (eh + (REAL)1) * (eh + (REAL)1));
+  REAL d_an = -AN1 * F(vtrap_dx)(xn, (REAL)10), d_bn = -beta_n / (REAL)80;
+  REAL a[3] = {q10 * alpha_m, q10 * alpha_h, q10 * alpha_n};
+  REAL b[3] = {q10 * (alpha_m + beta_m), q10 * (alpha_h + beta_h), q10 * (alpha_n + beta_n)};
+  REAL da_v[3] = {q10 * d_am, q10 * d_ah, q10 * d_an};
+  REAL db_v[3] = {q10 * (d_am + d_bm), q10 * (d_ah + d_bh), q10 * (d_an + d_bn)};
+  for (int k = 0; k < 3; ++k) {
+    REAL dx, da, db;
+    mhn[k] = F(cnexp_d)(mhn[k], a[k], b[k], dt, &dx, &da, &db);
+    dg[k] = dx;
+    dg[3 + k] = da * da_v[k] + db * db_v[k];
+  }
+}
+
+/*
+ * Gradient of a recorded trace functional: runs the forward of orc_cable_run
+ * keeping the whole state tape in memory, then the reverse sweep.
+ *   trace_grad: (n_cables, n_rec) dLoss/dtrace for the trace orc_cable_run
+ *               records with the same arguments.
+ *   out: lam_v/m/h/n (n_comp) adjoint of the initial state; g_gna, g_gk, g_gl
+ *        (n_comp) dLoss/d(gnabar, gkbar, gl); g_ax (n_comp) lam_g * g over
+ *        both axial bands of each row.  v/m/h/n are left at the final state.
+ */
+void F(orc_cable_grad)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
+                       const int64_t* cable_ptr, REAL* v, REAL* m, REAL* h, REAL* n,
+                       const REAL* g_right, const REAL* g_left, const REAL* scale,
+                       const REAL* cm_inv, const REAL* field, const REAL* gnabar,
+                       const REAL* gkbar, const REAL* gl, const REAL* el, double ena_d,
+                       double ek_d, double q10_d, double dt_ms_d, double dt_s_d,
+                       double t0_ms, const REAL* ve_amp, const REAL* ve_delay,
+                       const REAL* ve_pw, const int32_t* in_idx, const REAL* in_amp,
+                       const REAL* in_delay, const REAL* in_pw, const int32_t* rec_idx,
+                       const REAL* trace_grad, int32_t gate_f32, REAL* lam_v, REAL* lam_m,
+                       REAL* lam_h, REAL* lam_n, REAL* g_gna, REAL* g_gk, REAL* g_gl,
+                       REAL* g_ax) {
+  const F(cable_prob) P = {cable_ptr, g_right, g_left, scale, cm_inv, field, gnabar, gkbar, gl,
+                           el, (REAL)ena_d, (REAL)ek_d, (REAL)q10_d, (REAL)dt_ms_d,
+                           (REAL)dt_s_d, dt_ms_d, t0_ms, ve_amp, ve_delay, ve_pw, in_idx,
+                           in_amp, in_delay, in_pw, gate_f32};
+  const REAL dt = P.dt, dt_s = P.dt_s, ena = P.ena, ek = P.ek;
+  const int64_t n_rec = 1 + (int64_t)n_steps / (rec_every > 0 ? rec_every : 1);
+  const int64_t kmax = F(max_cable)(n_cables, cable_ptr);
+#pragma omp parallel
+  {
+    REAL* w = (REAL*)malloc(sizeof(REAL) * 20 * (size_t)kmax);
+    REAL* tape = (REAL*)malloc(sizeof(REAL) * 4 * (size_t)kmax * ((size_t)n_steps + 1));
+#pragma omp for schedule(dynamic, 1)
+    for (int32_t c = 0; c < n_cables; ++c) {
+      const int64_t o = cable_ptr[c];
+      const int64_t K = cable_ptr[c + 1] - o;
+      REAL *vv = v + o, *mm = m + o, *hh = h + o, *nn = n + o;
+      for (int32_t s = 0; s <= n_steps; ++s) {
+        REAL* t = tape + (size_t)s * 4 * K;
+        if (s > 0) F(cable_step)(&P, c, s - 1, vv, mm, hh, nn, w, kmax);
+        for (int64_t i = 0; i < K; ++i) {
+          t[i] = vv[i];
+          t[K + i] = mm[i];
+          t[2 * K + i] = hh[i];
+          t[3 * K + i] = nn[i];
+        }
+      }
+      REAL *lv = lam_v + o, *lm = lam_m + o, *lh = lam_h + o, *ln = lam_n + o;
+      REAL *gga = g_gna + o, *ggk = g_gk + o, *ggl = g_gl + o;
+      REAL* gax = g_ax + o;
+      for (int64_t i = 0; i < K; ++i)
+        lv[i] = lm[i] = lh[i] = ln[i] = gga[i] = ggk[i] = ggl[i] = gax[i] = 0;
+      REAL *mu = w, *bb = w + kmax, *lo = w + 2 * kmax, *up = w + 3 * kmax, *G = w + 4 * kmax;
+      REAL *gm = w + 5 * kmax, *gh = w + 6 * kmax, *gn = w + 7 * kmax, *dg = w + 8 * kmax;
+      REAL *ve = w + 14 * kmax, *work = w + 15 * kmax, *lfn = w + 17 * kmax;
+      const int32_t ri = rec_idx ? rec_idx[c] : -1;
+      const int use_ve = field && ve_amp;
+      for (int32_t s = n_steps - 1; s >= 0; --s) {
+        const REAL* t = tape + (size_t)s * 4 * K;
+        const REAL* vn = tape + (size_t)(s + 1) * 4 * K;
+        if (trace_grad && ri >= 0 && ((s + 1) % rec_every) == 0)
+          lv[ri] += trace_grad[(int64_t)c * n_rec + (s + 1) / rec_every];
+        REAL I = 0;
+        if (use_ve) {
+          I = F(rect)(t0_ms, s, dt_ms_d, ve_amp[c], ve_delay[c], ve_pw[c], gate_f32);
+          for (int64_t i = 0; i < K; ++i) ve[i] = field[o + i] * I;
+        }
+        for (int64_t i = 0; i < K; ++i) {
+          REAL mhn[3] = {t[K + i], t[2 * K + i], t[3 * K + i]};
+          REAL d6[6];
+          F(gates_d)(t[i], P.q10, dt, mhn, d6);
+          gm[i] = mhn[0];
+          gh[i] = mhn[1];
+          gn[i] = mhn[2];
+          for (int k = 0; k < 6; ++k) dg[k * kmax + i] = d6[k];
+          REAL m3 = mhn[0] * mhn[0] * mhn[0];
+          REAL n4 = (mhn[2] * mhn[2]) * (mhn[2] * mhn[2]);
+          G[i] = gl[o + i] + gnabar[o + i] * m3 * mhn[1] + gkbar[o + i] * n4;
+          bb[i] = (REAL)1 - dt_s * ((-g_right[o + i] + -g_left[o + i]) - G[i] * scale[o + i]);
+        }
+        /* transposed bands: row i couples to i-1 through the forward's upper
+           band of row i-1 and to i+1 through the lower band of row i+1 */
+        for (int64_t i = 0; i + 1 < K; ++i) {
+          lo[i] = -dt_s * g_right[o + i];
+          up[i] = -dt_s * g_left[o + i + 1];
+        }
+        if (K == 1) {
+          mu[0] = lv[0] / bb[0];
+        } else {
+          F(orc_thomas)(K, lo, bb, up, lv, mu, work);
+        }
+        for (int64_t i = 0; i < K; ++i) lfn[i] = dt_s * mu[i];
+        for (int64_t i = 0; i < K; ++i) {
+          const REAL vi = t[i];
+          const REAL x = vn[i] - vi;
+          const REAL v_p = i > 0 ? t[i - 1] : (REAL)0, v_n = i + 1 < K ? t[i + 1] : (REAL)0;
+          const REAL x_p = i > 0 ? vn[i - 1] - v_p : (REAL)0;
+          const REAL x_n = i + 1 < K ? vn[i + 1] - v_n : (REAL)0;
+          const REAL gr = g_right[o + i], glf = g_left[o + i], scl = scale[o + i];
+          REAL dvr = v_n - vi, dvl = vi - v_p;
+          if (use_ve) {
+            const REAL ve_l = i > 0 ? ve[i - 1] : (REAL)0, ve_r = i + 1 < K ? ve[i + 1] : (REAL)0;
+            dvr = dvr + (ve_r - ve[i]);
+            dvl = dvl + (ve[i] - ve_l);
+          }
+          const REAL lb = -mu[i] * x, la = -mu[i] * x_p, lc = -mu[i] * x_n;
+          const REAL lgr = dt_s * (lb - lc) + dvr * lfn[i];
+          const REAL lglf = dt_s * (lb - la) - dvl * lfn[i];
+          gax[i] += lgr * gr + lglf * glf;
+          const REAL lG = dt_s * scl * lb - vi * scl * lfn[i];
+          const REAL lJ = scl * lfn[i];
+          const REAL mq = gm[i], hq = gh[i], nq = gn[i];
+          const REAL lgna = lG + ena * lJ, lgk = lG + ek * lJ;
+          gga[i] += mq * mq * mq * hq * lgna;
+          ggk[i] += (nq * nq) * (nq * nq) * lgk;
+          ggl[i] += lG + el[o + i] * lJ;
+          const REAL lmq = lm[i] + (REAL)3 * gnabar[o + i] * mq * mq * hq * lgna;
+          const REAL lhq = lh[i] + gnabar[o + i] * mq * mq * mq * lgna;
+          const REAL lnq = ln[i] + (REAL)4 * gkbar[o + i] * nq * nq * nq * lgk;
+          REAL lvi = lv[i] - (G[i] * scl + gr + glf) * lfn[i];
+          if (i > 0) lvi += g_right[o + i - 1] * lfn[i - 1];
+          if (i + 1 < K) lvi += g_left[o + i + 1] * lfn[i + 1];
+          lvi += dg[3 * kmax + i] * lmq + dg[4 * kmax + i] * lhq + dg[5 * kmax + i] * lnq;
+          lm[i] = dg[i] * lmq;
+          lh[i] = dg[kmax + i] * lhq;
+          ln[i] = dg[2 * kmax + i] * lnq;
+          lv[i] = lvi;
+        }
+      }
+      if (trace_grad && ri >= 0) lv[ri] += trace_grad[(int64_t)c * n_rec];
+    }
+    free(tape);
     free(w);
   }
 }

@@ -133,3 +133,43 @@ def oracle_thresholds(pop, lb, ub, n_steps, rtol=0.01, max_fix=10, max_tries=25,
     ub[ignore] = np.nan
     lb[ignore] = np.nan
     return ub, lb
+
+
+def golden_adjoint_population(g, dtype, device="cpu", params="guess", **kw):
+    """The single-cable reference models of adjoint_f64.npz packed as one population
+    (per-cable gnabar, gkbar, gl and Ra at the fixture's guess or hidden values)."""
+    B, K = int(g["amp_ma"].size), int(g["K"])
+    prm = {k: g[f"{params}_{k}"] for k in ("gnabar", "gkbar", "gl", "rhoa")}
+    pop = CablePopulation([K] * B, float(g["diam"]), float(g["dx"]),
+                          rhoa=torch.as_tensor(prm["rhoa"]), celsius=float(g["celsius"]),
+                          v_init=float(g["v_init"]), dtype=dtype, device=device,
+                          hh={k: torch.as_tensor(prm[k]) for k in ("gnabar", "gkbar", "gl")},
+                          **kw)
+    pop.inject(int(g["comp"]), torch.as_tensor(g["amp_ma"]), float(g["delay"]), float(g["pw"]))
+    return pop.initialize(float(g["dt"]))
+
+
+def mse_trace_grad(trace, target):
+    """dLoss/dtrace of Loss = sum over cables of mean over samples of (trace - target)^2."""
+    return 2.0 * (trace - target) / trace.shape[1]
+
+
+def oracle_param_grads(p, steps, target, rec_idx=0):
+    """Per-cable (gnabar, gkbar, gl, Ra) gradients of the MSE trace loss by the oracle.
+
+    Returns (trace, loss per cable, dict of per-cable gradients, raw cable_grad output)."""
+    import oracle
+
+    B = int(p["cable_ptr"].size - 1)
+    q = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in p.items()}
+    q["rec_idx"] = np.full(B, rec_idx, dtype=np.int32)
+    trace, *_ = oracle.cable_run({k: (v.copy() if isinstance(v, np.ndarray) else v)
+                                  for k, v in q.items()}, steps)
+    loss = ((trace - target) ** 2).mean(axis=1)
+    raw = oracle.cable_grad(q, steps, mse_trace_grad(trace, target))
+    counts = np.diff(p["cable_ptr"])
+    cab = np.repeat(np.arange(B), counts)
+    grads = {k: np.bincount(cab, raw["g_" + k], minlength=B) for k in ("gnabar", "gkbar", "gl")}
+    axial = np.bincount(cab, raw["g_axial"], minlength=B)
+    grads["rhoa"] = -axial / p["rhoa_per_cable"] if "rhoa_per_cable" in p else None
+    return trace, loss, grads, raw

@@ -14,6 +14,8 @@ compatibility shims) and records its outputs on seeded inputs:
                            dense-matrix solve of the reference's DHS parity test
   events.npz               dense_fixed_delay_transition ring sequence, Exp2Syn
                            factor and the NetCon delay-rounding known answers
+  adjoint_f64.npz          reference autograd gradients (gnabar, gkbar, gl, Ra) of
+                           a somatic-trace MSE through the CPU cable update
 
 Usage (in a container that holds the reference source):
 
@@ -267,8 +269,72 @@ def events():
     print("events")
 
 
+def adjoint():
+    """Reference autograd gradients of a somatic-trace MSE w.r.t. gnabar, gkbar,
+    gl and Ra: one single-cable float64 model per cable (the reference's HH
+    parameters are scalars per model), Unmyelinated(L=100, dx=10) -> K=11,
+    somatic current clamp, 400 steps of 0.025 ms.  Targets come from the same
+    model at hidden parameters (defaults x U[0.7, 1.3]); the gradient is taken
+    at the defaults, through the reference's CPU path (pcr_solve_t)."""
+    dn = _ref()
+    from dendra.models.mod import hh
+
+    steps, dt, K = 400, 0.025, 11
+    amp_na = np.array([0.3, 0.2, 0.15])
+    rng = np.random.default_rng(77)
+    defaults = dict(gnabar=0.12, gkbar=0.036, gl=0.0003, rhoa=100.0)
+    hidden = {k: (v * rng.uniform(0.7, 1.3, amp_na.size)).astype(np.float32).astype(np.float64)
+              for k, v in defaults.items()}
+    guess = {k: np.full(amp_na.size, float(np.float32(v))) for k, v in defaults.items()}
+
+    def model_run(i, prm, grad):
+        with dn.ctx(JIT=0, REQUIRE_GRAD=1 if grad else 0):
+            model = dn.Unmyelinated([1.0], L=100.0, dx=10.0, celsius=6.3, v_init=-65.0,
+                                    dtype=torch.float64, integrator=dn.bwd_euler_ub(),
+                                    rhoa=float(prm["rhoa"][i]))
+            model.insert(hh)
+            amp = torch.tensor([[amp_na[i] * 1e-6]], dtype=torch.float64)
+            model[..., 0].inject(dn.mono_rect(amp=amp, delay=1.0, pw=1.0))
+            model.initialize()
+            if grad:
+                model.train()
+            mech = model.mech.hh
+            with torch.no_grad():
+                mech.gnabar_param.fill_(float(prm["gnabar"][i]))
+                mech.gkbar_param.fill_(float(prm["gkbar"][i]))
+                mech.gl_param.fill_(float(prm["gl"][i]))
+            rec = dn.Recorder(("v",))
+            model.run(dt=dt, duration=steps * dt, callbacks=[rec])
+            v0 = torch.stack([x.reshape(-1)[0] for x in rec.rec["v"]])
+        return model, v0
+
+    targets, traces, loss, grads = [], [], [], {k: [] for k in defaults}
+    for i in range(amp_na.size):
+        _, tgt = model_run(i, hidden, False)
+        model, v0 = model_run(i, guess, True)
+        L = ((v0 - tgt.detach()) ** 2).sum() / (steps + 1)
+        named = dict(model.named_parameters())
+        keys = {"gnabar": "integrator.mech.mechanisms.hh.gnabar_param",
+                "gkbar": "integrator.mech.mechanisms.hh.gkbar_param",
+                "gl": "integrator.mech.mechanisms.hh.gl_param", "rhoa": "rhoa_param"}
+        g = torch.autograd.grad(L, [named[keys[k]] for k in defaults])
+        for k, gk in zip(defaults, g):
+            grads[k].append(float(gk))
+        targets.append(tgt.detach().numpy())
+        traces.append(v0.detach().numpy())
+        loss.append(float(L))
+    out = dict(K=K, steps=steps, dt=dt, diam=1.0, dx=10.0, celsius=6.3, v_init=-65.0,
+               amp_ma=amp_na * 1e-6, delay=1.0, pw=1.0, comp=0,
+               target=np.stack(targets), trace=np.stack(traces), loss=np.array(loss),
+               **{f"hidden_{k}": v for k, v in hidden.items()},
+               **{f"guess_{k}": v for k, v in guess.items()},
+               **{f"grad_{k}": np.array(v) for k, v in grads.items()})
+    np.savez_compressed(os.path.join(HERE, "adjoint_f64.npz"), **out)
+    print("adjoint", out["loss"], {k: out["grad_" + k] for k in defaults})
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["rates", "tridiag", "dhs", "events", "cable", "extra"]
+    what = sys.argv[1:] or ["rates", "tridiag", "dhs", "events", "cable", "extra", "adjoint"]
     if "rates" in what:
         rates()
     if "tridiag" in what:
@@ -283,3 +349,5 @@ if __name__ == "__main__":
     if "extra" in what:
         hh_extra(torch.float64, "f64")
         hh_extra(torch.float32, "f32")
+    if "adjoint" in what:
+        adjoint()

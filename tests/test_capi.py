@@ -47,6 +47,11 @@ def test_cable_args_mirror_matches_c_layout():
     assert L.dgb_cable_args_size() == ctypes.sizeof(_lib.CableArgs)
 
 
+def test_cable_adjoint_args_mirror_matches_c_layout():
+    L = dendra_gb300.load()
+    assert L.dgb_cable_adjoint_args_size() == ctypes.sizeof(_lib.CableAdjointArgs)
+
+
 def test_net_args_mirror_matches_c_layout():
     from dendra_gb300.network import NetArgs
 
@@ -72,3 +77,25 @@ def test_argument_errors_are_reported_without_touching_a_device():
     assert L.dgb_cable_run(ctypes.byref(args), None) == -1
     with pytest.raises(ValueError):
         _lib.check(-1, "probe")
+
+
+def test_taped_run_and_adjoint_reject_bad_arguments_on_the_host():
+    """Validation happens before any device work (the pointers are never read)."""
+    L = dendra_gb300.load()
+    a = _lib.CableArgs()
+    a.dtype, a.n_cables, a.n_steps, a.rec_every, a.max_k, a.n_comp = 0, 1, 4, 1, 11, 11
+    for name in ("cable_ptr", "v", "m", "h", "n", "g_right", "g_left", "scale", "cm_inv",
+                 "gnabar", "gkbar", "gl", "el", "scratch"):
+        setattr(a, name, 4096)
+    a.flags = _lib.CABLE_FAST_MATH
+    assert L.dgb_cable_run_taped(ctypes.byref(a), 4096, None) == -1
+    assert b"not accepted" in L.dgb_last_error()
+    a.flags = _lib.CABLE_STOP_ON_SPIKE
+    adj = _lib.CableAdjointArgs()
+    assert L.dgb_cable_adjoint(ctypes.byref(a), ctypes.byref(adj), None) == -1
+    a.flags = 0
+    assert L.dgb_cable_adjoint(ctypes.byref(a), ctypes.byref(adj), None) == -1
+    assert b"tape" in L.dgb_last_error()
+    adj.tape = 4096
+    assert L.dgb_cable_adjoint(ctypes.byref(a), ctypes.byref(adj), None) == -1
+    assert b"lam_v" in L.dgb_last_error()
