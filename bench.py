@@ -349,12 +349,12 @@ def bench_c4(args, world, rank, local):
     from dendra_gb300 import _lib
     L = _lib.load()
     args_f = run._args(steps, step0, work)
-    _lib.check(L.dgb_cable_run_taped(args_f, run._tape.data_ptr(), _lib.stream_ptr(dev)),
+    _lib.check(L.dgb_cable_run_taped(args_f, run._tapes[0].data_ptr(), _lib.stream_ptr(dev)),
                "dgb_cable_run_taped")
     adj = _lib.CableAdjointArgs()
     bufs = [torch.zeros(pop.N, device=dev) for _ in range(8)]
     gt = torch.zeros((pop.B, n_ts + 1), device=dev)
-    adj.tape, adj.trace_grad, adj.trace_len = run._tape.data_ptr(), gt.data_ptr(), n_ts + 1
+    adj.tape, adj.trace_grad, adj.trace_len = run._tapes[0].data_ptr(), gt.data_ptr(), n_ts + 1
     (adj.lam_v, adj.lam_m, adj.lam_h, adj.lam_n, adj.grad_gnabar, adj.grad_gkbar, adj.grad_gl,
      adj.grad_axial) = (b.data_ptr() for b in bufs)
     adj_ms = []

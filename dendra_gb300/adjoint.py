@@ -35,10 +35,13 @@ class CableGradient:
     pop: an initialized CablePopulation (its state is the initial state of
     every forward; it is not modified).  rec_idx: local compartment recorded
     per cable (int or per-cable sequence).  The trace has one sample per step,
-    (B, n_steps + 1), sample 0 being the initial state.
+    (B, n_steps + 1), sample 0 being the initial state.  overlap: recompute
+    the next segment on a side stream while the adjoint of the current one
+    runs (two tapes in memory instead of one).
     """
 
-    def __init__(self, pop: CablePopulation, n_steps: int, rec_idx=0, checkpoint_every=500):
+    def __init__(self, pop: CablePopulation, n_steps: int, rec_idx=0, checkpoint_every=500,
+                 overlap=True):
         if pop.dt is None:
             raise RuntimeError("Model must be initialized before running.")
         if pop.fast_math:
@@ -63,7 +66,11 @@ class CableGradient:
         self.rhoa0 = pop.rhoa.to(dev, torch.float64)[first]
         self.ra = self.rhoa0.clone()
         self.checkpoints = []
-        self._tape = None
+        self._tapes = []
+        self.overlap = bool(overlap)
+        if self.overlap:
+            self._side = torch.cuda.Stream(dev)
+            self._side_scratch = torch.zeros(4, dtype=torch.int32, device=dev)
 
     # -- parameters -------------------------------------------------------
     def set_params(self, gnabar=None, gkbar=None, gl=None, ra=None):
@@ -135,29 +142,68 @@ class CableGradient:
         gt = grad_trace.to(device=dev, dtype=pop.dtype).contiguous()
         if tuple(gt.shape) != (B, self.n_steps + 1):
             raise ValueError(f"grad_trace must be ({B}, {self.n_steps + 1})")
-        if self._tape is None or self._tape.dtype != pop.dtype:
-            self._tape = torch.empty((self.seg + 1, 4, N), dtype=pop.dtype, device=dev)
+        segs = self._segments()
+        nbuf = 2 if (self.overlap and len(segs) > 1) else 1
+        if len(self._tapes) != nbuf or self._tapes[0].dtype != pop.dtype:
+            self._tapes = [torch.empty((self.seg + 1, 4, N), dtype=pop.dtype, device=dev)
+                           for _ in range(nbuf)]
         lam = torch.zeros((4, N), dtype=pop.dtype, device=dev)
         gcomp = torch.zeros((3, N), dtype=pop.dtype, device=dev)
         gax = torch.zeros(N, dtype=pop.dtype, device=dev)
-        work = tuple(torch.empty_like(t) for t in self.state0)
+        works = [tuple(torch.empty_like(t) for t in self.state0) for _ in range(nbuf)]
         adj = _lib.CableAdjointArgs()
-        adj.tape = self._tape.data_ptr()
         adj.trace_grad = gt.data_ptr()
         adj.trace_len = self.n_steps + 1
         adj.lam_v, adj.lam_m, adj.lam_h, adj.lam_n = (lam[i].data_ptr() for i in range(4))
         adj.grad_gnabar, adj.grad_gkbar, adj.grad_gl = (gcomp[i].data_ptr() for i in range(3))
         adj.grad_axial = gax.data_ptr()
         L = _lib.load()
-        st = _lib.stream_ptr(dev)
-        with torch.cuda.device(dev):
-            for k, (step0, steps) in reversed(list(enumerate(self._segments()))):
-                for w, c in zip(work, self.checkpoints[k]):
+        main = torch.cuda.current_stream(dev)
+        # recompute runs on a side stream with its own work counter, so the
+        # recompute of segment k - 1 overlaps the adjoint of segment k (each
+        # kernel alone keeps only one warp per cable busy)
+        side = self._side if nbuf == 2 else main
+        rec_done = [torch.cuda.Event() for _ in range(nbuf)]
+        adj_done = [torch.cuda.Event() for _ in range(nbuf)]
+        used = [False] * nbuf
+
+        def recompute(k):
+            b = k % nbuf
+            step0, steps = segs[k]
+            with torch.cuda.stream(side):
+                if used[b]:
+                    side.wait_event(adj_done[b])
+                for w, c in zip(works[b], self.checkpoints[k]):
                     w.copy_(c)
-                args = self._args(steps, step0, work)
-                _lib.check(L.dgb_cable_run_taped(args, self._tape.data_ptr(), st),
-                           "dgb_cable_run_taped")
-                _lib.check(L.dgb_cable_adjoint(args, ctypes.byref(adj), st), "dgb_cable_adjoint")
+                args = self._args(steps, step0, works[b])
+                if nbuf == 2:
+                    args.scratch = self._side_scratch.data_ptr()
+                _lib.check(L.dgb_cable_run_taped(args, self._tapes[b].data_ptr(),
+                                                 side.cuda_stream), "dgb_cable_run_taped")
+                rec_done[b].record(side)
+
+        with torch.cuda.device(dev):
+            if nbuf == 2:
+                side.wait_stream(main)
+            last = len(segs) - 1
+            if nbuf == 2:
+                recompute(last)
+            for k in range(last, -1, -1):
+                b = k % nbuf
+                if nbuf == 2 and k >= 1:
+                    recompute(k - 1)
+                elif nbuf == 1:
+                    recompute(k)
+                main.wait_event(rec_done[b])
+                step0, steps = segs[k]
+                adj.tape = self._tapes[b].data_ptr()
+                args = self._args(steps, step0, works[b])
+                _lib.check(L.dgb_cable_adjoint(args, ctypes.byref(adj), main.cuda_stream),
+                           "dgb_cable_adjoint")
+                adj_done[b].record(main)
+                used[b] = True
+            if nbuf == 2:
+                main.wait_stream(side)
         # per-compartment results, kept for inspection: adjoint of the initial
         # state (v, m, h, n), dLoss/d(gnabar, gkbar, gl) and the axial term
         self.lam0, self.grad_comp, self.grad_axial = lam, gcomp, gax

@@ -108,12 +108,12 @@ def test_uniform_compression_gives_the_same_gradient(cuda):
         assert torch.equal(a, b)
 
 
-def test_checkpoint_interval_does_not_change_the_gradient(cuda):
+def test_checkpoint_interval_and_stream_overlap_do_not_change_the_gradient(cuda):
     steps = 200
     res = []
-    for every in (200, 64, 1):
+    for every, overlap in ((200, True), (64, True), (64, False), (1, True)):
         pop = _ragged_population(cuda, torch.float32)
-        run = CableGradient(pop, steps, checkpoint_every=every)
+        run = CableGradient(pop, steps, checkpoint_every=every, overlap=overlap)
         trace = run.forward()
         run.backward(torch.linspace(-1, 1, trace.numel(), device=cuda).reshape(trace.shape))
         res.append((trace, run.lam0, run.grad_comp, run.grad_axial))
