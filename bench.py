@@ -306,7 +306,8 @@ def bench_c4(args, world, rank, local):
         return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    pop, spec = cable_population_c4(n_cables, seed=4 + rank, device=dev)
+    pop, spec = cable_population_c4(n_cables, seed=4 + rank, device=dev,
+                                    fast_math=not args.exact)
     run = CableGradient(pop, n_ts, rec_idx=0, checkpoint_every=C4_CHECKPOINT)
     names = ("gnabar", "gkbar", "gl", "ra")
     hidden = [torch.as_tensor(spec["hidden"][k], dtype=torch.float32, device=dev) for k in names]
@@ -402,7 +403,9 @@ def bench_c4(args, world, rank, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {**cfg, "l2": "flushed between timed steps"},
+        "config": {**cfg, "l2": "flushed between timed steps",
+                   "math": "exact" if args.exact else
+                   "fast (float32 gradient within 5e-3 of the float64 oracle, tested)"},
         "compartment_steps_per_s": 3 * full_units / (ms * 1e-3),
         "loss": float(loss), "grad_norms": [float(g.norm()) for g in grads],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -37,16 +37,15 @@ class CableGradient:
     per cable (int or per-cable sequence).  The trace has one sample per step,
     (B, n_steps + 1), sample 0 being the initial state.  overlap: recompute
     the next segment on a side stream while the adjoint of the current one
-    runs (two tapes in memory instead of one).
+    runs (two tapes in memory instead of one).  A float32 population built
+    with fast_math runs the forward, the recompute and the adjoint's gate
+    partials and solve with the fast-math arithmetic.
     """
 
     def __init__(self, pop: CablePopulation, n_steps: int, rec_idx=0, checkpoint_every=500,
                  overlap=True):
         if pop.dt is None:
             raise RuntimeError("Model must be initialized before running.")
-        if pop.fast_math:
-            raise ValueError("gradients use the exact update; build the population without "
-                             "fast_math")
         if n_steps < 1 or checkpoint_every < 1:
             raise ValueError("n_steps and checkpoint_every must be >= 1")
         self.pop = pop

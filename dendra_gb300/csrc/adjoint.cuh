@@ -144,4 +144,84 @@ __device__ __forceinline__ void hh_gates_partials(T v, T q10, T dt, T& m, T& h, 
   dn_v = pa * q10 * dan + pb * q10 * (dan + dbn);
 }
 
+// ---------------------------------------------------------------------------
+// float32 fast-math variant (DGB_CABLE_FAST_MATH): the same gates and partials
+// with the forward fast path's shared exponentials (hh_gates_fast), fast
+// exponentials and approximate reciprocals, and a branch-free vtrap (both
+// branches evaluated, the forward's branch selected).  Derivatives change by
+// a few float32 ulps, far inside the float32 gradient tolerance.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float vtrap_fast_d(float x, float q, float e, float& dvx) {
+  const float u = q * q;
+  const float P = Math<float>::even_series(q);
+  const float dP = even_series_du<float>(u);
+  const float ser = (10.0f - x * 0.5f) + x * (q * P);
+  const float dser = -0.5f + 2.0f * q * P + 2.0f * q * u * dP;
+  const float rinv = __fdividef(1.0f, e - 1.0f);
+  const float ex = x * rinv;
+  const float dex = rinv * (1.0f - q * e * rinv);
+  const bool local = fabsf(q) <= 1.0f;
+  dvx = local ? dser : dex;
+  return local ? ser : ex;
+}
+
+__device__ __forceinline__ float cnexp_partials_fast(float x, float a, float b, float dt,
+                                                     float& dx, float& da, float& db) {
+  const float rate = a - b * x;
+  const float z = -b * dt;
+  if (fabsf(z) <= 0.5f) {
+    const float ph = Math<float>::phi1(z);
+    const float dph = phi1_dz<float>(z);
+    dx = 1.0f - dt * b * ph;
+    da = dt * ph;
+    db = -dt * x * ph - dt * dt * rate * dph;
+    return x + dt * rate * ph;
+  }
+  const float E = __expf(z);
+  const float binv = __fdividef(1.0f, b);
+  const float eq = a * binv;
+  const float omE = 1.0f - E;
+  dx = E;
+  da = omE * binv;
+  db = -eq * binv * omE - (x - eq) * E * dt;
+  return eq + (x - eq) * E;
+}
+
+__device__ __forceinline__ void hh_gates_partials_fast(float v, float q10, float dt, float& m,
+                                                       float& h, float& n, float& dm_m,
+                                                       float& dm_v, float& dh_h, float& dh_v,
+                                                       float& dn_n, float& dn_v) {
+  const float xm = -(v + 40.0f), xn = -(v + 55.0f);
+  const float qm = xm * 0.1f, qn = xn * 0.1f;
+  const float e10 = __expf(qm);                   // exp(-(v+40)/10)
+  const float e_n = e10 * 0.22313016014843f;      // exp(-(v+55)/10)
+  const float e_h = e10 * 1.6487212707001282f;    // exp(-(v+35)/10)
+  const float u = -(v + 65.0f);
+  const float e18 = __expf(u * (1.0f / 18.0f));
+  const float e80 = __expf(u * (1.0f / 80.0f));
+  const float e80_2 = e80 * e80;
+  const float e20 = e80_2 * e80_2;
+  float dvm, dvn;
+  const float alpha_m = 0.1f * vtrap_fast_d(xm, qm, e10, dvm);
+  const float beta_m = 4.0f * e18;
+  const float alpha_h = 0.07f * e20;
+  const float rh = __fdividef(1.0f, e_h + 1.0f);
+  const float beta_h = rh;
+  const float alpha_n = 0.01f * vtrap_fast_d(xn, qn, e_n, dvn);
+  const float beta_n = 0.125f * e80;
+  const float dam = -0.1f * dvm;
+  const float dbm = -beta_m * (1.0f / 18.0f);
+  const float dah = -alpha_h * (1.0f / 20.0f);
+  const float dbh = e_h * rh * rh * 0.1f;
+  const float dan = -0.01f * dvn;
+  const float dbn = -beta_n * (1.0f / 80.0f);
+  float pa, pb;
+  m = cnexp_partials_fast(m, q10 * alpha_m, q10 * (alpha_m + beta_m), dt, dm_m, pa, pb);
+  dm_v = pa * q10 * dam + pb * q10 * (dam + dbm);
+  h = cnexp_partials_fast(h, q10 * alpha_h, q10 * (alpha_h + beta_h), dt, dh_h, pa, pb);
+  dh_v = pa * q10 * dah + pb * q10 * (dah + dbh);
+  n = cnexp_partials_fast(n, q10 * alpha_n, q10 * (alpha_n + beta_n), dt, dn_n, pa, pb);
+  dn_v = pa * q10 * dan + pb * q10 * (dan + dbn);
+}
+
 }  // namespace dgb

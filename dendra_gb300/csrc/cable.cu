@@ -58,9 +58,9 @@ extern "C" int dgb_cable_solve_update(const dgb_cable_args* args, const void* lo
 static int validate_taped(const dgb_cable_args* args) {
   DGB_REQUIRE(args->scratch != nullptr, "scratch (2 x int32, device) is required");
   DGB_REQUIRE(args->n_comp >= 0, "n_comp must be the total compartment count");
-  DGB_REQUIRE((args->flags & (DGB_CABLE_STOP_ON_SPIKE | DGB_CABLE_FAST_MATH)) == 0,
-              "the taped run and the adjoint use the exact update without early stop "
-              "(DGB_CABLE_STOP_ON_SPIKE and DGB_CABLE_FAST_MATH are not accepted)");
+  DGB_REQUIRE((args->flags & DGB_CABLE_STOP_ON_SPIKE) == 0,
+              "the taped run and the adjoint cover every step of the segment "
+              "(DGB_CABLE_STOP_ON_SPIKE is not accepted)");
   const int64_t kmax = args->max_k;
   DGB_REQUIRE(kmax >= 1 && kmax <= 32 * kCableMaxCH,
               "max compartments per cable (max_k) must be in [1, %d], got %lld",

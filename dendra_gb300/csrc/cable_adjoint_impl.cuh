@@ -63,7 +63,7 @@ __host__ __device__ inline PlaneLayout adjoint_layout(bool geo_planes, bool fiel
 // planes: rows i = r*ch + j, coefficients from row(j, a, b, c, d); the
 // solution goes to plane qx.  Same elimination as the forward's fused solve
 // (local sweep per lane, reduced row per lane, PCR across the 32 lanes).
-template <typename T, class Row>
+template <typename T, bool FAST, class Row>
 __device__ __forceinline__ void plane_solve(const Planes<T>& P, int ch, int qx, Row row) {
   const int r = threadIdx.x & 31;
   const int last = ch - 1;
@@ -78,12 +78,12 @@ __device__ __forceinline__ void plane_solve(const Planes<T>& P, int ch, int qx, 
       Cs = c;
       Ds = d;
     } else if (j == 1) {
-      const T rinv = T(1) / b;
+      const T rinv = dv<T, FAST>(T(1), b);
       ap = a * rinv;
       cp = c * rinv;
       dp = d * rinv;
     } else {
-      const T rinv = T(1) / (b - a * cp);
+      const T rinv = dv<T, FAST>(T(1), b - a * cp);
       ap = -a * ap * rinv;
       dp = (d - a * dp) * rinv;
       cp = c * rinv;
@@ -141,8 +141,8 @@ __device__ __forceinline__ void plane_solve(const Planes<T>& P, int ch, int qx, 
     T ga_r = shfl_down<T>(ga, sh, 32), de_r = shfl_down<T>(de, sh, 32);
     const bool hl = r >= sh;
     const bool hr = r + sh < 32;
-    T k1 = hl ? al / be_l : T(0);
-    T k2 = hr ? ga / be_r : T(0);
+    T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
+    T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
     T al_n = hl ? -k1 * al_l : T(0);
     T ga_n = hr ? -k2 * ga_r : T(0);
     be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
@@ -150,7 +150,7 @@ __device__ __forceinline__ void plane_solve(const Planes<T>& P, int ch, int qx, 
     al = al_n;
     ga = ga_n;
   }
-  const T xs = de / be;
+  const T xs = dv<T, FAST>(de, be);
   T xe = xs;
   if (ch > 1) {
     T xs_next = shfl_down<T>(xs, 1, 32);
@@ -173,7 +173,7 @@ __device__ __forceinline__ T row_next(const Planes<T>& P, int q, int j, int r, i
   return j < last ? P.at(q, j + 1, r) : (r < 31 ? P.at(q, 0, r + 1) : T(0));
 }
 
-template <typename T>
+template <typename T, bool FAST>
 __device__ void adjoint_cable(const CableArgsT<T>& A, const AdjArgsT<T>& D, int cable, T* smw,
                               int ch, const PlaneLayout& lay) {
   const int r = threadIdx.x & 31;
@@ -295,7 +295,11 @@ __device__ void adjoint_cable(const CableArgsT<T>& A, const AdjArgsT<T>& D, int 
       const T v = P.at(qv, j, r);
       T m = P.at(Q_M, j, r), h = P.at(Q_H, j, r), n = P.at(Q_N, j, r);
       T dmm, dmv, dhh, dhv, dnn, dnv;
-      hh_gates_partials<T>(v, q10, dt, m, h, n, dmm, dmv, dhh, dhv, dnn, dnv);
+      if constexpr (FAST) {
+        hh_gates_partials_fast(v, q10, dt, m, h, n, dmm, dmv, dhh, dhv, dnn, dnv);
+      } else {
+        hh_gates_partials<T>(v, q10, dt, m, h, n, dmm, dmv, dhh, dhv, dnn, dnv);
+      }
       P.at(Q_M, j, r) = m;
       P.at(Q_H, j, r) = h;
       P.at(Q_N, j, r) = n;
@@ -316,7 +320,7 @@ __device__ void adjoint_cable(const CableArgsT<T>& A, const AdjArgsT<T>& D, int 
       P.at(Q_G, j, r) = gl + gna * m3 * h + gk * (n2 * n2);
     }
     // ---- phase 2: M^T mu = lv'
-    plane_solve<T>(P, ch, Q_MU, [&](int j, T& a, T& b, T& c, T& d) {
+    plane_solve<T, FAST>(P, ch, Q_MU, [&](int j, T& a, T& b, T& c, T& d) {
       T gr, glf, scl;
       geo(j, gr, glf, scl);
       b = T(1) - dt_s * ((-gr + -glf) - mul_rn(P.at(Q_G, j, r), scl));
@@ -414,7 +418,7 @@ __device__ void adjoint_cable(const CableArgsT<T>& A, const AdjArgsT<T>& D, int 
   __syncwarp();
 }
 
-template <typename T>
+template <typename T, bool FAST>
 __global__ void __launch_bounds__(kCableWarps * 32)
     cable_adjoint_kernel(CableArgsT<T> A, AdjArgsT<T> D, int ch_max, PlaneLayout lay) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -433,8 +437,37 @@ __global__ void __launch_bounds__(kCableWarps * 32)
       if (lane == 0) atomicOr(A.counter + 1, kErrChunk);
       continue;
     }
-    adjoint_cable<T>(A, D, cable, smw, ch, lay);
+    adjoint_cable<T, FAST>(A, D, cable, smw, ch, lay);
   }
+}
+
+template <typename T, bool FAST>
+static int launch_adjoint(const CableArgsT<T>& A, const AdjArgsT<T>& D, int ch_max,
+                          const PlaneLayout& lay, cudaStream_t st) {
+  const size_t per_warp = (size_t)lay.n_planes * ch_max * 32 * sizeof(T);
+  int wpb = kCableWarps;
+  while (wpb > 1 && (size_t)wpb * per_warp > 227 * 1024) wpb >>= 1;
+  if ((size_t)wpb * per_warp > 227 * 1024) {
+    set_error("cable too long for the adjoint's shared memory (%zu bytes per cable, limit %d)",
+              per_warp, 227 * 1024);
+    return DGB_ERANGE;
+  }
+  const int threads = wpb * 32;
+  const size_t smem = (size_t)wpb * per_warp;
+  auto kern = cable_adjoint_kernel<T, FAST>;
+  DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  int per_sm = 0;
+  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+  if (per_sm < 1) per_sm = 1;
+  int blocks = device_sm_count() * per_sm;
+  const int blocks_needed = (A.n_cables + wpb - 1) / wpb;
+  if (blocks > blocks_needed) blocks = blocks_needed;
+  if (blocks < 1) blocks = 1;
+  DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, 2 * sizeof(int32_t), st));
+  kern<<<blocks, threads, smem, st>>>(A, D, ch_max, lay);
+  DGB_LAUNCH_CHECK();
+  return DGB_OK;
 }
 
 template <typename T>
@@ -457,30 +490,10 @@ int cable_adjoint_t(const dgb_cable_args* args, const dgb_cable_adjoint_args* ad
   const bool chan_planes = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) == 0;
   const bool geo_planes = (args->flags & DGB_CABLE_UNIFORM_GEOMETRY) == 0;
   const PlaneLayout lay = adjoint_layout(geo_planes, field, chan_planes);
-  const size_t per_warp = (size_t)lay.n_planes * ch_max * 32 * sizeof(T);
-  int wpb = kCableWarps;
-  while (wpb > 1 && (size_t)wpb * per_warp > 227 * 1024) wpb >>= 1;
-  if ((size_t)wpb * per_warp > 227 * 1024) {
-    set_error("cable too long for the adjoint's shared memory (%zu bytes per cable, limit %d)",
-              per_warp, 227 * 1024);
-    return DGB_ERANGE;
+  if constexpr (sizeof(T) == 4) {
+    if (args->flags & DGB_CABLE_FAST_MATH) return launch_adjoint<T, true>(A, D, ch_max, lay, st);
   }
-  const int threads = wpb * 32;
-  const size_t smem = (size_t)wpb * per_warp;
-  auto kern = cable_adjoint_kernel<T>;
-  DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-  int per_sm = 0;
-  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
-  if (per_sm < 1) per_sm = 1;
-  int blocks = device_sm_count() * per_sm;
-  const int blocks_needed = (A.n_cables + wpb - 1) / wpb;
-  if (blocks > blocks_needed) blocks = blocks_needed;
-  if (blocks < 1) blocks = 1;
-  DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, 2 * sizeof(int32_t), st));
-  kern<<<blocks, threads, smem, st>>>(A, D, ch_max, lay);
-  DGB_LAUNCH_CHECK();
-  return DGB_OK;
+  return launch_adjoint<T, false>(A, D, ch_max, lay, st);
 }
 
 #define DGB_INSTANTIATE_CABLE_ADJOINT(T)                                                \

@@ -517,8 +517,11 @@ int cable_run_taped_t(const dgb_cable_args* args, void* tape, int ch_max, cudaSt
   const bool field = args->field != nullptr && args->ve_amp != nullptr;
   const bool chan_planes = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) == 0;
   const bool geo_planes = (args->flags & DGB_CABLE_UNIFORM_GEOMETRY) == 0;
-  return launch_cable_run<T, false, true>(A, ch_max, plane_layout(geo_planes, field, chan_planes),
-                                         st);
+  const PlaneLayout lay = plane_layout(geo_planes, field, chan_planes);
+  if constexpr (sizeof(T) == 4) {
+    if (args->flags & DGB_CABLE_FAST_MATH) return launch_cable_run<T, true, true>(A, ch_max, lay, st);
+  }
+  return launch_cable_run<T, false, true>(A, ch_max, lay, st);
 }
 
 template <typename T>

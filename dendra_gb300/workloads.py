@@ -92,10 +92,11 @@ def c4_spec(n_cables=1024, seed=4):
                 hidden=hidden, guess=guess)
 
 
-def cable_population_c4(n_cables=1024, seed=4, dtype=torch.float32, device="cuda"):
+def cable_population_c4(n_cables=1024, seed=4, dtype=torch.float32, device="cuda",
+                        fast_math=False):
     """Config-4 population at the default parameters (the guesses)."""
     s = c4_spec(n_cables, seed)
     pop = CablePopulation([s["K"]] * n_cables, 1.0, 10.0, rhoa=100.0, celsius=6.3,
-                          v_init=-65.0, dtype=dtype, device=device)
+                          v_init=-65.0, dtype=dtype, device=device, fast_math=fast_math)
     pop.inject(0, torch.as_tensor(s["amp_ma"]), s["delay"], s["pw"])
     return pop.initialize(0.025), s

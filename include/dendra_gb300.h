@@ -224,8 +224,7 @@ int dgb_cable_solve_update(const dgb_cable_args* args, const void* lower,
  * dgb_cable_run that also writes the state tape of the run, for the adjoint:
  *   tape: (n_steps + 1, 4, n_comp) in the state dtype; tape[k][q][g] is
  *   state q (0 v, 1 m, 2 h, 3 n) of compartment g after k steps of this call.
- * n_comp must be set; DGB_CABLE_STOP_ON_SPIKE and DGB_CABLE_FAST_MATH are
- * rejected (the adjoint differentiates the exact update).  This is the
+ * n_comp must be set; DGB_CABLE_STOP_ON_SPIKE is rejected.  This is the
  * recompute pass of checkpoint-and-recompute: run it from a checkpoint over
  * one segment, then dgb_cable_adjoint over the same segment.  tape = NULL
  * runs the same kernel without writing a tape: checkpoints taken that way lie
@@ -269,9 +268,10 @@ typedef struct dgb_cable_adjoint_args {
  * population, stimulus, rec_idx, rec_every, step0 and n_steps as the taped run;
  * v/m/h/n are not read).  One warp per cable; the transposed tridiagonal
  * system is solved with the same chunked elimination as the forward.
- * Exact (non-fast) float32 or float64 arithmetic; the cable size limit is set
- * by shared memory (float32: K <= 1024; float64: K <= 896 with every optional
- * plane present).
+ * DGB_CABLE_FAST_MATH (float32) evaluates the gate partials with shared
+ * exponentials, fast exponentials and approximate reciprocals, and the solve
+ * with approximate reciprocals.  The cable size limit is set by shared memory
+ * (float32: K <= 1024; float64: K <= 896 with every optional plane present).
  */
 int dgb_cable_adjoint(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj,
                       void* stream);

@@ -38,9 +38,10 @@ def test_float64_gradient_matches_reference_autograd(golden, cuda, every):
         np.testing.assert_allclose(grads[k], g[f"grad_{k}"], rtol=1e-6, err_msg=k)
 
 
-def test_float32_gradient_is_close_to_the_float64_reference(golden, cuda):
+@pytest.mark.parametrize("fast", [False, True])
+def test_float32_gradient_is_close_to_the_float64_reference(golden, cuda, fast):
     g = golden("adjoint_f64.npz")
-    pop = golden_adjoint_population(g, torch.float32, device=cuda)
+    pop = golden_adjoint_population(g, torch.float32, device=cuda, fast_math=fast)
     run = CableGradient(pop, int(g["steps"]), rec_idx=0, checkpoint_every=100)
     _, _, grads = _fit_step(run, g, cuda, torch.float32)
     for k in PARAMS:
@@ -49,7 +50,7 @@ def test_float32_gradient_is_close_to_the_float64_reference(golden, cuda):
         assert err <= 2e-2, (k, err, grads[k], ref)
 
 
-def _ragged_population(cuda, dtype, compress_uniform=True, planes=True):
+def _ragged_population(cuda, dtype, compress_uniform=True, planes=True, fast_math=False):
     """Ragged cables (K = 1 .. 200), per-compartment channel densities and
     geometry, extracellular point source plus a somatic current clamp."""
     rng = np.random.default_rng(11)
@@ -62,7 +63,7 @@ def _ragged_population(cuda, dtype, compress_uniform=True, planes=True):
     pop = CablePopulation(ks, torch.as_tensor(diam), torch.as_tensor(dx),
                           rhoa=torch.as_tensor(rng.uniform(80, 120, len(ks))), celsius=6.3,
                           v_init=-65.0, dtype=dtype, device=cuda, hh=hh,
-                          compress_uniform=compress_uniform)
+                          compress_uniform=compress_uniform, fast_math=fast_math)
     x = pop.positions()
     cab = np.repeat(np.arange(len(ks)), ks)
     r_cm = torch.sqrt(x ** 2 + torch.as_tensor(rng.uniform(300, 800, len(ks))[cab]) ** 2) * 1e-4
@@ -108,11 +109,12 @@ def test_uniform_compression_gives_the_same_gradient(cuda):
         assert torch.equal(a, b)
 
 
-def test_checkpoint_interval_and_stream_overlap_do_not_change_the_gradient(cuda):
+@pytest.mark.parametrize("fast", [False, True])
+def test_checkpoint_interval_and_stream_overlap_do_not_change_the_gradient(cuda, fast):
     steps = 200
     res = []
     for every, overlap in ((200, True), (64, True), (64, False), (1, True)):
-        pop = _ragged_population(cuda, torch.float32)
+        pop = _ragged_population(cuda, torch.float32, fast_math=fast)
         run = CableGradient(pop, steps, checkpoint_every=every, overlap=overlap)
         trace = run.forward()
         run.backward(torch.linspace(-1, 1, trace.numel(), device=cuda).reshape(trace.shape))
@@ -155,3 +157,26 @@ def test_oracle_param_grads_helper_agrees_with_gpu_per_cable_sums(golden, cuda):
     _, _, grads = _fit_step(run, g, cuda)
     for k in PARAMS:
         np.testing.assert_allclose(grads[k], ref[k], rtol=1e-7, err_msg=k)
+
+
+def test_fast_math_float32_adjoint_tracks_the_float64_oracle(cuda):
+    """Ragged cables with every optional plane: the fast float32 gradient against
+    the float64 oracle's reverse mode of the same (float32-rounded) problem."""
+    from tests._cases import as_f64
+
+    steps = 300
+    pop = _ragged_population(cuda, torch.float32, fast_math=True)
+    p = as_f64(pop.problem_dict())
+    run = CableGradient(pop, steps, rec_idx=0, checkpoint_every=64)
+    trace = run.forward()
+    rng = np.random.default_rng(5)
+    tg = rng.standard_normal(tuple(trace.shape)).astype(np.float32)
+    run.backward(torch.as_tensor(tg))
+    p["rec_idx"] = np.zeros(pop.B, dtype=np.int32)
+    ref = oracle.cable_grad(p, steps, tg.astype(np.float64), gate_f32=True)
+    got = {"g_gnabar": run.grad_comp[0], "g_gkbar": run.grad_comp[1], "g_gl": run.grad_comp[2],
+           "g_axial": run.grad_axial, "lam_v": run.lam0[0]}
+    for k, v in got.items():
+        v = v.double().cpu().numpy()
+        err = np.abs(v - ref[k]).max() / np.abs(ref[k]).max()
+        assert err <= 5e-3, (k, err)

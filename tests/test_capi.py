@@ -87,10 +87,9 @@ def test_taped_run_and_adjoint_reject_bad_arguments_on_the_host():
     for name in ("cable_ptr", "v", "m", "h", "n", "g_right", "g_left", "scale", "cm_inv",
                  "gnabar", "gkbar", "gl", "el", "scratch"):
         setattr(a, name, 4096)
-    a.flags = _lib.CABLE_FAST_MATH
+    a.flags = _lib.CABLE_STOP_ON_SPIKE
     assert L.dgb_cable_run_taped(ctypes.byref(a), 4096, None) == -1
     assert b"not accepted" in L.dgb_last_error()
-    a.flags = _lib.CABLE_STOP_ON_SPIKE
     adj = _lib.CableAdjointArgs()
     assert L.dgb_cable_adjoint(ctypes.byref(a), ctypes.byref(adj), None) == -1
     a.flags = 0
