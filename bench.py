@@ -240,6 +240,17 @@ def bench_c3(args, world, rank, local):
         "gpu_launches": args.steps * windows * 2, "spikes_per_run": spikes,
         "clocks": clocks.summary(),
     }
+    if rank == 0 and not args.no_cpu:
+        cnet, cn = random_network(64, seed=3, dtype=torch.float32, device="cpu",
+                                  t_stop_ms=min(t_stop, 50.0))
+        pd = cnet.problem_dict(cn)
+        t0 = time.perf_counter()
+        oracle.net_run(pd, cn)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": cnet.N * cn / dt, "unit": METRIC, "cores": 1,
+                                "kind": "port",
+                                "sample": f"64-cell network ({cnet.N} compartments), {cn} steps, "
+                                          "float32, one core (the network oracle is serial)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -432,6 +443,61 @@ def bench_c4(args, world, rank, local):
 MLP_FLOP_PER_SAMPLE = 2 * (4 * 256 + 256 * 256 + 256 * 256 + 256 * 1)
 
 
+def _c5_cpu(n_fibres, seed=7, lb0=0.0, ub0=0.1, rtol=0.01):
+    """Plain bisection with the Thresholder's rules (bound fixing x2 up to 10
+    times, inactive lower bound, bisection to rtol, at most 25 iterations) on
+    the oracle's float32 cable update, every trial simulating all open lanes.
+    Returns (thresholds/s, seconds, threads)."""
+    import torch
+
+    import oracle
+    from dendra_gb300.threshold import (fibre_params, fibre_population, horizon_steps,
+                                        node_compartment)
+
+    p = fibre_params(n_fibres, seed=seed)
+    pop = fibre_population(p, device="cpu")
+    base = pop.problem_dict()
+    n_steps = horizon_steps(p["pw"].max())
+    B = pop.B
+
+    def fired(amp, lanes):
+        q = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in base.items()}
+        q["ve_amp"] = (-amp).astype(np.float32)
+        q["spk_idx"] = np.full(B, node_compartment(5), dtype=np.int32)
+        q["spk_idx2"] = np.full(B, node_compartment(-5), dtype=np.int32)
+        q["spk_thr"] = 0.0
+        sel = np.flatnonzero(lanes)
+        if sel.size == 0:
+            return np.zeros(B, dtype=bool)
+        _, cnt, _, _ = oracle.cable_run(q, n_steps)
+        out = np.zeros(B, dtype=bool)
+        out[sel] = cnt[sel] > 0
+        return out
+
+    t0 = time.perf_counter()
+    lb, ub = np.full(B, lb0), np.full(B, ub0)
+    ignore = np.zeros(B, dtype=bool)
+    for tries in range(11):
+        act = fired(ub, ~ignore) | ignore
+        if act.all():
+            break
+        if tries == 10:
+            ignore |= ~act
+            break
+        ub = np.where(act, ub, ub * 2.0)
+    open_ = ((ub - lb) / ub >= rtol) & ~ignore
+    for _ in range(25):
+        if not open_.any():
+            break
+        stim = (ub + lb) / 2
+        f = fired(stim, open_)
+        ub = np.where(open_ & f, stim, ub)
+        lb = np.where(open_ & ~f, stim, lb)
+        open_ = ((ub - lb) / ub >= rtol) & ~ignore
+    dt = time.perf_counter() - t0
+    return B / dt, dt, oracle.num_threads()
+
+
 def bench_c5(args, world, rank, local):
     """Config 5: thresholds/s of the learned bracket + confirming bisection vs
     plain bisection, 65,536 myelinated-fibre-like cables (241 compartments),
@@ -528,6 +594,12 @@ def bench_c5(args, world, rank, local):
         "roofline": {"bound": "tensor", "achieved": flops, "peak": peak, "unit": "TFLOP/s",
                      "frac": flops / peak, "traffic": None, "note": MLP_FLOPS_NOTE},
     }
+    if rank == 0 and not args.no_cpu:
+        v, secs, cores = _c5_cpu(64)
+        line["cpu_baseline"] = {"value": v, "unit": "thresholds/s", "cores": cores,
+                                "kind": "port",
+                                "sample": "64 fibres, plain bisection on the oracle's float32 "
+                                          "cable update (all open lanes simulated per trial)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -11,13 +11,15 @@ reference implementation itself (``tests/golden/make_golden.py``), and
 
 Layers:
   * ``oracle.c`` / ``oracle_impl.h``  float64 and float32 C restatements of the
-    HH rates, cnexp, the backward-Euler cable update, Thomas, PCR and DHS,
-    and the reverse mode of the cable update (``cable_grad``: full state
-    tape, transposed Thomas solve, gate partials on the forward's branches).
-  * ``events.py``  numpy restatement of NetCon delay rounding, the dense delay
-    ring and bit-packed delivery (integer/index work).
-  * ``trees.py``   numpy restatement of the tree topology plan and the DHS
-    right-hand-side assembly.
+    HH rates, cnexp, the backward-Euler cable update, Thomas, PCR, DHS and the
+    branched-cell network step (``orc_net_run``: Exp2Syn delivery, soma HH,
+    tree solve, delay ring), and the reverse mode of the cable update
+    (``cable_grad``: full state tape, transposed Thomas solve, gate partials
+    on the forward's branches).
+  * ``core.py``  ctypes bindings; builds the C library with gcc on first use.
+  The integer/index event primitives (delay rounding, bit packing, sequential
+  delivery) are restated inline in ``tests/test_netcon.py``, next to the
+  reference known answers they are checked against.
 """
 
 from .core import (  # noqa: F401
