@@ -197,6 +197,8 @@ def bench_c3(args, world, rank, local):
                              "sample": f"64-cell network, {n} steps"},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
+    from dendra_gb300.autotune import tune_network
+
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     net, n = random_network(n_cells, seed=2024 + rank, dtype=torch.float32, device=dev,
@@ -204,9 +206,13 @@ def bench_c3(args, world, rank, local):
     comp_steps = net.N * n
     st = torch.cuda.current_stream(dev)
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    wpb, tune_ms = tune_network(net)
+    # the whole run's window loop, captured once as a CUDA graph
+    net.reset()
+    cap = net.capture(n)
     for _ in range(max(3, args.warmup)):
         net.reset()
-        net.run(n)
+        cap.replay()
     torch.cuda.synchronize()
     times, spikes = [], 0
     with ClockSampler(local) as clocks:
@@ -216,12 +222,22 @@ def bench_c3(args, world, rank, local):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
-            r = net.run(n)
+            r = cap.replay()
             e1.record(st)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
             spikes = int(r.sum())
     ms = float(np.mean(times))
+    # the same run launched window by window from the host, for comparison
+    net.reset()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    net.run(n)
+    e1.record(st)
+    e1.synchronize()
+    eager_ms = e0.elapsed_time(e1)
     value = comp_steps * world / (ms * 1e-3)
     peak, peak_kind = _peaks()
     achieved = C3_BYTES_PER_COMP_STEP * comp_steps / (ms * 1e-3) / 1e9
@@ -232,7 +248,10 @@ def bench_c3(args, world, rank, local):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "c3-branched-network", "n_cells": n_cells,
                    "compartments": net.N, "synapses": net.n_syn, "timesteps": n,
-                   "window_steps": net.window, "l2": "flushed between timed steps"},
+                   "window_steps": net.window, "l2": "flushed between timed steps",
+                   "launch": f"one CUDA graph of {cap.launches} kernels per run",
+                   "warps_per_block": wpb, "autotune_ms": tune_ms},
+        "eager_launch_ms_per_step": eager_ms,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
                      "note": f"{C3_BYTES_PER_COMP_STEP} algorithmic B per compartment-step of the "
@@ -655,6 +674,9 @@ def main():
     pop = cable_population_c2(n_cables=args.cables, dtype=torch.float32, device=dev,
                               seed=2024 + rank, fast_math=not args.exact)
     comp_steps = pop.N * n_ts
+    from dendra_gb300.autotune import tune_cable_run
+
+    wpb, tune_ms = tune_cable_run(pop, n_steps=100)
     v0, m0, h0, n0 = (t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
 
     def reset():
@@ -779,7 +801,8 @@ def main():
                    "timesteps": n_ts, "state_dtype": "float32",
                    "math": "exact" if args.exact else "fast (<=1e-3 mV vs float64, tested)",
                    "l2": "flushed between timed steps (256 MiB write, outside the events)",
-                   "launch": "one persistent dgb_cable_run launch per step"},
+                   "launch": "one persistent dgb_cable_run launch per step",
+                   "warps_per_block": wpb, "autotune_ms": tune_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
                      "note": (f"achieved = {ALG_BYTES_PER_COMP_STEP} algorithmic B per "

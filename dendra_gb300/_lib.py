@@ -52,7 +52,7 @@ class CableArgs(ctypes.Structure):
         ("spk_idx", _P), ("spk_thr", _D), ("spk_below", _P), ("spk_count", _P),
         ("spk_first", _P), ("spk_idx2", _P), ("spk_below2", _P),
         ("max_k", _I32), ("flags", _I32), ("n_comp", _I64),
-        ("comp_cable", _P), ("scratch", _P),
+        ("comp_cable", _P), ("scratch", _P), ("warps_per_block", _I32), ("reserved", _I32),
     ]
 
 

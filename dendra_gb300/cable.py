@@ -147,6 +147,9 @@ class CablePopulation:
             raise ValueError("fast_math applies to float32 state only")
         self.fast_math = bool(fast_math)
         self.compress_uniform = bool(compress_uniform)
+        # cables in flight per CTA of the persistent kernels (0 = library
+        # default); dendra_gb300.autotune.tune_cable_run picks it
+        self.warps_per_block = 0
         self.field = None
         self.ve = None
         self.intra = None
@@ -308,6 +311,7 @@ class CablePopulation:
         a.n_comp = self.N
         a.comp_cable = d["comp_cable"].data_ptr()
         a.scratch = d["scratch"].data_ptr()
+        a.warps_per_block = int(self.warps_per_block)
         return a
 
     def run(self, n_steps, *, rec_idx=None, rec_every=1, spk_idx=None, spk_thr=0.0,

@@ -419,7 +419,7 @@ __device__ void adjoint_cable(const CableArgsT<T>& A, const AdjArgsT<T>& D, int 
 }
 
 template <typename T, bool FAST>
-__global__ void __launch_bounds__(kCableWarps * 32)
+__global__ void __launch_bounds__(kCableMaxWarps * 32)
     cable_adjoint_kernel(CableArgsT<T> A, AdjArgsT<T> D, int ch_max, PlaneLayout lay) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5;
@@ -445,9 +445,8 @@ template <typename T, bool FAST>
 static int launch_adjoint(const CableArgsT<T>& A, const AdjArgsT<T>& D, int ch_max,
                           const PlaneLayout& lay, cudaStream_t st) {
   const size_t per_warp = (size_t)lay.n_planes * ch_max * 32 * sizeof(T);
-  int wpb = kCableWarps;
-  while (wpb > 1 && (size_t)wpb * per_warp > 227 * 1024) wpb >>= 1;
-  if ((size_t)wpb * per_warp > 227 * 1024) {
+  const int wpb = persistent_wpb(A.wpb, per_warp);
+  if (wpb == 0) {
     set_error("cable too long for the adjoint's shared memory (%zu bytes per cable, limit %d)",
               per_warp, 227 * 1024);
     return DGB_ERANGE;

@@ -6,7 +6,8 @@
 
 namespace dgb {
 
-constexpr int kCableWarps = 4;  // default warps (cables in flight) per block
+constexpr int kCableWarps = 4;     // default warps (cables in flight) per block
+constexpr int kCableMaxWarps = 4;  // largest accepted warps_per_block
 
 template <typename T>
 struct CableArgsT {
@@ -34,6 +35,7 @@ struct CableArgsT {
   int32_t* counter;
   T* tape;         // (n_steps + 1, 4, n_comp) state tape, nullptr = none
   int64_t n_comp;  // total compartments (tape plane stride)
+  int wpb;         // requested warps per block (0 = default)
 };
 
 template <typename T>
@@ -86,6 +88,7 @@ static CableArgsT<T> typed(const dgb_cable_args* a) {
   t.counter = a->scratch;
   t.tape = nullptr;
   t.n_comp = a->n_comp;
+  t.wpb = a->warps_per_block;
   return t;
 }
 
@@ -156,6 +159,15 @@ struct RowWalk {
     }
   }
 };
+
+// Warps per block for a persistent launch: the requested count (default
+// kCableWarps), halved while the block's shared memory exceeds 227 KB.
+// Returns 0 when even one warp does not fit.
+inline int persistent_wpb(int requested, size_t per_warp) {
+  int wpb = requested > 0 ? requested : kCableWarps;
+  while (wpb > 1 && (size_t)wpb * per_warp > 227 * 1024) wpb >>= 1;
+  return (size_t)wpb * per_warp <= 227 * 1024 ? wpb : 0;
+}
 
 // Copy planes q_v, q_m, q_h, q_n of one cable to dst[q * N + i] (coalesced).
 template <typename T>

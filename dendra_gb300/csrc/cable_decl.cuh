@@ -48,6 +48,8 @@ inline int validate_cable_args(const dgb_cable_args* a) {
               "unknown flags %d", a->flags);
   DGB_REQUIRE(!(a->flags & DGB_CABLE_FAST_MATH) || a->dtype == DGB_F32,
               "DGB_CABLE_FAST_MATH applies to float32 state only");
+  DGB_REQUIRE(a->warps_per_block >= 0 && a->warps_per_block <= 4 && a->warps_per_block != 3,
+              "warps_per_block must be 0 (default), 1, 2 or 4, got %d", a->warps_per_block);
   return DGB_OK;
 }
 

@@ -334,7 +334,7 @@ __device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
 }
 
 template <typename T, bool FAST, bool TAPE>
-__global__ void __launch_bounds__(kCableWarps * 32) cable_run_kernel(CableArgsT<T> A, int ch_max,
+__global__ void __launch_bounds__(kCableMaxWarps * 32) cable_run_kernel(CableArgsT<T> A, int ch_max,
                                                                      PlaneLayout lay) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5;
@@ -475,10 +475,8 @@ static int launch_cable_run(CableArgsT<T> A, int ch_max, const PlaneLayout& lay,
   // one warp per cable in flight; long cables get fewer warps per block so
   // the block's planes fit the 227 KB shared-memory limit
   const size_t per_warp = (size_t)lay.n_planes * ch_max * 32 * sizeof(T);
-  int wpb = kCableWarps;
-  while (wpb > 1 && (size_t)wpb * per_warp > 227 * 1024) wpb >>= 1;
-  DGB_REQUIRE((size_t)wpb * per_warp <= 227 * 1024,
-              "cable too long for shared memory (%zu bytes per cable)", per_warp);
+  const int wpb = persistent_wpb(A.wpb, per_warp);
+  DGB_REQUIRE(wpb > 0, "cable too long for shared memory (%zu bytes per cable)", per_warp);
   const int threads = wpb * 32;
   const size_t smem = (size_t)wpb * per_warp;
   auto kern = cable_run_kernel<T, FAST, TAPE>;

@@ -283,7 +283,7 @@ static int net_window_t(const dgb_net_args* a, cudaStream_t st) {
     return DGB_ERANGE;
   }
   const size_t per_warp = net_warp_smem<T>(kmax);
-  int wpb = 4;
+  int wpb = a->warps_per_block > 0 ? a->warps_per_block : 4;
   while (wpb > 1 && wpb * per_warp > 227 * 1024) wpb >>= 1;
   if (wpb * per_warp > 227 * 1024) {
     set_error("cell of %d compartments too large for shared memory", kmax);
@@ -327,6 +327,8 @@ extern "C" int dgb_net_window(const dgb_net_args* a, void* stream) {
               "synapse arrays and ring must be non-null");
   DGB_REQUIRE(a->below && a->spike_bits && a->spike_count, "spike outputs must be non-null");
   DGB_REQUIRE(a->forest.max_k >= 1, "cells must have at least one compartment");
+  DGB_REQUIRE(a->warps_per_block >= 0 && a->warps_per_block <= 4 && a->warps_per_block != 3,
+              "warps_per_block must be 0 (default), 1, 2 or 4, got %d", a->warps_per_block);
   cudaStream_t st = as_stream(stream);
   if (a->dtype == DGB_F32) return net_window_t<float>(a, st);
   return net_window_t<double>(a, st);

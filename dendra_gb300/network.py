@@ -55,6 +55,7 @@ class NetArgs(ctypes.Structure):
         ("bg_bits", ctypes.c_void_p), ("bg_words", ctypes.c_int64), ("bg_weight", ctypes.c_double),
         ("below", ctypes.c_void_p), ("spike_bits", ctypes.c_void_p),
         ("spike_count", ctypes.c_void_p),
+        ("warps_per_block", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
 
 
@@ -187,6 +188,9 @@ class TreeNetwork:
             else int(window)
         if dsteps.size and self.window > dsteps.min():
             raise ValueError("the window must not exceed the smallest delay")
+        # cells in flight per CTA of dgb_net_window (0 = library default);
+        # dendra_gb300.autotune.tune_network picks it
+        self.warps_per_block = 0
         csr = TargetCSR(torch.as_tensor(post_sorted), self.n_syn)
         perm = csr.perm.numpy()
         self.conn = dict(
@@ -226,29 +230,44 @@ class TreeNetwork:
         self.reset()
 
     def reset(self):
+        """Initial state (v_init, steady-state soma gates, empty synapses and
+        ring).  Tensors are refilled in place once they exist, so a captured
+        run (``capture``) stays bound to them."""
         dev, dt = self.device, self.dtype
-        self.v = torch.full((self.N,), self.v_init, dtype=dt, device=dev)
-        m, h, n = hh_steady_state(torch.full((self.n_cells,), self.v_init, dtype=dt))
-        self.m, self.h, self.n = (x.to(dev) for x in (m, h, n))
-        self.A = torch.zeros(self.n_syn, dtype=dt, device=dev)
-        self.B = torch.zeros(self.n_syn, dtype=dt, device=dev)
-        self.ring = torch.zeros(self.depth, self.n_syn, dtype=dt, device=dev)
-        self.below = torch.ones(self.n_cells, dtype=torch.uint8, device=dev)
-        self.spike_count = torch.zeros(self.n_cells, dtype=torch.int32, device=dev)
+        m, h, n = (x.to(dev) for x in hh_steady_state(
+            torch.full((self.n_cells,), self.v_init, dtype=dt)))
+        if getattr(self, "v", None) is None:
+            self.v = torch.empty((self.N,), dtype=dt, device=dev)
+            self.m, self.h, self.n = (torch.empty_like(x) for x in (m, h, n))
+            self.A = torch.empty(self.n_syn, dtype=dt, device=dev)
+            self.B = torch.empty(self.n_syn, dtype=dt, device=dev)
+            self.ring = torch.empty(self.depth, self.n_syn, dtype=dt, device=dev)
+            self.below = torch.empty(self.n_cells, dtype=torch.uint8, device=dev)
+            self.spike_count = torch.empty(self.n_cells, dtype=torch.int32, device=dev)
+        self.v.fill_(self.v_init)
+        for dst, src in zip((self.m, self.h, self.n), (m, h, n)):
+            dst.copy_(src)
+        for t in (self.A, self.B, self.ring, self.spike_count):
+            t.zero_()
+        self.below.fill_(1)
         self.step = 0
         self.slot = 0
 
-    def run(self, n_steps):
-        """Advance n_steps; returns the spike raster as a (n_steps, n_cells) uint8 tensor.
-
-        Steps run in windows of at most ``self.window`` (the smallest delay);
-        each window is one dgb_net_window launch plus one dgb_net_enqueue."""
+    def _windows(self, n_steps):
         W = self.window
-        n_steps = int(n_steps)
-        windows = [W] * (n_steps // W) + ([n_steps % W] if n_steps % W else [])
+        return [W] * (n_steps // W) + ([n_steps % W] if n_steps % W else [])
+
+    def _prepare(self, n_steps):
+        """Device inputs of a run of n_steps from the current step: background
+        event bits and the per-window spike masks."""
+        windows = self._windows(n_steps)
         bits_np, words = self._bg_bits(self.step + n_steps)
         bg = torch.as_tensor(bits_np.view(np.int64), device=self.device)
         masks = torch.zeros(len(windows), self.n_cells, dtype=torch.int64, device=self.device)
+        return windows, bg, words, masks
+
+    def _launch(self, windows, bg, words, masks):
+        """Enqueue the window loop on the current stream (no host synchronisation)."""
         L = _lib.load()
         st = _lib.stream_ptr(self.device)
         a = self._args()
@@ -270,10 +289,45 @@ class TreeNetwork:
                 _lib.check(rc, "dgb_net_enqueue")
             self.step += wl
             self.slot = (self.slot + wl) % self.depth
+
+    def _raster(self, windows, masks, n_steps):
+        W = self.window
         shifts = torch.arange(W, device=self.device, dtype=torch.int64)
         rows = ((masks[:, None, :] >> shifts[None, :, None]) & 1).to(torch.uint8)
         return rows.reshape(-1, self.n_cells)[:n_steps] if n_steps % W == 0 else \
             torch.cat([rows[i, :wl] for i, wl in enumerate(windows)])
+
+    def run(self, n_steps):
+        """Advance n_steps; returns the spike raster as a (n_steps, n_cells) uint8 tensor.
+
+        Steps run in windows of at most ``self.window`` (the smallest delay);
+        each window is one dgb_net_window launch plus one dgb_net_enqueue."""
+        n_steps = int(n_steps)
+        windows, bg, words, masks = self._prepare(n_steps)
+        self._launch(windows, bg, words, masks)
+        return self._raster(windows, masks, n_steps)
+
+    def capture(self, n_steps):
+        """Capture run(n_steps) from the current step as one CUDA graph.
+
+        The graph holds every window launch and enqueue of the run (their step,
+        slot and buffer arguments fixed at capture); ``CapturedRun.replay()``
+        replays it from the same starting step, e.g. after ``reset()``.  Only
+        kernels are captured: the host does nothing between windows."""
+        n_steps = int(n_steps)
+        start = (self.step, self.slot)
+        windows, bg, words, masks = self._prepare(n_steps)
+        dev = self.device
+        _lib.load()
+        graph = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.device(dev), torch.cuda.stream(side):
+            with torch.cuda.graph(graph, stream=side, capture_error_mode="relaxed"):
+                self._launch(windows, bg, words, masks)
+        torch.cuda.current_stream(dev).wait_stream(side)
+        self.step, self.slot = start  # capturing ran nothing
+        return CapturedRun(self, graph, start, n_steps, windows, (bg, masks))
 
     def _args(self):
         a = NetArgs()
@@ -300,6 +354,7 @@ class TreeNetwork:
         a.bg_weight = self.bg_weight
         a.below = self.below.data_ptr()
         a.spike_count = self.spike_count.data_ptr()
+        a.warps_per_block = int(self.warps_per_block)
         return a
 
     # -- oracle interchange ----------------------------------------------
@@ -317,6 +372,28 @@ class TreeNetwork:
             bg_bits=bits if self.bg_steps is not None else None, bg_words=words,
             bg_syn=int(self.bg_syn_sorted[0]), bg_weight=self.bg_weight, depth=self.depth,
             slot=self.slot, step=self.step, n_syn=self.n_syn, n_cells=self.n_cells)
+
+
+class CapturedRun:
+    """A network run captured as a CUDA graph (``TreeNetwork.capture``)."""
+
+    def __init__(self, net, graph, start, n_steps, windows, buffers):
+        self.net, self.graph, self.start = net, graph, start
+        self.n_steps, self.windows = n_steps, windows
+        self.bg, self.masks = buffers
+        self.launches = 2 * len(windows)
+
+    def replay(self):
+        """Run the captured steps; returns the spike raster like ``run``."""
+        net = self.net
+        if (net.step, net.slot) != self.start:
+            raise RuntimeError(f"the graph was captured at step/slot {self.start}, the network "
+                               f"is at {(net.step, net.slot)} (reset() first)")
+        self.masks.zero_()
+        self.graph.replay()
+        net.step += self.n_steps
+        net.slot = (net.slot + self.n_steps) % net.depth
+        return net._raster(self.windows, self.masks, self.n_steps)
 
 
 def random_network(n_cells, k_range=(200, 2000), syn_per_cell=100, seed=0, dt=0.025,

@@ -173,6 +173,11 @@ typedef struct dgb_cable_args {
   /* scratch, int32[2] on the device (dgb_cable_run only): [0] work counter,
      [1] error bits after the run (0 = every cable advanced) */
   int32_t* scratch;
+  /* launch tuning of the persistent kernels (dgb_cable_run, _taped, _adjoint):
+     cables in flight per CTA, 1, 2 or 4 (0 = 4); halved while the CTA's
+     shared memory would exceed 227 KB.  The autotuner's knob. */
+  int32_t warps_per_block;
+  int32_t reserved;  /* 0 */
 } dgb_cable_args;
 
 /* dgb_cable_args.flags bits.
@@ -368,6 +373,10 @@ typedef struct dgb_net_args {
   uint8_t* below;
   uint64_t* spike_bits;
   int32_t* spike_count;
+  /* cells in flight per CTA of dgb_net_window: 1, 2 or 4 (0 = 4), halved
+     while shared memory would exceed 227 KB.  The autotuner's knob. */
+  int32_t warps_per_block;
+  int32_t reserved;  /* 0 */
 } dgb_net_args;
 
 /* sizeof(dgb_net_args) as compiled (for foreign-language mirrors). */
