@@ -36,6 +36,87 @@ ALG_BYTES_PER_COMP_STEP = 48  # unfused per-step traffic of one float32 compartm
 L2_BYTES = 129 * 1024 * 1024
 
 
+def eager_reference_step(pop, bands, step):
+    """One timestep with the reference's eager structure on the packed population.
+
+    Every elementwise operation of the mechanism advance (mod/HH.py:24-40,
+    mechanisms/_cnexp.py:96-132), the current frame (HH.py:109-116) and the
+    increment-form assembly (integrators/implicit.py:569-664) is its own torch
+    kernel, as in the reference's JIT=0 CUDA path; the solve is one call of the
+    ragged tridiagonal kernel with the update v += dv (the reference calls its
+    Triton Thomas kernel there).  A measurement baseline only: the product
+    path is dgb_cable_run."""
+    import torch
+
+    from dendra_gb300 import _lib
+    from dendra_gb300.cable import AH1, AM1, AN1, q10_of
+
+    d = pop._dev
+    v, m, h, n = pop.v, pop.m, pop.h, pop.n
+    q10, dt, dt_s = q10_of(pop.celsius), pop.dt, pop.dt_s
+
+    def vtrap(x):
+        q = x / 10.0
+        local = q.abs() <= 1.0
+        q2 = q * q
+        val = q2 * (-691.0 / 1307674368000.0) + 1.0 / 47900160.0
+        val = val * q2 - 1.0 / 1209600.0
+        val = val * q2 + 1.0 / 30240.0
+        val = val * q2 - 1.0 / 720.0
+        val = val * q2 + 1.0 / 12.0
+        series = (10.0 - x / 2.0) + x * (q * val)
+        return torch.where(local, series, x / (torch.exp(q) - 1.0))
+
+    def phi1(z):
+        val = z * (1.0 / 3628800.0) + 1.0 / 362880.0
+        for c in (40320.0, 5040.0, 720.0, 120.0, 24.0, 6.0, 2.0, 1.0):
+            val = val * z + 1.0 / c
+        return val
+
+    def cnexp(x, a, b):
+        z = -b * dt
+        small = z.abs() <= 0.5
+        taylor = x + dt * (a - b * x) * phi1(z)
+        eq = a / b
+        return torch.where(small, taylor, eq + (x - eq) * torch.exp(z))
+
+    am = AM1 * vtrap(-(v + 40.0))
+    bm = 4.0 * torch.exp(-(v + 65.0) / 18.0)
+    ah = AH1 * torch.exp(-(v + 65.0) / 20.0)
+    bh = 1.0 / (torch.exp(-(v + 35.0) / 10.0) + 1.0)
+    an = AN1 * vtrap(-(v + 55.0))
+    bn = 0.125 * torch.exp(-(v + 65.0) / 80.0)
+    m.copy_(cnexp(m, q10 * am, q10 * (am + bm)))
+    h.copy_(cnexp(h, q10 * ah, q10 * (ah + bh)))
+    n.copy_(cnexp(n, q10 * an, q10 * (an + bn)))
+    gna = d["gnabar"] * m * m * m * h
+    n2 = n * n
+    gk = d["gkbar"] * (n2 * n2)
+    G = d["gl"] + gna + gk
+    J = d["gl"] * d["el"] + gna * pop.ena + gk * pop.ek
+    gr, gl = d["g_right"], d["g_left"]
+    v_next = torch.cat([v[1:], v[-1:]])
+    v_prev = torch.cat([v[:1], v[:-1]])
+    fn = (J - G * v) * d["scale"] + (gr * (v_next - v) - gl * (v - v_prev))
+    if "field" in d:
+        t = torch.tensor(step * dt, dtype=torch.float64, device=v.device).to(pop.dtype)
+        on = (t >= d["ve_delay"]) & (t < d["ve_delay"] + d["ve_pw"])
+        amp = torch.where(on, d["ve_amp"], torch.zeros_like(d["ve_amp"]))
+        ve = d["field"] * amp[d["comp_cable"].long()]
+        ve_next = torch.cat([ve[1:], ve[-1:]])
+        ve_prev = torch.cat([ve[:1], ve[:-1]])
+        fn = fn + (gr * (ve_next - ve) - gl * (ve - ve_prev))
+    torch.mul(fn, dt_s, out=bands[3])
+    torch.sub(1.0, dt_s * ((-gr - gl) - G * d["scale"]), out=bands[1])
+    torch.mul(gl, -dt_s, out=bands[0])
+    torch.mul(gr, -dt_s, out=bands[2])
+    args = pop._args(1)
+    with torch.cuda.device(v.device):
+        rc = _lib.load().dgb_cable_solve_update(args, *(bands[i].data_ptr() for i in range(4)),
+                                                _lib.stream_ptr(v.device))
+    _lib.check(rc, "dgb_cable_solve_update")
+
+
 def _peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -790,6 +871,40 @@ def main():
                  "timesteps_timed": n_plain,
                  "what": "dgb_cable_assemble + dgb_cable_solve_update per timestep (2 launches)"}
 
+    # ---- the reference's eager per-step structure (one kernel per op) ----
+    eager = None
+    if not args.no_plain:
+        reset()
+        bands = torch.empty((4, pop.N), dtype=pop.dtype, device=dev)
+        for i in range(3):
+            eager_reference_step(pop, bands, i)
+        reset()
+        torch.cuda.synchronize()
+        n_eager = 50
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for i in range(n_eager):
+            eager_reference_step(pop, bands, i)
+        e1.record(st)
+        e1.synchronize()
+        ems = e0.elapsed_time(e1) / n_eager
+        # same first 20 timesteps through the eager structure and the 2-kernel path
+        reset()
+        for i in range(20):
+            eager_reference_step(pop, bands, i)
+        v_eager = pop.v.clone()
+        reset()
+        for i in range(20):
+            pop.step_plain(bands)
+        dv = float((pop.v - v_eager).abs().max())
+        eager = {"value": pop.N / (ems * 1e-3), "unit": METRIC, "ms_per_timestep": ems,
+                 "timesteps_timed": n_eager, "max_abs_dv_vs_plain_mv_20_steps": dv,
+                 "what": "the reference's eager step structure: one torch kernel per "
+                         "elementwise op of the gate advance, current frame and assembly, "
+                         "then the ragged solve + update kernel"}
+        reset()
+
     peak, peak_kind = _peaks()
     achieved = ALG_BYTES_PER_COMP_STEP * comp_steps / (ms * 1e-3) / 1e9
     line = {
@@ -818,6 +933,9 @@ def main():
     if plain is not None:
         line["plain_gpu"] = plain
         line["speedup_vs_plain_gpu"] = value / plain["value"]
+    if eager is not None:
+        line["plain_eager_reference_structure"] = eager
+        line["speedup_vs_plain_eager"] = value / eager["value"]
         line["gpu_launches"] += 0  # plain path runs outside the timed region
     if rank == 0 and not args.no_cpu:
         v, n_comp, secs, cores = cpu_baseline(args.sample, 200)

@@ -93,6 +93,8 @@ SIGNATURES = {
     "dgb_net_args_size": (ctypes.c_size_t, []),
     "dgb_mlp_gemm": (_INT, [_I32, _I32, _I32, _P, _I64, _I64, _P, _I64, _I64, _P, _I32, _P, _P,
                             _P, _P]),
+    "dgb_mlp_gemm_path": (_INT, [_I32, _I32, _I32, _P, _I64, _I64, _P, _I64, _I64]),
+    "dgb_mlp_gemm_status": (_INT, [_P]),
     "dgb_colsum": (_INT, [_I32, _I32, _P, _P, _P]),
     "dgb_adam": (_INT, [_I64, _I32, _I32, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float,
                         ctypes.c_float, ctypes.c_float, _I32, _P, _P, _P]),

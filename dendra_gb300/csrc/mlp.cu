@@ -1,8 +1,12 @@
 // BF16 tensor-core kernels for the threshold-proposal MLP (sm_103a).
 //
-// dgb_mlp_gemm: C[M,N] = A[M,K] B[K,N] with BF16 operands read through
-// arbitrary element strides (so X, X^T, W, W^T, dY are all served without
-// transposed copies), FP32 accumulation on mma.sync.m16n8k16, and a fused
+// dgb_mlp_gemm: C[M,N] = A[M,K] B[K,N] with BF16 operands and FP32
+// accumulation.  K-major products with M % 128 == 0, N % 256 == 0, K % 64 == 0
+// and K <= 256 (the 256-wide hidden layers) run on the tcgen05 + TMA kernel of
+// mlp_tc.cu; every other shape (K = 4 input layer, N = 1 output layer, the
+// strided weight-gradient products) runs on the kernel below, which reads
+// operands through arbitrary element strides (X, X^T, W, W^T, dY without
+// transposed copies) on mma.sync.m16n8k16.  Both apply the same fused
 // epilogue:
 //   EPI_PLAIN      out32 = acc
 //   EPI_BIAS       out32 = acc + bias
@@ -17,6 +21,13 @@
 namespace dgb {
 
 enum { EPI_PLAIN = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2, EPI_GELU_GRAD = 3 };
+
+// tcgen05 + TMA kernel for K-major products (mlp_tc.cu)
+bool mlp_gemm_tc_eligible(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam,
+                          int64_t sak, const void* B, int64_t sbk, int64_t sbn);
+int mlp_gemm_tc(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, const void* B,
+                int64_t sbn, const float* bias, int32_t epi, const float* aux, float* out32,
+                void* out16, cudaStream_t st);
 
 constexpr int TM = 64, TN = 64, TK = 32, PAD = 8;
 
@@ -187,6 +198,8 @@ extern "C" int dgb_mlp_gemm(int32_t M, int32_t N, int32_t K, const void* A, int6
   DGB_REQUIRE(epi != EPI_BIAS_GELU || (out32 && out16), "gelu epilogue needs out32 and out16");
   DGB_REQUIRE(epi != EPI_GELU_GRAD || (aux && out16), "gelu-grad epilogue needs aux and out16");
   DGB_REQUIRE(epi == EPI_GELU_GRAD || out32, "out32 must be non-null");
+  if (mlp_gemm_tc_eligible(M, N, K, A, sam, sak, B, sbk, sbn))
+    return mlp_gemm_tc(M, N, K, A, sam, B, sbn, bias, epi, aux, out32, out16, as_stream(stream));
   dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
   gemm_bf16_kernel<<<grid, 128, 0, as_stream(stream)>>>(
       M, N, K, (const __nv_bfloat16*)A, sam, sak, (const __nv_bfloat16*)B, sbk, sbn, bias, epi,

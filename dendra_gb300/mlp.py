@@ -5,7 +5,9 @@ log pulse width; standardised) to the log threshold (standardised).  Layers
 4 -> 256 -> 256 -> 256 -> 1 with exact GELU between them; BF16 weights and
 activations, FP32 accumulation, FP32 master weights trained with Adam.
 Every forward, backward and optimizer operation runs in the library's
-kernels (``dgb_mlp_gemm``, ``dgb_colsum``, ``dgb_adam``, ``dgb_mse_grad``).
+kernels (``dgb_mlp_gemm``, ``dgb_colsum``, ``dgb_adam``, ``dgb_mse_grad``);
+the 256-wide hidden-layer products (forward and dH) run on tcgen05 tensor
+cores fed by TMA whenever the batch is a multiple of 128 rows.
 
 The reference has no learned component: the proposal only narrows the
 bracket that the plain bisection (threshold.Thresholder) then confirms.
@@ -21,8 +23,9 @@ from . import _lib
 EPI_PLAIN, EPI_BIAS, EPI_BIAS_GELU, EPI_GELU_GRAD = 0, 1, 2, 3
 
 MLP_FLOPS_NOTE = ("inference FLOPs 2*(4*256 + 2*256*256 + 256) per sample over the forward "
-                  "time; mma.sync m16n8k16 bf16 tiles of 64x64, far from the tensor peak at "
-                  "these sizes (K = 4 and N = 1 layers, 256-wide hidden layers)")
+                  "time (4 launches): the two 256x256 layers on tcgen05 (128x256 tiles, TMA "
+                  "128-byte swizzle, TMEM accumulator), the K = 4 input and N = 1 output "
+                  "layers on mma.sync")
 
 
 def _gemm(M, N, K, A, sam, sak, B, sbk, sbn, *, bias=None, epi=EPI_PLAIN, aux=None, out32=None,
@@ -49,6 +52,8 @@ class BF16MLP:
             self.W.append(((torch.rand(k, n, generator=g) * 2 - 1) * bound).to(self.device))
             self.b.append(((torch.rand(n, generator=g) * 2 - 1) * bound).to(self.device))
         self.W16 = [w.to(torch.bfloat16) for w in self.W]
+        # K-major copies [N][K]: the forward's B operand for the tcgen05 path
+        self.Wt16 = [w.t().contiguous().to(torch.bfloat16) for w in self.W]
         self.opt = None
         self.x_mean = self.x_std = None
         self.y_mean, self.y_std = 0.0, 1.0
@@ -61,16 +66,17 @@ class BF16MLP:
         acts = [h]
         zs = []
         L = len(self.W)
-        for li, (W16, b) in enumerate(zip(self.W16, self.b)):
-            K, N = W16.shape
+        for li, (Wt16, b) in enumerate(zip(self.Wt16, self.b)):
+            N, K = Wt16.shape
             z = torch.empty(M, N, dtype=torch.float32, device=self.device)
+            # B[k, n] = W[k, n] read K-major from W^T (sbk = 1, sbn = K)
             if li < L - 1:
                 hn = torch.empty(M, N, dtype=torch.bfloat16, device=self.device)
-                _gemm(M, N, K, h, K, 1, W16, N, 1, bias=b, epi=EPI_BIAS_GELU, out32=z, out16=hn)
+                _gemm(M, N, K, h, K, 1, Wt16, 1, K, bias=b, epi=EPI_BIAS_GELU, out32=z, out16=hn)
                 h = hn
                 acts.append(h)
             else:
-                _gemm(M, N, K, h, K, 1, W16, N, 1, bias=b, epi=EPI_BIAS, out32=z)
+                _gemm(M, N, K, h, K, 1, Wt16, 1, K, bias=b, epi=EPI_BIAS, out32=z)
             zs.append(z)
         return (zs[-1], acts, zs) if keep else zs[-1]
 
@@ -114,11 +120,13 @@ class BF16MLP:
         for i, (p, g) in enumerate(zip(params, grads)):
             m1, m2 = self.opt[i]
             w16 = self.W16[i // 2] if i % 2 == 0 else None
+            wt16 = self.Wt16[i // 2] if i % 2 == 0 else None
             K, N = (p.shape if p.ndim == 2 else (1, p.numel()))
             with torch.cuda.device(self.device):
                 rc = L.dgb_adam(p.numel(), N, K, p.data_ptr(), g.data_ptr(), m1.data_ptr(),
                                 m2.data_ptr(), lr, 0.9, 0.999, 1e-8, step,
-                                None if w16 is None else w16.data_ptr(), None,
+                                None if w16 is None else w16.data_ptr(),
+                                None if wt16 is None else wt16.data_ptr(),
                                 _lib.stream_ptr(self.device))
             _lib.check(rc, "dgb_adam")
 

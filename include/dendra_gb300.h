@@ -458,12 +458,23 @@ int dgb_ring_enqueue(int dtype, void* ring, int64_t depth, int64_t width,
 /*
  * C[M,N] = A[M,K] B[K,N] with bf16 operands addressed by element strides
  * (A[m,k] at A + m*sam + k*sak, B[k,n] at B + k*sbk + n*sbn), fp32
- * accumulation on mma.sync m16n8k16, and the epilogue above; outputs are
- * row-major [M][N] (out16 bf16, out32 / bias / aux fp32).
+ * accumulation and the epilogue above; outputs are row-major [M][N] (out16
+ * bf16, out32 / bias / aux fp32).  K-major operands (sak == sbk == 1, row
+ * strides multiples of 8, 16-byte aligned) with M % 128 == 0, N % 256 == 0,
+ * K % 64 == 0 and K <= 256 run on tcgen05 tensor cores fed by TMA
+ * (dgb_mlp_gemm_path returns 1); other shapes on mma.sync m16n8k16.
  */
 int dgb_mlp_gemm(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak,
                  const void* B, int64_t sbk, int64_t sbn, const float* bias, int32_t epi,
                  const float* aux, float* out32, void* out16, void* stream);
+
+/* 1 if dgb_mlp_gemm runs these arguments on the tcgen05 kernel, else 0. */
+int dgb_mlp_gemm_path(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, int64_t sak,
+                      const void* B, int64_t sbk, int64_t sbn);
+
+/* Synchronises the stream and returns DGB_ETIMEOUT if a bounded wait inside
+   the last tcgen05 GEMM on this device gave up (its output is then invalid). */
+int dgb_mlp_gemm_status(void* stream);
 
 /* out[n] = sum over m of x[m][n] (fp32, fixed order). */
 int dgb_colsum(int32_t M, int32_t N, const float* x, float* out, void* stream);

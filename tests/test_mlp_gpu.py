@@ -5,7 +5,9 @@ import pytest
 import torch
 from scipy.special import erf
 
-from dendra_gb300.mlp import BF16MLP
+from dendra_gb300 import _lib
+from dendra_gb300.mlp import (EPI_BIAS, EPI_BIAS_GELU, EPI_GELU_GRAD, EPI_PLAIN, BF16MLP,
+                              _gemm)
 
 pytestmark = pytest.mark.gpu
 
@@ -44,10 +46,10 @@ def oracle_forward_backward(W16, b, x16, dy16):
     return zs[-1], dW, db
 
 
-def test_forward_and_gradients_match_oracle(cuda):
+@pytest.mark.parametrize("M", [300, 512])  # 300: mma.sync everywhere; 512: tcgen05 hidden layers
+def test_forward_and_gradients_match_oracle(cuda, M):
     mlp = BF16MLP(device=cuda, seed=1)
     rng = np.random.default_rng(0)
-    M = 300  # not a multiple of the 64-row tile
     x = torch.as_tensor(rng.standard_normal((M, 4)), dtype=torch.float32)
     x16 = x.to(torch.bfloat16).to(cuda)
     y, acts, zs = mlp.forward(x16, keep=True)
@@ -77,3 +79,42 @@ def test_training_fits_a_smooth_function(cuda):
     pred = mlp.predict(X[:2048])
     err = (pred.cpu() - y[:2048]).abs().mean()
     assert float(err) < 0.08
+
+
+@pytest.mark.parametrize("K", [64, 128, 256])
+@pytest.mark.parametrize("N", [256, 512])
+def test_tcgen05_gemm_matches_float64_and_the_mma_sync_path(cuda, K, N):
+    """K-major operands run on tcgen05 (TMA + TMEM); the same product with B
+    addressed N-major runs on mma.sync.  Both against a float64 product."""
+    L = _lib.load()
+    rng = np.random.default_rng(K + N)
+    M = 384
+    A = torch.as_tensor(rng.standard_normal((M, K)), dtype=torch.float32).to(torch.bfloat16).to(cuda)
+    W = torch.as_tensor(rng.standard_normal((K, N)) / np.sqrt(K),
+                        dtype=torch.float32).to(torch.bfloat16).to(cuda)
+    Wt = W.t().contiguous()
+    bias = torch.as_tensor(rng.standard_normal(N), dtype=torch.float32).to(cuda)
+    aux = torch.as_tensor(rng.standard_normal((M, N)), dtype=torch.float32).to(cuda)
+    assert L.dgb_mlp_gemm_path(M, N, K, A.data_ptr(), K, 1, Wt.data_ptr(), 1, K) == 1
+    assert L.dgb_mlp_gemm_path(M, N, K, A.data_ptr(), K, 1, W.data_ptr(), N, 1) == 0
+    acc = A.double().cpu().numpy() @ W.double().cpu().numpy()
+    z = acc + bias.double().cpu().numpy()
+    ref = {EPI_PLAIN: (acc, None), EPI_BIAS: (z, None), EPI_BIAS_GELU: (z, bf16(gelu(z))),
+           EPI_GELU_GRAD: (acc * gelu_grad(aux.double().cpu().numpy()),
+                           bf16(acc * gelu_grad(aux.double().cpu().numpy())))}
+    for epi, (r32, r16) in ref.items():
+        outs = []
+        for B, sbk, sbn in ((Wt, 1, K), (W, N, 1)):
+            o32 = torch.full((M, N), float("nan"), dtype=torch.float32, device=cuda)
+            o16 = torch.zeros((M, N), dtype=torch.bfloat16, device=cuda)
+            _gemm(M, N, K, A, K, 1, B, sbk, sbn, bias=bias if epi in (EPI_BIAS, EPI_BIAS_GELU)
+                  else None, epi=epi, aux=aux if epi == EPI_GELU_GRAD else None, out32=o32,
+                  out16=o16)
+            outs.append((o32.double().cpu().numpy(), o16.double().cpu().numpy()))
+        assert L.dgb_mlp_gemm_status(None) == 0
+        scale = np.abs(r32).max()
+        for o32, o16 in outs:  # tcgen05, then mma.sync
+            np.testing.assert_allclose(o32, r32, rtol=0, atol=2e-5 * scale, err_msg=str(epi))
+            if r16 is not None:
+                np.testing.assert_allclose(o16, r16, rtol=1e-2, atol=1e-2 * scale)
+        np.testing.assert_allclose(outs[0][0], outs[1][0], rtol=0, atol=2e-5 * scale)
