@@ -664,7 +664,8 @@ def bench_c5(args, world, rank, local):
             agree = float(((llb <= pub) & (plb <= lub))[fin].float().mean())
     value = batch / float(np.mean(learned_t))
     plain_v = batch / float(np.mean(plain_t))
-    # MLP inference roofline on the tensor pipe
+    # MLP inference (whole forward) and its dominant kernel, one 256x256
+    # hidden layer on tcgen05, timed alone with CUDA events
     feats = fibre_features(fibre_params(batch, seed=99))
     for _ in range(3):
         mlp.predict(feats)
@@ -676,8 +677,40 @@ def bench_c5(args, world, rank, local):
     e1.record()
     e1.synchronize()
     mlp_ms = e0.elapsed_time(e1) / 10
-    flops = MLP_FLOP_PER_SAMPLE * batch / (mlp_ms * 1e-3) / 1e12
-    peak = 1927.7
+    from dendra_gb300.mlp import EPI_BIAS_GELU, _gemm
+
+    h1 = torch.randn(batch, 256, device=dev).to(torch.bfloat16)
+    z = torch.empty(batch, 256, device=dev)
+    h2 = torch.empty(batch, 256, device=dev, dtype=torch.bfloat16)
+    Wt = mlp.Wt16[1]
+    layer = lambda: _gemm(batch, 256, 256, h1, 256, 1, Wt, 1, 256, bias=mlp.b[1],  # noqa: E731
+                          epi=EPI_BIAS_GELU, out32=z, out16=h2)
+    for _ in range(3):
+        layer()
+    e0.record()
+    for _ in range(20):
+        layer()
+    e1.record()
+    e1.synchronize()
+    layer_ms = e0.elapsed_time(e1) / 20
+    layer_tf = 2.0 * batch * 256 * 256 / (layer_ms * 1e-3) / 1e12
+    peak_tf = 1927.7
+    # the dominant kernel of the whole search: the fibre trial (persistent
+    # cable run), one full-horizon trial of the batch without early stop
+    pf = fibre_params(batch, seed=123)
+    popf = fibre_population(pf, device=dev)
+    ns = horizon_steps(pf["pw"].max())
+    popf._dev["ve_amp"].fill_(-0.05)
+    popf.run(10)
+    torch.cuda.synchronize()
+    e0.record()
+    popf.run(ns)
+    e1.record()
+    e1.synchronize()
+    trial_ms = e0.elapsed_time(e1)
+    trial_units = popf.N * ns
+    peak, peak_kind = _peaks()
+    achieved = ALG_BYTES_PER_COMP_STEP * trial_units / (trial_ms * 1e-3) / 1e9
     line = {
         "metric": "thresholds/s", "value": value, "unit": "thresholds/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(learned_t)) * 1e3,
@@ -690,9 +723,18 @@ def bench_c5(args, world, rank, local):
         "speedup_vs_plain_bisection": value / plain_v,
         "mlp": {"median_abs_log_err": float(err.median()), "margin": margin,
                 "bracket_agreement": agree, "train_s": train_s, "data_generation_s": gen_s,
-                "inference_ms": mlp_ms},
-        "roofline": {"bound": "tensor", "achieved": flops, "peak": peak, "unit": "TFLOP/s",
-                     "frac": flops / peak, "traffic": None, "note": MLP_FLOPS_NOTE},
+                "inference_ms": mlp_ms,
+                "inference_tflops": MLP_FLOP_PER_SAMPLE * batch / (mlp_ms * 1e-3) / 1e12,
+                "roofline": {"bound": "tensor", "kernel": "gemm_tc_kernel (one 256x256 layer)",
+                             "achieved": layer_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                             "frac": layer_tf / peak_tf, "kernel_ms": layer_ms,
+                             "note": MLP_FLOPS_NOTE + "; peak: measured cuBLAS bf16 burst"}},
+        "roofline": {"bound": "hbm", "kernel": "cable_run_kernel (fibre trials)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel_ms": trial_ms,
+                     "note": f"{ALG_BYTES_PER_COMP_STEP} algorithmic B per compartment-step "
+                             f"x {trial_units} compartment-steps of one full-horizon trial of "
+                             f"the batch; peak {peak_kind} copy bandwidth"},
     }
     if rank == 0 and not args.no_cpu:
         v, secs, cores = _c5_cpu(64)

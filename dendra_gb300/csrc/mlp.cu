@@ -25,6 +25,7 @@ enum { EPI_PLAIN = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2, EPI_GELU_GRAD = 3 };
 // tcgen05 + TMA kernel for K-major products (mlp_tc.cu)
 bool mlp_gemm_tc_eligible(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam,
                           int64_t sak, const void* B, int64_t sbk, int64_t sbn);
+bool mlp_gemm_tc_aligned(const void* bias, const void* aux, const void* out32, const void* out16);
 int mlp_gemm_tc(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, const void* B,
                 int64_t sbn, const float* bias, int32_t epi, const float* aux, float* out32,
                 void* out16, cudaStream_t st);
@@ -198,7 +199,8 @@ extern "C" int dgb_mlp_gemm(int32_t M, int32_t N, int32_t K, const void* A, int6
   DGB_REQUIRE(epi != EPI_BIAS_GELU || (out32 && out16), "gelu epilogue needs out32 and out16");
   DGB_REQUIRE(epi != EPI_GELU_GRAD || (aux && out16), "gelu-grad epilogue needs aux and out16");
   DGB_REQUIRE(epi == EPI_GELU_GRAD || out32, "out32 must be non-null");
-  if (mlp_gemm_tc_eligible(M, N, K, A, sam, sak, B, sbk, sbn))
+  if (mlp_gemm_tc_eligible(M, N, K, A, sam, sak, B, sbk, sbn) &&
+      mlp_gemm_tc_aligned(bias, aux, out32, out16))
     return mlp_gemm_tc(M, N, K, A, sam, B, sbn, bias, epi, aux, out32, out16, as_stream(stream));
   dim3 grid((N + TN - 1) / TN, (M + TM - 1) / TM);
   gemm_bf16_kernel<<<grid, 128, 0, as_stream(stream)>>>(

@@ -211,22 +211,55 @@ __global__ void __launch_bounds__(128, 1)
       float v[16];
       tmem_ld16(lane_base + col, v);
       const int n = n0 + col;
-      const int64_t o = (int64_t)m * N + n;
+      const int64_t o = (int64_t)m * N + n;  // multiple of 16: 16-byte vector accesses
+      if (epi == 1 || epi == 2) {
+        const float4* b4 = reinterpret_cast<const float4*>(bias + n);
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        float x = v[i];
-        if (epi == 1 || epi == 2) x += bias[n + i];
-        if (epi == 2) {
-          out32[o + i] = x;
-          out16[o + i] = __float2bfloat16(gelu_tc(x));
-        } else if (epi == 3) {
-          const float dz = x * gelu_grad_tc(aux[o + i]);
-          if (out32) out32[o + i] = dz;
-          out16[o + i] = __float2bfloat16(dz);
-        } else {
-          out32[o + i] = x;
-          if (out16) out16[o + i] = __float2bfloat16(x);
+        for (int q = 0; q < 4; ++q) {
+          const float4 b = b4[q];
+          v[4 * q] += b.x;
+          v[4 * q + 1] += b.y;
+          v[4 * q + 2] += b.z;
+          v[4 * q + 3] += b.w;
         }
+      }
+      float w[16];  // the value written to out16
+      if (epi == 2) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = gelu_tc(v[i]);
+      } else if (epi == 3) {
+        const float4* a4 = reinterpret_cast<const float4*>(aux + o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float4 a = a4[q];
+          v[4 * q] *= gelu_grad_tc(a.x);
+          v[4 * q + 1] *= gelu_grad_tc(a.y);
+          v[4 * q + 2] *= gelu_grad_tc(a.z);
+          v[4 * q + 3] *= gelu_grad_tc(a.w);
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = v[i];
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = v[i];
+      }
+      if (out32) {
+        float4* d4 = reinterpret_cast<float4*>(out32 + o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      }
+      if (out16) {
+        uint4 pk[2];
+        uint32_t* pw = reinterpret_cast<uint32_t*>(pk);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const __nv_bfloat162 h2 = __floats2bfloat162_rn(w[2 * i], w[2 * i + 1]);
+          pw[i] = *reinterpret_cast<const uint32_t*>(&h2);
+        }
+        uint4* d16 = reinterpret_cast<uint4*>(out16 + o);
+        d16[0] = pk[0];
+        d16[1] = pk[1];
       }
     }
   }
@@ -281,6 +314,11 @@ static int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t K, 
 }  // namespace tc
 
 // Whether dgb_mlp_gemm runs a product on the tcgen05 kernel.
+bool mlp_gemm_tc_aligned(const void* bias, const void* aux, const void* out32, const void* out16) {
+  auto al = [](const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; };
+  return al(bias) && al(aux) && al(out32) && al(out16);
+}
+
 bool mlp_gemm_tc_eligible(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam,
                           int64_t sak, const void* B, int64_t sbk, int64_t sbn) {
   return M > 0 && M % tc::BM == 0 && N > 0 && N % tc::BN == 0 && K > 0 && K % tc::BK == 0 &&
