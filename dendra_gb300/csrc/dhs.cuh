@@ -74,4 +74,77 @@ __device__ __forceinline__ void dhs_substitute(const TreeTopoT<I>& t, const T* g
   }
 }
 
+// Chain schedule of the same elimination.  A chain is a maximal unbranched
+// path: its top is the root or a child of a branch node, every node above its
+// bottom has exactly one child (the next node down), and its bottom is a leaf
+// or a branch node.  Chains are listed bottom -> top (nodes), chain after
+// chain (chain_ptr), grouped by level (level_ptr): a level-0 chain ends in a
+// leaf, a level-l chain ends in a branch node whose child chains all have
+// lower levels.  One lane eliminates a whole chain with the recurrence in
+// registers (no shared-memory round trip or warp synchronisation per node);
+// the warp synchronises once per level.  Every node performs exactly the
+// operations of dhs_eliminate / dhs_substitute, so the results are identical.
+template <typename I>
+struct ChainTopoT {
+  const I* nodes;      // [K]
+  const I* chain_ptr;  // [n_chains + 1]
+  const I* level_ptr;  // [n_levels + 1]
+  int32_t n_levels;
+};
+
+template <typename T, typename I>
+__device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const ChainTopoT<I>& c,
+                                                const T* g, T* sD, T* sB, int lane) {
+  for (int l = 0; l < c.n_levels; ++l) {
+    const int c1 = c.level_ptr[l + 1];
+    for (int ch = c.level_ptr[l] + lane; ch < c1; ch += 32) {
+      const int p = c.chain_ptr[ch], e = c.chain_ptr[ch + 1];
+      int i = c.nodes[p];
+      T D = sD[i], Bv = sB[i];
+      const int k1 = t.child_ptr[i + 1];
+      for (int k = t.child_ptr[i]; k < k1; ++k) {
+        const int cc = t.child_idx[k];
+        const T gc = g[cc];
+        const T Dc = sD[cc];
+        const T f = gc * (T(1) / (Dc + gc));
+        D = D + f * Dc;
+        Bv = Bv + f * sB[cc];
+      }
+      sD[i] = D;
+      sB[i] = Bv;
+      for (int q = p + 1; q < e; ++q) {  // up the chain: the single child is node i
+        const int j = c.nodes[q];
+        const T gc = g[i];
+        const T f = gc * (T(1) / (D + gc));
+        D = sD[j] + f * D;
+        Bv = sB[j] + f * Bv;
+        sD[j] = D;
+        sB[j] = Bv;
+        i = j;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <typename T, typename I>
+__device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const ChainTopoT<I>& c,
+                                                 const T* g, T* sD, T* sB, int lane) {
+  for (int l = c.n_levels - 1; l >= 0; --l) {
+    const int c1 = c.level_ptr[l + 1];
+    for (int ch = c.level_ptr[l] + lane; ch < c1; ch += 32) {
+      const int p = c.chain_ptr[ch], e = c.chain_ptr[ch + 1];
+      const I par = t.parent[c.nodes[e - 1]];
+      T xp = has_parent(par) ? sB[par] : T(0);
+      for (int q = e - 1; q >= p; --q) {  // down the chain from its top
+        const int j = c.nodes[q];
+        const T gj = g[j];
+        xp = (sB[j] + gj * xp) / (sD[j] + gj);
+        sB[j] = xp;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 }  // namespace dgb

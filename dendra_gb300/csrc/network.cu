@@ -31,6 +31,9 @@ struct NetArgsT {
   const int64_t* plan_node_ptr;
   const int64_t* plan_layer_off;
   const int32_t *parent, *order, *layer_ptr, *child_ptr, *child_idx;
+  // chain schedule (chain_nodes == nullptr: layer schedule)
+  const int64_t *plan_chain_off, *plan_clevel_off;
+  const int32_t *chain_nodes, *chain_ptr, *chain_level;
   // per node
   T* v;
   const T *area, *cm_dt, *a_geom, *gl, *el;
@@ -57,12 +60,13 @@ struct NetArgsT {
 
 // Shared memory of one warp (one cell): values sV, sD, sB, sG (axial
 // conductance) of kmax entries in T, then the cell's plan as 16-bit indices
-// (order, parent, child_ptr, child_idx, layer_ptr), staged once per window so
-// that the per-layer index chains of the DHS sweeps stay on chip.
+// (order or chain nodes, parent, child_ptr, child_idx, and layer_ptr or
+// chain_ptr + chain levels), staged once per window so that the index chains
+// of the DHS sweeps stay on chip.
 template <typename T>
 __host__ __device__ inline size_t net_warp_smem(int kmax) {
   const size_t vals = (size_t)4 * kmax * sizeof(T);
-  const size_t idx = (size_t)2 * (5 * (size_t)kmax + 2);
+  const size_t idx = (size_t)2 * (6 * (size_t)kmax + 3);
   return (vals + idx + 15) & ~(size_t)15;
 }
 
@@ -80,7 +84,8 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
   uint16_t* sParent = sOrder + kmax;
   uint16_t* sCptr = sParent + kmax;
   uint16_t* sCidx = sCptr + kmax + 1;
-  uint16_t* sLptr = sCidx + kmax;
+  uint16_t* sLptr = sCidx + kmax;      // layer_ptr, or chain_ptr then chain levels
+  const bool chains = A.chain_nodes != nullptr;
   for (int cell = blockIdx.x * wpb + warp; cell < A.n_cells; cell += gridDim.x * wpb) {
     const int64_t base = A.node_ptr[cell];
     const int K = (int)(A.node_ptr[cell + 1] - base);
@@ -98,8 +103,21 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
       sV[i] = A.v[base + i];
     }
     if (lane == 0) sCptr[K] = (uint16_t)A.child_ptr[pn + plan + K];
-    for (int l = lane; l <= L; l += 32) sLptr[l] = (uint16_t)A.layer_ptr[pl + l];
     TreeTopoT<uint16_t> t{sParent, sOrder, sLptr, sCptr, sCidx, K, L};
+    ChainTopoT<uint16_t> ct{sOrder, sLptr, sLptr, 0};
+    if (chains) {
+      // chain nodes replace the order; chain_ptr and the chain levels follow
+      const int64_t cp0 = A.plan_chain_off[plan], cl0 = A.plan_clevel_off[plan];
+      const int NC = (int)(A.plan_chain_off[plan + 1] - cp0 - 1);
+      const int NL = (int)(A.plan_clevel_off[plan + 1] - cl0 - 1);
+      uint16_t* sLev = sLptr + NC + 1;
+      for (int i = lane; i < K; i += 32) sOrder[i] = (uint16_t)A.chain_nodes[pn + i];
+      for (int c = lane; c <= NC; c += 32) sLptr[c] = (uint16_t)A.chain_ptr[cp0 + c];
+      for (int l = lane; l <= NL; l += 32) sLev[l] = (uint16_t)A.chain_level[cl0 + l];
+      ct = ChainTopoT<uint16_t>{sOrder, sLptr, sLev, NL};
+    } else {
+      for (int l = lane; l <= L; l += 32) sLptr[l] = (uint16_t)A.layer_ptr[pl + l];
+    }
     const int32_t* nsp = A.node_syn_ptr + base + cell;  // K+1 entries
     const int64_t s0 = A.syn_ptr[cell];
     const int S = (int)(A.syn_ptr[cell + 1] - s0);
@@ -180,8 +198,13 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
         sD[i] = cmdt[i] + mul_rn(G, ar);
       }
       __syncwarp();
-      dhs_eliminate<T, uint16_t>(t, sG, sD, sB, lane);
-      dhs_substitute<T, uint16_t>(t, sG, sD, sB, lane);
+      if (chains) {
+        chain_eliminate<T, uint16_t>(t, ct, sG, sD, sB, lane);
+        chain_substitute<T, uint16_t>(t, ct, sG, sD, sB, lane);
+      } else {
+        dhs_eliminate<T, uint16_t>(t, sG, sD, sB, lane);
+        dhs_substitute<T, uint16_t>(t, sG, sD, sB, lane);
+      }
       for (int i = lane; i < K; i += 32) sV[i] = sV[i] + sB[i];
       __syncwarp();
     }
@@ -240,6 +263,11 @@ static NetArgsT<T> net_typed(const dgb_net_args* a) {
   t.layer_ptr = a->forest.layer_ptr;
   t.child_ptr = a->forest.child_ptr;
   t.child_idx = a->forest.child_idx;
+  t.plan_chain_off = a->forest.plan_chain_off;
+  t.plan_clevel_off = a->forest.plan_clevel_off;
+  t.chain_nodes = a->forest.chain_nodes;
+  t.chain_ptr = a->forest.chain_ptr;
+  t.chain_level = a->forest.chain_level;
   t.v = (T*)a->v;
   t.area = (const T*)a->area;
   t.cm_dt = (const T*)a->cm_dt;
@@ -327,6 +355,9 @@ extern "C" int dgb_net_window(const dgb_net_args* a, void* stream) {
               "synapse arrays and ring must be non-null");
   DGB_REQUIRE(a->below && a->spike_bits && a->spike_count, "spike outputs must be non-null");
   DGB_REQUIRE(a->forest.max_k >= 1, "cells must have at least one compartment");
+  DGB_REQUIRE(!a->forest.chain_nodes || (a->forest.chain_ptr && a->forest.chain_level &&
+                                         a->forest.plan_chain_off && a->forest.plan_clevel_off),
+              "the chain schedule needs chain_ptr, chain_level and their plan offsets");
   DGB_REQUIRE(a->warps_per_block >= 0 && a->warps_per_block <= 4 && a->warps_per_block != 3,
               "warps_per_block must be 0 (default), 1, 2 or 4, got %d", a->warps_per_block);
   cudaStream_t st = as_stream(stream);

@@ -125,13 +125,15 @@ class TreeNetwork:
     def __init__(self, cells, syn_node, conn_pre, conn_post, conn_delay_ms, conn_weight, *,
                  dt=0.025, dtype=torch.float32, device="cuda", ra=100.0, cm=1.0, celsius=6.3,
                  v_init=-65.0, g_pas=0.001, e_pas=-70.0, tau1=0.5, tau2=5.0, e_syn=0.0,
-                 spk_thr=0.0, bg_steps=None, bg_weight=0.0, window=None):
+                 spk_thr=0.0, bg_steps=None, bg_weight=0.0, window=None, chains=True):
         self.dtype = dtype
         self.device = torch.device(device)
         self.dt = float(dt)
         self.n_cells = len(cells)
         dev = self.device
-        self.plan = ForestPlan([c.parent for c in cells], device=dev)
+        # chains=True: the window kernel eliminates one unbranched chain per
+        # lane (tree.build_chains); False: the depth-layer schedule.  Same results.
+        self.plan = ForestPlan([c.parent for c in cells], device=dev, chains=chains)
         node_ptr = self.plan.node_ptr
         N = int(node_ptr[-1])
         self.N = N

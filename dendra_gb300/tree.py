@@ -15,6 +15,10 @@ and adds the children CSR the deterministic kernel pulls from.  Solves:
 * :class:`ForestPlan` / :func:`dhs_solve_forest` — trees of different
   topologies packed into one launch (the role of dhs_solve_multi_cuda,
   triton/dhs_kernel_multi.py:831-888).
+* :func:`build_chains` — the chain schedule of the same elimination (one lane
+  per unbranched chain, one synchronisation per chain level instead of per
+  depth layer), the role the reference gives its tree-contraction solver for
+  deep trees (triton/tree_contraction.py, segment condensation).
 """
 
 from __future__ import annotations
@@ -208,6 +212,58 @@ def dhs_solve_cuda(d_mem, a_geom, b, parent_idx, order, layer_ptr, threads=32):
     return _DHSSolve.apply(d_mem, a_geom, b, topo)
 
 
+def build_chains(parent):
+    """Chain schedule of a tree: unbranched chains grouped by level.
+
+    A chain starts at the root or at a child of a branch node and runs down
+    through single-child nodes to a leaf or a branch node.  Returns
+    ``chain_nodes`` (K, int32: chains one after another, each listed from its
+    bottom node to its top), ``chain_ptr`` (n_chains + 1) and ``chain_level``
+    (n_levels + 1, offsets into the chains): level 0 holds the chains that end
+    in a leaf, level l the chains whose bottom's child chains all lie below l.
+    Within a level chains are sorted longest first (lanes take them in turn).
+    The elimination may then run level by level, one lane per chain, and the
+    back substitution in the reverse order (csrc/dhs.cuh chain_eliminate)."""
+    parent = [int(v) for v in parent]
+    K = len(parent)
+    children = [[] for _ in range(K)]
+    root = -1
+    for i, pp in enumerate(parent):
+        if pp < 0:
+            root = i
+        else:
+            children[pp].append(i)
+    chains, bottom_children = [], []
+    stack = [root]
+    while stack:
+        top = stack.pop()
+        nodes = [top]
+        i = top
+        while len(children[i]) == 1:
+            i = children[i][0]
+            nodes.append(i)
+        chains.append(nodes)
+        bottom_children.append(children[i])
+        stack.extend(children[i])
+    chain_of = np.empty(K, dtype=np.int64)
+    for c, nodes in enumerate(chains):
+        chain_of[nodes] = c
+    level = np.zeros(len(chains), dtype=np.int64)
+    for c in range(len(chains) - 1, -1, -1):  # child chains were created after their parent
+        kids = bottom_children[c]
+        if kids:
+            level[c] = 1 + max(level[chain_of[k]] for k in kids)
+    order = sorted(range(len(chains)), key=lambda c: (level[c], -len(chains[c]), c))
+    chain_nodes = np.concatenate([np.asarray(chains[c][::-1], dtype=np.int32) for c in order])
+    chain_ptr = np.zeros(len(chains) + 1, dtype=np.int32)
+    chain_ptr[1:] = np.cumsum([len(chains[c]) for c in order])
+    n_levels = int(level.max()) + 1 if len(chains) else 0
+    counts = np.bincount(level, minlength=n_levels)
+    chain_level = np.zeros(n_levels + 1, dtype=np.int32)
+    chain_level[1:] = np.cumsum(counts)
+    return chain_nodes, chain_ptr, chain_level
+
+
 class DgbForest(ctypes.Structure):
     _fields_ = [
         ("n_trees", ctypes.c_int32), ("max_k", ctypes.c_int32),
@@ -215,6 +271,9 @@ class DgbForest(ctypes.Structure):
         ("plan_node_ptr", ctypes.c_void_p), ("plan_layer_off", ctypes.c_void_p),
         ("parent", ctypes.c_void_p), ("order", ctypes.c_void_p), ("layer_ptr", ctypes.c_void_p),
         ("child_ptr", ctypes.c_void_p), ("child_idx", ctypes.c_void_p),
+        ("plan_chain_off", ctypes.c_void_p), ("plan_clevel_off", ctypes.c_void_p),
+        ("chain_nodes", ctypes.c_void_p), ("chain_ptr", ctypes.c_void_p),
+        ("chain_level", ctypes.c_void_p),
     ]
 
 
@@ -225,13 +284,21 @@ class ForestPlan:
     tree; trees may share a plan by passing ``plan_of``.
     """
 
-    def __init__(self, parents, device="cuda", threads=32, plan_of=None):
+    def __init__(self, parents, device="cuda", threads=32, plan_of=None, chains=True):
         self.n_plans = len(parents)
         node_counts = [len(p) for p in parents]
         plan_node_ptr = np.zeros(self.n_plans + 1, dtype=np.int64)
         plan_node_ptr[1:] = np.cumsum(node_counts)
         par, orders, layers, cptrs, cidxs, layer_off = [], [], [], [], [], [0]
+        cnodes, cptrs_c, clevels, chain_off, clevel_off = [], [], [], [0], [0]
         for p in parents:
+            if chains:
+                cn, cp, cl = build_chains(p)
+                cnodes.append(cn)
+                cptrs_c.append(cp)
+                clevels.append(cl)
+                chain_off.append(chain_off[-1] + cp.size)
+                clevel_off.append(clevel_off[-1] + cl.size)
             p = [int(v) for v in p]
             _, _, depth = build_morphology(p)
             order, layer_ptr = build_dhs_layers(depth, threads)
@@ -268,6 +335,12 @@ class ForestPlan:
             layer_ptr=t(layers, torch.int32), child_ptr=t(cptrs, torch.int32),
             child_idx=torch.as_tensor(cidx_all, dtype=torch.int32, device=dev).contiguous(),
         )
+        if chains:
+            self.tensors.update(
+                plan_chain_off=t(np.asarray(chain_off, dtype=np.int64), torch.int64),
+                plan_clevel_off=t(np.asarray(clevel_off, dtype=np.int64), torch.int64),
+                chain_nodes=t(cnodes, torch.int32), chain_ptr=t(cptrs_c, torch.int32),
+                chain_level=t(clevels, torch.int32))
         self.n_trees = int(plan_of_np.size)
         self.n_nodes = int(node_ptr[-1])
         self.max_k = int(tree_k.max()) if tree_k.size else 1

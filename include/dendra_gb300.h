@@ -318,6 +318,19 @@ typedef struct dgb_forest {
   const int32_t* layer_ptr;
   const int32_t* child_ptr;
   const int32_t* child_idx;
+  /* optional chain schedule (NULL chain_nodes: the layer schedule above).
+     Plan p's chain_nodes (K_p entries) start at plan_node_ptr[p]: unbranched
+     chains one after another, each from its bottom node to its top; its
+     chain_ptr (n_chains_p + 1 offsets into that block) at plan_chain_off[p];
+     its chain_level (n_levels_p + 1 offsets into its chains; level-0 chains
+     end in leaves, a level-l chain ends in a branch node whose child chains
+     have lower levels) at plan_clevel_off[p].  Same results as the layer
+     schedule; used by dgb_net_window. */
+  const int64_t* plan_chain_off;
+  const int64_t* plan_clevel_off;
+  const int32_t* chain_nodes;
+  const int32_t* chain_ptr;
+  const int32_t* chain_level;
 } dgb_forest;
 
 /*

@@ -59,3 +59,17 @@ def test_network_window_split_is_exact(cuda):
     rb = np.concatenate([_raster(b.run(n // 2), b.window), _raster(b.run(n // 2), b.window)])
     np.testing.assert_array_equal(ra, rb)
     torch.testing.assert_close(a.v, b.v, rtol=0, atol=0)
+
+
+def test_chain_and_layer_schedules_give_identical_runs(cuda):
+    from dendra_gb300.network import random_network
+
+    out = []
+    for chains in (True, False):
+        net, n = random_network(40, k_range=(100, 900), syn_per_cell=20, seed=12,
+                                dtype=torch.float32, device=cuda, t_stop_ms=25.0,
+                                rate_hz=40.0, chains=chains)
+        out.append((net.run(n), net.v.clone(), net.A.clone(), net.B.clone()))
+    for a, b in zip(*out):
+        assert torch.equal(a, b)
+    assert int(out[0][0].sum()) > 0
