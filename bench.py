@@ -331,7 +331,9 @@ def bench_c3(args, world, rank, local):
                    "compartments": net.N, "synapses": net.n_syn, "timesteps": n,
                    "window_steps": net.window, "l2": "flushed between timed steps",
                    "launch": f"one CUDA graph of {cap.launches} kernels per run",
-                   "warps_per_block": wpb, "autotune_ms": tune_ms},
+                   "threads_per_cell": wpb[0], "warps_per_block": wpb[1],
+                   "autotune_ms": None if tune_ms is None else
+                   {f"{k[0]}x{k[1]}": v for k, v in tune_ms.items()}},
         "eager_launch_ms_per_step": eager_ms,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,

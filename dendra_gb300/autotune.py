@@ -10,8 +10,9 @@ chosen by timing the candidates on the device:
 * the Thomas-versus-PCR split of the chunked tridiagonal solve (lanes per
   system 4 .. 32, i.e. rows per lane eliminated sequentially vs reduced by
   PCR) — ``tune_tridiag_lanes``;
-* cells per CTA of the network window kernel (``dgb_net_args.
-  warps_per_block``) — ``tune_network``.
+* threads per cell and warps per CTA of the network window kernel
+  (``dgb_net_args.threads_per_cell``, ``warps_per_block``: the tree-level
+  tiling) — ``tune_network``.
 
 Every candidate runs a short representative workload (warm-up, then the
 median of ``reps`` timings with CUDA events on the current stream).  Results
@@ -89,11 +90,12 @@ def tune(kind, key_parts, candidates, run, device, reps=3, force=False):
     with _lock:
         cache = _load_cache()
         if not force and key in cache:
-            return cache[key], None
+            v = cache[key]
+            return (tuple(v) if isinstance(v, list) else v), None
     timings = time_candidates(run, candidates, device, reps=reps)
     best = min(timings, key=timings.get)
     with _lock:
-        _store(key, best)
+        _store(key, list(best) if isinstance(best, tuple) else best)
     return best, timings
 
 
@@ -147,25 +149,29 @@ def tune_tridiag_lanes(B, K, dtype=torch.float32, device="cuda", candidates=(4, 
                 lambda n: tridiag_solve_lanes(a, b, c, d, lanes=n), device, reps, force)
 
 
-def tune_network(net, n_steps=None, candidates=(1, 2, 4), reps=2, force=False):
-    """Cells per CTA for ``net``'s window kernel; sets net.warps_per_block.
+def tune_network(net, n_steps=None, candidates=((32, 4), (64, 4), (128, 4), (128, 2)), reps=2,
+                 force=False):
+    """Threads per cell and warps per CTA for ``net``'s window kernel (the
+    tree-level tiling: how many threads share one cell's node, chain and
+    synapse loops); sets net.threads_per_cell and net.warps_per_block.
 
     Times ``n_steps`` (default two windows) from a reset network and leaves
-    the network reset."""
+    the network reset.  Returns ((threads_per_cell, warps_per_block), timings)."""
     n_steps = int(n_steps or 2 * net.window)
-    saved = net.warps_per_block
+    saved = (net.threads_per_cell, net.warps_per_block)
 
     def run(c):
-        net.warps_per_block = c
+        net.threads_per_cell, net.warps_per_block = c
         net.reset()
         net.run(n_steps)
 
-    parts = (str(net.dtype), net.n_cells, net.N, net.plan.max_k if hasattr(net.plan, "max_k")
-             else "-")
+    parts = (str(net.dtype), net.n_cells, net.N, net.plan.max_k)
     try:
-        best, timings = tune("net_window_wpb", parts, candidates, run, net.device, reps, force)
+        best, timings = tune("net_window_tiling", parts, candidates, run, net.device, reps,
+                             force)
     finally:
-        net.warps_per_block = saved
+        net.threads_per_cell, net.warps_per_block = saved
         net.reset()
-    net.warps_per_block = int(best)
-    return int(best), timings
+    best = tuple(int(x) for x in best)
+    net.threads_per_cell, net.warps_per_block = best
+    return best, timings

@@ -32,14 +32,27 @@ using TreeTopo = TreeTopoT<int32_t>;
 __device__ __forceinline__ bool has_parent(int32_t p) { return p >= 0; }
 __device__ __forceinline__ bool has_parent(uint16_t p) { return p != 0xFFFFu; }
 
+// Synchronisation of the threads that solve one tree: a warp, or a group of
+// warps meeting at named barrier `id` (1..15) with `count` threads.
+struct WarpSync {
+  __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+struct GroupSync {
+  int id, count;
+  __device__ __forceinline__ void operator()() const {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+  }
+};
+
+
 // sD, sB: shared arrays of K values holding d and b on entry; g: axial
 // conductances of this tree (global or shared).  On return sB holds x.
-template <typename T, typename I>
+template <typename T, typename I, int W = 32, class Sync = WarpSync>
 __device__ __forceinline__ void dhs_eliminate(const TreeTopoT<I>& t, const T* g, T* sD, T* sB,
-                                              int lane) {
+                                              int lane, Sync sync = Sync()) {
   for (int l = 0; l < t.L; ++l) {
     const int lo = t.layer_ptr[l], hi = t.layer_ptr[l + 1];
-    for (int o = lo + lane; o < hi; o += 32) {
+    for (int o = lo + lane; o < hi; o += W) {
       const int i = t.order[o];
       T D = sD[i], Bv = sB[i];
       const int c0 = t.child_ptr[i], c1 = t.child_ptr[i + 1];
@@ -54,23 +67,23 @@ __device__ __forceinline__ void dhs_eliminate(const TreeTopoT<I>& t, const T* g,
       sD[i] = D;
       sB[i] = Bv;
     }
-    __syncwarp();
+    sync();
   }
 }
 
-template <typename T, typename I>
+template <typename T, typename I, int W = 32, class Sync = WarpSync>
 __device__ __forceinline__ void dhs_substitute(const TreeTopoT<I>& t, const T* g, T* sD, T* sB,
-                                               int lane) {
+                                               int lane, Sync sync = Sync()) {
   for (int l = t.L - 1; l >= 0; --l) {
     const int lo = t.layer_ptr[l], hi = t.layer_ptr[l + 1];
-    for (int o = lo + lane; o < hi; o += 32) {
+    for (int o = lo + lane; o < hi; o += W) {
       const int i = t.order[o];
       const I p = t.parent[i];
       const T gi = g[i];
       const T xp = has_parent(p) ? sB[p] : T(0);
       sB[i] = (sB[i] + gi * xp) / (sD[i] + gi);
     }
-    __syncwarp();
+    sync();
   }
 }
 
@@ -92,12 +105,14 @@ struct ChainTopoT {
   int32_t n_levels;
 };
 
-template <typename T, typename I>
+// lane: index of the thread among the W threads solving this tree.
+template <typename T, typename I, int W = 32, class Sync = WarpSync>
 __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const ChainTopoT<I>& c,
-                                                const T* g, T* sD, T* sB, int lane) {
+                                                const T* g, T* sD, T* sB, int lane,
+                                                Sync sync = Sync()) {
   for (int l = 0; l < c.n_levels; ++l) {
     const int c1 = c.level_ptr[l + 1];
-    for (int ch = c.level_ptr[l] + lane; ch < c1; ch += 32) {
+    for (int ch = c.level_ptr[l] + lane; ch < c1; ch += W) {
       const int p = c.chain_ptr[ch], e = c.chain_ptr[ch + 1];
       int i = c.nodes[p];
       T D = sD[i], Bv = sB[i];
@@ -123,16 +138,17 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
         i = j;
       }
     }
-    __syncwarp();
+    sync();
   }
 }
 
-template <typename T, typename I>
+template <typename T, typename I, int W = 32, class Sync = WarpSync>
 __device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const ChainTopoT<I>& c,
-                                                 const T* g, T* sD, T* sB, int lane) {
+                                                 const T* g, T* sD, T* sB, int lane,
+                                                 Sync sync = Sync()) {
   for (int l = c.n_levels - 1; l >= 0; --l) {
     const int c1 = c.level_ptr[l + 1];
-    for (int ch = c.level_ptr[l] + lane; ch < c1; ch += 32) {
+    for (int ch = c.level_ptr[l] + lane; ch < c1; ch += W) {
       const int p = c.chain_ptr[ch], e = c.chain_ptr[ch + 1];
       const I par = t.parent[c.nodes[e - 1]];
       T xp = has_parent(par) ? sB[par] : T(0);
@@ -143,7 +159,7 @@ __device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const Ch
         sB[j] = xp;
       }
     }
-    __syncwarp();
+    sync();
   }
 }
 

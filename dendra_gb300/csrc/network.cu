@@ -17,6 +17,8 @@
 //      (dhs.cuh); v += dv.
 // dgb_net_enqueue then scatters the window's spikes into the delay ring,
 // one thread per target synapse, in connection then step order.
+#include <type_traits>
+
 #include "dhs.cuh"
 
 namespace dgb {
@@ -70,12 +72,28 @@ __host__ __device__ inline size_t net_warp_smem(int kmax) {
   return (vals + idx + 15) & ~(size_t)15;
 }
 
-template <typename T>
+// A group of TPC threads (one warp, or 2 or 4 warps meeting at a named
+// barrier) advances one cell; lane is the thread's index in the group.  Wider
+// groups spread every per-cell loop (nodes, chains of a level, synapses) over
+// more threads with the same shared memory per cell.
+template <typename T, int TPC>
+__device__ __forceinline__ void cell_sync(int group) {
+  if constexpr (TPC == 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(group + 1), "r"(TPC) : "memory");
+  }
+}
+
+template <typename T, int TPC>
 __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wpb = blockDim.x >> 5;
-  unsigned char* wbase = smem_raw + (size_t)warp * net_warp_smem<T>(kmax);
+  const int group = threadIdx.x / TPC, lane = threadIdx.x % TPC;
+  const int cpb = blockDim.x / TPC;  // cells in flight per block
+  unsigned char* wbase = smem_raw + (size_t)group * net_warp_smem<T>(kmax);
+  using Sync = typename std::conditional<TPC == 32, WarpSync, GroupSync>::type;
+  Sync sync;
+  if constexpr (TPC != 32) sync = Sync{group + 1, TPC};
   T* sV = reinterpret_cast<T*>(wbase);
   T* sD = sV + kmax;
   T* sB = sD + kmax;
@@ -86,14 +104,14 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
   uint16_t* sCidx = sCptr + kmax + 1;
   uint16_t* sLptr = sCidx + kmax;      // layer_ptr, or chain_ptr then chain levels
   const bool chains = A.chain_nodes != nullptr;
-  for (int cell = blockIdx.x * wpb + warp; cell < A.n_cells; cell += gridDim.x * wpb) {
+  for (int cell = blockIdx.x * cpb + group; cell < A.n_cells; cell += gridDim.x * cpb) {
     const int64_t base = A.node_ptr[cell];
     const int K = (int)(A.node_ptr[cell + 1] - base);
     const int plan = A.plan_of ? A.plan_of[cell] : cell;
     const int64_t pn = A.plan_node_ptr[plan], pl = A.plan_layer_off[plan];
     const int L = (int)(A.plan_layer_off[plan + 1] - pl - 1);
     // stage the plan (16-bit) and the axial conductances
-    for (int i = lane; i < K; i += 32) {
+    for (int i = lane; i < K; i += TPC) {
       sOrder[i] = (uint16_t)A.order[pn + i];
       const int32_t p = A.parent[pn + i];
       sParent[i] = p >= 0 ? (uint16_t)p : (uint16_t)0xFFFFu;
@@ -111,12 +129,12 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
       const int NC = (int)(A.plan_chain_off[plan + 1] - cp0 - 1);
       const int NL = (int)(A.plan_clevel_off[plan + 1] - cl0 - 1);
       uint16_t* sLev = sLptr + NC + 1;
-      for (int i = lane; i < K; i += 32) sOrder[i] = (uint16_t)A.chain_nodes[pn + i];
-      for (int c = lane; c <= NC; c += 32) sLptr[c] = (uint16_t)A.chain_ptr[cp0 + c];
-      for (int l = lane; l <= NL; l += 32) sLev[l] = (uint16_t)A.chain_level[cl0 + l];
+      for (int i = lane; i < K; i += TPC) sOrder[i] = (uint16_t)A.chain_nodes[pn + i];
+      for (int c = lane; c <= NC; c += TPC) sLptr[c] = (uint16_t)A.chain_ptr[cp0 + c];
+      for (int l = lane; l <= NL; l += TPC) sLev[l] = (uint16_t)A.chain_level[cl0 + l];
       ct = ChainTopoT<uint16_t>{sOrder, sLptr, sLev, NL};
     } else {
-      for (int l = lane; l <= L; l += 32) sLptr[l] = (uint16_t)A.layer_ptr[pl + l];
+      for (int l = lane; l <= L; l += TPC) sLptr[l] = (uint16_t)A.layer_ptr[pl + l];
     }
     const int32_t* nsp = A.node_syn_ptr + base + cell;  // K+1 entries
     const int64_t s0 = A.syn_ptr[cell];
@@ -135,14 +153,14 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
       count = A.spike_count[cell];
     }
     unsigned long long bits = 0ull;
-    __syncwarp();
+    cell_sync<T, TPC>(group);
     for (int s = 0; s < A.n_steps; ++s) {
       const int64_t g = A.step0 + s;
       const int64_t slot = (A.slot0 + s) % A.depth;
       T* row = A.ring + slot * A.n_syn + s0;
       // 1. deliver today's events (and clear the row)
       const bool bg = A.bg_bits && ((A.bg_bits[g * A.bg_words + (cell >> 6)] >> (cell & 63)) & 1ull);
-      for (int k = lane; k < S; k += 32) {
+      for (int k = lane; k < S; k += TPC) {
         T w = row[k];
         if (w != T(0)) {
           row[k] = T(0);
@@ -164,14 +182,14 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
         below = above ? 0 : 1;
       }
       // 3. state advance: synapse decay, soma gates at v_old
-      for (int k = lane; k < S; k += 32) {
+      for (int k = lane; k < S; k += TPC) {
         A.syn_A[s0 + k] = A.syn_A[s0 + k] * A.syn_decay_A[s0 + k];
         A.syn_B[s0 + k] = A.syn_B[s0 + k] * A.syn_decay_B[s0 + k];
       }
       if (lane == 0) hh_gates<T>(sV[0], A.q10, A.dt, m, h, nn);
-      __syncwarp();
+      cell_sync<T, TPC>(group);
       // 4. assemble the tree system into sD (main) and sB (rhs)
-      for (int i = lane; i < K; i += 32) {
+      for (int i = lane; i < K; i += TPC) {
         const T vi = sV[i];
         T G, J;
         if (i == 0) {
@@ -197,18 +215,18 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
         sB[i] = f;
         sD[i] = cmdt[i] + mul_rn(G, ar);
       }
-      __syncwarp();
+      cell_sync<T, TPC>(group);
       if (chains) {
-        chain_eliminate<T, uint16_t>(t, ct, sG, sD, sB, lane);
-        chain_substitute<T, uint16_t>(t, ct, sG, sD, sB, lane);
+        chain_eliminate<T, uint16_t, TPC>(t, ct, sG, sD, sB, lane, sync);
+        chain_substitute<T, uint16_t, TPC>(t, ct, sG, sD, sB, lane, sync);
       } else {
-        dhs_eliminate<T, uint16_t>(t, sG, sD, sB, lane);
-        dhs_substitute<T, uint16_t>(t, sG, sD, sB, lane);
+        dhs_eliminate<T, uint16_t, TPC>(t, sG, sD, sB, lane, sync);
+        dhs_substitute<T, uint16_t, TPC>(t, sG, sD, sB, lane, sync);
       }
-      for (int i = lane; i < K; i += 32) sV[i] = sV[i] + sB[i];
-      __syncwarp();
+      for (int i = lane; i < K; i += TPC) sV[i] = sV[i] + sB[i];
+      cell_sync<T, TPC>(group);
     }
-    for (int i = lane; i < K; i += 32) A.v[base + i] = sV[i];
+    for (int i = lane; i < K; i += TPC) A.v[base + i] = sV[i];
     if (lane == 0) {
       A.m[cell] = m;
       A.h[cell] = h;
@@ -217,7 +235,7 @@ __global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax
       A.spike_count[cell] = count;
       A.spike_bits[cell] = bits;
     }
-    __syncwarp();
+    cell_sync<T, TPC>(group);
   }
 }
 
@@ -310,24 +328,30 @@ static int net_window_t(const dgb_net_args* a, cudaStream_t st) {
     set_error("cells of more than 65,534 compartments are not supported (got %d)", kmax);
     return DGB_ERANGE;
   }
-  const size_t per_warp = net_warp_smem<T>(kmax);
-  int wpb = a->warps_per_block > 0 ? a->warps_per_block : 4;
-  while (wpb > 1 && wpb * per_warp > 227 * 1024) wpb >>= 1;
-  if (wpb * per_warp > 227 * 1024) {
+  const size_t per_cell = net_warp_smem<T>(kmax);
+  const int tpc = a->threads_per_cell > 0 ? a->threads_per_cell : 128;
+  // block: warps_per_block warps (at least one group), cells = threads / tpc,
+  // halved while the cells' shared memory exceeds 227 KB
+  int threads = 32 * (a->warps_per_block > 0 ? a->warps_per_block : 4);
+  if (threads < tpc) threads = tpc;
+  while (threads > tpc && (size_t)(threads / tpc) * per_cell > 227 * 1024) threads >>= 1;
+  const size_t smem = (size_t)(threads / tpc) * per_cell;
+  if (smem > 227 * 1024) {
     set_error("cell of %d compartments too large for shared memory", kmax);
     return DGB_ERANGE;
   }
-  const size_t smem = wpb * per_warp;
-  DGB_CUDA_CHECK(cudaFuncSetAttribute(net_window_kernel<T>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto kern = tpc == 128 ? net_window_kernel<T, 128>
+              : tpc == 64 ? net_window_kernel<T, 64> : net_window_kernel<T, 32>;
+  DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
   int per_sm = 0;
-  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, net_window_kernel<T>,
-                                                               wpb * 32, smem));
+  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
   if (per_sm < 1) per_sm = 1;
   int blocks = device_sm_count() * per_sm;
-  const int need = (a->n_cells + wpb - 1) / wpb;
+  const int cpb = threads / tpc;
+  const int need = (a->n_cells + cpb - 1) / cpb;
   if (blocks > need) blocks = need;
-  net_window_kernel<T><<<blocks, wpb * 32, smem, st>>>(net_typed<T>(a), kmax);
+  kern<<<blocks, threads, smem, st>>>(net_typed<T>(a), kmax);
   DGB_LAUNCH_CHECK();
   return DGB_OK;
 }
@@ -360,6 +384,10 @@ extern "C" int dgb_net_window(const dgb_net_args* a, void* stream) {
               "the chain schedule needs chain_ptr, chain_level and their plan offsets");
   DGB_REQUIRE(a->warps_per_block >= 0 && a->warps_per_block <= 4 && a->warps_per_block != 3,
               "warps_per_block must be 0 (default), 1, 2 or 4, got %d", a->warps_per_block);
+  DGB_REQUIRE(a->threads_per_cell == 0 || a->threads_per_cell == 32 ||
+                  a->threads_per_cell == 64 || a->threads_per_cell == 128,
+              "threads_per_cell must be 0 (default 128), 32, 64 or 128, got %d",
+              a->threads_per_cell);
   cudaStream_t st = as_stream(stream);
   if (a->dtype == DGB_F32) return net_window_t<float>(a, st);
   return net_window_t<double>(a, st);

@@ -55,7 +55,7 @@ class NetArgs(ctypes.Structure):
         ("bg_bits", ctypes.c_void_p), ("bg_words", ctypes.c_int64), ("bg_weight", ctypes.c_double),
         ("below", ctypes.c_void_p), ("spike_bits", ctypes.c_void_p),
         ("spike_count", ctypes.c_void_p),
-        ("warps_per_block", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("warps_per_block", ctypes.c_int32), ("threads_per_cell", ctypes.c_int32),
     ]
 
 
@@ -193,6 +193,9 @@ class TreeNetwork:
         # cells in flight per CTA of dgb_net_window (0 = library default);
         # dendra_gb300.autotune.tune_network picks it
         self.warps_per_block = 0
+        # threads advancing one cell (0 = library default 128); the autotuner's
+        # other knob
+        self.threads_per_cell = 0
         csr = TargetCSR(torch.as_tensor(post_sorted), self.n_syn)
         perm = csr.perm.numpy()
         self.conn = dict(
@@ -357,6 +360,7 @@ class TreeNetwork:
         a.below = self.below.data_ptr()
         a.spike_count = self.spike_count.data_ptr()
         a.warps_per_block = int(self.warps_per_block)
+        a.threads_per_cell = int(self.threads_per_cell)
         return a
 
     # -- oracle interchange ----------------------------------------------

@@ -386,10 +386,12 @@ typedef struct dgb_net_args {
   uint8_t* below;
   uint64_t* spike_bits;
   int32_t* spike_count;
-  /* cells in flight per CTA of dgb_net_window: 1, 2 or 4 (0 = 4), halved
-     while shared memory would exceed 227 KB.  The autotuner's knob. */
+  /* warps per CTA of dgb_net_window: 1, 2 or 4 (0 = 4), reduced while the
+     CTA's cells would need more than 227 KB of shared memory */
   int32_t warps_per_block;
-  int32_t reserved;  /* 0 */
+  /* threads advancing one cell: 32, 64 or 128 (0 = 128); identical results.
+     Both are the autotuner's knobs. */
+  int32_t threads_per_cell;
 } dgb_net_args;
 
 /* sizeof(dgb_net_args) as compiled (for foreign-language mirrors). */
