@@ -86,7 +86,8 @@ __device__ __forceinline__ void cell_sync(int group) {
 }
 
 template <typename T, int TPC>
-__global__ void __launch_bounds__(128) net_window_kernel(NetArgsT<T> A, int kmax) {
+__global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetArgsT<T> A,
+                                                                          int kmax) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int group = threadIdx.x / TPC, lane = threadIdx.x % TPC;
   const int cpb = blockDim.x / TPC;  // cells in flight per block
@@ -334,14 +335,18 @@ static int net_window_t(const dgb_net_args* a, cudaStream_t st) {
   // halved while the cells' shared memory exceeds 227 KB
   int threads = 32 * (a->warps_per_block > 0 ? a->warps_per_block : 4);
   if (threads < tpc) threads = tpc;
+  const int max_threads = tpc > 128 ? tpc : 128;  // the instantiation's launch bound
+  if (threads > max_threads) threads = max_threads;
   while (threads > tpc && (size_t)(threads / tpc) * per_cell > 227 * 1024) threads >>= 1;
   const size_t smem = (size_t)(threads / tpc) * per_cell;
   if (smem > 227 * 1024) {
     set_error("cell of %d compartments too large for shared memory", kmax);
     return DGB_ERANGE;
   }
-  auto kern = tpc == 128 ? net_window_kernel<T, 128>
-              : tpc == 64 ? net_window_kernel<T, 64> : net_window_kernel<T, 32>;
+  auto kern = tpc == 256   ? net_window_kernel<T, 256>
+              : tpc == 128 ? net_window_kernel<T, 128>
+              : tpc == 64  ? net_window_kernel<T, 64>
+                           : net_window_kernel<T, 32>;
   DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   int per_sm = 0;
@@ -382,11 +387,13 @@ extern "C" int dgb_net_window(const dgb_net_args* a, void* stream) {
   DGB_REQUIRE(!a->forest.chain_nodes || (a->forest.chain_ptr && a->forest.chain_level &&
                                          a->forest.plan_chain_off && a->forest.plan_clevel_off),
               "the chain schedule needs chain_ptr, chain_level and their plan offsets");
-  DGB_REQUIRE(a->warps_per_block >= 0 && a->warps_per_block <= 4 && a->warps_per_block != 3,
-              "warps_per_block must be 0 (default), 1, 2 or 4, got %d", a->warps_per_block);
+  DGB_REQUIRE(a->warps_per_block == 0 || a->warps_per_block == 1 || a->warps_per_block == 2 ||
+                  a->warps_per_block == 4 || a->warps_per_block == 8,
+              "warps_per_block must be 0 (default), 1, 2, 4 or 8, got %d", a->warps_per_block);
   DGB_REQUIRE(a->threads_per_cell == 0 || a->threads_per_cell == 32 ||
-                  a->threads_per_cell == 64 || a->threads_per_cell == 128,
-              "threads_per_cell must be 0 (default 128), 32, 64 or 128, got %d",
+                  a->threads_per_cell == 64 || a->threads_per_cell == 128 ||
+                  a->threads_per_cell == 256,
+              "threads_per_cell must be 0 (default 128), 32, 64, 128 or 256, got %d",
               a->threads_per_cell);
   cudaStream_t st = as_stream(stream);
   if (a->dtype == DGB_F32) return net_window_t<float>(a, st);

@@ -386,10 +386,11 @@ typedef struct dgb_net_args {
   uint8_t* below;
   uint64_t* spike_bits;
   int32_t* spike_count;
-  /* warps per CTA of dgb_net_window: 1, 2 or 4 (0 = 4), reduced while the
+  /* warps per CTA of dgb_net_window: 1, 2, 4 or 8 (0 = 4; at most
+     max(threads_per_cell, 128) threads), reduced while the
      CTA's cells would need more than 227 KB of shared memory */
   int32_t warps_per_block;
-  /* threads advancing one cell: 32, 64 or 128 (0 = 128); identical results.
+  /* threads advancing one cell: 32, 64, 128 or 256 (0 = 128); identical results.
      Both are the autotuner's knobs. */
   int32_t threads_per_cell;
 } dgb_net_args;
