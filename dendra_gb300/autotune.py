@@ -149,7 +149,8 @@ def tune_tridiag_lanes(B, K, dtype=torch.float32, device="cuda", candidates=(4, 
                 lambda n: tridiag_solve_lanes(a, b, c, d, lanes=n), device, reps, force)
 
 
-def tune_network(net, n_steps=None, candidates=((32, 4), (64, 4), (128, 4), (256, 8)), reps=2,
+def tune_network(net, n_steps=None, candidates=((32, 4), (64, 4), (128, 4), (256, 8), (512, 8)),
+                 reps=2,
                  force=False):
     """Threads per cell and warps per CTA for ``net``'s window kernel (the
     tree-level tiling: how many threads share one cell's node, chain and

@@ -343,7 +343,8 @@ static int net_window_t(const dgb_net_args* a, cudaStream_t st) {
     set_error("cell of %d compartments too large for shared memory", kmax);
     return DGB_ERANGE;
   }
-  auto kern = tpc == 256   ? net_window_kernel<T, 256>
+  auto kern = tpc == 512   ? net_window_kernel<T, 512>
+              : tpc == 256 ? net_window_kernel<T, 256>
               : tpc == 128 ? net_window_kernel<T, 128>
               : tpc == 64  ? net_window_kernel<T, 64>
                            : net_window_kernel<T, 32>;
@@ -392,8 +393,8 @@ extern "C" int dgb_net_window(const dgb_net_args* a, void* stream) {
               "warps_per_block must be 0 (default), 1, 2, 4 or 8, got %d", a->warps_per_block);
   DGB_REQUIRE(a->threads_per_cell == 0 || a->threads_per_cell == 32 ||
                   a->threads_per_cell == 64 || a->threads_per_cell == 128 ||
-                  a->threads_per_cell == 256,
-              "threads_per_cell must be 0 (default 128), 32, 64, 128 or 256, got %d",
+                  a->threads_per_cell == 256 || a->threads_per_cell == 512,
+              "threads_per_cell must be 0 (default 128), 32, 64, 128, 256 or 512, got %d",
               a->threads_per_cell);
   cudaStream_t st = as_stream(stream);
   if (a->dtype == DGB_F32) return net_window_t<float>(a, st);

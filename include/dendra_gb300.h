@@ -390,7 +390,7 @@ typedef struct dgb_net_args {
      max(threads_per_cell, 128) threads), reduced while the
      CTA's cells would need more than 227 KB of shared memory */
   int32_t warps_per_block;
-  /* threads advancing one cell: 32, 64, 128 or 256 (0 = 128); identical results.
+  /* threads advancing one cell: 32, 64, 128, 256 or 512 (0 = 128); identical results.
      Both are the autotuner's knobs. */
   int32_t threads_per_cell;
 } dgb_net_args;

@@ -71,9 +71,9 @@ def test_network_graph_replay_matches_the_eager_run(cuda):
 def test_network_tiling_choice_is_result_neutral(cuda):
     net, n = _net(cuda)
     best, timings = tune_network(net, force=True)
-    assert best in timings and len(timings) == 4
+    assert best in timings and len(timings) == 5
     rasters = []
-    for tpc, wpb in ((32, 1), (32, 4), (64, 2), (64, 4), (128, 4), (128, 2), (256, 8)):
+    for tpc, wpb in ((32, 1), (32, 4), (64, 2), (64, 4), (128, 4), (128, 2), (256, 8), (512, 8)):
         net.threads_per_cell, net.warps_per_block = tpc, wpb
         net.reset()
         rasters.append((net.run(n), net.v.clone(), net.A.clone(), net.ring.clone()))
