@@ -542,6 +542,100 @@ def bench_c4(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+BT_BYTES_PER_ROW = 84  # float32 block row: main 36 B + lower/upper 24 B + rhs 12 B + x 12 B
+
+
+def _bt_system(B, K, seed, dtype):
+    import torch
+
+    g = torch.Generator().manual_seed(seed)
+    lower = -torch.rand(B, K - 1, 3, generator=g)
+    upper = -torch.rand(B, K - 1, 3, generator=g)
+    main = 0.3 * torch.randn(B, K, 3, 3, generator=g)
+    main = main + torch.diag_embed(3.0 + torch.rand(B, K, 3, generator=g))
+    rhs = torch.randn(B, K, 3, generator=g)
+    return [t.to(dtype) for t in (lower, main, upper, rhs)]
+
+
+def bench_bt(args, world, rank, local):
+    """3x3 block-tridiagonal solves of multi-layer extracellular cables
+    (intracellular v and two extracellular shells per compartment): 16,384
+    systems of 201 block rows, float32.  One bench step = one batched solve."""
+    import torch
+
+    import oracle
+    from dendra_gb300.solvers import _block3
+
+    B = args.cables
+    K = args.timesteps or 201
+    units = B * K
+    metric = "compartment-solves/s"
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    host = _bt_system(B, K, 7 + rank, torch.float32)
+    lower, main, upper, rhs = (t.to(dev) for t in host)
+    for _ in range(max(3, args.warmup)):
+        _block3(lower, main, upper, rhs, False)
+    torch.cuda.synchronize()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            x = _block3(lower, main, upper, rhs, False)
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    pinned = [t.pin_memory() for t in host]
+    out = torch.empty_like(host[3]).pin_memory()
+    h2d = sum(t.numel() * 4 for t in pinned)
+    d2h = out.numel() * 4
+    dbuf = [torch.empty_like(t, device=dev) for t in host]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for d_, h_ in zip(dbuf, pinned):
+            d_.copy_(h_, non_blocking=True)
+        out.copy_(_block3(*dbuf, False), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    peak, peak_kind = _peaks()
+    achieved = BT_BYTES_PER_ROW * units / (ms * 1e-3) / 1e9
+    n_cpu = min(1024, B)
+    t0 = time.perf_counter()
+    ref = oracle.block3_solve(*(t[:n_cpu].numpy() for t in host))
+    cpu_s = time.perf_counter() - t0
+    err = float(np.abs(x[:n_cpu].cpu().numpy() - ref).max())
+    line = {
+        "metric": metric, "value": units / (ms * 1e-3), "unit": metric, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "bt-3x3-block-tridiagonal", "systems": B, "K": K,
+                   "l2": "flushed between timed steps"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel": "block3_kernel",
+                     "note": f"{BT_BYTES_PER_ROW} algorithmic B per float32 block row (read "
+                             "main, bands and rhs, write x); the inverse/rhs scratch "
+                             f"(48 B per row each way) stays in L2; peak {peak_kind}"},
+        "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps * 2,
+        "clocks": clocks.summary(),
+        "max_abs_diff_vs_oracle_f32": err,
+        "cpu_baseline": {"value": n_cpu * K / cpu_s, "unit": metric,
+                         "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"{n_cpu} systems x {K} block rows, float32 block Thomas"},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 MLP_FLOP_PER_SAMPLE = 2 * (4 * 256 + 256 * 256 + 256 * 256 + 256 * 1)
 
 
@@ -760,10 +854,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "bt"],
                     help="c2: uneven cable population (default); c3: branched-cell network; "
                          "c4: adjoint gradient of a trace fit; "
-                         "c5: learned threshold proposal vs plain bisection")
+                         "c5: learned threshold proposal vs plain bisection; "
+                         "bt: 3x3 block-tridiagonal (multi-layer extracellular) solves")
     ap.add_argument("--train", type=int, default=200000, help="c5 training thresholds")
     ap.add_argument("--cables", type=int, default=16384,
                     help="cables per rank (a smaller case for profiling)")
@@ -774,6 +869,8 @@ def main():
         return bench_c3(args, world, rank, local)
     if args.workload == "c4":
         return bench_c4(args, world, rank, local)
+    if args.workload == "bt":
+        return bench_bt(args, world, rank, local)
     if args.workload == "c5":
         return bench_c5(args, world, rank, local)
     if args.impl == "reference":

@@ -5,6 +5,8 @@ Drop-ins for the solver objects ``_bwd_euler_ub._select_solver`` installs as
 
 * :func:`thomas_solve_cuda_t` — replaces triton/t_kernel_thomas.py:218-232
 * :func:`pcr_solve_cuda_t`    — replaces triton/pcr_kernel_thomas.py:199-226
+* :func:`thomas_solve_cuda_bt` — the 3x3 block solver ``_bwd_euler_bt`` selects
+  on CUDA (implicit.py:905-950), replaces triton/bt_kernel.py:195-298
 
 Both take ``a (B,K-1), b (B,K), c (B,K-1), d (B,K)`` CUDA tensors of one float
 dtype and return a fresh ``x (B,K)``.  Gradients follow the reference's
@@ -138,3 +140,72 @@ def tridiag_solve_lanes(a, b, c, d, lanes: int):
 # The increment-RHS contract is granted to these solver identities only
 # (mirrors _BWD_EULER_INCREMENT_SOLVERS, integrators/implicit.py:59-82).
 INCREMENT_SOLVERS = (thomas_solve_cuda_t, pcr_solve_cuda_t)
+
+
+# ---------------------------------------------------------------------------
+# 3x3 block-tridiagonal systems (multi-layer extracellular cables)
+# ---------------------------------------------------------------------------
+def validate_block_tridiagonal(lower, main, upper, rhs):
+    """Contract of a batched 3x3 block-tridiagonal solve (triton/_contracts.py:162-196)."""
+    named = (("lower", lower), ("main", main), ("upper", upper), ("rhs", rhs))
+    for name, t in named:
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{name} must be a torch.Tensor")
+    if rhs.ndim != 3 or rhs.shape[-1] != 3:
+        raise ValueError(f"rhs must have shape (B, K, 3), got {tuple(rhs.shape)}")
+    batch, size, _ = map(int, rhs.shape)
+    if batch < 1 or size < 1:
+        raise ValueError("B and K must both be >= 1")
+    band = (batch, size - 1, 3)
+    if tuple(lower.shape) != band:
+        raise ValueError(f"lower must have shape {band}, got {tuple(lower.shape)}")
+    if tuple(upper.shape) != band:
+        raise ValueError(f"upper must have shape {band}, got {tuple(upper.shape)}")
+    expected_main = (batch, size, 3, 3)
+    if tuple(main.shape) != expected_main:
+        raise ValueError(f"main must have shape {expected_main}, got {tuple(main.shape)}")
+    _validate_float_group(named)
+    return batch, size
+
+
+def _block3(lower, main, upper, rhs, transpose):
+    B, K = rhs.shape[:2]
+    lower, main, upper, rhs = (t.contiguous() for t in (lower, main, upper, rhs))
+    x = torch.empty_like(rhs)
+    L = _lib.load()
+    code = _lib.dtype_code(rhs.dtype)
+    work = torch.empty(L.dgb_block3_work_size(code, B, K), dtype=torch.uint8, device=rhs.device)
+    with torch.cuda.device(rhs.device):
+        rc = L.dgb_block3_solve(code, B, K, lower.data_ptr(), main.data_ptr(), upper.data_ptr(),
+                                rhs.data_ptr(), x.data_ptr(), work.data_ptr(), int(transpose),
+                                _lib.stream_ptr(rhs.device))
+    _lib.check(rc, "dgb_block3_solve")
+    return x
+
+
+class _Block3Solve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, lower, main, upper, rhs):
+        x = _block3(lower, main, upper, rhs, False)
+        ctx.save_for_backward(lower, main, upper, x)
+        return x
+
+    @staticmethod
+    def backward(ctx, grad_x):
+        # adjoint solve A^T g = grad_x on the kernel (transposed blocks,
+        # exchanged bands), then the outer products of triton/bt_kernel.py:268-290
+        lower, main, upper, x = ctx.saved_tensors
+        g = _block3(lower, main, upper, grad_x.contiguous(), True)
+        grad_main = -(g.unsqueeze(-1) * x.unsqueeze(-2))
+        grad_upper = -(g[:, :-1] * x[:, 1:])
+        grad_lower = -(g[:, 1:] * x[:, :-1])
+        return grad_lower, grad_main, grad_upper, g
+
+
+def thomas_solve_cuda_bt(lower, main, upper, rhs):
+    """Drop-in for the reference's thomas_solve_cuda_bt (triton/bt_kernel.py:295-298).
+
+    lower, upper: (B, K-1, 3) diagonals of the off-diagonal blocks; main:
+    (B, K, 3, 3); rhs: (B, K, 3).  Returns x (B, K, 3); differentiable."""
+    validate_block_tridiagonal(lower, main, upper, rhs)
+    return _Block3Solve.apply(lower, main, upper, rhs)

@@ -17,6 +17,9 @@
  *                             (pcr_solve_cuda_t); solver callable selected in
  *                             integrators/implicit.py:364-440, called at :647
  *   dgb_tridiag_solve_transpose  ThomasSolve.backward, t_kernel_thomas.py:147-189
+ *   dgb_block3_solve          thomas_solve_cuda_bt, triton/bt_kernel.py:195-298
+ *                             (3x3 block Thomas of the multi-layer extracellular
+ *                             integrator, implicit.py:669-1136)
  *   dgb_cable_run             one Population.run over an unbranched HH cable
  *                             population: models/core.py:4555-4628 driving
  *                             integrators/core.py:769-834 and
@@ -105,6 +108,25 @@ int dgb_tridiag_solve_lanes(int dtype, int64_t B, int64_t K, const void* a,
 int dgb_tridiag_solve_transpose(int dtype, int64_t B, int64_t K,
                                 const void* a, const void* b, const void* c,
                                 const void* g, void* y, void* stream);
+
+/*
+ * Batched block-tridiagonal solve with 3x3 main blocks and diagonal
+ * off-diagonal blocks (multi-layer extracellular cables: intracellular v and
+ * two extracellular shells per compartment).  Row k of system b:
+ *   diag(lower[k-1]) x[k-1] + main[k] x[k] + diag(upper[k]) x[k+1] = rhs[k]
+ *   lower, upper: (B, K-1, 3); main: (B, K, 3, 3) row-major; rhs, x: (B, K, 3).
+ * Block Thomas with 3x3 inverses by cofactors, one thread per system.
+ * work: caller scratch of dgb_block3_work_size(dtype, B, K) bytes.
+ * transpose = 1 solves A^T y = rhs (the adjoint solve).  x must not alias rhs.
+ * Replaces thomas_solve_cuda_bt (triton/bt_kernel.py:195-262), selected by
+ * _bwd_euler_bt._select_solver (integrators/implicit.py:905-950).
+ */
+int dgb_block3_solve(int dtype, int64_t B, int64_t K, const void* lower,
+                     const void* main_blocks, const void* upper, const void* rhs,
+                     void* x, void* work, int32_t transpose, void* stream);
+
+/* Scratch bytes dgb_block3_solve needs: B * K * 12 values of dtype. */
+size_t dgb_block3_work_size(int dtype, int64_t B, int64_t K);
 
 /*
  * Arguments of a multi-step unbranched Hodgkin–Huxley cable run.

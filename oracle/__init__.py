@@ -11,7 +11,8 @@ reference implementation itself (``tests/golden/make_golden.py``), and
 
 Layers:
   * ``oracle.c`` / ``oracle_impl.h``  float64 and float32 C restatements of the
-    HH rates, cnexp, the backward-Euler cable update, Thomas, PCR, DHS and the
+    HH rates, cnexp, the backward-Euler cable update, Thomas, PCR, 3x3 block
+    Thomas, DHS and the
     branched-cell network step (``orc_net_run``: Exp2Syn delivery, soma HH,
     tree solve, delay ring), and the reverse mode of the cable update
     (``cable_grad``: full state tape, transposed Thomas solve, gate partials
@@ -32,6 +33,7 @@ from .core import (  # noqa: F401
     cnexp,
     thomas,
     pcr,
+    block3_solve,
     cable_run,
     cable_grad,
     dhs_solve,

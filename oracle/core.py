@@ -71,6 +71,7 @@ def _declare(L):
             [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
             + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P, _I32, _P, _P]
         )
+        getattr(L, "orc_block3_thomas" + sfx).argtypes = [_I64, _I64, _P, _P, _P, _P, _P]
         getattr(L, "orc_cable_grad" + sfx).argtypes = (
             [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
             + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _I32] + [_P] * 8
@@ -156,6 +157,18 @@ def pcr(a, b, c, d):
     f = getattr(lib(), "orc_pcr" + _sfx(dtype))
     for i in range(B):
         f(K, _ptr(a[i]), _ptr(b[i]), _ptr(c[i]), _ptr(d[i]), _ptr(x[i]))
+    return x
+
+
+def block3_solve(lower, main, upper, rhs):
+    """Block Thomas on (B, K) systems of 3x3 blocks (diagonal off-diagonal blocks)."""
+    dtype = rhs.dtype
+    lower, main, upper, rhs = (np.ascontiguousarray(t, dtype=dtype)
+                               for t in (lower, main, upper, rhs))
+    B, K = rhs.shape[:2]
+    x = np.empty_like(rhs)
+    getattr(lib(), "orc_block3_thomas" + _sfx(dtype))(
+        B, K, _ptr(lower), _ptr(main), _ptr(upper), _ptr(rhs), _ptr(x))
     return x
 
 

@@ -211,6 +211,72 @@ void F(orc_pcr)(int64_t K, const REAL* a_in, const REAL* b_in, const REAL* c_in,
   free(buf);
 }
 
+/* 3x3 inverse by cofactors over the determinant. */
+static void F(inv3)(const REAL* a, REAL* v) {
+  REAL c0 = a[4] * a[8] - a[5] * a[7];
+  REAL c3 = a[5] * a[6] - a[3] * a[8];
+  REAL c6 = a[3] * a[7] - a[4] * a[6];
+  REAL det = a[0] * c0 + a[1] * c3 + a[2] * c6;
+  REAL r = (REAL)1 / det;
+  v[0] = c0 * r;
+  v[1] = (a[2] * a[7] - a[1] * a[8]) * r;
+  v[2] = (a[1] * a[5] - a[2] * a[4]) * r;
+  v[3] = c3 * r;
+  v[4] = (a[0] * a[8] - a[2] * a[6]) * r;
+  v[5] = (a[2] * a[3] - a[0] * a[5]) * r;
+  v[6] = c6 * r;
+  v[7] = (a[1] * a[6] - a[0] * a[7]) * r;
+  v[8] = (a[0] * a[4] - a[1] * a[3]) * r;
+}
+
+/* Block Thomas for 3x3 main blocks and diagonal off-diagonal blocks, the
+ * algorithm of the reference's thomas_bt3_kernel (triton/bt_kernel.py:38-170):
+ *   P_k = main_k - diag(lower_{k-1}) P_{k-1}^{-1} diag(upper_{k-1}),
+ *   r_k = rhs_k - diag(lower_{k-1}) P_{k-1}^{-1} r_{k-1},
+ *   x_k = P_k^{-1} (r_k - diag(upper_k) x_{k+1}).
+ * lower, upper (B, K-1, 3); main (B, K, 3, 3); rhs, x (B, K, 3). */
+void F(orc_block3_thomas)(int64_t B, int64_t K, const REAL* lower, const REAL* mainb,
+                          const REAL* upper, const REAL* rhs, REAL* x) {
+#pragma omp parallel
+  {
+    REAL* pinv = (REAL*)malloc(sizeof(REAL) * 9 * (size_t)K);
+    REAL* r = (REAL*)malloc(sizeof(REAL) * 3 * (size_t)K);
+#pragma omp for schedule(static)
+    for (int64_t b = 0; b < B; ++b) {
+      const REAL* lo = lower + b * (K - 1) * 3;
+      const REAL* up = upper + b * (K - 1) * 3;
+      const REAL* mb = mainb + b * K * 9;
+      const REAL* rb = rhs + b * K * 3;
+      REAL* xb = x + b * K * 3;
+      F(inv3)(mb, pinv);
+      for (int q = 0; q < 3; ++q) r[q] = rb[q];
+      for (int64_t k = 1; k < K; ++k) {
+        const REAL* pp = pinv + (k - 1) * 9;
+        REAL m[9];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j)
+            m[i * 3 + j] = mb[k * 9 + i * 3 + j] - lo[(k - 1) * 3 + i] * (pp[i * 3 + j] * up[(k - 1) * 3 + j]);
+        for (int i = 0; i < 3; ++i) {
+          REAL w = pp[i * 3] * r[(k - 1) * 3] + pp[i * 3 + 1] * r[(k - 1) * 3 + 1] +
+                   pp[i * 3 + 2] * r[(k - 1) * 3 + 2];
+          r[k * 3 + i] = rb[k * 3 + i] - lo[(k - 1) * 3 + i] * w;
+        }
+        F(inv3)(m, pinv + k * 9);
+      }
+      for (int64_t k = K - 1; k >= 0; --k) {
+        REAL d[3];
+        for (int i = 0; i < 3; ++i)
+          d[i] = r[k * 3 + i] - (k + 1 < K ? up[k * 3 + i] * xb[(k + 1) * 3 + i] : (REAL)0);
+        const REAL* pp = pinv + k * 9;
+        for (int i = 0; i < 3; ++i)
+          xb[k * 3 + i] = pp[i * 3] * d[0] + pp[i * 3 + 1] * d[1] + pp[i * 3 + 2] * d[2];
+      }
+    }
+    free(r);
+    free(pinv);
+  }
+}
+
 /* Rectangular pulse gate on [delay, delay+pw) at time t (_gates.py:50-65).
    The reference forms the time grid and delay+pw in the state dtype, so a
    float64 judge of a float32 run evaluates the gate in float32 (gate_f32). */

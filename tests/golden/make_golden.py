@@ -16,6 +16,7 @@ compatibility shims) and records its outputs on seeded inputs:
                            factor and the NetCon delay-rounding known answers
   adjoint_f64.npz          reference autograd gradients (gnabar, gkbar, gl, Ra) of
                            a somatic-trace MSE through the CPU cable update
+  block3.npz               block_pcr_solve_t on 3x3 block-tridiagonal systems
 
 Usage (in a container that holds the reference source):
 
@@ -269,6 +270,31 @@ def events():
     print("events")
 
 
+def block3():
+    """The reference's functional block PCR (tridiag/block.py:80-219) on seeded
+    3x3 block-tridiagonal systems shaped like the multi-layer extracellular
+    cable (diagonally dominant main blocks, negative diagonal couplings)."""
+    _ref()
+    from dendra.models.integrators.tridiag.block import block_pcr_solve_t
+
+    out = {}
+    g = torch.Generator().manual_seed(33)
+    for K in (1, 2, 3, 8, 33, 101, 257):
+        B = 4
+        lower = -torch.rand(B, max(K - 1, 0), 3, generator=g, dtype=torch.float64)
+        upper = -torch.rand(B, max(K - 1, 0), 3, generator=g, dtype=torch.float64)
+        main = 0.3 * torch.randn(B, K, 3, 3, generator=g, dtype=torch.float64)
+        main = main + torch.diag_embed(3.0 + torch.rand(B, K, 3, generator=g, dtype=torch.float64))
+        rhs = torch.randn(B, K, 3, generator=g, dtype=torch.float64)
+        for name, t in (("lower", lower), ("upper", upper), ("main", main), ("rhs", rhs)):
+            out[f"K{K}_{name}"] = t.numpy()
+        for tag, dt in (("f64", torch.float64), ("f32", torch.float32)):
+            x = block_pcr_solve_t(lower.to(dt), main.to(dt), upper.to(dt), rhs.to(dt))
+            out[f"K{K}_x_{tag}"] = x.double().numpy()
+    np.savez_compressed(os.path.join(HERE, "block3.npz"), **out)
+    print("block3", len(out))
+
+
 def adjoint():
     """Reference autograd gradients of a somatic-trace MSE w.r.t. gnabar, gkbar,
     gl and Ra: one single-cable float64 model per cable (the reference's HH
@@ -334,7 +360,8 @@ def adjoint():
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["rates", "tridiag", "dhs", "events", "cable", "extra", "adjoint"]
+    what = sys.argv[1:] or ["rates", "tridiag", "dhs", "events", "cable", "extra", "adjoint",
+                            "block3"]
     if "rates" in what:
         rates()
     if "tridiag" in what:
@@ -351,3 +378,5 @@ if __name__ == "__main__":
         hh_extra(torch.float32, "f32")
     if "adjoint" in what:
         adjoint()
+    if "block3" in what:
+        block3()

@@ -98,3 +98,24 @@ def test_taped_run_and_adjoint_reject_bad_arguments_on_the_host():
     adj.tape = 4096
     assert L.dgb_cable_adjoint(ctypes.byref(a), ctypes.byref(adj), None) == -1
     assert b"lam_v" in L.dgb_last_error()
+
+
+def test_block3_contract_errors_on_the_host():
+    import torch
+
+    from dendra_gb300.solvers import validate_block_tridiagonal
+
+    lo = torch.zeros(2, 4, 3)
+    mn = torch.zeros(2, 5, 3, 3)
+    rhs = torch.zeros(2, 5, 3)
+    with pytest.raises(ValueError, match="rhs must have shape"):
+        validate_block_tridiagonal(lo, mn, lo, torch.zeros(2, 5))
+    with pytest.raises(ValueError, match="lower must have shape"):
+        validate_block_tridiagonal(torch.zeros(2, 5, 3), mn, lo, rhs)
+    with pytest.raises(ValueError, match="main must have shape"):
+        validate_block_tridiagonal(lo, torch.zeros(2, 5, 9), lo, rhs)
+    with pytest.raises(ValueError, match="CUDA"):
+        validate_block_tridiagonal(lo, mn, lo, rhs)
+    L = dendra_gb300.load()
+    assert L.dgb_block3_work_size(0, 10, 7) == 10 * 7 * 12 * 4
+    assert L.dgb_block3_solve(0, 0, 4, None, None, None, None, None, None, 0, None) == -1

@@ -105,3 +105,15 @@ def test_oracle_float32_is_within_tolerance_of_float64(golden):
     g64 = golden("hh_cable_f64.npz")
     g32 = golden("hh_cable_f32.npz")
     assert np.abs(g64["v_trace"] - g32["v_trace"]).max() < 0.05
+
+
+@pytest.mark.parametrize("K", [1, 2, 3, 8, 33, 101, 257])
+def test_block3_thomas_matches_reference_block_pcr(golden, K):
+    """The oracle's 3x3 block Thomas against the reference's block PCR
+    (tridiag/block.py) on the same systems (different elimination orders)."""
+    g = golden("block3.npz")
+    args = [g[f"K{K}_{n}"] for n in ("lower", "main", "upper", "rhs")]
+    x64 = oracle.block3_solve(*args)
+    np.testing.assert_allclose(x64, g[f"K{K}_x_f64"], rtol=1e-11, atol=1e-12)
+    x32 = oracle.block3_solve(*(a.astype(np.float32) for a in args))
+    np.testing.assert_allclose(x32, g[f"K{K}_x_f32"], rtol=1e-4, atol=1e-5)
