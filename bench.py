@@ -286,7 +286,7 @@ def bench_c3(args, world, rank, local):
                             t_stop_ms=t_stop)
     comp_steps = net.N * n
     st = torch.cuda.current_stream(dev)
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     wpb, tune_ms = tune_network(net)
     # the whole run's window loop, captured once as a CUDA graph
     net.reset()
@@ -299,7 +299,7 @@ def bench_c3(args, world, rank, local):
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             net.reset()
-            flush.fill_(1.0)
+            flush.sum()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
@@ -439,13 +439,13 @@ def bench_c4(args, world, rank, local):
     for _ in range(max(3, args.warmup)):
         grad_step(guess, target)
     torch.cuda.synchronize()
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     st = torch.cuda.current_stream(dev)
     times = []
     with ClockSampler(local) as clocks:
         torch.cuda.synchronize()
         for _ in range(args.steps):
-            flush.fill_(1.0)
+            flush.sum()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
@@ -560,7 +560,8 @@ def _bt_system(B, K, seed, dtype):
 def bench_bt(args, world, rank, local):
     """3x3 block-tridiagonal solves of multi-layer extracellular cables
     (intracellular v and two extracellular shells per compartment): 16,384
-    systems of 201 block rows, float32.  One bench step = one batched solve."""
+    systems of 201 block rows, float32.  One bench step = one batched solve.
+    Inputs exceed L2 (275 MB)."""
     import torch
 
     import oracle
@@ -577,12 +578,12 @@ def bench_bt(args, world, rank, local):
     for _ in range(max(3, args.warmup)):
         _block3(lower, main, upper, rhs, False)
     torch.cuda.synchronize()
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     st = torch.cuda.current_stream(dev)
     times = []
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
-            flush.fill_(1.0)
+            flush.sum()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
@@ -621,8 +622,8 @@ def bench_bt(args, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "kernel": "block3_kernel",
                      "note": f"{BT_BYTES_PER_ROW} algorithmic B per float32 block row (read "
-                             "main, bands and rhs, write x); the inverse/rhs scratch "
-                             f"(48 B per row each way) stays in L2; peak {peak_kind}"},
+                             "main, bands and rhs, write x); one warp per system, factors "
+                             f"in shared memory; peak {peak_kind}"},
         "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": args.steps * 2,
@@ -908,7 +909,7 @@ def main():
         pop.n.copy_(n0)
         pop.step_index = 0
 
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     st = torch.cuda.current_stream(dev)
 
     def one(spk=False):
@@ -930,7 +931,7 @@ def main():
         torch.cuda.synchronize()
         for _ in range(args.steps):
             reset()
-            flush.fill_(1.0)  # evict L2 between timed steps (outside the events)
+            flush.sum()  # evict L2 between timed steps (outside the events; read: no dirty lines)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
@@ -1056,7 +1057,7 @@ def main():
                    "compartments_per_rank": pop.N, "k_range": [51, 401], "dt_ms": 0.005,
                    "timesteps": n_ts, "state_dtype": "float32",
                    "math": "exact" if args.exact else "fast (<=1e-3 mV vs float64, tested)",
-                   "l2": "flushed between timed steps (256 MiB write, outside the events)",
+                   "l2": "flushed between timed steps (256 MiB read, outside the events)",
                    "launch": "one persistent dgb_cable_run launch per step",
                    "warps_per_block": wpb, "autotune_ms": tune_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

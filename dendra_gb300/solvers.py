@@ -174,10 +174,12 @@ def _block3(lower, main, upper, rhs, transpose):
     x = torch.empty_like(rhs)
     L = _lib.load()
     code = _lib.dtype_code(rhs.dtype)
-    work = torch.empty(L.dgb_block3_work_size(code, B, K), dtype=torch.uint8, device=rhs.device)
+    nwork = L.dgb_block3_work_size(code, B, K)
+    work = torch.empty(nwork, dtype=torch.uint8, device=rhs.device) if nwork else None
     with torch.cuda.device(rhs.device):
         rc = L.dgb_block3_solve(code, B, K, lower.data_ptr(), main.data_ptr(), upper.data_ptr(),
-                                rhs.data_ptr(), x.data_ptr(), work.data_ptr(), int(transpose),
+                                rhs.data_ptr(), x.data_ptr(),
+                                None if work is None else work.data_ptr(), int(transpose),
                                 _lib.stream_ptr(rhs.device))
     _lib.check(rc, "dgb_block3_solve")
     return x

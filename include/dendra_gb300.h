@@ -115,8 +115,10 @@ int dgb_tridiag_solve_transpose(int dtype, int64_t B, int64_t K,
  * two extracellular shells per compartment).  Row k of system b:
  *   diag(lower[k-1]) x[k-1] + main[k] x[k] + diag(upper[k]) x[k+1] = rhs[k]
  *   lower, upper: (B, K-1, 3); main: (B, K, 3, 3) row-major; rhs, x: (B, K, 3).
- * Block Thomas with 3x3 inverses by cofactors, one thread per system.
- * work: caller scratch of dgb_block3_work_size(dtype, B, K) bytes.
+ * One warp per system: each lane eliminates its chunk of block rows (3x3
+ * inverses by cofactors), the 32 reduced block rows are decoupled by block
+ * PCR over warp shuffles, then back substitution; K <= 1024.
+ * work: unused (may be NULL; dgb_block3_work_size returns 0).
  * transpose = 1 solves A^T y = rhs (the adjoint solve).  x must not alias rhs.
  * Replaces thomas_solve_cuda_bt (triton/bt_kernel.py:195-262), selected by
  * _bwd_euler_bt._select_solver (integrators/implicit.py:905-950).
@@ -125,7 +127,7 @@ int dgb_block3_solve(int dtype, int64_t B, int64_t K, const void* lower,
                      const void* main_blocks, const void* upper, const void* rhs,
                      void* x, void* work, int32_t transpose, void* stream);
 
-/* Scratch bytes dgb_block3_solve needs: B * K * 12 values of dtype. */
+/* Scratch bytes dgb_block3_solve needs (0: its factors stay on chip). */
 size_t dgb_block3_work_size(int dtype, int64_t B, int64_t K);
 
 /*
