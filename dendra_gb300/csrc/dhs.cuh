@@ -127,15 +127,37 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
       }
       sD[i] = D;
       sB[i] = Bv;
-      for (int q = p + 1; q < e; ++q) {  // up the chain: the single child is node i
-        const int j = c.nodes[q];
-        const T gc = g[i];
+      // up the chain (the single child of node j is the node below it); the
+      // next node's index and values are loaded one node ahead, before this
+      // node's division and stores (chains are disjoint: nothing else writes them)
+      T gc = g[i];
+      int q = p + 1;
+      int j = q < e ? c.nodes[q] : 0;
+      T dj = T(0), bj = T(0), gj = T(0);
+      if (q < e) {
+        dj = sD[j];
+        bj = sB[j];
+        gj = g[j];
+      }
+      for (; q < e; ++q) {
+        int jn = 0;
+        T dn = T(0), bn = T(0), gn = T(0);
+        if (q + 1 < e) {
+          jn = c.nodes[q + 1];
+          dn = sD[jn];
+          bn = sB[jn];
+          gn = g[jn];
+        }
         const T f = gc * (T(1) / (D + gc));
-        D = sD[j] + f * D;
-        Bv = sB[j] + f * Bv;
+        D = dj + f * D;
+        Bv = bj + f * Bv;
         sD[j] = D;
         sB[j] = Bv;
-        i = j;
+        gc = gj;
+        j = jn;
+        dj = dn;
+        bj = bn;
+        gj = gn;
       }
     }
     sync();
@@ -152,11 +174,24 @@ __device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const Ch
       const int p = c.chain_ptr[ch], e = c.chain_ptr[ch + 1];
       const I par = t.parent[c.nodes[e - 1]];
       T xp = has_parent(par) ? sB[par] : T(0);
-      for (int q = e - 1; q >= p; --q) {  // down the chain from its top
-        const int j = c.nodes[q];
-        const T gj = g[j];
-        xp = (sB[j] + gj * xp) / (sD[j] + gj);
+      // down the chain from its top, the next node's loads one node ahead
+      int j = c.nodes[e - 1];
+      T bj = sB[j], dj = sD[j], gj = g[j];
+      for (int q = e - 1; q >= p; --q) {
+        int jn = 0;
+        T bn = T(0), dn = T(0), gn = T(0);
+        if (q > p) {
+          jn = c.nodes[q - 1];
+          bn = sB[jn];
+          dn = sD[jn];
+          gn = g[jn];
+        }
+        xp = (bj + gj * xp) / (dj + gj);
         sB[j] = xp;
+        j = jn;
+        bj = bn;
+        dj = dn;
+        gj = gn;
       }
     }
     sync();
