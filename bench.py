@@ -637,6 +637,180 @@ def bench_bt(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+# unfused per-step two-tap op, per connection-step with one connection per
+# target slot (float32): weight, share, two addresses, source index and gate
+# 36 B + two tap read-modify-writes 16 B + the delivered row read, cleared and
+# written out 12 B
+DELAY_BYTES_PER_CONN_STEP = 64
+
+
+def _delay_case(n_conn, n_src, depth, seed, dt_ms=0.025):
+    """Config-3 connectivity as a transport rollout: n_conn connections from
+    n_src sources, each into its own synapse slot (width n_conn, post slots
+    shuffled), delays U[1,5] ms at dt 0.025 ms (positions 40-200 steps),
+    lognormal(-7, 0.5) weights."""
+    rng = np.random.default_rng(seed)
+    post = rng.permutation(n_conn)
+    pre = rng.integers(0, n_src, n_conn)
+    pos = np.maximum(rng.uniform(1.0, 5.0, n_conn) / dt_ms, 1.0).astype(np.float32)
+    off = np.floor(pos).astype(np.int64)
+    frac = (pos - off).astype(np.float32)
+    w = rng.lognormal(-7.0, 0.5, n_conn).astype(np.float32)
+    lower = (off % depth) * n_conn + post
+    upper = (lower + n_conn) % (depth * n_conn)
+    return post, pre, frac, w, lower, upper
+
+
+def _delay_gates(steps, n_src, seed, rate_hz=5.0, dt_ms=0.025):
+    """Per-step source gates: 0/1 spikes of independent 5 Hz sources."""
+    rng = np.random.default_rng(seed)
+    return (rng.random((steps, n_src)) < rate_hz * dt_ms * 1e-3).astype(np.float32)
+
+
+def bench_delay(args, world, rank, local):
+    """Differentiable event transport (interpolated two-tap delays) at config-3
+    scale: 409,600 connections from 4,096 sources into a [201][409,600] ring,
+    a 2,000-step rollout forward (one launch) and its reverse sweep (one launch
+    + the per-source gate reduction) through two_tap_rollout and autograd.
+    One bench step = forward + backward; unit = connection-steps/s."""
+    import torch
+
+    import oracle
+    from dendra_gb300 import delays
+
+    n_conn, n_src, depth = 409_600, 4096, 201
+    steps = args.timesteps or 2000
+    units = n_conn * steps
+    metric = "connection-steps/s"
+    cfg = {"workload": "delay-two-tap-rollout", "connections": n_conn, "sources": n_src,
+           "ring": [depth, n_conn], "timesteps": steps, "pass": "forward + reverse sweep",
+           "l2": "flushed between timed steps"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        post, pre, frac, w, lower, upper = _delay_case(n_conn, n_src, depth, 31)
+        n_s = 100
+        g = _delay_gates(n_s, n_src, 32)
+        rng = np.random.default_rng(5)
+        gp = rng.standard_normal((n_s, n_conn)).astype(np.float32)
+        q = np.zeros((depth, n_conn), np.float32)
+        vals, secs = [], 0.0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            oracle.two_tap_rollout(q, 0, w, g, frac, lower, upper, pre_idx=pre)
+            oracle.two_tap_rollout_vjp(q, 0, w, g, frac, lower, upper, gp, pre_idx=pre)
+            secs = time.perf_counter() - t0
+            vals.append(n_conn * n_s / secs)
+        v = float(np.median(vals))
+        print(json.dumps({
+            "impl": "reference", "metric": metric, "value": v, "unit": metric, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": units / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": metric, "cores": 1, "kind": "port",
+                             "sample": f"all {n_conn} connections x {n_s} steps forward + "
+                                       "reverse, float32, sequential ordered adds"},
+            "e2e": {"value": v, "unit": metric, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}), flush=True)
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    post, pre, frac, w, lower, upper = _delay_case(n_conn, n_src, depth, 31 + rank)
+    gates_h = torch.from_numpy(_delay_gates(steps, n_src, 32 + rank))
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    tw, tf, tlo, tup, tpre = T(w), T(frac), T(lower), T(upper), T(pre)
+    tg = gates_h.to(dev)
+    q0 = torch.zeros(depth, n_conn, dtype=torch.float32, device=dev)
+    gpay = torch.randn(steps, n_conn, dtype=torch.float32, device=dev,
+                       generator=torch.Generator(dev).manual_seed(5))
+    leaves = [t.requires_grad_() for t in (tw, tg, tf)]
+
+    def step():
+        for t in leaves:
+            t.grad = None
+        pay, fin = delays.two_tap_rollout(q0, 0, tw, tg, tf, tlo, tup, tpre)
+        torch.autograd.backward([pay], [gpay])
+        return pay
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    times, fwd = [], []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.sum()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(st)
+            with torch.no_grad():
+                delays.two_tap_rollout(q0, 0, tw, tg, tf, tlo, tup, tpre)
+            e1.record(st)
+            e1.synchronize()
+            fwd.append(e0.elapsed_time(e1))
+            flush.sum()
+            e0.record(st)
+            step()
+            e2.record(st)
+            e2.synchronize()
+            times.append(e0.elapsed_time(e2))
+    ms = float(np.mean(times))
+    ms_fwd = float(np.mean(fwd))
+    # end to end: gates in from pinned host memory, gradients out
+    gates_pin = gates_h.pin_memory()
+    outs = [torch.empty(n_conn, dtype=torch.float32).pin_memory() for _ in range(2)]
+    gout = torch.empty(steps, n_src, dtype=torch.float32).pin_memory()
+    h2d = gates_pin.numel() * 4
+    d2h = (2 * n_conn + steps * n_src) * 4
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.no_grad():
+            tg.copy_(gates_pin, non_blocking=True)
+        step()
+        outs[0].copy_(tw.grad, non_blocking=True)
+        outs[1].copy_(tf.grad, non_blocking=True)
+        gout.copy_(tg.grad, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    # check a prefix of the rollout against the oracle
+    n_chk = 200
+    pay = delays.two_tap_rollout(q0, 0, tw.detach(), tg.detach()[:n_chk], tf.detach(), tlo, tup,
+                                 tpre)[0]
+    t0 = time.perf_counter()
+    _, opay = oracle.two_tap_rollout(np.zeros((depth, n_conn), np.float32), 0, w,
+                                     gates_h[:n_chk].numpy(), frac, lower, upper, pre_idx=pre)
+    cpu_s = time.perf_counter() - t0
+    exact = bool(np.array_equal(pay.cpu().numpy(), opay))
+    peak, peak_kind = _peaks()
+    achieved = DELAY_BYTES_PER_CONN_STEP * units / (ms_fwd * 1e-3) / 1e9
+    line = {
+        "metric": metric, "value": units / (ms * 1e-3), "unit": metric, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": cfg,
+        "forward_ms": ms_fwd, "forward_connection_steps_per_s": units / (ms_fwd * 1e-3),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "two_tap_window_kernel",
+                     "note": f"{DELAY_BYTES_PER_CONN_STEP} algorithmic B per float32 "
+                             "connection-step of the unfused per-step op; forward rollout "
+                             f"(one launch) timed alone; peak {peak_kind}"},
+        "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": 3,
+        "clocks": clocks.summary(),
+        "bit_exact_vs_oracle": exact,
+        "cpu_baseline": {"value": n_conn * n_chk / cpu_s, "unit": metric, "cores": 1,
+                         "kind": "port",
+                         "sample": f"forward rollout of all {n_conn} connections over "
+                                   f"{n_chk} steps, float32, sequential ordered adds"},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 MLP_FLOP_PER_SAMPLE = 2 * (4 * 256 + 256 * 256 + 256 * 256 + 256 * 1)
 
 
@@ -855,11 +1029,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5", "bt"],
+    ap.add_argument("--workload", default="c2",
+                    choices=["c2", "c3", "c4", "c5", "bt", "delay"],
                     help="c2: uneven cable population (default); c3: branched-cell network; "
                          "c4: adjoint gradient of a trace fit; "
                          "c5: learned threshold proposal vs plain bisection; "
-                         "bt: 3x3 block-tridiagonal (multi-layer extracellular) solves")
+                         "bt: 3x3 block-tridiagonal (multi-layer extracellular) solves; "
+                         "delay: differentiable two-tap event transport rollout")
     ap.add_argument("--train", type=int, default=200000, help="c5 training thresholds")
     ap.add_argument("--cables", type=int, default=16384,
                     help="cables per rank (a smaller case for profiling)")
@@ -874,6 +1050,8 @@ def main():
         return bench_bt(args, world, rank, local)
     if args.workload == "c5":
         return bench_c5(args, world, rank, local)
+    if args.workload == "delay":
+        return bench_delay(args, world, rank, local)
     if args.impl == "reference":
         return run_reference(args, world, rank)
 

@@ -101,6 +101,21 @@ SIGNATURES = {
     "dgb_adam": (_INT, [_I64, _I32, _I32, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float,
                         ctypes.c_float, ctypes.c_float, _I32, _P, _P, _P]),
     "dgb_mse_grad": (_INT, [_I64, _P, _P, ctypes.c_float, _P, _P, _P]),
+    "dgb_two_tap_enqueue": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P,
+                                   _P, _P, _P, _P, _P, _P, _P]),
+    "dgb_three_tap_enqueue": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P,
+                                     _P, _P, _P, _P, _P]),
+    "dgb_two_tap_gather": (_INT, [_INT, _P, _I64, _P, _I64, _P, _P, _P, _P, _P]),
+    "dgb_two_tap_vjp": (_INT, [_INT, _P, _I64, _P, _I64, _P, _P, _P, _I64, _P, _P, _P, _P, _P,
+                               _P, _P, _P, _P]),
+    "dgb_three_tap_vjp": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P,
+                                 _P, _P]),
+    "dgb_two_tap_window": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64, _P,
+                                  _P, _P, _P, _P, _P, _P]),
+    "dgb_two_tap_window_vjp": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64,
+                                      _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P, _P,
+                                      _P]),
+    "dgb_delay_status": (_INT, [_P]),
 }
 
 

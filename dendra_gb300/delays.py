@@ -1,0 +1,536 @@
+"""Interpolated (differentiable) delay transport on the GB300 kernels.
+
+Host mirrors of the reference's interpolated-delay pieces, every per-step
+operation on the GPU and deterministic (one thread owns one ring column and
+adds in the reference's order; no floating-point atomics):
+
+* :func:`linear_delay_taps`, :func:`delay_interpolation` — positions
+  ``max(delay / dt, 1)`` split into offsets and shares
+  (networks/_event_delivery.py:202-226); elementwise, once per rollout
+* :func:`ordered_two_tap_enqueue`, :func:`ordered_two_tap_enqueue_from_source`
+  and the in-place ``..._`` forms — the ordered two-tap op
+  (networks/_two_tap_enqueue_cpu.cpp:61-152, 317-342) with its adjoint
+  (networks/_two_tap_enqueue.py:94-150) as a ``torch.autograd.Function``
+* :func:`delay_ring_gather_two_tap`, :func:`delay_ring_two_tap_vjp`
+  (_two_tap_enqueue_cpu.cpp:206-315)
+* :func:`dense_interpolated_delay_transition` — the two- and three-tap
+  transition (networks/_event_delivery.py:229-308)
+* :func:`two_tap_rollout` — many steps of the two-tap transition in one
+  launch, with a hand-written reverse sweep (the adjoint the reference takes by
+  autograd through its per-step loop)
+
+Ring layout: ``queue[depth][width]`` (row = delivery step, column = target
+slot).  Two-tap addresses are flat and relative to the start of row ``slot``:
+destination ``(slot*width + address) mod (depth*width)``.
+"""
+
+from __future__ import annotations
+
+from typing import NamedTuple
+
+import torch
+
+from . import _lib
+
+ERR_SLOT, ERR_ADDRESS, ERR_SOURCE, ERR_PLAN = 1, 2, 3, 4
+
+
+class DenseTransition(NamedTuple):
+    """Result of one transition (the reference's networks/_event_delivery.py:25-29)."""
+
+    queue: torch.Tensor
+    slot: torch.Tensor
+    global_step: torch.Tensor
+    event_queue: torch.Tensor | None
+
+
+# ---------------------------------------------------------------------------
+# delay positions
+# ---------------------------------------------------------------------------
+def linear_delay_taps(positions):
+    """(lower offset as int64, upper-tap share) of positions in steps."""
+    lower = torch.floor(positions)
+    return lower.to(torch.int64), positions - lower
+
+
+def delay_interpolation(delays, dt, *, dtype, taps, sigma):
+    """Offsets and shares of physical delays.
+
+    Positions are ``max(delay / dt, 1)`` steps.  Two taps: the floor and the
+    upper share (the fractional part).  Three taps: offsets ``floor - 1,
+    floor, floor + 1`` with Gaussian weights ``softmax(-((pos - centre) /
+    (sigma + 1e-6))**2 / 2)`` (the reference's 1e-6 denominator offset).
+    """
+    pos = (delays.to(dtype) / dt.to(dtype).reshape(1)).clamp_min(1.0)
+    if taps == 2:
+        return linear_delay_taps(pos)
+    base = torch.floor(pos).to(torch.int64)
+    offsets = torch.stack([base - 1, base, base + 1], dim=-1)
+    z = (pos.unsqueeze(-1) - offsets.to(dtype)) / (sigma + 1e-6)
+    return offsets, torch.softmax(-0.5 * z ** 2, dim=-1)
+
+
+# ---------------------------------------------------------------------------
+# column plans
+# ---------------------------------------------------------------------------
+def _column_lists(keys, n):
+    """(ptr[n+1], edge ids grouped by key, ascending within a key)."""
+    order = torch.argsort(keys, stable=True)
+    ptr = torch.zeros(n + 1, dtype=torch.int64, device=keys.device)
+    if keys.numel():
+        torch.cumsum(torch.bincount(keys, minlength=n), 0, out=ptr[1:])
+    return ptr, order.to(torch.int64).contiguous()
+
+
+class TapPlan:
+    """Per-column edge lists of a set of two-tap addresses.
+
+    ``lower_ptr/lower_edge`` list, for every ring column, the edges whose
+    lower address lies in it (ascending), ``upper_ptr/upper_edge`` the same for
+    upper addresses.  ``consistent`` is true when every edge's two taps share a
+    column; then ``col_ptr/col_edge`` serve both (the multi-step kernels need
+    this).  With source indices, ``src_ptr/src_edge`` list each source's edges.
+    """
+
+    def __init__(self, depth, width, lower, upper, pre_idx=None, n_sources=0,
+                 post_idx=None):
+        self.depth, self.width = int(depth), int(width)
+        size = self.depth * self.width
+        self.n_edges = int(lower.numel() if lower is not None else post_idx.numel())
+        if post_idx is not None:
+            # both taps in column post_idx[e] (the transition's own addresses)
+            if self.n_edges and not bool(((post_idx >= 0) & (post_idx < self.width)).all()):
+                raise IndexError("post_idx is outside the delivery ring width")
+            self.lower_ptr, self.lower_edge = _column_lists(post_idx, self.width)
+            self.upper_ptr, self.upper_edge = self.lower_ptr, self.lower_edge
+            self.consistent = True
+        else:
+            if self.n_edges and not bool(
+                ((lower >= 0) & (lower < size) & (upper >= 0) & (upper < size)).all()):
+                raise RuntimeError("Two-tap address is outside the delivery ring")
+            lo_col = lower.remainder(self.width) if self.width else lower
+            up_col = upper.remainder(self.width) if self.width else upper
+            self.lower_ptr, self.lower_edge = _column_lists(lo_col, self.width)
+            self.consistent = bool(torch.equal(lo_col, up_col))
+            if self.consistent:
+                self.upper_ptr, self.upper_edge = self.lower_ptr, self.lower_edge
+            else:
+                self.upper_ptr, self.upper_edge = _column_lists(up_col, self.width)
+        self.col_ptr = self.lower_ptr if self.consistent else None
+        self.col_edge = self.lower_edge if self.consistent else None
+        self.src_ptr = self.src_edge = None
+        self.n_sources = int(n_sources)
+        if pre_idx is not None:
+            if self.n_edges and not bool(((pre_idx >= 0) & (pre_idx < self.n_sources)).all()):
+                raise IndexError("Two-tap source index is out of range")
+            self.src_ptr, self.src_edge = _column_lists(pre_idx, self.n_sources)
+
+
+_plans: list = []
+_MAX_PLANS = 16
+
+
+def _cached_plan(key_tensors, versions, depth, width, n_sources, build):
+    """Plan cache keyed on tensor identity and version (entries hold the tensors)."""
+    for ent in _plans:
+        tens, vers, d, w, ns, plan = ent
+        if (d, w, ns) == (depth, width, n_sources) and vers == versions and all(
+                a is b for a, b in zip(tens, key_tensors)):
+            return plan
+    plan = build()
+    _plans.append((key_tensors, versions, depth, width, n_sources, plan))
+    if len(_plans) > _MAX_PLANS:
+        _plans.pop(0)
+    return plan
+
+
+def two_tap_plan(depth, width, lower, upper, pre_idx=None, n_sources=0):
+    """Cached :class:`TapPlan` of flat two-tap addresses."""
+    keys = (lower, upper, pre_idx)
+    vers = tuple(None if t is None else t._version for t in keys)
+    return _cached_plan(keys, vers, int(depth), int(width), int(n_sources),
+                        lambda: TapPlan(depth, width, lower, upper, pre_idx, n_sources))
+
+
+def post_plan(depth, width, post_idx, pre_idx=None, n_sources=0):
+    """Cached :class:`TapPlan` for taps in column ``post_idx[e]``."""
+    keys = (post_idx, pre_idx)
+    vers = tuple(None if t is None else t._version for t in keys)
+    return _cached_plan(keys, vers, int(depth), int(width), int(n_sources),
+                        lambda: TapPlan(depth, width, None, None, pre_idx, n_sources,
+                                        post_idx=post_idx))
+
+
+# ---------------------------------------------------------------------------
+# argument checks (the reference's TORCH_CHECK messages, _two_tap_enqueue_cpu.cpp:12-100)
+# ---------------------------------------------------------------------------
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def _check_queue(queue):
+    if not (isinstance(queue, torch.Tensor) and queue.is_cuda and queue.dim() == 2
+            and queue.size(0) > 0 and queue.dtype in (torch.float32, torch.float64)):
+        raise RuntimeError(
+            "Two-tap queue must be a CUDA float32 or float64 matrix with positive depth")
+
+
+def _check_vec(t, dtype, n, name, device):
+    if not (isinstance(t, torch.Tensor) and t.device == device and t.dim() == 1
+            and t.dtype == dtype and t.numel() == n and t.is_contiguous()):
+        raise RuntimeError(f"{name} must be a contiguous CUDA tensor of the required dtype "
+                           "and size")
+
+
+def _slot_tensor(slot, depth, device):
+    """Slot as a one-element int64 device tensor; host values are range-checked here,
+    device values by the kernels (``delay_status``)."""
+    if isinstance(slot, torch.Tensor) and slot.is_cuda:
+        if slot.numel() != 1 or slot.dtype != torch.int64:
+            raise RuntimeError("slot must be a one-element int64 tensor")
+        return slot.reshape(1)
+    value = int(slot.reshape(-1)[0]) if isinstance(slot, torch.Tensor) else int(slot)
+    if not 0 <= value < depth:
+        raise RuntimeError("Two-tap slot is outside the delivery ring")
+    return torch.tensor([value], dtype=torch.int64, device=device)
+
+
+def delay_status() -> int:
+    """First device-side index error of the delay kernels (0 = none), cleared."""
+    rc = _lib.load().dgb_delay_status(_lib.stream_ptr())
+    if rc < 0:
+        _lib.check(rc, "dgb_delay_status")
+    return rc
+
+
+# ---------------------------------------------------------------------------
+# raw launches
+# ---------------------------------------------------------------------------
+def _enqueue_into(ring, slot_t, weights, gates, fraction, lower, upper, pre_idx, plan,
+                  payload=None):
+    L = _lib.load()
+    depth, width = ring.shape
+    _lib.check(L.dgb_two_tap_enqueue(
+        _lib.dtype_code(ring.dtype), ring.data_ptr(), depth, width, slot_t.data_ptr(),
+        plan.n_edges, _ptr(weights), _ptr(gates), _ptr(pre_idx), plan.n_sources,
+        _ptr(fraction), _ptr(lower), _ptr(upper), plan.lower_ptr.data_ptr(),
+        _ptr(plan.lower_edge), plan.upper_ptr.data_ptr(), _ptr(plan.upper_edge),
+        _ptr(payload), _lib.stream_ptr(ring.device)), "dgb_two_tap_enqueue")
+
+
+def _vjp(ring, offset_t, weights, gates, fraction, lower, upper, pre_idx, plan):
+    L = _lib.load()
+    dw = torch.empty_like(weights)
+    dg = torch.empty_like(gates)
+    df = torch.empty_like(fraction)
+    _lib.check(L.dgb_two_tap_vjp(
+        _lib.dtype_code(ring.dtype), ring.data_ptr(), ring.numel(), offset_t.data_ptr(),
+        weights.numel(), _ptr(weights), _ptr(gates), _ptr(pre_idx),
+        plan.n_sources if pre_idx is not None else 0, _ptr(fraction), _ptr(lower),
+        _ptr(upper), _ptr(plan.src_ptr), _ptr(plan.src_edge), dw.data_ptr(), dg.data_ptr(),
+        df.data_ptr(), _lib.stream_ptr(ring.device)), "dgb_two_tap_vjp")
+    return dw, dg, df
+
+
+def _prepare(queue, weights, gates, fraction, lower, upper, pre_idx):
+    _check_queue(queue)
+    dev, dt = queue.device, queue.dtype
+    for name, t in (("weights", weights), ("gates", gates), ("fraction", fraction),
+                    ("lower", lower), ("upper", upper)):
+        if not isinstance(t, torch.Tensor) or t.dim() != 1:
+            raise RuntimeError("Two-tap edge inputs must be vectors")
+    n = weights.numel()
+    if queue.numel() == 0 and n:
+        raise RuntimeError("Empty ring cannot receive edges")
+    _check_vec(weights, dt, n, "weights", dev)
+    _check_vec(gates, dt, gates.numel() if pre_idx is not None else n, "gates", dev)
+    _check_vec(fraction, dt, n, "fraction", dev)
+    _check_vec(lower, torch.int64, n, "lower", dev)
+    _check_vec(upper, torch.int64, n, "upper", dev)
+    if pre_idx is not None:
+        _check_vec(pre_idx, torch.int64, n, "source indices", dev)
+    return n
+
+
+# ---------------------------------------------------------------------------
+# autograd operators
+# ---------------------------------------------------------------------------
+class _TwoTapEnqueue(torch.autograd.Function):
+    """queue -> new queue (row slot cleared, two taps added); linear in queue."""
+
+    @staticmethod
+    def forward(ctx, queue, slot_t, weights, gates, fraction, lower, upper, pre_idx, plan):
+        out = queue.clone(memory_format=torch.contiguous_format)
+        _enqueue_into(out, slot_t, weights, gates, fraction, lower, upper, pre_idx, plan)
+        ctx.save_for_backward(slot_t, weights, gates, fraction, lower, upper,
+                              *(() if pre_idx is None else (pre_idx,)))
+        ctx.plan = plan
+        ctx.width = queue.shape[1]
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        slot_t, weights, gates, fraction, lower, upper, *rest = ctx.saved_tensors
+        pre_idx = rest[0] if rest else None
+        need_q, _, need_w, need_g, need_f = ctx.needs_input_grad[:5]
+        grad_out = grad_out.contiguous()
+        gq = grad_out.index_fill(0, slot_t, 0) if need_q else None
+        dw = dg = df = None
+        if need_w or need_g or need_f:
+            offset_t = slot_t * ctx.width
+            dw, dg, df = _vjp(grad_out, offset_t, weights, gates, fraction, lower, upper,
+                              pre_idx, ctx.plan)
+            dw, dg, df = (dw if need_w else None, dg if need_g else None,
+                          df if need_f else None)
+        return gq, None, dw, dg, df, None, None, None, None
+
+
+class _ThreeTapEnqueue(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, queue, slot_t, weights, gates, coeff, offsets, post_idx, plan):
+        out = queue.clone(memory_format=torch.contiguous_format)
+        L = _lib.load()
+        depth, width = out.shape
+        n = weights.numel()
+        _lib.check(L.dgb_three_tap_enqueue(
+            _lib.dtype_code(out.dtype), out.data_ptr(), depth, width, slot_t.data_ptr(), n,
+            _ptr(weights), _ptr(gates), None, 0, _ptr(coeff), _ptr(offsets), _ptr(post_idx),
+            plan.lower_ptr.data_ptr(), _ptr(plan.lower_edge), None,
+            _lib.stream_ptr(out.device)), "dgb_three_tap_enqueue")
+        ctx.save_for_backward(slot_t, weights, gates, coeff, offsets, post_idx)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        slot_t, weights, gates, coeff, offsets, post_idx = ctx.saved_tensors
+        grad_out = grad_out.contiguous()
+        gq = grad_out.index_fill(0, slot_t, 0) if ctx.needs_input_grad[0] else None
+        dw = torch.empty_like(weights)
+        dg = torch.empty_like(gates)
+        dc = torch.empty_like(coeff)
+        depth, width = grad_out.shape
+        _lib.check(_lib.load().dgb_three_tap_vjp(
+            _lib.dtype_code(grad_out.dtype), grad_out.data_ptr(), depth, width,
+            slot_t.data_ptr(), weights.numel(), _ptr(weights), _ptr(gates), _ptr(coeff),
+            _ptr(offsets), _ptr(post_idx), dw.data_ptr(), dg.data_ptr(), dc.data_ptr(),
+            _lib.stream_ptr(grad_out.device)), "dgb_three_tap_vjp")
+        need = ctx.needs_input_grad
+        return (gq, None, dw if need[2] else None, dg if need[3] else None,
+                dc if need[4] else None, None, None, None)
+
+
+def ordered_two_tap_enqueue(queue, slot, weights, gates, fraction, lower, upper):
+    """New queue: row ``slot`` cleared, then ``(w g)(1-f)`` at every lower address
+    (edge order) and ``(w g) f`` at every upper address (edge order)."""
+    _prepare(queue, weights, gates, fraction, lower, upper, None)
+    slot_t = _slot_tensor(slot, queue.shape[0], queue.device)
+    plan = two_tap_plan(queue.shape[0], queue.shape[1], lower, upper)
+    return _TwoTapEnqueue.apply(queue, slot_t, weights, gates, fraction, lower, upper, None,
+                                plan)
+
+
+def ordered_two_tap_enqueue_from_source(queue, slot, weights, gates, fraction, lower, upper,
+                                        pre_idx):
+    """As :func:`ordered_two_tap_enqueue` with edge e's gate ``gates[pre_idx[e]]``."""
+    _prepare(queue, weights, gates, fraction, lower, upper, pre_idx)
+    slot_t = _slot_tensor(slot, queue.shape[0], queue.device)
+    plan = two_tap_plan(queue.shape[0], queue.shape[1], lower, upper, pre_idx, gates.numel())
+    return _TwoTapEnqueue.apply(queue, slot_t, weights, gates, fraction, lower, upper, pre_idx,
+                                plan)
+
+
+def ordered_two_tap_enqueue_(queue, slot, weights, gates, fraction, lower, upper,
+                             pre_idx=None, payload=None):
+    """In-place form (no autograd).  ``payload`` (optional, ``width``) receives
+    row ``slot`` before it is cleared."""
+    _prepare(queue, weights, gates, fraction, lower, upper, pre_idx)
+    if not queue.is_contiguous():
+        raise RuntimeError("The private two-tap queue must be contiguous")
+    slot_t = _slot_tensor(slot, queue.shape[0], queue.device)
+    plan = two_tap_plan(queue.shape[0], queue.shape[1], lower, upper, pre_idx,
+                        gates.numel() if pre_idx is not None else 0)
+    with torch.no_grad():
+        _enqueue_into(queue, slot_t, weights, gates, fraction, lower, upper, pre_idx, plan,
+                      payload)
+    return queue
+
+
+def ordered_two_tap_enqueue_from_source_(queue, slot, weights, gates, fraction, lower, upper,
+                                         pre_idx, payload=None):
+    return ordered_two_tap_enqueue_(queue, slot, weights, gates, fraction, lower, upper,
+                                    pre_idx, payload)
+
+
+def delay_ring_gather_two_tap(ring, offset, lower, upper):
+    """(ring[(lower + offset) mod size], ring[(upper + offset) mod size])."""
+    if not (ring.is_cuda and ring.dim() == 2 and ring.numel() > 0 and ring.is_contiguous()
+            and ring.dtype in (torch.float32, torch.float64)):
+        raise RuntimeError("Two-tap gather requires a nonempty contiguous CUDA float matrix")
+    off = offset if isinstance(offset, torch.Tensor) and offset.is_cuda else torch.tensor(
+        [int(offset)], dtype=torch.int64, device=ring.device)
+    lo = torch.empty(lower.numel(), dtype=ring.dtype, device=ring.device)
+    hi = torch.empty_like(lo)
+    _lib.check(_lib.load().dgb_two_tap_gather(
+        _lib.dtype_code(ring.dtype), ring.data_ptr(), ring.numel(), off.data_ptr(),
+        lower.numel(), _ptr(lower), _ptr(upper), lo.data_ptr(), hi.data_ptr(),
+        _lib.stream_ptr(ring.device)), "dgb_two_tap_gather")
+    return lo, hi
+
+
+def delay_ring_two_tap_vjp(ring, offset, weights, gates, fraction, lower, upper,
+                           source_indices=None):
+    """(grad_weights, grad_gates, grad_fraction) at ring cotangent ``ring``."""
+    if not (ring.is_cuda and ring.dim() == 2 and ring.numel() > 0 and ring.is_contiguous()):
+        raise RuntimeError("Two-tap VJP requires a nonempty contiguous CUDA float matrix")
+    _prepare(ring, weights, gates, fraction, lower, upper, source_indices)
+    off = offset if isinstance(offset, torch.Tensor) and offset.is_cuda else torch.tensor(
+        [int(offset)], dtype=torch.int64, device=ring.device)
+    plan = two_tap_plan(ring.shape[0], ring.shape[1], lower, upper, source_indices,
+                        gates.numel() if source_indices is not None else 0)
+    return _vjp(ring, off.reshape(1), weights, gates, fraction, lower, upper, source_indices,
+                plan)
+
+
+def dense_interpolated_delay_transition(queue, slot, global_step, weights, connection_gates,
+                                        delays, dt, *, post_idx, depth, width, taps, sigma,
+                                        delay_taps=None, _clone_once=False):
+    """One interpolated transition: the returned queue has row ``slot`` cleared
+    and every connection's ``w g`` split over its taps (two: floor / floor+1 by
+    the fractional position; three: Gaussian weights around the floor).  Today's
+    row must be read (``queue[slot]``) before this call.  Returns a
+    :class:`DenseTransition` with the slot and step advanced by one."""
+    if delay_taps is None:
+        delay_taps = delay_interpolation(delays, dt, dtype=queue.dtype, taps=taps, sigma=sigma)
+    offsets, shares = delay_taps
+    _check_queue(queue)
+    if tuple(queue.shape) != (depth, width):
+        raise RuntimeError("queue must have shape (depth, width)")
+    slot_t = _slot_tensor(slot, depth, queue.device)
+    plan = post_plan(depth, width, post_idx)
+    if taps == 2:
+        lower = offsets.remainder(depth) * width + post_idx
+        upper = (lower + width).remainder(depth * width)
+        _check_vec(weights, queue.dtype, lower.numel(), "weights", queue.device)
+        _check_vec(connection_gates, queue.dtype, lower.numel(), "gates", queue.device)
+        frac = shares.contiguous()
+        nxt = _TwoTapEnqueue.apply(queue, slot_t, weights, connection_gates, frac,
+                                   lower.contiguous(), upper.contiguous(), None, plan)
+    else:
+        nxt = _ThreeTapEnqueue.apply(queue, slot_t, weights, connection_gates,
+                                     shares.contiguous(), offsets.contiguous(), post_idx, plan)
+    gs = global_step + 1 if isinstance(global_step, torch.Tensor) else int(global_step) + 1
+    return DenseTransition(nxt, (slot_t + 1).remainder(depth), gs, None)
+
+
+# ---------------------------------------------------------------------------
+# multi-step rollout
+# ---------------------------------------------------------------------------
+_SCRATCH_BYTES = 256 << 20
+
+
+class _TwoTapRollout(torch.autograd.Function):
+    """(payload[n][width], final queue) of n two-tap steps from ``queue0``."""
+
+    @staticmethod
+    def forward(ctx, queue0, slot_t, weights, gates, fraction, lower, upper, pre_idx, plan):
+        ring = queue0.clone(memory_format=torch.contiguous_format)
+        n = gates.shape[0]
+        depth, width = ring.shape
+        payload = torch.empty(n, width, dtype=ring.dtype, device=ring.device)
+        _lib.check(_lib.load().dgb_two_tap_window(
+            _lib.dtype_code(ring.dtype), ring.data_ptr(), depth, width, slot_t.data_ptr(), n,
+            plan.n_edges, _ptr(weights), _ptr(gates), _ptr(pre_idx),
+            plan.n_sources if pre_idx is not None else 0, _ptr(fraction), _ptr(lower),
+            _ptr(upper), plan.col_ptr.data_ptr(), _ptr(plan.col_edge), payload.data_ptr(),
+            _lib.stream_ptr(ring.device)), "dgb_two_tap_window")
+        ctx.save_for_backward(slot_t, weights, gates, fraction, lower, upper,
+                              *(() if pre_idx is None else (pre_idx,)))
+        ctx.plan = plan
+        return payload, ring
+
+    @staticmethod
+    def backward(ctx, grad_payload, grad_final):
+        slot_t, weights, gates, fraction, lower, upper, *rest = ctx.saved_tensors
+        pre_idx = rest[0] if rest else None
+        plan = ctx.plan
+        n = gates.shape[0]
+        depth, width = plan.depth, plan.width
+        dev, dt = weights.device, weights.dtype
+        R = (torch.zeros(depth, width, dtype=dt, device=dev) if grad_final is None
+             else grad_final.clone(memory_format=torch.contiguous_format))
+        gp = None if grad_payload is None else grad_payload.contiguous()
+        dw = torch.empty_like(weights)
+        df = torch.empty_like(fraction)
+        dgates = torch.empty_like(gates)
+        E = plan.n_edges
+        chunk = n
+        scratch = None
+        if pre_idx is not None and E:
+            chunk = max(1, min(n, _SCRATCH_BYTES // (E * weights.element_size())))
+            scratch = torch.empty(chunk * E, dtype=dt, device=dev)
+        stride = gates.shape[1] if gates.dim() == 2 else 0
+        L = _lib.load()
+        stream = _lib.stream_ptr(dev)
+        hi = n
+        first = True
+        while hi > 0:  # newest chunk first
+            lo = max(0, hi - chunk)
+            k = hi - lo
+            s_lo = (slot_t + lo).remainder(depth)
+            _lib.check(L.dgb_two_tap_window_vjp(
+                _lib.dtype_code(dt), R.data_ptr(), depth, width, s_lo.data_ptr(), k, E,
+                _ptr(weights), gates[lo:hi].data_ptr() if stride else _ptr(gates),
+                _ptr(pre_idx), plan.n_sources if pre_idx is not None else 0, _ptr(fraction),
+                _ptr(lower), _ptr(upper), plan.col_ptr.data_ptr(), _ptr(plan.col_edge),
+                _ptr(plan.src_ptr), _ptr(plan.src_edge),
+                None if gp is None else gp[lo:hi].data_ptr(), 0 if first else 1,
+                dw.data_ptr(), dgates[lo:hi].data_ptr() if stride else _ptr(dgates),
+                df.data_ptr(), _ptr(scratch), stream), "dgb_two_tap_window_vjp")
+            first = False
+            hi = lo
+        if n == 0:
+            dw.zero_()
+            df.zero_()
+        return R, None, dw, dgates, df, None, None, None, None
+
+
+def two_tap_rollout(queue0, slot, weights, gates, fraction, lower, upper, pre_idx=None):
+    """``n = gates.shape[0]`` two-tap steps from row ``slot`` in one launch.
+
+    ``gates[k]`` are step k's gates (per source with ``pre_idx``, else per
+    edge); returns ``(payload, queue)``: ``payload[k]`` is the row delivered at
+    step k (``queue[slot_k]`` before the step), ``queue`` the ring after the
+    last step.  Differentiable in queue0, weights, gates and fraction; the
+    backward runs the reverse sweep on the GPU.  Both taps of every edge must
+    lie in one column (true for transition addresses ``off*width + post``).
+    """
+    _check_queue(queue0)
+    if gates.dim() != 2:
+        raise RuntimeError("rollout gates must be (n_steps, n_sources or n_edges)")
+    n = weights.numel()
+    dev, dt = queue0.device, queue0.dtype
+    _check_vec(weights, dt, n, "weights", dev)
+    _check_vec(fraction, dt, n, "fraction", dev)
+    _check_vec(lower, torch.int64, n, "lower", dev)
+    _check_vec(upper, torch.int64, n, "upper", dev)
+    if pre_idx is not None:
+        _check_vec(pre_idx, torch.int64, n, "source indices", dev)
+    elif gates.shape[1] != n:
+        raise RuntimeError("gates must have one column per edge without pre_idx")
+    if not (gates.device == dev and gates.dtype == dt):
+        raise RuntimeError("gates must match the queue's device and dtype")
+    gates = gates.contiguous()
+    depth, width = queue0.shape
+    slot_t = _slot_tensor(slot, depth, dev)
+    plan = two_tap_plan(depth, width, lower, upper, pre_idx,
+                        gates.shape[1] if pre_idx is not None else 0)
+    if not plan.consistent:
+        raise RuntimeError("two_tap_rollout needs both taps of every edge in one column")
+    return _TwoTapRollout.apply(queue0, slot_t, weights, gates, fraction, lower, upper,
+                                pre_idx, plan)
+
+
+def transition_addresses(offsets, post_idx, depth, width):
+    """Flat (lower, upper) addresses of the two-tap transition."""
+    lower = offsets.remainder(depth) * width + post_idx
+    return lower.contiguous(), (lower + width).remainder(depth * width).contiguous()

@@ -42,6 +42,11 @@
  *   dgb_cable_assemble        the eager per-step assembly of the same update
  *                             (mechanism advance + membrane frame + RHS),
  *                             integrators/core.py:769-834, implicit.py:569-646
+ *   dgb_two_tap_enqueue /     interpolated delays: ordered_two_tap_enqueue,
+ *   dgb_two_tap_vjp /         delay_ring_two_tap_vjp, delay_ring_gather_two_tap
+ *   dgb_two_tap_gather        (networks/_two_tap_enqueue_cpu.cpp:61-315) and
+ *                             dense_interpolated_delay_transition
+ *                             (networks/_event_delivery.py:229-308)
  */
 #ifndef DENDRA_GB300_H
 #define DENDRA_GB300_H
@@ -545,6 +550,145 @@ int dgb_mse_grad(int64_t n, const float* y, const float* target, float scale, fl
  * the array needs clearing; each call writes the bands before reading them.
  */
 int dgb_cable_step_static(const dgb_cable_args* args, int32_t step, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Interpolated (differentiable) delay transport on a dense delivery ring
+ * queue[depth][width] (networks/_event_delivery.py:202-308 and the ordered
+ * CPU op of networks/_two_tap_enqueue_cpu.cpp).
+ *
+ * Edges: weights[e], fraction[e] (upper-tap share), gates[pre_idx[e]] when
+ * pre_idx is non-null (n_sources gates) else gates[e]; lower[e] / upper[e] are
+ * flat ring addresses relative to the start of row *slot, in [0, depth*width):
+ * the destination is (slot*width + address) mod (depth*width), its column
+ * address mod width.
+ *
+ * Column plans: lower_ptr (width+1) / lower_edge (n_edges) list, for every
+ * column, the edges whose lower address lies in it, in ascending edge order
+ * (upper_ptr / upper_edge the same for upper addresses).  One thread owns one
+ * column and adds its values one after another in the order of the
+ * reference's CPU op, so every ring value is bit-identical to it (no
+ * floating-point atomics).  A plan is a function of the addresses only; the
+ * package builds it once per rollout.
+ *
+ * Indices are checked on the device: a slot outside [0, depth), an address
+ * outside the ring, a source index outside [0, n_sources) or a plan entry that
+ * does not match its column is skipped and recorded; dgb_delay_status
+ * returns (and clears) the first such error.
+ * ------------------------------------------------------------------------- */
+#define DGB_DELAY_ERR_SLOT 1
+#define DGB_DELAY_ERR_ADDRESS 2
+#define DGB_DELAY_ERR_SOURCE 3
+#define DGB_DELAY_ERR_PLAN 4
+
+/*
+ * ordered_two_tap_enqueue (networks/_two_tap_enqueue_cpu.cpp:61-126, in place
+ * as ordered_two_tap_enqueue_ :317-328; pure-torch form
+ * dense_interpolated_delay_transition, _event_delivery.py:229-308 with
+ * taps = 2).  When payload is non-null it first receives row *slot (the row
+ * delivered this step, dense_due); then the row is cleared and, for every
+ * edge in order, queue[lower] += (w g) (1 - f), then for every edge in order
+ * queue[upper] += (w g) f, each product and sum rounded separately.
+ */
+int dgb_two_tap_enqueue(int dtype, void* queue, int64_t depth, int64_t width,
+                        const int64_t* slot, int64_t n_edges, const void* weights,
+                        const void* gates, const int64_t* pre_idx, int64_t n_sources,
+                        const void* fraction, const int64_t* lower, const int64_t* upper,
+                        const int64_t* lower_ptr, const int64_t* lower_edge,
+                        const int64_t* upper_ptr, const int64_t* upper_edge, void* payload,
+                        void* stream);
+
+/*
+ * Three-tap form of the same transition (_event_delivery.py:294-306): for
+ * every edge in order and tap t = 0, 1, 2,
+ *   queue[((slot + offsets[e][t]) mod depth) * width + post_idx[e]] += (w g) coeff[e][t].
+ * post_ptr / post_edge: edges by post column in ascending order.
+ */
+int dgb_three_tap_enqueue(int dtype, void* queue, int64_t depth, int64_t width,
+                          const int64_t* slot, int64_t n_edges, const void* weights,
+                          const void* gates, const int64_t* pre_idx, int64_t n_sources,
+                          const void* coeff, const int64_t* offsets, const int64_t* post_idx,
+                          const int64_t* post_ptr, const int64_t* post_edge, void* payload,
+                          void* stream);
+
+/*
+ * delay_ring_gather_two_tap (_two_tap_enqueue_cpu.cpp:206-233):
+ * lower_values[e] = ring[wrap(lower[e] + offset)], upper_values likewise,
+ * wrap = remainder modulo ring_size.  offset is a device scalar.
+ */
+int dgb_two_tap_gather(int dtype, const void* ring, int64_t ring_size, const int64_t* offset,
+                       int64_t n_edges, const int64_t* lower, const int64_t* upper,
+                       void* lower_values, void* upper_values, void* stream);
+
+/*
+ * delay_ring_two_tap_vjp (_two_tap_enqueue_cpu.cpp:235-315) and the unfused
+ * adjoint of _two_tap_enqueue.py:94-150: with lo / hi the cotangent ring read
+ * at the two taps,
+ *   dw = (hi f + lo (1 - f)) g,  dg = (hi f + lo (1 - f)) w,
+ *   df = hi (w g) - lo (w g).
+ * With pre_idx, grad_gates[s] sums its edges' dg in ascending edge order from
+ * +0 (index_select_backward); source_ptr (n_sources+1) / source_edge list the
+ * edges of every source in ascending order.  grad_queue is the cotangent with
+ * row slot cleared; the caller forms it.
+ */
+int dgb_two_tap_vjp(int dtype, const void* ring, int64_t ring_size, const int64_t* offset,
+                    int64_t n_edges, const void* weights, const void* gates,
+                    const int64_t* pre_idx, int64_t n_sources, const void* fraction,
+                    const int64_t* lower, const int64_t* upper, const int64_t* source_ptr,
+                    const int64_t* source_edge, void* grad_weights, void* grad_gates,
+                    void* grad_fraction, void* stream);
+
+/*
+ * Cotangents of the three-tap enqueue, gates per edge (the derivative torch
+ * autograd takes through _event_delivery.py:294-306): with gv_t the ring
+ * cotangent at tap t, grad_coeff[e][t] = gv_t (w g) and, with
+ * s = (gv_0 c_0 + gv_1 c_1) + gv_2 c_2, grad_weights = s g, grad_gates = s w.
+ */
+int dgb_three_tap_vjp(int dtype, const void* ring, int64_t depth, int64_t width,
+                      const int64_t* slot, int64_t n_edges, const void* weights,
+                      const void* gates, const void* coeff, const int64_t* offsets,
+                      const int64_t* post_idx, void* grad_weights, void* grad_gates,
+                      void* grad_coeff, void* stream);
+
+/*
+ * Multi-step rollout of dgb_two_tap_enqueue: n_steps consecutive steps from
+ * row *slot (slot advancing by one, modulo depth, every step) in one launch,
+ * gates[k] holding step k's gates (row stride n_sources, or n_edges without
+ * pre_idx) and payload[k] step k's delivered row.  Requires a consistent
+ * plan: every edge's lower and upper address in the same column, and one
+ * column list (col_ptr / col_edge) for both.  Each column's values are
+ * bit-identical to n_steps single-step calls.
+ */
+int dgb_two_tap_window(int dtype, void* queue, int64_t depth, int64_t width,
+                       const int64_t* slot, int64_t n_steps, int64_t n_edges,
+                       const void* weights, const void* gates, const int64_t* pre_idx,
+                       int64_t n_sources, const void* fraction, const int64_t* lower,
+                       const int64_t* upper, const int64_t* col_ptr, const int64_t* col_edge,
+                       void* payload, void* stream);
+
+/*
+ * Reverse sweep of dgb_two_tap_window over the same n_steps (newest first).
+ * grad_queue (in/out) holds the cotangent of the ring after the window and
+ * leaves holding the cotangent before it; grad_payload[k] is the cotangent of
+ * step k's delivered row (it replaces the cotangent of row slot_k, which the
+ * forward cleared).  Per step the VJP above is taken; grad_weights /
+ * grad_fraction accumulate over steps newest first (stored, not added, at the
+ * newest step when accumulate == 0).  grad_gates[k] receives step k's gate
+ * gradients; with pre_idx the per-edge values go to edge_scratch
+ * (n_steps * n_edges) and are summed per source in ascending edge order.
+ */
+int dgb_two_tap_window_vjp(int dtype, void* grad_queue, int64_t depth, int64_t width,
+                           const int64_t* slot, int64_t n_steps, int64_t n_edges,
+                           const void* weights, const void* gates, const int64_t* pre_idx,
+                           int64_t n_sources, const void* fraction, const int64_t* lower,
+                           const int64_t* upper, const int64_t* col_ptr,
+                           const int64_t* col_edge, const int64_t* source_ptr,
+                           const int64_t* source_edge, const void* grad_payload,
+                           int32_t accumulate, void* grad_weights, void* grad_gates,
+                           void* grad_fraction, void* edge_scratch, void* stream);
+
+/* First device-side index error of the delay kernels since the last call
+   (0 = none, else DGB_DELAY_ERR_*), cleared on read; synchronises stream. */
+int dgb_delay_status(void* stream);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,9 @@ Layers:
     branched-cell network step (``orc_net_run``: Exp2Syn delivery, soma HH,
     tree solve, delay ring), and the reverse mode of the cable update
     (``cable_grad``: full state tape, transposed Thomas solve, gate partials
-    on the forward's branches).
+    on the forward's branches), and the interpolated delay transport
+    (``two_tap_enqueue`` / ``three_tap_enqueue`` / ``two_tap_vjp`` and their
+    multi-step rollouts: the reference's ordered CPU op, sequential adds).
   * ``core.py``  ctypes bindings; builds the C library with gcc on first use.
   The integer/index event primitives (delay rounding, bit packing, sequential
   delivery) are restated inline in ``tests/test_netcon.py``, next to the
@@ -39,4 +41,9 @@ from .core import (  # noqa: F401
     dhs_solve,
     net_run,
     num_threads,
+    two_tap_enqueue,
+    three_tap_enqueue,
+    two_tap_vjp,
+    two_tap_rollout,
+    two_tap_rollout_vjp,
 )

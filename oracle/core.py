@@ -80,6 +80,19 @@ def _declare(L):
             [_I32, _I32, _I64, _I64, _P, _I64] + [_P] * 9 + [_P] * 9 + [_D] * 7
             + [_P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _I64, _I32, _D, _I64, _P, _P, _P, _P, _P,
                _P, _P])
+        getattr(L, "orc_two_tap_enqueue" + sfx).restype = ctypes.c_int
+        getattr(L, "orc_two_tap_enqueue" + sfx).argtypes = (
+            [_I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _P])
+        getattr(L, "orc_three_tap_enqueue" + sfx).restype = ctypes.c_int
+        getattr(L, "orc_three_tap_enqueue" + sfx).argtypes = (
+            [_I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _P])
+        getattr(L, "orc_two_tap_vjp" + sfx).argtypes = (
+            [_I64, _P, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P])
+        getattr(L, "orc_two_tap_rollout" + sfx).restype = ctypes.c_int
+        getattr(L, "orc_two_tap_rollout" + sfx).argtypes = (
+            [_I64, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _P])
+        getattr(L, "orc_two_tap_rollout_vjp" + sfx).argtypes = (
+            [_I64, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P])
     L.orc_num_threads.restype = ctypes.c_int
 
 
@@ -332,3 +345,100 @@ def net_run(pd: dict, n_steps: int):
         _ptr(raster))
     pd["slot"] = int(slot[0])
     return raster
+
+
+# ---------------------------------------------------------------------------
+# Interpolated delay transport (networks/_two_tap_enqueue_cpu.cpp,
+# networks/_event_delivery.py:229-308)
+# ---------------------------------------------------------------------------
+def _edges(dtype, weights, gates, fraction, pre_idx):
+    w = np.ascontiguousarray(weights, dtype=dtype)
+    g = np.ascontiguousarray(gates, dtype=dtype)
+    f = np.ascontiguousarray(fraction, dtype=dtype)
+    pre = None if pre_idx is None else np.ascontiguousarray(pre_idx, dtype=np.int64)
+    n_src = 0 if pre is None else int(g.shape[-1])
+    return w, g, f, pre, n_src
+
+
+def two_tap_enqueue(queue, slot, weights, gates, fraction, lower, upper, pre_idx=None):
+    """ordered_two_tap_enqueue: returns (new queue, delivered row of slot)."""
+    ring = np.array(queue, copy=True, order="C")
+    dtype = ring.dtype
+    depth, width = ring.shape
+    w, g, f, pre, n_src = _edges(dtype, weights, gates, fraction, pre_idx)
+    lower = np.ascontiguousarray(lower, dtype=np.int64)
+    upper = np.ascontiguousarray(upper, dtype=np.int64)
+    payload = np.empty(width, dtype)
+    rc = getattr(lib(), "orc_two_tap_enqueue" + _sfx(dtype))(
+        depth, width, _ptr(ring), int(slot), w.size, _ptr(w), _ptr(g), _ptr(pre), n_src,
+        _ptr(f), _ptr(lower), _ptr(upper), _ptr(payload))
+    if rc:
+        raise IndexError("two-tap address, source or slot outside the ring")
+    return ring, payload
+
+
+def three_tap_enqueue(queue, slot, weights, gates, coeff, offsets, post_idx, pre_idx=None):
+    """Three-tap branch of dense_interpolated_delay_transition (edge-major order)."""
+    ring = np.array(queue, copy=True, order="C")
+    dtype = ring.dtype
+    depth, width = ring.shape
+    w, g, c, pre, n_src = _edges(dtype, weights, gates, coeff, pre_idx)
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    post = np.ascontiguousarray(post_idx, dtype=np.int64)
+    payload = np.empty(width, dtype)
+    rc = getattr(lib(), "orc_three_tap_enqueue" + _sfx(dtype))(
+        depth, width, _ptr(ring), int(slot), w.size, _ptr(w), _ptr(g), _ptr(pre), n_src,
+        _ptr(c), _ptr(offsets), _ptr(post), _ptr(payload))
+    if rc:
+        raise IndexError("three-tap post, source or slot outside the ring")
+    return ring, payload
+
+
+def two_tap_vjp(ring, offset, weights, gates, fraction, lower, upper, pre_idx=None):
+    """delay_ring_two_tap_vjp: (grad_weights, grad_gates, grad_fraction)."""
+    R = np.ascontiguousarray(ring)
+    dtype = R.dtype
+    w, g, f, pre, n_src = _edges(dtype, weights, gates, fraction, pre_idx)
+    lower = np.ascontiguousarray(lower, dtype=np.int64)
+    upper = np.ascontiguousarray(upper, dtype=np.int64)
+    dw, df, dg = np.empty_like(w), np.empty_like(f), np.empty_like(g)
+    getattr(lib(), "orc_two_tap_vjp" + _sfx(dtype))(
+        R.size, _ptr(R), int(offset), w.size, _ptr(w), _ptr(g), _ptr(pre), n_src, _ptr(f),
+        _ptr(lower), _ptr(upper), _ptr(dw), _ptr(dg), _ptr(df))
+    return dw, dg, df
+
+
+def two_tap_rollout(queue, slot0, weights, gates, fraction, lower, upper, pre_idx=None):
+    """n_steps = len(gates) steps: returns (final queue, payload[n_steps][width])."""
+    ring = np.array(queue, copy=True, order="C")
+    dtype = ring.dtype
+    depth, width = ring.shape
+    w, g, f, pre, n_src = _edges(dtype, weights, gates, fraction, pre_idx)
+    lower = np.ascontiguousarray(lower, dtype=np.int64)
+    upper = np.ascontiguousarray(upper, dtype=np.int64)
+    n_steps = g.shape[0]
+    payload = np.empty((n_steps, width), dtype)
+    rc = getattr(lib(), "orc_two_tap_rollout" + _sfx(dtype))(
+        depth, width, _ptr(ring), int(slot0), n_steps, w.size, _ptr(w), _ptr(g), _ptr(pre),
+        n_src, _ptr(f), _ptr(lower), _ptr(upper), _ptr(payload))
+    if rc:
+        raise IndexError("two-tap address, source or slot outside the ring")
+    return ring, payload
+
+
+def two_tap_rollout_vjp(grad_queue, slot0, weights, gates, fraction, lower, upper,
+                        grad_payload, pre_idx=None):
+    """Reverse of two_tap_rollout: (grad_queue0, grad_weights, grad_gates, grad_fraction)."""
+    R = np.array(grad_queue, copy=True, order="C")
+    dtype = R.dtype
+    depth, width = R.shape
+    w, g, f, pre, n_src = _edges(dtype, weights, gates, fraction, pre_idx)
+    lower = np.ascontiguousarray(lower, dtype=np.int64)
+    upper = np.ascontiguousarray(upper, dtype=np.int64)
+    gp = np.ascontiguousarray(grad_payload, dtype=dtype)
+    n_steps = g.shape[0]
+    dw, df, dg = np.zeros_like(w), np.zeros_like(f), np.empty_like(g)
+    getattr(lib(), "orc_two_tap_rollout_vjp" + _sfx(dtype))(
+        depth, width, _ptr(R), int(slot0), n_steps, w.size, _ptr(w), _ptr(g), _ptr(pre), n_src,
+        _ptr(f), _ptr(lower), _ptr(upper), _ptr(gp), _ptr(dw), _ptr(dg), _ptr(df))
+    return R, dw, dg, df

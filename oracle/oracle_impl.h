@@ -870,6 +870,154 @@ void F(orc_net_run)(int32_t n_cells, int32_t n_steps, int64_t step0, int64_t dep
   free(spiked);
 }
 
+/* ---------------------------------------------------------------------------
+ * Interpolated delay transport on a dense ring [depth][width]:
+ *   enqueue  networks/_two_tap_enqueue_cpu.cpp:26-126 (ordered_two_tap_enqueue)
+ *            and networks/_event_delivery.py:229-308 (taps 2 and 3)
+ *   vjp      networks/_two_tap_enqueue_cpu.cpp:235-315 / _two_tap_enqueue.py:94-150
+ * ------------------------------------------------------------------------- */
+
+/* Gate of edge e (pre: per source, else per edge); -1 for a bad source. */
+static int F(tap_gate)(const REAL* g, const int64_t* pre, int64_t n_src, int64_t e, REAL* out) {
+  int64_t s = e;
+  if (pre) {
+    s = pre[e];
+    if (s < 0 || s >= n_src) return -1;
+  }
+  *out = g[s];
+  return 0;
+}
+
+/* One step in place.  Row slot -> payload (if non-null), cleared; every edge in
+ * order adds (w g)(1 - f) at (slot*width + lower) mod size, then every edge in
+ * order (w g) f at its upper address.  Returns 0, or -1 when an address, a
+ * source index or the slot is out of range (the reference's TORCH_CHECKs). */
+int F(orc_two_tap_enqueue)(int64_t depth, int64_t width, REAL* ring, int64_t slot,
+                           int64_t n_edges, const REAL* w, const REAL* g, const int64_t* pre,
+                           int64_t n_src, const REAL* f, const int64_t* lower,
+                           const int64_t* upper, REAL* payload) {
+  const int64_t size = depth * width;
+  if (slot < 0 || slot >= depth) return -1;
+  const int64_t start = slot * width, tail = size - start;
+  for (int64_t c = 0; c < width; ++c) {
+    if (payload) payload[c] = ring[start + c];
+    ring[start + c] = 0;
+  }
+  for (int tap = 0; tap < 2; ++tap) {
+    const int64_t* addr = tap ? upper : lower;
+    for (int64_t e = 0; e < n_edges; ++e) {
+      const int64_t base = addr[e];
+      REAL ge;
+      if (base < 0 || base >= size || F(tap_gate)(g, pre, n_src, e, &ge)) return -1;
+      const int64_t d = base < tail ? start + base : base - tail;
+      const REAL wg = w[e] * ge;
+      const REAL share = tap ? f[e] : (REAL)1 - f[e];
+      ring[d] = ring[d] + wg * share;
+    }
+  }
+  return 0;
+}
+
+/* Three taps: every edge in order, taps 0..2, at
+ * ((slot + offsets[e][t]) mod depth) * width + post[e], value (w g) coeff[e][t]. */
+int F(orc_three_tap_enqueue)(int64_t depth, int64_t width, REAL* ring, int64_t slot,
+                             int64_t n_edges, const REAL* w, const REAL* g, const int64_t* pre,
+                             int64_t n_src, const REAL* coeff, const int64_t* offsets,
+                             const int64_t* post, REAL* payload) {
+  if (slot < 0 || slot >= depth) return -1;
+  for (int64_t c = 0; c < width; ++c) {
+    if (payload) payload[c] = ring[slot * width + c];
+    ring[slot * width + c] = 0;
+  }
+  for (int64_t e = 0; e < n_edges; ++e) {
+    REAL ge;
+    if (post[e] < 0 || post[e] >= width || F(tap_gate)(g, pre, n_src, e, &ge)) return -1;
+    const REAL wg = w[e] * ge;
+    for (int t = 0; t < 3; ++t) {
+      int64_t r = (slot + offsets[3 * e + t]) % depth;
+      if (r < 0) r += depth;
+      const int64_t d = r * width + post[e];
+      ring[d] = ring[d] + wg * coeff[3 * e + t];
+    }
+  }
+  return 0;
+}
+
+static int64_t F(wrap_tap)(int64_t base, int64_t offset, int64_t size) {
+  int64_t r = (int64_t)((uint64_t)base + (uint64_t)offset) % size;
+  return r < 0 ? r + size : r;
+}
+
+/* Cotangents of weights, gates and fractions from the ring cotangent R read
+ * at the two taps (offset = slot*width).  With pre, dg[s] sums its edges'
+ * values in edge order from +0. */
+void F(orc_two_tap_vjp)(int64_t size, const REAL* R, int64_t offset, int64_t n_edges,
+                        const REAL* w, const REAL* g, const int64_t* pre, int64_t n_src,
+                        const REAL* f, const int64_t* lower, const int64_t* upper, REAL* dw,
+                        REAL* dg, REAL* df) {
+  if (pre)
+    for (int64_t s = 0; s < n_src; ++s) dg[s] = 0;
+  for (int64_t e = 0; e < n_edges; ++e) {
+    int64_t s = e;
+    if (pre) {
+      s = pre[e];
+      if (s < 0) s += n_src;
+    }
+    const REAL lo = R[F(wrap_tap)(lower[e], offset, size)];
+    const REAL hi = R[F(wrap_tap)(upper[e], offset, size)];
+    const REAL dweighted = hi * f[e] + lo * ((REAL)1 - f[e]);
+    const REAL weighted = w[e] * g[s];
+    dw[e] = dweighted * g[s];
+    df[e] = hi * weighted - lo * weighted;
+    const REAL gg = dweighted * w[e];
+    if (pre)
+      dg[s] = dg[s] + gg;
+    else
+      dg[e] = gg;
+  }
+}
+
+/* n_steps enqueue steps from slot0, gates[k] of stride n_src (pre) or n_edges,
+ * payload[k][width]. */
+int F(orc_two_tap_rollout)(int64_t depth, int64_t width, REAL* ring, int64_t slot0,
+                           int64_t n_steps, int64_t n_edges, const REAL* w, const REAL* gates,
+                           const int64_t* pre, int64_t n_src, const REAL* f,
+                           const int64_t* lower, const int64_t* upper, REAL* payload) {
+  const int64_t stride = pre ? n_src : n_edges;
+  for (int64_t k = 0; k < n_steps; ++k) {
+    if (F(orc_two_tap_enqueue)(depth, width, ring, (slot0 + k) % depth, n_edges, w,
+                               gates + k * stride, pre, n_src, f, lower, upper,
+                               payload ? payload + k * width : 0))
+      return -1;
+  }
+  return 0;
+}
+
+/* Reverse of orc_two_tap_rollout, newest step first: per step the VJP at the
+ * cotangent R of the ring after the step (dw, df accumulated newest first,
+ * stored at the newest step), then R[row slot_k] = gpay[k]. */
+void F(orc_two_tap_rollout_vjp)(int64_t depth, int64_t width, REAL* R, int64_t slot0,
+                                int64_t n_steps, int64_t n_edges, const REAL* w,
+                                const REAL* gates, const int64_t* pre, int64_t n_src,
+                                const REAL* f, const int64_t* lower, const int64_t* upper,
+                                const REAL* gpay, REAL* dw, REAL* dgates, REAL* df) {
+  const int64_t stride = pre ? n_src : n_edges;
+  REAL* tw = (REAL*)malloc(sizeof(REAL) * (size_t)(n_edges + 1));
+  REAL* tf = (REAL*)malloc(sizeof(REAL) * (size_t)(n_edges + 1));
+  for (int64_t k = n_steps - 1; k >= 0; --k) {
+    const int64_t slot = (slot0 + k) % depth;
+    F(orc_two_tap_vjp)(depth * width, R, slot * width, n_edges, w, gates + k * stride, pre,
+                       n_src, f, lower, upper, tw, dgates + k * stride, tf);
+    for (int64_t e = 0; e < n_edges; ++e) {
+      dw[e] = (k == n_steps - 1) ? tw[e] : dw[e] + tw[e];
+      df[e] = (k == n_steps - 1) ? tf[e] : df[e] + tf[e];
+    }
+    for (int64_t c = 0; c < width; ++c) R[slot * width + c] = gpay ? gpay[k * width + c] : 0;
+  }
+  free(tw);
+  free(tf);
+}
+
 #undef AM1
 #undef AH1
 #undef AN1

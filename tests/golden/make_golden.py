@@ -17,6 +17,12 @@ compatibility shims) and records its outputs on seeded inputs:
   adjoint_f64.npz          reference autograd gradients (gnabar, gkbar, gl, Ra) of
                            a somatic-trace MSE through the CPU cable update
   block3.npz               block_pcr_solve_t on 3x3 block-tridiagonal systems
+  delay_{f64,f32}.npz      interpolated delays: the reference's ordered two-tap
+                           CPU op and its VJP/gather ops (compiled from the
+                           reference's _two_tap_enqueue_cpu.cpp by
+                           torch.utils.cpp_extension into oracle/_ref/), the
+                           pure-torch dense_interpolated_delay_transition (two
+                           and three taps) and a 40-step rollout with autograd
 
 Usage (in a container that holds the reference source):
 
@@ -359,9 +365,117 @@ def adjoint():
     print("adjoint", out["loss"], {k: out["grad_" + k] for k in defaults})
 
 
+def _two_tap_ops():
+    """The reference's ordered two-tap CPU operators, built from its source."""
+    os.environ.setdefault("TORCH_EXTENSIONS_DIR",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "oracle", "_ref",
+                                       "torch_ext"))
+    from dendra.models.networks._two_tap_enqueue import get_cpu_two_tap_enqueue
+
+    get_cpu_two_tap_enqueue()
+    return torch.ops.dendra_native
+
+
+def delay(dtype, tag):
+    _ref()
+    from dendra.models.networks._event_delivery import (
+        delay_interpolation, dense_due, dense_interpolated_delay_transition)
+
+    ops = _two_tap_ops()
+    out = {}
+    rng = np.random.default_rng(77 if tag == "f64" else 78)
+    T = lambda a: torch.as_tensor(np.asarray(a)).to(dtype)  # noqa: E731
+    L = lambda a: torch.as_tensor(np.asarray(a), dtype=torch.long)  # noqa: E731
+
+    # one step of the ordered op: heavy collisions, a tap on the slot row
+    depth, width, E, n_src = 7, 5, 48, 6
+    post = rng.integers(0, width, E)
+    lam = rng.uniform(1.0, 7.6, E)
+    dt = 0.025
+    delays = lam * dt
+    off, frac = delay_interpolation(T(delays), T([dt]), dtype=dtype, taps=2, sigma=0.0)
+    lower = (off.remainder(depth) * width + L(post))
+    upper = (lower + width).remainder(depth * width)
+    general_upper = L(rng.integers(0, depth * width, E))  # any column
+    w = rng.standard_normal(E)
+    g = rng.random(E)
+    g[rng.random(E) < 0.3] = 0.0
+    g_src = rng.random(n_src)
+    pre = rng.integers(0, n_src, E)
+    queue = rng.standard_normal((depth, width))
+    slot = 3
+    out.update(depth=depth, width=width, post=post, delays=delays, dt=dt, w=w, g=g,
+               g_src=g_src, pre=pre, queue=queue, slot=slot, lower=lower.numpy(),
+               upper=upper.numpy(), fraction=frac.numpy(), general_upper=general_upper.numpy())
+    Q, S = T(queue), L([slot])
+    out["op_edge"] = ops.ordered_two_tap_enqueue(Q, S, T(w), T(g), frac, lower, upper).numpy()
+    out["op_src"] = ops.ordered_two_tap_enqueue_from_source(
+        Q, S, T(w), T(g_src), frac, lower, upper, L(pre)).numpy()
+    out["op_general"] = ops.ordered_two_tap_enqueue(
+        Q, S, T(w), T(g), frac, lower, general_upper).numpy()
+    pure = dense_interpolated_delay_transition(
+        Q, S, L([0]), T(w), T(g), T(delays), T([dt]), post_idx=L(post), depth=depth,
+        width=width, taps=2, sigma=0.0).queue.numpy()
+    assert np.array_equal(pure, out["op_edge"]), "ordered op != pure-torch transition"
+    cot = rng.standard_normal((depth, width))
+    out["cot"] = cot
+    for name, src in (("edge", None), ("src", L(pre))):
+        gates = T(g) if src is None else T(g_src)
+        dw, dg, df = ops.delay_ring_two_tap_vjp(T(cot), L([slot * width]), T(w), gates, frac,
+                                                lower, upper, src)
+        out[f"vjp_{name}_dw"], out[f"vjp_{name}_dg"], out[f"vjp_{name}_df"] = (
+            dw.numpy(), dg.numpy(), df.numpy())
+    lo, hi = ops.delay_ring_gather_two_tap(T(cot), L([slot * width]), lower, upper)
+    out["gather_lo"], out["gather_hi"] = lo.numpy(), hi.numpy()
+
+    # three taps, one step, with autograd of weights / gates / coefficients
+    sigma = 0.6
+    off3, c3 = delay_interpolation(T(delays), T([dt]), dtype=dtype, taps=3, sigma=sigma)
+    wt, gt, ct = (T(w).requires_grad_(), T(g).requires_grad_(), c3.detach().requires_grad_())
+    q3 = dense_interpolated_delay_transition(
+        Q, S, L([0]), wt, gt, None, None, post_idx=L(post), depth=depth, width=width,
+        taps=3, sigma=sigma, delay_taps=(off3, ct)).queue
+    (q3 * T(cot)).sum().backward()
+    out.update(sigma=sigma, offsets3=off3.numpy(), coeff3=c3.detach().numpy(),
+               three_tap=q3.detach().numpy(), three_dw=wt.grad.numpy(),
+               three_dg=gt.grad.numpy(), three_dc=ct.grad.numpy())
+
+    # a rollout with autograd: source gates per step, delays differentiated
+    depth, width, E, n_src, steps = 9, 6, 24, 5, 40
+    post = rng.integers(0, width, E)
+    pre = rng.integers(0, n_src, E)
+    delays = rng.uniform(1.0, 8.7, E) * dt
+    w = rng.standard_normal(E)
+    gates = rng.random((steps, n_src))
+    gates[rng.random((steps, n_src)) < 0.5] = 0.0
+    queue0 = rng.standard_normal((depth, width))
+    cpay = rng.standard_normal((steps, width))
+    cfin = rng.standard_normal((depth, width))
+    wt, gt, dlt, qt = (T(w).requires_grad_(), T(gates).requires_grad_(),
+                       T(delays).requires_grad_(), T(queue0).requires_grad_())
+    queue, slot, gs = qt, L([2]), L([0])
+    payloads = []
+    for k in range(steps):
+        payloads.append(dense_due(queue, slot).payload)
+        src_g = gt[k].index_select(0, L(pre))
+        queue, slot, gs, _ = dense_interpolated_delay_transition(
+            queue, slot, gs, wt, src_g, dlt, T([dt]), post_idx=L(post), depth=depth,
+            width=width, taps=2, sigma=0.0)
+    pay = torch.stack(payloads)
+    loss = (pay * T(cpay)).sum() + (queue * T(cfin)).sum()
+    loss.backward()
+    out.update(r_depth=depth, r_width=width, r_post=post, r_pre=pre, r_delays=delays, r_w=w,
+               r_gates=gates, r_queue0=queue0, r_slot0=2, r_cpay=cpay, r_cfin=cfin,
+               r_payload=pay.detach().numpy(), r_final=queue.detach().numpy(),
+               r_dw=wt.grad.numpy(), r_dgates=gt.grad.numpy(), r_ddelays=dlt.grad.numpy(),
+               r_dqueue0=qt.grad.numpy())
+    np.savez_compressed(os.path.join(HERE, f"delay_{tag}.npz"), **out)
+    print("delay", tag)
+
+
 if __name__ == "__main__":
     what = sys.argv[1:] or ["rates", "tridiag", "dhs", "events", "cable", "extra", "adjoint",
-                            "block3"]
+                            "block3", "delay"]
     if "rates" in what:
         rates()
     if "tridiag" in what:
@@ -380,3 +494,6 @@ if __name__ == "__main__":
         adjoint()
     if "block3" in what:
         block3()
+    if "delay" in what:
+        delay(torch.float64, "f64")
+        delay(torch.float32, "f32")

@@ -119,3 +119,29 @@ def test_block3_contract_errors_on_the_host():
     L = dendra_gb300.load()
     assert L.dgb_block3_work_size(0, 10, 7) == 0
     assert L.dgb_block3_solve(0, 0, 4, None, None, None, None, None, None, 0, None) == -1
+
+
+def test_delay_contract_errors_on_the_host():
+    """Argument errors of the interpolated-delay entry points come back before
+    any launch (dummy pointers are never dereferenced)."""
+    L = dendra_gb300.load()
+    p = 16  # a non-null address that is never touched
+    # dtype
+    assert L.dgb_two_tap_enqueue(7, p, 4, 4, p, 1, p, p, None, 0, p, p, p, p, p, p, p, None,
+                                 None) == -1
+    # an empty ring cannot receive edges
+    assert L.dgb_two_tap_enqueue(0, p, 4, 0, p, 3, p, p, None, 0, p, p, p, p, p, p, p, None,
+                                 None) == -1
+    assert b"Empty ring" in L.dgb_last_error()
+    # missing column plan
+    assert L.dgb_two_tap_enqueue(0, p, 4, 4, p, 3, p, p, None, 0, p, p, p, None, p, p, p, None,
+                                 None) == -1
+    # source indices without sources
+    assert L.dgb_two_tap_window(0, p, 4, 4, p, 2, 3, p, p, p, 0, p, p, p, p, p, None,
+                                None) == -1
+    # negative step count
+    assert L.dgb_two_tap_window_vjp(1, p, 4, 4, p, -1, 3, p, p, None, 0, p, p, p, p, p, None,
+                                    None, None, 0, p, p, p, None, None) == -1
+    # gather of an empty ring
+    assert L.dgb_two_tap_gather(0, p, 0, p, 3, p, p, p, p, None) == -1
+    assert L.dgb_three_tap_vjp(0, p, 0, 4, p, 2, p, p, p, p, p, p, p, p, None) == -1
