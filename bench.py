@@ -672,7 +672,8 @@ def bench_delay(args, world, rank, local):
     scale: 409,600 connections from 4,096 sources into a [201][409,600] ring,
     a 2,000-step rollout forward (one launch) and its reverse sweep (one launch
     + the per-source gate reduction) through two_tap_rollout and autograd.
-    One bench step = forward + backward; unit = connection-steps/s."""
+    The rollout starts from an empty ring.  One bench step = forward +
+    backward; unit = connection-steps/s."""
     import torch
 
     import oracle
@@ -720,7 +721,6 @@ def bench_delay(args, world, rank, local):
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
     tw, tf, tlo, tup, tpre = T(w), T(frac), T(lower), T(upper), T(pre)
     tg = gates_h.to(dev)
-    q0 = torch.zeros(depth, n_conn, dtype=torch.float32, device=dev)
     gpay = torch.randn(steps, n_conn, dtype=torch.float32, device=dev,
                        generator=torch.Generator(dev).manual_seed(5))
     leaves = [t.requires_grad_() for t in (tw, tg, tf)]
@@ -728,7 +728,8 @@ def bench_delay(args, world, rank, local):
     def step():
         for t in leaves:
             t.grad = None
-        pay, fin = delays.two_tap_rollout(q0, 0, tw, tg, tf, tlo, tup, tpre)
+        pay, fin = delays.two_tap_rollout(None, 0, tw, tg, tf, tlo, tup, tpre, depth=depth,
+                                          width=n_conn)
         torch.autograd.backward([pay], [gpay])
         return pay
 
@@ -744,7 +745,8 @@ def bench_delay(args, world, rank, local):
             e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record(st)
             with torch.no_grad():
-                delays.two_tap_rollout(q0, 0, tw, tg, tf, tlo, tup, tpre)
+                delays.two_tap_rollout(None, 0, tw, tg, tf, tlo, tup, tpre, depth=depth,
+                                       width=n_conn)
             e1.record(st)
             e1.synchronize()
             fwd.append(e0.elapsed_time(e1))
@@ -775,8 +777,8 @@ def bench_delay(args, world, rank, local):
     e2e_s = (time.perf_counter() - t0) / args.steps
     # check a prefix of the rollout against the oracle
     n_chk = 200
-    pay = delays.two_tap_rollout(q0, 0, tw.detach(), tg.detach()[:n_chk], tf.detach(), tlo, tup,
-                                 tpre)[0]
+    pay = delays.two_tap_rollout(None, 0, tw.detach(), tg.detach()[:n_chk], tf.detach(), tlo,
+                                 tup, tpre, depth=depth, width=n_conn)[0]
     t0 = time.perf_counter()
     _, opay = oracle.two_tap_rollout(np.zeros((depth, n_conn), np.float32), 0, w,
                                      gates_h[:n_chk].numpy(), frac, lower, upper, pre_idx=pre)
@@ -793,10 +795,11 @@ def bench_delay(args, world, rank, local):
         "forward_ms": ms_fwd, "forward_connection_steps_per_s": units / (ms_fwd * 1e-3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": "two_tap_window_kernel",
+                     "kernel": "two_tap_rollout_kernel",
                      "note": f"{DELAY_BYTES_PER_CONN_STEP} algorithmic B per float32 "
                              "connection-step of the unfused per-step op; forward rollout "
-                             f"(one launch) timed alone; peak {peak_kind}"},
+                             "(one launch, ring in shared memory) timed alone; peak "
+                             f"{peak_kind}"},
         "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": 3,

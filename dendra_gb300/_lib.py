@@ -110,11 +110,11 @@ SIGNATURES = {
                                _P, _P, _P, _P]),
     "dgb_three_tap_vjp": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P,
                                  _P, _P]),
-    "dgb_two_tap_window": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64, _P,
-                                  _P, _P, _P, _P, _P, _P]),
-    "dgb_two_tap_window_vjp": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64,
-                                      _P, _P, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P, _P,
-                                      _P]),
+    "dgb_two_tap_rollout": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64, _P,
+                                   _P, _P, _P, _P, _I32, _P, _P]),
+    "dgb_two_tap_rollout_vjp": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64,
+                                       _P, _P, _P, _P, _P, _I32, _P, _P, _P, _I32, _P, _P, _P,
+                                       _P, _P]),
     "dgb_delay_status": (_INT, [_P]),
 }
 

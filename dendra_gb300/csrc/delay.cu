@@ -11,7 +11,8 @@
 //                           networks/_two_tap_enqueue.py:94-150
 //   dgb_three_tap_vjp       torch autograd of the three-tap scatter (gather of the
 //                           cotangent, products, tap sum in order)
-//   dgb_two_tap_window(_vjp) many steps of the above in one launch (rollouts)
+//   dgb_two_tap_rollout(_vjp) many steps of the above in one launch, each
+//                           block's ring columns held in shared memory
 //
 // Determinism: the reference's CPU op adds every edge's lower-tap value in
 // edge order, then every upper-tap value in edge order, into a ring it owns
@@ -20,6 +21,8 @@
 // each ring value sees exactly the reference's sequence of additions: results
 // are bit-identical, with no floating-point atomics.  Every product and sum is
 // rounded on its own (no FMA contraction), as the CPU op computes them.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace dgb {
@@ -307,107 +310,280 @@ __global__ void three_tap_vjp_kernel(const T* __restrict__ R, int64_t depth, int
   dg[e] = mul_rn(dwg, w);
 }
 
-// n_steps enqueue steps, thread = column (consistent plan: both taps of an
-// edge in its column).  Columns never touch each other, so no step needs a
-// grid-wide barrier; the addresses are checked against the column once.
+// ---------------------------------------------------------------------------
+// Rollouts: many steps per launch, the ring on chip.
+//
+// One thread owns one ring column for the whole rollout: its values never
+// leave the thread, so no step needs a barrier and the whole rollout is one
+// launch.  A block keeps its columns' full ring depth in shared memory
+// (row-major [depth][block], so a warp's accesses hit 32 distinct banks
+// whatever rows its lanes touch); the ring is read from HBM once at the start
+// and written once at the end, and the delivered rows leave as coalesced
+// stores.  Rings too deep for shared memory run in place in HBM.  Plan: the
+// column lists col_ptr / col_edge (edges ascending) and, per list position j,
+// the row distances lo_row[j] / hi_row[j] in [0, depth) of the edge's taps.
+// ---------------------------------------------------------------------------
+
+// A rollout thread's column (32-bit: the host checks depth*width, n_edges and
+// n_sources against 2^31).  A column with exactly one edge (n == 1) keeps that
+// edge's operands in registers; others read their lists every step.  n < 0
+// marks a column outside the ring or one that failed its checks (left
+// untouched, error recorded).
 template <typename T>
-__global__ void __launch_bounds__(256)
-    two_tap_window_kernel(T* __restrict__ ring, int64_t depth, int64_t width,
-                          const int64_t* __restrict__ slot_ptr, int64_t n_steps, TapEdges<T> E,
-                          const T* __restrict__ gates, int64_t gate_stride,
-                          const int64_t* __restrict__ lower, const int64_t* __restrict__ upper,
-                          const int64_t* __restrict__ ptr, const int64_t* __restrict__ edge,
-                          T* __restrict__ payload) {
-  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+struct RollCol {
+  int32_t j0, n, src, e, lo, hi;
+  T w, f;
+};
+
+__device__ __forceinline__ int32_t tap_row32(int32_t slot, int32_t d, int32_t depth) {
+  const int32_t r = slot + d;
+  return r >= depth ? r - depth : r;
+}
+
+template <typename T>
+__device__ __forceinline__ void roll_col_load(RollCol<T>& C, int64_t col, int64_t depth,
+                                              int64_t width, const TapEdges<T>& E,
+                                              const int64_t* __restrict__ ptr,
+                                              const int64_t* __restrict__ edge,
+                                              const int32_t* __restrict__ lo_row,
+                                              const int32_t* __restrict__ hi_row) {
+  C.n = -1;
   if (col >= width) return;
-  int64_t slot = slot_ptr[0];
-  if (slot < 0 || slot >= depth) {
-    if (col == 0) delay_fail(DGB_DELAY_ERR_SLOT);
-    return;
-  }
-  const int64_t size = depth * width;
-  {  // the column's addresses, once
-    int64_t j0, j1;
-    if (!column_range(ptr, col, E.n_edges, j0, j1)) return;
-    for (int64_t j = j0; j < j1; ++j) {
-      const int64_t e = edge[j];
-      if ((uint64_t)e >= (uint64_t)E.n_edges || (uint64_t)lower[e] >= (uint64_t)size ||
-          (uint64_t)upper[e] >= (uint64_t)size || lower[e] % width != col ||
-          upper[e] % width != col) {
-        delay_fail(DGB_DELAY_ERR_PLAN);
-        return;
-      }
+  int64_t j0, j1;
+  if (!column_range(ptr, col, E.n_edges, j0, j1)) return;
+  for (int64_t j = j0; j < j1; ++j) {
+    const int64_t e = edge[j];
+    if ((uint64_t)e >= (uint64_t)E.n_edges || (uint32_t)lo_row[j] >= (uint64_t)depth ||
+        (uint32_t)hi_row[j] >= (uint64_t)depth ||
+        (E.pre && (uint64_t)E.pre[e] >= (uint64_t)E.n_src)) {
+      delay_fail(DGB_DELAY_ERR_PLAN);
+      return;
     }
   }
-  for (int64_t k = 0; k < n_steps; ++k) {
-    const RingPos P = ring_pos(slot, width, size);
-    const T* g = gates + k * gate_stride;
-    if (payload) payload[k * width + col] = ring[P.start + col];
-    ring[P.start + col] = T(0);
-    column_taps<T, false, false>(ring, P, width, col, E, g, lower, ptr, edge);
-    column_taps<T, true, false>(ring, P, width, col, E, g, upper, ptr, edge);
-    if (++slot == depth) slot = 0;
+  C.j0 = (int32_t)j0;
+  C.n = (int32_t)(j1 - j0);
+  if (C.n == 1) {
+    const int64_t e = edge[j0];
+    C.e = (int32_t)e;
+    C.lo = lo_row[j0];
+    C.hi = hi_row[j0];
+    C.src = (int32_t)(E.pre ? E.pre[e] : e);
+    C.w = E.w[e];
+    C.f = E.f[e];
   }
 }
 
-// Reverse of two_tap_window_kernel, thread = column, steps newest first.
+// Ring column of a rollout thread: element r at rb[r * rs].
+template <typename T>
+struct ColRing {
+  T* rb;
+  int32_t rs;
+  __device__ __forceinline__ T& operator[](int32_t r) const { return rb[(int64_t)r * rs]; }
+};
+
+// One step of a column with several edges: clear the delivered value, then
+// both taps of every edge, lower taps in list order, then upper taps.  Out of
+// line: rare, and inlined it would raise every thread's register count.
+template <typename T>
+__device__ __noinline__ void roll_col_generic(ColRing<T> R, int32_t slot, int32_t depth,
+                                              int32_t j0, int32_t n, TapEdges<T> E,
+                                              const T* __restrict__ g,
+                                              const int64_t* __restrict__ edge,
+                                              const int32_t* __restrict__ lo_row,
+                                              const int32_t* __restrict__ hi_row) {
+  R[slot] = T(0);
+  for (int tap = 0; tap < 2; ++tap) {
+    for (int32_t j = j0; j < j0 + n; ++j) {
+      const int64_t e = edge[j];
+      const T wg = mul_rn(E.w[e], g[E.pre ? E.pre[e] : e]);
+      const T fe = E.f[e];
+      const T share = tap ? fe : sub_rn(T(1), fe);
+      T& v = R[tap_row32(slot, tap ? hi_row[j] : lo_row[j], depth)];
+      v = add_rn(v, mul_rn(wg, share));
+    }
+  }
+}
+
+// Reverse step of a column with several edges (see the reverse kernel).
 template <typename T, bool PRE>
-__global__ void __launch_bounds__(256)
-    two_tap_window_vjp_kernel(T* __restrict__ R, int64_t depth, int64_t width,
-                              const int64_t* __restrict__ slot_ptr, int64_t n_steps,
-                              TapEdges<T> E, const T* __restrict__ gates, int64_t gate_stride,
-                              const int64_t* __restrict__ lower,
-                              const int64_t* __restrict__ upper,
-                              const int64_t* __restrict__ ptr, const int64_t* __restrict__ edge,
-                              const T* __restrict__ gpay, int accumulate, T* __restrict__ dw,
-                              T* __restrict__ dgate, T* __restrict__ df,
-                              T* __restrict__ scratch) {
+__device__ __noinline__ void roll_col_generic_vjp(ColRing<T> R, int32_t slot, int32_t depth,
+                                                  int32_t j0, int32_t n, TapEdges<T> E,
+                                                  const T* __restrict__ g,
+                                                  const int64_t* __restrict__ edge,
+                                                  const int32_t* __restrict__ lo_row,
+                                                  const int32_t* __restrict__ hi_row, bool first,
+                                                  T* __restrict__ dw, T* __restrict__ df,
+                                                  T* __restrict__ gate_out) {
+  for (int32_t j = j0; j < j0 + n; ++j) {
+    const int64_t e = edge[j];
+    T dwk, dgk, dfk;
+    edge_vjp(R[tap_row32(slot, lo_row[j], depth)], R[tap_row32(slot, hi_row[j], depth)],
+             E.w[e], g[PRE ? E.pre[e] : e], E.f[e], dwk, dgk, dfk);
+    dw[e] = first ? dwk : add_rn(dw[e], dwk);
+    df[e] = first ? dfk : add_rn(df[e], dfk);
+    gate_out[PRE ? j : e] = dgk;
+  }
+}
+
+constexpr int kRollBlock = 128;
+
+// The thread's ring column: in shared memory (loaded from HBM, or zeros when
+// the rollout starts empty) or, for deep rings, in place in HBM.
+template <typename T, bool SMEM>
+__device__ __forceinline__ ColRing<T> roll_ring(T* ring, int64_t width, int64_t col,
+                                                int32_t depth, bool live, bool empty) {
+  if (SMEM) {
+    extern __shared__ __align__(16) unsigned char roll_smem[];
+    ColRing<T> R{reinterpret_cast<T*>(roll_smem) + threadIdx.x, (int32_t)blockDim.x};
+    if (live)
+      for (int32_t r = 0; r < depth; ++r) R[r] = empty ? T(0) : ring[(int64_t)r * width + col];
+    return R;
+  }
+  ColRing<T> R{ring + col, (int32_t)width};
+  if (live && empty)
+    for (int32_t r = 0; r < depth; ++r) R[r] = T(0);
+  return R;
+}
+
+// n_steps steps from row *slot: deliver row slot (payload[k][col]), clear it,
+// add both taps of every edge.  Thread = external column.
+template <typename T, bool SMEM, bool ONE>
+__global__ void __launch_bounds__(kRollBlock)
+    two_tap_rollout_kernel(T* __restrict__ ring, int64_t depth, int64_t width,
+                           const int64_t* __restrict__ slot_ptr, int64_t n_steps, TapEdges<T> E,
+                           const T* __restrict__ gates, int64_t gate_stride,
+                           const int64_t* __restrict__ ptr, const int64_t* __restrict__ edge,
+                           const int32_t* __restrict__ lo_row,
+                           const int32_t* __restrict__ hi_row, int flags,
+                           T* __restrict__ payload) {
   const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= width) return;
   const int64_t slot0 = slot_ptr[0];
   if (slot0 < 0 || slot0 >= depth) {
     if (col == 0) delay_fail(DGB_DELAY_ERR_SLOT);
     return;
   }
-  const int64_t size = depth * width;
-  int64_t j0, j1;
-  if (!column_range(ptr, col, E.n_edges, j0, j1)) return;
-  for (int64_t j = j0; j < j1; ++j) {
-    const int64_t e = edge[j];
-    if ((uint64_t)e >= (uint64_t)E.n_edges || (uint64_t)lower[e] >= (uint64_t)size ||
-        (uint64_t)upper[e] >= (uint64_t)size || lower[e] % width != col ||
-        upper[e] % width != col ||
-        (PRE && (uint64_t)E.pre[e] >= (uint64_t)E.n_src)) {
-      delay_fail(DGB_DELAY_ERR_PLAN);
-      return;
-    }
+  RollCol<T> C;
+  roll_col_load(C, col, depth, width, E, ptr, edge, lo_row, hi_row);
+  if (ONE && C.n > 1) {  // the lean variant was promised one edge per column
+    delay_fail(DGB_DELAY_ERR_PLAN);
+    C.n = -1;
   }
-  int64_t slot = (slot0 + n_steps - 1) % depth;
-  for (int64_t k = n_steps - 1; k >= 0; --k) {
-    const RingPos P = ring_pos(slot, width, size);
+  const bool live = C.n >= 0;
+  const int32_t D = (int32_t)depth;
+  const ColRing<T> R =
+      roll_ring<T, SMEM>(ring, width, col, D, live, (flags & DGB_ROLLOUT_EMPTY_START) != 0);
+  if (!live) return;
+  int32_t slot = (int32_t)slot0;
+  T gnext = (C.n == 1 && n_steps > 0) ? gates[C.src] : T(0);
+  for (int64_t k = 0; k < n_steps; ++k) {
     const T* g = gates + k * gate_stride;
-    const bool store = (k == n_steps - 1) && !accumulate;
-    for (int64_t j = j0; j < j1; ++j) {
-      const int64_t e = edge[j];
-      const int64_t bl = lower[e], bu = upper[e];
-      const T lo = R[bl < P.tail ? P.start + bl : bl - P.tail];
-      const T hi = R[bu < P.tail ? P.start + bu : bu - P.tail];
-      const int64_t s = PRE ? E.pre[e] : e;
-      T dwk, dgk, dfk;
-      edge_vjp(lo, hi, E.w[e], g[s], E.f[e], dwk, dgk, dfk);
-      dw[e] = store ? dwk : add_rn(dw[e], dwk);
-      df[e] = store ? dfk : add_rn(df[e], dfk);
-      if (PRE)
-        scratch[k * E.n_edges + e] = dgk;
+    const T gk = gnext;
+    if (C.n == 1 && k + 1 < n_steps) gnext = g[gate_stride + C.src];  // next step's gate
+    if (C.n == 1) {
+      // all three loads first, then the reference's order: clear, lower tap,
+      // upper tap (a tap may land on the cleared row, or both on one value)
+      const int32_t rl = tap_row32(slot, C.lo, D), rh = tap_row32(slot, C.hi, D);
+      const T vs = R[slot], vl = R[rl], vh = R[rh];
+      if (payload) payload[k * width + col] = vs;
+      const T wg = mul_rn(C.w, gk);
+      const T a = mul_rn(wg, sub_rn(T(1), C.f)), b = mul_rn(wg, C.f);
+      T ns = T(0), l = vl, h = vh;
+      if (rl == slot)
+        ns = add_rn(ns, a);
       else
-        dgate[k * gate_stride + e] = dgk;
+        l = add_rn(l, a);
+      if (rh == slot)
+        ns = add_rn(ns, b);
+      else if (rh == rl)
+        l = add_rn(l, b);
+      else
+        h = add_rn(h, b);
+      R[slot] = ns;
+      if (rl != slot) R[rl] = l;
+      if (rh != slot && rh != rl) R[rh] = h;
+    } else {
+      if (payload) payload[k * width + col] = R[slot];
+      if (ONE || C.n == 0)
+        R[slot] = T(0);
+      else
+        roll_col_generic(R, slot, D, C.j0, C.n, E, g, edge, lo_row, hi_row);
     }
-    R[P.start + col] = gpay ? gpay[k * width + col] : T(0);
-    slot = slot == 0 ? depth - 1 : slot - 1;
+    if (++slot == D) slot = 0;
   }
+  if (SMEM && !(flags & DGB_ROLLOUT_NO_FINAL))
+    for (int32_t r = 0; r < D; ++r) ring[(int64_t)r * width + col] = R[r];
 }
 
-// dgate[k][s] = sum of scratch[k][e] over the source's edges, ascending, from +0.
+// Reverse sweep of two_tap_rollout_kernel over the same steps, newest first,
+// on the cotangent ring (grad_ring: in, after the rollout; out, before it).
+// Per step and edge the two-tap VJP at the cotangent of the ring after the
+// step; weight and share cotangents accumulate newest first (in registers for
+// one-edge columns); gate cotangents go to scratch[k][j] (with sources, j =
+// list position) or dgate[k][e]; then row slot_k takes the delivered row's
+// cotangent gpay[k][col].
+template <typename T, bool SMEM, bool PRE, bool ONE>
+__global__ void __launch_bounds__(kRollBlock)
+    two_tap_rollout_vjp_kernel(T* __restrict__ ring, int64_t depth, int64_t width,
+                               const int64_t* __restrict__ slot_ptr, int64_t n_steps,
+                               TapEdges<T> E, const T* __restrict__ gates, int64_t gate_stride,
+                               const int64_t* __restrict__ ptr, const int64_t* __restrict__ edge,
+                               const int32_t* __restrict__ lo_row,
+                               const int32_t* __restrict__ hi_row, int flags,
+                               const T* __restrict__ gpay, int accumulate, T* __restrict__ dw,
+                               T* __restrict__ dgate, T* __restrict__ df,
+                               T* __restrict__ scratch) {
+  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t slot0 = slot_ptr[0];
+  if (slot0 < 0 || slot0 >= depth) {
+    if (col == 0) delay_fail(DGB_DELAY_ERR_SLOT);
+    return;
+  }
+  RollCol<T> C;
+  roll_col_load(C, col, depth, width, E, ptr, edge, lo_row, hi_row);
+  if (ONE && C.n > 1) {
+    delay_fail(DGB_DELAY_ERR_PLAN);
+    C.n = -1;
+  }
+  const bool live = C.n >= 0;
+  const int32_t D = (int32_t)depth;
+  const ColRing<T> R =
+      roll_ring<T, SMEM>(ring, width, col, D, live, (flags & DGB_ROLLOUT_EMPTY_START) != 0);
+  if (!live) return;
+  T aw = T(0), af = T(0);
+  if (C.n == 1 && accumulate) {
+    aw = dw[C.e];
+    af = df[C.e];
+  }
+  int32_t slot = (int32_t)((slot0 + n_steps - 1) % depth);
+  for (int64_t k = n_steps - 1; k >= 0; --k) {
+    const T* g = gates + k * gate_stride;
+    const bool first = (k == n_steps - 1) && !accumulate;
+    T* gate_out = PRE ? scratch + k * E.n_edges : dgate + k * gate_stride;
+    const T pv = gpay ? gpay[k * width + col] : T(0);
+    if (C.n == 1) {
+      T dwk, dgk, dfk;
+      edge_vjp(R[tap_row32(slot, C.lo, D)], R[tap_row32(slot, C.hi, D)], C.w, g[C.src], C.f,
+               dwk, dgk, dfk);
+      aw = first ? dwk : add_rn(aw, dwk);
+      af = first ? dfk : add_rn(af, dfk);
+      gate_out[PRE ? C.j0 : C.e] = dgk;
+    } else if (!ONE && C.n > 1) {
+      roll_col_generic_vjp<T, PRE>(R, slot, D, C.j0, C.n, E, g, edge, lo_row, hi_row, first, dw,
+                                   df, gate_out);
+    }
+    R[slot] = pv;
+    slot = slot == 0 ? D - 1 : slot - 1;
+  }
+  if (C.n == 1 && n_steps > 0) {
+    dw[C.e] = aw;
+    df[C.e] = af;
+  }
+  if (SMEM && !(flags & DGB_ROLLOUT_NO_FINAL))
+    for (int32_t r = 0; r < D; ++r) ring[(int64_t)r * width + col] = R[r];
+}
+
+// dgate[k][s] = sum of scratch[k][pos] over the source's edges in ascending
+// edge order (pos = each edge's scratch position), from +0.
 template <typename T>
 __global__ void source_sum_kernel(const T* __restrict__ scratch, int64_t n_steps,
                                   int64_t n_edges, int64_t n_src,
@@ -597,81 +773,150 @@ extern "C" int dgb_three_tap_vjp(int dtype, const void* ring, int64_t depth, int
   return DGB_OK;
 }
 
-extern "C" int dgb_two_tap_window(int dtype, void* queue, int64_t depth, int64_t width,
-                                  const int64_t* slot, int64_t n_steps, int64_t n_edges,
-                                  const void* weights, const void* gates,
-                                  const int64_t* pre_idx, int64_t n_sources,
-                                  const void* fraction, const int64_t* lower,
-                                  const int64_t* upper, const int64_t* col_ptr,
-                                  const int64_t* col_edge, void* payload, void* stream) {
+// Rollout launch: the ring in shared memory when a 128-column block's ring
+// fits (opt-in size), else in place in HBM.
+template <typename K>
+static int roll_smem_setup(K kernel, size_t bytes) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return 0;
+  if (bytes > (size_t)optin) return 0;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) ==
+         cudaSuccess;
+}
+
+template <typename T, bool ONE>
+static void launch_rollout(T* ring, int64_t depth, int64_t width, const int64_t* slot,
+                           int64_t n_steps, TapEdges<T> E, const T* gates, int64_t stride,
+                           const int64_t* ptr, const int64_t* edge, const int32_t* lo,
+                           const int32_t* hi, int flags, T* payload, cudaStream_t st) {
+  const size_t bytes = (size_t)kRollBlock * depth * sizeof(T);
+  const unsigned blocks = blocks_for(width, kRollBlock);
+  if (roll_smem_setup(two_tap_rollout_kernel<T, true, ONE>, bytes))
+    two_tap_rollout_kernel<T, true, ONE><<<blocks, kRollBlock, bytes, st>>>(
+        ring, depth, width, slot, n_steps, E, gates, stride, ptr, edge, lo, hi, flags, payload);
+  else
+    two_tap_rollout_kernel<T, false, ONE><<<blocks, kRollBlock, 0, st>>>(
+        ring, depth, width, slot, n_steps, E, gates, stride, ptr, edge, lo, hi, flags, payload);
+}
+
+template <typename T, bool PRE, bool ONE>
+static void launch_rollout_vjp(T* ring, int64_t depth, int64_t width, const int64_t* slot,
+                               int64_t n_steps, TapEdges<T> E, const T* gates, int64_t stride,
+                               const int64_t* ptr, const int64_t* edge, const int32_t* lo,
+                               const int32_t* hi, int flags, const T* gpay, int accumulate,
+                               T* dw, T* dgate, T* df, T* scratch, cudaStream_t st) {
+  const size_t bytes = (size_t)kRollBlock * depth * sizeof(T);
+  const unsigned blocks = blocks_for(width, kRollBlock);
+  if (roll_smem_setup(two_tap_rollout_vjp_kernel<T, true, PRE, ONE>, bytes))
+    two_tap_rollout_vjp_kernel<T, true, PRE, ONE><<<blocks, kRollBlock, bytes, st>>>(
+        ring, depth, width, slot, n_steps, E, gates, stride, ptr, edge, lo, hi, flags, gpay,
+        accumulate, dw, dgate, df, scratch);
+  else
+    two_tap_rollout_vjp_kernel<T, false, PRE, ONE><<<blocks, kRollBlock, 0, st>>>(
+        ring, depth, width, slot, n_steps, E, gates, stride, ptr, edge, lo, hi, flags, gpay,
+        accumulate, dw, dgate, df, scratch);
+}
+
+extern "C" int dgb_two_tap_rollout(int dtype, void* ring, int64_t depth, int64_t width,
+                                   const int64_t* slot, int64_t n_steps, int64_t n_edges,
+                                   const void* weights, const void* gates,
+                                   const int64_t* pre_idx, int64_t n_sources,
+                                   const void* fraction, const int64_t* col_ptr,
+                                   const int64_t* col_edge, const int32_t* lower_row,
+                                   const int32_t* upper_row, int32_t flags, void* payload,
+                                   void* stream) {
   clear_error();
-  int rc = check_ring(dtype, queue, depth, width, slot, n_edges, weights, gates, pre_idx,
+  int rc = check_ring(dtype, ring, depth, width, slot, n_edges, weights, gates, pre_idx,
                       n_sources, fraction);
   if (rc) return rc;
   DGB_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
   if (width == 0 || n_steps == 0) return DGB_OK;
-  DGB_REQUIRE(col_ptr && (n_edges == 0 || (lower && upper && col_edge)),
-              "addresses and the column plan must be non-null");
+  DGB_REQUIRE(col_ptr && (n_edges == 0 || (col_edge && lower_row && upper_row)),
+              "the rollout plan must be non-null");
+  DGB_REQUIRE(depth * width < (1ll << 31) && n_edges < (1ll << 31) &&
+                  n_sources < (1ll << 31),
+              "rollout ring size, edge and source counts must be below 2^31");
   const int64_t stride = pre_idx ? n_sources : n_edges;
-  DGB_DELAY_DISPATCH(dtype, two_tap_window_kernel<T><<<blocks_for(width, 256), 256, 0,
-                                                       as_stream(stream)>>>(
-                                (T*)queue, depth, width, slot, n_steps,
-                                tap_edges<T>(weights, pre_idx, n_sources, fraction, n_edges),
-                                (const T*)gates, stride, lower, upper, col_ptr, col_edge,
-                                (T*)payload));
+  const bool one = (flags & DGB_ROLLOUT_ONE_EDGE) != 0;
+  cudaStream_t st = as_stream(stream);
+  DGB_DELAY_DISPATCH(dtype, {
+    const TapEdges<T> E = tap_edges<T>(weights, pre_idx, n_sources, fraction, n_edges);
+    if (one)
+      launch_rollout<T, true>((T*)ring, depth, width, slot, n_steps, E, (const T*)gates, stride,
+                              col_ptr, col_edge, lower_row, upper_row, flags, (T*)payload, st);
+    else
+      launch_rollout<T, false>((T*)ring, depth, width, slot, n_steps, E, (const T*)gates,
+                               stride, col_ptr, col_edge, lower_row, upper_row, flags,
+                               (T*)payload, st);
+  });
   DGB_LAUNCH_CHECK();
   return DGB_OK;
 }
 
-extern "C" int dgb_two_tap_window_vjp(int dtype, void* grad_queue, int64_t depth, int64_t width,
-                                      const int64_t* slot, int64_t n_steps, int64_t n_edges,
-                                      const void* weights, const void* gates,
-                                      const int64_t* pre_idx, int64_t n_sources,
-                                      const void* fraction, const int64_t* lower,
-                                      const int64_t* upper, const int64_t* col_ptr,
-                                      const int64_t* col_edge, const int64_t* source_ptr,
-                                      const int64_t* source_edge, const void* grad_payload,
-                                      int32_t accumulate, void* grad_weights, void* grad_gates,
-                                      void* grad_fraction, void* edge_scratch, void* stream) {
+extern "C" int dgb_two_tap_rollout_vjp(int dtype, void* grad_ring, int64_t depth, int64_t width,
+                                       const int64_t* slot, int64_t n_steps, int64_t n_edges,
+                                       const void* weights, const void* gates,
+                                       const int64_t* pre_idx, int64_t n_sources,
+                                       const void* fraction, const int64_t* col_ptr,
+                                       const int64_t* col_edge, const int32_t* lower_row,
+                                       const int32_t* upper_row, int32_t flags,
+                                       const int64_t* source_ptr, const int64_t* source_pos,
+                                       const void* grad_payload, int32_t accumulate,
+                                       void* grad_weights, void* grad_gates, void* grad_fraction,
+                                       void* edge_scratch, void* stream) {
   clear_error();
-  int rc = check_ring(dtype, grad_queue, depth, width, slot, n_edges, weights, gates, pre_idx,
+  int rc = check_ring(dtype, grad_ring, depth, width, slot, n_edges, weights, gates, pre_idx,
                       n_sources, fraction);
   if (rc) return rc;
   DGB_REQUIRE(n_steps >= 0, "n_steps must be >= 0");
   if (width == 0 || n_steps == 0) return DGB_OK;
-  DGB_REQUIRE(col_ptr && (n_edges == 0 || (lower && upper && col_edge)),
-              "addresses and the column plan must be non-null");
+  DGB_REQUIRE(col_ptr && (n_edges == 0 || (col_edge && lower_row && upper_row)),
+              "the rollout plan must be non-null");
+  DGB_REQUIRE(depth * width < (1ll << 31) && n_edges < (1ll << 31) &&
+                  n_sources < (1ll << 31),
+              "rollout ring size, edge and source counts must be below 2^31");
   DGB_REQUIRE(n_edges == 0 || (grad_weights && grad_fraction), "gradients must be non-null");
   DGB_REQUIRE(grad_gates || (pre_idx ? n_sources : n_edges) == 0, "grad_gates must be non-null");
   const bool pre = pre_idx != nullptr;
-  DGB_REQUIRE(!pre || (source_ptr && (n_edges == 0 || (source_edge && edge_scratch))),
+  DGB_REQUIRE(!pre || (source_ptr && (n_edges == 0 || (source_pos && edge_scratch))),
               "the source plan and edge_scratch must be non-null with pre_idx");
   const int64_t stride = pre ? n_sources : n_edges;
+  const bool one = (flags & DGB_ROLLOUT_ONE_EDGE) != 0;
   cudaStream_t st = as_stream(stream);
-  if (pre) {
-    DGB_DELAY_DISPATCH(dtype, two_tap_window_vjp_kernel<T, true><<<blocks_for(width, 256), 256,
-                                                                   0, st>>>(
-                                  (T*)grad_queue, depth, width, slot, n_steps,
-                                  tap_edges<T>(weights, pre_idx, n_sources, fraction, n_edges),
-                                  (const T*)gates, stride, lower, upper, col_ptr, col_edge,
-                                  (const T*)grad_payload, accumulate, (T*)grad_weights, nullptr,
-                                  (T*)grad_fraction, (T*)edge_scratch));
-    DGB_LAUNCH_CHECK();
-    if (n_sources > 0)
-      DGB_DELAY_DISPATCH(dtype, source_sum_kernel<T><<<blocks_for(n_steps * n_sources, 256), 256,
-                                                       0, st>>>(
-                                    (const T*)edge_scratch, n_steps, n_edges, n_sources,
-                                    source_ptr, source_edge, (T*)grad_gates));
-  } else {
-    DGB_DELAY_DISPATCH(dtype, two_tap_window_vjp_kernel<T, false><<<blocks_for(width, 256), 256,
-                                                                    0, st>>>(
-                                  (T*)grad_queue, depth, width, slot, n_steps,
-                                  tap_edges<T>(weights, nullptr, 0, fraction, n_edges),
-                                  (const T*)gates, stride, lower, upper, col_ptr, col_edge,
-                                  (const T*)grad_payload, accumulate, (T*)grad_weights,
-                                  (T*)grad_gates, (T*)grad_fraction, nullptr));
-  }
+  DGB_DELAY_DISPATCH(dtype, {
+    const TapEdges<T> E = tap_edges<T>(weights, pre_idx, n_sources, fraction, n_edges);
+    T* R = (T*)grad_ring;
+    T* gw = (T*)grad_weights;
+    T* gf = (T*)grad_fraction;
+    const T* gg = (const T*)gates;
+    const T* gp = (const T*)grad_payload;
+    if (pre && one)
+      launch_rollout_vjp<T, true, true>(R, depth, width, slot, n_steps, E, gg, stride, col_ptr,
+                                        col_edge, lower_row, upper_row, flags, gp, accumulate,
+                                        gw, nullptr, gf, (T*)edge_scratch, st);
+    else if (pre)
+      launch_rollout_vjp<T, true, false>(R, depth, width, slot, n_steps, E, gg, stride, col_ptr,
+                                         col_edge, lower_row, upper_row, flags, gp, accumulate,
+                                         gw, nullptr, gf, (T*)edge_scratch, st);
+    else if (one)
+      launch_rollout_vjp<T, false, true>(R, depth, width, slot, n_steps, E, gg, stride, col_ptr,
+                                         col_edge, lower_row, upper_row, flags, gp, accumulate,
+                                         gw, (T*)grad_gates, gf, nullptr, st);
+    else
+      launch_rollout_vjp<T, false, false>(R, depth, width, slot, n_steps, E, gg, stride,
+                                          col_ptr, col_edge, lower_row, upper_row, flags, gp,
+                                          accumulate, gw, (T*)grad_gates, gf, nullptr, st);
+  });
   DGB_LAUNCH_CHECK();
+  if (pre && n_sources > 0) {
+    DGB_DELAY_DISPATCH(dtype, source_sum_kernel<T><<<blocks_for(n_steps * n_sources, 256), 256,
+                                                     0, st>>>(
+                                  (const T*)edge_scratch, n_steps, n_edges, n_sources,
+                                  source_ptr, source_pos, (T*)grad_gates));
+    DGB_LAUNCH_CHECK();
+  }
   return DGB_OK;
 }
 

@@ -16,8 +16,9 @@ adds in the reference's order; no floating-point atomics):
 * :func:`dense_interpolated_delay_transition` — the two- and three-tap
   transition (networks/_event_delivery.py:229-308)
 * :func:`two_tap_rollout` — many steps of the two-tap transition in one
-  launch, with a hand-written reverse sweep (the adjoint the reference takes by
-  autograd through its per-step loop)
+  launch, each block's ring columns held in shared memory for the whole
+  rollout, with a hand-written reverse sweep (the adjoint the reference takes
+  by autograd through its per-step loop)
 
 Ring layout: ``queue[depth][width]`` (row = delivery step, column = target
 slot).  Two-tap addresses are flat and relative to the start of row ``slot``:
@@ -425,42 +426,83 @@ def dense_interpolated_delay_transition(queue, slot, global_step, weights, conne
 # ---------------------------------------------------------------------------
 # multi-step rollout
 # ---------------------------------------------------------------------------
-_SCRATCH_BYTES = 256 << 20
+# gate-cotangent scratch per reverse-sweep launch (the sweep is split into
+# launches of at most this many bytes of per-edge gate cotangents)
+_SCRATCH_BYTES = 1 << 30
+ONE_EDGE, EMPTY_START, NO_FINAL = 1, 2, 4  # DGB_ROLLOUT_* flags
+
+
+class RolloutPlan:
+    """Tap rows per list position of a consistent plan, for the rollout kernels.
+
+    ``lo_row/hi_row[j]`` are the row distances of the two taps of the edge at
+    position j of the column lists; ``src_pos`` lists each source's edges
+    (ascending by edge) as list positions; ``flags`` marks plans with at most
+    one edge per column.
+    """
+
+    def __init__(self, plan, lower, upper):
+        W, E = plan.width, plan.n_edges
+        dev = plan.col_ptr.device
+        edge = plan.col_edge
+        self.lo_row = (lower[edge] // W).to(torch.int32).contiguous()
+        self.hi_row = (upper[edge] // W).to(torch.int32).contiguous()
+        counts = plan.col_ptr[1:] - plan.col_ptr[:-1]
+        self.flags = ONE_EDGE if (E == 0 or int(counts.max()) <= 1) else 0
+        self.src_ptr = self.src_pos = None
+        if plan.src_ptr is not None:
+            pos = torch.empty(E, dtype=torch.int64, device=dev)
+            pos[edge] = torch.arange(E, device=dev)
+            self.src_ptr = plan.src_ptr
+            self.src_pos = pos[plan.src_edge].contiguous()
 
 
 class _TwoTapRollout(torch.autograd.Function):
-    """(payload[n][width], final queue) of n two-tap steps from ``queue0``."""
+    """(payload[n][width], final queue) of n two-tap steps from ``queue0``
+    (None: an empty ring)."""
 
     @staticmethod
-    def forward(ctx, queue0, slot_t, weights, gates, fraction, lower, upper, pre_idx, plan):
-        ring = queue0.clone(memory_format=torch.contiguous_format)
+    def forward(ctx, queue0, slot_t, weights, gates, fraction, pre_idx, plan, rp, shape):
         n = gates.shape[0]
-        depth, width = ring.shape
-        payload = torch.empty(n, width, dtype=ring.dtype, device=ring.device)
-        _lib.check(_lib.load().dgb_two_tap_window(
-            _lib.dtype_code(ring.dtype), ring.data_ptr(), depth, width, slot_t.data_ptr(), n,
+        depth, width = shape
+        dev, dt = weights.device, weights.dtype
+        flags = rp.flags
+        if queue0 is None:
+            ring = torch.empty(depth, width, dtype=dt, device=dev)
+            flags |= EMPTY_START
+        else:
+            ring = queue0.clone(memory_format=torch.contiguous_format)
+        payload = torch.empty(n, width, dtype=dt, device=dev)
+        _lib.check(_lib.load().dgb_two_tap_rollout(
+            _lib.dtype_code(dt), ring.data_ptr(), depth, width, slot_t.data_ptr(), n,
             plan.n_edges, _ptr(weights), _ptr(gates), _ptr(pre_idx),
-            plan.n_sources if pre_idx is not None else 0, _ptr(fraction), _ptr(lower),
-            _ptr(upper), plan.col_ptr.data_ptr(), _ptr(plan.col_edge), payload.data_ptr(),
-            _lib.stream_ptr(ring.device)), "dgb_two_tap_window")
-        ctx.save_for_backward(slot_t, weights, gates, fraction, lower, upper,
+            plan.n_sources if pre_idx is not None else 0, _ptr(fraction),
+            plan.col_ptr.data_ptr(), _ptr(plan.col_edge), _ptr(rp.lo_row), _ptr(rp.hi_row),
+            flags, payload.data_ptr(), _lib.stream_ptr(dev)), "dgb_two_tap_rollout")
+        ctx.save_for_backward(slot_t, weights, gates, fraction,
                               *(() if pre_idx is None else (pre_idx,)))
-        ctx.plan = plan
+        ctx.plan, ctx.rp = plan, rp
+        ctx.has_queue0 = queue0 is not None
         return payload, ring
 
     @staticmethod
     def backward(ctx, grad_payload, grad_final):
-        slot_t, weights, gates, fraction, lower, upper, *rest = ctx.saved_tensors
+        slot_t, weights, gates, fraction, *rest = ctx.saved_tensors
         pre_idx = rest[0] if rest else None
-        plan = ctx.plan
+        plan, rp = ctx.plan, ctx.rp
         n = gates.shape[0]
         depth, width = plan.depth, plan.width
         dev, dt = weights.device, weights.dtype
-        R = (torch.zeros(depth, width, dtype=dt, device=dev) if grad_final is None
-             else grad_final.clone(memory_format=torch.contiguous_format))
+        flags = rp.flags
+        if grad_final is None:
+            R = torch.empty(depth, width, dtype=dt, device=dev)
+            empty = True
+        else:
+            R = grad_final.clone(memory_format=torch.contiguous_format)
+            empty = False
         gp = None if grad_payload is None else grad_payload.contiguous()
-        dw = torch.empty_like(weights)
-        df = torch.empty_like(fraction)
+        dw = torch.zeros_like(weights)
+        df = torch.zeros_like(fraction)
         dgates = torch.empty_like(gates)
         E = plan.n_edges
         chunk = n
@@ -468,47 +510,55 @@ class _TwoTapRollout(torch.autograd.Function):
         if pre_idx is not None and E:
             chunk = max(1, min(n, _SCRATCH_BYTES // (E * weights.element_size())))
             scratch = torch.empty(chunk * E, dtype=dt, device=dev)
-        stride = gates.shape[1] if gates.dim() == 2 else 0
         L = _lib.load()
         stream = _lib.stream_ptr(dev)
         hi = n
-        first = True
-        while hi > 0:  # newest chunk first
+        while hi > 0:  # newest chunk first; the cotangent ring carries between chunks
             lo = max(0, hi - chunk)
-            k = hi - lo
             s_lo = (slot_t + lo).remainder(depth)
-            _lib.check(L.dgb_two_tap_window_vjp(
-                _lib.dtype_code(dt), R.data_ptr(), depth, width, s_lo.data_ptr(), k, E,
-                _ptr(weights), gates[lo:hi].data_ptr() if stride else _ptr(gates),
-                _ptr(pre_idx), plan.n_sources if pre_idx is not None else 0, _ptr(fraction),
-                _ptr(lower), _ptr(upper), plan.col_ptr.data_ptr(), _ptr(plan.col_edge),
-                _ptr(plan.src_ptr), _ptr(plan.src_edge),
-                None if gp is None else gp[lo:hi].data_ptr(), 0 if first else 1,
-                dw.data_ptr(), dgates[lo:hi].data_ptr() if stride else _ptr(dgates),
-                df.data_ptr(), _ptr(scratch), stream), "dgb_two_tap_window_vjp")
-            first = False
+            _lib.check(L.dgb_two_tap_rollout_vjp(
+                _lib.dtype_code(dt), R.data_ptr(), depth, width, s_lo.data_ptr(), hi - lo, E,
+                _ptr(weights), gates[lo:hi].data_ptr(), _ptr(pre_idx),
+                plan.n_sources if pre_idx is not None else 0, _ptr(fraction),
+                plan.col_ptr.data_ptr(), _ptr(plan.col_edge), _ptr(rp.lo_row), _ptr(rp.hi_row),
+                flags | (EMPTY_START if empty else 0), _ptr(rp.src_ptr), _ptr(rp.src_pos),
+                None if gp is None else gp[lo:hi].data_ptr(), 0 if hi == n else 1,
+                dw.data_ptr(), dgates[lo:hi].data_ptr(), df.data_ptr(), _ptr(scratch), stream),
+                "dgb_two_tap_rollout_vjp")
+            empty = False
             hi = lo
-        if n == 0:
-            dw.zero_()
-            df.zero_()
-        return R, None, dw, dgates, df, None, None, None, None
+        if n == 0 and empty:
+            R.zero_()
+        return (R if ctx.has_queue0 else None), None, dw, dgates, df, None, None, None, None
 
 
-def two_tap_rollout(queue0, slot, weights, gates, fraction, lower, upper, pre_idx=None):
+def two_tap_rollout(queue0, slot, weights, gates, fraction, lower, upper, pre_idx=None,
+                    depth=None, width=None):
     """``n = gates.shape[0]`` two-tap steps from row ``slot`` in one launch.
 
     ``gates[k]`` are step k's gates (per source with ``pre_idx``, else per
     edge); returns ``(payload, queue)``: ``payload[k]`` is the row delivered at
     step k (``queue[slot_k]`` before the step), ``queue`` the ring after the
-    last step.  Differentiable in queue0, weights, gates and fraction; the
-    backward runs the reverse sweep on the GPU.  Both taps of every edge must
-    lie in one column (true for transition addresses ``off*width + post``).
+    last step.  ``queue0=None`` starts from an empty ring of shape
+    ``(depth, width)``.  Differentiable in queue0, weights, gates and
+    fraction; the backward runs the reverse sweep on the GPU.  Both taps of
+    every edge must lie in one column (true for transition addresses
+    ``off*width + post``).
     """
-    _check_queue(queue0)
+    if queue0 is not None:
+        _check_queue(queue0)
+        depth, width = queue0.shape
+    elif depth is None or width is None:
+        raise RuntimeError("two_tap_rollout needs queue0 or depth and width")
+    depth, width = int(depth), int(width)
     if gates.dim() != 2:
         raise RuntimeError("rollout gates must be (n_steps, n_sources or n_edges)")
     n = weights.numel()
-    dev, dt = queue0.device, queue0.dtype
+    dev, dt = weights.device, weights.dtype
+    if not (weights.is_cuda and dt in (torch.float32, torch.float64)):
+        raise RuntimeError("rollout weights must be a CUDA float32 or float64 vector")
+    if queue0 is not None and (queue0.device != dev or queue0.dtype != dt):
+        raise RuntimeError("queue0 must match the weights' device and dtype")
     _check_vec(weights, dt, n, "weights", dev)
     _check_vec(fraction, dt, n, "fraction", dev)
     _check_vec(lower, torch.int64, n, "lower", dev)
@@ -518,16 +568,17 @@ def two_tap_rollout(queue0, slot, weights, gates, fraction, lower, upper, pre_id
     elif gates.shape[1] != n:
         raise RuntimeError("gates must have one column per edge without pre_idx")
     if not (gates.device == dev and gates.dtype == dt):
-        raise RuntimeError("gates must match the queue's device and dtype")
+        raise RuntimeError("gates must match the weights' device and dtype")
     gates = gates.contiguous()
-    depth, width = queue0.shape
     slot_t = _slot_tensor(slot, depth, dev)
     plan = two_tap_plan(depth, width, lower, upper, pre_idx,
                         gates.shape[1] if pre_idx is not None else 0)
     if not plan.consistent:
         raise RuntimeError("two_tap_rollout needs both taps of every edge in one column")
-    return _TwoTapRollout.apply(queue0, slot_t, weights, gates, fraction, lower, upper,
-                                pre_idx, plan)
+    if getattr(plan, "rollout", None) is None:
+        plan.rollout = RolloutPlan(plan, lower, upper)
+    return _TwoTapRollout.apply(queue0, slot_t, weights, gates, fraction, pre_idx, plan,
+                                plan.rollout, (depth, width))
 
 
 def transition_addresses(offsets, post_idx, depth, width):

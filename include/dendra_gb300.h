@@ -650,41 +650,54 @@ int dgb_three_tap_vjp(int dtype, const void* ring, int64_t depth, int64_t width,
                       void* grad_coeff, void* stream);
 
 /*
- * Multi-step rollout of dgb_two_tap_enqueue: n_steps consecutive steps from
- * row *slot (slot advancing by one, modulo depth, every step) in one launch,
- * gates[k] holding step k's gates (row stride n_sources, or n_edges without
- * pre_idx) and payload[k] step k's delivered row.  Requires a consistent
- * plan: every edge's lower and upper address in the same column, and one
- * column list (col_ptr / col_edge) for both.  Each column's values are
- * bit-identical to n_steps single-step calls.
+ * Multi-step rollout of dgb_two_tap_enqueue in one launch, in place on ring:
+ * n_steps consecutive steps from row *slot (advancing by one, modulo depth,
+ * every step); gates[k] holds step k's gates (row stride n_sources, or n_edges
+ * without pre_idx) and payload[k] (optional) step k's delivered row.  Both
+ * taps of every edge must lie in one column: col_ptr (width+1) / col_edge list
+ * each column's edges ascending, and lower_row[j] / upper_row[j], in
+ * [0, depth), are the row distances of the two taps of the edge at list
+ * position j (its flat addresses divided by width).  One thread owns one
+ * column for the whole rollout, its ring depth held in shared memory when it
+ * fits; each value is bit-identical to n_steps dgb_two_tap_enqueue calls.
+ * flags: DGB_ROLLOUT_ONE_EDGE (no column holds more than one edge: a leaner
+ * kernel; a column with more is skipped and reported), DGB_ROLLOUT_EMPTY_START
+ * (ring contents ignored, the rollout starts from zeros),
+ * DGB_ROLLOUT_NO_FINAL (the ring is not written back at the end).
+ * depth*width, n_edges and n_sources below 2^31.
  */
-int dgb_two_tap_window(int dtype, void* queue, int64_t depth, int64_t width,
-                       const int64_t* slot, int64_t n_steps, int64_t n_edges,
-                       const void* weights, const void* gates, const int64_t* pre_idx,
-                       int64_t n_sources, const void* fraction, const int64_t* lower,
-                       const int64_t* upper, const int64_t* col_ptr, const int64_t* col_edge,
-                       void* payload, void* stream);
+#define DGB_ROLLOUT_ONE_EDGE 1
+#define DGB_ROLLOUT_EMPTY_START 2
+#define DGB_ROLLOUT_NO_FINAL 4
+int dgb_two_tap_rollout(int dtype, void* ring, int64_t depth, int64_t width,
+                        const int64_t* slot, int64_t n_steps, int64_t n_edges,
+                        const void* weights, const void* gates, const int64_t* pre_idx,
+                        int64_t n_sources, const void* fraction, const int64_t* col_ptr,
+                        const int64_t* col_edge, const int32_t* lower_row,
+                        const int32_t* upper_row, int32_t flags, void* payload, void* stream);
 
 /*
- * Reverse sweep of dgb_two_tap_window over the same n_steps (newest first).
- * grad_queue (in/out) holds the cotangent of the ring after the window and
- * leaves holding the cotangent before it; grad_payload[k] is the cotangent of
- * step k's delivered row (it replaces the cotangent of row slot_k, which the
- * forward cleared).  Per step the VJP above is taken; grad_weights /
- * grad_fraction accumulate over steps newest first (stored, not added, at the
- * newest step when accumulate == 0).  grad_gates[k] receives step k's gate
- * gradients; with pre_idx the per-edge values go to edge_scratch
- * (n_steps * n_edges) and are summed per source in ascending edge order.
+ * Reverse sweep of dgb_two_tap_rollout over the same n_steps (newest first),
+ * in place on the cotangent ring grad_ring (in: after the rollout, ignored
+ * with DGB_ROLLOUT_EMPTY_START; out: before it).  grad_payload[k] (optional)
+ * is the cotangent of step k's delivered row; it replaces the cotangent of row
+ * slot_k, which the forward cleared.  Per step the VJP of dgb_two_tap_vjp;
+ * grad_weights / grad_fraction accumulate over steps newest first (stored, not
+ * added, at the newest step when accumulate == 0).  grad_gates[k] receives
+ * step k's gate cotangents; with pre_idx the per-edge values go to
+ * edge_scratch[k][j] (j = list position, n_steps * n_edges values) and are
+ * summed per source in ascending edge order: source_ptr (n_sources+1) /
+ * source_pos give each source's edges, ascending by edge, as list positions.
  */
-int dgb_two_tap_window_vjp(int dtype, void* grad_queue, int64_t depth, int64_t width,
-                           const int64_t* slot, int64_t n_steps, int64_t n_edges,
-                           const void* weights, const void* gates, const int64_t* pre_idx,
-                           int64_t n_sources, const void* fraction, const int64_t* lower,
-                           const int64_t* upper, const int64_t* col_ptr,
-                           const int64_t* col_edge, const int64_t* source_ptr,
-                           const int64_t* source_edge, const void* grad_payload,
-                           int32_t accumulate, void* grad_weights, void* grad_gates,
-                           void* grad_fraction, void* edge_scratch, void* stream);
+int dgb_two_tap_rollout_vjp(int dtype, void* grad_ring, int64_t depth, int64_t width,
+                            const int64_t* slot, int64_t n_steps, int64_t n_edges,
+                            const void* weights, const void* gates, const int64_t* pre_idx,
+                            int64_t n_sources, const void* fraction, const int64_t* col_ptr,
+                            const int64_t* col_edge, const int32_t* lower_row,
+                            const int32_t* upper_row, int32_t flags, const int64_t* source_ptr,
+                            const int64_t* source_pos, const void* grad_payload,
+                            int32_t accumulate, void* grad_weights, void* grad_gates,
+                            void* grad_fraction, void* edge_scratch, void* stream);
 
 /* First device-side index error of the delay kernels since the last call
    (0 = none, else DGB_DELAY_ERR_*), cleared on read; synchronises stream. */

@@ -160,9 +160,10 @@ def test_rollout_in_one_launch_matches_reference(cuda, golden, tag, npt, tdt):
 
 
 def _network_case(seed, depth, width, E, n_src, steps, npt):
-    """Connections into few targets (heavy collisions) with delays wrapping the ring."""
+    """Connections into few targets (heavy collisions) with delays wrapping the
+    ring; width == E: one connection per target slot (the register path)."""
     rng = np.random.default_rng(seed)
-    post = rng.integers(0, width, E)
+    post = rng.permutation(E) if width == E else rng.integers(0, width, E)
     pre = rng.integers(0, n_src, E)
     pos = rng.uniform(1.0, depth + 0.9, E)
     off = np.floor(pos).astype(np.int64)
@@ -176,9 +177,11 @@ def _network_case(seed, depth, width, E, n_src, steps, npt):
     return post, pre, frac, lower, upper, w, gates, q0
 
 
+@pytest.mark.parametrize("depth,width", [(33, 700), (33, 5000), (600, 700)])
 @pytest.mark.parametrize("tag,npt,tdt", TAGS)
-def test_window_equals_single_steps_and_oracle(cuda, tag, npt, tdt):
-    depth, width, E, n_src, steps = 33, 700, 5000, 97, 70
+def test_window_equals_single_steps_and_oracle(cuda, tag, npt, tdt, depth, width):
+    """Shared-memory ring (depth 33) and, for depth 600, the ring in place in HBM."""
+    E, n_src, steps = 5000, 97, 70
     post, pre, frac, lower, upper, w, gates, q0 = _network_case(5, depth, width, E, n_src,
                                                                 steps, npt)
     T = lambda a, dt=tdt: _t(a, cuda, dt)  # noqa: E731
@@ -197,10 +200,11 @@ def test_window_equals_single_steps_and_oracle(cuda, tag, npt, tdt):
     assert delays.delay_status() == 0
 
 
+@pytest.mark.parametrize("width", [300, 2000])
 @pytest.mark.parametrize("with_pre", [True, False])
 @pytest.mark.parametrize("tag,npt,tdt", TAGS)
-def test_rollout_adjoint_matches_oracle(cuda, tag, npt, tdt, with_pre, monkeypatch):
-    depth, width, E, n_src, steps = 21, 300, 2000, 41, 50
+def test_rollout_adjoint_matches_oracle(cuda, tag, npt, tdt, with_pre, width, monkeypatch):
+    depth, E, n_src, steps = 21, 2000, 41, 50
     post, pre, frac, lower, upper, w, gates, q0 = _network_case(9, depth, width, E, n_src,
                                                                 steps, npt)
     if not with_pre:
@@ -221,6 +225,27 @@ def test_rollout_adjoint_matches_oracle(cuda, tag, npt, tdt, with_pre, monkeypat
     np.testing.assert_array_equal(tw.grad.cpu().numpy(), dw)
     np.testing.assert_array_equal(tg.grad.cpu().numpy(), dg)
     np.testing.assert_array_equal(tf.grad.cpu().numpy(), df)
+
+
+@pytest.mark.parametrize("tag,npt,tdt", TAGS)
+def test_rollout_from_an_empty_ring(cuda, tag, npt, tdt):
+    depth, width, E, n_src, steps = 40, 3000, 3000, 50, 90
+    post, pre, frac, lower, upper, w, gates, _ = _network_case(13, depth, width, E, n_src, steps,
+                                                               npt)
+    T = lambda a, dt=tdt: _t(a, cuda, dt)  # noqa: E731
+    args = (T(w), T(gates), T(frac), T(lower, None), T(upper, None), T(pre, None))
+    zeros = torch.zeros(depth, width, dtype=tdt, device=cuda)
+    pay0, fin0 = delays.two_tap_rollout(zeros, 7, *args)
+    pay1, fin1 = delays.two_tap_rollout(None, 7, *args, depth=depth, width=width)
+    torch.testing.assert_close(pay1, pay0, rtol=0, atol=0)
+    torch.testing.assert_close(fin1, fin0, rtol=0, atol=0)
+    tw = args[0].clone().requires_grad_()
+    pay, _ = delays.two_tap_rollout(None, 7, tw, *args[1:], depth=depth, width=width)
+    pay.sum().backward()
+    cpay = np.ones((steps, width), npt)
+    _, dw, _, _ = oracle.two_tap_rollout_vjp(np.zeros((depth, width), npt), 7, w, gates, frac,
+                                             lower, upper, cpay, pre_idx=pre)
+    np.testing.assert_array_equal(tw.grad.cpu().numpy(), dw)
 
 
 def test_device_slot_outside_the_ring_is_reported(cuda):

@@ -110,6 +110,31 @@ def test_plan_lists_each_column_in_ascending_edge_order():
         np.testing.assert_array_equal(got, np.flatnonzero(pre.numpy() == s))
 
 
+def test_rollout_plan_rows_and_source_positions():
+    rng = np.random.default_rng(4)
+    depth, width, E = 9, 40, 120
+    post = torch.as_tensor(rng.integers(0, width - 3, E))  # three empty columns
+    off = torch.as_tensor(rng.integers(1, depth + 1, E))
+    pre = torch.as_tensor(rng.integers(0, 5, E))
+    lower, upper = delays.transition_addresses(off, post, depth, width)
+    plan = delays.TapPlan(depth, width, lower, upper, pre, 5)
+    rp = delays.RolloutPlan(plan, lower, upper)
+    edge = plan.col_edge.numpy()
+    np.testing.assert_array_equal(rp.lo_row.numpy(), lower.numpy()[edge] // width)
+    np.testing.assert_array_equal(rp.hi_row.numpy(), upper.numpy()[edge] // width)
+    np.testing.assert_array_equal(rp.hi_row.numpy(), (rp.lo_row.numpy() + 1) % depth)
+    assert rp.flags == 0  # several edges per column
+    pos = np.empty(E, np.int64)
+    pos[edge] = np.arange(E)
+    for s_ in range(5):
+        got = rp.src_pos.numpy()[rp.src_ptr[s_]:rp.src_ptr[s_ + 1]]
+        np.testing.assert_array_equal(got, pos[np.flatnonzero(pre.numpy() == s_)])
+    one = torch.as_tensor(rng.permutation(width))
+    lo1, up1 = delays.transition_addresses(off[:width], one, depth, width)
+    assert delays.RolloutPlan(delays.TapPlan(depth, width, lo1, up1), lo1, up1).flags == \
+        delays.ONE_EDGE
+
+
 def test_plan_rejects_addresses_and_sources_out_of_range():
     lower = torch.tensor([0, 5, 12])
     with pytest.raises(RuntimeError, match="outside the delivery ring"):
