@@ -637,11 +637,18 @@ def bench_bt(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
-# unfused per-step two-tap op, per connection-step with one connection per
-# target slot (float32): weight, share, two addresses, source index and gate
-# 36 B + two tap read-modify-writes 16 B + the delivered row read, cleared and
-# written out 12 B
-DELAY_BYTES_PER_CONN_STEP = 64
+def _delay_bytes(n_edges, width, n_src, depth, steps, elem=4):
+    """Algorithmic bytes of the direct rollout's forward launch and of its
+    reverse launch (sweep + per-source sum), one edge per column, an empty
+    starting ring."""
+    edge_ops = n_edges * (4 + 4 + 4 + 4 + 8 + 8 + 8)  # w, f, two tap rows, source, plan
+    fwd = steps * width * elem + depth * width * elem + steps * n_src * elem + edge_ops
+    rev = (steps * width * elem            # delivered-row cotangents in
+           + 2 * steps * n_edges * elem    # per-edge gate cotangents out and back in
+           + 2 * steps * n_src * elem      # gates in, gate cotangents out
+           + depth * width * elem          # ring cotangent out
+           + edge_ops + 2 * n_edges * elem + n_edges * 8)  # dw, df, source plan
+    return fwd, rev
 
 
 def _delay_case(n_conn, n_src, depth, seed, dt_ms=0.025):
@@ -738,26 +745,24 @@ def bench_delay(args, world, rank, local):
     torch.cuda.synchronize()
     flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
     st = torch.cuda.current_stream(dev)
-    times, fwd = [], []
+    times = []
+    delays.launch_events = []  # per-launch CUDA events on the launching stream
     with ClockSampler(local) as clocks:
         for _ in range(args.steps):
             flush.sum()
-            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-            e0.record(st)
-            with torch.no_grad():
-                delays.two_tap_rollout(None, 0, tw, tg, tf, tlo, tup, tpre, depth=depth,
-                                       width=n_conn)
-            e1.record(st)
-            e1.synchronize()
-            fwd.append(e0.elapsed_time(e1))
-            flush.sum()
+            e0, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
             e0.record(st)
             step()
             e2.record(st)
             e2.synchronize()
             times.append(e0.elapsed_time(e2))
+    launch_ms = {}
+    for name, a, b in delays.launch_events:
+        launch_ms.setdefault(name, []).append(a.elapsed_time(b))
+    delays.launch_events = None
     ms = float(np.mean(times))
-    ms_fwd = float(np.mean(fwd))
+    ms_fwd = float(np.mean(launch_ms["two_tap_rollout"]))
+    ms_rev = float(np.mean(launch_ms["two_tap_rollout_vjp"]))
     # end to end: gates in from pinned host memory, gradients out
     gates_pin = gates_h.pin_memory()
     outs = [torch.empty(n_conn, dtype=torch.float32).pin_memory() for _ in range(2)]
@@ -785,24 +790,30 @@ def bench_delay(args, world, rank, local):
     cpu_s = time.perf_counter() - t0
     exact = bool(np.array_equal(pay.cpu().numpy(), opay))
     peak, peak_kind = _peaks()
-    achieved = DELAY_BYTES_PER_CONN_STEP * units / (ms_fwd * 1e-3) / 1e9
+    fwd_bytes, rev_bytes = _delay_bytes(n_conn, n_conn, n_src, depth, steps)
+    dominant = "reverse" if ms_rev >= ms_fwd else "forward"
+    kbytes, kms = (rev_bytes, ms_rev) if dominant == "reverse" else (fwd_bytes, ms_fwd)
+    achieved = kbytes / (kms * 1e-3) / 1e9
     line = {
         "metric": metric, "value": units / (ms * 1e-3), "unit": metric, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": cfg,
-        "forward_ms": ms_fwd, "forward_connection_steps_per_s": units / (ms_fwd * 1e-3),
+        "forward_ms": ms_fwd, "reverse_ms": ms_rev,
+        "forward_connection_steps_per_s": units / (ms_fwd * 1e-3),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": "two_tap_rollout_kernel",
-                     "note": f"{DELAY_BYTES_PER_CONN_STEP} algorithmic B per float32 "
-                             "connection-step of the unfused per-step op; forward rollout "
-                             "(one launch, ring in shared memory) timed alone; peak "
-                             f"{peak_kind}"},
+                     "kernel": "two_tap_direct_vjp_kernel + source_sum_kernel"
+                     if dominant == "reverse" else "two_tap_direct_kernel",
+                     "note": f"{dominant} pass, {kbytes / 1e9:.2f} GB algorithmic per launch "
+                             "(reverse: delivered-row cotangents in, per-edge gate cotangents "
+                             "out and back in, gates, ring cotangent, edge operands; forward: "
+                             "delivered rows out, final ring, gates, edge operands), timed with "
+                             f"CUDA events on its stream; peak {peak_kind}"},
         "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": 3,
+        "gpu_launches": 4,
         "clocks": clocks.summary(),
         "bit_exact_vs_oracle": exact,
         "cpu_baseline": {"value": n_conn * n_chk / cpu_s, "unit": metric, "cores": 1,

@@ -110,11 +110,12 @@ SIGNATURES = {
                                _P, _P, _P, _P]),
     "dgb_three_tap_vjp": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _P, _P, _P, _P, _P, _P, _P,
                                  _P, _P]),
-    "dgb_two_tap_rollout": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64, _P,
-                                   _P, _P, _P, _P, _I32, _P, _P]),
-    "dgb_two_tap_rollout_vjp": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64,
-                                       _P, _P, _P, _P, _P, _I32, _P, _P, _P, _I32, _P, _P, _P,
-                                       _P, _P]),
+    "dgb_two_tap_rollout": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _I64, _P,
+                                   _I64, _P, _P, _P, _P, _P, _I32, _P, _P]),
+    "dgb_two_tap_rollout_vjp": (_INT, [_INT, _P, _I64, _I64, _P, _I64, _I64, _P, _P, _I64, _P,
+                                       _I64, _P, _P, _P, _P, _P, _I32, _P, _P, _P, _I32, _P, _P,
+                                       _P, _P, _P]),
+    "dgb_gates_by_source": (_INT, [_INT, _I64, _I64, _P, _P, _I64, _P]),
     "dgb_delay_status": (_INT, [_P]),
 }
 

@@ -426,10 +426,34 @@ def dense_interpolated_delay_transition(queue, slot, global_step, weights, conne
 # ---------------------------------------------------------------------------
 # multi-step rollout
 # ---------------------------------------------------------------------------
+# Optional launch timing: while ``launch_events`` is a list, every rollout
+# launch appends (name, start event, end event) recorded on its stream (the
+# reverse launch covers the sweep and the per-source sum).
+launch_events = None
+
+
+class _Timed:
+    def __init__(self, name, dev):
+        self.name, self.dev = name, dev
+
+    def __enter__(self):
+        if launch_events is not None:
+            self.e0 = torch.cuda.Event(enable_timing=True)
+            self.e0.record(torch.cuda.current_stream(self.dev))
+        return self
+
+    def __exit__(self, *exc):
+        if launch_events is not None:
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record(torch.cuda.current_stream(self.dev))
+            launch_events.append((self.name, self.e0, e1))
+
+
 # gate-cotangent scratch per reverse-sweep launch (the sweep is split into
 # launches of at most this many bytes of per-edge gate cotangents)
-_SCRATCH_BYTES = 1 << 30
-ONE_EDGE, EMPTY_START, NO_FINAL = 1, 2, 4  # DGB_ROLLOUT_* flags
+_SCRATCH_BYTES = 4 << 30
+# DGB_ROLLOUT_* flags
+ONE_EDGE, EMPTY_START, NO_FINAL, CHAINED, GATES_BY_SOURCE = 1, 2, 4, 8, 16
 
 
 class RolloutPlan:
@@ -449,6 +473,13 @@ class RolloutPlan:
         self.hi_row = (upper[edge] // W).to(torch.int32).contiguous()
         counts = plan.col_ptr[1:] - plan.col_ptr[:-1]
         self.flags = ONE_EDGE if (E == 0 or int(counts.max()) <= 1) else 0
+        # every edge's taps at lo and lo + 1 with 1 <= lo <= depth - 2: each
+        # delivered value is a closed form of two gates (the direct kernels)
+        D = plan.depth
+        if self.flags & ONE_EDGE and (E == 0 or bool(
+                ((self.lo_row >= 1) & (self.lo_row <= D - 2)
+                 & (self.hi_row == self.lo_row + 1)).all())):
+            self.flags |= CHAINED
         self.src_ptr = self.src_pos = None
         if plan.src_ptr is not None:
             pos = torch.empty(E, dtype=torch.int64, device=dev)
@@ -473,16 +504,30 @@ class _TwoTapRollout(torch.autograd.Function):
         else:
             ring = queue0.clone(memory_format=torch.contiguous_format)
         payload = torch.empty(n, width, dtype=dt, device=dev)
-        _lib.check(_lib.load().dgb_two_tap_rollout(
-            _lib.dtype_code(dt), ring.data_ptr(), depth, width, slot_t.data_ptr(), n,
-            plan.n_edges, _ptr(weights), _ptr(gates), _ptr(pre_idx),
-            plan.n_sources if pre_idx is not None else 0, _ptr(fraction),
-            plan.col_ptr.data_ptr(), _ptr(plan.col_edge), _ptr(rp.lo_row), _ptr(rp.hi_row),
-            flags, payload.data_ptr(), _lib.stream_ptr(dev)), "dgb_two_tap_rollout")
+        g_use, g_row, gates_t = gates, 0, None
+        if pre_idx is not None and flags & CHAINED and gates.numel():
+            # per-source rows: a column's consecutive steps share cache sectors
+            g_row = (n + 7) // 8 * 8
+            gates_t = torch.empty(gates.shape[1], g_row, dtype=dt, device=dev)
+            _lib.check(_lib.load().dgb_gates_by_source(
+                _lib.dtype_code(dt), n, gates.shape[1], gates.data_ptr(), gates_t.data_ptr(),
+                g_row, _lib.stream_ptr(dev)), "dgb_gates_by_source")
+            g_use, flags = gates_t, flags | GATES_BY_SOURCE
+        with _Timed("two_tap_rollout", dev):
+            _lib.check(_lib.load().dgb_two_tap_rollout(
+                _lib.dtype_code(dt), ring.data_ptr(), depth, width, slot_t.data_ptr(), n,
+                plan.n_edges, _ptr(weights), _ptr(g_use), g_row, _ptr(pre_idx),
+                plan.n_sources if pre_idx is not None else 0, _ptr(fraction),
+                plan.col_ptr.data_ptr(), _ptr(plan.col_edge), _ptr(rp.lo_row),
+                _ptr(rp.hi_row), flags, payload.data_ptr(), _lib.stream_ptr(dev)),
+                "dgb_two_tap_rollout")
         ctx.save_for_backward(slot_t, weights, gates, fraction,
                               *(() if pre_idx is None else (pre_idx,)))
         ctx.plan, ctx.rp = plan, rp
+        ctx.gates_t, ctx.g_row = gates_t, g_row
         ctx.has_queue0 = queue0 is not None
+        # an unused output's cotangent stays None (no zero ring to read back)
+        ctx.set_materialize_grads(False)
         return payload, ring
 
     @staticmethod
@@ -508,23 +553,30 @@ class _TwoTapRollout(torch.autograd.Function):
         chunk = n
         scratch = None
         if pre_idx is not None and E:
-            chunk = max(1, min(n, _SCRATCH_BYTES // (E * weights.element_size())))
-            scratch = torch.empty(chunk * E, dtype=dt, device=dev)
+            chunk = max(8, min(n, _SCRATCH_BYTES // (E * weights.element_size())) // 8 * 8)
+            # one row of chunk (rounded up to 8) steps per list position
+            scratch = torch.empty(E * ((chunk + 7) // 8 * 8), dtype=dt, device=dev)
         L = _lib.load()
         stream = _lib.stream_ptr(dev)
+        gates_t, g_row = ctx.gates_t, ctx.g_row
+        if gates_t is not None:
+            flags |= GATES_BY_SOURCE
         hi = n
         while hi > 0:  # newest chunk first; the cotangent ring carries between chunks
             lo = max(0, hi - chunk)
             s_lo = (slot_t + lo).remainder(depth)
-            _lib.check(L.dgb_two_tap_rollout_vjp(
-                _lib.dtype_code(dt), R.data_ptr(), depth, width, s_lo.data_ptr(), hi - lo, E,
-                _ptr(weights), gates[lo:hi].data_ptr(), _ptr(pre_idx),
-                plan.n_sources if pre_idx is not None else 0, _ptr(fraction),
-                plan.col_ptr.data_ptr(), _ptr(plan.col_edge), _ptr(rp.lo_row), _ptr(rp.hi_row),
-                flags | (EMPTY_START if empty else 0), _ptr(rp.src_ptr), _ptr(rp.src_pos),
-                None if gp is None else gp[lo:hi].data_ptr(), 0 if hi == n else 1,
-                dw.data_ptr(), dgates[lo:hi].data_ptr(), df.data_ptr(), _ptr(scratch), stream),
-                "dgb_two_tap_rollout_vjp")
+            g_ptr = (gates_t.data_ptr() + lo * gates_t.element_size() if gates_t is not None
+                     else gates[lo:hi].data_ptr())
+            with _Timed("two_tap_rollout_vjp", dev):
+                _lib.check(L.dgb_two_tap_rollout_vjp(
+                    _lib.dtype_code(dt), R.data_ptr(), depth, width, s_lo.data_ptr(), hi - lo, E,
+                    _ptr(weights), g_ptr, g_row, _ptr(pre_idx),
+                    plan.n_sources if pre_idx is not None else 0, _ptr(fraction),
+                    plan.col_ptr.data_ptr(), _ptr(plan.col_edge), _ptr(rp.lo_row), _ptr(rp.hi_row),
+                    flags | (EMPTY_START if empty else 0), _ptr(rp.src_ptr), _ptr(rp.src_pos),
+                    None if gp is None else gp[lo:hi].data_ptr(), 0 if hi == n else 1,
+                    dw.data_ptr(), dgates[lo:hi].data_ptr(), df.data_ptr(), _ptr(scratch), stream),
+                    "dgb_two_tap_rollout_vjp")
             empty = False
             hi = lo
         if n == 0 and empty:

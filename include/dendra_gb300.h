@@ -663,15 +663,25 @@ int dgb_three_tap_vjp(int dtype, const void* ring, int64_t depth, int64_t width,
  * flags: DGB_ROLLOUT_ONE_EDGE (no column holds more than one edge: a leaner
  * kernel; a column with more is skipped and reported), DGB_ROLLOUT_EMPTY_START
  * (ring contents ignored, the rollout starts from zeros),
- * DGB_ROLLOUT_NO_FINAL (the ring is not written back at the end).
+ * DGB_ROLLOUT_NO_FINAL (the ring is not written back at the end),
+ * DGB_ROLLOUT_CHAINED (every column has at most one edge, with taps at lo and
+ * lo + 1, 1 <= lo <= depth - 2: the cell delivered at step k then holds
+ * (c0 + upper tap of step k-lo-1) + lower tap of step k-lo, so every step is
+ * computed independently, with no ring held during the rollout; a column that
+ * breaks the promise is skipped and reported), DGB_ROLLOUT_GATES_BY_SOURCE
+ * (with pre_idx and CHAINED: gates given per source, gates[s][k], rows of
+ * gate_row >= n_steps values; see dgb_gates_by_source).
  * depth*width, n_edges and n_sources below 2^31.
  */
 #define DGB_ROLLOUT_ONE_EDGE 1
 #define DGB_ROLLOUT_EMPTY_START 2
 #define DGB_ROLLOUT_NO_FINAL 4
+#define DGB_ROLLOUT_CHAINED 8
+#define DGB_ROLLOUT_GATES_BY_SOURCE 16
 int dgb_two_tap_rollout(int dtype, void* ring, int64_t depth, int64_t width,
                         const int64_t* slot, int64_t n_steps, int64_t n_edges,
-                        const void* weights, const void* gates, const int64_t* pre_idx,
+                        const void* weights, const void* gates, int64_t gate_row,
+                        const int64_t* pre_idx,
                         int64_t n_sources, const void* fraction, const int64_t* col_ptr,
                         const int64_t* col_edge, const int32_t* lower_row,
                         const int32_t* upper_row, int32_t flags, void* payload, void* stream);
@@ -685,19 +695,26 @@ int dgb_two_tap_rollout(int dtype, void* ring, int64_t depth, int64_t width,
  * grad_weights / grad_fraction accumulate over steps newest first (stored, not
  * added, at the newest step when accumulate == 0).  grad_gates[k] receives
  * step k's gate cotangents; with pre_idx the per-edge values go to
- * edge_scratch[k][j] (j = list position, n_steps * n_edges values) and are
- * summed per source in ascending edge order: source_ptr (n_sources+1) /
- * source_pos give each source's edges, ascending by edge, as list positions.
+ * edge_scratch[j][k] (j = list position; rows of kc = n_steps rounded up to 8
+ * values, n_edges * kc in all, 32-byte aligned) and are summed per source in
+ * ascending edge order: source_ptr (n_sources+1) / source_pos give each
+ * source's edges, ascending by edge, as list positions.
  */
 int dgb_two_tap_rollout_vjp(int dtype, void* grad_ring, int64_t depth, int64_t width,
                             const int64_t* slot, int64_t n_steps, int64_t n_edges,
-                            const void* weights, const void* gates, const int64_t* pre_idx,
+                            const void* weights, const void* gates, int64_t gate_row,
+                            const int64_t* pre_idx,
                             int64_t n_sources, const void* fraction, const int64_t* col_ptr,
                             const int64_t* col_edge, const int32_t* lower_row,
                             const int32_t* upper_row, int32_t flags, const int64_t* source_ptr,
                             const int64_t* source_pos, const void* grad_payload,
                             int32_t accumulate, void* grad_weights, void* grad_gates,
                             void* grad_fraction, void* edge_scratch, void* stream);
+
+/* gates_t[s][k] = gates[k][s] for k < n_steps (rows of gate_row >= n_steps
+   values): the per-source layout of DGB_ROLLOUT_GATES_BY_SOURCE. */
+int dgb_gates_by_source(int dtype, int64_t n_steps, int64_t n_sources, const void* gates,
+                        void* gates_t, int64_t gate_row, void* stream);
 
 /* First device-side index error of the delay kernels since the last call
    (0 = none, else DGB_DELAY_ERR_*), cleared on read; synchronises stream. */

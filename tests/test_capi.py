@@ -137,14 +137,18 @@ def test_delay_contract_errors_on_the_host():
     assert L.dgb_two_tap_enqueue(0, p, 4, 4, p, 3, p, p, None, 0, p, p, p, None, p, p, p, None,
                                  None) == -1
     # source indices without sources
-    assert L.dgb_two_tap_rollout(0, p, 4, 4, p, 2, 3, p, p, p, 0, p, p, p, p, p, 0, None,
+    assert L.dgb_two_tap_rollout(0, p, 4, 4, p, 2, 3, p, p, 0, p, 0, p, p, p, p, p, 0, None,
                                  None) == -1
     # negative step count
-    assert L.dgb_two_tap_rollout_vjp(1, p, 4, 4, p, -1, 3, p, p, None, 0, p, p, p, p, p, 0,
+    assert L.dgb_two_tap_rollout_vjp(1, p, 4, 4, p, -1, 3, p, p, 0, None, 0, p, p, p, p, p, 0,
                                      None, None, None, 0, p, p, p, None, None) == -1
     # a rollout plan is required
-    assert L.dgb_two_tap_rollout(0, p, 4, 4, p, 2, 3, p, p, None, 0, p, None, p, p, p, 0, None,
-                                 None) == -1
+    assert L.dgb_two_tap_rollout(0, p, 4, 4, p, 2, 3, p, p, 0, None, 0, p, None, p, p, p, 0,
+                                 None, None) == -1
+    # gates by source need source indices
+    assert L.dgb_two_tap_rollout(0, p, 4, 4, p, 2, 3, p, p, 8, None, 0, p, p, p, p, p, 8 | 16,
+                                 None, None) == -1
+    assert L.dgb_gates_by_source(0, 10, 3, p, p, 9, None) == -1
     # gather of an empty ring
     assert L.dgb_two_tap_gather(0, p, 0, p, 3, p, p, p, p, None) == -1
     assert L.dgb_three_tap_vjp(0, p, 0, 4, p, 2, p, p, p, p, p, p, p, p, None) == -1

@@ -159,13 +159,15 @@ def test_rollout_in_one_launch_matches_reference(cuda, golden, tag, npt, tdt):
     np.testing.assert_allclose(dl.grad.cpu().numpy(), ref, rtol=tol, atol=tol * np.abs(ref).max())
 
 
-def _network_case(seed, depth, width, E, n_src, steps, npt):
+def _network_case(seed, depth, width, E, n_src, steps, npt, chained=False):
     """Connections into few targets (heavy collisions) with delays wrapping the
-    ring; width == E: one connection per target slot (the register path)."""
+    ring; width == E: one connection per target slot (the register path);
+    chained: one per slot with both taps clear of the delivered row (the
+    direct kernels)."""
     rng = np.random.default_rng(seed)
     post = rng.permutation(E) if width == E else rng.integers(0, width, E)
     pre = rng.integers(0, n_src, E)
-    pos = rng.uniform(1.0, depth + 0.9, E)
+    pos = rng.uniform(1.0, depth - 1.0 if chained else depth + 0.9, E)
     off = np.floor(pos).astype(np.int64)
     frac = (pos - off).astype(npt)
     lower = (off % depth) * width + post
@@ -177,13 +179,16 @@ def _network_case(seed, depth, width, E, n_src, steps, npt):
     return post, pre, frac, lower, upper, w, gates, q0
 
 
-@pytest.mark.parametrize("depth,width", [(33, 700), (33, 5000), (600, 700)])
+@pytest.mark.parametrize("depth,width,chained", [(33, 700, False), (33, 5000, False),
+                                                (600, 700, False), (33, 5000, True),
+                                                (600, 5000, True)])
 @pytest.mark.parametrize("tag,npt,tdt", TAGS)
-def test_window_equals_single_steps_and_oracle(cuda, tag, npt, tdt, depth, width):
-    """Shared-memory ring (depth 33) and, for depth 600, the ring in place in HBM."""
+def test_window_equals_single_steps_and_oracle(cuda, tag, npt, tdt, depth, width, chained):
+    """Shared-memory ring (depth 33), the ring in place in HBM (depth 600) and
+    the direct kernels (chained)."""
     E, n_src, steps = 5000, 97, 70
     post, pre, frac, lower, upper, w, gates, q0 = _network_case(5, depth, width, E, n_src,
-                                                                steps, npt)
+                                                                steps, npt, chained)
     T = lambda a, dt=tdt: _t(a, cuda, dt)  # noqa: E731
     tl, tu, tp = T(lower, None), T(upper, None), T(pre, None)
     pay, fin = delays.two_tap_rollout(T(q0), 4, T(w), T(gates), T(frac), tl, tu, tp)
@@ -198,15 +203,18 @@ def test_window_equals_single_steps_and_oracle(cuda, tag, npt, tdt, depth, width
     np.testing.assert_array_equal(fin.cpu().numpy(), ofin)
     np.testing.assert_array_equal(pay.cpu().numpy(), opay)
     assert delays.delay_status() == 0
+    assert bool(delays.two_tap_plan(depth, width, tl, tu, tp, n_src).rollout.flags
+                & delays.CHAINED) == chained
 
 
-@pytest.mark.parametrize("width", [300, 2000])
+@pytest.mark.parametrize("width,chained", [(300, False), (2000, False), (2000, True)])
 @pytest.mark.parametrize("with_pre", [True, False])
 @pytest.mark.parametrize("tag,npt,tdt", TAGS)
-def test_rollout_adjoint_matches_oracle(cuda, tag, npt, tdt, with_pre, width, monkeypatch):
+def test_rollout_adjoint_matches_oracle(cuda, tag, npt, tdt, with_pre, width, chained,
+                                        monkeypatch):
     depth, E, n_src, steps = 21, 2000, 41, 50
     post, pre, frac, lower, upper, w, gates, q0 = _network_case(9, depth, width, E, n_src,
-                                                                steps, npt)
+                                                                steps, npt, chained)
     if not with_pre:
         gates = np.ascontiguousarray(gates[:, pre])
     rng = np.random.default_rng(10)
@@ -227,11 +235,12 @@ def test_rollout_adjoint_matches_oracle(cuda, tag, npt, tdt, with_pre, width, mo
     np.testing.assert_array_equal(tf.grad.cpu().numpy(), df)
 
 
+@pytest.mark.parametrize("chained", [False, True])
 @pytest.mark.parametrize("tag,npt,tdt", TAGS)
-def test_rollout_from_an_empty_ring(cuda, tag, npt, tdt):
+def test_rollout_from_an_empty_ring(cuda, tag, npt, tdt, chained):
     depth, width, E, n_src, steps = 40, 3000, 3000, 50, 90
     post, pre, frac, lower, upper, w, gates, _ = _network_case(13, depth, width, E, n_src, steps,
-                                                               npt)
+                                                               npt, chained)
     T = lambda a, dt=tdt: _t(a, cuda, dt)  # noqa: E731
     args = (T(w), T(gates), T(frac), T(lower, None), T(upper, None), T(pre, None))
     zeros = torch.zeros(depth, width, dtype=tdt, device=cuda)
