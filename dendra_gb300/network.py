@@ -125,7 +125,8 @@ class TreeNetwork:
     def __init__(self, cells, syn_node, conn_pre, conn_post, conn_delay_ms, conn_weight, *,
                  dt=0.025, dtype=torch.float32, device="cuda", ra=100.0, cm=1.0, celsius=6.3,
                  v_init=-65.0, g_pas=0.001, e_pas=-70.0, tau1=0.5, tau2=5.0, e_syn=0.0,
-                 spk_thr=0.0, bg_steps=None, bg_weight=0.0, window=None, chains=True):
+                 spk_thr=0.0, bg_steps=None, bg_weight=0.0, window=None, chains=True,
+                 bg_netstim=None):
         self.dtype = dtype
         self.device = torch.device(device)
         self.dt = float(dt)
@@ -204,8 +205,14 @@ class TreeNetwork:
         self.csr = dict(ptr=csr.ptr, pre=torch.as_tensor(self.conn["pre"][perm]),
                         delay=torch.as_tensor(dsteps[perm]),
                         weight=torch.as_tensor(self.conn["weight"][perm], dtype=dtype))
-        # background events: bit (step, cell)
+        # background events: bit (step, cell), from host lists or generated on
+        # the device by a NetStim with one generator per cell
+        if bg_netstim is not None and bg_netstim.N != self.n_cells:
+            raise ValueError("bg_netstim needs one generator per cell")
+        if bg_netstim is not None and bg_steps is not None:
+            raise ValueError("give bg_steps or bg_netstim, not both")
         self.bg_steps = bg_steps
+        self.bg_netstim = bg_netstim
         self.bg_weight = float(bg_weight)
         self.params = dict(gnabar=hh["gnabar"], gkbar=hh["gkbar"], ena=hh["ena"], ek=hh["ek"],
                            q10=q10_of(celsius), dt_ms=float(dt), spk_thr=float(spk_thr),
@@ -215,7 +222,25 @@ class TreeNetwork:
         self._node_syn_ptr = node_syn_ptr
         self._upload()
 
+    @property
+    def _has_bg(self):
+        return self.bg_steps is not None or self.bg_netstim is not None
+
+    def _bg_device(self, n_steps):
+        """Background bits of steps [0, n_steps) as a device tensor: generated
+        by the NetStim (counter-based draws: the same bits for any split of the
+        run) or uploaded from the host lists."""
+        if self.bg_netstim is not None:
+            ns = self.bg_netstim.initialize()
+            bits = ns.run(n_steps, self.params["dt_ms"], spikes=False, bits=True)
+            return bits, bits.shape[1]
+        bits_np, words = self._bg_bits(n_steps)
+        return torch.as_tensor(bits_np.view(np.int64), device=self.device), words
+
     def _bg_bits(self, n_steps):
+        if self.bg_netstim is not None:
+            bits, words = self._bg_device(n_steps)
+            return bits.cpu().numpy().view(np.uint64), words
         words = max(1, -(-self.n_cells // 64))
         bits = np.zeros((n_steps, words), dtype=np.uint64)
         if self.bg_steps is not None:
@@ -266,8 +291,7 @@ class TreeNetwork:
         """Device inputs of a run of n_steps from the current step: background
         event bits and the per-window spike masks."""
         windows = self._windows(n_steps)
-        bits_np, words = self._bg_bits(self.step + n_steps)
-        bg = torch.as_tensor(bits_np.view(np.int64), device=self.device)
+        bg, words = self._bg_device(self.step + n_steps)
         masks = torch.zeros(len(windows), self.n_cells, dtype=torch.int64, device=self.device)
         return windows, bg, words, masks
 
@@ -276,7 +300,7 @@ class TreeNetwork:
         L = _lib.load()
         st = _lib.stream_ptr(self.device)
         a = self._args()
-        a.bg_bits = bg.data_ptr() if self.bg_steps is not None else None
+        a.bg_bits = bg.data_ptr() if self._has_bg else None
         a.bg_words = words
         d = self.d
         for w, wl in enumerate(windows):
@@ -375,7 +399,7 @@ class TreeNetwork:
             spike_count=c(self.spike_count), nodes={k: c(v) for k, v in self.nodes.items()},
             syn={k: c(v) for k, v in self.syn.items()}, syn_ptr=self._syn_ptr.copy(),
             node_syn_ptr=self._node_syn_ptr.copy(), conn=self.conn, params=self.params,
-            bg_bits=bits if self.bg_steps is not None else None, bg_words=words,
+            bg_bits=bits if self._has_bg else None, bg_words=words,
             bg_syn=int(self.bg_syn_sorted[0]), bg_weight=self.bg_weight, depth=self.depth,
             slot=self.slot, step=self.step, n_syn=self.n_syn, n_cells=self.n_cells)
 
@@ -404,10 +428,12 @@ class CapturedRun:
 
 def random_network(n_cells, k_range=(200, 2000), syn_per_cell=100, seed=0, dt=0.025,
                    rate_hz=5.0, t_stop_ms=200.0, bg_weight=0.05, delay_range=(1.0, 5.0),
-                   **kw):
+                   bg="host", **kw):
     """Config-3-style network: random trees, syn_per_cell Exp2Syn inputs from random
     pre cells (lognormal(-7, 0.5) uS, delays U[1,5] ms), one background synapse at
-    the soma driven by a seeded 5 Hz Poisson process."""
+    the soma driven by a seeded 5 Hz Poisson process: event times drawn on the
+    host (bg="host") or a NetStim per cell on the device (bg="netstim":
+    interval 1000/rate_hz ms, noise 1)."""
     rng = np.random.default_rng(seed)
     cells = [random_cell(rng, int(rng.integers(k_range[0], k_range[1] + 1)))
              for _ in range(n_cells)]
@@ -429,5 +455,12 @@ def random_network(n_cells, k_range=(200, 2000), syn_per_cell=100, seed=0, dt=0.
         isi = rng.exponential(1000.0 / rate_hz, int(3 + 2 * rate_hz * t_stop_ms / 1000.0))
         times = np.cumsum(isi)
         bg_steps.append(np.floor(times[times < t_stop_ms] / dt).astype(np.int64))
+    if bg == "netstim":
+        from .netstim import NetStim
+
+        ns = NetStim(n_cells, interval=1000.0 / rate_hz, noise=1.0, start=0.0, seed=seed,
+                     dtype=kw.get("dtype", torch.float32), device=kw.get("device", "cuda"))
+        return TreeNetwork(cells, syn_node, pre, post, delay, weight, dt=dt, bg_netstim=ns,
+                           bg_weight=bg_weight, **kw), n_steps
     return TreeNetwork(cells, syn_node, pre, post, delay, weight, dt=dt, bg_steps=bg_steps,
                        bg_weight=bg_weight, **kw), n_steps

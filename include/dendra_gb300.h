@@ -47,6 +47,8 @@
  *   dgb_two_tap_gather        (networks/_two_tap_enqueue_cpu.cpp:61-315) and
  *                             dense_interpolated_delay_transition
  *                             (networks/_event_delivery.py:229-308)
+ *   dgb_netstim_init /        NetStim.initialize / NetStim.forward renewal,
+ *   dgb_netstim_run           networks/_netstim_renewal.py:70-159
  */
 #ifndef DENDRA_GB300_H
 #define DENDRA_GB300_H
@@ -715,6 +717,32 @@ int dgb_two_tap_rollout_vjp(int dtype, void* grad_ring, int64_t depth, int64_t w
    values): the per-source layout of DGB_ROLLOUT_GATES_BY_SOURCE. */
 int dgb_gates_by_source(int dtype, int64_t n_steps, int64_t n_sources, const void* gates,
                         void* gates_t, int64_t gate_row, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * NetStim renewal generators (networks/_netstim_renewal.py:70-159), one
+ * thread per generator.  Draws: Philox4x32-10 with key seed and counter
+ * (step, generator), E = -ln(U) evaluated with rounded IEEE operations only
+ * (reproducible on any host), or a caller-supplied table `draws`.
+ * ------------------------------------------------------------------------- */
+
+/* Initial clocks (netstim_initial_state): next_time = start + (noise interval) E
+   when any_noise (any generator has noise > 0), else start; counts = 0.
+   draws (optional): n initial draws. */
+int dgb_netstim_init(int dtype, int64_t n, const void* interval, const void* noise,
+                     const void* start, int32_t any_noise, uint64_t seed, const void* draws,
+                     void* next_time, int64_t* counts, void* stream);
+
+/* n_steps renewal steps (netstim_renewal without calendars) from absolute
+   step step0, t = t0 + step*dt in the state dtype: a generator fires when
+   t >= next_time and counts < number (NULL: unlimited); on firing next_time
+   advances by interval (1 - noise) + (interval noise) E and counts by one; a
+   draw is consumed every step.  draws (optional): [n_steps][n].  Outputs
+   (optional): spikes[k][g] (uint8) and bits[k][n_words] (bit g & 63 of word
+   g >> 6, as dgb_net_args.bg_bits). */
+int dgb_netstim_run(int dtype, int64_t n, int64_t n_steps, int64_t step0, double t0, double dt,
+                    const void* interval, const void* noise, const int64_t* number,
+                    uint64_t seed, const void* draws, void* next_time, int64_t* counts,
+                    uint8_t* spikes, uint64_t* bits, int64_t n_words, void* stream);
 
 /* First device-side index error of the delay kernels since the last call
    (0 = none, else DGB_DELAY_ERR_*), cleared on read; synchronises stream. */

@@ -18,7 +18,9 @@ Layers:
     (``cable_grad``: full state tape, transposed Thomas solve, gate partials
     on the forward's branches), and the interpolated delay transport
     (``two_tap_enqueue`` / ``three_tap_enqueue`` / ``two_tap_vjp`` and their
-    multi-step rollouts: the reference's ordered CPU op, sequential adds).
+    multi-step rollouts: the reference's ordered CPU op, sequential adds), and
+    the NetStim renewal with counter-based draws (Philox4x32-10, a series
+    logarithm in rounded operations).
   * ``core.py``  ctypes bindings; builds the C library with gcc on first use.
   The integer/index event primitives (delay rounding, bit packing, sequential
   delivery) are restated inline in ``tests/test_netcon.py``, next to the
@@ -46,4 +48,9 @@ from .core import (  # noqa: F401
     two_tap_vjp,
     two_tap_rollout,
     two_tap_rollout_vjp,
+    philox4x32_10,
+    series_log,
+    unit_exponential,
+    netstim_init,
+    netstim_run,
 )

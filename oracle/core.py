@@ -93,6 +93,16 @@ def _declare(L):
             [_I64, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _P])
         getattr(L, "orc_two_tap_rollout_vjp" + sfx).argtypes = (
             [_I64, _I64, _P, _I64, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P])
+        getattr(L, "orc_philox4x32_10" + sfx).argtypes = [_P, _P, _P]
+        getattr(L, "orc_series_log" + sfx).restype = ctypes.c_double
+        getattr(L, "orc_series_log" + sfx).argtypes = [ctypes.c_double]
+        getattr(L, "orc_unit_exponential" + sfx).restype = real
+        getattr(L, "orc_unit_exponential" + sfx).argtypes = [
+            ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32]
+        getattr(L, "orc_netstim_init" + sfx).argtypes = [
+            _I64, _P, _P, _P, _I32, ctypes.c_uint64, _P, _P, _P]
+        getattr(L, "orc_netstim_run" + sfx).argtypes = [
+            _I64, _I64, _I64, _D, _D, _P, _P, _P, ctypes.c_uint64, _P, _P, _P, _P]
     L.orc_num_threads.restype = ctypes.c_int
 
 
@@ -442,3 +452,53 @@ def two_tap_rollout_vjp(grad_queue, slot0, weights, gates, fraction, lower, uppe
         depth, width, _ptr(R), int(slot0), n_steps, w.size, _ptr(w), _ptr(g), _ptr(pre), n_src,
         _ptr(f), _ptr(lower), _ptr(upper), _ptr(gp), _ptr(dw), _ptr(dg), _ptr(df))
     return R, dw, dg, df
+
+
+# ---------------------------------------------------------------------------
+# NetStim renewal (networks/_netstim_renewal.py:70-159)
+# ---------------------------------------------------------------------------
+def philox4x32_10(counter, key):
+    """Philox4x32-10 block: 4 x uint32 counter, 2 x uint32 key -> 4 x uint32."""
+    c = np.ascontiguousarray(counter, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.empty(4, np.uint32)
+    lib().orc_philox4x32_10_f64(_ptr(c), _ptr(k), _ptr(out))
+    return out
+
+
+def series_log(x):
+    return float(lib().orc_series_log_f64(float(x)))
+
+
+def unit_exponential(seed, step, gen, stream=0, dtype=np.float64):
+    return getattr(lib(), "orc_unit_exponential" + _sfx(dtype))(seed, step, gen, stream)
+
+
+def netstim_init(interval, noise, start, seed=0, draws=None, dtype=np.float64):
+    """(next_time, counts) of netstim_initial_state."""
+    iv, nz, st = (np.ascontiguousarray(a, dtype=dtype) for a in (interval, noise, start))
+    n = iv.size
+    d = None if draws is None else np.ascontiguousarray(draws, dtype=dtype)
+    nxt = np.empty(n, dtype)
+    cnt = np.empty(n, np.int64)
+    getattr(lib(), "orc_netstim_init" + _sfx(dtype))(
+        n, _ptr(iv), _ptr(nz), _ptr(st), int(bool((nz > 0).any())), seed, _ptr(d), _ptr(nxt),
+        _ptr(cnt))
+    return nxt, cnt
+
+
+def netstim_run(next_time, counts, n_steps, interval, noise, number=None, step0=0, t0=0.0,
+                dt=0.025, seed=0, draws=None):
+    """n_steps renewal steps: returns (next_time, counts, spikes[n_steps][n])."""
+    nxt = np.array(next_time, copy=True)
+    dtype = nxt.dtype
+    cnt = np.array(counts, dtype=np.int64, copy=True)
+    iv, nz = (np.ascontiguousarray(a, dtype=dtype) for a in (interval, noise))
+    num = None if number is None else np.ascontiguousarray(number, dtype=np.int64)
+    d = None if draws is None else np.ascontiguousarray(draws, dtype=dtype)
+    n = nxt.size
+    spikes = np.empty((n_steps, n), np.uint8)
+    getattr(lib(), "orc_netstim_run" + _sfx(dtype))(
+        n, n_steps, step0, float(t0), float(dt), _ptr(iv), _ptr(nz), _ptr(num), seed, _ptr(d),
+        _ptr(nxt), _ptr(cnt), _ptr(spikes))
+    return nxt, cnt, spikes

@@ -1018,6 +1018,108 @@ void F(orc_two_tap_rollout_vjp)(int64_t depth, int64_t width, REAL* R, int64_t s
   free(tf);
 }
 
+/* ---------------------------------------------------------------------------
+ * NetStim renewal (networks/_netstim_renewal.py:70-159) with counter-based
+ * draws: Philox4x32-10 (Salmon et al., SC'11), E = -ln(U) by the atanh series
+ * in double precision with rounded operations only (same draws as the GPU).
+ * ------------------------------------------------------------------------- */
+static void F(philox4x32_10)(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    c[0] = n0;
+    c[1] = (uint32_t)p1;
+    c[2] = n2;
+    c[3] = (uint32_t)p0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+void F(orc_philox4x32_10)(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
+  for (int i = 0; i < 4; ++i) out[i] = ctr[i];
+  F(philox4x32_10)(out, key[0], key[1]);
+}
+
+double F(orc_series_log)(double x) {
+  int e = 0;
+  double m = frexp(x, &e);
+  if (m < 0.70710678118654752440) {
+    m = m * 2.0;
+    e -= 1;
+  }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double s2 = s * s;
+  double p = 1.0 / 23.0;
+  p = p * s2 + 1.0 / 21.0;
+  p = p * s2 + 1.0 / 19.0;
+  p = p * s2 + 1.0 / 17.0;
+  p = p * s2 + 1.0 / 15.0;
+  p = p * s2 + 1.0 / 13.0;
+  p = p * s2 + 1.0 / 11.0;
+  p = p * s2 + 1.0 / 9.0;
+  p = p * s2 + 1.0 / 7.0;
+  p = p * s2 + 1.0 / 5.0;
+  p = p * s2 + 1.0 / 3.0;
+  p = p * s2 + 1.0;
+  const double lm = (2.0 * s) * p;
+  return (double)e * 0.69314718055994530942 + lm;
+}
+
+REAL F(orc_unit_exponential)(uint64_t seed, uint64_t step, uint32_t gen, uint32_t stream) {
+  uint32_t c[4] = {(uint32_t)step, gen, stream, (uint32_t)(step >> 32)};
+  F(philox4x32_10)(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  double u;
+  if (IS_F64) {
+    const uint64_t b = ((uint64_t)c[0] << 21) ^ (uint64_t)(c[1] >> 11);
+    u = ((double)(b & ((1ull << 53) - 1)) + 0.5) * 1.1102230246251565e-16;
+  } else {
+    u = ((double)(c[0] >> 8) + 0.5) * 5.9604644775390625e-08;
+  }
+  return (REAL)(-F(orc_series_log)(u));
+}
+
+void F(orc_netstim_init)(int64_t n, const REAL* interval, const REAL* noise, const REAL* start,
+                         int32_t any_noise, uint64_t seed, const REAL* draws, REAL* next,
+                         int64_t* counts) {
+  for (int64_t g = 0; g < n; ++g) {
+    REAL clock = start[g];
+    if (any_noise) {
+      const REAL E = draws ? draws[g] : F(orc_unit_exponential)(seed, 0, (uint32_t)g, 1u);
+      clock = clock + (noise[g] * interval[g]) * E;
+    }
+    next[g] = clock;
+    counts[g] = 0;
+  }
+}
+
+void F(orc_netstim_run)(int64_t n, int64_t n_steps, int64_t step0, double t0, double dt,
+                        const REAL* interval, const REAL* noise, const int64_t* number,
+                        uint64_t seed, const REAL* draws, REAL* next, int64_t* counts,
+                        uint8_t* spikes) {
+  const REAL T0 = (REAL)t0, DT = (REAL)dt;
+  for (int64_t g = 0; g < n; ++g) {
+    REAL clock = next[g];
+    int64_t count = counts[g];
+    const int64_t cap = number ? number[g] : INT64_MAX;
+    const REAL a = interval[g] * ((REAL)1 - noise[g]), b = interval[g] * noise[g];
+    for (int64_t k = 0; k < n_steps; ++k) {
+      const int64_t step = step0 + k;
+      const REAL t = T0 + (REAL)step * DT;
+      const REAL E = draws ? draws[k * n + g]
+                           : F(orc_unit_exponential)(seed, (uint64_t)step, (uint32_t)g, 0u);
+      const int fire = (t >= clock) && count < cap;
+      const REAL gate = fire ? (REAL)1 : (REAL)0;
+      const REAL nxt = a + b * E;
+      clock = clock + (nxt * gate) * gate;
+      count += fire;
+      if (spikes) spikes[k * n + g] = (uint8_t)fire;
+    }
+    next[g] = clock;
+    counts[g] = count;
+  }
+}
+
 #undef AM1
 #undef AH1
 #undef AN1

@@ -23,6 +23,8 @@ compatibility shims) and records its outputs on seeded inputs:
                            torch.utils.cpp_extension into oracle/_ref/), the
                            pure-torch dense_interpolated_delay_transition (two
                            and three taps) and a 40-step rollout with autograd
+  netstim_{f64,f32}.npz    NetStim renewal: netstim_initial_state and 600 steps of
+                           netstim_renewal with supplied unit-exponential draws
 
 Usage (in a container that holds the reference source):
 
@@ -473,9 +475,39 @@ def delay(dtype, tag):
     print("delay", tag)
 
 
+def netstim(dtype, tag):
+    _ref()
+    from dendra.models.networks._netstim_renewal import netstim_initial_state, netstim_renewal
+
+    rng = np.random.default_rng(91 if tag == "f64" else 92)
+    N, T, dt = 9, 600, 0.025
+    interval = np.array([10.0, 5.0, 200.0, 1.3, 7.0, 50.0, 0.02, 1e30, 3.0])
+    noise = np.array([0.0, 0.5, 1.0, 1.0, 0.3, 0.0, 1.0, 0.7, 0.2])
+    start = np.array([0.0, 2.0, 0.0, 1.5, 0.0, 10.0, 0.0, 0.0, 0.1])
+    number = np.array([10**9, 3, 10**9, 5, 10**9, 2, 10**9, 10**9, 0], dtype=np.int64)
+    draws0 = rng.exponential(size=N)
+    draws = rng.exponential(size=(T, N))
+    tt = lambda a: torch.as_tensor(a).to(dtype)  # noqa: E731
+    state = netstim_initial_state(tt(interval), tt(start), tt(noise), tt(draws0))
+    nxt, cnt, spk = [state.next_stoch_time.numpy().copy()], [state.spike_counts.numpy().copy()], []
+    for k in range(T):
+        t = torch.zeros((), dtype=dtype) + torch.tensor(float(k), dtype=dtype) * dt
+        tr = netstim_renewal(state, tt(interval), tt(noise), torch.as_tensor(number), t,
+                             tt(draws[k]), tau=0.5, bptt=False)
+        state = tr.state
+        nxt.append(state.next_stoch_time.numpy().copy())
+        cnt.append(state.spike_counts.numpy().copy())
+        spk.append(tr.spikes.numpy().astype(np.uint8))
+    out = dict(interval=interval, noise=noise, start=start, number=number, dt=dt,
+               draws0=draws0, draws=draws, next_time=np.stack(nxt), counts=np.stack(cnt),
+               spikes=np.stack(spk))
+    np.savez_compressed(os.path.join(HERE, f"netstim_{tag}.npz"), **out)
+    print("netstim", tag, int(out["spikes"].sum()))
+
+
 if __name__ == "__main__":
     what = sys.argv[1:] or ["rates", "tridiag", "dhs", "events", "cable", "extra", "adjoint",
-                            "block3", "delay"]
+                            "block3", "delay", "netstim"]
     if "rates" in what:
         rates()
     if "tridiag" in what:
@@ -497,3 +529,6 @@ if __name__ == "__main__":
     if "delay" in what:
         delay(torch.float64, "f64")
         delay(torch.float32, "f32")
+    if "netstim" in what:
+        netstim(torch.float64, "f64")
+        netstim(torch.float32, "f32")

@@ -73,3 +73,23 @@ def test_chain_and_layer_schedules_give_identical_runs(cuda):
     for a, b in zip(*out):
         assert torch.equal(a, b)
     assert int(out[0][0].sum()) > 0
+
+
+@pytest.mark.parametrize("dtype", [torch.float64])
+def test_network_with_device_netstim_background(cuda, dtype):
+    """Background events generated on the device by a NetStim per cell; the
+    oracle runs on the same event bits (read back from the device)."""
+    net, n_steps = random_network(16, k_range=(30, 400), syn_per_cell=12, seed=4, dtype=dtype,
+                                  device=cuda, t_stop_ms=60.0, bg_weight=0.05, rate_hz=40.0,
+                                  bg="netstim")
+    pd = net.problem_dict(n_steps)
+    assert pd["bg_bits"] is not None and int(np.unpackbits(pd["bg_bits"].view(np.uint8)).sum())
+    if dtype == torch.float32:
+        for grp in ("nodes", "syn"):
+            pd[grp] = {k: v.astype(np.float64) for k, v in pd[grp].items()}
+        for k in ("v", "m", "h", "n", "A", "B", "ring"):
+            pd[k] = pd[k].astype(np.float64)
+    ref = oracle.net_run(pd, n_steps)
+    raster = net.run(n_steps).cpu().numpy()
+    assert ref.sum() > 0
+    np.testing.assert_array_equal(raster, ref)
