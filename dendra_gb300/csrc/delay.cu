@@ -769,13 +769,21 @@ __global__ void source_sum_kernel(const T* __restrict__ scratch, int64_t n_steps
   T acc = T(0);
   int64_t j0, j1;
   if (column_range(src_ptr, s, n_edges, j0, j1)) {
-    for (int64_t j = j0; j < j1; ++j) {
-      const int64_t pos = src_pos[j];
-      if ((uint64_t)pos >= (uint64_t)n_edges) {
-        delay_fail(DGB_DELAY_ERR_PLAN);
-        continue;
+    // eight loads in flight, then their additions in order
+    for (int64_t jb = j0; jb < j1; jb += 8) {
+      T v[8];
+      bool ok[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int64_t j = jb + q;
+        const int64_t pos = j < j1 ? src_pos[j] : 0;
+        ok[q] = j < j1 && (uint64_t)pos < (uint64_t)n_edges;
+        if (j < j1 && !ok[q]) delay_fail(DGB_DELAY_ERR_PLAN);
+        v[q] = ok[q] ? scratch[pos * kc + k] : T(0);
       }
-      acc = add_rn(acc, scratch[pos * kc + k]);
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (ok[q]) acc = add_rn(acc, v[q]);
     }
   }
   dgate[k * n_src + s] = acc;
@@ -884,7 +892,6 @@ __global__ void __launch_bounds__(128)
   };
   int32_t row = (int32_t)slot0;
   // gates one group ahead: gq holds steps kb - lo .. kb - lo + 7
-  T gprev = T(0);
   T gq[8], gn[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -892,6 +899,12 @@ __global__ void __launch_bounds__(128)
     gq[i] = (ne == 1 && j >= 0 && j < n_steps) ? gate_at<T, GT>(gates, j, src, gate_stride, g_kc)
                                                : T(0);
   }
+  // the upper-tap term of step k is the lower-tap product of step k - 1:
+  // (w g[j-1]) is carried, and each delivered value is
+  //   ((c0 + wg_prev f) + wg (1 - f)),  terms present once their step exists
+  T wg_prev = T(0);
+  T* out = payload ? payload + col : nullptr;
+  const T* init = ring + (int64_t)row * width + col;
   for (int64_t kb = 0; kb < n_steps; kb += 8) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -903,9 +916,24 @@ __global__ void __launch_bounds__(128)
     for (int i = 0; i < 8; ++i) {
       const int64_t k = kb + i;
       if (k >= n_steps) break;
-      if (payload) payload[k * width + col] = cell(k, row, gq[i], gprev);
-      gprev = gq[i];
-      if (++row == D) row = 0;
+      T v = (k < D && !empty) ? *init : T(0);
+      const int64_t j = k - lo;
+      const T wg = mul_rn(w, gq[i]);
+      if (ne == 1) {
+        if (j >= 1) v = add_rn(v, mul_rn(wg_prev, f));
+        if (j >= 0) v = add_rn(v, mul_rn(wg, share));
+      }
+      wg_prev = wg;
+      if (out) {
+        *out = v;
+        out += width;
+      }
+      if (++row == D) {
+        row = 0;
+        init = ring + col;
+      } else {
+        init += width;
+      }
     }
 #pragma unroll
     for (int i = 0; i < 8; ++i) gq[i] = gn[i];
