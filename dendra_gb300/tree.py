@@ -212,6 +212,103 @@ def dhs_solve_cuda(d_mem, a_geom, b, parent_idx, order, layer_ptr, threads=32):
     return _DHSSolve.apply(d_mem, a_geom, b, topo)
 
 
+def validate_tree_block(main, edge, rhs, parent_idx, order, layer_ptr, threads):
+    """Contract of the 3x3 block tree solve (triton/_contracts.py:232-268)."""
+    data = (("main", main), ("edge", edge), ("rhs", rhs))
+    topo = (("parent_idx", parent_idx), ("order", order), ("layer_ptr", layer_ptr))
+    for name, t in data + topo:
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{name} must be a torch.Tensor")
+    if rhs.ndim != 3 or rhs.shape[-1] != 3:
+        raise ValueError(f"rhs must have shape (B, K, 3), got {tuple(rhs.shape)}")
+    batch, size, _ = map(int, rhs.shape)
+    if batch < 1 or size < 1:
+        raise ValueError("B and K must both be >= 1")
+    if tuple(edge.shape) != (batch, size, 3):
+        raise ValueError(f"edge must have shape {(batch, size, 3)}, got {tuple(edge.shape)}")
+    if tuple(main.shape) != (batch, size, 3, 3):
+        raise ValueError(
+            f"main must have shape {(batch, size, 3, 3)}, got {tuple(main.shape)}")
+    _validate_float_group(data)
+    for name, t in topo:
+        if t.ndim != 1:
+            raise ValueError(f"{name} must be 1-D")
+        if t.dtype not in _INDEX_DTYPES:
+            raise TypeError(f"{name} must have dtype int32 or int64")
+        if t.device != rhs.device:
+            raise ValueError(f"{name} must be on device {rhs.device}; got {t.device}")
+    if parent_idx.numel() != size or order.numel() != size:
+        raise ValueError("parent_idx and order must each contain K entries")
+    if layer_ptr.numel() < 2:
+        raise ValueError("layer_ptr must contain at least two entries")
+    return batch, size, validate_threads(threads)
+
+
+def _checked_topology(parent_idx, order, layer_ptr):
+    """Device plan with the children CSR, after checking it indexes K nodes:
+    parents in [-1, K), order a permutation, layer_ptr from 0 to K, nondecreasing."""
+    K = parent_idx.numel()
+    p = parent_idx.detach().cpu().numpy().astype(np.int64)
+    o = order.detach().cpu().numpy().astype(np.int64)
+    lp = layer_ptr.detach().cpu().numpy().astype(np.int64)
+    if (p < -1).any() or (p >= K).any():
+        raise ValueError("parent_idx entries must lie in [-1, K)")
+    if not np.array_equal(np.sort(o), np.arange(K)):
+        raise ValueError("order must be a permutation of range(K)")
+    if lp[0] != 0 or lp[-1] != K or (np.diff(lp) < 0).any():
+        raise ValueError("layer_ptr must rise from 0 to K")
+    return _device_topology(parent_idx, order, layer_ptr)
+
+
+def _block_solve(main, edge, rhs, topo, transpose):
+    parent, order, layer_ptr, cptr, cidx = topo
+    B, K = rhs.shape[:2]
+    main, edge, rhs = (t.contiguous() for t in (main, edge, rhs))
+    x = torch.empty_like(rhs)
+    with torch.cuda.device(rhs.device):
+        rc = _lib.load().dgb_dhs_block3_solve(
+            _lib.dtype_code(rhs.dtype), B, K, main.data_ptr(), edge.data_ptr(), rhs.data_ptr(),
+            parent.data_ptr(), order.data_ptr(), layer_ptr.data_ptr(), layer_ptr.numel() - 1,
+            cptr.data_ptr(), cidx.data_ptr(), x.data_ptr(), 1 if transpose else 0,
+            _lib.stream_ptr(rhs.device))
+    _lib.check(rc, "dgb_dhs_block3_solve")
+    return x
+
+
+class _DHSBTSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, main, edge, rhs, topo):
+        x = _block_solve(main, edge, rhs, topo, False)
+        ctx.topo = topo
+        ctx.save_for_backward(main, edge, x)
+        return x
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        main, edge, X = ctx.saved_tensors
+        g = _block_solve(main, edge, grad_out.contiguous(), ctx.topo, True)  # A^T
+        parent_idx = ctx.topo[0].long()
+        parent = parent_idx.clamp_min(0)
+        Xp = X.index_select(1, parent)
+        gp = g.index_select(1, parent)
+        root = (parent_idx < 0).view(1, -1, 1)
+        grad_edge = torch.where(root, -(g * X), -((g - gp) * (X - Xp)))
+        grad_main = -(g.unsqueeze(-1) * X.unsqueeze(-2))
+        return grad_main, grad_edge, g, None
+
+
+def dhs_bt_solve_cuda(D_blocks, G_vec, b, parent_idx, order, layer_ptr, threads=16):
+    """Tree solve for 3-component unknowns (v_i, ve0, ve1) per node, drop-in for
+    the reference's dhs_bt_solve_cuda (triton/dhs_kernel_bt.py:465-479): D_blocks
+    (B, K, 3, 3), G_vec (B, K, 3) edge conductances to the parent, b (B, K, 3),
+    all in solver order.  Differentiable in D_blocks, G_vec and b (the
+    reference's DHSBTSolve3.backward formulas; the adjoint is the transposed
+    block solve).  ``threads`` is validated like the reference's."""
+    validate_tree_block(D_blocks, G_vec, b, parent_idx, order, layer_ptr, threads)
+    topo = _checked_topology(parent_idx, order, layer_ptr)
+    return _DHSBTSolve.apply(D_blocks, G_vec, b, topo)
+
+
 def build_chains(parent):
     """Chain schedule of a tree: unbranched chains grouped by level.
 

@@ -26,6 +26,7 @@
  *                             integrators/implicit.py:569-664
  *   dgb_dhs_solve             dhs_solve_cuda, triton/dhs_kernel.py:634-651
  *   dgb_dhs_solve_forest      dhs_solve_multi_cuda, triton/dhs_kernel_multi.py:831-888
+ *   dgb_dhs_block3_solve      dhs_bt_solve_cuda, triton/dhs_kernel_bt.py:465-479
  *   dgb_detect_spikes         threshold_transition, networks/spiking.py:43-73
  *   dgb_pack_source_spikes    pack_source_spikes, networks/netcon_bitpack_kernel.cpp:145-149
  *   dgb_build_delivery        build_delivery, networks/netcon_bitpack_kernel.cpp:145-149
@@ -136,6 +137,25 @@ int dgb_block3_solve(int dtype, int64_t B, int64_t K, const void* lower,
 
 /* Scratch bytes dgb_block3_solve needs (0: its factors stay on chip). */
 size_t dgb_block3_work_size(int dtype, int64_t B, int64_t K);
+
+/*
+ * Tree solve with 3x3 blocks (multi-layer extracellular trees), B trees of K
+ * nodes sharing one topology, in solver order:
+ *   main (B, K, 3, 3) row-major node blocks D_i, edge (B, K, 3) the diagonal
+ *   conductances g_i to the parent, rhs / x (B, K, 3);
+ *   A_ii = D_i + diag(g_i) + sum_children diag(g_c),  A_ic = A_ci = -diag(g_c).
+ * parent / order / layer_ptr: the reference's plan (order deepest layer
+ * first); child_ptr (K+1) / child_idx (K-1): children of every node.  One
+ * warp per tree, children pulled in CSR order (deterministic); needs
+ * 12*K*sizeof(T) bytes of shared memory.  transpose = 1 solves with main
+ * blocks transposed (the adjoint system).  x must not alias rhs.
+ * Replaces dhs_bt_solve_cuda (triton/dhs_kernel_bt.py:465-479).
+ */
+int dgb_dhs_block3_solve(int dtype, int64_t B, int64_t K, const void* main_blocks,
+                         const void* edge, const void* rhs, const int32_t* parent,
+                         const int32_t* order, const int32_t* layer_ptr, int32_t n_layers,
+                         const int32_t* child_ptr, const int32_t* child_idx, void* x,
+                         int32_t transpose, void* stream);
 
 /*
  * Arguments of a multi-step unbranched Hodgkin–Huxley cable run.

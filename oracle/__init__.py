@@ -53,4 +53,6 @@ from .core import (  # noqa: F401
     unit_exponential,
     netstim_init,
     netstim_run,
+    dhs_block3_matrix,
+    dhs_block3_solve,
 )

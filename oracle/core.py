@@ -502,3 +502,34 @@ def netstim_run(next_time, counts, n_steps, interval, noise, number=None, step0=
         n, n_steps, step0, float(t0), float(dt), _ptr(iv), _ptr(nz), _ptr(num), seed, _ptr(d),
         _ptr(nxt), _ptr(cnt), _ptr(spikes))
     return nxt, cnt, spikes
+
+
+# ---------------------------------------------------------------------------
+# 3x3 block tree solve (triton/dhs_kernel_bt.py: the matrix its kernel factors)
+# ---------------------------------------------------------------------------
+def dhs_block3_matrix(D, G, parent):
+    """Dense (B, 3K, 3K) matrices: A_ii = D_i + diag(g_i) + sum_children diag(g_c),
+    A_ic = A_ci = -diag(g_c)."""
+    D = np.asarray(D, dtype=np.float64)
+    G = np.asarray(G, dtype=np.float64)
+    B, K = G.shape[:2]
+    A = np.zeros((B, 3 * K, 3 * K))
+    for i in range(K):
+        A[:, 3 * i:3 * i + 3, 3 * i:3 * i + 3] += D[:, i] + np.einsum("bj,jk->bjk", G[:, i],
+                                                                        np.eye(3))
+    for c, p in enumerate(parent):
+        if p < 0:
+            continue
+        for r in range(3):
+            A[:, 3 * p + r, 3 * p + r] += G[:, c, r]
+            A[:, 3 * c + r, 3 * p + r] -= G[:, c, r]
+            A[:, 3 * p + r, 3 * c + r] -= G[:, c, r]
+    return A
+
+
+def dhs_block3_solve(D, G, b, parent):
+    """Dense solve of the block tree systems, (B, K, 3) solutions (float64)."""
+    A = dhs_block3_matrix(D, G, parent)
+    B, K = np.asarray(b).shape[:2]
+    return np.linalg.solve(A, np.asarray(b, dtype=np.float64).reshape(B, 3 * K, 1)).reshape(
+        B, K, 3)

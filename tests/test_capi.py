@@ -152,3 +152,27 @@ def test_delay_contract_errors_on_the_host():
     # gather of an empty ring
     assert L.dgb_two_tap_gather(0, p, 0, p, 3, p, p, p, p, None) == -1
     assert L.dgb_three_tap_vjp(0, p, 0, 4, p, 2, p, p, p, p, p, p, p, p, None) == -1
+
+
+def test_block_tree_contract_errors_on_the_host():
+    import torch
+
+    from dendra_gb300.tree import validate_tree_block
+
+    rhs = torch.zeros(2, 5, 3)
+    main = torch.zeros(2, 5, 3, 3)
+    edge = torch.zeros(2, 5, 3)
+    i = torch.zeros(5, dtype=torch.int64)
+    lp = torch.tensor([0, 5])
+    with pytest.raises(ValueError, match="rhs must have shape"):
+        validate_tree_block(main, edge, torch.zeros(2, 5), i, i, lp, 16)
+    with pytest.raises(ValueError, match="edge must have shape"):
+        validate_tree_block(main, torch.zeros(2, 5, 2), rhs, i, i, lp, 16)
+    with pytest.raises(ValueError, match="main must have shape"):
+        validate_tree_block(torch.zeros(2, 5, 9), edge, rhs, i, i, lp, 16)
+    with pytest.raises(ValueError, match="CUDA"):  # data must live on the GPU
+        validate_tree_block(main, edge, rhs, i, i, lp, 16)
+    L = dendra_gb300.load()
+    p = 16
+    assert L.dgb_dhs_block3_solve(0, 0, 4, p, p, p, p, p, p, 1, p, p, p, 0, None) == -1
+    assert L.dgb_dhs_block3_solve(0, 2, 4, p, p, p, p, p, p, 1, p, p, p, 0, None) == -1  # alias
