@@ -117,6 +117,8 @@ SIGNATURES = {
                                        _P, _P, _P]),
     "dgb_gates_by_source": (_INT, [_INT, _I64, _I64, _P, _P, _I64, _P]),
     "dgb_delay_status": (_INT, [_P]),
+    "dgb_block3_spd_solve": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "dgb_block3_spd_solve_chol": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P]),
     "dgb_dhs_block3_solve": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P,
                                     _I32, _P]),
     "dgb_netstim_init": (_INT, [_INT, _I64, _P, _P, _P, _I32, ctypes.c_uint64, _P, _P, _P, _P]),

@@ -211,3 +211,81 @@ def thomas_solve_cuda_bt(lower, main, upper, rhs):
     (B, K, 3, 3); rhs: (B, K, 3).  Returns x (B, K, 3); differentiable."""
     validate_block_tridiagonal(lower, main, upper, rhs)
     return _Block3Solve.apply(lower, main, upper, rhs)
+
+
+# ---------------------------------------------------------------------------
+# SPD block Thomas (triton/bt_spd_kernel.py:583-755)
+# ---------------------------------------------------------------------------
+def _symmetric_part(value):
+    """(value + value^T) / 2 per 3x3 block without overflow or loss of
+    subnormals (the reference's integrators/_symmetry.py:6-30 rule)."""
+    t = value.transpose(-1, -2)
+    lim = torch.finfo(value.dtype)
+    half_max = lim.max / 2.0
+    bounded = (value.abs() <= half_max) & (t.abs() <= half_max)
+    extreme = torch.where(value.abs() < 2.0 * lim.tiny, value + t * 0.5,
+                          torch.where(t.abs() < 2.0 * lim.tiny, value * 0.5 + t,
+                                      value * 0.5 + t * 0.5))
+    return torch.where(bounded, (value + t) * 0.5, extreme)
+
+
+def _block3_spd(lower, main, upper, rhs):
+    B, K = rhs.shape[:2]
+    lower, main, upper, rhs = (t.contiguous() for t in (lower, main, upper, rhs))
+    x = torch.empty_like(rhs)
+    chol = torch.empty(B, K, 9, dtype=rhs.dtype, device=rhs.device)
+    info = torch.empty(B, K, dtype=torch.int32, device=rhs.device)
+    with torch.cuda.device(rhs.device):
+        rc = _lib.load().dgb_block3_spd_solve(
+            _lib.dtype_code(rhs.dtype), B, K, lower.data_ptr(), main.data_ptr(),
+            upper.data_ptr(), rhs.data_ptr(), x.data_ptr(), chol.data_ptr(), info.data_ptr(),
+            _lib.stream_ptr(rhs.device))
+    _lib.check(rc, "dgb_block3_spd_solve")
+    # the reference asserts on the device; here the host reads the flags, so
+    # a failed factorisation raises without faulting the context
+    if bool((info != 0).any()):
+        raise RuntimeError("solve_bt_spd_cuda: Cholesky failed after all diagonal bumps")
+    return x, chol
+
+
+def _block3_spd_with_chol(lower, upper, chol, rhs):
+    B, K = rhs.shape[:2]
+    rhs = rhs.contiguous()
+    x = torch.empty_like(rhs)
+    with torch.cuda.device(rhs.device):
+        rc = _lib.load().dgb_block3_spd_solve_chol(
+            _lib.dtype_code(rhs.dtype), B, K, lower.contiguous().data_ptr(),
+            upper.contiguous().data_ptr(), chol.data_ptr(), rhs.data_ptr(), x.data_ptr(),
+            _lib.stream_ptr(rhs.device))
+    _lib.check(rc, "dgb_block3_spd_solve_chol")
+    return x
+
+
+class _Block3SpdSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, lower, main, upper, rhs):
+        x, chol = _block3_spd(lower, main, upper, rhs)
+        ctx.save_for_backward(lower, upper, x, chol)
+        return x
+
+    @staticmethod
+    def backward(ctx, grad_x):
+        # the reference's _SolveBTSPDCudaConsumeUnchecked.backward
+        # (bt_spd_kernel.py:697-712): the cached factors solve the (symmetric)
+        # system again; the main-block gradient is the symmetric part
+        lower, upper, x, chol = ctx.saved_tensors
+        g = _block3_spd_with_chol(lower, upper, chol, grad_x)
+        grad_main = -_symmetric_part(g.unsqueeze(-1) * x.unsqueeze(-2))
+        grad_upper = -(g[:, :-1] * x[:, 1:])
+        grad_lower = -(g[:, 1:] * x[:, :-1])
+        return grad_lower, grad_main, grad_upper, g
+
+
+def solve_bt_spd_cuda(lower, main, upper, rhs):
+    """Drop-in for the reference's solve_bt_spd_cuda (triton/bt_spd_kernel.py:744-755):
+    SPD block Thomas on (B, K) systems of 3x3 blocks (lower/upper (B, K-1, 3),
+    main (B, K, 3, 3), rhs (B, K, 3)); blocks are symmetrised and, when not
+    positive definite, shifted on the diagonal like the reference's;
+    differentiable with the reference's gradients."""
+    validate_block_tridiagonal(lower, main, upper, rhs)
+    return _Block3SpdSolve.apply(lower, main, upper, rhs)

@@ -18,6 +18,7 @@
  *                             integrators/implicit.py:364-440, called at :647
  *   dgb_tridiag_solve_transpose  ThomasSolve.backward, t_kernel_thomas.py:147-189
  *   dgb_block3_solve          thomas_solve_cuda_bt, triton/bt_kernel.py:195-298
+ *   dgb_block3_spd_solve      solve_bt_spd_cuda, triton/bt_spd_kernel.py:583-755
  *                             (3x3 block Thomas of the multi-layer extracellular
  *                             integrator, implicit.py:669-1136)
  *   dgb_cable_run             one Population.run over an unbranched HH cable
@@ -137,6 +138,22 @@ int dgb_block3_solve(int dtype, int64_t B, int64_t K, const void* lower,
 
 /* Scratch bytes dgb_block3_solve needs (0: its factors stay on chip). */
 size_t dgb_block3_work_size(int dtype, int64_t B, int64_t K);
+
+/*
+ * SPD block Thomas on the same systems (solve_bt_spd_cuda,
+ * triton/bt_spd_kernel.py:174-370, 583-755): one thread per system; every
+ * Schur block symmetrised and Cholesky-factored, with the reference's
+ * diagonal shifts when it is not positive definite (info[b][k] = 1 when even
+ * the last shift failed).  chol (B, K, 9) receives the factors; x must not
+ * alias rhs.  dgb_block3_spd_solve_chol solves the same system again with
+ * the cached factors (the backward's solve).
+ */
+int dgb_block3_spd_solve(int dtype, int64_t B, int64_t K, const void* lower,
+                         const void* main_blocks, const void* upper, const void* rhs, void* x,
+                         void* chol, int32_t* info, void* stream);
+int dgb_block3_spd_solve_chol(int dtype, int64_t B, int64_t K, const void* lower,
+                              const void* upper, const void* chol, const void* rhs, void* x,
+                              void* stream);
 
 /*
  * Tree solve with 3x3 blocks (multi-layer extracellular trees), B trees of K

@@ -55,4 +55,5 @@ from .core import (  # noqa: F401
     netstim_run,
     dhs_block3_matrix,
     dhs_block3_solve,
+    block3_spd_solve,
 )

@@ -533,3 +533,98 @@ def dhs_block3_solve(D, G, b, parent):
     B, K = np.asarray(b).shape[:2]
     return np.linalg.solve(A, np.asarray(b, dtype=np.float64).reshape(B, 3 * K, 1)).reshape(
         B, K, 3)
+
+
+# ---------------------------------------------------------------------------
+# SPD block Thomas (triton/bt_spd_kernel.py:9-370), restated in numpy
+# ---------------------------------------------------------------------------
+def _spd_mid(a, b, dt):
+    fi = np.finfo(dt)
+    hm, tt = fi.max / 2, 2 * fi.tiny
+    bounded = (np.abs(a) <= hm) & (np.abs(b) <= hm)
+    extreme = np.where(np.abs(a) < tt, a + 0.5 * b,
+                       np.where(np.abs(b) < tt, 0.5 * a + b, 0.5 * a + 0.5 * b))
+    return np.where(bounded, 0.5 * (a + b), extreme)
+
+
+def _chol3(a):
+    c0 = a[..., 0] > 0
+    l00 = np.sqrt(np.where(c0, a[..., 0], 1.0))
+    l10, l20 = a[..., 1] / l00, a[..., 2] / l00
+    s11 = a[..., 4] - l10 * l10
+    c1 = s11 > 0
+    l11 = np.sqrt(np.where(c1, s11, 1.0))
+    l21 = (a[..., 5] - l10 * l20) / l11
+    s22 = a[..., 8] - l20 * l20 - l21 * l21
+    c2 = s22 > 0
+    l22 = np.sqrt(np.where(c2, s22, 1.0))
+    z = np.zeros_like(l00)
+    L = np.stack([l00, z, z, l10, l11, z, l20, l21, l22], -1)
+    return L, c0 & c1 & c2
+
+
+def _chol3_bumped(a, eps_rel, eps_abs):
+    a = a.copy()
+    for i, j in ((1, 3), (2, 6), (5, 7)):
+        m = _spd_mid(a[..., i], a[..., j], a.dtype)
+        a[..., i] = m
+        a[..., j] = m
+    L1, s1 = _chol3(a)
+    tr = np.abs(a[..., 0]) + np.abs(a[..., 4]) + np.abs(a[..., 8])
+    g = np.stack([a[..., 0] - (np.abs(a[..., 1]) + np.abs(a[..., 2])),
+                  a[..., 4] - (np.abs(a[..., 3]) + np.abs(a[..., 5])),
+                  a[..., 8] - (np.abs(a[..., 6]) + np.abs(a[..., 7]))], -1).min(-1)
+    margin = np.maximum(eps_abs, eps_rel * tr)
+    tau = np.where(g > 0, margin, -g + margin)
+    b = a.copy()
+    for q in (0, 4, 8):
+        b[..., q] = a[..., q] + tau
+    L2, s2 = _chol3(b)
+    for q in (0, 4, 8):
+        b[..., q] = b[..., q] + 10.0 * margin
+    L3, s3 = _chol3(b)
+    L = np.where(s1[..., None], L1, np.where(s2[..., None], L2, L3))
+    return L, s1 | s2 | s3
+
+
+def _chol_solve3(L, b):
+    y0 = b[..., 0] / L[..., 0]
+    y1 = (b[..., 1] - L[..., 3] * y0) / L[..., 4]
+    y2 = (b[..., 2] - L[..., 6] * y0 - L[..., 7] * y1) / L[..., 8]
+    x2 = y2 / L[..., 8]
+    x1 = (y1 - L[..., 7] * x2) / L[..., 4]
+    x0 = (y0 - L[..., 3] * x1 - L[..., 6] * x2) / L[..., 0]
+    return np.stack([x0, x1, x2], -1)
+
+
+def block3_spd_solve(lower, main, upper, rhs):
+    """(x, info) of the SPD block Thomas with symmetrisation and diagonal shifts."""
+    dt = np.asarray(rhs).dtype
+    eps_rel, eps_abs = (1e-12, 1e-30) if dt == np.float64 else (1e-6, 1e-18)
+    lower, upper, rhs = (np.asarray(t, dtype=dt) for t in (lower, upper, rhs))
+    M = np.asarray(main, dtype=dt).reshape(rhs.shape[0], rhs.shape[1], 9)
+    B, K = rhs.shape[:2]
+    Ls, info, d = [], np.zeros((B, K), np.int32), [rhs[:, 0].copy()]
+    L, ok = _chol3_bumped(M[:, 0], eps_rel, eps_abs)
+    info[:, 0] = ~ok
+    Ls.append(L)
+    for k in range(1, K):
+        u, lo = upper[:, k - 1], lower[:, k - 1]
+        cols = [_chol_solve3(L, np.stack([u[:, 0] * (j == 0), u[:, 1] * (j == 1),
+                                          u[:, 2] * (j == 2)], -1).astype(dt)) for j in range(3)]
+        a = M[:, k].copy()
+        for r in range(3):
+            for c in range(3):
+                a[:, r * 3 + c] = M[:, k, r * 3 + c] - lo[:, r] * cols[c][:, r]
+        t = _chol_solve3(L, d[-1])
+        d.append(rhs[:, k] - lo * t)
+        L, ok = _chol3_bumped(a, eps_rel, eps_abs)
+        info[:, k] = ~ok
+        Ls.append(L)
+    x = np.empty_like(rhs)
+    xn = _chol_solve3(Ls[-1], d[-1])
+    x[:, -1] = xn
+    for k in range(K - 2, -1, -1):
+        xn = _chol_solve3(Ls[k], d[k] - upper[:, k] * xn)
+        x[:, k] = xn
+    return x, info
