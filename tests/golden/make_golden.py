@@ -471,6 +471,25 @@ def delay(dtype, tag):
                r_payload=pay.detach().numpy(), r_final=queue.detach().numpy(),
                r_dw=wt.grad.numpy(), r_dgates=gt.grad.numpy(), r_ddelays=dlt.grad.numpy(),
                r_dqueue0=qt.grad.numpy())
+    # the inputs of the reference's own transition tests
+    # (tests/networks/test_pure_delay_interpolation.py:24-47): collisions, a
+    # wrap past the ring's end, sub-step delays clamped to one step
+    for taps in (2, 3):
+        qt = (torch.arange(18).reshape(3, 6).t() / 10).to(dtype).contiguous().requires_grad_()
+        wt = tt_ = torch.tensor([0.5, 1.0, -2.0, 3.0, 0.0], dtype=dtype, requires_grad=True)
+        gt = torch.tensor([-0.2, 0.4, 0.5, 1.0, 2.0], dtype=dtype, requires_grad=True)
+        dlt = torch.tensor([0.02, 0.1, 0.23, 0.2, 0.6], dtype=dtype, requires_grad=True)
+        tr = dense_interpolated_delay_transition(
+            qt, L([4]), L([17]), wt, gt, dlt, torch.tensor(0.1, dtype=dtype),
+            post_idx=L([1, 1, 2, 0, 1]), depth=6, width=3, taps=taps, sigma=0.5)
+        cq = torch.as_tensor(rng.standard_normal((6, 3))).to(dtype)
+        (tr.queue * cq).sum().backward()
+        out.update({f"pure{taps}_queue": tr.queue.detach().numpy(), f"pure{taps}_cot": cq.numpy(),
+                    f"pure{taps}_dq": qt.grad.numpy(), f"pure{taps}_dw": wt.grad.numpy(),
+                    f"pure{taps}_dg": gt.grad.numpy(), f"pure{taps}_dd": dlt.grad.numpy(),
+                    f"pure{taps}_slot": int(tr.slot.item()), f"pure{taps}_step": int(
+                        tr.global_step.item())})
+        del tt_
     np.savez_compressed(os.path.join(HERE, f"delay_{tag}.npz"), **out)
     print("delay", tag)
 

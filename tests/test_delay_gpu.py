@@ -270,3 +270,52 @@ def test_device_slot_outside_the_ring_is_reported(cuda):
         delays.ordered_two_tap_enqueue_(q, 5, v, v, v, a, a)
     with pytest.raises(RuntimeError, match="address is outside the delivery ring"):
         delays.ordered_two_tap_enqueue_(q, 0, v, v, v, a, a + 100)
+
+
+@pytest.mark.parametrize("taps", [2, 3])
+@pytest.mark.parametrize("tag,npt,tdt", TAGS)
+def test_reference_transition_cases(cuda, golden, tag, npt, tdt, taps):
+    """The inputs of the reference's own transition tests (collisions, a wrap
+    past the ring's end, sub-step delays clamped to one step): queue, slot,
+    step and every gradient as the reference computes them."""
+    z = golden(f"delay_{tag}.npz")
+    q = (torch.arange(18).reshape(3, 6).t() / 10).to(tdt).contiguous().to(cuda).requires_grad_()
+    w = torch.tensor([0.5, 1.0, -2.0, 3.0, 0.0], dtype=tdt, device=cuda, requires_grad=True)
+    g = torch.tensor([-0.2, 0.4, 0.5, 1.0, 2.0], dtype=tdt, device=cuda, requires_grad=True)
+    d = torch.tensor([0.02, 0.1, 0.23, 0.2, 0.6], dtype=tdt, device=cuda, requires_grad=True)
+    L = lambda v: torch.tensor(v, dtype=torch.int64, device=cuda)  # noqa: E731
+    tr = delays.dense_interpolated_delay_transition(
+        q, L([4]), L([17]), w, g, d, torch.tensor(0.1, dtype=tdt, device=cuda),
+        post_idx=L([1, 1, 2, 0, 1]), depth=6, width=3, taps=taps, sigma=0.5)
+    # two taps: bit for bit.  Three taps: the Gaussian weights come from
+    # torch's softmax on the device, whose exponential rounds differently from
+    # the CPU's by an ulp (with the same weights the kernel is bit-exact:
+    # test_three_tap_transition_and_gradients_match_reference)
+    exact = taps == 2
+    ulp = dict(rtol=4e-16, atol=4e-16) if tag == "f64" else dict(rtol=3e-7, atol=3e-7)
+    check = (np.testing.assert_array_equal if exact else
+             (lambda a, b: np.testing.assert_allclose(a, b, **ulp)))
+    check(tr.queue.detach().cpu().numpy(), z[f"pure{taps}_queue"])
+    assert int(tr.slot.item()) == z[f"pure{taps}_slot"]
+    assert int(tr.global_step.item()) == z[f"pure{taps}_step"]
+    (tr.queue * _t(z[f"pure{taps}_cot"], cuda, tdt)).sum().backward()
+    np.testing.assert_array_equal(q.grad.cpu().numpy(), z[f"pure{taps}_dq"])
+    check(w.grad.cpu().numpy(), z[f"pure{taps}_dw"])
+    check(g.grad.cpu().numpy(), z[f"pure{taps}_dg"])
+    tol = 1e-12 if tag == "f64" else 1e-5
+    np.testing.assert_allclose(d.grad.cpu().numpy(), z[f"pure{taps}_dd"], rtol=tol, atol=tol)
+    assert d.grad[0].item() == 0  # a sub-step delay is clamped to one step
+
+
+@pytest.mark.parametrize("taps", [2, 3])
+def test_empty_connections_clear_the_due_row(cuda, taps):
+    """The reference's empty-transition case: no connections, depth 1."""
+    queue = torch.tensor([[1.0, 2.0]], dtype=torch.float64, device=cuda)
+    empty = torch.empty(0, dtype=torch.float64, device=cuda)
+    slot = torch.zeros(1, dtype=torch.int64, device=cuda)
+    tr = delays.dense_interpolated_delay_transition(
+        queue, slot, slot, empty, empty, empty, torch.tensor(0.1, device=cuda),
+        post_idx=torch.empty(0, dtype=torch.int64, device=cuda), depth=1, width=2, taps=taps,
+        sigma=0.5)
+    torch.testing.assert_close(tr.queue, torch.zeros_like(queue), rtol=0, atol=0)
+    assert int(tr.slot.item()) == 0 and int(tr.global_step.item()) == 1
