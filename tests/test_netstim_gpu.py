@@ -73,3 +73,13 @@ def test_background_rate(cuda):
     total = int(spikes.sum())
     # first clock E*200 ms plus renewals: expected count 4096 * (1 - e^-1) + ... ~ 4096
     assert 3600 < total < 4600
+
+
+def test_deterministic_initialisation_keeps_start_for_nonfinite_intervals(cuda):
+    """Without noise the first clock is start itself (the reference's
+    netstim_initial_state: no inf * 0, a negative zero stays negative)."""
+    ns = NetStim(2, interval=[float("inf"), float("nan")], noise=0.0, start=[-0.0, 2.0],
+                 dtype=torch.float64, device=cuda)
+    clock = ns.next_stoch_time.cpu()
+    assert clock[1].item() == 2.0 and clock[0].item() == 0.0
+    assert torch.signbit(clock[0])
