@@ -98,37 +98,72 @@ def _solve_transpose(a, b, c, g):
     return y
 
 
-class _TridiagSolve(torch.autograd.Function):
-    @staticmethod
-    def forward(ctx, a, b, c, d, method):
-        x = _solve(a, b, c, d, method)
-        ctx.save_for_backward(a, b, c, x)
-        return x
+# The solve as a torch.library operator, like the reference's
+# (t_kernel_thomas.py:192-215): a fake (shape) rule for torch.compile, the
+# transpose-solve adjoint as its autograd rule, and a vmap rule that folds
+# mapped dimensions into the system batch.
+@torch.library.custom_op("dendra_gb300::tridiag_solve", mutates_args=())
+def tridiag_solve_op(a: torch.Tensor, b: torch.Tensor, c: torch.Tensor, d: torch.Tensor,
+                     method: int, transpose: bool) -> torch.Tensor:
+    """x with A x = d (transpose: A^T x = d); A has sub-diagonal a, diagonal b,
+    super-diagonal c."""
+    if transpose:
+        return _solve_transpose(a, b, c, d)
+    return _solve(a, b, c, d, method)
 
-    @staticmethod
-    def backward(ctx, grad_x):
-        a, b, c, x = ctx.saved_tensors
-        need = ctx.needs_input_grad
-        if not any(need[:4]):
-            return None, None, None, None, None
-        y = _solve_transpose(a, b, c, grad_x)
-        grad_a = -y[:, 1:] * x[:, :-1] if need[0] else None
-        grad_b = -y * x if need[1] else None
-        grad_c = -y[:, :-1] * x[:, 1:] if need[2] else None
-        grad_d = y if need[3] else None
-        return grad_a, grad_b, grad_c, grad_d, None
+
+@tridiag_solve_op.register_fake
+def _(a, b, c, d, method, transpose):
+    return d.new_empty(d.shape)
+
+
+def _tridiag_setup(ctx, inputs, output):
+    a, b, c, _, method, transpose = inputs
+    ctx.save_for_backward(a, b, c, output)
+    ctx.method, ctx.transpose = method, transpose
+
+
+def _tridiag_backward(ctx, grad_x):
+    # ThomasSolve.backward (t_kernel_thomas.py:147-189): one solve with the
+    # transposed matrix, then outer products along the three diagonals
+    a, b, c, x = ctx.saved_tensors
+    need = ctx.needs_input_grad
+    if not any(need[:4]):
+        return None, None, None, None, None, None
+    y = tridiag_solve_op(a, b, c, grad_x.contiguous(), ctx.method, not ctx.transpose)
+    lower = -y[:, 1:] * x[:, :-1]   # cotangent of the sub-diagonal actually used
+    upper = -y[:, :-1] * x[:, 1:]
+    grad_a, grad_c = (upper, lower) if ctx.transpose else (lower, upper)
+    return (grad_a if need[0] else None, -y * x if need[1] else None,
+            grad_c if need[2] else None, y if need[3] else None, None, None)
+
+
+tridiag_solve_op.register_autograd(_tridiag_backward, setup_context=_tridiag_setup)
+
+
+@tridiag_solve_op.register_vmap
+def _(info, in_dims, a, b, c, d, method, transpose):
+    V = info.batch_size
+
+    def fold(t, dim):
+        t = t.movedim(dim, 0) if dim is not None else t.unsqueeze(0).expand(V, *t.shape)
+        return t.reshape(V * t.shape[1], *t.shape[2:]).contiguous()
+
+    a, b, c, d = (fold(t, dim) for t, dim in zip((a, b, c, d), in_dims[:4]))
+    x = tridiag_solve_op(a, b, c, d, method, transpose)
+    return x.reshape(V, -1, x.shape[-1]), 0
 
 
 def thomas_solve_cuda_t(a, b, c, d):
     """Batched tridiagonal solve (drop-in for the reference's Triton Thomas)."""
     validate_tridiagonal(a, b, c, d)
-    return _TridiagSolve.apply(a, b, c, d, _lib.THOMAS)
+    return tridiag_solve_op(a, b, c, d, _lib.THOMAS, False)
 
 
 def pcr_solve_cuda_t(a, b, c, d):
     """Batched tridiagonal solve (drop-in for the reference's Triton PCR)."""
     validate_tridiagonal(a, b, c, d)
-    return _TridiagSolve.apply(a, b, c, d, _lib.PCR)
+    return tridiag_solve_op(a, b, c, d, _lib.PCR, False)
 
 
 def tridiag_solve_lanes(a, b, c, d, lanes: int):
