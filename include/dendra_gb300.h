@@ -28,6 +28,9 @@
  *   dgb_dhs_solve             dhs_solve_cuda, triton/dhs_kernel.py:634-651
  *   dgb_dhs_solve_forest      dhs_solve_multi_cuda, triton/dhs_kernel_multi.py:831-888
  *   dgb_dhs_block3_solve      dhs_bt_solve_cuda, triton/dhs_kernel_bt.py:465-479
+ *   dgb_tree_contract_solve   tree_contraction.solve, triton/tree_contraction.py:748-768
+ *                             (plan: dendra_solvers.TreeContractionPlan,
+ *                             integrators/tree.py:841-867)
  *   dgb_detect_spikes         threshold_transition, networks/spiking.py:43-73
  *   dgb_pack_source_spikes    pack_source_spikes, networks/netcon_bitpack_kernel.cpp:145-149
  *   dgb_build_delivery        build_delivery, networks/netcon_bitpack_kernel.cpp:145-149
@@ -780,6 +783,51 @@ int dgb_netstim_run(int dtype, int64_t n, int64_t n_steps, int64_t step0, double
                     const void* interval, const void* noise, const int64_t* number,
                     uint64_t seed, const void* draws, void* next_time, int64_t* counts,
                     uint8_t* spikes, uint64_t* bits, int64_t n_words, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Tree contraction (conductance form).  Plan tables are int32 device arrays,
+ * fields stored row after row ([field][count]), as built by
+ * dendra_gb300/contraction.py (build_contraction_tables):
+ *   seg        [4][n_segments]   ancestor node, child node, interior start/end
+ *   interior   [n_interior]      node ids, each segment top to bottom
+ *   retained   [4][n_retained]   node, incoming segment (-1), endpoint start, count
+ *   endpoint   [2][n_endpoints]  segment, side (0 ancestor end, 1 child end)
+ *   round_ptr  [2][n_rounds+1]   update offsets, recovery offsets
+ *   update     [3][n_updates]    source state slot, incidence start, count
+ *   incidence  [4][n_incidence]  removed state slot, near edge, far edge (-1),
+ *                                bridge slot written (-1)
+ *   recovery   [6][n_eliminated] retained index, state slot, ancestor, child (-1),
+ *                                near edge, far edge (-1)
+ *   roots      [2][n_roots]      retained index, final state slot
+ * Every slot index must lie inside its table (the builder checks this).
+ * ------------------------------------------------------------------------- */
+typedef struct dgb_contract_plan {
+  int32_t size, n_segments, n_interior, n_retained;
+  int32_t n_endpoints, n_rounds, n_updates, n_incidence;
+  int32_t n_eliminated, n_roots, n_bridges, reserved;
+  const int32_t* seg;
+  const int32_t* interior;
+  const int32_t* retained;
+  const int32_t* endpoint;
+  const int32_t* round_ptr;
+  const int32_t* update;
+  const int32_t* incidence;
+  const int32_t* recovery;
+  const int32_t* roots;
+} dgb_contract_plan;
+
+/* B scalar Hines systems of plan->size nodes sharing the plan's topology:
+ * d (shunt), g (conductance to the parent; a root's g is a second shunt), rhs
+ * and x are (B, K) row-major:  d_i x_i + g_i (x_i - x_p(i)) + sum_c g_c (x_i - x_c)
+ * = rhs_i.  One warp per row, scratch in shared memory (errors DGB_ERANGE
+ * when a row's scratch exceeds it); correctly rounded operations only.  x
+ * must not alias an input.  Replaces tree_contraction.solve
+ * (triton/tree_contraction.py:748-768; kernels :14-480). */
+int dgb_tree_contract_solve(int dtype, int64_t B, const dgb_contract_plan* plan, const void* d,
+                            const void* g, const void* rhs, void* x, void* stream);
+
+/* sizeof(dgb_contract_plan), for bindings that mirror the struct. */
+size_t dgb_contract_plan_size(void);
 
 /* First device-side index error of the delay kernels since the last call
    (0 = none, else DGB_DELAY_ERR_*), cleared on read; synchronises stream. */

@@ -21,7 +21,10 @@ Layers:
     multi-step rollouts: the reference's ordered CPU op, sequential adds), and
     the NetStim renewal with counter-based draws (Philox4x32-10, a series
     logarithm in rounded operations).
-  * ``core.py``  ctypes bindings; builds the C library with gcc on first use.
+  * ``core.py``  ctypes bindings; builds the C library with gcc on first use;
+    numpy restatements of the 3x3 block tree and SPD solves and of the tree
+    contraction solve (``tree_contract_solve``: the reference kernel's
+    operation order on a given plan).
   The integer/index event primitives (delay rounding, bit packing, sequential
   delivery) are restated inline in ``tests/test_netcon.py``, next to the
   reference known answers they are checked against.
@@ -56,4 +59,6 @@ from .core import (  # noqa: F401
     dhs_block3_matrix,
     dhs_block3_solve,
     block3_spd_solve,
+    tree_contract_solve,
+    hines_matrix,
 )

@@ -628,3 +628,126 @@ def block3_spd_solve(lower, main, upper, rhs):
         xn = _chol_solve3(Ls[k], d[k] - upper[:, k] * xn)
         x[:, k] = xn
     return x, info
+
+
+def _schur(left, right, pivot):
+    """small * (large / pivot) of the pair, by magnitude (the conductance-form
+    Schur product of models/integrators/triton/tree_contraction.py:22-30)."""
+    left_small = np.abs(left) < np.abs(right)
+    small = np.where(left_small, left, right)
+    large = np.where(left_small, right, left)
+    return small * (large / pivot)
+
+
+def tree_contract_solve(d, g, rhs, tables):
+    """Tree-contraction solve of (B, K) Hines systems, numpy restatement.
+
+    Follows models/integrators/triton/tree_contraction.py: segment
+    condensation (_condense_segment_tile :237-287), endpoint gather
+    (_gather_segment_tile :290-328), rounds of updates (_update :33-74,
+    _solve_contracted_tree :110-178), recovery (_recover :77-107,
+    _recover_segment_tile :331-361), on the plan tables of
+    ``dendra_gb300.contraction.build_contraction_tables`` (the reference's
+    plan comes from the dendra-solvers package, absent here).  Every
+    operation is a single correctly rounded numpy operation in the input
+    dtype, in the kernel's order.
+    """
+    d, g, rhs = (np.asarray(a) for a in (d, g, rhs))
+    dt = d.dtype
+    B, K = d.shape
+    T = {k: np.asarray(v, dtype=np.int64) for k, v in tables.items()}
+    seg, interior, retained = T["seg"], T["interior"], T["retained"]
+    S, R = seg.shape[1], retained.shape[1]
+    zero = np.zeros(B, dtype=dt)
+    out = np.zeros((B, K), dtype=dt)
+    saved = np.zeros((B, max(1, interior.size)), dtype=dt)
+    pivots = np.ones_like(saved)
+    bridges = np.zeros_like(saved)
+    summ = np.zeros((5, B, max(1, S)), dtype=dt)
+    for s in range(S):
+        child, a0, a1 = seg[1, s], seg[2, s], seg[3, s]
+        near = g[:, interior[a0]]
+        left_d, left_r, carry_d, carry_r = zero, zero, zero, zero
+        for pos in range(a0, a1):
+            node = interior[pos]
+            succ = interior[pos + 1] if pos + 1 < a1 else child
+            far = g[:, succ]
+            shunt = d[:, node] + carry_d
+            value = rhs[:, node] + carry_r
+            pivot = shunt + (near + far)
+            saved[:, pos], pivots[:, pos], bridges[:, pos] = value, pivot, near
+            left_d = left_d + _schur(near, shunt, pivot)
+            left_r = left_r + (near / pivot) * value
+            carry_d = _schur(far, shunt, pivot)
+            carry_r = (far / pivot) * value
+            near = _schur(near, far, pivot)
+        summ[:, :, s] = (left_d, left_r, carry_d, carry_r, near)
+    U = T["update"].shape[1]
+    n_br = (T["incidence"][3].max() + 1 - R) if T["incidence"].size else 0
+    st_s = np.zeros((B, R + U), dtype=dt)
+    st_r = np.zeros((B, R + U), dtype=dt)
+    edge = np.zeros((B, R + max(int(n_br), 0)), dtype=dt)
+    ep = T["endpoint"]
+    for r in range(R):
+        node, inc, e0, ne = retained[:, r]
+        diag, val = d[:, node], rhs[:, node]
+        for e in range(e0, e0 + ne):
+            s, side = ep[0, e], ep[1, e]
+            diag = diag + summ[2 * side, :, s]
+            val = val + summ[2 * side + 1, :, s]
+        st_s[:, r], st_r[:, r] = diag, val
+        edge[:, r] = summ[4, :, inc] if inc >= 0 else g[:, node]
+    rp, upd, inc = T["round_ptr"], T["update"], T["incidence"]
+    P = rp.shape[1] - 1
+    for p in range(P):
+        for u in range(rp[0, p], rp[0, p + 1]):
+            src, q0, nq = upd[:, u]
+            diag, val = st_s[:, src], st_r[:, src]
+            for q in range(q0, q0 + nq):
+                m, ns, fs, dest = inc[:, q]
+                shunt, value, near = st_s[:, m], st_r[:, m], edge[:, ns]
+                far = edge[:, fs] if fs >= 0 else zero
+                pivot = shunt + (near + far)
+                diag = diag + _schur(near, shunt, pivot)
+                val = val + (near / pivot) * value
+                if dest >= 0:
+                    edge[:, dest] = _schur(near, far, pivot)
+            st_s[:, R + u], st_r[:, R + u] = diag, val
+    xr = np.zeros((B, R), dtype=dt)
+    roots = T["roots"]
+    for k in range(roots.shape[1]):
+        r, st = roots[:, k]
+        xr[:, r] = st_r[:, st] / (st_s[:, st] + edge[:, r])
+    rec = T["recovery"]
+    for p in range(P - 1, -1, -1):
+        for e in range(rp[1, p], rp[1, p + 1]):
+            node, st, a, c, ns, fs = rec[:, e]
+            near = edge[:, ns]
+            far = edge[:, fs] if fs >= 0 else zero
+            xc = xr[:, c] if c >= 0 else zero
+            pivot = st_s[:, st] + (near + far)
+            xr[:, node] = ((st_r[:, st] + near * xr[:, a]) + far * xc) / pivot
+    out[:, retained[0]] = xr
+    for s in range(S):
+        anc, succ, a0, a1 = seg[:, s]
+        xa, xs = out[:, anc], out[:, succ]
+        for pos in range(a1 - 1, a0 - 1, -1):
+            node = interior[pos]
+            x = ((saved[:, pos] + bridges[:, pos] * xa) + g[:, succ] * xs) / pivots[:, pos]
+            out[:, node] = x
+            succ, xs = node, x
+    return out
+
+
+def hines_matrix(d, g, parent):
+    """Dense matrix of one scalar Hines system (conductance form: shunt d_i,
+    edge g_i to the parent, a root's g_i a second shunt)."""
+    K = len(parent)
+    A = np.diag(np.asarray(d, dtype=np.float64) + np.asarray(g, dtype=np.float64))
+    for i in range(K):
+        p = parent[i]
+        if p >= 0:
+            A[p, p] += g[i]
+            A[i, p] -= g[i]
+            A[p, i] -= g[i]
+    return A
