@@ -637,6 +637,132 @@ def bench_bt(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+TREE_BYTES_PER_NODE = 16  # float32: read d, g, rhs, write x
+
+
+def _tree_systems(B, seed, K=2000):
+    """B Hines systems on one random branched cell of ~K compartments (branch
+    lengths U[20,200] um, <= 12 branch levels): shunt cm/dt*area + g_pas*area,
+    axial conductances from Ra = 100 ohm cm, right-hand sides of a voltage
+    field; float32, (B, K) node order with the soma first."""
+    from dendra_gb300.network import axial_conductance, random_cell
+
+    rng = np.random.default_rng(seed)
+    cell = random_cell(rng, K)
+    K = cell.parent.size
+    area = np.pi * cell.diam * cell.length * 1e-8                   # cm^2
+    shunt = (1e-6 * 1.0 / (0.025 * 1e-3) + 1e-3) * area             # S
+    axial = axial_conductance(cell.parent, cell.length, cell.diam, 100.0)
+    axial[0] = 0.0
+    d = shunt[None, :] * rng.uniform(0.9, 1.1, (B, K))
+    g = np.broadcast_to(axial, (B, K)).copy()
+    v = rng.uniform(-70.0, -50.0, (B, K))
+    rhs = d * v
+    return cell.parent, [np.ascontiguousarray(a, dtype=np.float32) for a in (d, g, rhs)]
+
+
+def bench_tree(args, world, rank, local):
+    """Tree solves of branched cells: B = 8192 systems sharing one ~2000-node
+    topology (the C3 cell morphology), float32; one bench step = one batched
+    tree-contraction solve (segments of <= 16 interior nodes, rake/compress
+    rounds).  The DHS depth-layer solve of the same systems is timed beside
+    it.  Inputs exceed L2 (262 MB)."""
+    import torch
+
+    import oracle
+    from dendra_gb300.contraction import TreeContractionPlan, solve
+    from dendra_gb300.tree import build_dhs_layers, build_morphology, dhs_solve_cuda
+
+    B = args.cables if args.cables != 16384 else 8192
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    parent, host = _tree_systems(B, 13 + rank)
+    K = parent.size
+    units = B * K
+    metric = "node-solves/s"
+    plan = TreeContractionPlan(parent, 16)
+    d, g, rhs = (torch.as_tensor(t).to(dev) for t in host)
+    _, _, depth = build_morphology([int(p) for p in parent])
+    order, layer_ptr = build_dhs_layers(depth, 32)
+    topo = (torch.as_tensor(parent).to(dev), order.to(dev), layer_ptr.to(dev))
+    for _ in range(max(3, args.warmup)):
+        solve(d, g, rhs, plan)
+        dhs_solve_cuda(d, g, rhs, *topo)
+    torch.cuda.synchronize()
+    flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        out, times = None, []
+        for _ in range(args.steps):
+            flush.sum()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            out = fn()
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return out, float(np.mean(times))
+
+    with ClockSampler(local) as clocks:
+        x, ms = timed(lambda: solve(d, g, rhs, plan))
+        x_dhs, ms_dhs = timed(lambda: dhs_solve_cuda(d, g, rhs, *topo))
+    pinned = [torch.as_tensor(t).pin_memory() for t in host]
+    out = torch.empty(B, K, dtype=torch.float32).pin_memory()
+    h2d = sum(t.numel() * 4 for t in pinned)
+    d2h = out.numel() * 4
+    dbuf = [torch.empty_like(t, device=dev) for t in pinned]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for d_, h_ in zip(dbuf, pinned):
+            d_.copy_(h_, non_blocking=True)
+        out.copy_(solve(*dbuf, plan), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    peak, peak_kind = _peaks()
+    achieved = TREE_BYTES_PER_NODE * units / (ms * 1e-3) / 1e9
+    n_cpu = min(1024, B)
+    t0 = time.perf_counter()
+    ref = oracle.dhs_solve(*(t[:n_cpu] for t in host), parent, order.numpy(), layer_ptr.numpy())
+    cpu_s = time.perf_counter() - t0
+    xs = x[:n_cpu].cpu().numpy()
+    rel = float(np.abs(xs - ref).max() / np.abs(ref).max())
+    exact = oracle.tree_contract_solve(*(t[:4] for t in host), plan.tables)
+    c = plan.counts
+    line = {
+        "metric": metric, "value": units / (ms * 1e-3), "unit": metric, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "tree-contraction-solve", "systems": B, "K": K,
+                   "segment_cap": 16, "segments": c["n_segments"], "retained": c["n_retained"],
+                   "rounds": c["n_rounds"], "l2": "flushed between timed steps"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel": "tree_contract_kernel",
+                     "note": f"{TREE_BYTES_PER_NODE} algorithmic B per float32 node (read d, "
+                             "g, rhs, write x); one warp per system, scratch in shared "
+                             f"memory; peak {peak_kind}"},
+        "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps,
+        "clocks": clocks.summary(),
+        "dhs_same_systems": {"ms_per_step": ms_dhs, "value": units / (ms_dhs * 1e-3),
+                             "kernel": "dhs_forest_kernel (depth layers)"},
+        "max_rel_diff_vs_cpu_dhs_f32": rel,
+        "bit_exact_vs_oracle_rows_0_3": bool(np.array_equal(x[:4].cpu().numpy(), exact)),
+        "agrees_with_gpu_dhs_rel": float((x - x_dhs).abs().max() / x_dhs.abs().max()),
+        "cpu_baseline": {"value": n_cpu * K / cpu_s, "unit": metric,
+                         "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"{n_cpu} systems x {K} nodes, float32 sequential DHS "
+                                   "(C restatement; the reference's CPU tree solvers live in "
+                                   "the absent dendra-solvers package)"},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def _delay_bytes(n_edges, width, n_src, depth, steps, elem=4):
     """Algorithmic bytes of the direct rollout's forward launch and of its
     reverse launch (sweep + per-source sum), one edge per column, an empty
@@ -1044,12 +1170,13 @@ def main():
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c3", "c4", "c5", "bt", "delay"],
+                    choices=["c2", "c3", "c4", "c5", "bt", "delay", "tree"],
                     help="c2: uneven cable population (default); c3: branched-cell network; "
                          "c4: adjoint gradient of a trace fit; "
                          "c5: learned threshold proposal vs plain bisection; "
                          "bt: 3x3 block-tridiagonal (multi-layer extracellular) solves; "
-                         "delay: differentiable two-tap event transport rollout")
+                         "delay: differentiable two-tap event transport rollout; "
+                         "tree: tree-contraction solves of branched cells")
     ap.add_argument("--train", type=int, default=200000, help="c5 training thresholds")
     ap.add_argument("--cables", type=int, default=16384,
                     help="cables per rank (a smaller case for profiling)")
@@ -1066,6 +1193,8 @@ def main():
         return bench_c5(args, world, rank, local)
     if args.workload == "delay":
         return bench_delay(args, world, rank, local)
+    if args.workload == "tree":
+        return bench_tree(args, world, rank, local)
     if args.impl == "reference":
         return run_reference(args, world, rank)
 

@@ -28,7 +28,7 @@ The plan (host, once per topology):
 1. **Segments** (``max_segment_interior_nodes = cap``): maximal runs of
    non-root nodes with exactly one child, cut into pieces of at most ``cap``
    interior nodes (a retained node separates pieces).  Each piece is condensed
-   by one lane, top to bottom, into summaries for its two retained endpoints
+   by one thread, top to bottom, into summaries for its two retained endpoints
    and a bridge between them (tree_contraction.py:237-287).  ``cap = None``
    skips this step.
 2. **Skeleton contraction**: the retained nodes form a smaller tree that is
@@ -38,14 +38,14 @@ The plan (host, once per topology):
    takes O(log R) rounds for a balanced shape.  Every surviving neighbour
    gathers the contributions of its removed neighbours in ascending order
    (deterministic, no atomics); results go to fresh state and edge slots, so a
-   round never overwrites what another lane of the same round reads.
+   round never overwrites what another thread of the same round reads.
 3. The roots solve ``x = value / (shunt + g_root)``; the rounds are undone in
    reverse (``x = (value + near x_a + far x_c) / pivot``) and finally every
    segment is recovered bottom to top.
 
-The kernel runs one warp per batch row with all scratch in shared memory and
-uses correctly rounded operations only, so the oracle's numpy restatement of
-the same plan reproduces it bit for bit.
+The kernel runs one block (32-256 threads) per batch row with all scratch in
+shared memory and uses correctly rounded operations only, so the oracle's
+numpy restatement of the same plan reproduces it bit for bit.
 """
 
 from __future__ import annotations
@@ -70,7 +70,7 @@ class DgbContractPlan(ctypes.Structure):
         ("size", _I32), ("n_segments", _I32), ("n_interior", _I32), ("n_retained", _I32),
         ("n_endpoints", _I32), ("n_rounds", _I32), ("n_updates", _I32),
         ("n_incidence", _I32), ("n_eliminated", _I32), ("n_roots", _I32),
-        ("n_bridges", _I32), ("reserved", _I32),
+        ("n_bridges", _I32), ("threads", _I32),
         ("seg", _P), ("interior", _P), ("retained", _P), ("endpoint", _P),
         ("round_ptr", _P), ("update", _P), ("incidence", _P), ("recovery", _P),
         ("roots", _P),
@@ -142,7 +142,7 @@ def build_contraction_tables(parent, cap=16):
     ``parent[i]`` is node i's parent or -1 for a root (any node order; several
     roots make a forest).  Table layout (every row a field):
 
-    * ``seg`` (4, S): ancestor node, child node, interior start, interior end
+    * ``seg`` (4, S): ancestor and child (retained indices), interior start, end
     * ``interior`` (I,): node ids, each segment's run top to bottom
     * ``retained`` (4, R): node, incoming segment (-1), endpoint start, count
     * ``endpoint`` (2, E): segment, side (0 the ancestor end, 1 the child end)
@@ -193,6 +193,8 @@ def build_contraction_tables(parent, cap=16):
                     pos = len(run)
         for _, _, piece in segs:
             is_interior[piece] = True
+    # longest first: threads take segments in turn, so this balances them
+    segs.sort(key=lambda sg: -len(sg[2]))
     S = len(segs)
     interior = [n for _, _, piece in segs for n in piece]
     seg = np.zeros((4, S), dtype=np.int64)
@@ -219,6 +221,8 @@ def build_contraction_tables(parent, cap=16):
         retained[:, r] = (ret_nodes[r], incoming[r], len(endpoint), len(e))
         endpoint.extend(e)
     endpoint = np.asarray(endpoint, dtype=np.int64).reshape(-1, 2).T
+    if S:
+        seg[:2] = local[seg[:2]]  # endpoints as retained indices
     lpar = np.full(R, -1, dtype=np.int64)
     for r in range(R):
         node = ret_nodes[r]
@@ -324,7 +328,7 @@ def _check_tables(t, c):
             raise RuntimeError(f"contraction plan: {what} out of range")
 
     seg, ret, upd, inc, rec = t["seg"], t["retained"], t["update"], t["incidence"], t["recovery"]
-    within(seg[:2], 0, K, "segment endpoint")
+    within(seg[:2], 0, R, "segment endpoint")
     within(seg[2:], 0, I + 1, "segment interior range")
     if S and ((seg[2] >= seg[3]).any()):
         raise RuntimeError("contraction plan: empty segment")
@@ -367,8 +371,11 @@ class TreeContractionPlan:
     ``dn.tree_contraction``); None contracts every node in rounds.
     """
 
-    def __init__(self, parent, max_segment_interior_nodes=16):
+    def __init__(self, parent, max_segment_interior_nodes=16, threads=0):
         self.max_segment_interior_nodes = _validate_cap(max_segment_interior_nodes)
+        if threads not in (0, 32, 64, 128, 256):
+            raise ValueError("threads must be 0 (automatic), 32, 64, 128 or 256")
+        self.threads = int(threads)
         self.tables, self.counts = build_contraction_tables(
             parent, self.max_segment_interior_nodes)
         self.size = self.counts["size"]
@@ -403,6 +410,7 @@ class TreeContractionPlan:
         s = DgbContractPlan()
         for k, v in self.counts.items():
             setattr(s, k, v)
+        s.threads = self.threads
         base = packed.data_ptr()
         for k in _TABLES:
             setattr(s, k, base + 4 * offsets[k])
@@ -411,8 +419,8 @@ class TreeContractionPlan:
     def smem_values(self):
         """Scratch values per batch row the kernel keeps in shared memory."""
         c = self.counts
-        return (3 * c["n_interior"] + 5 * c["n_segments"] + 2 * (c["n_retained"] + c["n_updates"])
-                + 2 * c["n_retained"] + c["n_bridges"])
+        return (3 * c["size"] + c["n_interior"] + 5 * c["n_segments"]
+                + 2 * (c["n_retained"] + c["n_updates"]) + 2 * c["n_retained"] + c["n_bridges"])
 
 
 def prepare(plan, device):

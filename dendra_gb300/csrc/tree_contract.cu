@@ -3,20 +3,24 @@
 // :14-480, solve :748-768) on a plan of dendra_gb300/contraction.py.
 //
 // Scalar Hines systems in conductance form: shunt d_i, conductance g_i to the
-// parent (a root's g a second shunt).  One warp per batch row; every scratch
-// value of the row lives in shared memory:
-//   saved/pivot/bridge  [3][n_interior]  segment elimination, for recovery
+// parent (a root's g a second shunt).  One block (32-256 threads) per batch
+// row; the row and every scratch value live in shared memory:
+//   d, g, rhs           [3][K]           the row, loaded coalesced; an
+//                                        interior node's pivot and reduced
+//                                        value overwrite its d and rhs when
+//                                        it is eliminated, and x overwrites
+//                                        rhs when it is recovered
+//   bridge              [n_interior]     segment elimination, for recovery
 //   summary             [5][n_segments]  ancestor shunt/value, child
 //                                        shunt/value, bridge
 //   shunt/value         [2][R + U]       state slots (SSA: update u writes R+u)
 //   edge                [R + n_bridges]  edge slots
-//   xr                  [R]              solution of the retained nodes
-// Phases, separated by __syncwarp: condense segments (lane per segment, top
-// to bottom), gather the retained nodes' reduced state, contraction rounds
-// (lane per update; each update pulls its removed neighbours in plan order),
-// root solves, recovery rounds in reverse, retained x to HBM, segment
-// recovery (lane per segment, bottom to top; reads the endpoints' x back from
-// HBM, written by this warp before the barrier).
+//   xr                  [R]              x of the retained nodes
+// Phases, separated by block barriers: load the row, condense
+// segments (thread per segment, top to bottom), gather the retained nodes'
+// reduced state, contraction rounds (thread per update; each update pulls its
+// removed neighbours in plan order), root solves, recovery rounds in reverse,
+// segment recovery (thread per segment, bottom to top), store x coalesced.
 // Only correctly rounded single operations (no contraction into FMA), so the
 // numpy restatement of the same plan reproduces every bit.
 #include "common.cuh"
@@ -28,13 +32,12 @@ __device__ __forceinline__ double tc_add(double a, double b) { return __dadd_rn(
 __device__ __forceinline__ float tc_div(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ double tc_div(double a, double b) { return __ddiv_rn(a, b); }
 
-// small * (large / pivot) of the pair, ordered by magnitude
+// small * (large / pivot) of the pair (a, b), ordered by magnitude, given
+// the rounded quotients qa = a / pivot and qb = b / pivot: the same value as
+// dividing the larger factor inside the product.
 template <typename T>
-__device__ __forceinline__ T schur(T left, T right, T pivot) {
-  const bool left_small = fabs(left) < fabs(right);
-  const T small = left_small ? left : right;
-  const T large = left_small ? right : left;
-  return mul_rn(small, tc_div(large, pivot));
+__device__ __forceinline__ T schur_q(T a, T qa, T b, T qb) {
+  return fabs(a) < fabs(b) ? mul_rn(a, qb) : mul_rn(b, qa);
 }
 
 struct TcCounts {
@@ -42,24 +45,26 @@ struct TcCounts {
 };
 
 static __host__ __device__ __forceinline__ int64_t tc_row_values(const TcCounts& c) {
-  return 3ll * c.I + 5ll * c.S + 2ll * (c.R + c.U) + 2ll * c.R + c.NB;
+  return 3ll * c.K + c.I + 5ll * c.S + 2ll * (c.R + c.U) + 2ll * c.R + c.NB;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(128)
+// One CTA of TPR threads per batch row (grid-stride over rows); phases are
+// separated by __syncthreads.
+template <typename T, int TPR>
+__global__ void __launch_bounds__(TPR)
     tree_contract_kernel(dgb_contract_plan p, TcCounts c, int64_t B, const T* __restrict__ d,
                          const T* __restrict__ g, const T* __restrict__ rhs, T* __restrict__ x) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int wpb = blockDim.x >> 5;
-  T* saved = reinterpret_cast<T*>(smem_raw) + (size_t)warp * tc_row_values(c);
-  T* pivots = saved + c.I;
-  T* bridges = pivots + c.I;
-  T* summ = bridges + c.I;        // [5][S]
-  T* st_s = summ + 5 * c.S;       // [R+U]
-  T* st_r = st_s + (c.R + c.U);   // [R+U]
-  T* edge = st_r + (c.R + c.U);   // [R+NB]
-  T* xr = edge + (c.R + c.NB);    // [R]
+  const int tid = threadIdx.x;
+  T* sd = reinterpret_cast<T*>(smem_raw);  // [K]: d, then interior pivots
+  T* sg = sd + c.K;                          // [K]
+  T* sb = sg + c.K;                          // [K]: rhs, interior values, then x
+  T* bridges = sb + c.K;                     // [I]
+  T* summ = bridges + c.I;                   // [5][S]
+  T* st_s = summ + 5 * c.S;                  // [R+U]
+  T* st_r = st_s + (c.R + c.U);              // [R+U]
+  T* edge = st_r + (c.R + c.U);              // [R+NB]
+  T* xr = edge + (c.R + c.NB);               // [R]
   const int32_t* seg_anc = p.seg;
   const int32_t* seg_child = p.seg + c.S;
   const int32_t* seg_a0 = p.seg + 2 * c.S;
@@ -69,31 +74,42 @@ __global__ void __launch_bounds__(128)
   const int32_t* ret_e0 = p.retained + 2 * c.R;
   const int32_t* ret_ne = p.retained + 3 * c.R;
   const int NE = p.n_endpoints, Q = p.n_incidence, NRT = p.n_roots;
-  for (int64_t row = (int64_t)blockIdx.x * wpb + warp; row < B; row += (int64_t)gridDim.x * wpb) {
-    const T* dr = d + row * c.K;
-    const T* gr = g + row * c.K;
-    const T* br = rhs + row * c.K;
-    T* xo = x + row * c.K;
+  for (int64_t row = blockIdx.x; row < B; row += gridDim.x) {
+    {  // 0. stage the row
+      const T* dr = d + row * c.K;
+      const T* gr = g + row * c.K;
+      const T* br = rhs + row * c.K;
+      for (int i = tid; i < c.K; i += TPR) {
+        sd[i] = __ldcs(dr + i);
+        sg[i] = __ldcs(gr + i);
+        sb[i] = __ldcs(br + i);
+      }
+    }
+    __syncthreads();
     // 1. segment condensation, top to bottom
-    for (int s = lane; s < c.S; s += 32) {
-      const int child = seg_child[s], a0 = seg_a0[s], a1 = seg_a1[s];
-      T near = gr[p.interior[a0]];
+    for (int s = tid; s < c.S; s += TPR) {
+      const int child = ret_node[seg_child[s]], a0 = seg_a0[s], a1 = seg_a1[s];
+      int node = p.interior[a0];
+      T near = sg[node];
       T left_d = T(0), left_r = T(0), carry_d = T(0), carry_r = T(0);
       for (int pos = a0; pos < a1; ++pos) {
-        const int node = p.interior[pos];
         const int succ = pos + 1 < a1 ? p.interior[pos + 1] : child;
-        const T far = gr[succ];
-        const T shunt = tc_add(dr[node], carry_d);
-        const T value = tc_add(br[node], carry_r);
+        const T far = sg[succ];
+        const T shunt = tc_add(sd[node], carry_d);
+        const T value = tc_add(sb[node], carry_r);
         const T pivot = tc_add(shunt, tc_add(near, far));
-        saved[pos] = value;
-        pivots[pos] = pivot;
+        const T qn = tc_div(near, pivot), qf = tc_div(far, pivot);
+        const T as = fabs(shunt);
+        const T qs = (fabs(near) < as || fabs(far) < as) ? tc_div(shunt, pivot) : T(0);
+        sb[node] = value;  // this node's d and rhs are read only here
+        sd[node] = pivot;
         bridges[pos] = near;
-        left_d = tc_add(left_d, schur(near, shunt, pivot));
-        left_r = tc_add(left_r, mul_rn(tc_div(near, pivot), value));
-        carry_d = schur(far, shunt, pivot);
-        carry_r = mul_rn(tc_div(far, pivot), value);
-        near = schur(near, far, pivot);
+        left_d = tc_add(left_d, schur_q(near, qn, shunt, qs));
+        left_r = tc_add(left_r, mul_rn(qn, value));
+        carry_d = schur_q(far, qf, shunt, qs);
+        carry_r = mul_rn(qf, value);
+        near = schur_q(near, qn, far, qf);
+        node = succ;
       }
       summ[s] = left_d;
       summ[c.S + s] = left_r;
@@ -101,11 +117,11 @@ __global__ void __launch_bounds__(128)
       summ[3 * c.S + s] = carry_r;
       summ[4 * c.S + s] = near;
     }
-    __syncwarp();
+    __syncthreads();
     // 2. reduced state of the retained nodes
-    for (int r = lane; r < c.R; r += 32) {
+    for (int r = tid; r < c.R; r += TPR) {
       const int node = ret_node[r], in = ret_in[r], e0 = ret_e0[r], ne = ret_ne[r];
-      T diag = dr[node], val = br[node];
+      T diag = sd[node], val = sb[node];
       for (int e = e0; e < e0 + ne; ++e) {
         const int s = p.endpoint[e], side = p.endpoint[NE + e];
         diag = tc_add(diag, summ[2 * side * c.S + s]);
@@ -113,13 +129,13 @@ __global__ void __launch_bounds__(128)
       }
       st_s[r] = diag;
       st_r[r] = val;
-      edge[r] = in >= 0 ? summ[4 * c.S + in] : gr[node];
+      edge[r] = in >= 0 ? summ[4 * c.S + in] : sg[node];
     }
-    __syncwarp();
+    __syncthreads();
     // 3. contraction rounds
     for (int ph = 0; ph < c.P; ++ph) {
       const int u1 = p.round_ptr[ph + 1];
-      for (int u = p.round_ptr[ph] + lane; u < u1; u += 32) {
+      for (int u = p.round_ptr[ph] + tid; u < u1; u += TPR) {
         const int src = p.update[u], q0 = p.update[c.U + u], nq = p.update[2 * c.U + u];
         T diag = st_s[src], val = st_r[src];
         for (int q = q0; q < q0 + nq; ++q) {
@@ -128,26 +144,31 @@ __global__ void __launch_bounds__(128)
           const T shunt = st_s[m], value = st_r[m], near = edge[ns];
           const T far = fs >= 0 ? edge[fs] : T(0);
           const T pivot = tc_add(shunt, tc_add(near, far));
-          diag = tc_add(diag, schur(near, shunt, pivot));
-          val = tc_add(val, mul_rn(tc_div(near, pivot), value));
-          if (dest >= 0) edge[dest] = schur(near, far, pivot);
+          const T qn = tc_div(near, pivot);
+          const T qs = fabs(near) < fabs(shunt) ? tc_div(shunt, pivot) : T(0);
+          diag = tc_add(diag, schur_q(near, qn, shunt, qs));
+          val = tc_add(val, mul_rn(qn, value));
+          if (dest >= 0) {
+            const T qf = fabs(far) <= fabs(near) ? T(0) : tc_div(far, pivot);
+            edge[dest] = schur_q(near, qn, far, qf);
+          }
         }
         st_s[c.R + u] = diag;
         st_r[c.R + u] = val;
       }
-      __syncwarp();
+      __syncthreads();
     }
     // 4. roots
-    for (int k = lane; k < NRT; k += 32) {
+    for (int k = tid; k < NRT; k += TPR) {
       const int r = p.roots[k], st = p.roots[NRT + k];
       xr[r] = tc_div(st_r[st], tc_add(st_s[st], edge[r]));
     }
-    __syncwarp();
+    __syncthreads();
     // 5. recovery rounds, last round first
     const int32_t* rp = p.round_ptr + (c.P + 1);
     for (int ph = c.P - 1; ph >= 0; --ph) {
       const int e1 = rp[ph + 1];
-      for (int e = rp[ph] + lane; e < e1; e += 32) {
+      for (int e = rp[ph] + tid; e < e1; e += TPR) {
         const int node = p.recovery[e], st = p.recovery[c.NR + e];
         const int a = p.recovery[2 * c.NR + e], ch = p.recovery[3 * c.NR + e];
         const int ns = p.recovery[4 * c.NR + e], fs = p.recovery[5 * c.NR + e];
@@ -157,27 +178,30 @@ __global__ void __launch_bounds__(128)
         const T pivot = tc_add(st_s[st], tc_add(near, far));
         xr[node] = tc_div(tc_add(tc_add(st_r[st], mul_rn(near, xr[a])), mul_rn(far, xc)), pivot);
       }
-      __syncwarp();
+      __syncthreads();
     }
-    // 6. retained nodes to HBM
-    for (int r = lane; r < c.R; r += 32) xo[ret_node[r]] = xr[r];
-    __syncwarp();
-    // 7. segment recovery, bottom to top
-    for (int s = lane; s < c.S; s += 32) {
-      int succ = seg_child[s];
-      const T xa = xo[seg_anc[s]];
-      T xs = xo[succ];
+    // 6. retained x into the row (their rhs is dead after the gather)
+    for (int r = tid; r < c.R; r += TPR) sb[ret_node[r]] = xr[r];
+    // 7. segment recovery, bottom to top (endpoint x from xr)
+    for (int s = tid; s < c.S; s += TPR) {
+      int succ = ret_node[seg_child[s]];
+      const T xa = xr[seg_anc[s]];
+      T xs = xr[seg_child[s]];
       for (int pos = seg_a1[s] - 1; pos >= seg_a0[s]; --pos) {
         const int node = p.interior[pos];
-        const T v = tc_div(tc_add(tc_add(saved[pos], mul_rn(bridges[pos], xa)),
-                                  mul_rn(gr[succ], xs)),
-                           pivots[pos]);
-        xo[node] = v;
+        const T v = tc_div(tc_add(tc_add(sb[node], mul_rn(bridges[pos], xa)),
+                                  mul_rn(sg[succ], xs)),
+                           sd[node]);
+        sb[node] = v;
         succ = node;
         xs = v;
       }
     }
-    __syncwarp();
+    __syncthreads();
+    // 8. x to HBM, coalesced
+    T* xrow = x + row * c.K;
+    for (int i = tid; i < c.K; i += TPR) __stcs(xrow + i, sb[i]);
+    __syncthreads();
   }
 }
 
@@ -186,6 +210,23 @@ __global__ void single_node_kernel(int64_t B, const T* __restrict__ d, const T* 
                                    const T* __restrict__ rhs, T* __restrict__ x) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < B) x[i] = tc_div(rhs[i], tc_add(d[i], g[i]));
+}
+
+template <typename T, int TPR>
+static int launch_tpr(int64_t B, const dgb_contract_plan& p, const TcCounts& c, size_t smem,
+                      int sms, const void* d, const void* g, const void* rhs, void* x,
+                      cudaStream_t st) {
+  auto kern = tree_contract_kernel<T, TPR>;
+  DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  int per_sm = 0;
+  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPR, smem));
+  if (per_sm < 1) per_sm = 1;
+  const int64_t cap = (int64_t)sms * per_sm;
+  const unsigned blocks = (unsigned)(B < cap ? B : cap);
+  kern<<<blocks, TPR, smem, st>>>(p, c, B, (const T*)d, (const T*)g, (const T*)rhs, (T*)x);
+  DGB_LAUNCH_CHECK();
+  return DGB_OK;
 }
 
 template <typename T>
@@ -199,28 +240,29 @@ static int launch_contract(int64_t B, const dgb_contract_plan& p, const void* d,
   }
   const TcCounts c{p.size, p.n_segments, p.n_interior, p.n_retained,
                    p.n_updates, p.n_rounds, p.n_eliminated, p.n_bridges};
-  const size_t row_bytes = (size_t)tc_row_values(c) * sizeof(T);
+  const size_t smem = (size_t)tc_row_values(c) * sizeof(T);
   int dev = 0, optin = 0, sms = 0;
   DGB_CUDA_CHECK(cudaGetDevice(&dev));
   DGB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   DGB_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  if (row_bytes > (size_t)optin) {
-    set_error("tree contraction scratch of %zu bytes per row exceeds shared memory", row_bytes);
+  if (smem > (size_t)optin) {
+    set_error("tree contraction scratch of %zu bytes per row exceeds shared memory", smem);
     return DGB_ERANGE;
   }
-  // up to 4 rows (warps) per block while the scratch fits comfortably
-  int wpb = 4;
-  while (wpb > 1 && (size_t)wpb * row_bytes > 96 * 1024) wpb >>= 1;
-  const size_t smem = (size_t)wpb * row_bytes;
-  const int64_t need = (B + wpb - 1) / wpb;
-  const int64_t cap = (int64_t)sms * 64;
-  const unsigned blocks = (unsigned)(need < cap ? need : cap);
-  DGB_CUDA_CHECK(cudaFuncSetAttribute(tree_contract_kernel<T>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  tree_contract_kernel<T><<<blocks, 32 * wpb, smem, st>>>(p, c, B, (const T*)d, (const T*)g,
-                                                          (const T*)rhs, (T*)x);
-  DGB_LAUNCH_CHECK();
-  return DGB_OK;
+  int tpr = p.threads;
+  if (tpr == 0) {  // about one thread per two items of the widest phase, at most 256
+    const int wide = c.S > c.R ? c.S : c.R;
+    tpr = wide > 160 ? 256 : (wide > 80 ? 128 : (wide > 40 ? 64 : 32));
+  }
+  switch (tpr) {
+    case 32: return launch_tpr<T, 32>(B, p, c, smem, sms, d, g, rhs, x, st);
+    case 64: return launch_tpr<T, 64>(B, p, c, smem, sms, d, g, rhs, x, st);
+    case 128: return launch_tpr<T, 128>(B, p, c, smem, sms, d, g, rhs, x, st);
+    case 256: return launch_tpr<T, 256>(B, p, c, smem, sms, d, g, rhs, x, st);
+    default:
+      set_error("threads per row must be 0, 32, 64, 128 or 256; got %d", tpr);
+      return DGB_EINVAL;
+  }
 }
 
 }  // namespace dgb

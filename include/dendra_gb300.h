@@ -788,7 +788,7 @@ int dgb_netstim_run(int dtype, int64_t n, int64_t n_steps, int64_t step0, double
  * Tree contraction (conductance form).  Plan tables are int32 device arrays,
  * fields stored row after row ([field][count]), as built by
  * dendra_gb300/contraction.py (build_contraction_tables):
- *   seg        [4][n_segments]   ancestor node, child node, interior start/end
+ *   seg        [4][n_segments]   ancestor, child (retained indices), interior start/end
  *   interior   [n_interior]      node ids, each segment top to bottom
  *   retained   [4][n_retained]   node, incoming segment (-1), endpoint start, count
  *   endpoint   [2][n_endpoints]  segment, side (0 ancestor end, 1 child end)
@@ -804,7 +804,8 @@ int dgb_netstim_run(int dtype, int64_t n, int64_t n_steps, int64_t step0, double
 typedef struct dgb_contract_plan {
   int32_t size, n_segments, n_interior, n_retained;
   int32_t n_endpoints, n_rounds, n_updates, n_incidence;
-  int32_t n_eliminated, n_roots, n_bridges, reserved;
+  int32_t n_eliminated, n_roots, n_bridges;
+  int32_t threads; /* threads per batch row: 32, 64, 128 or 256; 0 picks by the plan's width */
   const int32_t* seg;
   const int32_t* interior;
   const int32_t* retained;
@@ -819,7 +820,7 @@ typedef struct dgb_contract_plan {
 /* B scalar Hines systems of plan->size nodes sharing the plan's topology:
  * d (shunt), g (conductance to the parent; a root's g is a second shunt), rhs
  * and x are (B, K) row-major:  d_i x_i + g_i (x_i - x_p(i)) + sum_c g_c (x_i - x_c)
- * = rhs_i.  One warp per row, scratch in shared memory (errors DGB_ERANGE
+ * = rhs_i.  One block per row, scratch in shared memory (errors DGB_ERANGE
  * when a row's scratch exceeds it); correctly rounded operations only.  x
  * must not alias an input.  Replaces tree_contraction.solve
  * (triton/tree_contraction.py:748-768; kernels :14-480). */

@@ -665,7 +665,7 @@ def tree_contract_solve(d, g, rhs, tables):
     bridges = np.zeros_like(saved)
     summ = np.zeros((5, B, max(1, S)), dtype=dt)
     for s in range(S):
-        child, a0, a1 = seg[1, s], seg[2, s], seg[3, s]
+        child, a0, a1 = retained[0, seg[1, s]], seg[2, s], seg[3, s]
         near = g[:, interior[a0]]
         left_d, left_r, carry_d, carry_r = zero, zero, zero, zero
         for pos in range(a0, a1):
@@ -729,7 +729,8 @@ def tree_contract_solve(d, g, rhs, tables):
             xr[:, node] = ((st_r[:, st] + near * xr[:, a]) + far * xc) / pivot
     out[:, retained[0]] = xr
     for s in range(S):
-        anc, succ, a0, a1 = seg[:, s]
+        anc, succ = retained[0, seg[0, s]], retained[0, seg[1, s]]
+        a0, a1 = seg[2, s], seg[3, s]
         xa, xs = out[:, anc], out[:, succ]
         for pos in range(a1 - 1, a0 - 1, -1):
             node = interior[pos]

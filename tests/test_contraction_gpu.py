@@ -44,6 +44,18 @@ def test_bit_exact_against_oracle(cuda, dtype, cap, K, branch, B):
     np.testing.assert_array_equal(x.cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("threads", [32, 64, 128, 256])
+def test_every_block_width_is_bit_exact(cuda, threads):
+    rng = np.random.default_rng(threads)
+    parent = random_tree(rng, 700, 0.05)
+    d, g, b = systems(rng, 50, 700, np.float32)
+    for cap in (16, None):
+        plan = TreeContractionPlan(parent, cap, threads=threads)
+        x = solve(*(torch.as_tensor(a).to(cuda) for a in (d, g, b)), plan)
+        np.testing.assert_array_equal(x.cpu().numpy(),
+                                      oracle.tree_contract_solve(d, g, b, plan.tables))
+
+
 @pytest.mark.parametrize("dtype", DTYPES)
 def test_large_tree_many_rows(cuda, dtype):
     # C3-sized tree (2000 nodes, runs of several compartments), 600 rows
