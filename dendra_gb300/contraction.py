@@ -392,13 +392,15 @@ class TreeContractionPlan:
             device = torch.device("cuda", torch.cuda.current_device())
         hit = self._devices.get(device)
         if hit is None:
-            flat = np.concatenate([self.tables[k].ravel() for k in _TABLES] + [
-                np.zeros(1, dtype=np.int32)])
-            packed = torch.as_tensor(flat).to(device)
-            offsets, off = {}, 0
+            parts, offsets, off = [], {}, 0
             for k in _TABLES:
+                a = _device_layout(k, self.tables[k])
                 offsets[k] = off
-                off += self.tables[k].size
+                pad = (-a.size) % 4  # every table starts on 16 bytes
+                parts += [a, np.zeros(pad, dtype=np.int32)]
+                off += a.size + pad
+            packed = torch.as_tensor(np.concatenate(parts + [np.zeros(4, dtype=np.int32)])).to(
+                device)
             parent = torch.as_tensor(self.parent, dtype=torch.int64).to(device)
             is_root = parent < 0
             hit = (packed, offsets, parent.clamp_min(0), is_root)
@@ -421,6 +423,19 @@ class TreeContractionPlan:
         c = self.counts
         return (3 * c["size"] + c["n_interior"] + 5 * c["n_segments"]
                 + 2 * (c["n_retained"] + c["n_updates"]) + 2 * c["n_retained"] + c["n_bridges"])
+
+
+def _device_layout(name, table):
+    """Device form of a plan table: the round tables as 16-byte records (one
+    vector load each), the others field after field."""
+    if name == "update":      # {source, incidence start, count, 0}
+        return np.vstack([table, np.zeros((1, table.shape[1]), np.int32)]).T.ravel().copy()
+    if name == "incidence":   # {removed, near, far, bridge}
+        return table.T.ravel().copy()
+    if name == "recovery":    # {node, state, ancestor, child}, {near, far, 0, 0}
+        z = np.zeros((2, table.shape[1]), np.int32)
+        return np.vstack([table, z]).T.ravel().copy()
+    return table.ravel()
 
 
 def prepare(plan, device):

@@ -51,7 +51,7 @@ static __host__ __device__ __forceinline__ int64_t tc_row_values(const TcCounts&
 // One CTA of TPR threads per batch row (grid-stride over rows); phases are
 // separated by __syncthreads.
 template <typename T, int TPR>
-__global__ void __launch_bounds__(TPR)
+__global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
     tree_contract_kernel(dgb_contract_plan p, TcCounts c, int64_t B, const T* __restrict__ d,
                          const T* __restrict__ g, const T* __restrict__ rhs, T* __restrict__ x) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -73,27 +73,59 @@ __global__ void __launch_bounds__(TPR)
   const int32_t* ret_in = p.retained + c.R;
   const int32_t* ret_e0 = p.retained + 2 * c.R;
   const int32_t* ret_ne = p.retained + 3 * c.R;
-  const int NE = p.n_endpoints, Q = p.n_incidence, NRT = p.n_roots;
+  const int NE = p.n_endpoints, NRT = p.n_roots;
   for (int64_t row = blockIdx.x; row < B; row += gridDim.x) {
-    {  // 0. stage the row
+    {  // 0. stage the row: four loads per array in flight per thread
       const T* dr = d + row * c.K;
       const T* gr = g + row * c.K;
       const T* br = rhs + row * c.K;
-      for (int i = tid; i < c.K; i += TPR) {
-        sd[i] = __ldcs(dr + i);
-        sg[i] = __ldcs(gr + i);
-        sb[i] = __ldcs(br + i);
+      for (int i0 = tid; i0 < c.K; i0 += 4 * TPR) {
+        T vd[4], vg[4], vb[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int i = i0 + k * TPR;
+          if (i < c.K) {
+            vd[k] = __ldcs(dr + i);
+            vg[k] = __ldcs(gr + i);
+            vb[k] = __ldcs(br + i);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int i = i0 + k * TPR;
+          if (i < c.K) {
+            sd[i] = vd[k];
+            sg[i] = vg[k];
+            sb[i] = vb[k];
+          }
+        }
       }
     }
     __syncthreads();
+    {  // the next row of this block into L2 while this one computes
+      const int64_t nrow = row + gridDim.x;
+      if (nrow < B) {
+        const int lines = (int)(((int64_t)c.K * sizeof(T) + 127) / 128);
+        const char* pd = reinterpret_cast<const char*>(d + nrow * c.K);
+        const char* pg = reinterpret_cast<const char*>(g + nrow * c.K);
+        const char* pb = reinterpret_cast<const char*>(rhs + nrow * c.K);
+        for (int l = tid; l < lines; l += TPR) {
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(pd + 128 * (int64_t)l));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(pg + 128 * (int64_t)l));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(pb + 128 * (int64_t)l));
+        }
+      }
+    }
     // 1. segment condensation, top to bottom
     for (int s = tid; s < c.S; s += TPR) {
       const int child = ret_node[seg_child[s]], a0 = seg_a0[s], a1 = seg_a1[s];
       int node = p.interior[a0];
+      int succ = a0 + 1 < a1 ? p.interior[a0 + 1] : child;
       T near = sg[node];
       T left_d = T(0), left_r = T(0), carry_d = T(0), carry_r = T(0);
       for (int pos = a0; pos < a1; ++pos) {
-        const int succ = pos + 1 < a1 ? p.interior[pos + 1] : child;
+        // the index after next is loaded while this step computes
+        const int next = pos + 2 < a1 ? p.interior[pos + 2] : child;
         const T far = sg[succ];
         const T shunt = tc_add(sd[node], carry_d);
         const T value = tc_add(sb[node], carry_r);
@@ -110,6 +142,7 @@ __global__ void __launch_bounds__(TPR)
         carry_r = mul_rn(qf, value);
         near = schur_q(near, qn, far, qf);
         node = succ;
+        succ = next;
       }
       summ[s] = left_d;
       summ[c.S + s] = left_r;
@@ -136,11 +169,12 @@ __global__ void __launch_bounds__(TPR)
     for (int ph = 0; ph < c.P; ++ph) {
       const int u1 = p.round_ptr[ph + 1];
       for (int u = p.round_ptr[ph] + tid; u < u1; u += TPR) {
-        const int src = p.update[u], q0 = p.update[c.U + u], nq = p.update[2 * c.U + u];
+        const int4 up = __ldg(reinterpret_cast<const int4*>(p.update) + u);
+        const int src = up.x, q0 = up.y, nq = up.z;
         T diag = st_s[src], val = st_r[src];
         for (int q = q0; q < q0 + nq; ++q) {
-          const int m = p.incidence[q], ns = p.incidence[Q + q];
-          const int fs = p.incidence[2 * Q + q], dest = p.incidence[3 * Q + q];
+          const int4 in = __ldg(reinterpret_cast<const int4*>(p.incidence) + q);
+          const int m = in.x, ns = in.y, fs = in.z, dest = in.w;
           const T shunt = st_s[m], value = st_r[m], near = edge[ns];
           const T far = fs >= 0 ? edge[fs] : T(0);
           const T pivot = tc_add(shunt, tc_add(near, far));
@@ -169,9 +203,9 @@ __global__ void __launch_bounds__(TPR)
     for (int ph = c.P - 1; ph >= 0; --ph) {
       const int e1 = rp[ph + 1];
       for (int e = rp[ph] + tid; e < e1; e += TPR) {
-        const int node = p.recovery[e], st = p.recovery[c.NR + e];
-        const int a = p.recovery[2 * c.NR + e], ch = p.recovery[3 * c.NR + e];
-        const int ns = p.recovery[4 * c.NR + e], fs = p.recovery[5 * c.NR + e];
+        const int4 r0 = __ldg(reinterpret_cast<const int4*>(p.recovery) + 2 * e);
+        const int4 r1 = __ldg(reinterpret_cast<const int4*>(p.recovery) + 2 * e + 1);
+        const int node = r0.x, st = r0.y, a = r0.z, ch = r0.w, ns = r1.x, fs = r1.y;
         const T near = edge[ns];
         const T far = fs >= 0 ? edge[fs] : T(0);
         const T xc = ch >= 0 ? xr[ch] : T(0);
@@ -187,14 +221,17 @@ __global__ void __launch_bounds__(TPR)
       int succ = ret_node[seg_child[s]];
       const T xa = xr[seg_anc[s]];
       T xs = xr[seg_child[s]];
-      for (int pos = seg_a1[s] - 1; pos >= seg_a0[s]; --pos) {
-        const int node = p.interior[pos];
+      const int a0 = seg_a0[s];
+      int node = p.interior[seg_a1[s] - 1];
+      for (int pos = seg_a1[s] - 1; pos >= a0; --pos) {
+        const int prev = pos > a0 ? p.interior[pos - 1] : 0;  // loaded ahead
         const T v = tc_div(tc_add(tc_add(sb[node], mul_rn(bridges[pos], xa)),
                                   mul_rn(sg[succ], xs)),
                            sd[node]);
         sb[node] = v;
         succ = node;
         xs = v;
+        node = prev;
       }
     }
     __syncthreads();
@@ -294,6 +331,10 @@ extern "C" int dgb_tree_contract_solve(int dtype, int64_t B, const dgb_contract_
                     (p.n_eliminated == 0 || p.recovery),
                 "plan table pointers must be non-null");
   }
+  DGB_REQUIRE((p.n_updates == 0 || ((uintptr_t)p.update & 15) == 0) &&
+                  (p.n_incidence == 0 || ((uintptr_t)p.incidence & 15) == 0) &&
+                  (p.n_eliminated == 0 || ((uintptr_t)p.recovery & 15) == 0),
+              "update, incidence and recovery tables must be 16-byte aligned");
   cudaStream_t st = as_stream(stream);
   if (dtype == DGB_F32) return launch_contract<float>(B, p, d, g, rhs, x, st);
   return launch_contract<double>(B, p, d, g, rhs, x, st);

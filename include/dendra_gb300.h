@@ -785,21 +785,23 @@ int dgb_netstim_run(int dtype, int64_t n, int64_t n_steps, int64_t step0, double
                     uint8_t* spikes, uint64_t* bits, int64_t n_words, void* stream);
 
 /* ---------------------------------------------------------------------------
- * Tree contraction (conductance form).  Plan tables are int32 device arrays,
- * fields stored row after row ([field][count]), as built by
+ * Tree contraction (conductance form).  Plan tables are int32 device arrays
+ * as built by
  * dendra_gb300/contraction.py (build_contraction_tables):
  *   seg        [4][n_segments]   ancestor, child (retained indices), interior start/end
  *   interior   [n_interior]      node ids, each segment top to bottom
  *   retained   [4][n_retained]   node, incoming segment (-1), endpoint start, count
  *   endpoint   [2][n_endpoints]  segment, side (0 ancestor end, 1 child end)
  *   round_ptr  [2][n_rounds+1]   update offsets, recovery offsets
- *   update     [3][n_updates]    source state slot, incidence start, count
- *   incidence  [4][n_incidence]  removed state slot, near edge, far edge (-1),
+ *   update     [n_updates][4]    source state slot, incidence start, count, 0
+ *   incidence  [n_incidence][4]  removed state slot, near edge, far edge (-1),
  *                                bridge slot written (-1)
- *   recovery   [6][n_eliminated] retained index, state slot, ancestor, child (-1),
- *                                near edge, far edge (-1)
+ *   recovery   [n_eliminated][8] retained index, state slot, ancestor, child (-1),
+ *                                near edge, far edge (-1), 0, 0
  *   roots      [2][n_roots]      retained index, final state slot
- * Every slot index must lie inside its table (the builder checks this).
+ * update, incidence and recovery are records (one 16-byte load each) and must
+ * start on 16-byte boundaries.  Every slot index must lie inside its table
+ * (the builder checks this).
  * ------------------------------------------------------------------------- */
 typedef struct dgb_contract_plan {
   int32_t size, n_segments, n_interior, n_retained;
