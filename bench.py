@@ -638,6 +638,7 @@ def bench_bt(args, world, rank, local):
 
 
 TREE_BYTES_PER_NODE = 16  # float32: read d, g, rhs, write x
+TREE_NCU_TRAFFIC = 196546048 + 12276736  # dram read + write of one 8,192-row launch (ncu)
 
 
 def _tree_systems(B, seed, K=2000):
@@ -740,10 +741,12 @@ def bench_tree(args, world, rank, local):
                    "segment_cap": 16, "segments": c["n_segments"], "retained": c["n_retained"],
                    "rounds": c["n_rounds"], "l2": "flushed between timed steps"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "tree_contract_kernel",
+                     "frac": achieved / peak, "traffic": TREE_NCU_TRAFFIC if B == 8192 else None,
+                     "kernel": "tree_contract_kernel",
                      "note": f"{TREE_BYTES_PER_NODE} algorithmic B per float32 node (read d, "
-                             "g, rhs, write x); one warp per system, scratch in shared "
-                             f"memory; peak {peak_kind}"},
+                             "g, rhs, write x); one block per system, the row and its "
+                             "scratch in shared memory; traffic = DRAM read + write of one "
+                             f"8,192-row launch under ncu; peak {peak_kind}"},
         "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": args.steps,
