@@ -33,7 +33,7 @@ def test_float64_gradient_matches_reference_autograd(golden, cuda, every):
     run = CableGradient(pop, int(g["steps"]), rec_idx=0, checkpoint_every=every)
     trace, loss, grads = _fit_step(run, g, cuda)
     np.testing.assert_allclose(trace.detach().cpu().numpy(), g["trace"], rtol=0, atol=1e-7)
-    np.testing.assert_allclose(float(loss), g["loss"].sum(), rtol=1e-8)
+    np.testing.assert_allclose(float(loss.detach()), g["loss"].sum(), rtol=1e-8)
     for k in PARAMS:
         np.testing.assert_allclose(grads[k], g[f"grad_{k}"], rtol=1e-6, err_msg=k)
 
