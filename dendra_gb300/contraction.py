@@ -142,7 +142,9 @@ def build_contraction_tables(parent, cap=16):
     ``parent[i]`` is node i's parent or -1 for a root (any node order; several
     roots make a forest).  Table layout (every row a field):
 
-    * ``seg`` (4, S): ancestor and child (retained indices), interior start, end
+    * ``seg`` (6, S): ancestor and child (retained indices), interior start,
+      end, first interior node, stride (+1 or -1 when the run's node ids are
+      consecutive, else 0)
     * ``interior`` (I,): node ids, each segment's run top to bottom
     * ``retained`` (4, R): node, incoming segment (-1), endpoint start, count
     * ``endpoint`` (2, E): segment, side (0 the ancestor end, 1 the child end)
@@ -197,10 +199,12 @@ def build_contraction_tables(parent, cap=16):
     segs.sort(key=lambda sg: -len(sg[2]))
     S = len(segs)
     interior = [n for _, _, piece in segs for n in piece]
-    seg = np.zeros((4, S), dtype=np.int64)
+    seg = np.zeros((6, S), dtype=np.int64)
     start = 0
     for s, (a, c, piece) in enumerate(segs):
-        seg[:, s] = (a, c, start, start + len(piece))
+        step = np.diff(piece)
+        stride = 1 if (step == 1).all() else (-1 if (step == -1).all() else 0)
+        seg[:, s] = (a, c, start, start + len(piece), piece[0], stride)
         start += len(piece)
 
     # 2. retained nodes and their endpoint summaries
@@ -329,9 +333,14 @@ def _check_tables(t, c):
 
     seg, ret, upd, inc, rec = t["seg"], t["retained"], t["update"], t["incidence"], t["recovery"]
     within(seg[:2], 0, R, "segment endpoint")
-    within(seg[2:], 0, I + 1, "segment interior range")
+    within(seg[2:4], 0, I + 1, "segment interior range")
     if S and ((seg[2] >= seg[3]).any()):
         raise RuntimeError("contraction plan: empty segment")
+    for s in range(S):
+        run = t["interior"][seg[2, s]:seg[3, s]]
+        if seg[4, s] != run[0] or (seg[5, s] != 0 and (
+                run != seg[4, s] + seg[5, s] * np.arange(run.size)).any()):
+            raise RuntimeError("contraction plan: segment stride")
     within(t["interior"], 0, K, "interior node")
     within(ret[0], 0, K, "retained node")
     within(ret[1], -1, S, "incoming segment")
@@ -344,7 +353,7 @@ def _check_tables(t, c):
     if rp.shape != (2, P + 1) or rp[0, -1] != U or rp[1, -1] != N or (np.diff(rp, axis=1) < 0).any():
         raise RuntimeError("contraction plan: round offsets")
     within(upd[0], 0, n_state, "update source")
-    if U and ((upd[1] < 0).any() or (upd[1] + upd[2] > Q).any()):
+    if U and ((upd[1] < 0).any() or (upd[2] < 1).any() or (upd[1] + upd[2] > Q).any()):
         raise RuntimeError("contraction plan: incidence range out of range")
     within(inc[0], 0, n_state, "removed state slot")
     within(inc[1], 0, n_edge, "near edge")
@@ -394,7 +403,7 @@ class TreeContractionPlan:
         if hit is None:
             parts, offsets, off = [], {}, 0
             for k in _TABLES:
-                a = _device_layout(k, self.tables[k])
+                a = _device_layout(k, self.tables[k], self.tables)
                 offsets[k] = off
                 pad = (-a.size) % 4  # every table starts on 16 bytes
                 parts += [a, np.zeros(pad, dtype=np.int32)]
@@ -425,9 +434,23 @@ class TreeContractionPlan:
                 + 2 * (c["n_retained"] + c["n_updates"]) + 2 * c["n_retained"] + c["n_bridges"])
 
 
-def _device_layout(name, table):
-    """Device form of a plan table: the round tables as 16-byte records (one
-    vector load each), the others field after field."""
+def _device_layout(name, table, tables):
+    """Device form of a plan table: records of 16 bytes (one vector load
+    each) except ``interior`` and ``roots``, stored field after field."""
+    if name == "seg":         # {ancestor, child, start, end}, {first, stride, child, ancestor nodes}
+        ret_node = tables["retained"][0]
+        ends = ret_node[table[:2]] if table.shape[1] else np.zeros((2, 0), np.int32)
+        return np.vstack([table, ends[1:2], ends[0:1]]).T.ravel().copy()
+    if name == "retained":    # {node, incoming, endpoint start, count}, 4 endpoint codes
+        ep = tables["endpoint"]
+        codes = np.full((4, table.shape[1]), -1, np.int32)
+        for r in range(table.shape[1]):
+            e0, ne = table[2, r], table[3, r]
+            for k in range(min(ne, 4)):
+                codes[k, r] = 2 * ep[0, e0 + k] + ep[1, e0 + k]
+        return np.vstack([table, codes]).T.ravel().copy()
+    if name == "endpoint":    # {segment, side}
+        return table.T.ravel().copy()
     if name == "update":      # {source, incidence start, count, 0}
         return np.vstack([table, np.zeros((1, table.shape[1]), np.int32)]).T.ravel().copy()
     if name == "incidence":   # {removed, near, far, bridge}

@@ -48,8 +48,17 @@ static __host__ __device__ __forceinline__ int64_t tc_row_values(const TcCounts&
   return 3ll * c.K + c.I + 5ll * c.S + 2ll * (c.R + c.U) + 2ll * c.R + c.NB;
 }
 
+// Node of interior position pos of a segment: arithmetic when the run's ids
+// are consecutive (stride +1/-1), else from the interior table.
+__device__ __forceinline__ int seg_node(const int32_t* __restrict__ interior, int first,
+                                        int stride, int a0, int pos) {
+  return stride != 0 ? first + stride * (pos - a0) : __ldg(interior + pos);
+}
+
 // One CTA of TPR threads per batch row (grid-stride over rows); phases are
-// separated by __syncthreads.
+// separated by __syncthreads.  Plan tables are records (vector loads); the
+// records of a thread's next contraction or recovery round are loaded while
+// the current round computes.
 template <typename T, int TPR>
 __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
     tree_contract_kernel(dgb_contract_plan p, TcCounts c, int64_t B, const T* __restrict__ d,
@@ -65,24 +74,32 @@ __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
   T* st_r = st_s + (c.R + c.U);              // [R+U]
   T* edge = st_r + (c.R + c.U);              // [R+NB]
   T* xr = edge + (c.R + c.NB);               // [R]
-  const int32_t* seg_anc = p.seg;
-  const int32_t* seg_child = p.seg + c.S;
-  const int32_t* seg_a0 = p.seg + 2 * c.S;
-  const int32_t* seg_a1 = p.seg + 3 * c.S;
-  const int32_t* ret_node = p.retained;
-  const int32_t* ret_in = p.retained + c.R;
-  const int32_t* ret_e0 = p.retained + 2 * c.R;
-  const int32_t* ret_ne = p.retained + 3 * c.R;
-  const int NE = p.n_endpoints, NRT = p.n_roots;
+  const int4* seg4 = reinterpret_cast<const int4*>(p.seg);        // 2 per segment
+  const int4* ret4 = reinterpret_cast<const int4*>(p.retained);   // 2 per retained node
+  const int2* end2 = reinterpret_cast<const int2*>(p.endpoint);   // 1 per endpoint
+  const int4* upd4 = reinterpret_cast<const int4*>(p.update);
+  const int4* inc4 = reinterpret_cast<const int4*>(p.incidence);
+  const int4* rec4 = reinterpret_cast<const int4*>(p.recovery);   // 2 per record
+  const int NRT = p.n_roots;
+  // round offsets and roots: read on every round's critical path, so kept in
+  // shared memory for the block's lifetime
+  int32_t* s_int = reinterpret_cast<int32_t*>(xr + c.R);
+  for (int i = tid; i < 2 * (c.P + 1); i += TPR) s_int[i] = __ldg(p.round_ptr + i);
+  for (int i = tid; i < 2 * NRT; i += TPR) s_int[2 * (c.P + 1) + i] = __ldg(p.roots + i);
+  const int32_t* rp_upd = s_int;
+  const int32_t* rp_rec = s_int + (c.P + 1);
+  const int32_t* roots = s_int + 2 * (c.P + 1);
+  __syncthreads();
   for (int64_t row = blockIdx.x; row < B; row += gridDim.x) {
-    {  // 0. stage the row: four loads per array in flight per thread
+    {  // 0. stage the row: UNR loads per array in flight per thread
+      constexpr int UNR = TPR >= 256 ? 2 : 4;
       const T* dr = d + row * c.K;
       const T* gr = g + row * c.K;
       const T* br = rhs + row * c.K;
-      for (int i0 = tid; i0 < c.K; i0 += 4 * TPR) {
-        T vd[4], vg[4], vb[4];
+      for (int i0 = tid; i0 < c.K; i0 += UNR * TPR) {
+        T vd[UNR], vg[UNR], vb[UNR];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < UNR; ++k) {
           const int i = i0 + k * TPR;
           if (i < c.K) {
             vd[k] = __ldcs(dr + i);
@@ -91,7 +108,7 @@ __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
           }
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < UNR; ++k) {
           const int i = i0 + k * TPR;
           if (i < c.K) {
             sd[i] = vd[k];
@@ -118,14 +135,15 @@ __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
     }
     // 1. segment condensation, top to bottom
     for (int s = tid; s < c.S; s += TPR) {
-      const int child = ret_node[seg_child[s]], a0 = seg_a0[s], a1 = seg_a1[s];
-      int node = p.interior[a0];
-      int succ = a0 + 1 < a1 ? p.interior[a0 + 1] : child;
+      const int4 h = __ldg(seg4 + 2 * s), h2 = __ldg(seg4 + 2 * s + 1);
+      const int a0 = h.z, a1 = h.w, first = h2.x, stride = h2.y, child = h2.z;
+      int node = first;
+      int succ = a0 + 1 < a1 ? seg_node(p.interior, first, stride, a0, a0 + 1) : child;
       T near = sg[node];
       T left_d = T(0), left_r = T(0), carry_d = T(0), carry_r = T(0);
       for (int pos = a0; pos < a1; ++pos) {
         // the index after next is loaded while this step computes
-        const int next = pos + 2 < a1 ? p.interior[pos + 2] : child;
+        const int next = pos + 2 < a1 ? seg_node(p.interior, first, stride, a0, pos + 2) : child;
         const T far = sg[succ];
         const T shunt = tc_add(sd[node], carry_d);
         const T value = tc_add(sb[node], carry_r);
@@ -150,15 +168,34 @@ __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
       summ[3 * c.S + s] = carry_r;
       summ[4 * c.S + s] = near;
     }
+    // records of this thread's first contraction round, fetched before the barrier
+    int4 up_next = make_int4(-1, 0, 0, 0), in_next = make_int4(0, 0, -1, -1);
+    if (c.P > 0) {
+      const int u = rp_upd[0] + tid;
+      if (u < rp_upd[1]) {
+        up_next = __ldg(upd4 + u);
+        in_next = __ldg(inc4 + up_next.y);
+      }
+    }
     __syncthreads();
     // 2. reduced state of the retained nodes
     for (int r = tid; r < c.R; r += TPR) {
-      const int node = ret_node[r], in = ret_in[r], e0 = ret_e0[r], ne = ret_ne[r];
+      const int4 rr = __ldg(ret4 + 2 * r), codes = __ldg(ret4 + 2 * r + 1);
+      const int node = rr.x, in = rr.y, e0 = rr.z, ne = rr.w;
       T diag = sd[node], val = sb[node];
-      for (int e = e0; e < e0 + ne; ++e) {
-        const int s = p.endpoint[e], side = p.endpoint[NE + e];
-        diag = tc_add(diag, summ[2 * side * c.S + s]);
-        val = tc_add(val, summ[(2 * side + 1) * c.S + s]);
+      for (int k = 0; k < ne; ++k) {
+        int sg_, side;
+        if (k < 4) {
+          const int code = k == 0 ? codes.x : k == 1 ? codes.y : k == 2 ? codes.z : codes.w;
+          sg_ = code >> 1;
+          side = code & 1;
+        } else {
+          const int2 ep = __ldg(end2 + e0 + k);
+          sg_ = ep.x;
+          side = ep.y;
+        }
+        diag = tc_add(diag, summ[2 * side * c.S + sg_]);
+        val = tc_add(val, summ[(2 * side + 1) * c.S + sg_]);
       }
       st_s[r] = diag;
       st_r[r] = val;
@@ -167,13 +204,22 @@ __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
     __syncthreads();
     // 3. contraction rounds
     for (int ph = 0; ph < c.P; ++ph) {
-      const int u1 = p.round_ptr[ph + 1];
-      for (int u = p.round_ptr[ph] + tid; u < u1; u += TPR) {
-        const int4 up = __ldg(reinterpret_cast<const int4*>(p.update) + u);
+      const int u0 = rp_upd[ph], u1 = rp_upd[ph + 1];
+      const int4 up_first = up_next, in_first = in_next;
+      up_next = make_int4(-1, 0, 0, 0);
+      if (ph + 1 < c.P) {  // prefetch the next round's first record of this thread
+        const int un = u1 + tid;
+        if (un < rp_upd[ph + 2]) {
+          up_next = __ldg(upd4 + un);
+          in_next = __ldg(inc4 + up_next.y);
+        }
+      }
+      for (int u = u0 + tid; u < u1; u += TPR) {
+        const int4 up = u == u0 + tid ? up_first : __ldg(upd4 + u);
         const int src = up.x, q0 = up.y, nq = up.z;
         T diag = st_s[src], val = st_r[src];
         for (int q = q0; q < q0 + nq; ++q) {
-          const int4 in = __ldg(reinterpret_cast<const int4*>(p.incidence) + q);
+          const int4 in = (u == u0 + tid && q == q0) ? in_first : __ldg(inc4 + q);
           const int m = in.x, ns = in.y, fs = in.z, dest = in.w;
           const T shunt = st_s[m], value = st_r[m], near = edge[ns];
           const T far = fs >= 0 ? edge[fs] : T(0);
@@ -192,19 +238,37 @@ __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
       }
       __syncthreads();
     }
+    // records of this thread's first recovery round (the last round)
+    int4 rc_a = make_int4(-1, 0, 0, 0), rc_b = make_int4(0, 0, 0, 0);
+    if (c.P > 0) {
+      const int e = rp_rec[c.P - 1] + tid;
+      if (e < rp_rec[c.P]) {
+        rc_a = __ldg(rec4 + 2 * e);
+        rc_b = __ldg(rec4 + 2 * e + 1);
+      }
+    }
     // 4. roots
     for (int k = tid; k < NRT; k += TPR) {
-      const int r = p.roots[k], st = p.roots[NRT + k];
+      const int r = roots[k], st = roots[NRT + k];
       xr[r] = tc_div(st_r[st], tc_add(st_s[st], edge[r]));
     }
     __syncthreads();
     // 5. recovery rounds, last round first
-    const int32_t* rp = p.round_ptr + (c.P + 1);
     for (int ph = c.P - 1; ph >= 0; --ph) {
-      const int e1 = rp[ph + 1];
-      for (int e = rp[ph] + tid; e < e1; e += TPR) {
-        const int4 r0 = __ldg(reinterpret_cast<const int4*>(p.recovery) + 2 * e);
-        const int4 r1 = __ldg(reinterpret_cast<const int4*>(p.recovery) + 2 * e + 1);
+      const int e0 = rp_rec[ph], e1 = rp_rec[ph + 1];
+      const int4 fa = rc_a, fb = rc_b;
+      rc_a = make_int4(-1, 0, 0, 0);
+      if (ph > 0) {
+        const int en = rp_rec[ph - 1] + tid;
+        if (en < e0) {
+          rc_a = __ldg(rec4 + 2 * en);
+          rc_b = __ldg(rec4 + 2 * en + 1);
+        }
+      }
+      for (int e = e0 + tid; e < e1; e += TPR) {
+        const bool mine = e == e0 + tid;
+        const int4 r0 = mine ? fa : __ldg(rec4 + 2 * e);
+        const int4 r1 = mine ? fb : __ldg(rec4 + 2 * e + 1);
         const int node = r0.x, st = r0.y, a = r0.z, ch = r0.w, ns = r1.x, fs = r1.y;
         const T near = edge[ns];
         const T far = fs >= 0 ? edge[fs] : T(0);
@@ -215,16 +279,17 @@ __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
       __syncthreads();
     }
     // 6. retained x into the row (their rhs is dead after the gather)
-    for (int r = tid; r < c.R; r += TPR) sb[ret_node[r]] = xr[r];
+    for (int r = tid; r < c.R; r += TPR) sb[__ldg(ret4 + 2 * r).x] = xr[r];
     // 7. segment recovery, bottom to top (endpoint x from xr)
     for (int s = tid; s < c.S; s += TPR) {
-      int succ = ret_node[seg_child[s]];
-      const T xa = xr[seg_anc[s]];
-      T xs = xr[seg_child[s]];
-      const int a0 = seg_a0[s];
-      int node = p.interior[seg_a1[s] - 1];
-      for (int pos = seg_a1[s] - 1; pos >= a0; --pos) {
-        const int prev = pos > a0 ? p.interior[pos - 1] : 0;  // loaded ahead
+      const int4 h = __ldg(seg4 + 2 * s), h2 = __ldg(seg4 + 2 * s + 1);
+      const int a0 = h.z, a1 = h.w, first = h2.x, stride = h2.y;
+      int succ = h2.z;
+      const T xa = xr[h.x];
+      T xs = xr[h.y];
+      int node = seg_node(p.interior, first, stride, a0, a1 - 1);
+      for (int pos = a1 - 1; pos >= a0; --pos) {
+        const int prev = pos > a0 ? seg_node(p.interior, first, stride, a0, pos - 1) : 0;
         const T v = tc_div(tc_add(tc_add(sb[node], mul_rn(bridges[pos], xa)),
                                   mul_rn(sg[succ], xs)),
                            sd[node]);
@@ -277,7 +342,7 @@ static int launch_contract(int64_t B, const dgb_contract_plan& p, const void* d,
   }
   const TcCounts c{p.size, p.n_segments, p.n_interior, p.n_retained,
                    p.n_updates, p.n_rounds, p.n_eliminated, p.n_bridges};
-  const size_t smem = (size_t)tc_row_values(c) * sizeof(T);
+  const size_t smem = (size_t)tc_row_values(c) * sizeof(T) + 4 * (2 * (c.P + 1) + 2 * p.n_roots);
   int dev = 0, optin = 0, sms = 0;
   DGB_CUDA_CHECK(cudaGetDevice(&dev));
   DGB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -287,9 +352,9 @@ static int launch_contract(int64_t B, const dgb_contract_plan& p, const void* d,
     return DGB_ERANGE;
   }
   int tpr = p.threads;
-  if (tpr == 0) {  // about one thread per two items of the widest phase, at most 256
+  if (tpr == 0) {  // by the widest phase: 128 threads from 80 items, 256 from 640
     const int wide = c.S > c.R ? c.S : c.R;
-    tpr = wide > 160 ? 256 : (wide > 80 ? 128 : (wide > 40 ? 64 : 32));
+    tpr = wide > 640 ? 256 : (wide > 80 ? 128 : (wide > 40 ? 64 : 32));
   }
   switch (tpr) {
     case 32: return launch_tpr<T, 32>(B, p, c, smem, sms, d, g, rhs, x, st);
@@ -331,10 +396,14 @@ extern "C" int dgb_tree_contract_solve(int dtype, int64_t B, const dgb_contract_
                     (p.n_eliminated == 0 || p.recovery),
                 "plan table pointers must be non-null");
   }
-  DGB_REQUIRE((p.n_updates == 0 || ((uintptr_t)p.update & 15) == 0) &&
-                  (p.n_incidence == 0 || ((uintptr_t)p.incidence & 15) == 0) &&
-                  (p.n_eliminated == 0 || ((uintptr_t)p.recovery & 15) == 0),
-              "update, incidence and recovery tables must be 16-byte aligned");
+  DGB_REQUIRE(p.size == 1 ||
+                  (((uintptr_t)p.retained & 15) == 0 &&
+                   (p.n_segments == 0 ||
+                    (((uintptr_t)p.seg & 15) == 0 && ((uintptr_t)p.endpoint & 7) == 0)) &&
+                   (p.n_updates == 0 || ((uintptr_t)p.update & 15) == 0) &&
+                   (p.n_incidence == 0 || ((uintptr_t)p.incidence & 15) == 0) &&
+                   (p.n_eliminated == 0 || ((uintptr_t)p.recovery & 15) == 0)),
+              "plan record tables must be 16-byte aligned (endpoint 8-byte)");
   cudaStream_t st = as_stream(stream);
   if (dtype == DGB_F32) return launch_contract<float>(B, p, d, g, rhs, x, st);
   return launch_contract<double>(B, p, d, g, rhs, x, st);

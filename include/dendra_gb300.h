@@ -788,10 +788,14 @@ int dgb_netstim_run(int dtype, int64_t n, int64_t n_steps, int64_t step0, double
  * Tree contraction (conductance form).  Plan tables are int32 device arrays
  * as built by
  * dendra_gb300/contraction.py (build_contraction_tables):
- *   seg        [4][n_segments]   ancestor, child (retained indices), interior start/end
+ *   seg        [n_segments][8]   ancestor, child (retained indices), interior start,
+ *                                end, first interior node, stride (+1/-1 when the
+ *                                run's node ids are consecutive, else 0), child
+ *                                node, ancestor node
  *   interior   [n_interior]      node ids, each segment top to bottom
- *   retained   [4][n_retained]   node, incoming segment (-1), endpoint start, count
- *   endpoint   [2][n_endpoints]  segment, side (0 ancestor end, 1 child end)
+ *   retained   [n_retained][8]   node, incoming segment (-1), endpoint start, count,
+ *                                the first four endpoints as 2*segment + side (-1)
+ *   endpoint   [n_endpoints][2]  segment, side (0 ancestor end, 1 child end)
  *   round_ptr  [2][n_rounds+1]   update offsets, recovery offsets
  *   update     [n_updates][4]    source state slot, incidence start, count, 0
  *   incidence  [n_incidence][4]  removed state slot, near edge, far edge (-1),
@@ -799,8 +803,8 @@ int dgb_netstim_run(int dtype, int64_t n, int64_t n_steps, int64_t step0, double
  *   recovery   [n_eliminated][8] retained index, state slot, ancestor, child (-1),
  *                                near edge, far edge (-1), 0, 0
  *   roots      [2][n_roots]      retained index, final state slot
- * update, incidence and recovery are records (one 16-byte load each) and must
- * start on 16-byte boundaries.  Every slot index must lie inside its table
+ * seg, retained, update, incidence and recovery are 16-byte records (vector
+ * loads) and must start on 16-byte boundaries; endpoint on 8 bytes.  Every slot index must lie inside its table
  * (the builder checks this).
  * ------------------------------------------------------------------------- */
 typedef struct dgb_contract_plan {
