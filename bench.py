@@ -638,7 +638,7 @@ def bench_bt(args, world, rank, local):
 
 
 TREE_BYTES_PER_NODE = 16  # float32: read d, g, rhs, write x
-TREE_NCU_TRAFFIC = 196546048 + 12276736  # dram read + write of one 8,192-row launch (ncu)
+TREE_NCU_TRAFFIC = 196502528 + 12083200  # dram read + write of one 8,192-row launch (ncu)
 
 
 def _tree_systems(B, seed, K=2000):
