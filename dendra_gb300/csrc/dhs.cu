@@ -23,6 +23,9 @@ struct ForestArgsT {
   const int32_t* layer_ptr;
   const int32_t* child_ptr;
   const int32_t* child_idx;
+  // optional per-tree node counts (row-padded planes: tree t's K_t nodes
+  // start at node_ptr[t]); NULL: K_t = node_ptr[t+1] - node_ptr[t]
+  const int32_t* tree_k;
 };
 
 __device__ __forceinline__ TreeTopo forest_topo(const ForestArgsT& F, int plan, int K) {
@@ -61,7 +64,8 @@ __global__ void __launch_bounds__(128) dhs_forest_kernel(ForestArgsT F, const T*
   T* sB = sD + kmax;
   for (int tree = blockIdx.x * wpb + warp; tree < F.n_trees; tree += gridDim.x * wpb) {
     const int64_t base = F.shared_k > 0 ? (int64_t)tree * F.shared_k : F.node_ptr[tree];
-    const int K = F.shared_k > 0 ? F.shared_k : (int)(F.node_ptr[tree + 1] - base);
+    const int K = F.shared_k > 0 ? F.shared_k
+                  : (F.tree_k ? F.tree_k[tree] : (int)(F.node_ptr[tree + 1] - base));
     const int plan = F.shared_k > 0 ? 0 : (F.plan_of ? F.plan_of[tree] : tree);
     const TreeTopo t = forest_topo(F, plan, K);
     for (int i = lane; i < K; i += 32) {
@@ -128,7 +132,7 @@ extern "C" int dgb_dhs_solve_forest(int dtype, const dgb_forest* forest, const v
   DGB_REQUIRE(forest->n_trees >= 0, "n_trees must be >= 0");
   ForestArgsT F{forest->n_trees, 0, 0, forest->node_ptr, forest->plan_of, forest->plan_node_ptr,
                 forest->plan_layer_off, forest->parent, forest->order, forest->layer_ptr,
-                forest->child_ptr, forest->child_idx};
+                forest->child_ptr, forest->child_idx, forest->tree_k};
   return forest_dispatch(dtype, F, forest->max_k, d, a, b, x, stream);
 }
 
@@ -143,6 +147,6 @@ extern "C" int dgb_dhs_solve(int dtype, int64_t B, int64_t K, const void* d, con
   DGB_REQUIRE(n_layers >= 1, "layer_ptr must contain at least two entries");
   DGB_REQUIRE(B <= INT32_MAX && K <= INT32_MAX, "too many trees or nodes");
   ForestArgsT F{(int32_t)B, (int32_t)K, n_layers, nullptr, nullptr, nullptr, nullptr,
-                parent,     order,      layer_ptr, child_ptr, child_idx};
+                parent,     order,      layer_ptr, child_ptr, child_idx, nullptr};
   return forest_dispatch(dtype, F, (int)K, d, a, b, x, stream);
 }

@@ -370,7 +370,7 @@ class DgbForest(ctypes.Structure):
         ("child_ptr", ctypes.c_void_p), ("child_idx", ctypes.c_void_p),
         ("plan_chain_off", ctypes.c_void_p), ("plan_clevel_off", ctypes.c_void_p),
         ("chain_nodes", ctypes.c_void_p), ("chain_ptr", ctypes.c_void_p),
-        ("chain_level", ctypes.c_void_p),
+        ("chain_level", ctypes.c_void_p), ("tree_k", ctypes.c_void_p),
     ]
 
 
@@ -467,3 +467,187 @@ def dhs_solve_forest(d, a, b, plan: ForestPlan):
                                               x.data_ptr(), _lib.stream_ptr(d.device))
     _lib.check(rc, "dgb_dhs_solve_forest")
     return x
+
+
+_MULTI_PLAN = ("P_cat", "ORDER_cat", "LAYER_PTR_cat", "WARP_P_OFF", "WARP_ORDER_OFF",
+               "WARP_LPTR_OFF", "WARP_L", "WARP_ROW_BASE", "WARP_ROW_COUNT")
+
+
+def validate_tree_multi(d_mem, a_geom, b, plan, K_stride, L_max, threads, grid_x):
+    """The reference's checks of the row-padded multi-morphology launch
+    (triton/_contracts.py:271-341); ``plan`` is the nine index tensors in
+    signature order."""
+    data = (("d_mem", d_mem), ("a_geom", a_geom), ("b", b))
+    named = tuple(zip(_MULTI_PLAN, plan))
+    for name, t in data + named:
+        if not isinstance(t, torch.Tensor):
+            raise TypeError(f"{name} must be a torch.Tensor")
+    if d_mem.ndim != 2:
+        raise ValueError(f"d_mem must have shape (B, K_stride), got {tuple(d_mem.shape)}")
+    if a_geom.shape != d_mem.shape or b.shape != d_mem.shape:
+        raise ValueError("d_mem, a_geom, and b must have identical shapes")
+    batch, width = map(int, d_mem.shape)
+    if batch < 1 or width < 1:
+        raise ValueError("B and K_stride must both be >= 1")
+    if isinstance(K_stride, bool) or not isinstance(K_stride, int):
+        raise TypeError("K_stride must be an integer")
+    if K_stride != width:
+        raise ValueError(f"K_stride must equal the padded row width {width}")
+    if isinstance(L_max, bool) or not isinstance(L_max, int):
+        raise TypeError("L_max must be an integer")
+    if L_max < 1:
+        raise ValueError("L_max must be >= 1")
+    _validate_float_group(data)
+    for name, t in named:
+        if t.ndim != 1:
+            raise ValueError(f"{name} must be 1-D")
+        if t.dtype not in _INDEX_DTYPES:
+            raise TypeError(f"{name} must have dtype int32 or int64")
+        if t.device != d_mem.device:
+            raise ValueError(f"{name} must be on device {d_mem.device}; got {t.device}")
+    p_cat, order_cat, lptr_cat = plan[:3]
+    if p_cat.numel() != order_cat.numel() or p_cat.numel() < 1:
+        raise ValueError("P_cat and ORDER_cat must have the same non-zero length")
+    if lptr_cat.numel() < 2:
+        raise ValueError("LAYER_PTR_cat must contain at least two entries")
+    warp_count = int(plan[7].numel())
+    if warp_count < 1:
+        raise ValueError("the launch plan must contain at least one warp")
+    for name, t in named[3:]:
+        if t.numel() != warp_count:
+            raise ValueError(f"{name} must contain one entry per warp ({warp_count})")
+    if grid_x is not None:
+        if isinstance(grid_x, bool) or not isinstance(grid_x, int):
+            raise TypeError("grid_x must be an integer or None")
+        if grid_x != warp_count:
+            raise ValueError(f"grid_x must equal the plan warp count {warp_count}")
+    validate_threads(threads)
+    return batch, warp_count
+
+
+_multi_cache: dict = {}
+
+
+class _MultiPlan:
+    """Device form of a row-padded multi-morphology plan: a forest over the
+    covered rows (tree t = one row, its K_t nodes at row * K_stride) and the
+    flat parent index of every plane entry for the gradient."""
+
+    def __init__(self, plan, B, K_stride, device):
+        p_cat, _, lptr_cat, p_off, _, l_off, n_l, row_base, row_count = (
+            t.detach().cpu().numpy().astype(np.int64) for t in plan)
+        morphs, parents, tree_rows, tree_morph = {}, [], [], []
+        covered = np.zeros(B, dtype=bool)
+        for w in range(row_base.size):
+            if n_l[w] < 1 or l_off[w] < 0 or l_off[w] + n_l[w] >= lptr_cat.size:
+                raise ValueError(f"warp {w}: layer table out of range")
+            k = int(lptr_cat[l_off[w] + n_l[w]])  # the last layer ends at K_g
+            if k < 1 or k > K_stride or p_off[w] < 0 or p_off[w] + k > p_cat.size:
+                raise ValueError(f"warp {w}: morphology of {k} nodes does not fit")
+            key = (int(p_off[w]), k)
+            if key not in morphs:
+                morphs[key] = len(parents)
+                parents.append(p_cat[p_off[w]:p_off[w] + k])
+            rows = row_base[w] + np.arange(max(int(row_count[w]), 0))
+            if rows.size and (rows.min() < 0 or rows.max() >= B):
+                raise ValueError(f"warp {w}: rows out of range")
+            if covered[rows].any():
+                raise ValueError(f"warp {w}: a row is covered by two warps")
+            covered[rows] = True
+            tree_rows.extend(rows.tolist())
+            tree_morph.extend([morphs[key]] * rows.size)
+        self.n_trees = len(tree_rows)
+        self.forest = None
+        if self.n_trees:
+            f = ForestPlan([list(map(int, p)) for p in parents], device=device,
+                           plan_of=tree_morph, chains=False)
+            rows = np.asarray(tree_rows, dtype=np.int64)
+            k_of = np.asarray([len(parents[m]) for m in tree_morph], dtype=np.int32)
+            node_ptr = np.append(rows * K_stride, B * K_stride).astype(np.int64)
+            f.tensors["node_ptr"] = torch.as_tensor(node_ptr, device=device)
+            f.tensors["tree_k"] = torch.as_tensor(k_of, device=device)
+            f.max_k = int(k_of.max())
+            self.forest = f
+        # flat parent of every plane entry (-1: root, padding or uncovered row)
+        par = np.full(B * K_stride, -1, dtype=np.int64)
+        for r, m in zip(tree_rows, tree_morph):
+            p = parents[m]
+            base = r * K_stride
+            nz = p >= 0
+            idx = base + np.flatnonzero(nz)
+            par[idx] = base + p[nz]
+        self.is_node = np.zeros(B * K_stride, dtype=bool)
+        for r, m in zip(tree_rows, tree_morph):
+            self.is_node[r * K_stride:r * K_stride + len(parents[m])] = True
+        self.parent_flat = torch.as_tensor(par, device=device)
+        self.has_parent = self.parent_flat >= 0
+        self.node_mask = torch.as_tensor(self.is_node, device=device)
+
+
+def _multi_plan(plan, B, K_stride, device):
+    key = (B, K_stride, str(device)) + tuple(
+        (t.data_ptr(), t._version, t.numel(), t.dtype) for t in plan)
+    hit = _multi_cache.get(key)
+    if hit is None:
+        if len(_multi_cache) > 32:
+            _multi_cache.clear()
+        hit = _multi_cache[key] = _MultiPlan(plan, B, K_stride, device)
+    return hit
+
+
+def _multi_solve(d, a, b, mp):
+    x = torch.zeros_like(b)
+    if mp.forest is None:
+        return x
+    d, a, b = (t.contiguous() for t in (d, a, b))
+    f = mp.forest.struct()
+    with torch.cuda.device(d.device):
+        rc = _lib.load().dgb_dhs_solve_forest(_lib.dtype_code(d.dtype), ctypes.byref(f),
+                                              d.data_ptr(), a.data_ptr(), b.data_ptr(),
+                                              x.data_ptr(), _lib.stream_ptr(d.device))
+    _lib.check(rc, "dgb_dhs_solve_forest")
+    return x
+
+
+class _DHSMultiSolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, d_mem, a_geom, b, mp):
+        x = _multi_solve(d_mem, a_geom, b, mp)
+        ctx.mp = mp
+        ctx.save_for_backward(d_mem, a_geom, x)
+        return x
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        d_mem, a_geom, x = ctx.saved_tensors
+        mp = ctx.mp
+        g = _multi_solve(d_mem, a_geom, grad_out.contiguous(), mp)  # symmetric system
+        xf, gf = x.reshape(-1), g.reshape(-1)
+        par = mp.parent_flat.clamp_min(0)
+        drop_x = torch.where(mp.has_parent, xf - xf.index_select(0, par), xf)
+        drop_g = torch.where(mp.has_parent, gf - gf.index_select(0, par), gf)
+        grad_a = torch.where(mp.node_mask, -(drop_g * drop_x), torch.zeros_like(xf))
+        return -(g * x), grad_a.view_as(x), g, None
+
+
+def dhs_solve_multi_cuda(d_mem, a_geom, b, P_cat, ORDER_cat, LAYER_PTR_cat, WARP_P_OFF,
+                         WARP_ORDER_OFF, WARP_LPTR_OFF, WARP_L, WARP_ROW_BASE, WARP_ROW_COUNT,
+                         K_stride: int, L_max: int, threads: int, grid_x: int = None):
+    """Row-padded multi-morphology tree solve with the reference's signature
+    (triton/dhs_kernel_multi.py:831-888, called at integrators/tree.py:2273-2300).
+
+    ``d_mem``, ``a_geom``, ``b`` are (B_total, K_stride) planes; warp ``w``
+    covers rows ``WARP_ROW_BASE[w] ..`` (``WARP_ROW_COUNT[w]`` of them), all
+    of the morphology whose parents start at ``P_cat[WARP_P_OFF[w]]`` and
+    whose ``WARP_L[w]`` layers start at ``LAYER_PTR_cat[WARP_LPTR_OFF[w]]``
+    (the last layer ends at the morphology's node count).  Every covered row
+    is one tree in a single dgb_dhs_solve_forest launch (rows read in place);
+    entries past a morphology's nodes and uncovered rows return 0.  The
+    elimination order is this build's own (deterministic, children pulled in
+    index order), so ORDER_cat only has to be a valid plan.  Gradients follow
+    DHSSolveMultiPacked.backward (dhs_kernel_multi.py:699-780)."""
+    plan = (P_cat, ORDER_cat, LAYER_PTR_cat, WARP_P_OFF, WARP_ORDER_OFF, WARP_LPTR_OFF, WARP_L,
+            WARP_ROW_BASE, WARP_ROW_COUNT)
+    B, _ = validate_tree_multi(d_mem, a_geom, b, plan, K_stride, L_max, threads, grid_x)
+    mp = _multi_plan(plan, B, K_stride, d_mem.device)
+    return _DHSMultiSolve.apply(d_mem, a_geom, b, mp)

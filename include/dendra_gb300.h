@@ -402,11 +402,15 @@ typedef struct dgb_forest {
   const int32_t* chain_nodes;
   const int32_t* chain_ptr;
   const int32_t* chain_level;
+  /* optional [n_trees] node counts for row-padded planes (dgb_dhs_solve_forest
+     only): tree t's K_t nodes start at node_ptr[t], the rest of its row is
+     not touched; NULL: K_t = node_ptr[t+1] - node_ptr[t] */
+  const int32_t* tree_k;
 } dgb_forest;
 
 /*
  * Heterogeneous trees (different sizes and topologies) in one launch, values
- * packed by node_ptr.  Replaces dhs_solve_multi_cuda
+ * packed by node_ptr (or in row-padded planes with tree_k).  Replaces dhs_solve_multi_cuda
  * (dendra/models/integrators/triton/dhs_kernel_multi.py:831-888).
  */
 int dgb_dhs_solve_forest(int dtype, const dgb_forest* forest, const void* d,
