@@ -534,6 +534,7 @@ class _MultiPlan:
     flat parent index of every plane entry for the gradient."""
 
     def __init__(self, plan, B, K_stride, device):
+        self.plan, self.K_stride = tuple(plan), int(K_stride)
         p_cat, _, lptr_cat, p_off, _, l_off, n_l, row_base, row_count = (
             t.detach().cpu().numpy().astype(np.int64) for t in plan)
         morphs, parents, tree_rows, tree_morph = {}, [], [], []
