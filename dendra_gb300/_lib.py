@@ -121,7 +121,8 @@ SIGNATURES = {
     "dgb_block3_spd_solve_chol": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P]),
     "dgb_dhs_block3_solve": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P, _I32, _P, _P, _P,
                                     _I32, _P]),
-    "dgb_tree_contract_solve": (_INT, [_INT, _I64, _P, _P, _P, _P, _P, _P]),
+    "dgb_tree_contract_solve": (_INT, [_INT, _I64, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P]),
+    "dgb_tree_contract_work_size": (ctypes.c_size_t, [_INT, _P, _I64]),
     "dgb_contract_plan_size": (ctypes.c_size_t, []),
     "dgb_netstim_init": (_INT, [_INT, _I64, _P, _P, _P, _I32, ctypes.c_uint64, _P, _P, _P, _P]),
     "dgb_netstim_run": (_INT, [_INT, _I64, _I64, _I64, ctypes.c_double, ctypes.c_double, _P, _P,

@@ -44,8 +44,9 @@ The plan (host, once per topology):
    segment is recovered bottom to top.
 
 The kernel runs one block (32-256 threads) per batch row with all scratch in
-shared memory and uses correctly rounded operations only, so the oracle's
-numpy restatement of the same plan reproduces it bit for bit.
+shared memory (in a global workspace when a row's scratch does not fit, for
+trees of any size) and uses correctly rounded operations only, so the
+oracle's numpy restatement of the same plan reproduces it bit for bit.
 """
 
 from __future__ import annotations
@@ -477,10 +478,15 @@ def _launch(d, g, rhs, plan):
         return out
     d, g, rhs = (v.contiguous() for v in (d, g, rhs))
     s = plan.struct(d.device)
+    L = _lib.load()
+    code = _lib.dtype_code(d.dtype)
     with torch.cuda.device(d.device):
-        rc = _lib.load().dgb_tree_contract_solve(
-            _lib.dtype_code(d.dtype), B, ctypes.byref(s), d.data_ptr(), g.data_ptr(),
-            rhs.data_ptr(), out.data_ptr(), _lib.stream_ptr(d.device))
+        nwork = L.dgb_tree_contract_work_size(code, ctypes.byref(s), B)
+        work = torch.empty(nwork, dtype=torch.uint8, device=d.device) if nwork else None
+        rc = L.dgb_tree_contract_solve(
+            code, B, ctypes.byref(s), d.data_ptr(), g.data_ptr(), rhs.data_ptr(),
+            out.data_ptr(), None if work is None else work.data_ptr(), nwork,
+            _lib.stream_ptr(d.device))
     _lib.check(rc, "dgb_tree_contract_solve")
     return out
 

@@ -59,13 +59,19 @@ __device__ __forceinline__ int seg_node(const int32_t* __restrict__ interior, in
 // separated by __syncthreads.  Plan tables are records (vector loads); the
 // records of a thread's next contraction or recovery round are loaded while
 // the current round computes.
-template <typename T, int TPR>
+//
+// GW = true keeps the row's values in a global workspace (one slice of
+// tc_row_values(c) per block) instead of shared memory: the same program for
+// trees whose scratch does not fit on chip.
+template <typename T, int TPR, bool GW>
 __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
     tree_contract_kernel(dgb_contract_plan p, TcCounts c, int64_t B, const T* __restrict__ d,
-                         const T* __restrict__ g, const T* __restrict__ rhs, T* __restrict__ x) {
+                         const T* __restrict__ g, const T* __restrict__ rhs, T* __restrict__ x,
+                         T* __restrict__ work) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
-  T* sd = reinterpret_cast<T*>(smem_raw);  // [K]: d, then interior pivots
+  T* sd = GW ? work + (size_t)blockIdx.x * tc_row_values(c)
+             : reinterpret_cast<T*>(smem_raw);  // [K]: d, then interior pivots
   T* sg = sd + c.K;                          // [K]
   T* sb = sg + c.K;                          // [K]: rhs, interior values, then x
   T* bridges = sb + c.K;                     // [I]
@@ -83,7 +89,7 @@ __global__ void __launch_bounds__(TPR, (TPR >= 256 && sizeof(T) == 4) ? 5 : 1)
   const int NRT = p.n_roots;
   // round offsets and roots: read on every round's critical path, so kept in
   // shared memory for the block's lifetime
-  int32_t* s_int = reinterpret_cast<int32_t*>(xr + c.R);
+  int32_t* s_int = GW ? reinterpret_cast<int32_t*>(smem_raw) : reinterpret_cast<int32_t*>(xr + c.R);
   for (int i = tid; i < 2 * (c.P + 1); i += TPR) s_int[i] = __ldg(p.round_ptr + i);
   for (int i = tid; i < 2 * NRT; i += TPR) s_int[2 * (c.P + 1) + i] = __ldg(p.roots + i);
   const int32_t* rp_upd = s_int;
@@ -314,57 +320,102 @@ __global__ void single_node_kernel(int64_t B, const T* __restrict__ d, const T* 
   if (i < B) x[i] = tc_div(rhs[i], tc_add(d[i], g[i]));
 }
 
-template <typename T, int TPR>
+// Blocks of the global-workspace variant per SM (its workspace is sized by
+// blocks x the row's values).
+constexpr int kGwBlocksPerSm = 4;
+
+template <typename T, int TPR, bool GW>
 static int launch_tpr(int64_t B, const dgb_contract_plan& p, const TcCounts& c, size_t smem,
                       int sms, const void* d, const void* g, const void* rhs, void* x,
-                      cudaStream_t st) {
-  auto kern = tree_contract_kernel<T, TPR>;
+                      void* work, cudaStream_t st) {
+  auto kern = tree_contract_kernel<T, TPR, GW>;
   DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   int per_sm = 0;
   DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TPR, smem));
   if (per_sm < 1) per_sm = 1;
+  if (GW) per_sm = kGwBlocksPerSm;  // the workspace holds exactly this many rows per SM
   const int64_t cap = (int64_t)sms * per_sm;
   const unsigned blocks = (unsigned)(B < cap ? B : cap);
-  kern<<<blocks, TPR, smem, st>>>(p, c, B, (const T*)d, (const T*)g, (const T*)rhs, (T*)x);
+  kern<<<blocks, TPR, smem, st>>>(p, c, B, (const T*)d, (const T*)g, (const T*)rhs, (T*)x,
+                                  (T*)work);
   DGB_LAUNCH_CHECK();
+  return DGB_OK;
+}
+
+static size_t tc_int_bytes(const dgb_contract_plan& p) {
+  return 4 * (2 * ((size_t)p.n_rounds + 1) + 2 * (size_t)p.n_roots);
+}
+
+static TcCounts tc_counts(const dgb_contract_plan& p) {
+  return TcCounts{p.size, p.n_segments, p.n_interior, p.n_retained,
+                  p.n_updates, p.n_rounds, p.n_eliminated, p.n_bridges};
+}
+
+// Workspace bytes of the global variant for B rows; 0 when the row's scratch
+// fits in shared memory (or the tree is a single node).
+static int tc_work_bytes(int dtype, const dgb_contract_plan& p, int64_t B, size_t* bytes) {
+  *bytes = 0;
+  if (p.size == 1 || B == 0) return DGB_OK;
+  const size_t elem = dtype == DGB_F32 ? 4 : 8;
+  const size_t row = (size_t)tc_row_values(tc_counts(p)) * elem;
+  int dev = 0, optin = 0, sms = 0;
+  DGB_CUDA_CHECK(cudaGetDevice(&dev));
+  DGB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  DGB_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  if (row + tc_int_bytes(p) <= (size_t)optin) return DGB_OK;
+  const int64_t cap = (int64_t)sms * kGwBlocksPerSm;
+  *bytes = (size_t)(B < cap ? B : cap) * row;
   return DGB_OK;
 }
 
 template <typename T>
 static int launch_contract(int64_t B, const dgb_contract_plan& p, const void* d, const void* g,
-                           const void* rhs, void* x, cudaStream_t st) {
+                           const void* rhs, void* x, void* work, size_t work_bytes,
+                           cudaStream_t st) {
   if (p.size == 1) {
     single_node_kernel<T><<<(unsigned)((B + 255) / 256), 256, 0, st>>>(
         B, (const T*)d, (const T*)g, (const T*)rhs, (T*)x);
     DGB_LAUNCH_CHECK();
     return DGB_OK;
   }
-  const TcCounts c{p.size, p.n_segments, p.n_interior, p.n_retained,
-                   p.n_updates, p.n_rounds, p.n_eliminated, p.n_bridges};
-  const size_t smem = (size_t)tc_row_values(c) * sizeof(T) + 4 * (2 * (c.P + 1) + 2 * p.n_roots);
-  int dev = 0, optin = 0, sms = 0;
-  DGB_CUDA_CHECK(cudaGetDevice(&dev));
-  DGB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  DGB_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  if (smem > (size_t)optin) {
-    set_error("tree contraction scratch of %zu bytes per row exceeds shared memory", smem);
-    return DGB_ERANGE;
+  const TcCounts c = tc_counts(p);
+  size_t need = 0;
+  const int rc = tc_work_bytes(sizeof(T) == 4 ? DGB_F32 : DGB_F64, p, B, &need);
+  if (rc != DGB_OK) return rc;
+  const bool gw = need > 0;
+  if (gw && (work == nullptr || work_bytes < need)) {
+    set_error("tree contraction needs a %zu-byte workspace (dgb_tree_contract_work_size)", need);
+    return DGB_EINVAL;
   }
+  if (gw && ((uintptr_t)work % sizeof(T)) != 0) {
+    set_error("workspace must be aligned to the element size");
+    return DGB_EINVAL;
+  }
+  const size_t smem = gw ? tc_int_bytes(p) : (size_t)tc_row_values(c) * sizeof(T) + tc_int_bytes(p);
+  int dev = 0, sms = 0;
+  DGB_CUDA_CHECK(cudaGetDevice(&dev));
+  DGB_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int tpr = p.threads;
   if (tpr == 0) {  // by the widest phase: 128 threads from 80 items, 256 from 640
     const int wide = c.S > c.R ? c.S : c.R;
     tpr = wide > 640 ? 256 : (wide > 80 ? 128 : (wide > 40 ? 64 : 32));
   }
-  switch (tpr) {
-    case 32: return launch_tpr<T, 32>(B, p, c, smem, sms, d, g, rhs, x, st);
-    case 64: return launch_tpr<T, 64>(B, p, c, smem, sms, d, g, rhs, x, st);
-    case 128: return launch_tpr<T, 128>(B, p, c, smem, sms, d, g, rhs, x, st);
-    case 256: return launch_tpr<T, 256>(B, p, c, smem, sms, d, g, rhs, x, st);
-    default:
-      set_error("threads per row must be 0, 32, 64, 128 or 256; got %d", tpr);
-      return DGB_EINVAL;
+  if (gw) {
+    if (tpr == 256) return launch_tpr<T, 256, true>(B, p, c, smem, sms, d, g, rhs, x, work, st);
+    if (tpr == 32 || tpr == 64 || tpr == 128)
+      return launch_tpr<T, 128, true>(B, p, c, smem, sms, d, g, rhs, x, work, st);
+  } else {
+    switch (tpr) {
+      case 32: return launch_tpr<T, 32, false>(B, p, c, smem, sms, d, g, rhs, x, nullptr, st);
+      case 64: return launch_tpr<T, 64, false>(B, p, c, smem, sms, d, g, rhs, x, nullptr, st);
+      case 128: return launch_tpr<T, 128, false>(B, p, c, smem, sms, d, g, rhs, x, nullptr, st);
+      case 256: return launch_tpr<T, 256, false>(B, p, c, smem, sms, d, g, rhs, x, nullptr, st);
+      default: break;
+    }
   }
+  set_error("threads per row must be 0, 32, 64, 128 or 256; got %d", tpr);
+  return DGB_EINVAL;
 }
 
 }  // namespace dgb
@@ -373,7 +424,7 @@ using namespace dgb;
 
 extern "C" int dgb_tree_contract_solve(int dtype, int64_t B, const dgb_contract_plan* plan,
                                        const void* d, const void* g, const void* rhs, void* x,
-                                       void* stream) {
+                                       void* work, size_t work_bytes, void* stream) {
   clear_error();
   DGB_REQUIRE(dtype == DGB_F32 || dtype == DGB_F64, "dtype must be DGB_F32 or DGB_F64");
   DGB_REQUIRE(plan != nullptr, "plan must be non-null");
@@ -405,8 +456,17 @@ extern "C" int dgb_tree_contract_solve(int dtype, int64_t B, const dgb_contract_
                    (p.n_eliminated == 0 || ((uintptr_t)p.recovery & 15) == 0)),
               "plan record tables must be 16-byte aligned (endpoint 8-byte)");
   cudaStream_t st = as_stream(stream);
-  if (dtype == DGB_F32) return launch_contract<float>(B, p, d, g, rhs, x, st);
-  return launch_contract<double>(B, p, d, g, rhs, x, st);
+  if (dtype == DGB_F32) return launch_contract<float>(B, p, d, g, rhs, x, work, work_bytes, st);
+  return launch_contract<double>(B, p, d, g, rhs, x, work, work_bytes, st);
+}
+
+extern "C" size_t dgb_tree_contract_work_size(int dtype, const dgb_contract_plan* plan,
+                                              int64_t B) {
+  clear_error();
+  if (plan == nullptr || B < 0 || (dtype != DGB_F32 && dtype != DGB_F64)) return 0;
+  size_t bytes = 0;
+  if (tc_work_bytes(dtype, *plan, B, &bytes) != DGB_OK) return 0;
+  return bytes;
 }
 
 extern "C" size_t dgb_contract_plan_size(void) { return sizeof(dgb_contract_plan); }

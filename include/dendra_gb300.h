@@ -830,12 +830,18 @@ typedef struct dgb_contract_plan {
 /* B scalar Hines systems of plan->size nodes sharing the plan's topology:
  * d (shunt), g (conductance to the parent; a root's g is a second shunt), rhs
  * and x are (B, K) row-major:  d_i x_i + g_i (x_i - x_p(i)) + sum_c g_c (x_i - x_c)
- * = rhs_i.  One block per row, scratch in shared memory (errors DGB_ERANGE
- * when a row's scratch exceeds it); correctly rounded operations only.  x
+ * = rhs_i.  One block per row, scratch in shared memory, or in the caller's
+ * workspace when it does not fit; correctly rounded operations only.  x
  * must not alias an input.  Replaces tree_contraction.solve
  * (triton/tree_contraction.py:748-768; kernels :14-480). */
 int dgb_tree_contract_solve(int dtype, int64_t B, const dgb_contract_plan* plan, const void* d,
-                            const void* g, const void* rhs, void* x, void* stream);
+                            const void* g, const void* rhs, void* x, void* work,
+                            size_t work_bytes, void* stream);
+
+/* Workspace bytes dgb_tree_contract_solve needs for B rows: 0 when a row's
+ * scratch fits in shared memory, else (rows in flight) x (the row's scratch)
+ * for the same program run from global memory (trees of any size). */
+size_t dgb_tree_contract_work_size(int dtype, const dgb_contract_plan* plan, int64_t B);
 
 /* sizeof(dgb_contract_plan), for bindings that mirror the struct. */
 size_t dgb_contract_plan_size(void);

@@ -9,6 +9,8 @@
   against dense float64 autograd.
 """
 
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -175,11 +177,29 @@ def test_contract_errors(cuda):
         solve(x.half(), x.half(), x.half(), plan)
     with pytest.raises(ValueError, match="same-shaped strided CUDA"):
         solve(x, x.cpu(), x, plan)
-    # a row scratch larger than shared memory is refused before launch
+    # a tree whose scratch needs the global workspace refuses a launch without one
     big = TreeContractionPlan(np.arange(30000) - 1, None)
     y = torch.ones(1, 30000, device=cuda, dtype=torch.float64)
-    with pytest.raises(ValueError, match="shared memory"):
-        solve(y, y, y, big)
+    L = _lib.load()
+    st = big.struct(y.device)
+    assert L.dgb_tree_contract_work_size(1, ctypes.byref(st), 1) > 0
+    x = torch.empty_like(y)
+    assert L.dgb_tree_contract_solve(1, 1, ctypes.byref(st), y.data_ptr(), y.data_ptr(),
+                                     y.data_ptr(), x.data_ptr(), None, 0, None) == -1
     # empty batch
     e = torch.ones(0, 3, device=cuda)
     assert solve(e, e, e, plan).shape == (0, 3)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("cap", [16, None])
+def test_trees_beyond_shared_memory(cuda, dtype, cap):
+    # scratch in the global workspace: a 30,000-node cable and a 20,000-node
+    # branched tree, bit-exact against the oracle like the on-chip path
+    rng = np.random.default_rng(21)
+    for parent in (np.arange(30000) - 1, random_tree(rng, 20000, 0.02)):
+        K = parent.size
+        plan = TreeContractionPlan(parent, cap)
+        d, g, b = systems(rng, 3, K, NP[dtype])
+        x = solve(*(torch.as_tensor(a).to(cuda, dtype) for a in (d, g, b)), plan)
+        np.testing.assert_array_equal(x.cpu().numpy(), oracle.tree_contract_solve(d, g, b, plan.tables))

@@ -126,9 +126,11 @@ def test_struct_mirror_and_host_errors():
     plan.size = 4
     p = 16
     # bad dtype, null plan, inconsistent counts: rejected before any device work
-    assert L.dgb_tree_contract_solve(7, 1, ctypes.byref(plan), p, p, p, 32, None) == -1
-    assert L.dgb_tree_contract_solve(0, 1, None, p, p, p, 32, None) == -1
-    assert L.dgb_tree_contract_solve(0, 1, ctypes.byref(plan), p, p, p, 32, None) == -1
-    assert L.dgb_tree_contract_solve(0, 1, ctypes.byref(plan), p, p, p, p, None) == -1  # alias
-    assert L.dgb_tree_contract_solve(0, 0, ctypes.byref(plan), None, None, None, None,
+    assert L.dgb_tree_contract_solve(7, 1, ctypes.byref(plan), p, p, p, 32, None, 0, None) == -1
+    assert L.dgb_tree_contract_solve(0, 1, None, p, p, p, 32, None, 0, None) == -1
+    assert L.dgb_tree_contract_solve(0, 1, ctypes.byref(plan), p, p, p, 32, None, 0, None) == -1
+    assert L.dgb_tree_contract_solve(0, 1, ctypes.byref(plan), p, p, p, p, None, 0,
+                                     None) == -1  # alias
+    assert L.dgb_tree_contract_solve(0, 0, ctypes.byref(plan), None, None, None, None, None, 0,
                                      None) == 0  # empty batch
+    assert L.dgb_tree_contract_work_size(0, None, 4) == 0
