@@ -56,11 +56,14 @@ template <typename T>
 __global__ void __launch_bounds__(128) dhs_forest_kernel(ForestArgsT F, const T* __restrict__ d,
                                                          const T* __restrict__ g,
                                                          const T* __restrict__ b, T* __restrict__ x,
-                                                         int kmax) {
+                                                         int kmax, T* __restrict__ work) {
+  // work == nullptr: the accumulators in shared memory; else each warp's
+  // 2*kmax values in the global workspace (trees too large for shared memory)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
-  T* sD = reinterpret_cast<T*>(smem_raw) + (size_t)warp * 2 * kmax;
+  T* sD = (work ? work + (size_t)blockIdx.x * wpb * 2 * kmax : reinterpret_cast<T*>(smem_raw)) +
+          (size_t)warp * 2 * kmax;
   T* sB = sD + kmax;
   for (int tree = blockIdx.x * wpb + warp; tree < F.n_trees; tree += gridDim.x * wpb) {
     const int64_t base = F.shared_k > 0 ? (int64_t)tree * F.shared_k : F.node_ptr[tree];
@@ -86,23 +89,27 @@ static int forest_launch(const ForestArgsT& F, int kmax, const void* d, const vo
   const size_t per_warp = (size_t)2 * kmax * sizeof(T);
   int wpb = 4;
   while (wpb > 1 && wpb * per_warp > 227 * 1024) wpb >>= 1;
-  if (wpb * per_warp > 227 * 1024) {
-    set_error("tree of %d nodes too large for shared memory", kmax);
-    return DGB_ERANGE;
-  }
-  const size_t smem = wpb * per_warp;
+  // a tree too large for shared memory: the same program on a stream-ordered
+  // global workspace, four warps per block, four blocks per SM
+  const bool global = wpb * per_warp > 227 * 1024;
+  if (global) wpb = 4;
+  const size_t smem = global ? 0 : wpb * per_warp;
   DGB_CUDA_CHECK(cudaFuncSetAttribute(dhs_forest_kernel<T>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dhs_forest_kernel<T>,
                                                                wpb * 32, smem));
   if (per_sm < 1) per_sm = 1;
+  if (global) per_sm = 4;
   int blocks = device_sm_count() * per_sm;
   const int need = (F.n_trees + wpb - 1) / wpb;
   if (blocks > need) blocks = need;
+  T* work = nullptr;
+  if (global) DGB_CUDA_CHECK(cudaMallocAsync((void**)&work, (size_t)blocks * wpb * per_warp, st));
   dhs_forest_kernel<T><<<blocks, wpb * 32, smem, st>>>(F, (const T*)d, (const T*)g, (const T*)b,
-                                                       (T*)x, kmax);
+                                                       (T*)x, kmax, work);
   DGB_LAUNCH_CHECK();
+  if (global) DGB_CUDA_CHECK(cudaFreeAsync(work, st));
   return DGB_OK;
 }
 

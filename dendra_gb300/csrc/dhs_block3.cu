@@ -20,6 +20,8 @@
 
 namespace dgb {
 
+// work == nullptr: scratch in shared memory; else each block uses its slice
+// of 12*K values of the global workspace (trees too large for shared memory).
 template <typename T, bool TR>
 __global__ void __launch_bounds__(32)
     dhs_block3_kernel(int64_t B, int32_t K, int32_t L, const T* __restrict__ D,
@@ -27,9 +29,11 @@ __global__ void __launch_bounds__(32)
                       const int32_t* __restrict__ parent, const int32_t* __restrict__ order,
                       const int32_t* __restrict__ layer_ptr,
                       const int32_t* __restrict__ child_ptr,
-                      const int32_t* __restrict__ child_idx, T* __restrict__ x) {
+                      const int32_t* __restrict__ child_idx, T* __restrict__ x,
+                      T* __restrict__ work) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* sMinv = reinterpret_cast<T*>(smem_raw);  // [K][9]
+  T* sMinv = work ? work + (size_t)blockIdx.x * 12 * K
+                  : reinterpret_cast<T*>(smem_raw);  // [K][9]
   T* sY = sMinv + (size_t)9 * K;              // [K][3]: y, then x
   const int lane = threadIdx.x;
   for (int64_t tree = blockIdx.x; tree < B; tree += gridDim.x) {
@@ -105,29 +109,34 @@ static int launch_dhs_block3(int64_t B, int32_t K, int32_t L, const void* D, con
                              const int32_t* layer_ptr, const int32_t* child_ptr,
                              const int32_t* child_idx, void* x, int transpose,
                              cudaStream_t st) {
-  const size_t smem = (size_t)12 * K * sizeof(T);
-  int dev = 0, optin = 0;
+  const size_t scratch = (size_t)12 * K * sizeof(T);
+  int dev = 0, optin = 0, sms = 0;
   DGB_CUDA_CHECK(cudaGetDevice(&dev));
   DGB_CUDA_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  if (smem > (size_t)optin) {
-    set_error("tree of %d nodes too large for shared memory (%zu bytes)", K, smem);
-    return DGB_ERANGE;
-  }
-  const unsigned blocks = (unsigned)(B < 65535 * 32 ? B : 65535 * 32);
+  DGB_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // trees whose scratch does not fit on chip: a stream-ordered workspace of
+  // 16 trees per SM in flight
+  const bool global = scratch > (size_t)optin;
+  const int64_t cap = global ? (int64_t)sms * 16 : (int64_t)65535 * 32;
+  const unsigned blocks = (unsigned)(B < cap ? B : cap);
+  const size_t smem = global ? 0 : scratch;
+  T* work = nullptr;
+  if (global) DGB_CUDA_CHECK(cudaMallocAsync((void**)&work, (size_t)blocks * scratch, st));
   if (transpose) {
     DGB_CUDA_CHECK(cudaFuncSetAttribute(dhs_block3_kernel<T, true>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dhs_block3_kernel<T, true><<<blocks, 32, smem, st>>>(
         B, K, L, (const T*)D, (const T*)G, (const T*)rhs, parent, order, layer_ptr, child_ptr,
-        child_idx, (T*)x);
+        child_idx, (T*)x, work);
   } else {
     DGB_CUDA_CHECK(cudaFuncSetAttribute(dhs_block3_kernel<T, false>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dhs_block3_kernel<T, false><<<blocks, 32, smem, st>>>(
         B, K, L, (const T*)D, (const T*)G, (const T*)rhs, parent, order, layer_ptr, child_ptr,
-        child_idx, (T*)x);
+        child_idx, (T*)x, work);
   }
   DGB_LAUNCH_CHECK();
+  if (global) DGB_CUDA_CHECK(cudaFreeAsync(work, st));
   return DGB_OK;
 }
 

@@ -166,8 +166,9 @@ int dgb_block3_spd_solve_chol(int dtype, int64_t B, int64_t K, const void* lower
  *   A_ii = D_i + diag(g_i) + sum_children diag(g_c),  A_ic = A_ci = -diag(g_c).
  * parent / order / layer_ptr: the reference's plan (order deepest layer
  * first); child_ptr (K+1) / child_idx (K-1): children of every node.  One
- * warp per tree, children pulled in CSR order (deterministic); needs
- * 12*K*sizeof(T) bytes of shared memory.  transpose = 1 solves with main
+ * warp per tree, children pulled in CSR order (deterministic); 12*K*sizeof(T)
+ * bytes of scratch per tree, in shared memory or, for larger trees, in a
+ * stream-ordered global workspace.  transpose = 1 solves with main
  * blocks transposed (the adjoint system).  x must not alias rhs.
  * Replaces dhs_bt_solve_cuda (triton/dhs_kernel_bt.py:465-479).
  */

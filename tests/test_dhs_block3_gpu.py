@@ -85,3 +85,23 @@ def test_gradients_match_dense_autograd(cuda):
     (xd * w).sum().backward()
     for gk, t in zip(grads, (D, G, b)):
         torch.testing.assert_close(gk, t.grad, rtol=1e-9, atol=1e-10)
+
+
+def test_tree_beyond_shared_memory(cuda):
+    # 3,000 float64 nodes need 288 KB of scratch: the global-workspace path,
+    # checked by the residual of the block Hines system
+    rng = np.random.default_rng(30)
+    K = 3000
+    parent = _random_tree(rng, K, branch=5)
+    B = 3
+    D, G, b = _system(rng, B, K, parent)
+    Dt, Gt, bt = (torch.as_tensor(t, device=cuda) for t in (D, G, b))
+    x = dhs_bt_solve_cuda(Dt, Gt, bt, *_plan(parent, cuda))
+    par = torch.as_tensor(np.asarray(parent), device=cuda)
+    has = par >= 0
+    ps = par.clamp_min(0)
+    # D_i x_i + g_i (x_i - x_p) (root: g_i x_i) + sum_c g_c (x_i - x_c) - b_i
+    res = (Dt @ x.unsqueeze(-1)).squeeze(-1) + Gt * x - bt
+    res = res - torch.where(has.view(1, -1, 1), Gt * x[:, ps], torch.zeros_like(x))
+    res = res.index_add(1, ps[has], Gt[:, has] * x[:, ps[has]] - Gt[:, has] * x[:, has])
+    assert float(res.abs().max()) < 1e-10 * float(bt.abs().max())

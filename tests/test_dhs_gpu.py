@@ -140,3 +140,19 @@ def test_contract_errors(cuda):
         dhs_solve_cuda(d, d, d, *plan, threads=3)
     with pytest.raises(TypeError, match="int32 or int64"):
         dhs_solve_cuda(d, d, d, plan[0].float(), plan[1], plan[2])
+
+
+def test_tree_beyond_shared_memory(cuda):
+    # 40,000 float64 nodes: the accumulators live in a global workspace
+    rng = np.random.default_rng(40)
+    K = 40000
+    parent = _random_tree(rng, K)
+    B = 5
+    d = 1.0 + rng.random((B, K))
+    a = 0.5 * rng.random((B, K))
+    a[:, 0] = 0.0
+    b = rng.standard_normal((B, K))
+    p, order, lptr = _plan(parent, 32, cuda)
+    x = dhs_solve_cuda(*(torch.as_tensor(t, device=cuda) for t in (d, a, b)), p, order, lptr)
+    ref = oracle.dhs_solve(d, a, b, np.asarray(parent), order.cpu().numpy(), lptr.cpu().numpy())
+    np.testing.assert_allclose(x.cpu().numpy(), ref, rtol=1e-11, atol=1e-12)
