@@ -298,6 +298,89 @@ __global__ void __launch_bounds__(128) block3_kernel(int64_t B, int K, int ch,
     block_system<T, TR>(b, K, lower, mainb, upper, rhs, x, sm, ch);
 }
 
+// Systems whose chunk planes exceed shared memory: one thread per system runs
+// the serial block Thomas recurrence (the algorithm of the reference's
+// thomas_bt3_kernel, triton/bt_kernel.py:38-170) with the 3x3 factors
+// C'_k = M_k^-1 diag(upper_k) in a stream-ordered workspace and d'_k in x:
+//   M_k = main_k - diag(lower_{k-1}) C'_{k-1}
+//   d'_k = M_k^-1 (rhs_k - diag(lower_{k-1}) d'_{k-1}),  x_k = d'_k - C'_k x_{k+1}.
+template <typename T, bool TR>
+__global__ void __launch_bounds__(128)
+    block3_serial_kernel(int64_t B, int K, const T* __restrict__ lower,
+                         const T* __restrict__ mainb, const T* __restrict__ upper,
+                         const T* __restrict__ rhs, T* __restrict__ x, T* __restrict__ cp) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  // the transposed system: main blocks transposed, lower and upper exchanged
+  const T* lo = (TR ? upper : lower) + s * (int64_t)(K - 1) * 3;
+  const T* up = (TR ? lower : upper) + s * (int64_t)(K - 1) * 3;
+  const T* mb = mainb + s * (int64_t)K * 9;
+  const T* rs = rhs + s * (int64_t)K * 3;
+  T* xs = x + s * (int64_t)K * 3;
+  T* cps = cp + s * (int64_t)K * 9;
+  M3<T> cprev;
+  T dprev[3] = {T(0), T(0), T(0)};
+  for (int k = 0; k < K; ++k) {
+    M3<T> m;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) m.a[q] = TR ? mb[k * 9 + (q % 3) * 3 + q / 3] : mb[k * 9 + q];
+    T r[3] = {rs[k * 3], rs[k * 3 + 1], rs[k * 3 + 2]};
+    if (k > 0) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const T l = lo[(k - 1) * 3 + i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) m.a[i * 3 + j] -= l * cprev.a[i * 3 + j];
+        r[i] -= l * dprev[i];
+      }
+    }
+    const M3<T> mi = inv3(m);
+    mv(mi, r, dprev);
+    xs[k * 3] = dprev[0];
+    xs[k * 3 + 1] = dprev[1];
+    xs[k * 3 + 2] = dprev[2];
+    if (k + 1 < K) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) cprev.a[i * 3 + j] = mi.a[i * 3 + j] * up[k * 3 + j];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) cps[k * 9 + q] = cprev.a[q];
+    }
+  }
+  T xn[3] = {dprev[0], dprev[1], dprev[2]};
+  for (int k = K - 2; k >= 0; --k) {
+    M3<T> c;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) c.a[q] = cps[k * 9 + q];
+    T cx[3];
+    mv(c, xn, cx);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      xn[i] = xs[k * 3 + i] - cx[i];
+      xs[k * 3 + i] = xn[i];
+    }
+  }
+}
+
+template <typename T>
+static int block3_serial(int64_t B, int K, const void* lower, const void* mainb,
+                         const void* upper, const void* rhs, void* x, int transpose,
+                         cudaStream_t st) {
+  T* cp = nullptr;
+  DGB_CUDA_CHECK(cudaMallocAsync((void**)&cp, (size_t)B * K * 9 * sizeof(T), st));
+  const unsigned blocks = (unsigned)((B + 127) / 128);
+  if (transpose)
+    block3_serial_kernel<T, true><<<blocks, 128, 0, st>>>(
+        B, K, (const T*)lower, (const T*)mainb, (const T*)upper, (const T*)rhs, (T*)x, cp);
+  else
+    block3_serial_kernel<T, false><<<blocks, 128, 0, st>>>(
+        B, K, (const T*)lower, (const T*)mainb, (const T*)upper, (const T*)rhs, (T*)x, cp);
+  DGB_LAUNCH_CHECK();
+  DGB_CUDA_CHECK(cudaFreeAsync(cp, st));
+  return DGB_OK;
+}
+
 template <typename T>
 static int block3_t(int64_t B, int K, const void* lower, const void* mainb, const void* upper,
                     const void* rhs, void* x, int transpose, cudaStream_t st) {
@@ -305,11 +388,8 @@ static int block3_t(int64_t B, int K, const void* lower, const void* mainb, cons
   const size_t per_warp = (size_t)kBlockPlanes * ch * 32 * sizeof(T);
   int wpb = 4;
   while (wpb > 1 && wpb * per_warp > 227 * 1024) wpb >>= 1;
-  if (wpb * per_warp > 227 * 1024) {
-    set_error("K = %d needs %zu bytes of shared memory per system (limit %d)", K, per_warp,
-              227 * 1024);
-    return DGB_ERANGE;
-  }
+  if (K > 1024 || wpb * per_warp > 227 * 1024)  // the chunked kernel holds <= 32 rows per lane
+    return block3_serial<T>(B, K, lower, mainb, upper, rhs, x, transpose, st);
   const size_t smem = wpb * per_warp;
   auto kern = transpose ? block3_kernel<T, true> : block3_kernel<T, false>;
   DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -344,7 +424,7 @@ extern "C" int dgb_block3_solve(int dtype, int64_t B, int64_t K, const void* low
   (void)work;
   DGB_REQUIRE(dtype == DGB_F32 || dtype == DGB_F64, "dtype must be DGB_F32 or DGB_F64");
   DGB_REQUIRE(B >= 1 && K >= 1, "B and K must both be >= 1");
-  DGB_REQUIRE(K <= 1024, "K must be <= 1024, got %lld", (long long)K);
+  DGB_REQUIRE(K <= (1 << 26), "K must be <= 2^26, got %lld", (long long)K);
   DGB_REQUIRE(main_blocks && rhs && x, "main, rhs and x must be non-null");
   DGB_REQUIRE(K == 1 || (lower && upper), "lower and upper must be non-null when K > 1");
   DGB_REQUIRE(transpose == 0 || transpose == 1, "transpose must be 0 or 1");

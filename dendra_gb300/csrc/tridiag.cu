@@ -5,7 +5,8 @@
 // systems with a (B,K-1), b (B,K), c (B,K-1), d (B,K) -> x (B,K).
 //
 // One group of P lanes owns one system, CH rows per lane, held in registers
-// for the whole solve (see chunk_solve.cuh).  The reference kernels instead
+// for the whole solve (see chunk_solve.cuh); systems longer than 1024 rows
+// run a serial Thomas per thread.  The reference kernels instead
 // run one program per system with a scalar loop over K (Thomas) or stage
 // every PCR stage through global memory.
 #include "chunk_solve.cuh"
@@ -74,6 +75,62 @@ static int launch_p(int ch, int64_t B, int64_t K, const T* a, const T* b, const 
   return DGB_OK;
 }
 
+// Systems longer than the register-resident chunks hold (K > 1024): one
+// thread per system runs the reference's serial Thomas recurrence
+// (tridiag/pcr.py:125-183, the loop of t_kernel_thomas.py) with c' in a
+// stream-ordered workspace and d' in x, each operation rounded on its own
+// (no FMA contraction), so the result equals the sequential CPU Thomas bit
+// for bit.  d may alias x.
+__device__ __forceinline__ float tri_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double tri_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float tri_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double tri_div(double a, double b) { return __ddiv_rn(a, b); }
+
+template <typename T>
+__global__ void __launch_bounds__(128)
+    thomas_serial_kernel(int64_t B, int64_t K, const T* __restrict__ a, const T* __restrict__ b,
+                         const T* __restrict__ c, const T* d, T* x, T* __restrict__ cp) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= B) return;
+  const T* as = a + s * (K - 1);
+  const T* bs = b + s * K;
+  const T* cs = c + s * (K - 1);
+  const T* ds = d + s * K;
+  T* xs = x + s * K;
+  T* cps = cp + s * K;
+  T denom = bs[0];
+  T cprev = tri_div(cs[0], denom);
+  T dprev = tri_div(ds[0], denom);
+  cps[0] = cprev;
+  xs[0] = dprev;
+  for (int64_t i = 1; i < K; ++i) {
+    const T ai = as[i - 1];
+    denom = tri_sub(bs[i], mul_rn(ai, cprev));
+    if (i < K - 1) {
+      cprev = tri_div(cs[i], denom);
+      cps[i] = cprev;
+    }
+    dprev = tri_div(tri_sub(ds[i], mul_rn(ai, dprev)), denom);
+    xs[i] = dprev;
+  }
+  T xnext = dprev;
+  for (int64_t i = K - 2; i >= 0; --i) {
+    xnext = tri_sub(xs[i], mul_rn(cps[i], xnext));
+    xs[i] = xnext;
+  }
+}
+
+template <typename T>
+static int thomas_serial(int64_t B, int64_t K, const T* a, const T* b, const T* c, const T* d,
+                         T* x, cudaStream_t st) {
+  T* cp = nullptr;
+  DGB_CUDA_CHECK(cudaMallocAsync((void**)&cp, (size_t)B * K * sizeof(T), st));
+  thomas_serial_kernel<T><<<(unsigned)((B + 127) / 128), 128, 0, st>>>(B, K, a, b, c, d, x, cp);
+  DGB_LAUNCH_CHECK();
+  DGB_CUDA_CHECK(cudaFreeAsync(cp, st));
+  return DGB_OK;
+}
+
 // Lanes per system: wide enough that each lane holds at most 8 rows, and
 // always a power of two dividing 32.
 static int default_lanes(int64_t K, int method) {
@@ -99,10 +156,7 @@ static int solve_t(int method, int64_t B, int64_t K, const T* a, const T* b, con
     P = 32;
     ch = chunk_for(K, P);
   }
-  if (ch < 0) {
-    set_error("tridiagonal size K=%lld exceeds the supported maximum of 1024", (long long)K);
-    return DGB_ERANGE;
-  }
+  if (ch < 0) return thomas_serial<T>(B, K, a, b, c, d, x, st);
   switch (P) {
     case 4: return launch_p<T, 4>(ch, B, K, a, b, c, d, x, st);
     case 8: return launch_p<T, 8>(ch, B, K, a, b, c, d, x, st);

@@ -98,7 +98,9 @@ size_t dgb_cable_args_size(void);
  * register-resident chunked solve (sequential elimination inside each lane's
  * chunk, parallel cyclic reduction across lanes by warp shuffles); the method
  * selects the lanes per system (THOMAS: the autotuned split, PCR: the widest
- * split).  Replaces thomas_solve_cuda_t / pcr_solve_cuda_t.
+ * split).  Systems longer than 1024 rows run the sequential Thomas recurrence,
+ * one thread per system, bit-identical to the CPU Thomas.  Replaces
+ * thomas_solve_cuda_t / pcr_solve_cuda_t.
  */
 int dgb_tridiag_solve(int dtype, int method, int64_t B, int64_t K,
                       const void* a, const void* b, const void* c,
@@ -129,7 +131,8 @@ int dgb_tridiag_solve_transpose(int dtype, int64_t B, int64_t K,
  *   lower, upper: (B, K-1, 3); main: (B, K, 3, 3) row-major; rhs, x: (B, K, 3).
  * One warp per system: each lane eliminates its chunk of block rows (3x3
  * inverses by cofactors), the 32 reduced block rows are decoupled by block
- * PCR over warp shuffles, then back substitution; K <= 1024.
+ * PCR over warp shuffles, then back substitution; longer systems (whose
+ * chunk planes exceed shared memory) run a serial block Thomas per thread.
  * work: unused (may be NULL; dgb_block3_work_size returns 0).
  * transpose = 1 solves A^T y = rhs (the adjoint solve).  x must not alias rhs.
  * Replaces thomas_solve_cuda_bt (triton/bt_kernel.py:195-262), selected by

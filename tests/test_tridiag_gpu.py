@@ -80,6 +80,32 @@ def test_contract_errors(cuda):
         thomas_solve_cuda_t(b, b, a, b)
     with pytest.raises(ValueError, match="same dtype"):
         thomas_solve_cuda_t(a, b.double(), a, b)
+    # no length limit: 1,100 rows run the sequential recurrence
     big = torch.ones(1, 1100, device=cuda)
-    with pytest.raises(ValueError, match="maximum"):
-        thomas_solve_cuda_t(big[:, 1:], big, big[:, 1:], big)
+    x = thomas_solve_cuda_t(-0.25 * big[:, 1:], big, -0.25 * big[:, 1:], big)
+    assert torch.isfinite(x).all()
+
+
+@pytest.mark.parametrize("K", [1025, 5000])
+def test_long_systems_equal_sequential_thomas(cuda, K):
+    # beyond the register-resident chunks: the serial recurrence, bit-identical
+    # to the oracle's sequential Thomas in both precisions
+    rng = np.random.default_rng(K)
+    B = 300
+    a = -rng.random((B, K - 1))
+    c = -rng.random((B, K - 1))
+    b = 2.2 + rng.random((B, K))
+    d = rng.standard_normal((B, K))
+    for dt in (np.float64, np.float32):
+        args = [torch.as_tensor(t.astype(dt), device=cuda) for t in (a, b, c, d)]
+        ref = oracle.thomas(*(t.astype(dt) for t in (a, b, c, d)))
+        np.testing.assert_array_equal(thomas_solve_cuda_t(*args).cpu().numpy(), ref)
+        np.testing.assert_array_equal(pcr_solve_cuda_t(*args).cpu().numpy(), ref)
+    # the adjoint (transpose solve) of a long system
+    at, bt, ct, dtn = (torch.as_tensor(t[:3], device=cuda).requires_grad_() for t in (a, b, c, d))
+    w = torch.as_tensor(rng.standard_normal((3, K)), device=cuda)
+    (thomas_solve_cuda_t(at, bt, ct, dtn) * w).sum().backward()
+    A = (torch.diag_embed(bt.detach()) + torch.diag_embed(at.detach(), -1)
+         + torch.diag_embed(ct.detach(), 1))
+    g = torch.linalg.solve(A.transpose(-1, -2), w)
+    torch.testing.assert_close(dtn.grad, g, rtol=1e-9, atol=1e-11)
