@@ -128,11 +128,13 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
       sD[i] = D;
       sB[i] = Bv;
       // up the chain (the single child of node j is the node below it); the
-      // next node's index and values are loaded one node ahead, before this
-      // node's division and stores (chains are disjoint: nothing else writes them)
+      // next node's values and the index after it are loaded ahead, before
+      // this node's division and stores, so neither load waits on the other
+      // (chains are disjoint: nothing else writes them)
       T gc = g[i];
       int q = p + 1;
       int j = q < e ? c.nodes[q] : 0;
+      int jn = q + 1 < e ? c.nodes[q + 1] : 0;
       T dj = T(0), bj = T(0), gj = T(0);
       if (q < e) {
         dj = sD[j];
@@ -140,10 +142,9 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
         gj = g[j];
       }
       for (; q < e; ++q) {
-        int jn = 0;
+        const int jnn = q + 2 < e ? c.nodes[q + 2] : 0;
         T dn = T(0), bn = T(0), gn = T(0);
         if (q + 1 < e) {
-          jn = c.nodes[q + 1];
           dn = sD[jn];
           bn = sB[jn];
           gn = g[jn];
@@ -155,6 +156,7 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
         sB[j] = Bv;
         gc = gj;
         j = jn;
+        jn = jnn;
         dj = dn;
         bj = bn;
         gj = gn;
@@ -174,14 +176,15 @@ __device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const Ch
       const int p = c.chain_ptr[ch], e = c.chain_ptr[ch + 1];
       const I par = t.parent[c.nodes[e - 1]];
       T xp = has_parent(par) ? sB[par] : T(0);
-      // down the chain from its top, the next node's loads one node ahead
+      // down the chain from its top: the next node's values and the index
+      // after it loaded ahead
       int j = c.nodes[e - 1];
+      int jn = e - 2 >= p ? c.nodes[e - 2] : 0;
       T bj = sB[j], dj = sD[j], gj = g[j];
       for (int q = e - 1; q >= p; --q) {
-        int jn = 0;
+        const int jnn = q - 2 >= p ? c.nodes[q - 2] : 0;
         T bn = T(0), dn = T(0), gn = T(0);
         if (q > p) {
-          jn = c.nodes[q - 1];
           bn = sB[jn];
           dn = sD[jn];
           gn = g[jn];
@@ -189,6 +192,7 @@ __device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const Ch
         xp = (bj + gj * xp) / (dj + gj);
         sB[j] = xp;
         j = jn;
+        jn = jnn;
         bj = bn;
         dj = dn;
         gj = gn;
