@@ -666,8 +666,8 @@ def bench_tree(args, world, rank, local):
     """Tree solves of branched cells: B = 8192 systems sharing one ~2000-node
     topology (the C3 cell morphology), float32; one bench step = one batched
     tree-contraction solve (segments of <= 16 interior nodes, rake/compress
-    rounds).  The DHS depth-layer solve of the same systems is timed beside
-    it.  Inputs exceed L2 (262 MB)."""
+    rounds).  The DHS solve of the same systems (dhs_solve_cuda, chain
+    schedule) is timed beside it.  Inputs exceed L2 (262 MB)."""
     import torch
 
     import oracle
@@ -752,7 +752,7 @@ def bench_tree(args, world, rank, local):
         "gpu_launches": args.steps,
         "clocks": clocks.summary(),
         "dhs_same_systems": {"ms_per_step": ms_dhs, "value": units / (ms_dhs * 1e-3),
-                             "kernel": "dhs_forest_kernel (depth layers)"},
+                             "kernel": "dhs_forest_kernel (chain schedule, one warp per tree)"},
         "max_rel_diff_vs_cpu_dhs_f32": rel,
         "bit_exact_vs_oracle_rows_0_3": bool(np.array_equal(x[:4].cpu().numpy(), exact)),
         "agrees_with_gpu_dhs_rel": float((x - x_dhs).abs().max() / x_dhs.abs().max()),

@@ -26,6 +26,12 @@ struct ForestArgsT {
   // optional per-tree node counts (row-padded planes: tree t's K_t nodes
   // start at node_ptr[t]); NULL: K_t = node_ptr[t+1] - node_ptr[t]
   const int32_t* tree_k;
+  // optional chain schedule of every plan (dgb_forest's chain arrays)
+  const int64_t* plan_chain_off;
+  const int64_t* plan_clevel_off;
+  const int32_t* chain_nodes;
+  const int32_t* chain_ptr;
+  const int32_t* chain_level;
 };
 
 __device__ __forceinline__ TreeTopo forest_topo(const ForestArgsT& F, int plan, int K) {
@@ -76,8 +82,19 @@ __global__ void __launch_bounds__(128) dhs_forest_kernel(ForestArgsT F, const T*
       sB[i] = b[base + i];
     }
     __syncwarp();
-    dhs_eliminate<T, int32_t>(t, g + base, sD, sB, lane);
-    dhs_substitute<T, int32_t>(t, g + base, sD, sB, lane);
+    if (F.chain_nodes && F.shared_k == 0) {
+      // chain schedule: one lane per unbranched chain, a sync per chain level
+      // (the same operations per node as the layer schedule)
+      const int64_t pn = F.plan_node_ptr[plan];
+      const int64_t cp0 = F.plan_chain_off[plan], cl0 = F.plan_clevel_off[plan];
+      const ChainTopoT<int32_t> ct{F.chain_nodes + pn, F.chain_ptr + cp0, F.chain_level + cl0,
+                                   (int32_t)(F.plan_clevel_off[plan + 1] - cl0 - 1)};
+      chain_eliminate<T, int32_t>(t, ct, g + base, sD, sB, lane);
+      chain_substitute<T, int32_t>(t, ct, g + base, sD, sB, lane);
+    } else {
+      dhs_eliminate<T, int32_t>(t, g + base, sD, sB, lane);
+      dhs_substitute<T, int32_t>(t, g + base, sD, sB, lane);
+    }
     for (int i = lane; i < K; i += 32) x[base + i] = sB[i];
     __syncwarp();
   }
@@ -139,7 +156,12 @@ extern "C" int dgb_dhs_solve_forest(int dtype, const dgb_forest* forest, const v
   DGB_REQUIRE(forest->n_trees >= 0, "n_trees must be >= 0");
   ForestArgsT F{forest->n_trees, 0, 0, forest->node_ptr, forest->plan_of, forest->plan_node_ptr,
                 forest->plan_layer_off, forest->parent, forest->order, forest->layer_ptr,
-                forest->child_ptr, forest->child_idx, forest->tree_k};
+                forest->child_ptr, forest->child_idx, forest->tree_k,
+                forest->plan_chain_off, forest->plan_clevel_off, forest->chain_nodes,
+                forest->chain_ptr, forest->chain_level};
+  DGB_REQUIRE(!F.chain_nodes || (F.chain_ptr && F.chain_level && F.plan_chain_off &&
+                                 F.plan_clevel_off),
+              "the chain schedule needs chain_ptr, chain_level and their plan offsets");
   return forest_dispatch(dtype, F, forest->max_k, d, a, b, x, stream);
 }
 
@@ -154,6 +176,7 @@ extern "C" int dgb_dhs_solve(int dtype, int64_t B, int64_t K, const void* d, con
   DGB_REQUIRE(n_layers >= 1, "layer_ptr must contain at least two entries");
   DGB_REQUIRE(B <= INT32_MAX && K <= INT32_MAX, "too many trees or nodes");
   ForestArgsT F{(int32_t)B, (int32_t)K, n_layers, nullptr, nullptr, nullptr, nullptr,
-                parent,     order,      layer_ptr, child_ptr, child_idx, nullptr};
+                parent,     order,      layer_ptr, child_ptr, child_idx, nullptr,
+                nullptr,    nullptr,    nullptr,   nullptr,   nullptr};
   return forest_dispatch(dtype, F, (int)K, d, a, b, x, stream);
 }

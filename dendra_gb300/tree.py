@@ -165,17 +165,35 @@ def _device_topology(parent_idx, order, layer_ptr):
     return topo
 
 
+_chain_cache: dict = {}
+
+
+def _chain_forest(topo, B):
+    """Chain-schedule forest of B copies of ``topo``'s tree (cached): the
+    elimination runs one lane per unbranched chain with a sync per chain
+    level, the same per-node operations as the depth-layer schedule."""
+    key = (id(topo), B)
+    hit = _chain_cache.get(key)
+    if hit is None or hit[0] is not topo:
+        if len(_chain_cache) > 64:
+            _chain_cache.clear()
+        parent = [int(p) for p in topo[0].detach().cpu().numpy()]
+        plan = ForestPlan([parent], device=topo[0].device, plan_of=np.zeros(B, dtype=np.int32),
+                          chains=True)
+        hit = _chain_cache[key] = (topo, plan)
+    return hit[1]
+
+
 def _solve(d, a, b, topo):
-    parent, order, layer_ptr, cptr, cidx = topo
     B, K = d.shape
     d, a, b = (t.contiguous() for t in (d, a, b))
     x = torch.empty_like(b)
+    f = _chain_forest(topo, B).struct()
     with torch.cuda.device(d.device):
-        rc = _lib.load().dgb_dhs_solve(
-            _lib.dtype_code(d.dtype), B, K, d.data_ptr(), a.data_ptr(), b.data_ptr(),
-            parent.data_ptr(), order.data_ptr(), layer_ptr.data_ptr(), layer_ptr.numel() - 1,
-            cptr.data_ptr(), cidx.data_ptr(), x.data_ptr(), _lib.stream_ptr(d.device))
-    _lib.check(rc, "dgb_dhs_solve")
+        rc = _lib.load().dgb_dhs_solve_forest(_lib.dtype_code(d.dtype), ctypes.byref(f),
+                                              d.data_ptr(), a.data_ptr(), b.data_ptr(),
+                                              x.data_ptr(), _lib.stream_ptr(d.device))
+    _lib.check(rc, "dgb_dhs_solve_forest")
     return x
 
 
@@ -205,7 +223,9 @@ def dhs_solve_cuda(d_mem, a_geom, b, parent_idx, order, layer_ptr, threads=32):
 
     All (B, K) tensors are in the solver order that ``order``/``layer_ptr``
     index; ``threads`` is validated like the reference (it sets the layer
-    chunking there; this kernel always runs one warp per tree).
+    chunking there).  One warp per tree runs the chain schedule of the same
+    elimination (one lane per unbranched chain), which gives the depth-layer
+    schedule's results bit for bit.
     """
     validate_tree(d_mem, a_geom, b, parent_idx, order, layer_ptr, threads)
     topo = _device_topology(parent_idx, order, layer_ptr)
@@ -561,7 +581,7 @@ class _MultiPlan:
         self.forest = None
         if self.n_trees:
             f = ForestPlan([list(map(int, p)) for p in parents], device=device,
-                           plan_of=tree_morph, chains=False)
+                           plan_of=tree_morph, chains=True)
             rows = np.asarray(tree_rows, dtype=np.int64)
             k_of = np.asarray([len(parents[m]) for m in tree_morph], dtype=np.int32)
             node_ptr = np.append(rows * K_stride, B * K_stride).astype(np.int64)

@@ -400,7 +400,8 @@ typedef struct dgb_forest {
      its chain_level (n_levels_p + 1 offsets into its chains; level-0 chains
      end in leaves, a level-l chain ends in a branch node whose child chains
      have lower levels) at plan_clevel_off[p].  Same results as the layer
-     schedule; used by dgb_net_window. */
+     schedule; used by dgb_net_window and, one warp per tree, by
+     dgb_dhs_solve_forest. */
   const int64_t* plan_chain_off;
   const int64_t* plan_clevel_off;
   const int32_t* chain_nodes;

@@ -156,3 +156,31 @@ def test_tree_beyond_shared_memory(cuda):
     x = dhs_solve_cuda(*(torch.as_tensor(t, device=cuda) for t in (d, a, b)), p, order, lptr)
     ref = oracle.dhs_solve(d, a, b, np.asarray(parent), order.cpu().numpy(), lptr.cpu().numpy())
     np.testing.assert_allclose(x.cpu().numpy(), ref, rtol=1e-11, atol=1e-12)
+
+
+def test_chain_and_layer_schedules_are_bit_identical(cuda):
+    # dhs_solve_cuda runs the chain schedule; the C entry dgb_dhs_solve the
+    # depth-layer schedule of the same elimination
+    import ctypes
+
+    from dendra_gb300 import _lib
+    from dendra_gb300.tree import _device_topology
+
+    rng = np.random.default_rng(77)
+    for K, dt in ((1, torch.float64), (2, torch.float32), (333, torch.float32),
+                  (1500, torch.float64)):
+        parent = _random_tree(rng, K)
+        B = 65
+        d = torch.as_tensor(1.0 + rng.random((B, K)), device=cuda, dtype=dt)
+        a = torch.as_tensor(0.5 * rng.random((B, K)), device=cuda, dtype=dt)
+        b = torch.as_tensor(rng.standard_normal((B, K)), device=cuda, dtype=dt)
+        p, order, lptr = _plan(parent, 32, cuda)
+        x = dhs_solve_cuda(d, a, b, p, order, lptr)
+        par, o, lp, cptr, cidx = _device_topology(p, order, lptr)
+        y = torch.empty_like(b)
+        rc = _lib.load().dgb_dhs_solve(_lib.dtype_code(dt), B, K, d.data_ptr(), a.data_ptr(),
+                                       b.data_ptr(), par.data_ptr(), o.data_ptr(), lp.data_ptr(),
+                                       lp.numel() - 1, cptr.data_ptr(), cidx.data_ptr(),
+                                       y.data_ptr(), _lib.stream_ptr(cuda))
+        assert rc == 0
+        torch.testing.assert_close(x, y, rtol=0, atol=0)
