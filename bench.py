@@ -1204,6 +1204,7 @@ def main():
     import torch
 
     import dendra_gb300
+    from dendra_gb300.shards import reduce_timing
     from dendra_gb300.workloads import C2_STEPS, cable_population_c2
 
     torch.cuda.set_device(local)
@@ -1266,15 +1267,8 @@ def main():
         torch.cuda.synchronize()
         barrier()
     ms = float(np.mean(times))
-    if pg is not None:
-        t = torch.tensor([ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-        n = torch.tensor([comp_steps], dtype=torch.float64, device=dev)
-        pg.all_reduce(n)
-        total_units = float(n.item())
-    else:
-        total_units = float(comp_steps)
+    # slowest rank's time, work summed over ranks (unchanged at one rank)
+    ms, total_units = reduce_timing(ms, comp_steps, device=dev)
     value = total_units / (ms * 1e-3)
 
     # ---- end-to-end through the public API from pinned host buffers ----
@@ -1308,10 +1302,7 @@ def main():
             e2e_step()
         torch.cuda.synchronize()
         e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    if pg is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms, _ = reduce_timing(e2e_ms, 0, device=dev)
     e2e_value = total_units / (e2e_ms * 1e-3)
     n_spiking = int((out_cnt > 0).sum())
 
