@@ -184,6 +184,21 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+COVERED_TIMING = ("CUDA events on the launching stream; a 0.1 ms device sleep before the "
+                  "start event keeps host enqueue out of the events")
+
+
+def _cover_enqueue():
+    """Queue a short device sleep (about 0.1 ms) right before a start event, so
+    the stream is still busy while the host enqueues the event and the timed
+    launch: the events then bracket the kernel, not host enqueue latency.  The
+    sleep runs before the start event and is not timed.  Host overhead is in
+    each line's ``e2e`` figure instead."""
+    import torch
+
+    torch.cuda._sleep(200_000)
+
+
 def _dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -543,6 +558,7 @@ def bench_c4(args, world, rank, local):
 
 
 BT_BYTES_PER_ROW = 84  # float32 block row: main 36 B + lower/upper 24 B + rhs 12 B + x 12 B
+BT_NCU_TRAFFIC = 236751104 + 28013056  # dram read + write of one 16,384 x 201 launch (ncu)
 
 
 def _bt_system(B, K, seed, dtype):
@@ -586,6 +602,7 @@ def bench_bt(args, world, rank, local):
             flush.sum()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            _cover_enqueue()
             e0.record(st)
             x = _block3(lower, main, upper, rhs, False)
             e1.record(st)
@@ -618,12 +635,15 @@ def bench_bt(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": "bt-3x3-block-tridiagonal", "systems": B, "K": K,
-                   "l2": "flushed between timed steps"},
+                   "l2": "flushed between timed steps",
+                   "timing": COVERED_TIMING},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "block3_kernel",
+                     "frac": achieved / peak, "kernel": "block3_kernel",
+                     "traffic": BT_NCU_TRAFFIC if (B, K) == (16384, 201) else None,
                      "note": f"{BT_BYTES_PER_ROW} algorithmic B per float32 block row (read "
                              "main, bands and rhs, write x); one warp per system, factors "
-                             f"in shared memory; peak {peak_kind}"},
+                             "in shared memory; traffic = DRAM read + write of one launch "
+                             f"under ncu; peak {peak_kind}"},
         "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": args.steps * 2,
@@ -632,6 +652,112 @@ def bench_bt(args, world, rank, local):
         "cpu_baseline": {"value": n_cpu * K / cpu_s, "unit": metric,
                          "cores": oracle.num_threads(), "kind": "port",
                          "sample": f"{n_cpu} systems x {K} block rows, float32 block Thomas"},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+TRIDIAG_BYTES_PER_ROW = 20  # float32 row: read a, b, c, d, write x
+TRIDIAG_NCU_TRAFFIC = 105014272 + 7976704  # dram read + write of one 16,384 x 401 launch (ncu)
+
+
+def _tridiag_system(B, K, seed, dtype):
+    """B diagonally dominant cable-like systems of K rows (the shape the
+    backward-Euler cable update hands its solver): off-diagonals -U[0.05, 1],
+    diagonal 1 + |a| + |c| + U[0, 0.5], right-hand side N(0, 1)."""
+    import torch
+
+    g = torch.Generator().manual_seed(seed)
+    a = -(0.05 + 0.95 * torch.rand(B, K - 1, generator=g, dtype=torch.float64))
+    c = -(0.05 + 0.95 * torch.rand(B, K - 1, generator=g, dtype=torch.float64))
+    b = 1.0 + 0.5 * torch.rand(B, K, generator=g, dtype=torch.float64)
+    b[:, 1:] -= a
+    b[:, :-1] -= c
+    d = torch.randn(B, K, generator=g, dtype=torch.float64)
+    return [t.to(dtype).contiguous() for t in (a, b, c, d)]
+
+
+def bench_tridiag(args, world, rank, local):
+    """The drop-in batched tridiagonal solve (thomas_solve_cuda_t's kernel,
+    dgb_tridiag_solve): 16,384 systems of 401 rows (the largest cable of the
+    uneven population), float32.  One bench step = one batched solve; L2 is
+    flushed between steps."""
+    import torch
+
+    import oracle
+    from dendra_gb300 import _lib
+    from dendra_gb300.solvers import _solve, thomas_solve_cuda_t
+
+    B = args.cables
+    K = args.timesteps or 401
+    units = B * K
+    metric = "row-solves/s"
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    host = _tridiag_system(B, K, 11 + rank, torch.float32)
+    a, b, c, d = (t.to(dev) for t in host)
+    for _ in range(max(3, args.warmup)):
+        _solve(a, b, c, d, _lib.THOMAS)
+    torch.cuda.synchronize()
+    flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.sum()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            _cover_enqueue()
+            e0.record(st)
+            x = _solve(a, b, c, d, _lib.THOMAS)
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    # end to end through the drop-in callable, from and to pinned host memory
+    pinned = [t.pin_memory() for t in host]
+    out = torch.empty_like(host[3]).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in pinned)
+    d2h = out.numel() * out.element_size()
+    dbuf = [torch.empty_like(t, device=dev) for t in host]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for d_, h_ in zip(dbuf, pinned):
+            d_.copy_(h_, non_blocking=True)
+        out.copy_(thomas_solve_cuda_t(*dbuf), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    peak, peak_kind = _peaks()
+    achieved = TRIDIAG_BYTES_PER_ROW * units / (ms * 1e-3) / 1e9
+    n_cpu = B
+    sample = [t[:n_cpu].numpy() for t in host]
+    t0 = time.perf_counter()
+    ref = oracle.thomas(*sample)
+    cpu_s = time.perf_counter() - t0
+    err = float(np.abs(x[:n_cpu].cpu().numpy() - ref).max())
+    line = {
+        "metric": metric, "value": units / (ms * 1e-3), "unit": metric, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "tridiag-cable-systems", "systems": B, "K": K,
+                   "l2": "flushed between timed steps (256 MiB read, outside the events)",
+                   "timing": COVERED_TIMING},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "kernel": "tridiag_kernel",
+                     "traffic": TRIDIAG_NCU_TRAFFIC if (B, K) == (16384, 401) else None,
+                     "note": f"{TRIDIAG_BYTES_PER_ROW} algorithmic B per float32 row (read "
+                             "a, b, c, d, write x); traffic = DRAM read + write of one "
+                             f"launch under ncu; peak {peak_kind}"},
+        "e2e": {"value": units / e2e_s, "unit": metric, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps * 2,
+        "clocks": clocks.summary(),
+        "max_abs_diff_vs_oracle_f32": err,
+        "cpu_baseline": {"value": n_cpu * K / cpu_s, "unit": metric,
+                         "cores": oracle.num_threads(), "kind": "port",
+                         "sample": f"{n_cpu} systems x {K} rows, float32 Thomas"},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -699,6 +825,7 @@ def bench_tree(args, world, rank, local):
             flush.sum()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            _cover_enqueue()
             e0.record(st)
             out = fn()
             e1.record(st)
@@ -739,7 +866,8 @@ def bench_tree(args, world, rank, local):
         "data": "synthetic",
         "config": {"workload": "tree-contraction-solve", "systems": B, "K": K,
                    "segment_cap": 16, "segments": c["n_segments"], "retained": c["n_retained"],
-                   "rounds": c["n_rounds"], "l2": "flushed between timed steps"},
+                   "rounds": c["n_rounds"], "l2": "flushed between timed steps",
+                   "timing": COVERED_TIMING},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": TREE_NCU_TRAFFIC if B == 8192 else None,
                      "kernel": "tree_contract_kernel",
@@ -1173,13 +1301,14 @@ def main():
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c3", "c4", "c5", "bt", "delay", "tree"],
+                    choices=["c2", "c3", "c4", "c5", "bt", "delay", "tree", "tridiag"],
                     help="c2: uneven cable population (default); c3: branched-cell network; "
                          "c4: adjoint gradient of a trace fit; "
                          "c5: learned threshold proposal vs plain bisection; "
                          "bt: 3x3 block-tridiagonal (multi-layer extracellular) solves; "
                          "delay: differentiable two-tap event transport rollout; "
-                         "tree: tree-contraction solves of branched cells")
+                         "tree: tree-contraction solves of branched cells; "
+                         "tridiag: the drop-in batched tridiagonal solve")
     ap.add_argument("--train", type=int, default=200000, help="c5 training thresholds")
     ap.add_argument("--cables", type=int, default=16384,
                     help="cables per rank (a smaller case for profiling)")
@@ -1198,6 +1327,8 @@ def main():
         return bench_delay(args, world, rank, local)
     if args.workload == "tree":
         return bench_tree(args, world, rank, local)
+    if args.workload == "tridiag":
+        return bench_tridiag(args, world, rank, local)
     if args.impl == "reference":
         return run_reference(args, world, rank)
 

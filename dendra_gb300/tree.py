@@ -664,7 +664,7 @@ def dhs_solve_multi_cuda(d_mem, a_geom, b, P_cat, ORDER_cat, LAYER_PTR_cat, WARP
     (the last layer ends at the morphology's node count).  Every covered row
     is one tree in a single dgb_dhs_solve_forest launch (rows read in place);
     entries past a morphology's nodes and uncovered rows return 0.  The
-    elimination order is this build's own (deterministic, children pulled in
+    elimination order is this library's own (deterministic, children pulled in
     index order), so ORDER_cat only has to be a valid plan.  Gradients follow
     DHSSolveMultiPacked.backward (dhs_kernel_multi.py:699-780)."""
     plan = (P_cat, ORDER_cat, LAYER_PTR_cat, WARP_P_OFF, WARP_ORDER_OFF, WARP_LPTR_OFF, WARP_L,

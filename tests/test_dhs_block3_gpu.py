@@ -1,7 +1,7 @@
 """3x3 block tree solves (multi-layer extracellular trees) on the GPU against the
 dense matrix the reference's dhs_kernel_bt.py factors (the reference's own
 block tree solvers need Triton on a GPU or the absent dendra-solvers package,
-so the dense restatement is the judge), with gradients against dense autograd."""
+so the dense restatement is the accuracy reference), with gradients against dense autograd."""
 
 import numpy as np
 import pytest
