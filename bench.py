@@ -384,7 +384,7 @@ def _c4_cpu(n_sample, n_steps, seed=4):
     import torch
 
     import oracle
-    from dendra_gb300.workloads import c4_spec, cable_population_c4
+    from dendra_gb300.workloads import cable_population_c4
 
     pop, spec = cable_population_c4(n_sample, seed=seed, dtype=torch.float32, device="cpu")
     p = pop.problem_dict()

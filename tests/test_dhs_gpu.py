@@ -161,8 +161,6 @@ def test_tree_beyond_shared_memory(cuda):
 def test_chain_and_layer_schedules_are_bit_identical(cuda):
     # dhs_solve_cuda runs the chain schedule; the C entry dgb_dhs_solve the
     # depth-layer schedule of the same elimination
-    import ctypes
-
     from dendra_gb300 import _lib
     from dendra_gb300.tree import _device_topology
 

@@ -9,7 +9,6 @@ import torch
 from dendra_gb300 import functional as F
 from dendra_gb300.solvers import solve_bt_spd_cuda, thomas_solve_cuda_bt, thomas_solve_cuda_t
 from dendra_gb300.tree import build_dhs_layers, build_morphology, dhs_solve_cuda
-from tests.test_contraction_plan import random_tree
 from tests.test_dhs_multi_gpu import case as multi_case
 from tests.test_dhs_multi_gpu import hines_dense
 
