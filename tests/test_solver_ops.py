@@ -22,6 +22,22 @@ def test_fake_rule_gives_the_solution_shape():
         assert y.shape == (4, 10)
 
 
+def test_contract_errors_before_any_device_work():
+    """Shape and device checks run on the host, with the reference's messages
+    (triton/_contracts.py:87-159), so they raise without a GPU."""
+    from dendra_gb300.solvers import pcr_solve_cuda_t
+
+    a, c = torch.zeros(2, 3), torch.zeros(2, 3)
+    b, d = torch.ones(2, 4), torch.zeros(2, 4)
+    for solve in (thomas_solve_cuda_t, pcr_solve_cuda_t):
+        with pytest.raises(ValueError, match="must be CUDA tensors"):
+            solve(a, b, c, d)
+        with pytest.raises(ValueError, match=r"d must have shape \(2, 4\), got \(2, 5\)"):
+            solve(a, b, c, torch.zeros(2, 5))
+        with pytest.raises(ValueError, match=r"a must have shape \(2, 3\)"):
+            solve(b, b, c, d)
+
+
 def _system(rng, B, K, dev):
     a = -rng.random((B, K - 1))
     c = -rng.random((B, K - 1))
