@@ -256,6 +256,35 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+
+def _reference_solve_line(args, world, metric, cfg, units, solve, sample):
+    """Reference arm of a single-solve workload: the oracle's CPU restatement
+    of the reference solver (all host threads it uses), timed with
+    perf_counter over ``args.steps`` solves after ``args.warmup`` warm-up
+    solves; prints the reference JSON line."""
+    import oracle
+
+    for _ in range(args.warmup):
+        solve()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        solve()
+        times.append(time.perf_counter() - t0)
+    secs = float(np.mean(times))
+    value = units / secs
+    line = {
+        "impl": "reference", "metric": metric, "value": value, "unit": metric, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": metric, "cores": oracle.num_threads(),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": metric, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
 C3_BYTES_PER_COMP_STEP = 24  # unfused tree step: v r/w 8 B + main/rhs/axial/parent 16 B
 
 
@@ -587,6 +616,15 @@ def bench_bt(args, world, rank, local):
     K = args.timesteps or 201
     units = B * K
     metric = "compartment-solves/s"
+    if args.impl == "reference":
+        if rank == 0:
+            arrays = [t.numpy() for t in _bt_system(B, K, 7, torch.float32)]
+            _reference_solve_line(
+                args, world, metric, {"workload": "bt-3x3-block-tridiagonal", "systems": B,
+                                      "K": K},
+                units, lambda: oracle.block3_solve(*arrays),
+                f"all {B} systems x {K} block rows per step, float32 block Thomas")
+        return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     host = _bt_system(B, K, 7 + rank, torch.float32)
@@ -692,6 +730,14 @@ def bench_tridiag(args, world, rank, local):
     K = args.timesteps or 401
     units = B * K
     metric = "row-solves/s"
+    if args.impl == "reference":
+        if rank == 0:
+            arrays = [t.numpy() for t in _tridiag_system(B, K, 11, torch.float32)]
+            _reference_solve_line(
+                args, world, metric, {"workload": "tridiag-cable-systems", "systems": B, "K": K},
+                units, lambda: oracle.thomas(*arrays),
+                f"all {B} systems x {K} rows per step, float32 sequential Thomas")
+        return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     host = _tridiag_system(B, K, 11 + rank, torch.float32)
@@ -801,12 +847,25 @@ def bench_tree(args, world, rank, local):
     from dendra_gb300.tree import build_dhs_layers, build_morphology, dhs_solve_cuda
 
     B = args.cables if args.cables != 16384 else 8192
+    metric = "node-solves/s"
+    if args.impl == "reference":
+        if rank == 0:
+            parent, host = _tree_systems(B, 13)
+            K = parent.size
+            _, _, depth = build_morphology([int(p) for p in parent])
+            order, layer_ptr = build_dhs_layers(depth, 32)
+            order, layer_ptr = order.numpy(), layer_ptr.numpy()
+            _reference_solve_line(
+                args, world, metric, {"workload": "tree-contraction-solve", "systems": B, "K": K},
+                B * K, lambda: oracle.dhs_solve(*host, parent, order, layer_ptr),
+                f"all {B} systems x {K} nodes per step, float32 sequential DHS (C restatement; "
+                "the reference's CPU tree solvers live in the absent dendra-solvers package)")
+        return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     parent, host = _tree_systems(B, 13 + rank)
     K = parent.size
     units = B * K
-    metric = "node-solves/s"
     plan = TreeContractionPlan(parent, 16)
     d, g, rhs = (torch.as_tensor(t).to(dev) for t in host)
     _, _, depth = build_morphology([int(p) for p in parent])

@@ -43,3 +43,24 @@ def test_tridiagonal_workload_is_diagonally_dominant_and_solvable():
     x = oracle.thomas(*(t.numpy() for t in (a, b, c, d)))
     A = np.diag(b[0].numpy()) + np.diag(a[0].numpy(), -1) + np.diag(c[0].numpy(), 1)
     assert np.abs(A @ x[0] - d[0].numpy()).max() < 1e-12
+
+
+def test_reference_arm_of_single_solve_workloads_runs_on_the_host():
+    """``bench.py --impl reference`` for the solver workloads times the
+    oracle's CPU solve and prints one reference line, without a GPU."""
+    import json
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for workload, unit in (("tridiag", "row-solves/s"), ("bt", "compartment-solves/s"),
+                           ("tree", "node-solves/s")):
+        out = subprocess.run(
+            [sys.executable, "bench.py", "--workload", workload, "--impl", "reference",
+             "--steps", "1", "--warmup", "0", "--cables", "64"],
+            cwd=root, capture_output=True, text=True, timeout=300, check=True)
+        line = json.loads(out.stdout.strip().splitlines()[-1])
+        assert line["impl"] == "reference" and line["unit"] == unit
+        assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
+        assert line["e2e"]["h2d_bytes_per_step"] == 0
