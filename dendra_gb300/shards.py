@@ -8,10 +8,12 @@ exchanges are host-side: after the run, the slowest rank's time and the total
 work over all ranks, or a gather of results.
 
 ``balanced_shards`` partitions cables by compartment count so that every rank
-gets nearly the same number of compartment-steps; ``reduce_timing`` turns each
-rank's timed region into the whole-job figure (max time over ranks, summed
-work).  Both work on any ``torch.distributed`` backend: NCCL with CUDA tensors
-on a GPU node, gloo with CPU tensors.
+gets nearly the same number of compartment-steps; ``gather_cables`` puts the
+ranks' per-cable results (spike counts, thresholds, gradients) back in
+population order; ``reduce_timing`` turns each rank's timed region into the
+whole-job figure (max time over ranks, summed work).  The collectives work on
+any ``torch.distributed`` backend: NCCL on a GPU node (each rank's device set
+current first), gloo on CPU.
 """
 
 from __future__ import annotations
@@ -53,6 +55,40 @@ def shard_of(sizes, world: int, rank: int) -> np.ndarray:
     if not 0 <= rank < world:
         raise ValueError(f"rank {rank} outside [0, {world})")
     return balanced_shards(sizes, world)[rank]
+
+
+def gather_cables(local: torch.Tensor, shard, n_total: int, group=None) -> torch.Tensor:
+    """Reassemble per-cable results of every rank in population order.
+
+    ``local`` holds this rank's results, one leading-dimension entry per cable
+    of ``shard`` (in the shard's order); the result, on every rank, is a CPU
+    tensor with ``n_total`` entries where entry ``shard[j]`` of each rank is
+    that rank's ``local[j]``.  Results travel once, at the end of a run, so
+    they go through the host (``all_gather_object``) on any backend.  Without
+    an initialised process group, ``shard`` must cover the whole population.
+    """
+    import torch.distributed as dist
+
+    shard = np.asarray(shard, dtype=np.int64)
+    local = local.detach().cpu()
+    if local.shape[0] != shard.size:
+        raise ValueError(f"local has {local.shape[0]} entries for a shard of {shard.size}")
+    if dist.is_available() and dist.is_initialized():
+        parts = [None] * dist.get_world_size(group)
+        dist.all_gather_object(parts, (shard, local), group=group)
+    else:
+        parts = [(shard, local)]
+    out = torch.empty((n_total, *local.shape[1:]), dtype=local.dtype)
+    seen = np.zeros(n_total, dtype=bool)
+    for idx, vals in parts:
+        if idx.size and (idx.min() < 0 or idx.max() >= n_total or seen[idx].any()
+                         or np.unique(idx).size != idx.size):
+            raise ValueError("shards overlap or fall outside the population")
+        seen[idx] = True
+        out[torch.as_tensor(idx)] = vals
+    if not seen.all():
+        raise ValueError(f"{int((~seen).sum())} cables are in no shard")
+    return out
 
 
 def reduce_timing(ms: float, units: float, group=None, device=None) -> tuple[float, float]:

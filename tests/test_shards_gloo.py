@@ -1,6 +1,7 @@
 """Multi-rank host logic on CPU: two gloo ranks partition a config-2-like
-population by compartment count and reduce their timings the way a
-``torchrun --nproc-per-node N bench.py`` run does on GPUs.
+population by compartment count, gather per-cable results back in population
+order, and reduce their timings the way a ``torchrun --nproc-per-node N
+bench.py`` run does on GPUs.
 
 Each rank builds its own shard's population on the host (geometry, workspace,
 extracellular field) and checks that the shards are disjoint, cover every
@@ -17,7 +18,7 @@ import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
-from dendra_gb300.shards import balanced_shards, reduce_timing, shard_of
+from dendra_gb300.shards import balanced_shards, gather_cables, reduce_timing, shard_of
 from dendra_gb300.workloads import c2_spec
 
 N_CABLES = 512
@@ -51,6 +52,15 @@ def _rank_main(rank, world, port):
         assert np.array_equal(np.sort(flat), np.arange(N_CABLES))  # disjoint and complete
         loads = [int(ks[np.asarray(s, dtype=np.int64)].sum()) for s in shards]
         assert max(loads) - min(loads) <= int(ks.max())
+
+        # per-cable results back in population order on every rank
+        local = torch.as_tensor(ks[mine] * 10.0 + rank, dtype=torch.float64)[:, None]
+        full = gather_cables(local, mine, N_CABLES)
+        owner = np.empty(N_CABLES)
+        for r, s in enumerate(shards):
+            owner[np.asarray(s, dtype=np.int64)] = r
+        assert full.shape == (N_CABLES, 1)
+        assert np.array_equal(full[:, 0].numpy(), ks * 10.0 + owner)
 
         steps = 2000
         ms, units = reduce_timing(10.0 + 5.0 * rank, pop.N * steps)
@@ -93,3 +103,15 @@ def test_balanced_shards_edges():
 
 def test_reduce_timing_without_group():
     assert reduce_timing(3.5, 7) == (3.5, 7.0)
+
+
+def test_gather_cables_without_group_checks_coverage():
+    vals = torch.arange(4.0)
+    out = gather_cables(vals, [2, 0, 3, 1], 4)
+    assert out.tolist() == [1.0, 3.0, 0.0, 2.0]
+    with pytest.raises(ValueError, match="in no shard"):
+        gather_cables(vals[:3], [0, 1, 2], 4)
+    with pytest.raises(ValueError, match="overlap"):
+        gather_cables(vals, [0, 0, 1, 2], 4)
+    with pytest.raises(ValueError, match="entries for a shard"):
+        gather_cables(vals, [0, 1], 4)
