@@ -35,6 +35,10 @@ class DgbError(RuntimeError):
     """A dendra_gb300 C-ABI call returned an error code."""
 
 
+class DgbTimeout(DgbError):
+    """A bounded device-side wait gave up (DGB_ETIMEOUT)."""
+
+
 class CableArgs(ctypes.Structure):
     """Mirror of ``dgb_cable_args`` (field order and types must match)."""
 
@@ -97,6 +101,7 @@ SIGNATURES = {
                             _P, _P]),
     "dgb_mlp_gemm_path": (_INT, [_I32, _I32, _I32, _P, _I64, _I64, _P, _I64, _I64]),
     "dgb_mlp_gemm_status": (_INT, [_P]),
+    "dgb_mlp_gemm_set_wait_limit": (_INT, [_I64]),
     "dgb_colsum": (_INT, [_I32, _I32, _P, _P, _P]),
     "dgb_adam": (_INT, [_I64, _I32, _I32, _P, _P, _P, _P, ctypes.c_float, ctypes.c_float,
                         ctypes.c_float, ctypes.c_float, _I32, _P, _P, _P]),
@@ -164,6 +169,8 @@ def check(rc: int, what: str) -> None:
         kind = {-1: ValueError, -4: ValueError}.get(rc)
         if kind is not None:
             raise kind(f"{what}: {msg}")
+        if rc == -3:
+            raise DgbTimeout(f"{what} timed out (code {rc}): {msg}")
         raise DgbError(f"{what} failed (code {rc}): {msg}")
 
 

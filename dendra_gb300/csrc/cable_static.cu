@@ -21,28 +21,62 @@ constexpr size_t kStaticBandBytes = size_t(4) << 20;  // 4 MiB
 static __device__ __align__(256) unsigned char g_static_bands[kStaticBandBytes];
 
 constexpr int kMaxDevices = 64;
-static void* g_band_ptr[kMaxDevices] = {nullptr};
+struct BandAddr {
+  void* ctx;  // context the address belongs to
+  void* ptr;  // device address of g_static_bands in that context
+};
+static BandAddr g_band[kMaxDevices] = {};
 static std::mutex g_band_mutex;
 
-// Device address of g_static_bands on the current device, looked up once per
-// device with that device current.  In host code the symbol is only a host
-// stand-in; kernels must be given this address.
+// The current context of the calling thread (the device's primary context
+// for runtime-API callers; NULL before the runtime has bound one), through the
+// driver entry point of cuCtxGetCurrent.
+static int current_context(void** ctx) {
+  using GetCurrent = int (*)(void**);
+  static GetCurrent fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<GetCurrent>(p);
+  });
+  DGB_REQUIRE(fn != nullptr, "cuCtxGetCurrent is not available from the driver");
+  *ctx = nullptr;
+  DGB_REQUIRE(fn(ctx) == 0, "cuCtxGetCurrent failed");
+  return DGB_OK;
+}
+
+// Device address of g_static_bands on the current device.  In host code the
+// symbol is only a host stand-in; kernels must be given this address.  It is
+// looked up with the device current on the first call and again whenever the
+// device's context has changed since (cudaDeviceReset destroys the primary
+// context and the library's module with it, so the old address is stale).
 static int static_bands(void** out) {
   int dev = 0;
   DGB_CUDA_CHECK(cudaGetDevice(&dev));
   DGB_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal %d beyond %d", dev, kMaxDevices);
+  void* ctx = nullptr;
+  int rc = current_context(&ctx);
+  if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_band_mutex);
-  if (g_band_ptr[dev] == nullptr) {
+  if (g_band[dev].ptr == nullptr || ctx == nullptr || g_band[dev].ctx != ctx) {
     void* ptr = nullptr;
+    // also binds the device's primary context if none is current yet
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_static_bands);
     if (e != cudaSuccess || ptr == nullptr) {
       set_error("cudaGetSymbolAddress(static cable bands) failed on device %d: %s", dev,
                 cudaGetErrorString(e));
       return DGB_ECUDA;
     }
-    g_band_ptr[dev] = ptr;
+    rc = current_context(&ctx);
+    if (rc) return rc;
+    DGB_REQUIRE(ctx != nullptr, "no current CUDA context on device %d", dev);
+    g_band[dev] = BandAddr{ctx, ptr};
   }
-  *out = g_band_ptr[dev];
+  *out = g_band[dev].ptr;
   return DGB_OK;
 }
 

@@ -14,12 +14,17 @@
 //     times per chunk as the chunk lands, then tcgen05.commit to an mbarrier;
 //   * all four warps read their 32 accumulator lanes with tcgen05.ld and apply
 //     the same fused epilogues as the mma.sync kernel in mlp.cu.
-// Every mbarrier wait is bounded; a wait that gives up sets an error word
-// that the host reads, and the CTA still releases its TMEM.
+// Every mbarrier wait is bounded.  A load wait that gives up sets an error
+// word that the host reads; the CTA then drains the copies still in flight
+// and the MMAs already issued (with the full bound) before it frees its TMEM.
+// Only if that drain also gives up does the CTA exit with work outstanding:
+// it then keeps its TMEM and sets a second bit, and the host reports the
+// context as unusable.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "common.cuh"
@@ -42,10 +47,15 @@ constexpr uint32_t B_CHUNK = BN * BK * 2;  // 32 KB
 constexpr uint32_t TILE_BYTES = MAX_KC * (A_CHUNK + B_CHUNK);  // 192 KB
 constexpr uint32_t SMEM_BYTES = TILE_BYTES + 1024;             // + 1024-byte alignment slack
 constexpr uint32_t WAIT_LIMIT = 1u << 22;                      // polls before giving up
-constexpr int kErrTimeout = 1;
+constexpr int kErrTimeout = 1;  // a load wait gave up; the CTA drained and skipped its tile
+constexpr int kErrSuspect = 2;  // the drain gave up too: copies or MMAs may still be running
 
 // error word of the last launch on this device (nonzero: a bounded wait gave up)
 __device__ int g_tc_err;
+
+// polls a CTA spends on each TMA load wait before it gives up (the drain waits
+// always use WAIT_LIMIT); lowered only by dgb_mlp_gemm_set_wait_limit
+std::atomic<uint32_t> g_load_wait_limit{WAIT_LIMIT};
 
 // Instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B
 // BF16 (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
@@ -67,9 +77,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
 }
 
 // true once the phase with the given parity has completed; false after
-// WAIT_LIMIT polls
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+// `limit` polls
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          uint32_t limit = WAIT_LIMIT) {
+  for (uint32_t i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -141,12 +152,14 @@ __global__ void __launch_bounds__(128, 1)
     gemm_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    int M, int N, int K, const float* __restrict__ bias, int epi,
                    const float* __restrict__ aux, float* __restrict__ out32,
-                   __nv_bfloat16* __restrict__ out16, int* __restrict__ err) {
+                   __nv_bfloat16* __restrict__ out16, int* __restrict__ err,
+                   uint32_t load_wait_limit) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t bar_full[MAX_KC];
   __shared__ __align__(8) uint64_t bar_mma;
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
+  __shared__ int stuck;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
   const uint32_t sA = base, sB = base + MAX_KC * A_CHUNK;
@@ -155,6 +168,7 @@ __global__ void __launch_bounds__(128, 1)
 
   if (threadIdx.x == 0) {
     failed = 0;
+    stuck = 0;
     for (int c = 0; c < nk; ++c) mbar_init(smem_u32(&bar_full[c]), 1);
     mbar_init(smem_u32(&bar_mma), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -181,7 +195,7 @@ __global__ void __launch_bounds__(128, 1)
     }
     int landed = 0;
     for (int c = 0; c < nk; ++c) {
-      if (!mbar_wait(smem_u32(&bar_full[c]), 0)) break;
+      if (!mbar_wait(smem_u32(&bar_full[c]), 0, load_wait_limit)) break;
       landed = c + 1;
       tc_fence_after();
 #pragma unroll
@@ -195,15 +209,27 @@ __global__ void __launch_bounds__(128, 1)
       failed = 1;
       atomicOr(err, kErrTimeout);
       // let the copies still in flight land before the CTA's memory is reused
-      for (int c = landed; c < nk; ++c) mbar_wait(smem_u32(&bar_full[c]), 0);
+      for (int c = landed; c < nk; ++c)
+        if (!mbar_wait(smem_u32(&bar_full[c]), 0)) {
+          stuck = 1;
+          atomicOr(err, kErrSuspect);
+        }
     }
     umma_commit(smem_u32(&bar_mma));  // arrives once every MMA issued above is done
   }
   __syncthreads();
   // the epilogue's tcgen05.ld is warp-collective: decide per warp
-  const bool done = __all_sync(0xffffffffu, mbar_wait(smem_u32(&bar_mma), 0));
+  bool done = __all_sync(0xffffffffu, mbar_wait(smem_u32(&bar_mma), 0));
+  if (!done) {
+    if (lane == 0) atomicOr(err, kErrTimeout);
+    // the MMAs issued so far must finish before their TMEM is freed
+    done = __all_sync(0xffffffffu, mbar_wait(smem_u32(&bar_mma), 0));
+    if (!done && lane == 0) {
+      stuck = 1;
+      atomicOr(err, kErrSuspect);
+    }
+  }
   tc_fence_after();
-  if (!done && lane == 0) atomicOr(err, kErrTimeout);
   if (done && !failed) {
     const int m = m0 + warp * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
@@ -265,7 +291,7 @@ __global__ void __launch_bounds__(128, 1)
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 0 && !stuck) {  // a CTA with MMAs outstanding keeps its TMEM
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"((uint32_t)BN)
@@ -343,7 +369,8 @@ int mlp_gemm_tc(int32_t M, int32_t N, int32_t K, const void* A, int64_t sam, con
                                       (int)tc::SMEM_BYTES));
   dim3 grid(M / tc::BM, N / tc::BN);
   tc::gemm_tc_kernel<<<grid, 128, tc::SMEM_BYTES, st>>>(
-      mA, mB, M, N, K, bias, epi, aux, out32, reinterpret_cast<__nv_bfloat16*>(out16), err);
+      mA, mB, M, N, K, bias, epi, aux, out32, reinterpret_cast<__nv_bfloat16*>(out16), err,
+      tc::g_load_wait_limit.load());
   DGB_LAUNCH_CHECK();
   return DGB_OK;
 }
@@ -355,10 +382,26 @@ extern "C" int dgb_mlp_gemm_status(void* stream) {
   DGB_CUDA_CHECK(cudaStreamSynchronize(dgb::as_stream(stream)));
   int h = 0;
   DGB_CUDA_CHECK(cudaMemcpyFromSymbol(&h, dgb::tc::g_tc_err, sizeof(int)));
-  if (h) {
-    dgb::set_error("a tcgen05 GEMM wait gave up (error bits %d)", h);
+  if (h & dgb::tc::kErrSuspect) {
+    dgb::set_error("a tcgen05 GEMM wait gave up and its drain did not finish (error bits %d): "
+                   "copies or MMAs may still be outstanding, treat this CUDA context as unusable",
+                   h);
     return DGB_ETIMEOUT;
   }
+  if (h) {
+    dgb::set_error("a tcgen05 GEMM load wait gave up (error bits %d); the affected tiles were "
+                   "not written, the context is still usable", h);
+    return DGB_ETIMEOUT;
+  }
+  return DGB_OK;
+}
+
+extern "C" int dgb_mlp_gemm_set_wait_limit(int64_t polls) {
+  dgb::clear_error();
+  const uint32_t v = polls < 0 ? dgb::tc::WAIT_LIMIT
+                               : (uint32_t)(polls > (int64_t)dgb::tc::WAIT_LIMIT
+                                                ? dgb::tc::WAIT_LIMIT : polls);
+  dgb::tc::g_load_wait_limit.store(v);
   return DGB_OK;
 }
 

@@ -32,6 +32,7 @@ from typing import NamedTuple
 import torch
 
 from . import _lib
+from ._cache import TensorKeyedCache
 
 ERR_SLOT, ERR_ADDRESS, ERR_SOURCE, ERR_PLAN = 1, 2, 3, 4
 
@@ -127,37 +128,25 @@ class TapPlan:
             self.src_ptr, self.src_edge = _column_lists(pre_idx, self.n_sources)
 
 
-_plans: list = []
-_MAX_PLANS = 16
+_plans = TensorKeyedCache(16)
 
 
-def _cached_plan(key_tensors, versions, depth, width, n_sources, build):
+def _cached_plan(key_tensors, depth, width, n_sources, build):
     """Plan cache keyed on tensor identity and version (entries hold the tensors)."""
-    for ent in _plans:
-        tens, vers, d, w, ns, plan = ent
-        if (d, w, ns) == (depth, width, n_sources) and vers == versions and all(
-                a is b for a, b in zip(tens, key_tensors)):
-            return plan
-    plan = build()
-    _plans.append((key_tensors, versions, depth, width, n_sources, plan))
-    if len(_plans) > _MAX_PLANS:
-        _plans.pop(0)
-    return plan
+    return _plans.get(key_tensors, (depth, width, n_sources), build)
 
 
 def two_tap_plan(depth, width, lower, upper, pre_idx=None, n_sources=0):
     """Cached :class:`TapPlan` of flat two-tap addresses."""
     keys = (lower, upper, pre_idx)
-    vers = tuple(None if t is None else t._version for t in keys)
-    return _cached_plan(keys, vers, int(depth), int(width), int(n_sources),
+    return _cached_plan(keys, int(depth), int(width), int(n_sources),
                         lambda: TapPlan(depth, width, lower, upper, pre_idx, n_sources))
 
 
 def post_plan(depth, width, post_idx, pre_idx=None, n_sources=0):
     """Cached :class:`TapPlan` for taps in column ``post_idx[e]``."""
     keys = (post_idx, pre_idx)
-    vers = tuple(None if t is None else t._version for t in keys)
-    return _cached_plan(keys, vers, int(depth), int(width), int(n_sources),
+    return _cached_plan(keys, int(depth), int(width), int(n_sources),
                         lambda: TapPlan(depth, width, None, None, pre_idx, n_sources,
                                         post_idx=post_idx))
 

@@ -41,6 +41,15 @@ def _gemm(M, N, K, A, sam, sak, B, sbk, sbn, *, bias=None, epi=EPI_PLAIN, aux=No
     _lib.check(rc, "dgb_mlp_gemm")
 
 
+def gemm_status(device) -> None:
+    """Raise ``DgbTimeout`` if a bounded wait inside the last tcgen05 GEMM on
+    ``device`` gave up (that GEMM's output is then invalid).  Synchronises the
+    current stream."""
+    with torch.cuda.device(device):
+        rc = _lib.load().dgb_mlp_gemm_status(_lib.stream_ptr(device))
+    _lib.check(rc, "tcgen05 GEMM")
+
+
 class BF16MLP:
     def __init__(self, dims=(4, 256, 256, 256, 1), device="cuda", seed=0):
         self.dims = tuple(dims)
@@ -168,12 +177,14 @@ class BF16MLP:
                 params = [p for pair in zip(self.W, self.b) for p in pair]
                 grads = [q for pair in zip(dW, db) for q in pair]
                 self._adam(params, grads, lr_t, step)
+            gemm_status(self.device)
             losses.append(float(((out - yb) ** 2).mean()))
         return losses
 
     def predict(self, X):
         """Predicted targets (de-standardised) for features X (M, 4)."""
         out = self.forward(self._inputs(X.to(self.device)))
+        gemm_status(self.device)
         return out.reshape(-1) * self.y_std + self.y_mean
 
 

@@ -22,6 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from ._cache import TensorKeyedCache
 
 BITS_PER_WORD = 63
 
@@ -98,18 +99,14 @@ class TargetCSR:
         return self
 
 
-_csr_cache: dict = {}
+_csr_cache = TensorKeyedCache(32)
 
 
 def _target_csr(post_idx, n_post):
-    key = (post_idx.data_ptr(), post_idx._version, post_idx.numel(), int(n_post))
-    hit = _csr_cache.get(key)
-    if hit is None:
-        hit = TargetCSR(post_idx, n_post).to(post_idx.device)
-        if len(_csr_cache) > 32:
-            _csr_cache.clear()
-        _csr_cache[key] = hit
-    return hit
+    """Target CSR of a connection list, cached on the identity and version of
+    ``post_idx`` (the entry holds it, so its address cannot be reused)."""
+    return _csr_cache.get((post_idx,), int(n_post),
+                          lambda: TargetCSR(post_idx, n_post).to(post_idx.device))
 
 
 def build_delivery(packed_history, current_time_step, delay_steps, conn_word_idx,

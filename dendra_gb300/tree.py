@@ -30,6 +30,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from ._cache import TensorKeyedCache
 from .solvers import _validate_float_group
 
 _INDEX_DTYPES = (torch.int32, torch.int64)
@@ -144,25 +145,22 @@ def validate_tree(d_mem, a_geom, b, parent_idx, order, layer_ptr, threads):
     return batch, size, validate_threads(threads)
 
 
-_topo_cache: dict = {}
+_topo_cache = TensorKeyedCache(64)
 
 
 def _device_topology(parent_idx, order, layer_ptr):
-    """int32 device copies of the plan plus the children CSR, cached per tensor version."""
-    key = tuple((t.data_ptr(), t._version, t.numel(), str(t.device))
-                for t in (parent_idx, order, layer_ptr))
-    hit = _topo_cache.get(key)
-    if hit is not None:
-        return hit
-    dev = parent_idx.device
-    parent_np = parent_idx.detach().cpu().numpy().astype(np.int64)
-    cptr, cidx = children_csr(parent_np)
-    topo = tuple(torch.as_tensor(x, dtype=torch.int32, device=dev).contiguous() for x in (
-        parent_np, order.detach().cpu().numpy(), layer_ptr.detach().cpu().numpy(), cptr, cidx))
-    if len(_topo_cache) > 64:
-        _topo_cache.clear()
-    _topo_cache[key] = topo
-    return topo
+    """int32 device copies of the plan plus the children CSR, cached on the
+    identity and version of the three plan tensors (the entry holds them)."""
+
+    def build():
+        dev = parent_idx.device
+        parent_np = parent_idx.detach().cpu().numpy().astype(np.int64)
+        cptr, cidx = children_csr(parent_np)
+        return tuple(torch.as_tensor(x, dtype=torch.int32, device=dev).contiguous() for x in (
+            parent_np, order.detach().cpu().numpy(), layer_ptr.detach().cpu().numpy(),
+            cptr, cidx))
+
+    return _topo_cache.get((parent_idx, order, layer_ptr), None, build)
 
 
 _chain_cache: dict = {}
@@ -545,7 +543,7 @@ def validate_tree_multi(d_mem, a_geom, b, plan, K_stride, L_max, threads, grid_x
     return batch, warp_count
 
 
-_multi_cache: dict = {}
+_multi_cache = TensorKeyedCache(32)
 
 
 class _MultiPlan:
@@ -606,14 +604,8 @@ class _MultiPlan:
 
 
 def _multi_plan(plan, B, K_stride, device):
-    key = (B, K_stride, str(device)) + tuple(
-        (t.data_ptr(), t._version, t.numel(), t.dtype) for t in plan)
-    hit = _multi_cache.get(key)
-    if hit is None:
-        if len(_multi_cache) > 32:
-            _multi_cache.clear()
-        hit = _multi_cache[key] = _MultiPlan(plan, B, K_stride, device)
-    return hit
+    return _multi_cache.get(tuple(plan), (B, K_stride, str(device)),
+                            lambda: _MultiPlan(plan, B, K_stride, device))
 
 
 def _multi_solve(d, a, b, mp):

@@ -569,8 +569,17 @@ int dgb_mlp_gemm_path(int32_t M, int32_t N, int32_t K, const void* A, int64_t sa
                       const void* B, int64_t sbk, int64_t sbn);
 
 /* Synchronises the stream and returns DGB_ETIMEOUT if a bounded wait inside
-   the last tcgen05 GEMM on this device gave up (its output is then invalid). */
+   the last tcgen05 GEMM on this device gave up (its output is then invalid).
+   A load wait that gave up is recoverable: the CTA drained its copies and
+   MMAs and freed its tensor memory.  If the drain gave up as well, the
+   message says so and the CUDA context should be treated as unusable. */
 int dgb_mlp_gemm_status(void* stream);
+
+/* Diagnostic: polls each tcgen05 GEMM CTA spends on a TMA load wait before it
+   gives up (0 = give up at the first poll; negative restores the default
+   2^22).  The drain waits after a give-up always use the default.  Lets a
+   test exercise the timeout path without a fault; no reference counterpart. */
+int dgb_mlp_gemm_set_wait_limit(int64_t polls);
 
 /* out[n] = sum over m of x[m][n] (fp32, fixed order). */
 int dgb_colsum(int32_t M, int32_t N, const float* x, float* out, void* stream);
@@ -595,7 +604,8 @@ int dgb_mse_grad(int64_t n, const float* y, const float* target, float scale, fl
  * another runtime owns the allocator).  The caller passes inputs and
  * outputs as for dgb_cable_assemble (comp_cable required; scratch unused).
  * The first call on a device looks up the array's device address (with that
- * device current) and should come before any stream capture.  All calls
+ * device current) and should come before any stream capture; the lookup is
+ * repeated if the device's context changed since (after cudaDeviceReset).  All calls
  * share the one array: calls that overlap on the GPU race and must be
  * serialised by the caller (one stream, or events between them).  Nothing in
  * the array needs clearing; each call writes the bands before reading them.

@@ -118,3 +118,33 @@ def test_tcgen05_gemm_matches_float64_and_the_mma_sync_path(cuda, K, N):
             if r16 is not None:
                 np.testing.assert_allclose(o16, r16, rtol=1e-2, atol=1e-2 * scale)
         np.testing.assert_allclose(outs[0][0], outs[1][0], rtol=0, atol=2e-5 * scale)
+
+
+def test_tcgen05_load_wait_timeout_surfaces(cuda):
+    """A TMA load wait limited to zero polls gives up at once: the kernel drains
+    its copies, frees its tensor memory and flags the error; the status call
+    raises DgbTimeout, and with the default limit restored the same GEMM runs
+    correctly on the same context.  Nothing faults or hangs: every wait is
+    bounded and the copies are real, in-bounds TMA loads."""
+    from dendra_gb300.mlp import gemm_status
+
+    L = _lib.load()
+    rng = np.random.default_rng(3)
+    M, N, K = 128, 256, 256
+    A = torch.as_tensor(rng.standard_normal((M, K)), dtype=torch.float32).to(torch.bfloat16).to(cuda)
+    Wt = torch.as_tensor(rng.standard_normal((N, K)) / 16, dtype=torch.float32).to(
+        torch.bfloat16).to(cuda)
+    assert L.dgb_mlp_gemm_path(M, N, K, A.data_ptr(), K, 1, Wt.data_ptr(), 1, K) == 1
+    o32 = torch.zeros((M, N), dtype=torch.float32, device=cuda)
+    try:
+        assert L.dgb_mlp_gemm_set_wait_limit(0) == 0
+        _gemm(M, N, K, A, K, 1, Wt, 1, K, epi=EPI_PLAIN, out32=o32)
+        with pytest.raises(_lib.DgbTimeout, match="still usable"):
+            gemm_status(cuda)
+    finally:
+        assert L.dgb_mlp_gemm_set_wait_limit(-1) == 0
+    _gemm(M, N, K, A, K, 1, Wt, 1, K, epi=EPI_PLAIN, out32=o32)
+    gemm_status(cuda)
+    ref = A.double().cpu().numpy() @ Wt.double().cpu().numpy().T
+    np.testing.assert_allclose(o32.double().cpu().numpy(), ref, rtol=0,
+                               atol=2e-5 * np.abs(ref).max())

@@ -21,8 +21,8 @@ from tests._cases import synthetic_population
 
 pytestmark = pytest.mark.gpu
 
-# tolerances of the plain-path tests (test_cable_gpu.py)
-TOL = {torch.float64: dict(rtol=1e-12, atol=1e-10), torch.float32: dict(rtol=1e-6, atol=1e-5)}
+# Both paths run the same two kernels on the same inputs; only the band
+# scratch lives elsewhere, so the states must agree bit for bit.
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
@@ -39,7 +39,7 @@ def test_static_step_matches_allocating_step(cuda, dtype):
         new.t += new.dt
         torch.cuda.synchronize()
         for name in ("v", "m", "h", "n"):
-            torch.testing.assert_close(getattr(new, name), getattr(ref, name), **TOL[dtype])
+            assert torch.equal(getattr(new, name), getattr(ref, name)), name
     assert bool(torch.isfinite(new.v).all())
 
 
