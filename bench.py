@@ -1564,7 +1564,9 @@ def main():
                    "math": "exact" if args.exact else "fast (<=1e-3 mV vs float64, tested)",
                    "l2": "flushed between timed steps (256 MiB read, outside the events)",
                    "launch": "one persistent dgb_cable_run launch per step",
-                   "warps_per_block": wpb, "autotune_ms": tune_ms},
+                   "warps_per_block": wpb[0], "lanes_split_k16_k8": list(wpb[1:]),
+                   "autotune_ms": None if tune_ms is None else
+                   {str(k): v for k, v in tune_ms.items()}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
                      "note": (f"achieved = {ALG_BYTES_PER_COMP_STEP} algorithmic B per "

@@ -56,7 +56,10 @@ class CableArgs(ctypes.Structure):
         ("spk_idx", _P), ("spk_thr", _D), ("spk_below", _P), ("spk_count", _P),
         ("spk_first", _P), ("spk_idx2", _P), ("spk_below2", _P),
         ("max_k", _I32), ("flags", _I32), ("n_comp", _I64),
-        ("comp_cable", _P), ("scratch", _P), ("warps_per_block", _I32), ("reserved", _I32),
+        ("comp_cable", _P), ("scratch", _P), ("warps_per_block", _I32), ("n_rast", _I32),
+        ("rast_idx", _P), ("rast_below", _P), ("rast_count", _P), ("rast_steps", _P),
+        ("rast_cap", _I32), ("lanes_mode", _I32), ("n_lanes32", _I32), ("n_lanes16", _I32),
+        ("trace_all", _P),
     ]
 
 

@@ -6,7 +6,9 @@ implicit.py:364-440).  Here each knob is a parameter of the C ABI and is
 chosen by timing the candidates on the device:
 
 * cables per CTA of the persistent cable kernels (``dgb_cable_args.
-  warps_per_block``: 1, 2 or 4) — ``tune_cable_run``;
+  warps_per_block``: 1, 2 or 4) and the persistent run's Thomas/PCR split
+  (``lanes_mode``/``n_lanes32``/``n_lanes16``: short cables on 8 or 16 lanes,
+  i.e. longer sequential chunks and fewer PCR stages) — ``tune_cable_run``;
 * the Thomas-versus-PCR split of the chunked tridiagonal solve (lanes per
   system 4 .. 32, i.e. rows per lane eliminated sequentially vs reduced by
   PCR) — ``tune_tridiag_lanes``;
@@ -17,9 +19,11 @@ chosen by timing the candidates on the device:
 Every candidate runs a short representative workload (warm-up, then the
 median of ``reps`` timings with CUDA events on the current stream).  Results
 are cached per (knob, shape key, device name) for the process; a JSON file
-named by ``DGB_TUNE_CACHE`` keeps them across processes.  Candidates change
-only the launch shape, never the arithmetic, so every choice gives identical
-results.
+named by ``DGB_TUNE_CACHE`` keeps them across processes.  Launch-shape
+candidates (CTA sizes, threads per cell) never change the arithmetic, so they
+give identical results; the lane splits of the tridiagonal solves change the
+order of the elimination and so the rounding (every split is tested against
+the oracle within the solver tolerances).
 """
 
 from __future__ import annotations
@@ -99,17 +103,30 @@ def tune(kind, key_parts, candidates, run, device, reps=3, force=False):
     return best, timings
 
 
-def tune_cable_run(pop, n_steps=50, candidates=(1, 2, 4), reps=3, force=False):
-    """Pick cables per CTA for ``pop``'s persistent runs; sets pop.warps_per_block.
+# (cables per CTA, k16, k8): cables with K <= k8 on 8 lanes, K <= k16 on 16
+# lanes, the rest on 32 ((0, 0): every cable on 32 lanes)
+CABLE_RUN_CANDIDATES = tuple((w, k16, k8) for w in (2, 4)
+                             for k16, k8 in ((0, 0), (96, 0), (128, 0), (128, 48), (128, 64)))
+
+
+def tune_cable_run(pop, n_steps=50, candidates=CABLE_RUN_CANDIDATES, reps=3, force=False):
+    """Pick cables per CTA and the lane split for ``pop``'s persistent runs;
+    sets pop.warps_per_block and pop.lanes_split.
 
     Times ``n_steps`` steps from the population's current state (restored
-    after every timing).  Returns (choice, {candidate: ms} or None if cached)."""
+    after every timing).  Returns ((wpb, k16, k8), {candidate: ms} or None if
+    cached)."""
     state = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
     step, t = pop.step_index, pop.t
-    saved = pop.warps_per_block
+    saved = (pop.warps_per_block, pop.lanes_split)
+
+    def apply(c):
+        w, k16, k8 = (int(x) for x in c)
+        pop.warps_per_block = w
+        pop.lanes_split = None if k16 == 0 and k8 == 0 else (k16, k8)
 
     def run(c):
-        pop.warps_per_block = c
+        apply(c)
         for dst, src in zip((pop.v, pop.m, pop.h, pop.n), state):
             dst.copy_(src)
         pop.step_index, pop.t = step, t
@@ -119,14 +136,15 @@ def tune_cable_run(pop, n_steps=50, candidates=(1, 2, 4), reps=3, force=False):
     parts = (str(pop.dtype), pop.B, kmax, pop.N, pop.fast_math, "ve" if pop.field is not None
              else "-")
     try:
-        best, timings = tune("cable_run_wpb", parts, candidates, run, pop.device, reps, force)
+        best, timings = tune("cable_run_split", parts, candidates, run, pop.device, reps, force)
     finally:
         for dst, src in zip((pop.v, pop.m, pop.h, pop.n), state):
             dst.copy_(src)
         pop.step_index, pop.t = step, t
-        pop.warps_per_block = saved
-    pop.warps_per_block = int(best)
-    return int(best), timings
+        pop.warps_per_block, pop.lanes_split = saved
+    best = tuple(int(x) for x in best)
+    apply(best)
+    return best, timings
 
 
 def tune_tridiag_lanes(B, K, dtype=torch.float32, device="cuda", candidates=(4, 8, 16, 32),

@@ -88,10 +88,38 @@ def waveform_param(x):
 
 
 @dataclass
+class RasterState:
+    """Upward threshold crossings at checked compartments (Raster/APCount).
+
+    idx (B, R) int32 local compartments (-1: none); below (B, R) int32 latch
+    (1 = below threshold); count (B, R) int32 crossings counted so far; steps
+    (B, R, cap) int64 absolute step index (1-based, counted from
+    initialize) of each crossing while its ordinal is below cap, -1 after.
+    A count above cap means later crossings were counted but not stored.
+    Pass it back as ``raster_state`` to continue counting in a later run."""
+
+    idx: torch.Tensor
+    below: torch.Tensor
+    count: torch.Tensor
+    steps: torch.Tensor
+
+    @property
+    def overflow(self) -> bool:
+        return bool((self.count > self.steps.shape[-1]).any())
+
+    def spike_steps(self, cable: int, q: int = 0):
+        """The stored crossing steps of one cable's check q (a numpy array)."""
+        c = int(self.count[cable, q])
+        return self.steps[cable, q, :min(c, self.steps.shape[-1])].cpu().numpy()
+
+
+@dataclass
 class RunResult:
     trace: torch.Tensor | None
     spk_count: torch.Tensor | None
     spk_first: torch.Tensor | None
+    trace_all: torch.Tensor | None = None
+    raster: RasterState | None = None
 
 
 class CablePopulation:
@@ -150,6 +178,10 @@ class CablePopulation:
         # cables in flight per CTA of the persistent kernels (0 = library
         # default); dendra_gb300.autotune.tune_cable_run picks it
         self.warps_per_block = 0
+        # Thomas/PCR split of the persistent run: None = 32 lanes per cable;
+        # (k16, k8) = cables with K <= k8 (<= 64) run on 8 lanes, K <= k16
+        # (<= 128) on 16 lanes, longer ones on 32.  tune_cable_run picks it.
+        self.lanes_split = None
         self.field = None
         self.ve = None
         self.intra = None
@@ -312,10 +344,26 @@ class CablePopulation:
         a.comp_cable = d["comp_cable"].data_ptr()
         a.scratch = d["scratch"].data_ptr()
         a.warps_per_block = int(self.warps_per_block)
+        if self.lanes_split is not None:
+            n32, n16 = self._lane_counts(self.lanes_split)
+            a.lanes_mode, a.n_lanes32, a.n_lanes16 = 1, n32, n16
         return a
 
+    def _lane_counts(self, split):
+        """Cables on 32 and on 16 lanes for split (k16, k8); the work order
+        lists cables by non-increasing K, so each class is one contiguous run."""
+        k16, k8 = (int(x) for x in split)
+        if not (0 <= k8 <= 64 and 0 <= k16 <= 128):
+            raise ValueError("lanes_split (k16, k8) needs k16 <= 128 and k8 <= 64")
+        k8 = min(k8, k16)
+        ks = np.asarray(self.n_comp)
+        n32 = int((ks > k16).sum())
+        n16 = int(((ks > k8) & (ks <= k16)).sum())
+        return n32, n16
+
     def run(self, n_steps, *, rec_idx=None, rec_every=1, spk_idx=None, spk_thr=0.0,
-            spk_state=None, spk_idx2=None, stop_on_spike=False, cables=None):
+            spk_state=None, spk_idx2=None, stop_on_spike=False, cables=None,
+            record_all=False, raster=None, raster_cap=64, raster_state=None):
         """Advance every cable by n_steps in one persistent launch.
 
         rec_idx / spk_idx: per-cable local compartment (int, sequence or
@@ -326,6 +374,15 @@ class CablePopulation:
         stop_on_spike: a cable stops after the step of its first spike.
         cables: optional int32 device tensor of the cables to advance (others
         are left untouched).
+        record_all: also record v of every compartment every rec_every steps
+        (``trace_all``, shape (1 + n_steps//rec_every, N), packed like the
+        state; Recorder(("v",)) of the reference).
+        raster: up to 4 checked compartments per cable (a sequence of local
+        indices applied to every cable, negative counting from the far end like
+        Raster's node_check, or a (B, R) tensor); every upward crossing of
+        spk_thr is counted and its step stored (``raster``, a RasterState,
+        at most raster_cap steps per check).  raster_state continues an
+        earlier run's raster (its idx is reused).
         """
         if self.dt is None:
             raise RuntimeError("Model must be initialized before running.")
@@ -359,12 +416,48 @@ class CablePopulation:
         if cables is not None:
             args.order = cables.data_ptr()
             args.n_cables = int(cables.numel())
+            args.lanes_mode = 0  # the lane classes are positions of the full order
+        trace_all = None
+        if record_all:
+            trace_all = torch.full((1 + int(n_steps) // int(rec_every), self.N), float("nan"),
+                                   dtype=self.dtype, device=dev)
+            args.trace_all = trace_all.data_ptr()
+        rs = None
+        if raster is not None or raster_state is not None:
+            rs = raster_state if raster_state is not None else self._raster(raster, raster_cap)
+            args.n_rast = int(rs.idx.shape[1])
+            args.rast_idx, args.rast_below, args.rast_count = (
+                t.data_ptr() for t in (rs.idx, rs.below, rs.count))
+            args.rast_steps = rs.steps.data_ptr()
+            args.rast_cap = int(rs.steps.shape[2])
+            args.spk_thr = float(spk_thr)
         with torch.cuda.device(dev):
             rc = _lib.load().dgb_cable_run(args, _lib.stream_ptr(dev))
         _lib.check(rc, "dgb_cable_run")
         self.t = self.t + int(n_steps) * self.dt
         self.step_index += int(n_steps)
-        return RunResult(trace, spk[2] if spk else None, spk[3] if spk else None)
+        return RunResult(trace, spk[2] if spk else None, spk[3] if spk else None, trace_all, rs)
+
+    def _raster(self, raster, cap):
+        """A fresh RasterState for the checked compartments ``raster``."""
+        kk = torch.as_tensor(self.n_comp, dtype=torch.int64)
+        idx = torch.as_tensor(raster, dtype=torch.int64)
+        if idx.ndim == 1:
+            idx = idx.reshape(1, -1).expand(self.B, -1)
+        if idx.ndim != 2 or idx.shape[0] != self.B or not 1 <= idx.shape[1] <= 4:
+            raise ValueError("raster takes 1 to 4 checked compartments per cable")
+        idx = torch.where(idx < 0, idx + kk.reshape(-1, 1), idx)
+        if bool(((idx < 0) | (idx >= kk.reshape(-1, 1))).any()):
+            raise ValueError("raster compartment out of range for some cable")
+        if int(cap) < 0:
+            raise ValueError("raster_cap must be >= 0")
+        dev = self.device
+        R = idx.shape[1]
+        return RasterState(idx.to(torch.int32).contiguous().to(dev),
+                           torch.ones((self.B, R), dtype=torch.int32, device=dev),
+                           torch.zeros((self.B, R), dtype=torch.int32, device=dev),
+                           torch.full((self.B, R, max(int(cap), 0)), -1, dtype=torch.int64,
+                                      device=dev))
 
     def check_status(self):
         """Raise if the last persistent run flagged a cable it could not advance."""

@@ -18,8 +18,10 @@ extern "C" int dgb_cable_run(const dgb_cable_args* args, void* stream) {
   // shared memory is sized for the largest chunk (rows per lane) of any cable
   const int ch_max = (int)((kmax + 31) / 32);
   cudaStream_t st = as_stream(stream);
-  if (args->dtype == DGB_F32) return cable_run_t<float>(args, ch_max, st);
-  return cable_run_t<double>(args, ch_max, st);
+  if (args->dtype == DGB_F64) return cable_run_launch<double, false, false>(args, nullptr, ch_max, st);
+  if (args->flags & DGB_CABLE_FAST_MATH)
+    return cable_run_launch<float, true, false>(args, nullptr, ch_max, st);
+  return cable_run_launch<float, false, false>(args, nullptr, ch_max, st);
 }
 
 extern "C" int dgb_cable_assemble(const dgb_cable_args* args, int32_t step, void* lower,
@@ -77,8 +79,10 @@ extern "C" int dgb_cable_run_taped(const dgb_cable_args* args, void* tape, void*
   if (args->n_cables == 0) return DGB_OK;
   const int ch_max = (args->max_k + 31) / 32;
   cudaStream_t st = as_stream(stream);
-  if (args->dtype == DGB_F32) return cable_run_taped_t<float>(args, tape, ch_max, st);
-  return cable_run_taped_t<double>(args, tape, ch_max, st);
+  if (args->dtype == DGB_F64) return cable_run_launch<double, false, true>(args, tape, ch_max, st);
+  if (args->flags & DGB_CABLE_FAST_MATH)
+    return cable_run_launch<float, true, true>(args, tape, ch_max, st);
+  return cable_run_launch<float, false, true>(args, tape, ch_max, st);
 }
 
 extern "C" int dgb_cable_adjoint(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj,

@@ -36,6 +36,12 @@ struct CableArgsT {
   T* tape;         // (n_steps + 1, 4, n_comp) state tape, nullptr = none
   int64_t n_comp;  // total compartments (tape plane stride)
   int wpb;         // requested warps per block (0 = default)
+  int n_rast, rast_cap;
+  const int32_t* rast_idx;
+  int32_t *rast_below, *rast_count;
+  int64_t* rast_steps;
+  int lanes_mode, n_lanes32, n_lanes16;
+  T* trace_all;
 };
 
 template <typename T>
@@ -89,6 +95,16 @@ static CableArgsT<T> typed(const dgb_cable_args* a) {
   t.tape = nullptr;
   t.n_comp = a->n_comp;
   t.wpb = a->warps_per_block;
+  t.n_rast = a->rast_idx ? a->n_rast : 0;
+  t.rast_cap = a->rast_cap;
+  t.rast_idx = a->rast_idx;
+  t.rast_below = a->rast_below;
+  t.rast_count = a->rast_count;
+  t.rast_steps = a->rast_steps;
+  t.lanes_mode = a->lanes_mode;
+  t.n_lanes32 = a->n_lanes32;
+  t.n_lanes16 = a->n_lanes16;
+  t.trace_all = (T*)a->trace_all;
   return t;
 }
 

@@ -11,10 +11,10 @@ namespace dgb {
 constexpr int kCableMaxCH = 32;        // persistent run: K <= 1024
 constexpr int kSolveUpdateMaxCH = 16;  // plain per-step solve: K <= 512
 
-template <typename T>
-int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st);
-template <typename T>
-int cable_run_taped_t(const dgb_cable_args* args, void* tape, int ch_max, cudaStream_t st);
+// Persistent run of one (dtype, arithmetic, tape) variant; each variant is
+// compiled in its own translation unit (cable_run_*.cu, cable_taped_*.cu).
+template <typename T, bool FAST, bool TAPE>
+int cable_run_launch(const dgb_cable_args* args, void* tape, int ch_max, cudaStream_t st);
 template <typename T>
 int cable_adjoint_t(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj, int ch_max,
                     cudaStream_t st);
@@ -50,6 +50,18 @@ inline int validate_cable_args(const dgb_cable_args* a) {
               "DGB_CABLE_FAST_MATH applies to float32 state only");
   DGB_REQUIRE(a->warps_per_block >= 0 && a->warps_per_block <= 4 && a->warps_per_block != 3,
               "warps_per_block must be 0 (default), 1, 2 or 4, got %d", a->warps_per_block);
+  DGB_REQUIRE(a->n_rast >= 0 && a->n_rast <= 4, "n_rast must be in [0, 4], got %d", a->n_rast);
+  DGB_REQUIRE(a->n_rast == 0 || (a->rast_idx && a->rast_below && a->rast_count),
+              "n_rast > 0 requires rast_idx, rast_below and rast_count");
+  DGB_REQUIRE(a->n_rast == 0 || a->rast_cap >= 0, "rast_cap must be >= 0");
+  DGB_REQUIRE(a->n_rast == 0 || a->rast_cap == 0 || a->rast_steps,
+              "rast_cap > 0 requires rast_steps");
+  DGB_REQUIRE(a->lanes_mode == 0 || a->lanes_mode == 1, "lanes_mode must be 0 or 1");
+  DGB_REQUIRE(a->lanes_mode == 0 ||
+                  (a->n_lanes32 >= 0 && a->n_lanes16 >= 0 &&
+                   (int64_t)a->n_lanes32 + a->n_lanes16 <= a->n_cables),
+              "n_lanes32 + n_lanes16 must lie in [0, n_cables]");
+  DGB_REQUIRE(!a->trace_all || a->n_comp >= 0, "trace_all requires n_comp");
   return DGB_OK;
 }
 

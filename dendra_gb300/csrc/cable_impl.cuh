@@ -16,6 +16,7 @@
 //   5. the rising-edge spike check (_threshold_callbacks.py:50-53) and trace
 //      recording at one compartment.
 // Cables are handed out through an atomic work counter in largest-first order.
+// The per-cable work is run_rows (cable_rows.cuh).
 //
 // dgb_cable_assemble / dgb_cable_solve_update: the same step split into an
 // elementwise assembly kernel (one thread per compartment, bands to global
@@ -28,331 +29,73 @@
   DGB_CASE_F32(10) DGB_CASE_F32(11) DGB_CASE_F32(12) DGB_CASE_F32(13)             \
   DGB_CASE_F32(14) DGB_CASE_F32(15)
 #include "cable_common.cuh"
+#include "cable_rows.cuh"
 #include "chunk_solve.cuh"
 
 namespace dgb {
 
-// One cable, all steps, one warp.  ch = rows per lane (runtime), rows of lane
-// r are i = r*ch + j.  Rows with i >= K are identity rows with zero
-// coefficients and zero state.
-template <typename T, bool FAST, bool TAPE>
-__device__ void run_cable(const CableArgsT<T>& A, int cable, T* smw, int ch,
-                          const PlaneLayout& lay) {
-  const int r = threadIdx.x & 31;
-  const int64_t off = A.cable_ptr[cable];
-  const int K = (int)(A.cable_ptr[cable + 1] - off);
-  Planes<T> P{smw, ch};
-  const bool use_ve = lay.q_fld >= 0;
-
-  for (int j = 0; j < ch; ++j) {
-    const int i = r * ch + j;
-    const bool in = i < K;
-    const int64_t g = off + i;
-    P.at(P_V, j, r) = in ? A.v[g] : T(0);
-    P.at(P_M, j, r) = in ? A.m[g] : T(0);
-    P.at(P_H, j, r) = in ? A.h[g] : T(0);
-    P.at(P_N, j, r) = in ? A.n[g] : T(0);
-    if (lay.q_geo >= 0) {
-      P.at(lay.q_geo + 0, j, r) = in ? A.g_right[g] : T(0);
-      P.at(lay.q_geo + 1, j, r) = in ? A.g_left[g] : T(0);
-      P.at(lay.q_geo + 2, j, r) = in ? A.scale[g] : T(0);
-    }
-    if (use_ve) P.at(lay.q_fld, j, r) = in ? A.field[g] : T(0);
-    if (lay.q_chan >= 0) {
-      P.at(lay.q_chan + 0, j, r) = in ? A.gnabar[g] : T(0);
-      P.at(lay.q_chan + 1, j, r) = in ? A.gkbar[g] : T(0);
-      P.at(lay.q_chan + 2, j, r) = in ? A.gl[g] : T(0);
-      P.at(lay.q_chan + 3, j, r) = in ? A.el[g] : T(0);
-    }
+// The order positions and lanes per cable of work item `item` (false when
+// the item index is past the last item).
+__device__ __forceinline__ bool item_range(int item, int n_cables, int lanes_mode, int n32,
+                                           int n16, int& pos0, int& pos_end, int& lanes) {
+  if (lanes_mode == 0) {
+    pos0 = item;
+    pos_end = n_cables;
+    lanes = 32;
+    return item < n_cables;
   }
-  // uniform coefficients: the cable's values, identical on every compartment
-  // (interior edges for g_right / g_left), so reading them once is exact
-  T gna_c = T(0), gk_c = T(0), gl_c = T(0), el_c = T(0);
-  if (lay.q_chan < 0) {
-    gna_c = A.gnabar[off];
-    gk_c = A.gkbar[off];
-    gl_c = A.gl[off];
-    el_c = A.el[off];
+  if (item < n32) {
+    pos0 = item;
+    pos_end = n32;
+    lanes = 32;
+    return true;
   }
-  T gr_c = T(0), glf_c = T(0), sc_c = T(0);
-  if (lay.q_geo < 0) {
-    gr_c = K > 1 ? A.g_right[off] : T(0);
-    glf_c = K > 1 ? A.g_left[off + 1] : T(0);
-    sc_c = A.scale[off];
+  item -= n32;
+  const int items16 = (n16 + 1) / 2;
+  if (item < items16) {
+    pos0 = n32 + 2 * item;
+    pos_end = n32 + n16;
+    lanes = 16;
+    return true;
   }
-  __syncwarp();
-
-  T ve_amp = T(0), ve_delay = T(0), ve_pw = T(0);
-  if (use_ve) {
-    ve_amp = A.ve_amp[cable];
-    ve_delay = A.ve_delay[cable];
-    ve_pw = A.ve_pw[cable];
-  }
-  const int in_i = A.in_idx ? A.in_idx[cable] : -1;
-  T in_amp = T(0), in_delay = T(0), in_pw = T(0), in_cm = T(0);
-  if (in_i >= 0 && in_i < K) {
-    in_amp = A.in_amp[cable];
-    in_delay = A.in_delay[cable];
-    in_pw = A.in_pw[cable];
-    in_cm = A.cm_inv[off + in_i];
-  }
-  const int rec_i = (A.rec_idx && A.trace) ? A.rec_idx[cable] : -1;
-  const int spk_i = A.spk_idx ? A.spk_idx[cable] : -1;
-  const int spk_i2 = A.spk_idx2 ? A.spk_idx2[cable] : -1;
-  // the count and first step live in lane 0; each detection compartment keeps
-  // its latch in the lane that owns it
-  int below = 1, below2 = 1, count = 0, first = -1;
-  if (spk_i >= 0 && r == 0) {
-    count = A.spk_count[cable];
-    first = A.spk_first[cable];
-  }
-  if (spk_i >= 0 && r == spk_i / ch) below = A.spk_below[cable];
-  if (spk_i2 >= 0 && r == spk_i2 / ch) below2 = A.spk_below2[cable];
-  if (rec_i >= 0 && r == rec_i / ch) A.trace[(int64_t)cable * A.n_rec] = P.at(P_V, rec_i % ch, r);
-  if constexpr (TAPE) {
-    if (A.tape) {
-      tape_store<T>(P, K, ch, P_V, P_M, P_H, P_N, A.tape + off, A.n_comp);
-      __syncwarp();
-    }
-  }
-
-  const T dt = A.dt, dt_s = A.dt_s, q10 = A.q10, ena = A.ena, ek = A.ek;
-  const int last = ch - 1;
-  for (int s = 0; s < A.n_steps; ++s) {
-    const T t = (T)(A.t0_ms + (double)(A.step0 + s) * A.dt_ms_d);
-    const T Ive = use_ve ? rect_pulse<T>(t, ve_amp, ve_delay, ve_pw) : T(0);
-    const T Iin = (in_i >= 0) ? rect_pulse<T>(t, in_amp, in_delay, in_pw) : T(0);
-    const bool ve_on = Ive != T(0);  // per cable: warp-uniform
-
-    // ---- phase A: gates, membrane frame, row assembly fused with the
-    //      forward sweep of the chunk elimination (chunk_solve.cuh, step 1)
-    T As = T(0), Bs = T(1), Cs = T(0), Ds = T(0);
-    T ap = T(0), cp = T(0), dp = T(0);
-    T v_prev = (r > 0) ? P.at(P_V, last, r - 1) : T(0);
-    T vj = P.at(P_V, 0, r);
-    T f_prev = T(0), fj = T(0);
-    if (ve_on) {
-      f_prev = (r > 0) ? P.at(lay.q_fld, last, r - 1) : T(0);
-      fj = P.at(lay.q_fld, 0, r);
-    }
-    for (int j = 0; j < ch; ++j) {
-      const T v_next = (j < last) ? P.at(P_V, j + 1, r) : ((r < 31) ? P.at(P_V, 0, r + 1) : T(0));
-      T m = P.at(P_M, j, r), h = P.at(P_H, j, r), n = P.at(P_N, j, r);
-      if constexpr (FAST) {
-        hh_gates_fast(vj, q10, dt, m, h, n);
-      } else {
-        hh_gates<T>(vj, q10, dt, m, h, n);
-      }
-      P.at(P_M, j, r) = m;
-      P.at(P_H, j, r) = h;
-      P.at(P_N, j, r) = n;
-      T G, J;
-      if (lay.q_chan >= 0) {
-        hh_affine<T>(m, h, n, P.at(lay.q_chan, j, r), P.at(lay.q_chan + 1, j, r),
-                     P.at(lay.q_chan + 2, j, r), P.at(lay.q_chan + 3, j, r), ena, ek, G, J);
-      } else {
-        hh_affine<T>(m, h, n, gna_c, gk_c, gl_c, el_c, ena, ek, G, J);
-      }
-      T scl, gr, glf;
-      if (lay.q_geo >= 0) {
-        gr = P.at(lay.q_geo, j, r);
-        glf = P.at(lay.q_geo + 1, j, r);
-        scl = P.at(lay.q_geo + 2, j, r);
-      } else {
-        const int i = r * ch + j;
-        gr = i < K - 1 ? gr_c : T(0);
-        glf = (i >= 1 && i < K) ? glf_c : T(0);
-        scl = i < K ? sc_c : T(0);
-      }
-      // row i couples to i-1 through glf and to i+1 through gr; at a cable
-      // end (or past it) that coefficient is exactly zero
-      T fn = (J - mul_rn(G, vj)) * scl;
-      fn = fn + (mul_rn(gr, v_next - vj) - mul_rn(glf, vj - v_prev));
-      if (ve_on) {
-        const T f_next = (j < last) ? P.at(lay.q_fld, j + 1, r)
-                                    : ((r < 31) ? P.at(lay.q_fld, 0, r + 1) : T(0));
-        // ve values are rounded before they are differenced, as the reference
-        // materialises its ve tape; a fused field*I - ve would skip that rounding
-        const T ve_l = mul_rn(f_prev, Ive), ve_c = mul_rn(fj, Ive), ve_r = mul_rn(f_next, Ive);
-        fn = fn + (mul_rn(gr, ve_r - ve_c) - mul_rn(glf, ve_c - ve_l));
-        f_prev = fj;
-        fj = f_next;
-      }
-      if (r * ch + j == in_i) fn = fn + Iin * in_cm;
-      const T b = T(1) - dt_s * ((-gr + -glf) - mul_rn(G, scl));
-      const T a = -dt_s * glf;
-      const T c = -dt_s * gr;
-      const T d = dt_s * fn;
-      if (j == 0) {
-        As = a;
-        Bs = b;
-        Cs = c;
-        Ds = d;
-      } else if (j == 1) {
-        const T rinv = dv<T, FAST>(T(1), b);
-        ap = a * rinv;
-        cp = c * rinv;
-        dp = d * rinv;
-      } else {
-        const T rinv = dv<T, FAST>(T(1), b - a * cp);
-        ap = -a * ap * rinv;
-        dp = (d - a * dp) * rinv;
-        cp = c * rinv;
-      }
-      if (j >= 1) {
-        P.at(P_AP, j, r) = ap;
-        P.at(P_CP, j, r) = cp;
-        P.at(P_DP, j, r) = dp;
-      }
-      v_prev = vj;
-      vj = v_next;
-    }
-    // ---- phase B: backward sweep (rows ch-3 .. 1) and the reduced row
-    T al, be, ga, de, Ae = ap, Ce = cp, De = dp;
-    if (ch == 1) {
-      al = As;
-      be = Bs;
-      ga = Cs;
-      de = Ds;
-    } else {
-      T a2 = ap, c2 = cp, d2 = dp;  // row ch-2 after the loop below
-      if (ch >= 3) {
-        a2 = P.at(P_AP, ch - 2, r);
-        c2 = P.at(P_CP, ch - 2, r);
-        d2 = P.at(P_DP, ch - 2, r);
-        for (int j = ch - 3; j >= 1; --j) {
-          const T cj = P.at(P_CP, j, r);
-          d2 = P.at(P_DP, j, r) - cj * d2;
-          a2 = P.at(P_AP, j, r) - cj * a2;
-          c2 = -cj * c2;
-          P.at(P_AP, j, r) = a2;
-          P.at(P_CP, j, r) = c2;
-          P.at(P_DP, j, r) = d2;
-        }
-      }
-      T Bs2 = Bs, Cs2 = Cs, Ds2 = Ds;
-      if (ch >= 3) {
-        Bs2 = Bs - Cs * a2;
-        Cs2 = -Cs * c2;
-        Ds2 = Ds - Cs * d2;
-      }
-      T Ae_l = shfl_up<T>(Ae, 1, 32), Ce_l = shfl_up<T>(Ce, 1, 32), De_l = shfl_up<T>(De, 1, 32);
-      if (r == 0) {
-        Ae_l = T(0);
-        Ce_l = T(0);
-        De_l = T(0);
-      }
-      al = -As * Ae_l;
-      be = Bs2 - As * Ce_l - Cs2 * Ae;
-      ga = -Cs2 * Ce;
-      de = Ds2 - As * De_l - Cs2 * De;
-    }
-    // ---- phase C: PCR across the 32 lanes, then back-substitution
-#pragma unroll
-    for (int sh = 1; sh < 32; sh <<= 1) {
-      T al_l = shfl_up<T>(al, sh, 32), be_l = shfl_up<T>(be, sh, 32);
-      T ga_l = shfl_up<T>(ga, sh, 32), de_l = shfl_up<T>(de, sh, 32);
-      T al_r = shfl_down<T>(al, sh, 32), be_r = shfl_down<T>(be, sh, 32);
-      T ga_r = shfl_down<T>(ga, sh, 32), de_r = shfl_down<T>(de, sh, 32);
-      const bool hl = r >= sh;
-      const bool hr = r + sh < 32;
-      T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
-      T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
-      T al_n = hl ? -k1 * al_l : T(0);
-      T ga_n = hr ? -k2 * ga_r : T(0);
-      be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
-      de = de - (hl ? k1 * de_l : T(0)) - (hr ? k2 * de_r : T(0));
-      al = al_n;
-      ga = ga_n;
-    }
-    const T xs = dv<T, FAST>(de, be);
-    T xe = xs;
-    if (ch > 1) {
-      T xs_next = shfl_down<T>(xs, 1, 32);
-      if (r == 31) xs_next = T(0);
-      xe = De - Ae * xs - Ce * xs_next;
-    }
-    __syncwarp();  // every lane has read its neighbours' v for this step
-    P.at(P_V, 0, r) = P.at(P_V, 0, r) + xs;
-    for (int j = 1; j < last; ++j)
-      P.at(P_V, j, r) = P.at(P_V, j, r) + (P.at(P_DP, j, r) - P.at(P_AP, j, r) * xs -
-                                           P.at(P_CP, j, r) * xe);
-    if (ch > 1) P.at(P_V, last, r) = P.at(P_V, last, r) + xe;
-    if (spk_i >= 0) {
-      int edge = 0;
-      if (r == spk_i / ch) {
-        const int above = P.at(P_V, spk_i % ch, r) >= A.spk_thr;
-        edge = above && below;
-        below = !above;
-      }
-      int edge2 = 0;
-      if (spk_i2 >= 0 && r == spk_i2 / ch) {
-        const int above = P.at(P_V, spk_i2 % ch, r) >= A.spk_thr;
-        edge2 = above && below2;
-        below2 = !above;
-      }
-      const unsigned fired = __ballot_sync(0xffffffffu, edge || edge2);
-      if (fired && r == 0) {
-        if (count == 0) first = s + 1;
-        count += 1;
-      }
-      if (A.stop_on_spike && fired) {
-        if (rec_i >= 0 && r == rec_i / ch && ((s + 1) % A.rec_every) == 0)
-          A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = P.at(P_V, rec_i % ch, r);
-        __syncwarp();
-        break;
-      }
-    }
-    if (rec_i >= 0 && r == rec_i / ch && ((s + 1) % A.rec_every) == 0)
-      A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = P.at(P_V, rec_i % ch, r);
-    __syncwarp();  // new v visible to the neighbouring lanes
-    if constexpr (TAPE) {
-      if (A.tape) {
-        tape_store<T>(P, K, ch, P_V, P_M, P_H, P_N,
-                      A.tape + (int64_t)(s + 1) * 4 * A.n_comp + off, A.n_comp);
-        __syncwarp();  // the next step rewrites rows other lanes just read
-      }
-    }
-  }
-  for (int j = 0; j < ch; ++j) {
-    const int i = r * ch + j;
-    if (i < K) {
-      const int64_t g = off + i;
-      A.v[g] = P.at(P_V, j, r);
-      A.m[g] = P.at(P_M, j, r);
-      A.h[g] = P.at(P_H, j, r);
-      A.n[g] = P.at(P_N, j, r);
-    }
-  }
-  if (spk_i >= 0 && r == 0) {
-    A.spk_count[cable] = count;
-    A.spk_first[cable] = first;
-  }
-  if (spk_i >= 0 && r == spk_i / ch) A.spk_below[cable] = below;
-  if (spk_i2 >= 0 && r == spk_i2 / ch) A.spk_below2[cable] = below2;
-  __syncwarp();
+  item -= items16;
+  const int n8 = n_cables - n32 - n16;
+  pos0 = n32 + n16 + 4 * item;
+  pos_end = n_cables;
+  lanes = 8;
+  return item < (n8 + 3) / 4;
 }
 
 template <typename T, bool FAST, bool TAPE>
-__global__ void __launch_bounds__(kCableMaxWarps * 32) cable_run_kernel(CableArgsT<T> A, int ch_max,
-                                                                     PlaneLayout lay) {
+__global__ void __launch_bounds__(kCableMaxWarps * 32)
+    cable_run_kernel(CableArgsT<T> A, int ch_alloc, int nq, int geo_planes, int chan_planes) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5;
-  T* smw = reinterpret_cast<T*>(smem_raw) + (size_t)warp * lay.n_planes * ch_max * 32;
+  T* smw = reinterpret_cast<T*>(smem_raw) + (size_t)warp * nq * ch_alloc * 32;
   const int lane = threadIdx.x & 31;
   for (;;) {
-    int idx = 0;
-    if (lane == 0) idx = atomicAdd(A.counter, 1);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
-    if (idx >= A.n_cables) break;
-    const int cable = A.order ? A.order[idx] : idx;
-    const int K = (int)(A.cable_ptr[cable + 1] - A.cable_ptr[cable]);
-    const int ch = (K + 31) / 32;
-    if (ch > ch_max) {  // the host sized shared memory for smaller cables: flag, never skip silently
-      if (lane == 0) atomicOr(A.counter + 1, kErrChunk);
+    int item = 0;
+    if (lane == 0) item = atomicAdd(A.counter, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    int pos0, pos_end, lanes;
+    if (!item_range(item, A.n_cables, A.lanes_mode, A.n_lanes32, A.n_lanes16, pos0, pos_end,
+                    lanes))
+      break;
+    // rows per lane: the item's longest cable over its lanes
+    const int pos = pos0 + lane / lanes;
+    int K = 0;
+    if (pos < pos_end) {
+      const int c = A.order ? A.order[pos] : pos;
+      K = (int)(A.cable_ptr[c + 1] - A.cable_ptr[c]);
+    }
+    const int kmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)K);
+    const int ch = (kmax + lanes - 1) / lanes;
+    if (ch > ch_alloc) {  // the host sized shared memory for smaller cables:
+      if (lane == 0) atomicOr(A.counter + 1, kErrChunk);  // flag, never skip silently
       continue;
     }
-    run_cable<T, FAST, TAPE>(A, cable, smw, ch, lay);
+    if (ch > 0) run_rows<T, FAST, TAPE>(A, pos0, pos_end, lanes, ch, smw, nq, geo_planes != 0,
+                                        chan_planes != 0);
   }
 }
 
@@ -470,11 +213,12 @@ __global__ void __launch_bounds__(128) cable_solve_update_kernel(CableArgsT<T> A
 }
 
 template <typename T, bool FAST, bool TAPE = false>
-static int launch_cable_run(CableArgsT<T> A, int ch_max, const PlaneLayout& lay,
+static int launch_cable_run(CableArgsT<T> A, int ch_max, bool geo_planes, bool chan_planes,
                             cudaStream_t st) {
-  // one warp per cable in flight; long cables get fewer warps per block so
-  // the block's planes fit the 227 KB shared-memory limit
-  const size_t per_warp = (size_t)lay.n_planes * ch_max * 32 * sizeof(T);
+  // rows per lane: ch_max at 32 lanes, up to 8 on 16 or 8 lanes when split
+  const int ch_alloc = (A.lanes_mode != 0 && ch_max < 8) ? 8 : ch_max;
+  const int nq = rows_nq(geo_planes, chan_planes);
+  const size_t per_warp = (size_t)nq * ch_alloc * 32 * sizeof(T);
   const int wpb = persistent_wpb(A.wpb, per_warp);
   DGB_REQUIRE(wpb > 0, "cable too long for shared memory (%zu bytes per cable)", per_warp);
   const int threads = wpb * 32;
@@ -486,40 +230,27 @@ static int launch_cable_run(CableArgsT<T> A, int ch_max, const PlaneLayout& lay,
   DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
   if (per_sm < 1) per_sm = 1;
   int blocks = device_sm_count() * per_sm;
-  const int blocks_needed = (A.n_cables + wpb - 1) / wpb;
+  int items = A.n_cables;
+  if (A.lanes_mode != 0) {
+    const int n8 = A.n_cables - A.n_lanes32 - A.n_lanes16;
+    items = A.n_lanes32 + (A.n_lanes16 + 1) / 2 + (n8 + 3) / 4;
+  }
+  const int blocks_needed = (items + wpb - 1) / wpb;
   if (blocks > blocks_needed) blocks = blocks_needed;
   if (blocks < 1) blocks = 1;
   DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, 2 * sizeof(int32_t), st));
-  kern<<<blocks, threads, smem, st>>>(A, ch_max, lay);
+  kern<<<blocks, threads, smem, st>>>(A, ch_alloc, nq, geo_planes ? 1 : 0, chan_planes ? 1 : 0);
   DGB_LAUNCH_CHECK();
   return DGB_OK;
 }
 
-template <typename T>
-int cable_run_t(const dgb_cable_args* args, int ch_max, cudaStream_t st) {
-  CableArgsT<T> A = typed<T>(args);
-  const bool field = args->field != nullptr && args->ve_amp != nullptr;
-  const bool chan_planes = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) == 0;
-  const bool geo_planes = (args->flags & DGB_CABLE_UNIFORM_GEOMETRY) == 0;
-  const PlaneLayout lay = plane_layout(geo_planes, field, chan_planes);
-  if constexpr (sizeof(T) == 4) {
-    if (args->flags & DGB_CABLE_FAST_MATH) return launch_cable_run<T, true>(A, ch_max, lay, st);
-  }
-  return launch_cable_run<T, false>(A, ch_max, lay, st);
-}
-
-template <typename T>
-int cable_run_taped_t(const dgb_cable_args* args, void* tape, int ch_max, cudaStream_t st) {
+template <typename T, bool FAST, bool TAPE>
+int cable_run_launch(const dgb_cable_args* args, void* tape, int ch_max, cudaStream_t st) {
   CableArgsT<T> A = typed<T>(args);
   A.tape = (T*)tape;
-  const bool field = args->field != nullptr && args->ve_amp != nullptr;
   const bool chan_planes = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) == 0;
   const bool geo_planes = (args->flags & DGB_CABLE_UNIFORM_GEOMETRY) == 0;
-  const PlaneLayout lay = plane_layout(geo_planes, field, chan_planes);
-  if constexpr (sizeof(T) == 4) {
-    if (args->flags & DGB_CABLE_FAST_MATH) return launch_cable_run<T, true, true>(A, ch_max, lay, st);
-  }
-  return launch_cable_run<T, false, true>(A, ch_max, lay, st);
+  return launch_cable_run<T, FAST, TAPE>(A, ch_max, geo_planes, chan_planes, st);
 }
 
 template <typename T>
@@ -547,9 +278,11 @@ int cable_solve_update_t(const dgb_cable_args* args, const void* lower, const vo
   return DGB_OK;
 }
 
-#define DGB_INSTANTIATE_CABLE(T)                                                         \
-  template int cable_run_t<T>(const dgb_cable_args*, int, cudaStream_t);               \
-  template int cable_run_taped_t<T>(const dgb_cable_args*, void*, int, cudaStream_t);   \
+// Instantiations, split so that the persistent run variants and the plain
+// per-step kernels compile in parallel translation units.
+#define DGB_INSTANTIATE_CABLE_RUN(T, FAST, TAPE) \
+  template int cable_run_launch<T, FAST, TAPE>(const dgb_cable_args*, void*, int, cudaStream_t);
+#define DGB_INSTANTIATE_CABLE_PLAIN(T)                                                   \
   template int cable_assemble_t<T>(const dgb_cable_args*, int32_t, void*, void*, void*, \
                                    void*, cudaStream_t);                               \
   template int cable_solve_update_t<T>(const dgb_cable_args*, const void*, const void*, \

@@ -1,0 +1,420 @@
+// Persistent cable update of dgb_cable_run: one work item is one cable on 32
+// lanes, two cables on 16 lanes or four cables on 8 lanes (P lanes per cable:
+// the Thomas/PCR split).  Lane r of a cable owns rows r*ch .. r*ch+ch-1.  Per
+// step and row, fused (integrators/core.py:769-834,
+// integrators/implicit.py:569-664): gates at v_old (mechanisms/_cnexp.py:
+// 96-132, mod/HH.py:24-40) -> G, J (mod/HH.py:109-116) -> increment RHS and
+// diagonal -> the forward sweep of the lane's chunk elimination; then the
+// backward sweep, PCR across the P lanes by shuffles (chunk_solve.cuh), back
+// substitution and v += dv, spike checks and recording.
+//
+// Shared memory of a warp: ch_alloc rows of NQ planes, row-interleaved,
+//   element (row j, plane q, lane L) at [(j * NQ + q) * 32 + L]
+// so one row pointer reaches every plane of its row at a compile-time offset
+// (q * 32 elements) and a warp's access to one (j, q) touches 32 consecutive
+// words (conflict free).  The row loop is not unrolled: the kernel's code
+// stays small enough for the instruction cache while warps of different
+// cable lengths share an SM.
+//   planes 0..6   v, m, h, n, and the elimination's a', c', d'
+//   plane  7      extracellular axial term (constant while a pulse is on)
+//   planes 8..10  g_right, g_left, scale   (only when geometry varies)
+//   planes 11..14 gnabar, gkbar, gl, el    (only when channels vary)
+#pragma once
+#include "cable_common.cuh"
+#include "chunk_solve.cuh"
+
+namespace dgb {
+
+enum {
+  Q_V = 0, Q_M, Q_H, Q_N, Q_AP, Q_CP, Q_DP, Q_VAX,
+  Q_GR, Q_GL, Q_SC, Q_GNA, Q_GK, Q_GLK, Q_EL,
+  Q_BASE = 8,  // planes without per-compartment coefficients
+  Q_ALL = 15   // with geometry and channel planes
+};
+
+// Planes per row for a launch: per-compartment geometry or channels need all 15.
+__host__ __device__ inline int rows_nq(bool geo_planes, bool chan_planes) {
+  return (geo_planes || chan_planes) ? Q_ALL : Q_BASE;
+}
+
+// Coalesced copy between global rows [0, K) of one cable and its plane q:
+// the group's P lanes visit rows r, r + P, ... (row i lives in group lane
+// i / ch, slot i % ch).
+template <typename T>
+__device__ __forceinline__ void rows_load(T* wsm, int NQ, int q, int ch, int lane0, int P, int r,
+                                          const T* __restrict__ src, int K) {
+  for (int i = r; i < P * ch; i += P) {
+    const int j = i % ch, L = lane0 + i / ch;
+    wsm[(j * NQ + q) * 32 + L] = i < K ? src[i] : T(0);
+  }
+}
+template <typename T>
+__device__ __forceinline__ void rows_store(const T* wsm, int NQ, int q, int ch, int lane0, int P,
+                                           int r, T* dst, int K) {
+  for (int i = r; i < K; i += P) {
+    const int j = i % ch, L = lane0 + i / ch;
+    dst[i] = wsm[(j * NQ + q) * 32 + L];
+  }
+}
+
+template <typename T, bool FAST, bool TAPE>
+__device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int pos_end, int P,
+                                         int ch, T* wsm, int NQ, bool geo_planes,
+                                         bool chan_planes) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int grp = lane / P;
+  const int r = lane - grp * P;
+  const int lane0 = grp * P;
+  const int pos = pos0 + grp;
+  const int cable = pos < pos_end ? (A.order ? A.order[pos] : pos) : -1;
+  const int64_t off = cable >= 0 ? A.cable_ptr[cable] : 0;
+  const int K = cable >= 0 ? (int)(A.cable_ptr[cable + 1] - off) : 0;
+  const int row0 = r * ch;
+  const int rs = NQ * 32;  // elements from one row to the next
+  T* const p0 = wsm + lane;  // this lane's row 0
+  const bool use_ve = A.field != nullptr && A.ve_amp != nullptr;
+
+  // ---- load state and coefficients (rows past K are zero: identity rows)
+  rows_load<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
+  rows_load<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);
+  rows_load<T>(wsm, NQ, Q_H, ch, lane0, P, r, A.h + off, K);
+  rows_load<T>(wsm, NQ, Q_N, ch, lane0, P, r, A.n + off, K);
+  if (geo_planes) {
+    rows_load<T>(wsm, NQ, Q_GR, ch, lane0, P, r, A.g_right + off, K);
+    rows_load<T>(wsm, NQ, Q_GL, ch, lane0, P, r, A.g_left + off, K);
+    rows_load<T>(wsm, NQ, Q_SC, ch, lane0, P, r, A.scale + off, K);
+  }
+  if (chan_planes) {
+    rows_load<T>(wsm, NQ, Q_GNA, ch, lane0, P, r, A.gnabar + off, K);
+    rows_load<T>(wsm, NQ, Q_GK, ch, lane0, P, r, A.gkbar + off, K);
+    rows_load<T>(wsm, NQ, Q_GLK, ch, lane0, P, r, A.gl + off, K);
+    rows_load<T>(wsm, NQ, Q_EL, ch, lane0, P, r, A.el + off, K);
+  }
+  if (use_ve) rows_load<T>(wsm, NQ, Q_VAX, ch, lane0, P, r, A.field + off, K);
+  __syncwarp();
+  // uniform coefficients: the cable's values, identical on every compartment
+  // (interior edges for g_right / g_left), so reading them once is exact
+  T gna_c = T(0), gk_c = T(0), gl_c = T(0), el_c = T(0);
+  if (!chan_planes && K > 0) {
+    gna_c = A.gnabar[off];
+    gk_c = A.gkbar[off];
+    gl_c = A.gl[off];
+    el_c = A.el[off];
+  }
+  T gr_c = T(0), glf_c = T(0), sc_c = T(0);
+  if (!geo_planes && K > 0) {
+    gr_c = K > 1 ? A.g_right[off] : T(0);
+    glf_c = K > 1 ? A.g_left[off + 1] : T(0);
+    sc_c = A.scale[off];
+  }
+  // coefficients of row j (pointer pr): zero past the cable's ends
+  auto coef = [&](const T* pr, int j, T& gr, T& glf, T& scl) {
+    if (geo_planes) {  // planes hold 0 past K, and 0 at the ends by contract
+      gr = pr[Q_GR * 32];
+      glf = pr[Q_GL * 32];
+      scl = pr[Q_SC * 32];
+    } else {
+      const int i = row0 + j;
+      gr = i < K - 1 ? gr_c : T(0);
+      glf = (i >= 1 && i < K) ? glf_c : T(0);
+      scl = i < K ? sc_c : T(0);
+    }
+  };
+
+  // extracellular drive: the axial ve term at ve = field * amp, evaluated
+  // once with the rounded operations of the per-step form (the field rows are
+  // replaced by the term in place, after every lane has read its neighbours)
+  T ve_amp = T(0), ve_delay = T(0), ve_pw = T(0);
+  if (use_ve) {
+    if (K > 0) {
+      ve_amp = A.ve_amp[cable];
+      ve_delay = A.ve_delay[cable];
+      ve_pw = A.ve_pw[cable];
+    }
+    T f_prev = r > 0 ? wsm[((ch - 1) * NQ + Q_VAX) * 32 + lane - 1] : T(0);
+    T f_hi = r < P - 1 ? wsm[Q_VAX * 32 + lane + 1] : T(0);
+    T fj = p0[Q_VAX * 32];
+    __syncwarp();
+    T* pr = p0;
+    for (int j = 0; j < ch; ++j, pr += rs) {
+      const T f_next = j < ch - 1 ? pr[rs + Q_VAX * 32] : f_hi;
+      T gr, glf, scl;
+      coef(pr, j, gr, glf, scl);
+      const T ve_l = mul_rn(f_prev, ve_amp), ve_c = mul_rn(fj, ve_amp);
+      const T ve_r = mul_rn(f_next, ve_amp);
+      pr[Q_VAX * 32] = mul_rn(gr, ve_r - ve_c) - mul_rn(glf, ve_c - ve_l);
+      f_prev = fj;
+      fj = f_next;
+    }
+    __syncwarp();
+  }
+  const int in_i = (A.in_idx && K > 0) ? A.in_idx[cable] : -1;
+  T in_amp = T(0), in_delay = T(0), in_pw = T(0), in_cm = T(0);
+  int in_j = -1;  // this lane's row of the clamp
+  if (in_i >= 0 && in_i < K) {
+    in_amp = A.in_amp[cable];
+    in_delay = A.in_delay[cable];
+    in_pw = A.in_pw[cable];
+    in_cm = A.cm_inv[off + in_i];
+    if (in_i / ch == r) in_j = in_i % ch;
+  }
+  // single-compartment trace and Active-style detection (count, first step)
+  auto vat = [&](int i) { return wsm[((i % ch) * NQ + Q_V) * 32 + lane0 + i / ch]; };
+  const int rec_i = (A.rec_idx && A.trace && K > 0) ? A.rec_idx[cable] : -1;
+  const int spk_i = (A.spk_idx && K > 0) ? A.spk_idx[cable] : -1;
+  const int spk_i2 = (A.spk_idx2 && spk_i >= 0) ? A.spk_idx2[cable] : -1;
+  int below = 1, below2 = 1, count = 0, first = -1;
+  if (spk_i >= 0 && r == 0) {
+    count = A.spk_count[cable];
+    first = A.spk_first[cable];
+    below = A.spk_below[cable];
+    if (spk_i2 >= 0) below2 = A.spk_below2[cable];
+  }
+  // raster: group lane q < n_rast keeps check q
+  int r_idx = -1, r_latch = 1, r_count = 0;
+  if (r < A.n_rast && K > 0) {
+    r_idx = A.rast_idx[(int64_t)cable * A.n_rast + r];
+    if (r_idx >= K) r_idx = -1;
+    if (r_idx >= 0) {
+      r_latch = A.rast_below[(int64_t)cable * A.n_rast + r];
+      r_count = A.rast_count[(int64_t)cable * A.n_rast + r];
+    }
+  }
+  if (rec_i >= 0 && r == 0) A.trace[(int64_t)cable * A.n_rec] = vat(rec_i);
+  if (A.trace_all) rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.trace_all + off, K);
+  if constexpr (TAPE) {
+    if (A.tape) {
+      T* tp = A.tape + off;
+      rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, tp, K);
+      rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, tp + A.n_comp, K);
+      rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, tp + 2 * A.n_comp, K);
+      rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, tp + 3 * A.n_comp, K);
+    }
+  }
+  __syncwarp();  // the first step rewrites rows other lanes just stored
+
+  bool live = K > 0;  // this group's cable is still advancing
+  const T dt = A.dt, dt_s = A.dt_s, q10 = A.q10, ena = A.ena, ek = A.ek;
+  for (int s = 0; s < A.n_steps; ++s) {
+    const T t = (T)(A.t0_ms + (double)(A.step0 + s) * A.dt_ms_d);
+    const bool ve_on = use_ve && rect_pulse<T>(t, ve_amp, ve_delay, ve_pw) != T(0);
+    const T Iin = in_j >= 0 ? rect_pulse<T>(t, in_amp, in_delay, in_pw) : T(0);
+
+    // ---- gates, membrane frame, row assembly fused with the forward sweep.
+    // Row 0 keeps its row (As, Bs, Cs, Ds); rows j >= 1 are eliminated against
+    // the previous one, x_j + a'_j x_s + c'_j x_{j+1} = d'_j, starting from
+    // (a', c', d') = (-1, 0, 0), which reproduces row 1's own division.
+    T As = T(0), Bs = T(1), Cs = T(0), Ds = T(0);
+    T ap = T(-1), cp = T(0), dp = T(0);
+    T v_prev = r > 0 ? wsm[((ch - 1) * NQ + Q_V) * 32 + lane - 1] : T(0);
+    const T v_hi = r < P - 1 ? wsm[Q_V * 32 + lane + 1] : T(0);
+    T vj = p0[Q_V * 32];
+    T* pr = p0;
+    for (int j = 0; j < ch; ++j, pr += rs) {
+      const T v_next = j < ch - 1 ? pr[rs + Q_V * 32] : v_hi;
+      T m = pr[Q_M * 32], h = pr[Q_H * 32], n = pr[Q_N * 32];
+      if constexpr (FAST) {
+        hh_gates_fast(vj, q10, dt, m, h, n);
+      } else {
+        hh_gates<T>(vj, q10, dt, m, h, n);
+      }
+      pr[Q_M * 32] = m;
+      pr[Q_H * 32] = h;
+      pr[Q_N * 32] = n;
+      T G, J;
+      if (chan_planes) {
+        hh_affine<T>(m, h, n, pr[Q_GNA * 32], pr[Q_GK * 32], pr[Q_GLK * 32], pr[Q_EL * 32], ena,
+                     ek, G, J);
+      } else {
+        hh_affine<T>(m, h, n, gna_c, gk_c, gl_c, el_c, ena, ek, G, J);
+      }
+      T gr, glf, scl;
+      coef(pr, j, gr, glf, scl);
+      // row i couples to i-1 through glf and to i+1 through gr; at a cable
+      // end (or past it) that coefficient is exactly zero
+      T fn = (J - mul_rn(G, vj)) * scl;
+      fn = fn + (mul_rn(gr, v_next - vj) - mul_rn(glf, vj - v_prev));
+      if (ve_on) fn = fn + pr[Q_VAX * 32];
+      if (j == in_j) fn = fn + Iin * in_cm;
+      const T b = T(1) - dt_s * ((-gr + -glf) - mul_rn(G, scl));
+      const T a = -dt_s * glf;
+      const T c = -dt_s * gr;
+      const T d = dt_s * fn;
+      if (j == 0) {
+        As = a;
+        Bs = b;
+        Cs = c;
+        Ds = d;
+      } else {
+        const T rinv = dv<T, FAST>(T(1), b - a * cp);
+        ap = -a * ap * rinv;
+        dp = (d - a * dp) * rinv;
+        cp = c * rinv;
+        pr[Q_AP * 32] = ap;
+        pr[Q_CP * 32] = cp;
+        pr[Q_DP * 32] = dp;
+      }
+      v_prev = vj;
+      vj = v_next;
+    }
+    // ---- backward sweep (rows ch-3 .. 1) and the lane's reduced row
+    T al, be, ga, de;
+    const T Ae = ap, Ce = cp, De = dp;  // row ch-1 (forward form)
+    if (ch == 1) {
+      al = As;
+      be = Bs;
+      ga = Cs;
+      de = Ds;
+    } else {
+      T a2 = ap, c2 = cp, d2 = dp;  // row 1 once the loop below has run
+      if (ch >= 3) {
+        T* q = p0 + (ch - 2) * rs;
+        a2 = q[Q_AP * 32];
+        c2 = q[Q_CP * 32];
+        d2 = q[Q_DP * 32];
+        for (int j = ch - 3; j >= 1; --j) {
+          q -= rs;
+          const T cj = q[Q_CP * 32];
+          d2 = q[Q_DP * 32] - cj * d2;
+          a2 = q[Q_AP * 32] - cj * a2;
+          c2 = -cj * c2;
+          q[Q_AP * 32] = a2;
+          q[Q_CP * 32] = c2;
+          q[Q_DP * 32] = d2;
+        }
+      }
+      T Bs2 = Bs, Cs2 = Cs, Ds2 = Ds;
+      if (ch >= 3) {
+        Bs2 = Bs - Cs * a2;
+        Cs2 = -Cs * c2;
+        Ds2 = Ds - Cs * d2;
+      }
+      T Ae_l = shfl_up<T>(Ae, 1, P), Ce_l = shfl_up<T>(Ce, 1, P), De_l = shfl_up<T>(De, 1, P);
+      if (r == 0) {
+        Ae_l = T(0);
+        Ce_l = T(0);
+        De_l = T(0);
+      }
+      al = -As * Ae_l;
+      be = Bs2 - As * Ce_l - Cs2 * Ae;
+      ga = -Cs2 * Ce;
+      de = Ds2 - As * De_l - Cs2 * De;
+    }
+    // ---- PCR across the P lanes, then back substitution
+#pragma unroll
+    for (int sh = 1; sh < 32; sh <<= 1) {
+      if (sh >= P) break;
+      T al_l = shfl_up<T>(al, sh, P), be_l = shfl_up<T>(be, sh, P);
+      T ga_l = shfl_up<T>(ga, sh, P), de_l = shfl_up<T>(de, sh, P);
+      T al_r = shfl_down<T>(al, sh, P), be_r = shfl_down<T>(be, sh, P);
+      T ga_r = shfl_down<T>(ga, sh, P), de_r = shfl_down<T>(de, sh, P);
+      const bool hl = r >= sh;
+      const bool hr = r + sh < P;
+      T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
+      T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
+      T al_n = hl ? -k1 * al_l : T(0);
+      T ga_n = hr ? -k2 * ga_r : T(0);
+      be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
+      de = de - (hl ? k1 * de_l : T(0)) - (hr ? k2 * de_r : T(0));
+      al = al_n;
+      ga = ga_n;
+    }
+    const T xs = dv<T, FAST>(de, be);
+    T xe = xs;
+    if (ch > 1) {
+      T xs_next = shfl_down<T>(xs, 1, P);
+      if (r == P - 1) xs_next = T(0);
+      xe = De - Ae * xs - Ce * xs_next;
+    }
+    __syncwarp();  // every lane has read its neighbours' v for this step
+    p0[Q_V * 32] = p0[Q_V * 32] + xs;
+    {
+      T* q = p0;
+      for (int j = 1; j < ch - 1; ++j) {
+        q += rs;
+        q[Q_V * 32] = q[Q_V * 32] + (q[Q_DP * 32] - q[Q_AP * 32] * xs - q[Q_CP * 32] * xe);
+      }
+    }
+    if (ch > 1) p0[(ch - 1) * rs + Q_V * 32] = p0[(ch - 1) * rs + Q_V * 32] + xe;
+    __syncwarp();  // new v visible to every lane of the group
+
+    // ---- detection (group lane 0), raster (group lanes < n_rast), recording
+    bool stop_now = false;
+    if (A.spk_idx) {
+      int edge = 0;
+      if (live && spk_i >= 0 && r == 0) {
+        const int above = vat(spk_i) >= A.spk_thr;
+        edge = above && below;
+        below = !above;
+        if (spk_i2 >= 0) {
+          const int above2 = vat(spk_i2) >= A.spk_thr;
+          edge = edge || (above2 && below2);
+          below2 = !above2;
+        }
+        if (edge) {
+          if (count == 0) first = s + 1;
+          count += 1;
+        }
+      }
+      stop_now = A.stop_on_spike && __shfl_sync(FULL, edge, lane0) && live;
+    }
+    if (live && r_idx >= 0) {
+      const int above = vat(r_idx) >= A.spk_thr;
+      if (above && r_latch) {
+        if (r_count < A.rast_cap)
+          A.rast_steps[((int64_t)cable * A.n_rast + r) * A.rast_cap + r_count] = A.step0 + s + 1;
+        r_count += 1;
+      }
+      r_latch = !above;
+    }
+    const bool rec_due = ((s + 1) % A.rec_every) == 0;
+    if (rec_due && live && rec_i >= 0 && r == 0)
+      A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = vat(rec_i);
+    if (rec_due && A.trace_all)
+      rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r,
+                    A.trace_all + (int64_t)((s + 1) / A.rec_every) * A.n_comp + off,
+                    live ? K : 0);
+    if constexpr (TAPE) {
+      if (A.tape) {
+        T* tp = A.tape + (int64_t)(s + 1) * 4 * A.n_comp + off;
+        rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, tp, K);
+        rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, tp + A.n_comp, K);
+        rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, tp + 2 * A.n_comp, K);
+        rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, tp + 3 * A.n_comp, K);
+      }
+    }
+    if (A.stop_on_spike) {
+      // a cable that fired stops here: its state is written now and frozen
+      if (stop_now) {
+        rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
+        rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);
+        rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, A.h + off, K);
+        rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, A.n + off, K);
+        live = false;
+      }
+      if (!__any_sync(FULL, live)) break;
+    }
+    __syncwarp();  // the next step rewrites rows other lanes just read
+  }
+  // ---- write back the state of cables still advancing, and the counters
+  if (live) {
+    rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
+    rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);
+    rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, A.h + off, K);
+    rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, A.n + off, K);
+  }
+  if (spk_i >= 0 && r == 0) {
+    A.spk_count[cable] = count;
+    A.spk_first[cable] = first;
+    A.spk_below[cable] = below;
+    if (spk_i2 >= 0) A.spk_below2[cable] = below2;
+  }
+  if (r_idx >= 0) {
+    A.rast_below[(int64_t)cable * A.n_rast + r] = r_latch;
+    A.rast_count[(int64_t)cable * A.n_rast + r] = r_count;
+  }
+  __syncwarp();
+}
+
+}  // namespace dgb

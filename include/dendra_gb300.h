@@ -252,7 +252,33 @@ typedef struct dgb_cable_args {
      cables in flight per CTA, 1, 2 or 4 (0 = 4); halved while the CTA's
      shared memory would exceed 227 KB.  The autotuner's knob. */
   int32_t warps_per_block;
-  int32_t reserved;  /* 0 */
+  /* raster (Raster / APCount / threshold_crossing at callbacks.py:2114,
+     _threshold_callbacks.py:50-53): n_rast (0..4) checked compartments per
+     cable.  For cable c and check q: local compartment rast_idx[c*n_rast+q]
+     (-1: none), the below latch rast_below[c*n_rast+q] (in/out, 1 = below),
+     the crossing count rast_count[c*n_rast+q] (in/out, accumulates over
+     calls) and the absolute step index (step0 + s + 1) of the count's k-th
+     crossing in rast_steps[(c*n_rast+q)*rast_cap + k] while k < rast_cap.
+     A final count above rast_cap means the later steps were not stored. */
+  int32_t n_rast;
+  const int32_t* rast_idx;
+  int32_t* rast_below;
+  int32_t* rast_count;
+  int64_t* rast_steps;
+  int32_t rast_cap;
+  /* lanes per cable, the Thomas/PCR split of the persistent run: each lane
+     eliminates ceil(K/lanes) rows (Thomas), the lanes' reduced rows are then
+     solved by PCR across the lanes.  lanes_mode 0: 32 lanes for every cable.
+     lanes_mode 1: the first n_lanes32 cables of `order` run 32 lanes, the next
+     n_lanes16 run 16 lanes (two cables per warp, K <= 128), the rest 8 lanes
+     (four per warp, K <= 64); order should list cables by non-increasing K. */
+  int32_t lanes_mode;
+  int32_t n_lanes32;
+  int32_t n_lanes16;
+  /* full voltage recording (Recorder(("v",)), callbacks.py:522):
+     trace_all[k * n_comp + g] = v of compartment g after k*rec_every steps of
+     this call, k = 0 .. n_steps/rec_every, in the state dtype (NULL: off) */
+  void* trace_all;
 } dgb_cable_args;
 
 /* dgb_cable_args.flags bits.

@@ -70,6 +70,7 @@ def _declare(L):
         getattr(L, "orc_cable_run" + sfx).argtypes = (
             [_I32, _I32, _I32, _P] + [_P] * 4 + [_P] * 9 + [_D] * 6
             + [_P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _P, _I32, _P, _P]
+            + [_P, _I32, _P, _P, _P, _I32, _P, _I64]
         )
         getattr(L, "orc_block3_thomas" + sfx).argtypes = [_I64, _I64, _P, _P, _P, _P, _P]
         getattr(L, "orc_cable_grad" + sfx).argtypes = (
@@ -211,7 +212,8 @@ def dhs_solve(d, a, b, parent, order, layer_ptr):
 
 
 def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
-              gate_f32: bool = False):
+              gate_f32: bool = False, record_all: bool = False, raster=None,
+              raster_cap: int = 64, step0: int = 0):
     """Run the HH cable update on a packed problem dict (see dendra_gb300.cable).
 
     ``p`` holds numpy arrays: cable_ptr, v, m, h, n (modified in place),
@@ -221,6 +223,12 @@ def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
     ``gate_f32`` evaluates the pulse gates on a float32 time grid (how a
     float32 model sees its pulses) while the arithmetic stays in p's dtype.
     Returns (trace, spk_count, spk_first, spk_below).
+
+    record_all / raster: with either, a fifth element is returned, a dict with
+    ``trace_all`` (1 + n_steps // rec_every, N) of every compartment's v and,
+    for ``raster`` ((B, R) local checked compartments, -1 none), ``rast_count``
+    (B, R), ``rast_steps`` (B, R, raster_cap) absolute crossing steps
+    (step0 + s + 1; -1 unused) and ``rast_below`` (B, R) latches.
     """
     dtype = p["v"].dtype
     sfx = _sfx(dtype)
@@ -247,6 +255,16 @@ def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
         keep[k] = arr(k, np.int32)
     spk_below2 = np.ones(B, dtype=np.int32)
     cable_ptr = np.ascontiguousarray(p["cable_ptr"], dtype=np.int64)
+    N = int(cable_ptr[-1])
+    trace_all = np.full((n_rec, N), np.nan, dtype=dtype) if record_all else None
+    if raster is not None:
+        r_idx = np.ascontiguousarray(raster, dtype=np.int32).reshape(B, -1)
+    else:
+        r_idx = np.zeros((B, 0), dtype=np.int32)
+    R = r_idx.shape[1]
+    r_below = np.ones((B, R), dtype=np.int32)
+    r_count = np.zeros((B, R), dtype=np.int32)
+    r_steps = np.full((B, R, max(int(raster_cap), 0)), -1, dtype=np.int64)
     getattr(lib(), "orc_cable_run" + sfx)(
         B, int(n_steps), int(rec_every), _ptr(cable_ptr),
         _ptr(p["v"]), _ptr(p["m"]), _ptr(p["h"]), _ptr(p["n"]),
@@ -260,9 +278,14 @@ def cable_run(p: dict, n_steps: int, rec_every: int = 1, t0_ms: float = 0.0,
         _ptr(keep["in_pw"]), _ptr(keep["rec_idx"]), _ptr(trace),
         _ptr(keep["spk_idx"]), float(p.get("spk_thr", 0.0)), _ptr(spk_below),
         _ptr(spk_count), _ptr(spk_first), int(bool(gate_f32)), _ptr(keep["spk_idx2"]),
-        _ptr(spk_below2),
+        _ptr(spk_below2), _ptr(trace_all), int(R), _ptr(r_idx), _ptr(r_below), _ptr(r_count),
+        int(raster_cap), _ptr(r_steps), int(step0),
     )
-    return trace, spk_count, spk_first, spk_below
+    if not record_all and raster is None:
+        return trace, spk_count, spk_first, spk_below
+    extra = {"trace_all": trace_all, "rast_count": r_count, "rast_steps": r_steps,
+             "rast_below": r_below}
+    return trace, spk_count, spk_first, spk_below, extra
 
 
 def cable_grad(p: dict, n_steps: int, trace_grad, rec_every: int = 1, t0_ms: float = 0.0,

@@ -419,7 +419,10 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
                       const REAL* in_delay, const REAL* in_pw, const int32_t* rec_idx,
                       REAL* trace, const int32_t* spk_idx, double spk_thr_d,
                       int32_t* spk_below, int32_t* spk_count, int32_t* spk_first,
-                      int32_t gate_f32, const int32_t* spk_idx2, int32_t* spk_below2) {
+                      int32_t gate_f32, const int32_t* spk_idx2, int32_t* spk_below2,
+                      REAL* trace_all, int32_t n_rast, const int32_t* rast_idx,
+                      int32_t* rast_below, int32_t* rast_count, int32_t rast_cap,
+                      int64_t* rast_steps, int64_t step0) {
   const F(cable_prob) P = {cable_ptr, g_right, g_left, scale, cm_inv, field, gnabar, gkbar, gl,
                            el, (REAL)ena_d, (REAL)ek_d, (REAL)q10_d, (REAL)dt_ms_d,
                            (REAL)dt_s_d, dt_ms_d, t0_ms, ve_amp, ve_delay, ve_pw, in_idx,
@@ -439,6 +442,9 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
       const int32_t si = spk_idx ? spk_idx[c] : -1;
       const int32_t si2 = spk_idx2 ? spk_idx2[c] : -1;
       if (trace && ri >= 0) trace[(int64_t)c * n_rec] = vv[ri];
+      const int64_t Kc = cable_ptr[c + 1] - o;
+      if (trace_all)
+        for (int64_t i = 0; i < Kc; ++i) trace_all[o + i] = vv[i];
       for (int32_t s = 0; s < n_steps; ++s) {
         F(cable_step)(&P, c, s, vv, mm, hh, nn, w, kmax);
         if (si >= 0) {
@@ -458,6 +464,23 @@ void F(orc_cable_run)(int32_t n_cables, int32_t n_steps, int32_t rec_every,
         }
         if (trace && ri >= 0 && ((s + 1) % rec_every) == 0)
           trace[(int64_t)c * n_rec + (s + 1) / rec_every] = vv[ri];
+        /* Raster / threshold_crossing: every upward crossing at each checked
+           compartment, with its absolute step */
+        for (int32_t q = 0; q < n_rast; ++q) {
+          const int64_t e = (int64_t)c * n_rast + q;
+          const int32_t ci = rast_idx[e];
+          if (ci < 0 || ci >= Kc) continue;
+          const int above = vv[ci] >= thr;
+          if (above && rast_below[e]) {
+            if (rast_count[e] < rast_cap) rast_steps[e * rast_cap + rast_count[e]] = step0 + s + 1;
+            rast_count[e] += 1;
+          }
+          rast_below[e] = !above;
+        }
+        if (trace_all && ((s + 1) % rec_every) == 0) {
+          REAL* row = trace_all + (int64_t)((s + 1) / rec_every) * cable_ptr[n_cables] + o;
+          for (int64_t i = 0; i < Kc; ++i) row[i] = vv[i];
+        }
       }
     }
     free(w);

@@ -11,24 +11,31 @@ from tests._cases import synthetic_population
 pytestmark = pytest.mark.gpu
 
 
-def test_cable_run_warps_per_block_choice_is_result_neutral(cuda):
+def test_cable_run_tuning_picks_a_candidate_and_cta_size_is_result_neutral(cuda):
+    """The tuner picks one of its (cables per CTA, lane split) candidates; the
+    CTA size alone never changes a result (the lane split changes rounding
+    only, within the oracle tolerances tested in test_config1_gpu.py)."""
+    from dendra_gb300.autotune import CABLE_RUN_CANDIDATES
+
     pop = synthetic_population(3, 300, 1, 401, torch.float32, cuda, fast_math=True)
     state = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
     best, timings = tune_cable_run(pop, n_steps=20, force=True)
-    assert best in (1, 2, 4) and pop.warps_per_block == best
-    assert set(timings) == {1, 2, 4}
-    outs = []
-    for wpb in (1, 2, 4):
-        for dst, src in zip((pop.v, pop.m, pop.h, pop.n), state):
-            dst.copy_(src)
-        pop.step_index = 0
-        pop.warps_per_block = wpb
-        res = pop.run(100, rec_idx=0, spk_idx=0)
-        pop.check_status()
-        outs.append((pop.v.clone(), res.trace.clone(), res.spk_count.clone()))
-    for other in outs[1:]:
-        for a, b in zip(outs[0], other):
-            assert torch.equal(a, b)
+    assert best in CABLE_RUN_CANDIDATES and pop.warps_per_block == best[0]
+    assert set(timings) == set(CABLE_RUN_CANDIDATES)
+    for split in (None, (128, 64)):
+        outs = []
+        for wpb in (1, 2, 4):
+            for dst, src in zip((pop.v, pop.m, pop.h, pop.n), state):
+                dst.copy_(src)
+            pop.step_index = 0
+            pop.warps_per_block = wpb
+            pop.lanes_split = split
+            res = pop.run(100, rec_idx=0, spk_idx=0)
+            pop.check_status()
+            outs.append((pop.v.clone(), res.trace.clone(), res.spk_count.clone()))
+        for other in outs[1:]:
+            for a, b in zip(outs[0], other):
+                assert torch.equal(a, b)
 
 
 def test_tridiag_lane_split_tuning(cuda):

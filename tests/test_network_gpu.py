@@ -41,7 +41,7 @@ def test_network_matches_oracle(cuda, dtype, seed):
     np.testing.assert_array_equal(raster, ref_raster)
     np.testing.assert_array_equal(net.spike_count.cpu().numpy(), pd["spike_count"])
     v = net.v.double().cpu().numpy()
-    tol = 1e-9 if dtype == torch.float64 else 2e-3
+    tol = 1e-9 if dtype == torch.float64 else 1e-3
     assert np.abs(v - pd["v"]).max() < tol
     # float32: 2400 rounded decay multiplies accumulate a few 1e-6 relative
     np.testing.assert_allclose(net.B.double().cpu().numpy(), pd["B"], rtol=1e-4 if dtype ==
