@@ -1372,6 +1372,8 @@ def main():
     ap.add_argument("--cables", type=int, default=16384,
                     help="cables per rank (a smaller case for profiling)")
     ap.add_argument("--timesteps", type=int, default=0, help="timesteps per run (default 2000)")
+    ap.add_argument("--launch", default="",
+                    help="c2: fixed 'wpb,k16,k8' instead of autotuning (profiling runs)")
     args = ap.parse_args()
     world, rank, local = _dist()
     if args.workload == "c3":
@@ -1414,7 +1416,12 @@ def main():
     comp_steps = pop.N * n_ts
     from dendra_gb300.autotune import tune_cable_run
 
-    wpb, tune_ms = tune_cable_run(pop, n_steps=100)
+    if args.launch:
+        wpb, tune_ms = tuple(int(x) for x in args.launch.split(",")), None
+        pop.warps_per_block = wpb[0]
+        pop.lanes_split = None if wpb[1:] == (0, 0) else wpb[1:]
+    else:
+        wpb, tune_ms = tune_cable_run(pop, n_steps=100)
     v0, m0, h0, n0 = (t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
 
     def reset():

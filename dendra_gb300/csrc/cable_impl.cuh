@@ -66,12 +66,13 @@ __device__ __forceinline__ bool item_range(int item, int n_cables, int lanes_mod
   return item < (n8 + 3) / 4;
 }
 
-template <typename T, bool FAST, bool TAPE>
-__global__ void __launch_bounds__(kCableMaxWarps * 32)
-    cable_run_kernel(CableArgsT<T> A, int ch_alloc, int nq, int geo_planes, int chan_planes) {
+template <typename T, bool FAST, bool TAPE, bool PLANES>
+__global__ void __launch_bounds__(kCableMaxWarps * 32) cable_run_kernel(CableArgsT<T> A,
+                                                                        int ch_alloc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5;
-  T* smw = reinterpret_cast<T*>(smem_raw) + (size_t)warp * nq * ch_alloc * 32;
+  T* smw = reinterpret_cast<T*>(smem_raw) +
+           (size_t)warp * RowsNQ<PLANES>::value * ch_alloc * 32;
   const int lane = threadIdx.x & 31;
   for (;;) {
     int item = 0;
@@ -94,8 +95,7 @@ __global__ void __launch_bounds__(kCableMaxWarps * 32)
       if (lane == 0) atomicOr(A.counter + 1, kErrChunk);  // flag, never skip silently
       continue;
     }
-    if (ch > 0) run_rows<T, FAST, TAPE>(A, pos0, pos_end, lanes, ch, smw, nq, geo_planes != 0,
-                                        chan_planes != 0);
+    if (ch > 0) run_rows<T, FAST, TAPE, PLANES>(A, pos0, pos_end, lanes, ch, smw);
   }
 }
 
@@ -212,18 +212,16 @@ __global__ void __launch_bounds__(128) cable_solve_update_kernel(CableArgsT<T> A
   }
 }
 
-template <typename T, bool FAST, bool TAPE = false>
-static int launch_cable_run(CableArgsT<T> A, int ch_max, bool geo_planes, bool chan_planes,
-                            cudaStream_t st) {
+template <typename T, bool FAST, bool TAPE, bool PLANES>
+static int launch_cable_run(CableArgsT<T> A, int ch_max, cudaStream_t st) {
   // rows per lane: ch_max at 32 lanes, up to 8 on 16 or 8 lanes when split
   const int ch_alloc = (A.lanes_mode != 0 && ch_max < 8) ? 8 : ch_max;
-  const int nq = rows_nq(geo_planes, chan_planes);
-  const size_t per_warp = (size_t)nq * ch_alloc * 32 * sizeof(T);
+  const size_t per_warp = (size_t)RowsNQ<PLANES>::value * ch_alloc * 32 * sizeof(T);
   const int wpb = persistent_wpb(A.wpb, per_warp);
   DGB_REQUIRE(wpb > 0, "cable too long for shared memory (%zu bytes per cable)", per_warp);
   const int threads = wpb * 32;
   const size_t smem = (size_t)wpb * per_warp;
-  auto kern = cable_run_kernel<T, FAST, TAPE>;
+  auto kern = cable_run_kernel<T, FAST, TAPE, PLANES>;
   DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   int per_sm = 0;
@@ -239,7 +237,7 @@ static int launch_cable_run(CableArgsT<T> A, int ch_max, bool geo_planes, bool c
   if (blocks > blocks_needed) blocks = blocks_needed;
   if (blocks < 1) blocks = 1;
   DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, 2 * sizeof(int32_t), st));
-  kern<<<blocks, threads, smem, st>>>(A, ch_alloc, nq, geo_planes ? 1 : 0, chan_planes ? 1 : 0);
+  kern<<<blocks, threads, smem, st>>>(A, ch_alloc);
   DGB_LAUNCH_CHECK();
   return DGB_OK;
 }
@@ -250,7 +248,8 @@ int cable_run_launch(const dgb_cable_args* args, void* tape, int ch_max, cudaStr
   A.tape = (T*)tape;
   const bool chan_planes = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) == 0;
   const bool geo_planes = (args->flags & DGB_CABLE_UNIFORM_GEOMETRY) == 0;
-  return launch_cable_run<T, FAST, TAPE>(A, ch_max, geo_planes, chan_planes, st);
+  if (chan_planes || geo_planes) return launch_cable_run<T, FAST, TAPE, true>(A, ch_max, st);
+  return launch_cable_run<T, FAST, TAPE, false>(A, ch_max, st);
 }
 
 template <typename T>

@@ -19,6 +19,13 @@
 //   plane  7      extracellular axial term (constant while a pulse is on)
 //   planes 8..10  g_right, g_left, scale   (only when geometry varies)
 //   planes 11..14 gnabar, gkbar, gl, el    (only when channels vary)
+// Rows past a cable's end (i >= K, padding of the last lanes) run the same
+// update with the cable's own membrane and axial coefficients but no
+// extracellular or clamp drive: the last real row has exactly zero coupling to
+// them (g_right = 0 there), so they never change a real row's value, and they
+// stay finite (undriven HH compartments; a NaN there would reach real rows
+// through 0 * NaN in the reduction).  With per-compartment planes they read
+// zero coefficients.
 #pragma once
 #include "cable_common.cuh"
 #include "chunk_solve.cuh"
@@ -32,10 +39,17 @@ enum {
   Q_ALL = 15   // with geometry and channel planes
 };
 
-// Planes per row for a launch: per-compartment geometry or channels need all 15.
-__host__ __device__ inline int rows_nq(bool geo_planes, bool chan_planes) {
-  return (geo_planes || chan_planes) ? Q_ALL : Q_BASE;
-}
+// Planes per row for a launch: per-compartment geometry or channels need all 15
+// (both sets are then read from planes).
+template <bool PLANES>
+struct RowsNQ {
+  static constexpr int value = PLANES ? Q_ALL : Q_BASE;
+};
+
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
+};
 
 // Coalesced copy between global rows [0, K) of one cable and its plane q:
 // the group's P lanes visit rows r, r + P, ... (row i lives in group lane
@@ -57,11 +71,12 @@ __device__ __forceinline__ void rows_store(const T* wsm, int NQ, int q, int ch, 
   }
 }
 
-template <typename T, bool FAST, bool TAPE>
+template <typename T, bool FAST, bool TAPE, bool PLANES>
 __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int pos_end, int P,
-                                         int ch, T* wsm, int NQ, bool geo_planes,
-                                         bool chan_planes) {
+                                         int ch, T* wsm) {
   constexpr unsigned FULL = 0xffffffffu;
+  constexpr int NQ = RowsNQ<PLANES>::value;
+  constexpr int rs = NQ * 32;  // elements from one row to the next
   const int lane = threadIdx.x & 31;
   const int grp = lane / P;
   const int r = lane - grp * P;
@@ -71,21 +86,18 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
   const int64_t off = cable >= 0 ? A.cable_ptr[cable] : 0;
   const int K = cable >= 0 ? (int)(A.cable_ptr[cable + 1] - off) : 0;
   const int row0 = r * ch;
-  const int rs = NQ * 32;  // elements from one row to the next
   T* const p0 = wsm + lane;  // this lane's row 0
   const bool use_ve = A.field != nullptr && A.ve_amp != nullptr;
 
-  // ---- load state and coefficients (rows past K are zero: identity rows)
+  // ---- load state and coefficients (rows past K start at zero)
   rows_load<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
   rows_load<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);
   rows_load<T>(wsm, NQ, Q_H, ch, lane0, P, r, A.h + off, K);
   rows_load<T>(wsm, NQ, Q_N, ch, lane0, P, r, A.n + off, K);
-  if (geo_planes) {
+  if constexpr (PLANES) {
     rows_load<T>(wsm, NQ, Q_GR, ch, lane0, P, r, A.g_right + off, K);
     rows_load<T>(wsm, NQ, Q_GL, ch, lane0, P, r, A.g_left + off, K);
     rows_load<T>(wsm, NQ, Q_SC, ch, lane0, P, r, A.scale + off, K);
-  }
-  if (chan_planes) {
     rows_load<T>(wsm, NQ, Q_GNA, ch, lane0, P, r, A.gnabar + off, K);
     rows_load<T>(wsm, NQ, Q_GK, ch, lane0, P, r, A.gkbar + off, K);
     rows_load<T>(wsm, NQ, Q_GLK, ch, lane0, P, r, A.gl + off, K);
@@ -96,29 +108,28 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
   // uniform coefficients: the cable's values, identical on every compartment
   // (interior edges for g_right / g_left), so reading them once is exact
   T gna_c = T(0), gk_c = T(0), gl_c = T(0), el_c = T(0);
-  if (!chan_planes && K > 0) {
+  T gr_c = T(0), glf_c = T(0), sc_c = T(0);
+  if (!PLANES && K > 0) {
     gna_c = A.gnabar[off];
     gk_c = A.gkbar[off];
     gl_c = A.gl[off];
     el_c = A.el[off];
-  }
-  T gr_c = T(0), glf_c = T(0), sc_c = T(0);
-  if (!geo_planes && K > 0) {
     gr_c = K > 1 ? A.g_right[off] : T(0);
     glf_c = K > 1 ? A.g_left[off + 1] : T(0);
     sc_c = A.scale[off];
   }
-  // coefficients of row j (pointer pr): zero past the cable's ends
+  // row j of this lane is the cable's last row (no right coupling)
+  const int j_last = K - 1 - row0;
+  // coefficients of row j (pointer pr); the first row has no left coupling
   auto coef = [&](const T* pr, int j, T& gr, T& glf, T& scl) {
-    if (geo_planes) {  // planes hold 0 past K, and 0 at the ends by contract
+    if constexpr (PLANES) {  // planes hold 0 past K, and 0 at the ends by contract
       gr = pr[Q_GR * 32];
       glf = pr[Q_GL * 32];
       scl = pr[Q_SC * 32];
     } else {
-      const int i = row0 + j;
-      gr = i < K - 1 ? gr_c : T(0);
-      glf = (i >= 1 && i < K) ? glf_c : T(0);
-      scl = i < K ? sc_c : T(0);
+      gr = j == j_last ? T(0) : gr_c;
+      glf = (j == 0 && r == 0) ? T(0) : glf_c;
+      scl = sc_c;
     }
   };
 
@@ -143,7 +154,8 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
       coef(pr, j, gr, glf, scl);
       const T ve_l = mul_rn(f_prev, ve_amp), ve_c = mul_rn(fj, ve_amp);
       const T ve_r = mul_rn(f_next, ve_amp);
-      pr[Q_VAX * 32] = mul_rn(gr, ve_r - ve_c) - mul_rn(glf, ve_c - ve_l);
+      // zero on rows past the end: they must not be driven (see the header)
+      pr[Q_VAX * 32] = row0 + j < K ? mul_rn(gr, ve_r - ve_c) - mul_rn(glf, ve_c - ve_l) : T(0);
       f_prev = fj;
       fj = f_next;
     }
@@ -207,56 +219,69 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
     // (a', c', d') = (-1, 0, 0), which reproduces row 1's own division.
     T As = T(0), Bs = T(1), Cs = T(0), Ds = T(0);
     T ap = T(-1), cp = T(0), dp = T(0);
-    T v_prev = r > 0 ? wsm[((ch - 1) * NQ + Q_V) * 32 + lane - 1] : T(0);
-    const T v_hi = r < P - 1 ? wsm[Q_V * 32 + lane + 1] : T(0);
-    T vj = p0[Q_V * 32];
-    T* pr = p0;
-    for (int j = 0; j < ch; ++j, pr += rs) {
-      const T v_next = j < ch - 1 ? pr[rs + Q_V * 32] : v_hi;
-      T m = pr[Q_M * 32], h = pr[Q_H * 32], n = pr[Q_N * 32];
-      if constexpr (FAST) {
-        hh_gates_fast(vj, q10, dt, m, h, n);
+    {
+      // the neighbouring lanes' boundary values
+      const T v_hi = r < P - 1 ? wsm[Q_V * 32 + lane + 1] : T(0);
+      const T v_lo = r > 0 ? wsm[((ch - 1) * NQ + Q_V) * 32 + lane - 1] : T(0);
+      // one row: gates advanced in place, returns the row's a, b, c, d
+      auto assemble = [&](T* pr, int j, T v_prev, T vj, T v_next, auto ve_tag, T& a, T& b,
+                          T& c, T& d) {
+        T m = pr[Q_M * 32], h = pr[Q_H * 32], n = pr[Q_N * 32];
+        if constexpr (FAST) {
+          hh_gates_fast_warp(vj, q10, dt, m, h, n);
+        } else {
+          hh_gates<T>(vj, q10, dt, m, h, n);
+        }
+        pr[Q_M * 32] = m;
+        pr[Q_H * 32] = h;
+        pr[Q_N * 32] = n;
+        T G, J;
+        if constexpr (PLANES) {
+          hh_affine<T>(m, h, n, pr[Q_GNA * 32], pr[Q_GK * 32], pr[Q_GLK * 32], pr[Q_EL * 32],
+                       ena, ek, G, J);
+        } else {
+          hh_affine<T>(m, h, n, gna_c, gk_c, gl_c, el_c, ena, ek, G, J);
+        }
+        T gr, glf, scl;
+        coef(pr, j, gr, glf, scl);
+        // row i couples to i-1 through glf and to i+1 through gr
+        T fn = (J - mul_rn(G, vj)) * scl;
+        fn = fn + (mul_rn(gr, v_next - vj) - mul_rn(glf, vj - v_prev));
+        if constexpr (decltype(ve_tag)::value) fn = fn + pr[Q_VAX * 32];
+        if (j == in_j) fn = fn + Iin * in_cm;
+        b = T(1) - dt_s * ((-gr + -glf) - mul_rn(G, scl));
+        a = -dt_s * glf;
+        c = -dt_s * gr;
+        d = dt_s * fn;
+      };
+      auto sweep = [&](auto ve_tag) {
+        T* pr = p0;
+        T vj = pr[Q_V * 32];
+        T v_next = ch > 1 ? pr[rs + Q_V * 32] : v_hi;
+        assemble(pr, 0, v_lo, vj, v_next, ve_tag, As, Bs, Cs, Ds);
+        T v_prev = vj;
+        vj = v_next;
+        for (int j = 1; j < ch; ++j) {
+          pr += rs;
+          v_next = j < ch - 1 ? pr[rs + Q_V * 32] : v_hi;
+          T a, b, c, d;
+          assemble(pr, j, v_prev, vj, v_next, ve_tag, a, b, c, d);
+          const T rinv = dv<T, FAST>(T(1), b - a * cp);
+          ap = -a * ap * rinv;
+          dp = (d - a * dp) * rinv;
+          cp = c * rinv;
+          pr[Q_AP * 32] = ap;
+          pr[Q_CP * 32] = cp;
+          pr[Q_DP * 32] = dp;
+          v_prev = vj;
+          vj = v_next;
+        }
+      };
+      if (ve_on) {
+        sweep(BoolTag<true>{});
       } else {
-        hh_gates<T>(vj, q10, dt, m, h, n);
+        sweep(BoolTag<false>{});
       }
-      pr[Q_M * 32] = m;
-      pr[Q_H * 32] = h;
-      pr[Q_N * 32] = n;
-      T G, J;
-      if (chan_planes) {
-        hh_affine<T>(m, h, n, pr[Q_GNA * 32], pr[Q_GK * 32], pr[Q_GLK * 32], pr[Q_EL * 32], ena,
-                     ek, G, J);
-      } else {
-        hh_affine<T>(m, h, n, gna_c, gk_c, gl_c, el_c, ena, ek, G, J);
-      }
-      T gr, glf, scl;
-      coef(pr, j, gr, glf, scl);
-      // row i couples to i-1 through glf and to i+1 through gr; at a cable
-      // end (or past it) that coefficient is exactly zero
-      T fn = (J - mul_rn(G, vj)) * scl;
-      fn = fn + (mul_rn(gr, v_next - vj) - mul_rn(glf, vj - v_prev));
-      if (ve_on) fn = fn + pr[Q_VAX * 32];
-      if (j == in_j) fn = fn + Iin * in_cm;
-      const T b = T(1) - dt_s * ((-gr + -glf) - mul_rn(G, scl));
-      const T a = -dt_s * glf;
-      const T c = -dt_s * gr;
-      const T d = dt_s * fn;
-      if (j == 0) {
-        As = a;
-        Bs = b;
-        Cs = c;
-        Ds = d;
-      } else {
-        const T rinv = dv<T, FAST>(T(1), b - a * cp);
-        ap = -a * ap * rinv;
-        dp = (d - a * dp) * rinv;
-        cp = c * rinv;
-        pr[Q_AP * 32] = ap;
-        pr[Q_CP * 32] = cp;
-        pr[Q_DP * 32] = dp;
-      }
-      v_prev = vj;
-      vj = v_next;
     }
     // ---- backward sweep (rows ch-3 .. 1) and the lane's reduced row
     T al, be, ga, de;

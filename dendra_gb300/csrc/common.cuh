@@ -220,6 +220,88 @@ __device__ __forceinline__ void hh_gates_fast(float v, float q10, float dt, floa
   n = cnexp_fast(n, q10 * alpha_n, q10 * (alpha_n + beta_n), dt);
 }
 
+// ---------------------------------------------------------------------------
+// float32 fast-math gate advance for code in which all 32 lanes of a warp
+// call it together (the persistent cable kernel's row loop).  Same formulas
+// as hh_gates_fast with three changes, each tested to the same float64 bound:
+//   * exponentials by __expf (ex2.approx of x log2 e);
+//   * the branch of vtrap and of the cnexp step is chosen per warp by vote:
+//     a side no lane needs is not evaluated, and lanes on different sides
+//     both evaluate and select;
+//   * when every lane's |z| = |b dt| <= 1/16, phi1 is its Taylor polynomial
+//     of degree 4 (truncation below 1.3e-9 relative, under float32
+//     rounding) instead of degree 9.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float phi1_deg4(float z) {
+  float value = z * (1.0f / 120.0f) + (1.0f / 24.0f);
+  value = value * z + (1.0f / 6.0f);
+  value = value * z + 0.5f;
+  value = value * z + 1.0f;
+  return value;
+}
+
+__device__ __forceinline__ void hh_gates_fast_warp(float v, float q10, float dt, float& m,
+                                                   float& h, float& n) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const float xm = -(v + 40.0f), xn = -(v + 55.0f);
+  const float qm = xm * 0.1f, qn = xn * 0.1f;
+  const float e10 = __expf(qm);                 // exp(-(v+40)/10)
+  const float e_n = e10 * 0.22313016014843f;    // exp(-(v+55)/10) = e10 * e^{-1.5}
+  const float e_h = e10 * 1.6487212707001282f;  // exp(-(v+35)/10) = e10 * e^{0.5}
+  const float u = -(v + 65.0f);
+  const float e18 = __expf(u * (1.0f / 18.0f));
+  const float e80 = __expf(u * (1.0f / 80.0f));
+  const float e80_2 = e80 * e80;
+  const float e20 = e80_2 * e80_2;
+  // vtrap(x, 10) = x / (exp(x/10) - 1), local series for |x/10| <= 1
+  const bool sm = fabsf(qm) <= 1.0f, sn = fabsf(qn) <= 1.0f;
+  float vm = __fdividef(xm, e10 - 1.0f), vn = __fdividef(xn, e_n - 1.0f);
+  if (__any_sync(FULL, sm || sn)) {
+    const float tm = (10.0f - xm * 0.5f) + xm * (qm * Math<float>::even_series(qm));
+    const float tn = (10.0f - xn * 0.5f) + xn * (qn * Math<float>::even_series(qn));
+    vm = sm ? tm : vm;
+    vn = sn ? tn : vn;
+  }
+  const float alpha_m = 0.1f * vm;
+  const float beta_m = 4.0f * e18;
+  const float alpha_h = 0.07f * e20;
+  const float beta_h = __fdividef(1.0f, e_h + 1.0f);
+  const float alpha_n = 0.01f * vn;
+  const float beta_n = 0.125f * e80;
+  const float am = q10 * alpha_m, bm = q10 * (alpha_m + beta_m);
+  const float ah = q10 * alpha_h, bh = q10 * (alpha_h + beta_h);
+  const float an = q10 * alpha_n, bn = q10 * (alpha_n + beta_n);
+  const float zm = -bm * dt, zh = -bh * dt, zn = -bn * dt;
+  const float zmax = fmaxf(fabsf(zm), fmaxf(fabsf(zh), fabsf(zn)));
+  const float rm = am - bm * m, rh = ah - bh * h, rn = an - bn * n;
+  if (__all_sync(FULL, zmax <= 0.0625f)) {
+    m = m + dt * rm * phi1_deg4(zm);
+    h = h + dt * rh * phi1_deg4(zh);
+    n = n + dt * rn * phi1_deg4(zn);
+    return;
+  }
+  float mt = m + dt * rm * Math<float>::phi1(zm);
+  float ht = h + dt * rh * Math<float>::phi1(zh);
+  float nt = n + dt * rn * Math<float>::phi1(zn);
+  if (__any_sync(FULL, zmax > 0.5f)) {
+    if (fabsf(zm) > 0.5f) {
+      const float eq = __fdividef(am, bm);
+      mt = eq + (m - eq) * __expf(zm);
+    }
+    if (fabsf(zh) > 0.5f) {
+      const float eq = __fdividef(ah, bh);
+      ht = eq + (h - eq) * __expf(zh);
+    }
+    if (fabsf(zn) > 0.5f) {
+      const float eq = __fdividef(an, bn);
+      nt = eq + (n - eq) * __expf(zn);
+    }
+  }
+  m = mt;
+  h = ht;
+  n = nt;
+}
+
 // Rounded product that the compiler may not fuse into an FMA.  Used where the
 // reference rounds a product before a cancelling add: the extracellular
 // voltages field*I (large, then differenced between neighbours), the axial
