@@ -225,36 +225,224 @@ def cpu_baseline(n_sample: int, steps: int, threads: int | None = None):
     return pop.N * steps / dt, pop.N, dt, oracle.num_threads()
 
 
+def _c2_samples():
+    """Two config-2 accuracy samples: every 128th cable, and the 128 most
+    strongly driven cables (largest |amp| / distance; about half of them fire)."""
+    from dendra_gb300.workloads import c2_spec
+
+    s = c2_spec()
+    drive = np.abs(s["amp"]) / s["dist"]
+    return (("every 128th cable", np.arange(0, 16384, 128)),
+            ("128 most strongly driven cables", np.sort(np.argsort(-drive)[:128])))
+
+
+def _c2_gpu_outputs(dev, fast_math, steps=2000, every=10):
+    """The float32 GPU run of each accuracy sample: traces of every compartment
+    every `every` steps and the crossings at both ends and the middle."""
+    from dendra_gb300.workloads import cable_population_c2
+
+    outs = []
+    for name, sub in _c2_samples():
+        pop = cable_population_c2(device=dev, subset=sub, fast_math=fast_math)
+        idx = np.array([[0, k // 2, k - 1] for k in pop.n_comp], dtype=np.int32)
+        import torch
+
+        r = pop.run(steps, rec_every=every, record_all=True, raster=torch.as_tensor(idx),
+                    raster_cap=64)
+        outs.append((name, sub, idx, r.trace_all.double().cpu().numpy(),
+                     r.raster.count.cpu().numpy(), r.raster.steps.cpu().numpy()))
+    return outs
+
+
+def _c2_accuracy(gpu_outs, steps=2000, every=10):
+    """float32 GPU vs the float64 oracle judge (float32 pulse grid, same inputs),
+    and the reference's own float32 arithmetic (the oracle in float32) beside it."""
+    import oracle
+    from dendra_gb300.workloads import cable_population_c2
+
+    res = {}
+    for name, sub, idx, tr, cnt, stp in gpu_outs:
+        pop = cable_population_c2(device="cpu", subset=sub)
+        p32 = pop.problem_dict()
+        p64 = {k: (v.astype(np.float64) if isinstance(v, np.ndarray) and v.dtype.kind == "f"
+                   else v) for k, v in p32.items()}
+        _, _, _, _, j = oracle.cable_run(p64, steps, rec_every=every, gate_f32=True,
+                                         record_all=True, raster=idx, raster_cap=64)
+        _, _, _, _, o32 = oracle.cable_run(pop.problem_dict(), steps, rec_every=every,
+                                           record_all=True)
+        res[name] = {
+            "max_abs_dv_mv": float(np.abs(tr - j["trace_all"]).max()),
+            "reference_float32_arithmetic_max_abs_dv_mv":
+                float(np.abs(o32["trace_all"].astype(np.float64) - j["trace_all"]).max()),
+            "spike_steps_identical": bool(np.array_equal(cnt, j["rast_count"]) and
+                                          np.array_equal(stp, j["rast_steps"])),
+            "crossings": int(j["rast_count"].sum()),
+            "cables_firing": int((j["rast_count"].max(axis=1) > 0).sum())}
+    return {"judge": "float64 oracle on the same inputs and float32 pulse grid; every "
+                     "compartment every 10 steps over 2000 steps; crossings at both ends and "
+                     "the middle", "samples": res}
+
+
+REF_DIR = os.path.join(ROOT, "baseline", "_ref")
+REF_SHIM = os.path.join(ROOT, "tests", "golden", "refshim")
+# config-2 cables grouped by compartment count, as the reference needs one
+# Unmyelinated population per K; the timed sample is these groups
+C2_REF_GROUPS = (51, 225, 401)
+
+
+def _ref_child(kind, steps, reps, warmup):
+    """Runs inside the reference child process (PYTHONPATH = the installed
+    reference + its import shims): the reference's own CPU solver path through
+    its public API, dn.Unmyelinated + insert(hh) + integrator bwd_euler_ub at
+    JIT=0 (pcr_solve_t without dendra-solvers), on all host cores.  Builds the
+    models once, runs `warmup` untimed and `reps` timed model.run calls of
+    `steps` timesteps each, and prints one JSON object with the
+    compartment-steps per call and the wall time of each timed call."""
+    import importlib.util
+    import types
+    import warnings
+
+    import torch
+
+    # networkx is imported by the reference's model modules but used only by
+    # its graph and tree front ends, never on the cable path timed here; where
+    # the host lacks it, an empty stand-in module satisfies the import
+    if importlib.util.find_spec("networkx") is None:
+        sys.modules["networkx"] = types.ModuleType("networkx")
+    import dendra as dn
+    from dendra.models.mod import hh
+
+    warnings.filterwarnings("ignore")
+    torch.set_num_threads(os.cpu_count() or 1)
+    models, groups = [], []
+    device = "cuda" if kind == "c2gpu" else "cpu"
+    if kind == "c2gpu":
+        kind = "c2"
+    with dn.ctx(JIT=0):
+        if kind == "c2":
+            from dendra_gb300.workloads import RHOE_OHM_CM, c2_spec
+
+            s = c2_spec()
+            for K in C2_REF_GROUPS:
+                idx = np.nonzero(s["ks"] == K)[0]
+                dx = float(np.mean(s["length"][idx] / K))
+                model = dn.Unmyelinated([float(d) for d in s["diam"][idx]], L=(K - 1) * dx,
+                                        dx=dx, celsius=6.3, v_init=-65.0, dtype=torch.float32,
+                                        integrator=dn.bwd_euler_ub(), rhoa=100.0)
+                model.insert(hh)
+                if device == "cuda":
+                    model.to("cuda")
+                model.initialize()
+                Kr = int(model.v.shape[-1])
+                x = (torch.arange(Kr, dtype=torch.float64) - (Kr - 1) / 2) * dx
+                r_cm = torch.sqrt(x[None, :] ** 2 +
+                                  torch.as_tensor(s["dist"][idx])[:, None] ** 2) * 1e-4
+                spatial = (RHOE_OHM_CM / (4 * torch.pi * r_cm)
+                           * torch.as_tensor(s["amp"][idx])[:, None]).to(torch.float32)
+                spatial = spatial.to(device)
+                extra = (spatial, dn.mono_rect(amp=1.0, delay=0.0, pw=0.1))
+                models.append((model, 0.005, dict(extra=extra)))
+                groups.append([K, int(len(idx)), Kr])
+        else:  # c1: 64 x 101 float64 cables, somatic clamp, Recorder(v) of every compartment
+            rng = np.random.default_rng(1)
+            amp = torch.as_tensor(rng.uniform(0.05, 0.5, 64) * 1e-6).reshape(64, 1)
+            model = dn.Unmyelinated([1.0] * 64, L=1000.0, dx=10.0, celsius=6.3, v_init=-65.0,
+                                    dtype=torch.float64, integrator=dn.bwd_euler_ub(),
+                                    rhoa=100.0)
+            model.insert(hh)
+            model[..., 0].inject(dn.mono_rect(amp=amp, delay=5.0, pw=1.0))
+            model.initialize()
+            models.append((model, 0.025, dict(callbacks=[dn.Recorder(("v",))])))
+            groups.append([101, 64, int(model.v.shape[-1])])
+        units = sum(int(m.v.numel()) for m, _, _ in models) * steps
+        times = []
+        for rep in range(warmup + reps):
+            secs = 0.0
+            for model, dt, kw in models:
+                model.initialize()
+                if device == "cuda":
+                    torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                model.run(dt=dt, duration=steps * dt, **kw)
+                if device == "cuda":
+                    torch.cuda.synchronize()
+                secs += time.perf_counter() - t0
+            if rep >= warmup:
+                times.append(secs)
+    print(json.dumps({"units": units, "times": times, "groups": groups,
+                      "threads": torch.get_num_threads(), "cores": os.cpu_count(),
+                      "torch": torch.__version__}), flush=True)
+
+
+def reference_cpu(kind, steps, reps=1, warmup=0, timeout=900):
+    """Time the installed reference (baseline/_ref) in a child process; returns
+    its JSON dict, or {"error": why} when the reference cannot run here."""
+    if not os.path.isdir(os.path.join(REF_DIR, "dendra")):
+        return {"error": "reference not installed in baseline/_ref"}
+    env = dict(os.environ)
+    env["PYTHONPATH"] = os.pathsep.join([REF_DIR, REF_SHIM, ROOT, env.get("PYTHONPATH", "")])
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--ref-child", kind,
+           "--ref-steps", str(steps), "--steps", str(reps), "--warmup", str(warmup)]
+    try:
+        r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=timeout)
+    except subprocess.TimeoutExpired:
+        return {"error": f"reference run exceeded {timeout} s"}
+    for line in reversed(r.stdout.splitlines()):
+        if line.startswith("{"):
+            return json.loads(line)
+    tail = (r.stderr or r.stdout).strip().splitlines()[-1:] or ["no output"]
+    return {"error": f"reference run failed (rc {r.returncode}): {tail[0][:300]}"}
+
+
+def reference_baseline(kind, steps, reps=1, warmup=0):
+    """cpu_baseline dict of the reference's own CPU path, or None (with the reason)."""
+    r = reference_cpu(kind, steps, reps, warmup)
+    if "error" in r:
+        return None, r["error"]
+    secs = float(np.median(r["times"]))
+    if kind == "c2":
+        what = (f"config-2 groups K={list(C2_REF_GROUPS)} ({sum(g[1] for g in r['groups'])} "
+                "cables with their own diameters and electrodes, one Unmyelinated population "
+                f"per K) x {steps} timesteps, float32")
+    else:
+        what = f"config 1 (64 x 101 cables, float64, Recorder(v)) for {steps} of its 2000 steps"
+    return {"value": r["units"] / secs, "unit": METRIC, "cores": r["threads"],
+            "kind": "reference",
+            "sample": f"{what}; the reference's model.run at JIT=0 (pcr_solve_t), torch "
+                      f"{r['torch']} with {r['threads']} threads", "seconds": secs}, None
+
+
 def run_reference(args, world, rank):
+    """Reference arm of config 2: the reference's own PyTorch CPU solver
+    (baseline/_ref, model.run through its public API) on all host cores, on
+    three of config 2's equal-K groups (their own cables, float32,
+    extracellular pulse) for --ref-steps timesteps per bench step.  The C port
+    of the same update (oracle) is timed beside it and reported as a second
+    figure; it becomes the line's value only when the reference cannot run."""
     if rank != 0:
         return
-    n_sample = args.sample
-    steps = 2000
-    vals = []
-    for _ in range(args.warmup):
-        cpu_baseline(max(8, n_sample // 8), 50)
-    last = None
-    for _ in range(args.steps):
-        v, n_comp, secs, cores = cpu_baseline(n_sample, steps)
-        vals.append(v)
-        last = (n_comp, secs, cores)
-    value = float(np.median(vals))
+    cpu, why = reference_baseline("c2", args.ref_steps, args.steps, args.warmup)
+    pv, n_comp, psecs, pcores = cpu_baseline(args.sample, 200)
+    port = {"value": pv, "unit": METRIC, "cores": pcores, "kind": "port",
+            "sample": f"{args.sample} of 16384 cables ({n_comp} compartments) x 200 timesteps, "
+                      "float32, the oracle's C restatement"}
+    if cpu is None:
+        cpu, ms = dict(port, note=why), psecs * 1e3
+    else:
+        ms = cpu.pop("seconds") * 1e3
+    value = cpu["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": last[1] * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": "c2-uneven-hh-cables-extracellular", "n_cables": 16384,
-                   "k_range": [51, 401], "dt_ms": 0.005, "timesteps": steps,
-                   "sample_cables": n_sample},
-        "cpu_baseline": {"value": value, "unit": METRIC, "cores": last[2], "kind": "port",
-                         "sample": f"{n_sample} of 16384 cables ({last[0]} compartments) x "
-                                   f"{steps} timesteps, float32, per bench step"},
+                   "k_range": [51, 401], "dt_ms": 0.005, "timesteps": 2000},
+        "cpu_baseline": cpu, "cpu_port": port,
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
-
 
 
 def _reference_solve_line(args, world, metric, cfg, units, solve, sample):
@@ -284,6 +472,184 @@ def _reference_solve_line(args, world, metric, cfg, units, solve, sample):
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+C1_RASTER = (0, 5, -5)  # soma and the reference Raster's default node_check [5, -5]
+
+
+def _c1_problem():
+    """Config-1 population on the host (float64) with its raster indices."""
+    import torch
+
+    from dendra_gb300.workloads import cable_population_c1
+
+    pop = cable_population_c1(device="cpu", dtype=torch.float64)
+    idx = np.array([[c % k for c in C1_RASTER] for k in pop.n_comp], dtype=np.int32)
+    return pop, idx
+
+
+def _c1_oracle(threads=None):
+    """The float64 oracle on the full config-1 run: (seconds, outputs, cores)."""
+    import oracle
+
+    pop, idx = _c1_problem()
+    p = pop.problem_dict()
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    from dendra_gb300.workloads import C1_STEPS
+
+    t0 = time.perf_counter()
+    _, _, _, _, out = oracle.cable_run(p, C1_STEPS, record_all=True, raster=idx, raster_cap=256)
+    return time.perf_counter() - t0, out, oracle.num_threads(), pop.N * C1_STEPS
+
+
+def bench_c1(args, world, rank, local):
+    """Config 1: 64 HH cables x 101 compartments (L 1000 um, dx 10 um, diam 1 um,
+    Ra 100 ohm cm), float64, backward Euler + cnexp at dt 0.025 ms for 2000
+    steps, a 1 ms somatic clamp at 5 ms of U[0.05, 0.5] nA.  One bench step is
+    the whole run with its outputs: the full (2001, 64, 101) voltage trace and
+    every 0 mV upward crossing at the soma and at compartments 5 and -5, from
+    one persistent launch."""
+    cfg = {"workload": "c1-hh-cables-full-traces", "n_cables": 64, "compartments": 101,
+           "dt_ms": 0.025, "timesteps": 2000, "state_dtype": "float64",
+           "outputs": "full (2001, 64, 101) v trace + every 0 mV upward crossing at "
+                      "compartments 0, 5, -5"}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        secs, _, cores, units = _c1_oracle()
+        port = {"value": units / secs, "unit": METRIC, "cores": cores, "kind": "port",
+                "sample": "the whole config-1 run (12.9 M compartment-steps, full traces and "
+                          "raster), the oracle's C restatement"}
+        cpu, why = reference_baseline("c1", args.ref_steps * 5, args.steps, args.warmup)
+        if cpu is None:
+            cpu, ms = dict(port, note=why), secs * 1e3
+        else:
+            ms = cpu.pop("seconds") * 1e3
+        value = cpu["value"]
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": METRIC,
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+                "cpu_baseline": cpu, "cpu_port": port,
+                "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    import torch
+
+    import dendra_gb300
+    from dendra_gb300.workloads import C1_STEPS, cable_population_c1
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dendra_gb300.load()
+    pop = cable_population_c1(device=dev)
+    state0 = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
+
+    def reset():
+        for dst, src in zip((pop.v, pop.m, pop.h, pop.n), state0):
+            dst.copy_(src)
+        pop.step_index, pop.t = 0, 0.0
+
+    def run():
+        reset()
+        return pop.run(C1_STEPS, record_all=True, raster=list(C1_RASTER), raster_cap=256,
+                       spk_thr=0.0)
+
+    for _ in range(max(3, args.warmup)):
+        run()
+    torch.cuda.synchronize()
+    pop.check_status()
+    flush = torch.ones(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.sum()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            res = run()
+            e1.record(st)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times))
+    units = pop.N * C1_STEPS
+    value = units / (ms * 1e-3)
+    trace = res.trace_all.cpu().numpy()
+    rast = {k: getattr(res.raster, k).cpu().numpy() for k in ("count", "steps")}
+
+    # end to end through the public API: inputs from pinned host memory, the
+    # full trace and the raster back to pinned host memory
+    host_in = {k: v.detach().cpu().pin_memory() for k, v in pop._dev.items()}
+    host_state = [t.cpu().pin_memory() for t in state0]
+    h2d = sum(t.numel() * t.element_size() for t in host_in.values())
+    h2d += sum(t.numel() * t.element_size() for t in host_state)
+    out_tr = torch.empty(trace.shape, dtype=torch.float64).pin_memory()
+    out_cnt = torch.empty(rast["count"].shape, dtype=torch.int32).pin_memory()
+    out_steps = torch.empty(rast["steps"].shape, dtype=torch.int64).pin_memory()
+    d2h = sum(t.numel() * t.element_size() for t in (out_tr, out_cnt, out_steps))
+
+    def e2e_step():
+        for k, t in host_in.items():
+            pop._dev[k].copy_(t, non_blocking=True)
+        for dst, src in zip((pop.v, pop.m, pop.h, pop.n), host_state):
+            dst.copy_(src, non_blocking=True)
+        pop.step_index, pop.t = 0, 0.0
+        r = pop.run(C1_STEPS, record_all=True, raster=list(C1_RASTER), raster_cap=256,
+                    spk_thr=0.0)
+        out_tr.copy_(r.trace_all, non_blocking=True)
+        out_cnt.copy_(r.raster.count, non_blocking=True)
+        out_steps.copy_(r.raster.steps, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    peak, peak_kind = _peaks()
+    achieved = 2 * ALG_BYTES_PER_COMP_STEP * units / (ms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {**cfg, "l2": "flushed between timed steps (256 MiB read, outside the events)",
+                   "launch": "one persistent dgb_cable_run launch per step (trace_all + raster)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": (f"{2 * ALG_BYTES_PER_COMP_STEP} algorithmic B per float64 "
+                              "compartment-step of the unfused update; 64 cables occupy 64 "
+                              f"warps of the GPU: latency bound, not HBM bound ({peak_kind} "
+                              "copy bandwidth)")},
+        "e2e": {"value": units / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clocks.summary(),
+        "spikes": {"crossings_soma": int(rast["count"][:, 0].sum()),
+                   "cables_firing": int((rast["count"][:, 0] > 0).sum())},
+    }
+    if rank == 0 and not args.no_cpu:
+        secs, ref, cores, _ = _c1_oracle()
+        port = {"value": units / secs, "unit": METRIC, "cores": cores, "kind": "port",
+                "sample": "the whole config-1 run, float64 oracle, full traces and raster"}
+        cpu, why = reference_baseline("c1", 200)
+        if cpu is None:
+            cpu = dict(port, note=why)
+        else:
+            cpu.pop("seconds")
+        line["cpu_baseline"] = cpu
+        line["cpu_port"] = port
+        line["accuracy"] = {
+            "max_abs_dv_mv_vs_float64_oracle": float(np.abs(trace - ref["trace_all"]).max()),
+            "spike_steps_identical": bool(np.array_equal(rast["count"], ref["rast_count"]) and
+                                          np.array_equal(rast["steps"], ref["rast_steps"])),
+            "judge": "float64 CPU oracle of the reference update, same inputs"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
 
 C3_BYTES_PER_COMP_STEP = 24  # unfused tree step: v r/w 8 B + main/rhs/axial/parent 16 B
 
@@ -1360,8 +1726,9 @@ def main():
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c3", "c4", "c5", "bt", "delay", "tree", "tridiag"],
-                    help="c2: uneven cable population (default); c3: branched-cell network; "
+                    choices=["c1", "c2", "c3", "c4", "c5", "bt", "delay", "tree", "tridiag"],
+                    help="c1: 64 x 101 float64 cables with full traces and rasters; "
+                         "c2: uneven cable population (default); c3: branched-cell network; "
                          "c4: adjoint gradient of a trace fit; "
                          "c5: learned threshold proposal vs plain bisection; "
                          "bt: 3x3 block-tridiagonal (multi-layer extracellular) solves; "
@@ -1372,10 +1739,17 @@ def main():
     ap.add_argument("--cables", type=int, default=16384,
                     help="cables per rank (a smaller case for profiling)")
     ap.add_argument("--timesteps", type=int, default=0, help="timesteps per run (default 2000)")
+    ap.add_argument("--ref-steps", type=int, default=100,
+                    help="timesteps of each reference CPU sample (reference arm)")
+    ap.add_argument("--ref-child", default="", help=argparse.SUPPRESS)
     ap.add_argument("--launch", default="",
                     help="c2: fixed 'wpb,k16,k8' instead of autotuning (profiling runs)")
     args = ap.parse_args()
+    if args.ref_child:
+        return _ref_child(args.ref_child, args.ref_steps, args.steps, args.warmup)
     world, rank, local = _dist()
+    if args.workload == "c1":
+        return bench_c1(args, world, rank, local)
     if args.workload == "c3":
         return bench_c3(args, world, rank, local)
     if args.workload == "c4":
@@ -1457,7 +1831,7 @@ def main():
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(st)
-            pop.run(n_ts)
+            pop.run(n_ts, spk_idx=0)  # with the spike detection (count and first step)
             e1.record(st)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
@@ -1594,10 +1968,19 @@ def main():
         line["speedup_vs_plain_eager"] = value / eager["value"]
         line["gpu_launches"] += 0  # plain path runs outside the timed region
     if rank == 0 and not args.no_cpu:
+        gpu_outs = _c2_gpu_outputs(dev, fast_math=not args.exact)
         v, n_comp, secs, cores = cpu_baseline(args.sample, 200)
-        line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
-                                "sample": f"{args.sample} of 16384 cables ({n_comp} "
-                                          f"compartments) x 200 timesteps, float32"}
+        port = {"value": v, "unit": METRIC, "cores": cores, "kind": "port",
+                "sample": f"{args.sample} of 16384 cables ({n_comp} compartments) x 200 "
+                          "timesteps, float32, the oracle's C restatement"}
+        cpu, why = reference_baseline("c2", 50)
+        if cpu is None:
+            cpu = dict(port, note=why)
+        else:
+            cpu.pop("seconds")
+        line["cpu_baseline"] = cpu
+        line["cpu_port"] = port
+        line["fp32_vs_fp64"] = _c2_accuracy(gpu_outs)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg is not None:
