@@ -71,6 +71,38 @@ __device__ __forceinline__ void rows_store(const T* wsm, int NQ, int q, int ch, 
   }
 }
 
+// First step s in [0, n_steps] whose stimulus time t(s) = T(t0 + (step0 + s) dt)
+// is >= tb (n_steps when none).  t(s) never decreases with s, so a rectangular
+// pulse on [delay, delay + pw) is on exactly for s in
+// [first_step_at(delay), first_step_at(delay + pw)): the same steps as testing
+// t(s) every step, found once per cable instead of per step.
+template <typename T>
+__device__ __forceinline__ int first_step_at(const CableArgsT<T>& A, T tb) {
+  int lo = 0, hi = A.n_steps;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    const T t = (T)(A.t0_ms + (double)(A.step0 + mid) * A.dt_ms_d);
+    if (t >= tb) {
+      hi = mid;
+    } else {
+      lo = mid + 1;
+    }
+  }
+  return lo;
+}
+
+// Steps [s0, s1) during which the pulse (amp on [delay, delay + pw)) is nonzero.
+template <typename T>
+__device__ __forceinline__ void pulse_steps(const CableArgsT<T>& A, T amp, T delay, T pw,
+                                            int& s0, int& s1) {
+  const T stop = delay + pw;
+  s0 = s1 = 0;
+  if (!(amp != T(0)) || stop != stop || delay != delay) return;
+  s0 = first_step_at<T>(A, delay);
+  s1 = first_step_at<T>(A, stop);
+  if (s1 < s0) s1 = s0;
+}
+
 template <typename T, bool FAST, bool TAPE, bool PLANES>
 __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int pos_end, int P,
                                          int ch, T* wsm) {
@@ -118,6 +150,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
     glf_c = K > 1 ? A.g_left[off + 1] : T(0);
     sc_c = A.scale[off];
   }
+  const T glel_c = mul_rn(gl_c, el_c);  // the leak's reversal term, rounded as per row
   // row j of this lane is the cable's last row (no right coupling)
   const int j_last = K - 1 - row0;
   // coefficients of row j (pointer pr); the first row has no left coupling
@@ -171,11 +204,19 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
     in_cm = A.cm_inv[off + in_i];
     if (in_i / ch == r) in_j = in_i % ch;
   }
-  // single-compartment trace and Active-style detection (count, first step)
-  auto vat = [&](int i) { return wsm[((i % ch) * NQ + Q_V) * 32 + lane0 + i / ch]; };
+  // pulse steps of the extracellular drive and of the clamp
+  int ve_s0 = 0, ve_s1 = 0, in_s0 = 0, in_s1 = 0;
+  if (use_ve && K > 0) pulse_steps<T>(A, ve_amp, ve_delay, ve_pw, ve_s0, ve_s1);
+  if (in_j >= 0) pulse_steps<T>(A, in_amp, in_delay, in_pw, in_s0, in_s1);
+  // single-compartment trace and Active-style detection (count, first step);
+  // v of compartment i sits at vofs(i) of the warp's planes
+  auto vofs = [&](int i) { return ((i % ch) * NQ + Q_V) * 32 + lane0 + i / ch; };
   const int rec_i = (A.rec_idx && A.trace && K > 0) ? A.rec_idx[cable] : -1;
   const int spk_i = (A.spk_idx && K > 0) ? A.spk_idx[cable] : -1;
   const int spk_i2 = (A.spk_idx2 && spk_i >= 0) ? A.spk_idx2[cable] : -1;
+  const int rec_o = rec_i >= 0 ? vofs(rec_i) : 0;
+  const int spk_o = spk_i >= 0 ? vofs(spk_i) : 0;
+  const int spk_o2 = spk_i2 >= 0 ? vofs(spk_i2) : 0;
   int below = 1, below2 = 1, count = 0, first = -1;
   if (spk_i >= 0 && r == 0) {
     count = A.spk_count[cable];
@@ -184,16 +225,17 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
     if (spk_i2 >= 0) below2 = A.spk_below2[cable];
   }
   // raster: group lane q < n_rast keeps check q
-  int r_idx = -1, r_latch = 1, r_count = 0;
+  int r_idx = -1, r_latch = 1, r_count = 0, r_o = 0;
   if (r < A.n_rast && K > 0) {
     r_idx = A.rast_idx[(int64_t)cable * A.n_rast + r];
     if (r_idx >= K) r_idx = -1;
     if (r_idx >= 0) {
+      r_o = vofs(r_idx);
       r_latch = A.rast_below[(int64_t)cable * A.n_rast + r];
       r_count = A.rast_count[(int64_t)cable * A.n_rast + r];
     }
   }
-  if (rec_i >= 0 && r == 0) A.trace[(int64_t)cable * A.n_rec] = vat(rec_i);
+  if (rec_i >= 0 && r == 0) A.trace[(int64_t)cable * A.n_rec] = wsm[rec_o];
   if (A.trace_all) rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.trace_all + off, K);
   if constexpr (TAPE) {
     if (A.tape) {
@@ -207,11 +249,11 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
   __syncwarp();  // the first step rewrites rows other lanes just stored
 
   bool live = K > 0;  // this group's cable is still advancing
+  int rec_left = A.rec_every, rec_k = 0;  // steps to the next record, records so far
   const T dt = A.dt, dt_s = A.dt_s, q10 = A.q10, ena = A.ena, ek = A.ek;
   for (int s = 0; s < A.n_steps; ++s) {
-    const T t = (T)(A.t0_ms + (double)(A.step0 + s) * A.dt_ms_d);
-    const bool ve_on = use_ve && rect_pulse<T>(t, ve_amp, ve_delay, ve_pw) != T(0);
-    const T Iin = in_j >= 0 ? rect_pulse<T>(t, in_amp, in_delay, in_pw) : T(0);
+    const bool ve_on = s >= ve_s0 && s < ve_s1;
+    const T Iin = (s >= in_s0 && s < in_s1) ? in_amp : T(0);
 
     // ---- gates, membrane frame, row assembly fused with the forward sweep.
     // Row 0 keeps its row (As, Bs, Cs, Ds); rows j >= 1 are eliminated against
@@ -240,7 +282,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
           hh_affine<T>(m, h, n, pr[Q_GNA * 32], pr[Q_GK * 32], pr[Q_GLK * 32], pr[Q_EL * 32],
                        ena, ek, G, J);
         } else {
-          hh_affine<T>(m, h, n, gna_c, gk_c, gl_c, el_c, ena, ek, G, J);
+          hh_affine_glel<T>(m, h, n, gna_c, gk_c, gl_c, glel_c, ena, ek, G, J);
         }
         T gr, glf, scl;
         coef(pr, j, gr, glf, scl);
@@ -369,11 +411,11 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
     if (A.spk_idx) {
       int edge = 0;
       if (live && spk_i >= 0 && r == 0) {
-        const int above = vat(spk_i) >= A.spk_thr;
+        const int above = wsm[spk_o] >= A.spk_thr;
         edge = above && below;
         below = !above;
         if (spk_i2 >= 0) {
-          const int above2 = vat(spk_i2) >= A.spk_thr;
+          const int above2 = wsm[spk_o2] >= A.spk_thr;
           edge = edge || (above2 && below2);
           below2 = !above2;
         }
@@ -385,7 +427,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
       stop_now = A.stop_on_spike && __shfl_sync(FULL, edge, lane0) && live;
     }
     if (live && r_idx >= 0) {
-      const int above = vat(r_idx) >= A.spk_thr;
+      const int above = wsm[r_o] >= A.spk_thr;
       if (above && r_latch) {
         if (r_count < A.rast_cap)
           A.rast_steps[((int64_t)cable * A.n_rast + r) * A.rast_cap + r_count] = A.step0 + s + 1;
@@ -393,13 +435,16 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
       }
       r_latch = !above;
     }
-    const bool rec_due = ((s + 1) % A.rec_every) == 0;
-    if (rec_due && live && rec_i >= 0 && r == 0)
-      A.trace[(int64_t)cable * A.n_rec + (s + 1) / A.rec_every] = vat(rec_i);
-    if (rec_due && A.trace_all)
-      rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r,
-                    A.trace_all + (int64_t)((s + 1) / A.rec_every) * A.n_comp + off,
-                    live ? K : 0);
+    // record every rec_every steps (a countdown: no division per step)
+    const bool rec_due = --rec_left == 0;
+    if (rec_due) {
+      rec_left = A.rec_every;
+      ++rec_k;
+      if (live && rec_i >= 0 && r == 0) A.trace[(int64_t)cable * A.n_rec + rec_k] = wsm[rec_o];
+      if (A.trace_all)
+        rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.trace_all + (int64_t)rec_k * A.n_comp + off,
+                      live ? K : 0);
+    }
     if constexpr (TAPE) {
       if (A.tape) {
         T* tp = A.tape + (int64_t)(s + 1) * 4 * A.n_comp + off;

@@ -323,6 +323,19 @@ __device__ __forceinline__ void hh_affine(T m, T h, T n, T gnabar, T gkbar, T gl
   J = mul_rn(gl, el) + mul_rn(gna, ena) + mul_rn(gk, ek);
 }
 
+// hh_affine with the leak's reversal product mul_rn(gl, el) supplied (the same
+// value, computed once per cable where gl and el are uniform).
+template <typename T>
+__device__ __forceinline__ void hh_affine_glel(T m, T h, T n, T gnabar, T gkbar, T gl, T glel,
+                                               T ena, T ek, T& G, T& J) {
+  T m3 = m * m * m;
+  T n2 = n * n;
+  T gna = gnabar * m3 * h;
+  T gk = gkbar * (n2 * n2);
+  G = gl + gna + gk;
+  J = glel + mul_rn(gna, ena) + mul_rn(gk, ek);
+}
+
 // Rectangular pulse amp on [delay, delay + pw).
 template <typename T>
 __device__ __forceinline__ T rect_pulse(T t, T amp, T delay, T pw) {
