@@ -106,7 +106,7 @@ def tune(kind, key_parts, candidates, run, device, reps=3, force=False):
 # (cables per CTA, k16, k8): cables with K <= k8 on 8 lanes, K <= k16 on 16
 # lanes, the rest on 32 ((0, 0): every cable on 32 lanes)
 CABLE_RUN_CANDIDATES = tuple((w, k16, k8) for w in (2, 4)
-                             for k16, k8 in ((0, 0), (96, 0), (128, 0), (128, 48), (128, 64)))
+                             for k16, k8 in ((0, 0), (96, 0), (128, 0), (128, 64), (160, 80)))
 
 
 def tune_cable_run(pop, n_steps=50, candidates=CABLE_RUN_CANDIDATES, reps=3, force=False):
@@ -125,6 +125,10 @@ def tune_cable_run(pop, n_steps=50, candidates=CABLE_RUN_CANDIDATES, reps=3, for
         pop.warps_per_block = w
         pop.lanes_split = None if k16 == 0 and k8 == 0 else (k16, k8)
 
+    kmax = max(pop.n_comp)
+    ch = max(-(-kmax // 32), 8)
+    candidates = tuple(c for c in candidates if c[1] <= 16 * ch and c[2] <= 8 * ch)
+
     def run(c):
         apply(c)
         for dst, src in zip((pop.v, pop.m, pop.h, pop.n), state):
@@ -132,7 +136,6 @@ def tune_cable_run(pop, n_steps=50, candidates=CABLE_RUN_CANDIDATES, reps=3, for
         pop.step_index, pop.t = step, t
         pop.run(n_steps)
 
-    kmax = max(pop.n_comp)
     parts = (str(pop.dtype), pop.B, kmax, pop.N, pop.fast_math, "ve" if pop.field is not None
              else "-")
     try:

@@ -179,8 +179,10 @@ class CablePopulation:
         # default); dendra_gb300.autotune.tune_cable_run picks it
         self.warps_per_block = 0
         # Thomas/PCR split of the persistent run: None = 32 lanes per cable;
-        # (k16, k8) = cables with K <= k8 (<= 64) run on 8 lanes, K <= k16
-        # (<= 128) on 16 lanes, longer ones on 32.  tune_cable_run picks it.
+        # (k16, k8) = cables with K <= k8 run on 8 lanes, K <= k16 on 16
+        # lanes, longer ones on 32 (rows per lane on 16 or 8 lanes may not
+        # exceed max(8, those of the longest cable on 32)).  tune_cable_run
+        # picks it.
         self.lanes_split = None
         self.field = None
         self.ve = None
@@ -353,8 +355,11 @@ class CablePopulation:
         """Cables on 32 and on 16 lanes for split (k16, k8); the work order
         lists cables by non-increasing K, so each class is one contiguous run."""
         k16, k8 = (int(x) for x in split)
-        if not (0 <= k8 <= 64 and 0 <= k16 <= 128):
-            raise ValueError("lanes_split (k16, k8) needs k16 <= 128 and k8 <= 64")
+        # rows per lane of the launch: those of the longest cable on 32 lanes, at least 8
+        ch = max(-(-max(self.n_comp) // 32), 8)
+        if not (0 <= k8 <= 8 * ch and 0 <= k16 <= 16 * ch):
+            raise ValueError(f"lanes_split (k16, k8) needs k16 <= {16 * ch} and k8 <= {8 * ch} "
+                             "for this population")
         k8 = min(k8, k16)
         ks = np.asarray(self.n_comp)
         n32 = int((ks > k16).sum())

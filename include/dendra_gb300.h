@@ -270,8 +270,10 @@ typedef struct dgb_cable_args {
      eliminates ceil(K/lanes) rows (Thomas), the lanes' reduced rows are then
      solved by PCR across the lanes.  lanes_mode 0: 32 lanes for every cable.
      lanes_mode 1: the first n_lanes32 cables of `order` run 32 lanes, the next
-     n_lanes16 run 16 lanes (two cables per warp, K <= 128), the rest 8 lanes
-     (four per warp, K <= 64); order should list cables by non-increasing K. */
+     n_lanes16 run 16 lanes (two cables per warp), the rest 8 lanes (four per
+     warp); order should list cables by non-increasing K.  A cable on 16 or 8
+     lanes may have at most max(8, ceil(max_k / 32)) rows per lane (K <= 16 or
+     8 times that); a longer one sets error bit 1 in scratch[1] and is skipped. */
   int32_t lanes_mode;
   int32_t n_lanes32;
   int32_t n_lanes16;
