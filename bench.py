@@ -376,11 +376,18 @@ def _ref_child(kind, steps, reps, warmup):
 
 def reference_cpu(kind, steps, reps=1, warmup=0, timeout=900):
     """Time the installed reference (baseline/_ref) in a child process; returns
-    its JSON dict, or {"error": why} when the reference cannot run here."""
+    its JSON dict, or {"error": why} when the reference cannot run here.
+    kind "c2gpu" runs the reference's own CUDA path (its Triton Thomas solver
+    and eager mechanism kernels); the Triton release on the GPU hosts bundles a
+    ptxas that does not know sm_103a, so Triton is pointed at the CUDA
+    toolkit's ptxas (TRITON_PTXAS_PATH) when one is installed."""
     if not os.path.isdir(os.path.join(REF_DIR, "dendra")):
         return {"error": "reference not installed in baseline/_ref"}
     env = dict(os.environ)
     env["PYTHONPATH"] = os.pathsep.join([REF_DIR, REF_SHIM, ROOT, env.get("PYTHONPATH", "")])
+    ptxas = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "ptxas")
+    if kind == "c2gpu" and "TRITON_PTXAS_PATH" not in env and os.path.exists(ptxas):
+        env["TRITON_PTXAS_PATH"] = ptxas
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--ref-child", kind,
            "--ref-steps", str(steps), "--steps", str(reps), "--warmup", str(warmup)]
     try:
@@ -1933,6 +1940,22 @@ def main():
                          "then the ragged solve + update kernel"}
         reset()
 
+    # ---- the reference's own GPU path on the same GPU (Triton Thomas solve +
+    #      eager mechanism kernels per step), on config-2 equal-K groups ----
+    ref_gpu = None
+    if rank == 0 and not args.no_plain:
+        r = reference_cpu("c2gpu", 200, reps=3, warmup=1)
+        if "error" in r:
+            ref_gpu = {"unavailable": r["error"]}
+        else:
+            secs = float(np.median(r["times"]))
+            ref_gpu = {"value": r["units"] / secs, "unit": METRIC, "seconds": secs,
+                       "what": (f"the reference's model.run on this GPU at JIT=0 (Triton "
+                                "thomas_solve_cuda_t + eager mechanism kernels per step), "
+                                f"config-2 groups K={list(C2_REF_GROUPS)} "
+                                f"({sum(g[1] for g in r['groups'])} cables, one Unmyelinated "
+                                "population per K) x 200 timesteps, float32")}
+
     peak, peak_kind = _peaks()
     achieved = ALG_BYTES_PER_COMP_STEP * comp_steps / (ms * 1e-3) / 1e9
     line = {
@@ -1966,6 +1989,10 @@ def main():
     if eager is not None:
         line["plain_eager_reference_structure"] = eager
         line["speedup_vs_plain_eager"] = value / eager["value"]
+    if ref_gpu is not None:
+        line["plain_reference_gpu"] = ref_gpu
+        if "value" in ref_gpu:
+            line["speedup_vs_plain_reference_gpu"] = value / ref_gpu["value"]
         line["gpu_launches"] += 0  # plain path runs outside the timed region
     if rank == 0 and not args.no_cpu:
         gpu_outs = _c2_gpu_outputs(dev, fast_math=not args.exact)

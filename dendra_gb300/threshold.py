@@ -93,12 +93,16 @@ def fibre_population(p, dtype=torch.float32, device="cuda", dt=0.005,
 class Thresholder:
     """Batched bisection on the GPU with the reference's rules.
 
-    Amplitudes are positive magnitudes (mA) of a cathodic pulse.
+    Amplitudes are positive magnitudes (mA) of a cathodic pulse.  Activity is
+    a rising edge at either of two compartments: the fibre nodes ``node_check``
+    (node indices of the myelinated fibre layout) or, for any other cables,
+    ``compartments`` (local indices, negative counting from the far end, like
+    the reference's ``Active(node_check=...)``).
     """
 
     def __init__(self, pop: CablePopulation, lb, ub, *, rtol=0.01, atol=None,
                  max_tries_bound_fix=10, max_tries_thresh=25, fix_bound_up=2.0,
-                 node_check=(5, -5), thr_mv=0.0):
+                 node_check=(5, -5), thr_mv=0.0, compartments=None):
         if rtol is None and atol is None:
             raise ValueError("Either atol or rtol must be provided.")
         self.pop = pop
@@ -110,7 +114,14 @@ class Thresholder:
         self.max_tries_bound_fix = max_tries_bound_fix
         self.max_tries_thresh = max_tries_thresh
         self.fix_bound_up = fix_bound_up
-        self.spk = [node_compartment(n) for n in node_check]
+        # detection compartments: fibre nodes (node_check) or, for any other
+        # cable, two compartment indices (negative: from the far end)
+        if compartments is None:
+            self.spk = [node_compartment(n) for n in node_check]
+        else:
+            kk = torch.as_tensor(pop.n_comp, dtype=torch.int32)
+            self.spk = [torch.where(torch.as_tensor(c) < 0, kk + int(c),
+                                    torch.full_like(kk, int(c))) for c in compartments]
         self.thr = thr_mv
         self.state0 = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
         self.trials = 0

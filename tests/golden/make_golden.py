@@ -25,6 +25,13 @@ compatibility shims) and records its outputs on seeded inputs:
                            and three taps) and a 40-step rollout with autograd
   netstim_{f64,f32}.npz    NetStim renewal: netstim_initial_state and 600 steps of
                            netstim_renewal with supplied unit-exponential draws
+  network_points.npz       a 16-cell Network of single-compartment HH cells with
+                           Exp2Syn synapses, periodic NetStim drive and all-to-all
+                           NetCons with delays, run through Network.run (CPU)
+  netcon_tapes.npz         the bit-pack known-answer tapes: fan-in/out across
+                           the ring wrap and the 63-bit word boundary
+  thresholds.npz           the reference Thresholder's brackets on twelve HH
+                           cables under a point-source pulse
 
 Usage (in a container that holds the reference source):
 
@@ -524,9 +531,162 @@ def netstim(dtype, tag):
     print("netstim", tag, int(out["spikes"].sum()))
 
 
+def network_points():
+    """A 16-cell network of single-compartment HH cells (the reference's
+    default Population geometry) with one Exp2Syn synapse each, driven by a
+    periodic NetStim per cell (noise 0: no random draws) through one-to-one
+    NetCons and coupled all-to-all (autapses included) with lognormal weights
+    and U[1, 5] ms delays, run step by step through Network.run on the CPU
+    (dense delay ring).  Records the NetStim emissions, the membrane trace of
+    every cell, the synapse states and the connection list in the reference's
+    edge order (source-major)."""
+    dn = _ref()
+    from dendra.models.mod import exp2syn, hh
+
+    N, dt, steps = 16, 0.025, 2000
+    w_bg, d_bg = 0.2, 1.0
+    rng = np.random.default_rng(11)
+    interval = rng.uniform(6.0, 14.0, N)
+    start = rng.uniform(0.5, 4.0, N)
+    W = rng.lognormal(-4.5, 0.5, (N, N))
+    D = rng.uniform(1.0, 5.0, (N, N))
+    with dn.ctx(JIT=0):
+        pop = dn.Population(N=N, C=1, v_init=-65.0, celsius=6.3, dtype=torch.float64)
+        pop.insert(hh)
+        pop.insert(exp2syn.rename("syn"), tau1=0.5, tau2=5.0, e=0.0)
+        stim = dn.NetStim(N=N, interval=torch.as_tensor(interval),
+                          start=torch.as_tensor(start), noise=0.0, dtype=torch.float64)
+        net = dn.Network({"cells": pop}, netstim=stim, track_netcon_events=False,
+                         netcon_delay_backend="dense")
+        net.connect_one_to_one(net.netstim[:], pop[:], pop.mech.syn, threshold=None,
+                               weight=torch.full((N,), w_bg, dtype=torch.float64),
+                               delay=torch.full((N,), d_bg, dtype=torch.float64))
+        net.connect_dense(pop[:], pop[:], pop.mech.syn, threshold=0.0,
+                          weight=torch.as_tensor(W.reshape(-1)),
+                          delay=torch.as_tensor(D.reshape(-1)), allow_autapses=True)
+        net.initialize(dt)
+        syn = pop.mech.syn
+        v = [pop.v.reshape(-1).clone()]
+        A, B, emitted = [syn.A.reshape(-1).clone()], [syn.B.reshape(-1).clone()], []
+        for _ in range(steps):
+            net.run(steps=1)
+            v.append(pop.v.reshape(-1).clone())
+            A.append(syn.A.reshape(-1).clone())
+            B.append(syn.B.reshape(-1).clone())
+            emitted.append(stim.spikes.reshape(-1).clone())
+    src = np.repeat(np.arange(N), N)  # connect_dense: source-major, then target
+    dst = np.tile(np.arange(N), N)
+    out = dict(N=N, dt=dt, steps=steps, celsius=6.3, v_init=-65.0,
+               diam=float(pop.diam.reshape(-1)[0]), length=float(pop.dx.reshape(-1)[0]),
+               tau1=0.5, tau2=5.0, e_syn=0.0, spk_thr=0.0, w_bg=w_bg, d_bg=d_bg,
+               interval=interval, start=start, pre=src, post=dst, weight=W.reshape(-1),
+               delay=D.reshape(-1), stim_emitted=torch.stack(emitted).numpy(),
+               v=torch.stack(v).numpy(), A=torch.stack(A).numpy(), B=torch.stack(B).numpy())
+    np.savez_compressed(os.path.join(HERE, "network_points.npz"), **out)
+    up = (out["v"][1:] >= 0) & (out["v"][:-1] < 0)
+    print("network_points spikes per cell", up.sum(0).tolist())
+
+
+def netcon_tapes():
+    """The reference's bit-pack known-answer tapes
+    (tests/networks/test_backend_equivalence.py:93-205), recorded from its dense
+    and bit-packed NetCon backends on the CPU: a fan-in/fan-out tape of three
+    sources onto two targets through 1-3 step delays that wraps the ring, and a
+    65-source one-to-one tape across the 63-bit word boundary.  ExpSyn g after
+    each NetCon.advance is the running sum of the delivered weights."""
+    dn = _ref()
+    from dendra.models.mod import expsyn
+
+    dt = 0.1
+    out = {}
+    w = torch.tensor([1.0, 2.0, 3.0, 4.0, 5.0, 6.0], dtype=torch.float64)
+    dly = torch.tensor([0.1, 0.2, 0.3, 0.1, 0.2, 0.3], dtype=torch.float64)
+    tape = np.array([[1, 1, 0], [0, 0, 1], [1, 0, 1], [0, 0, 0], [0, 1, 0], [1, 0, 0],
+                     [0, 0, 0], [0, 0, 0], [0, 0, 0]], dtype=bool)
+    active = np.zeros(65, dtype=bool)
+    active[[0, 62, 63, 64]] = True
+    word_tape = np.stack([active, np.zeros_like(active)])
+    for backend in ("dense", "bitpacked_history"):
+        post = dn.Population(N=2, C=1, v_init=-65.0, dtype=torch.float64)
+        post.insert(expsyn.rename("syn"), e=0.0, tau=1.0)
+        stim = dn.NetStim(N=3, dtype=torch.float64)
+        net = dn.Network({"post": post}, netstim=stim, track_netcon_events=False,
+                         netcon_delay_backend=backend)
+        net.connect_dense(net.netstim[:], post[:], post.mech.syn, threshold=None, weight=w,
+                          delay=dly)
+        net.build(dt)
+        net.init_synapses()
+        nc = next(iter(net.synapses.values()))
+        rows = []
+        for spikes in tape:
+            net.netstim.spikes.copy_(torch.as_tensor(spikes))
+            nc.advance()
+            rows.append(nc.syn.g.detach().reshape(-1).clone())
+        out[f"fan_g_{backend}"] = torch.stack(rows).numpy()
+
+        post = dn.Population(N=65, C=1, v_init=-65.0, dtype=torch.float64)
+        post.insert(expsyn.rename("syn"), e=0.0, tau=1.0)
+        stim = dn.NetStim(N=65, dtype=torch.float64)
+        net = dn.Network({"post": post}, netstim=stim, netcon_delay_backend=backend)
+        net.connect_one_to_one(net.netstim[:], post[:], post.mech.syn, threshold=None,
+                               weight=torch.ones(65, dtype=torch.float64),
+                               delay=torch.full((65,), dt, dtype=torch.float64))
+        net.build(dt)
+        net.init_synapses()
+        nc = next(iter(net.synapses.values()))
+        rows = []
+        for spikes in word_tape:
+            net.netstim.spikes.copy_(torch.as_tensor(spikes))
+            nc.advance()
+            rows.append(nc.syn.g.detach().reshape(-1).clone())
+        out[f"word_g_{backend}"] = torch.stack(rows).numpy()
+    out.update(dt=dt, fan_pre=np.array([0, 0, 1, 1, 2, 2]), fan_post=np.array([0, 1, 0, 1, 0, 1]),
+               fan_weight=w.numpy(), fan_delay=dly.numpy(), fan_tape=tape, word_tape=word_tape)
+    np.savez_compressed(os.path.join(HERE, "netcon_tapes.npz"), **out)
+    print("netcon_tapes", out["fan_g_dense"][-1], out["word_g_dense"][-1][[0, 61, 62, 63, 64]])
+
+
+def thresholds():
+    """The reference Thresholder (models/instruments/thresholder.py) on twelve
+    unbranched HH cables (Unmyelinated, L 2000 um, dx 20 um, diameters
+    U[1, 4] um, float64) under a cathodic 0.1 ms point-source pulse at
+    U[300, 1500] um: bound fixing from ub = 0.5 mA (doubling, at most ten
+    times), bisection to rtol 1 % at dt 0.005 ms over 2 ms, activity = a 0 mV
+    rising edge at compartment 5 or -5 (Active's default nodes), no
+    conduction-block test.  Records the field it was given and the final
+    brackets (NaN where bound fixing gave up)."""
+    dn = _ref()
+    from dendra.models import callbacks as cb
+    from dendra.models.instruments.thresholder import Thresholder
+    from dendra.models.mod import hh
+
+    B, dt, tstop, pw = 12, 0.005, 2.0, 0.1
+    rng = np.random.default_rng(21)
+    D = rng.uniform(1.0, 4.0, B)
+    dist = rng.uniform(300.0, 1500.0, B)
+    with dn.ctx(JIT=0):
+        model = dn.Unmyelinated(list(D), L=2000.0, dx=20.0, celsius=6.3, v_init=-65.0,
+                                dtype=torch.float64, integrator=dn.bwd_euler_ub(), rhoa=100.0)
+        model.insert(hh)
+        model.initialize()
+        K = model.v.shape[-1]
+        x = torch.linspace(-(K - 1) * 20.0 / 2, (K - 1) * 20.0 / 2, K, dtype=torch.float64)
+        r = torch.sqrt(x[None, :] ** 2 + torch.as_tensor(dist)[:, None] ** 2) * 1e-4
+        field = (1.0 / 0.3 * 100.0) / (4 * torch.pi * r)
+        th = Thresholder(model, cb.Active(threshold=0.0, node_check=[5, -5]), space=-field,
+                         time=dn.mono_rect(amp=1.0, delay=0.0, pw=pw),
+                         ub=torch.full((B,), 0.5, dtype=torch.float64),
+                         lb=torch.zeros(B, dtype=torch.float64), rtol=0.01)
+        ub, lb = th.calculate_thresholds(tstop=tstop, dt=dt, block_possible=False)
+    out = dict(B=B, K=K, dx=20.0, diam=D, dist=dist, field=field.numpy(), pw=pw, dt=dt,
+               tstop=tstop, ub0=0.5, lb0=0.0, rtol=0.01, ub=ub.numpy(), lb=lb.numpy())
+    np.savez_compressed(os.path.join(HERE, "thresholds.npz"), **out)
+    print("thresholds", out["ub"])
+
+
 if __name__ == "__main__":
     what = sys.argv[1:] or ["rates", "tridiag", "dhs", "events", "cable", "extra", "adjoint",
-                            "block3", "delay", "netstim"]
+                            "block3", "delay", "netstim", "network", "tapes", "thresholds"]
     if "rates" in what:
         rates()
     if "tridiag" in what:
@@ -551,3 +711,9 @@ if __name__ == "__main__":
     if "netstim" in what:
         netstim(torch.float64, "f64")
         netstim(torch.float32, "f32")
+    if "network" in what:
+        network_points()
+    if "tapes" in what:
+        netcon_tapes()
+    if "thresholds" in what:
+        thresholds()
