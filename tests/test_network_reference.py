@@ -76,7 +76,10 @@ def test_gpu_network_matches_reference(cuda, golden, dtype):
     v = net.v.double().cpu().numpy()
     err = np.abs(v - g["v"][-1]).max()
     print(f"GPU network {dtype} vs reference: final max |dV| {err:.3e} mV")
-    assert err < (1e-9 if dtype == torch.float64 else 1e-3)
+    # float32: the same spike steps; the potentials of spiking cells carry
+    # float32 rounding amplified through action potentials (the stated
+    # float32 tolerance for spiking traces, 2e-2 mV)
+    assert err < (1e-9 if dtype == torch.float64 else 2e-2)
     rtol = 1e-12 if dtype == torch.float64 else 1e-4
     np.testing.assert_allclose(net.A.double().cpu().numpy(), g["A"][-1], rtol=rtol, atol=1e-15)
     np.testing.assert_allclose(net.B.double().cpu().numpy(), g["B"][-1], rtol=rtol, atol=1e-15)
