@@ -96,6 +96,8 @@ SIGNATURES = {
     "dgb_pack_source_spikes": (_INT, [_P, _I64, _P, _I64, _P, _P]),
     "dgb_build_delivery": (_INT, [_INT, _P, _P, _P, _P, _P, _P, _I64, _P, _P, _I64, _I64, _I64,
                                   _P]),
+    "dgb_build_delivery_uniform": (_INT, [_INT, _P, _P, _I64, _P, _P, _P, _I64, _P, _P, _I64,
+                                          _I64, _I64, _P]),
     "dgb_ring_enqueue": (_INT, [_INT, _P, _I64, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P]),
     "dgb_net_window": (_INT, [_P, _P]),
     "dgb_net_enqueue": (_INT, [_INT, _P, _I64, _I64, _I64, _P, _I64, _P, _P, _P, _P, _P, _P]),

@@ -188,6 +188,9 @@ class CablePopulation:
         self.ve = None
         self.intra = None
         self.t = 0.0
+        # time origin of the stimulus grid: step k of a run sees
+        # t0_ms + (step_index + k) dt, in binary64, cast to the state dtype
+        self.t0_ms = 0.0
         self.dt = None
         self._dev = {}
 
@@ -330,7 +333,7 @@ class CablePopulation:
             a.in_idx, a.in_amp, a.in_delay, a.in_pw = (
                 d[k].data_ptr() for k in ("in_idx", "in_amp", "in_delay", "in_pw"))
         a.ena, a.ek, a.q10 = self.ena, self.ek, q10_of(self.celsius)
-        a.dt_ms, a.dt_s, a.t0_ms = self.dt, self.dt_s, 0.0
+        a.dt_ms, a.dt_s, a.t0_ms = self.dt, self.dt_s, float(self.t0_ms)
         a.step0 = self.step_index
         if rec_idx is not None:
             a.rec_idx = rec_idx.data_ptr()

@@ -45,11 +45,12 @@ __global__ void pack_kernel(const uint8_t* __restrict__ src, int64_t n_source,
 }
 
 // Connections sorted by target (CSR post_ptr); thread p sums its targets'
-// delayed events in connection order and adds the sum to out[p].
+// delayed events in connection order and adds the sum to out[p].  delay ==
+// nullptr: every connection has the delay uniform_delay.
 template <typename T>
 __global__ void deliver_kernel(const unsigned long long* __restrict__ hist,
                                const int64_t* __restrict__ step_ptr,
-                               const int64_t* __restrict__ delay,
+                               const int64_t* __restrict__ delay, int64_t uniform_delay,
                                const int64_t* __restrict__ word_idx,
                                const int64_t* __restrict__ bit_mask,
                                const int64_t* __restrict__ post_ptr, int64_t n_post,
@@ -63,7 +64,7 @@ __global__ void deliver_kernel(const unsigned long long* __restrict__ hist,
   T acc = out[p];
   bool any = false;
   for (int64_t e = post_ptr[p]; e < post_ptr[p + 1]; ++e) {
-    int64_t row = now - delay[e];
+    int64_t row = now - (delay ? delay[e] : uniform_delay);
     if (row < 0) row += max_delay;
     const unsigned long long w = hist[row * n_words + word_idx[e]];
     if (w & (unsigned long long)bit_mask[e]) {
@@ -158,12 +159,48 @@ extern "C" int dgb_build_delivery(int dtype, const int64_t* packed_history,
   cudaStream_t st = as_stream(stream);
   const auto* h = (const unsigned long long*)packed_history;
   if (dtype == DGB_F32)
-    deliver_kernel<float><<<blocks, th, 0, st>>>(h, current_time_step, delay_steps, conn_word_idx,
-                                                 conn_bit_mask, post_ptr, n_post,
+    deliver_kernel<float><<<blocks, th, 0, st>>>(h, current_time_step, delay_steps, 0,
+                                                 conn_word_idx, conn_bit_mask, post_ptr, n_post,
                                                  (const float*)weight, (float*)delivery_out,
                                                  max_delay_steps, n_words);
   else
-    deliver_kernel<double><<<blocks, th, 0, st>>>(h, current_time_step, delay_steps,
+    deliver_kernel<double><<<blocks, th, 0, st>>>(h, current_time_step, delay_steps, 0,
+                                                  conn_word_idx, conn_bit_mask, post_ptr, n_post,
+                                                  (const double*)weight, (double*)delivery_out,
+                                                  max_delay_steps, n_words);
+  DGB_LAUNCH_CHECK();
+  return DGB_OK;
+}
+
+extern "C" int dgb_build_delivery_uniform(int dtype, const int64_t* packed_history,
+                                          const int64_t* current_time_step, int64_t delay_step,
+                                          const int64_t* conn_word_idx,
+                                          const int64_t* conn_bit_mask, const int64_t* post_ptr,
+                                          int64_t n_post, const void* weight, void* delivery_out,
+                                          int64_t n_conn, int64_t max_delay_steps,
+                                          int64_t n_words, void* stream) {
+  clear_error();
+  DGB_REQUIRE(dtype == DGB_F32 || dtype == DGB_F64, "dtype must be DGB_F32 or DGB_F64");
+  DGB_REQUIRE(n_post >= 0 && n_conn >= 0, "sizes must be >= 0");
+  DGB_REQUIRE(max_delay_steps >= 1, "max_delay_steps must be >= 1");
+  DGB_REQUIRE(delay_step >= 0 && delay_step < max_delay_steps,
+              "delay_step must be in [0, max_delay_steps)");
+  if (n_post == 0) return DGB_OK;
+  DGB_REQUIRE(packed_history && current_time_step && post_ptr && delivery_out,
+              "pointers must be non-null");
+  DGB_REQUIRE(n_conn == 0 || (conn_word_idx && conn_bit_mask && weight),
+              "connection arrays must be non-null");
+  const int th = 256;
+  const unsigned blocks = (unsigned)((n_post + th - 1) / th);
+  cudaStream_t st = as_stream(stream);
+  const auto* h = (const unsigned long long*)packed_history;
+  if (dtype == DGB_F32)
+    deliver_kernel<float><<<blocks, th, 0, st>>>(h, current_time_step, nullptr, delay_step,
+                                                 conn_word_idx, conn_bit_mask, post_ptr, n_post,
+                                                 (const float*)weight, (float*)delivery_out,
+                                                 max_delay_steps, n_words);
+  else
+    deliver_kernel<double><<<blocks, th, 0, st>>>(h, current_time_step, nullptr, delay_step,
                                                   conn_word_idx, conn_bit_mask, post_ptr, n_post,
                                                   (const double*)weight, (double*)delivery_out,
                                                   max_delay_steps, n_words);

@@ -54,6 +54,11 @@ struct NetArgsT {
   int64_t bg_words;
   int32_t bg_syn;               // local synapse receiving background events
   T bg_weight;
+  // extracellular and injected drive (nullptr: none)
+  const T *ve_field, *ve_amp, *ve_delay, *ve_pw;
+  const int32_t* in_node;
+  const T *in_amp, *in_delay, *in_pw;
+  double t0_ms, dt_d;
   // spikes
   uint8_t* below;
   unsigned long long* spike_bits;  // [n_cells] for this window
@@ -144,6 +149,8 @@ __global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetAr
     const T* cmdt = A.cm_dt + base;
     const T* gl = A.gl + base;
     const T* el = A.el + base;
+    // local node of the cell's injected current (-1: none)
+    const int in_i = (A.in_node && A.in_amp) ? A.in_node[cell] : -1;
     T m = T(0), h = T(0), nn = T(0);
     int below = 1, count = 0;
     if (lane == 0) {
@@ -159,6 +166,14 @@ __global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetAr
       const int64_t g = A.step0 + s;
       const int64_t slot = (A.slot0 + s) % A.depth;
       T* row = A.ring + slot * A.n_syn + s0;
+      // this step's drive (uniform over the cell)
+      T Ive = T(0), Iin = T(0);
+      if (A.ve_field || in_i >= 0) {
+        const T t = (T)(A.t0_ms + (double)g * A.dt_d);
+        if (A.ve_field) Ive = rect_pulse<T>(t, A.ve_amp[cell], A.ve_delay[cell], A.ve_pw[cell]);
+        if (in_i >= 0) Iin = rect_pulse<T>(t, A.in_amp[cell], A.in_delay[cell], A.in_pw[cell]);
+      }
+      const bool ve_on = Ive != T(0);
       // 1. deliver today's events (and clear the row)
       const bool bg = A.bg_bits && ((A.bg_bits[g * A.bg_words + (cell >> 6)] >> (cell & 63)) & 1ull);
       for (int k = lane; k < S; k += TPC) {
@@ -213,6 +228,18 @@ __global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetAr
           const int c = sCidx[k];
           f = f + mul_rn(sG[c], sV[c] - vi);
         }
+        if (ve_on) {  // extracellular edge currents, summed on their own
+          const T* fld = A.ve_field + base;
+          const T vei = mul_rn(fld[i], Ive);
+          T S = T(0);
+          if (has_parent(p)) S = S - mul_rn(sG[i], vei - mul_rn(fld[p], Ive));
+          for (int k = sCptr[i]; k < sCptr[i + 1]; ++k) {
+            const int c = sCidx[k];
+            S = S + mul_rn(sG[c], mul_rn(fld[c], Ive) - vei);
+          }
+          f = f + S;
+        }
+        if (i == in_i) f = f + Iin;
         sB[i] = f;
         sD[i] = cmdt[i] + mul_rn(G, ar);
       }
@@ -316,6 +343,16 @@ static NetArgsT<T> net_typed(const dgb_net_args* a) {
   t.bg_words = a->bg_words;
   t.bg_syn = a->bg_syn;
   t.bg_weight = (T)a->bg_weight;
+  t.ve_field = (const T*)a->ve_field;
+  t.ve_amp = (const T*)a->ve_amp;
+  t.ve_delay = (const T*)a->ve_delay;
+  t.ve_pw = (const T*)a->ve_pw;
+  t.in_node = a->in_node;
+  t.in_amp = (const T*)a->in_amp;
+  t.in_delay = (const T*)a->in_delay;
+  t.in_pw = (const T*)a->in_pw;
+  t.t0_ms = a->t0_ms;
+  t.dt_d = a->dt_ms;
   t.below = a->below;
   t.spike_bits = (unsigned long long*)a->spike_bits;
   t.spike_count = a->spike_count;
@@ -385,6 +422,10 @@ extern "C" int dgb_net_window(const dgb_net_args* a, void* stream) {
               "synapse arrays and ring must be non-null");
   DGB_REQUIRE(a->below && a->spike_bits && a->spike_count, "spike outputs must be non-null");
   DGB_REQUIRE(a->forest.max_k >= 1, "cells must have at least one compartment");
+  DGB_REQUIRE(!a->ve_field || (a->ve_amp && a->ve_delay && a->ve_pw),
+              "ve_field requires ve_amp, ve_delay and ve_pw");
+  DGB_REQUIRE(!a->in_node || (a->in_amp && a->in_delay && a->in_pw),
+              "in_node requires in_amp, in_delay and in_pw");
   DGB_REQUIRE(!a->forest.chain_nodes || (a->forest.chain_ptr && a->forest.chain_level &&
                                          a->forest.plan_chain_off && a->forest.plan_clevel_off),
               "the chain schedule needs chain_ptr, chain_level and their plan offsets");

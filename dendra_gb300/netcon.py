@@ -129,6 +129,29 @@ def build_delivery(packed_history, current_time_step, delay_steps, conn_word_idx
     return delivery_out
 
 
+def build_delivery_uniform(packed_history, current_time_step, delay_step, conn_word_idx,
+                           conn_bit_mask, post_idx, weight, delivery_out):
+    """build_delivery with the same delay (an int, in steps) for every connection
+    (the reference's build_delivery_uniform, netcon_bitpack_ops.py:669-712)."""
+    depth, n_words = packed_history.shape
+    delay_step = int(delay_step)
+    if not 0 <= delay_step < depth:
+        raise ValueError(f"delay_step must lie in [0, {depth}) for this history")
+    csr = _target_csr(post_idx, delivery_out.numel())
+    perm = csr.perm
+    w_idx = conn_word_idx.index_select(0, perm).contiguous()
+    mask = conn_bit_mask.index_select(0, perm).contiguous()
+    w = weight.index_select(0, perm).contiguous()
+    with torch.cuda.device(delivery_out.device):
+        rc = _lib.load().dgb_build_delivery_uniform(
+            _lib.dtype_code(delivery_out.dtype), packed_history.data_ptr(),
+            current_time_step.data_ptr(), delay_step, w_idx.data_ptr(), mask.data_ptr(),
+            csr.ptr.data_ptr(), csr.n_post, w.data_ptr(), delivery_out.data_ptr(), w.numel(),
+            depth, n_words, _lib.stream_ptr(delivery_out.device))
+    _lib.check(rc, "dgb_build_delivery_uniform")
+    return delivery_out
+
+
 class DenseRing:
     """Dense delay ring [depth, width] with fixed per-connection delays.
 

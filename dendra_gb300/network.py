@@ -56,6 +56,9 @@ class NetArgs(ctypes.Structure):
         ("below", ctypes.c_void_p), ("spike_bits", ctypes.c_void_p),
         ("spike_count", ctypes.c_void_p),
         ("warps_per_block", ctypes.c_int32), ("threads_per_cell", ctypes.c_int32),
+        ("ve_field", ctypes.c_void_p), ("ve_amp", ctypes.c_void_p), ("ve_delay", ctypes.c_void_p),
+        ("ve_pw", ctypes.c_void_p), ("in_node", ctypes.c_void_p), ("in_amp", ctypes.c_void_p),
+        ("in_delay", ctypes.c_void_p), ("in_pw", ctypes.c_void_p), ("t0_ms", ctypes.c_double),
     ]
 
 
@@ -126,7 +129,7 @@ class TreeNetwork:
                  dt=0.025, dtype=torch.float32, device="cuda", ra=100.0, cm=1.0, celsius=6.3,
                  v_init=-65.0, g_pas=0.001, e_pas=-70.0, tau1=0.5, tau2=5.0, e_syn=0.0,
                  spk_thr=0.0, bg_steps=None, bg_weight=0.0, window=None, chains=True,
-                 bg_netstim=None):
+                 bg_netstim=None, extracellular=None, clamp=None):
         self.dtype = dtype
         self.device = torch.device(device)
         self.dt = float(dt)
@@ -218,6 +221,27 @@ class TreeNetwork:
                            q10=q10_of(celsius), dt_ms=float(dt), spk_thr=float(spk_thr),
                            e_syn=float(e_syn))
         self.v_init = float(v_init)
+        # optional drive of the tree step: extracellular (field per node in mV
+        # per unit amplitude; amp, delay, pw per cell, a rectangular pulse) and
+        # an injected current (local node, amp in mA, delay, pw per cell)
+        self.drive = {}
+        per_cell = lambda x: torch.as_tensor(x, dtype=dtype).reshape(-1).expand(  # noqa: E731
+            self.n_cells).clone()
+        if extracellular is not None:
+            field, amp, delay, pw = extracellular
+            field = torch.as_tensor(field, dtype=dtype).reshape(-1)
+            if field.numel() != N:
+                raise ValueError(f"the extracellular field needs one value per node ({N})")
+            self.drive.update(ve_field=field, ve_amp=per_cell(amp), ve_delay=per_cell(delay),
+                              ve_pw=per_cell(pw))
+        if clamp is not None:
+            node, amp, delay, pw = clamp
+            node = torch.as_tensor(node, dtype=torch.int32).reshape(-1).expand(self.n_cells)
+            kk = torch.as_tensor(np.diff(node_ptr), dtype=torch.int32)
+            if bool(((node < -1) | (node >= kk)).any()):
+                raise ValueError("clamp node out of range for some cell")
+            self.drive.update(in_node=node.clone(), in_amp=per_cell(amp),
+                              in_delay=per_cell(delay), in_pw=per_cell(pw))
         self._syn_ptr = syn_ptr
         self._node_syn_ptr = node_syn_ptr
         self._upload()
@@ -257,6 +281,7 @@ class TreeNetwork:
         self.d["syn_ptr"] = torch.as_tensor(self._syn_ptr, device=dev)
         self.d["node_syn_ptr"] = torch.as_tensor(self._node_syn_ptr, device=dev)
         self.d.update({f"csr_{k}": v.to(dev).contiguous() for k, v in self.csr.items()})
+        self.d.update({f"drive_{k}": v.to(dev).contiguous() for k, v in self.drive.items()})
         self.reset()
 
     def reset(self):
@@ -385,6 +410,9 @@ class TreeNetwork:
         a.spike_count = self.spike_count.data_ptr()
         a.warps_per_block = int(self.warps_per_block)
         a.threads_per_cell = int(self.threads_per_cell)
+        for k in self.drive:
+            setattr(a, k, d[f"drive_{k}"].data_ptr())
+        a.t0_ms = 0.0
         return a
 
     # -- oracle interchange ----------------------------------------------
@@ -401,7 +429,8 @@ class TreeNetwork:
             node_syn_ptr=self._node_syn_ptr.copy(), conn=self.conn, params=self.params,
             bg_bits=bits if self._has_bg else None, bg_words=words,
             bg_syn=int(self.bg_syn_sorted[0]), bg_weight=self.bg_weight, depth=self.depth,
-            slot=self.slot, step=self.step, n_syn=self.n_syn, n_cells=self.n_cells)
+            slot=self.slot, step=self.step, n_syn=self.n_syn, n_cells=self.n_cells,
+            t0_ms=0.0, **{k: c(v) for k, v in self.drive.items()})
 
 
 class CapturedRun:

@@ -34,6 +34,7 @@
  *   dgb_detect_spikes         threshold_transition, networks/spiking.py:43-73
  *   dgb_pack_source_spikes    pack_source_spikes, networks/netcon_bitpack_kernel.cpp:145-149
  *   dgb_build_delivery        build_delivery, networks/netcon_bitpack_kernel.cpp:145-149
+ *   dgb_build_delivery_uniform build_delivery_uniform, networks/netcon_bitpack_ops.py:669
  *   dgb_ring_enqueue          dense_fixed_delay_transition enqueue,
  *                             networks/_event_delivery.py:61-199
  *   dgb_net_window            Network.run step loop, networks/net.py:214-240 with
@@ -501,6 +502,21 @@ typedef struct dgb_net_args {
   /* threads advancing one cell: 32, 64, 128, 256 or 512 (0 = 128); identical results.
      Both are the autotuner's knobs. */
   int32_t threads_per_cell;
+  /* optional drive of the tree step (integrators/tree.py:1262-1302), NULL = none:
+     extracellular ve = ve_field[node] * amp on [delay, delay + pw) of the
+     cell (its edge currents g (ve_child - ve_parent) enter the parent and
+     leave the child), and an injected current (mA) of a rectangular pulse at
+     local node in_node[cell] (-1: none).  Pulse times are t0_ms + step dt in
+     binary64, cast to the state dtype. */
+  const void* ve_field;
+  const void* ve_amp;
+  const void* ve_delay;
+  const void* ve_pw;
+  const int32_t* in_node;
+  const void* in_amp;
+  const void* in_delay;
+  const void* in_pw;
+  double t0_ms;
 } dgb_net_args;
 
 /* sizeof(dgb_net_args) as compiled (for foreign-language mirrors). */
@@ -557,6 +573,20 @@ int dgb_build_delivery(int dtype, const int64_t* packed_history,
                        const int64_t* post_ptr, int64_t n_post, const void* weight,
                        void* delivery_out, int64_t n_conn, int64_t max_delay_steps,
                        int64_t n_words, void* stream);
+
+/*
+ * dgb_build_delivery with one delay for every connection (delay_step, in
+ * [0, max_delay_steps)): the uniform-delay launch of the reference,
+ * build_delivery_uniform, networks/netcon_bitpack_ops.py:669-712 and
+ * networks/netcon_bitpack_kernel.cu:95-126.  Same CSR layout and the same
+ * deterministic per-target order of additions.
+ */
+int dgb_build_delivery_uniform(int dtype, const int64_t* packed_history,
+                               const int64_t* current_time_step, int64_t delay_step,
+                               const int64_t* conn_word_idx, const int64_t* conn_bit_mask,
+                               const int64_t* post_ptr, int64_t n_post, const void* weight,
+                               void* delivery_out, int64_t n_conn, int64_t max_delay_steps,
+                               int64_t n_words, void* stream);
 
 /*
  * Dense delay-ring enqueue: ring is [depth][width]; for each target p (CSR

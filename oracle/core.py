@@ -80,7 +80,7 @@ def _declare(L):
         getattr(L, "orc_net_run" + sfx).argtypes = (
             [_I32, _I32, _I64, _I64, _P, _I64] + [_P] * 9 + [_P] * 9 + [_D] * 7
             + [_P, _P, _P, _P, _P, _P, _P, _D, _P, _P, _I64, _I32, _D, _I64, _P, _P, _P, _P, _P,
-               _P, _P])
+               _P, _P] + [_P] * 8 + [_D])
         getattr(L, "orc_two_tap_enqueue" + sfx).restype = ctypes.c_int
         getattr(L, "orc_two_tap_enqueue" + sfx).argtypes = (
             [_I64, _I64, _P, _I64, _I64, _P, _P, _P, _I64, _P, _P, _P, _P])
@@ -359,6 +359,9 @@ def net_run(pd: dict, n_steps: int):
         bg=None if pd["bg_bits"] is None else c(pd["bg_bits"], np.uint64),
         pre=c(conn["pre"], np.int64), post=c(conn["post"], np.int64),
         delay=c(conn["delay"], np.int64), weight=c(conn["weight"], dtype))
+    drive = {k: (None if pd.get(k) is None else c(pd[k], np.int32 if k == "in_node" else dtype))
+             for k in ("ve_field", "ve_amp", "ve_delay", "ve_pw", "in_node", "in_amp",
+                       "in_delay", "in_pw")}
     slot = np.array([pd["slot"]], dtype=np.int64)
     raster = np.zeros((n_steps, pd["n_cells"]), dtype=np.uint8)
     getattr(lib(), "orc_net_run" + sfx)(
@@ -375,7 +378,9 @@ def net_run(pd: dict, n_steps: int):
         _ptr(pd["ring"]), _ptr(keep["bg"]), int(pd["bg_words"]), int(pd["bg_syn"]),
         float(pd["bg_weight"]), int(keep["pre"].size), _ptr(keep["pre"]), _ptr(keep["post"]),
         _ptr(keep["delay"]), _ptr(keep["weight"]), _ptr(pd["below"]), _ptr(pd["spike_count"]),
-        _ptr(raster))
+        _ptr(raster), *(_ptr(drive[k]) for k in ("ve_field", "ve_amp", "ve_delay", "ve_pw",
+                                                  "in_node", "in_amp", "in_delay", "in_pw")),
+        float(pd.get("t0_ms", 0.0)))
     pd["slot"] = int(slot[0])
     return raster
 

@@ -789,7 +789,10 @@ void F(orc_net_run)(int32_t n_cells, int32_t n_steps, int64_t step0, int64_t dep
                     int64_t bg_words, int32_t bg_syn, double bg_weight_d, int64_t n_conn,
                     const int64_t* conn_pre, const int64_t* conn_post, const int64_t* conn_delay,
                     const REAL* conn_weight, uint8_t* below, int32_t* spike_count,
-                    uint8_t* raster /* [n_steps][n_cells] or NULL */) {
+                    uint8_t* raster /* [n_steps][n_cells] or NULL */,
+                    const REAL* ve_field, const REAL* ve_amp, const REAL* ve_delay,
+                    const REAL* ve_pw, const int32_t* in_node, const REAL* in_amp,
+                    const REAL* in_delay, const REAL* in_pw, double t0_ms) {
   const REAL gnabar = (REAL)gnabar_d, gkbar = (REAL)gkbar_d, ena = (REAL)ena_d, ek = (REAL)ek_d;
   const REAL q10 = (REAL)q10_d, dt = (REAL)dt_d, thr = (REAL)thr_d, e_syn = (REAL)e_syn_d;
   const REAL bg_weight = (REAL)bg_weight_d;
@@ -879,6 +882,23 @@ void F(orc_net_run)(int32_t n_cells, int32_t n_steps, int64_t step0, int64_t dep
           int32_t ch = cidx[k];
           f = f + a_geom[base + ch] * (v[base + ch] - vi);
         }
+        /* extracellular edge currents g (ve_child - ve_parent), summed on
+           their own, then the injected current (tree.py:1262-1302) */
+        if (ve_field && ve_amp) {
+          const REAL I = F(rect)(t0_ms, g, dt_d, ve_amp[c], ve_delay[c], ve_pw[c], 0);
+          if (I != (REAL)0) {
+            const REAL vei = ve_field[base + i] * I;
+            REAL S = (REAL)0;
+            if (par[i] >= 0) S = S - a_geom[base + i] * (vei - ve_field[base + par[i]] * I);
+            for (int32_t k = cptr[i]; k < cptr[i + 1]; ++k) {
+              int32_t ch = cidx[k];
+              S = S + a_geom[base + ch] * (ve_field[base + ch] * I - vei);
+            }
+            f = f + S;
+          }
+        }
+        if (in_node && in_amp && in_node[c] == i)
+          f = f + F(rect)(t0_ms, g, dt_d, in_amp[c], in_delay[c], in_pw[c], 0);
         rhs[i] = f;
         main_[i] = cm_dt[base + i] + G * ar;
       }

@@ -131,3 +131,29 @@ def test_netcon_known_answer_tapes(cuda, golden, packed):
                            g["word_tape"], n, cuda, packed)
     np.testing.assert_array_equal(word, g["word_g_dense"])
     np.testing.assert_array_equal(word, g["word_g_bitpacked_history"])
+
+
+@pytest.mark.gpu
+def test_uniform_delivery_word_boundary_tape(cuda, golden):
+    """The 63-bit word-boundary tape (one delay for every connection) through
+    build_delivery_uniform equals the reference's recorded conductance."""
+    from dendra_gb300.netcon import build_delivery_uniform
+
+    g = golden("netcon_tapes.npz")
+    tape = g["word_tape"]
+    n = tape.shape[1]
+    depth = 2
+    hist = torch.zeros((depth, n_words_for(n)), dtype=torch.int64, device=cuda)
+    idx = torch.arange(n, device=cuda)
+    word, mask = source_word_and_mask(idx)
+    w = torch.ones(n, dtype=torch.float64, device=cuda)
+    gsum = torch.zeros(n, dtype=torch.float64, device=cuda)
+    rows = []
+    for s, spikes in enumerate(tape):
+        t = torch.tensor([s % depth], device=cuda)
+        pack_source_spikes(torch.as_tensor(spikes, device=cuda), hist, t)
+        out = torch.zeros(n, dtype=torch.float64, device=cuda)
+        build_delivery_uniform(hist, t, 1, word, mask, idx, w, out)
+        gsum = gsum + out
+        rows.append(gsum.clone())
+    np.testing.assert_array_equal(torch.stack(rows).cpu().numpy(), g["word_g_dense"])
