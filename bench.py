@@ -1965,7 +1965,8 @@ def main():
         "config": {"workload": "c2-uneven-hh-cables-extracellular", "n_cables": args.cables * world,
                    "compartments_per_rank": pop.N, "k_range": [51, 401], "dt_ms": 0.005,
                    "timesteps": n_ts, "state_dtype": "float32",
-                   "math": "exact" if args.exact else "fast (<=1e-3 mV vs float64, tested)",
+                   "math": "exact" if args.exact else "fast (float32 error vs float64: "
+                                                       "fp32_vs_fp64)",
                    "l2": "flushed between timed steps (256 MiB read, outside the events)",
                    "launch": "one persistent dgb_cable_run launch per step",
                    "warps_per_block": wpb[0], "lanes_split_k16_k8": list(wpb[1:]),
