@@ -184,19 +184,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-COVERED_TIMING = ("CUDA events on the launching stream; a 0.1 ms device sleep before the "
+COVERED_TIMING = ("CUDA events on the launching stream; a 1 ms device sleep before the "
                   "start event keeps host enqueue out of the events")
 
 
 def _cover_enqueue():
-    """Queue a short device sleep (about 0.1 ms) right before a start event, so
+    """Queue a device sleep (about 1 ms) right before a start event, so
     the stream is still busy while the host enqueues the event and the timed
     launch: the events then bracket the kernel, not host enqueue latency.  The
     sleep runs before the start event and is not timed.  Host overhead is in
     each line's ``e2e`` figure instead."""
     import torch
 
-    torch.cuda._sleep(200_000)
+    torch.cuda._sleep(2_000_000)
 
 
 def _dist():
@@ -1069,7 +1069,8 @@ def bench_bt(args, world, rank, local):
 
 
 TRIDIAG_BYTES_PER_ROW = 20  # float32 row: read a, b, c, d, write x
-TRIDIAG_NCU_TRAFFIC = 105014272 + 7976704  # dram read + write of one 16,384 x 401 launch (ncu)
+# dram read + write of one 16,384 x 401 float32 launch of tridiag_bulk_kernel (ncu)
+TRIDIAG_NCU_TRAFFIC = 105026048 + 6610944
 
 
 def _tridiag_system(B, K, seed, dtype):
@@ -1139,12 +1140,18 @@ def bench_tridiag(args, world, rank, local):
     h2d = sum(t.numel() * t.element_size() for t in pinned)
     d2h = out.numel() * out.element_size()
     dbuf = [torch.empty_like(t, device=dev) for t in host]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+
+    def e2e_step():
         for d_, h_ in zip(dbuf, pinned):
             d_.copy_(h_, non_blocking=True)
         out.copy_(thomas_solve_cuda_t(*dbuf), non_blocking=True)
+
+    for _ in range(max(3, args.warmup)):  # the public op's first dispatches
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
     peak, peak_kind = _peaks()
@@ -1164,7 +1171,7 @@ def bench_tridiag(args, world, rank, local):
                    "l2": "flushed between timed steps (256 MiB read, outside the events)",
                    "timing": COVERED_TIMING},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "kernel": "tridiag_kernel",
+                     "frac": achieved / peak, "kernel": "tridiag_bulk_kernel",
                      "traffic": TRIDIAG_NCU_TRAFFIC if (B, K) == (16384, 401) else None,
                      "note": f"{TRIDIAG_BYTES_PER_ROW} algorithmic B per float32 row (read "
                              "a, b, c, d, write x); traffic = DRAM read + write of one "

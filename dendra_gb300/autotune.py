@@ -165,7 +165,7 @@ def tune_tridiag_lanes(B, K, dtype=torch.float32, device="cuda", candidates=(4, 
     c = (-torch.rand(B, K - 1, generator=g, dtype=torch.float64)).to(device, dtype)
     b = (3.0 + torch.rand(B, K, generator=g, dtype=torch.float64)).to(device, dtype)
     d = torch.randn(B, K, generator=g, dtype=torch.float64).to(device, dtype)
-    ok = [n for n in candidates if -(-K // n) <= 32]
+    ok = [n for n in candidates if -(-K // n) <= 33]
     return tune("tridiag_lanes", (str(dtype), B, K), ok,
                 lambda n: tridiag_solve_lanes(a, b, c, d, lanes=n), device, reps, force)
 

@@ -1,6 +1,8 @@
 // Library-wide C-ABI helpers: version, last error, device properties.
 #include <stdarg.h>
 
+#include <atomic>
+
 #include "common.cuh"
 
 namespace dgb {
@@ -16,11 +18,17 @@ void set_error(const char* fmt, ...) {
 
 void clear_error() { g_last_error[0] = 0; }
 
+// SM count of the current device, cached per device (launchers ask on every
+// call; the attribute query costs host time on the launch path).
 int device_sm_count() {
+  static std::atomic<int> cached[64];
   int dev = 0, n = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (dev >= 0 && dev < 64 && (n = cached[dev].load(std::memory_order_relaxed)) > 0) return n;
   if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
-  return n > 0 ? n : 1;
+  if (n < 1) n = 1;
+  if (dev >= 0 && dev < 64) cached[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 }  // namespace dgb

@@ -33,9 +33,33 @@ __device__ __forceinline__ T shfl_down(T v, int delta, int width) {
   return __shfl_down_sync(0xffffffffu, v, delta, width);
 }
 
+// Reciprocal used by the solve.  Exact mode: the correctly rounded 1/x.
+// Fast mode (float only): the hardware approximation rcp.approx.f32 refined by
+// one Newton-Raphson step, r' = r + r (1 - x r), which brings it to within
+// about one ulp of 1/x for normal x with three instructions and no branch.
+// The reference's Triton solves divide with the approximate float division,
+// so the fast mode stays inside its parity tolerances.
+template <typename T, bool FAST>
+__device__ __forceinline__ T solve_rcp(T x) {
+  if constexpr (FAST && sizeof(T) == 4) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return fmaf(r, fmaf(-x, r, 1.0f), r);
+  } else {
+    return T(1) / x;
+  }
+}
+
+// The tridiagonal drop-ins solve float systems in fast mode, double systems
+// exactly.
+template <typename T>
+constexpr bool kFastRcp = sizeof(T) == 4;
+
 // Solve in place: on return d[j] holds x for the lane's rows.  a, b, c are
 // clobbered.  All 32 lanes of the warp must call this together (groups of P).
-template <typename T, int CH, int P>
+// FAST selects the reciprocal (solve_rcp) and, in the reduction, multiplies
+// by the neighbours' reciprocal pivots instead of dividing by their pivots.
+template <typename T, int CH, int P, bool FAST = false>
 __device__ __forceinline__ void chunk_solve(T (&a)[CH], T (&b)[CH], T (&c)[CH], T (&d)[CH],
                                             int r) {
   T As, Bs, Cs, Ds;  // reduced row of x_s
@@ -52,14 +76,14 @@ __device__ __forceinline__ void chunk_solve(T (&a)[CH], T (&b)[CH], T (&c)[CH], 
     // Forward sweep over rows 1..CH-1, in terms of x_s:
     //   x_j + ap_j x_s + cp_j x_{j+1} = dp_j   (stored in a, c, d)
     {
-      T rinv = T(1) / b[1];
+      T rinv = solve_rcp<T, FAST>(b[1]);
       a[1] = a[1] * rinv;
       c[1] = c[1] * rinv;
       d[1] = d[1] * rinv;
     }
 #pragma unroll
     for (int j = 2; j < CH; ++j) {
-      T rinv = T(1) / (b[j] - a[j] * c[j - 1]);
+      T rinv = solve_rcp<T, FAST>(b[j] - a[j] * c[j - 1]);
       T aj = a[j];
       a[j] = -aj * a[j - 1] * rinv;
       d[j] = (d[j] - aj * d[j - 1]) * rinv;
@@ -116,14 +140,16 @@ __device__ __forceinline__ void chunk_solve(T (&a)[CH], T (&b)[CH], T (&c)[CH], 
   // Parallel cyclic reduction across the P lanes.
 #pragma unroll
   for (int s = 1; s < P; s <<= 1) {
-    T al_l = shfl_up<T>(al, s, P), be_l = shfl_up<T>(be, s, P);
+    // FAST: the neighbours' pivots travel as reciprocals (one per lane)
+    const T piv = FAST ? solve_rcp<T, FAST>(be) : be;
+    T al_l = shfl_up<T>(al, s, P), be_l = shfl_up<T>(piv, s, P);
     T ga_l = shfl_up<T>(ga, s, P), de_l = shfl_up<T>(de, s, P);
-    T al_r = shfl_down<T>(al, s, P), be_r = shfl_down<T>(be, s, P);
+    T al_r = shfl_down<T>(al, s, P), be_r = shfl_down<T>(piv, s, P);
     T ga_r = shfl_down<T>(ga, s, P), de_r = shfl_down<T>(de, s, P);
     const bool hl = r >= s;
     const bool hr = r + s < P;
-    T k1 = hl ? al / be_l : T(0);
-    T k2 = hr ? ga / be_r : T(0);
+    T k1 = hl ? (FAST ? al * be_l : al / be_l) : T(0);
+    T k2 = hr ? (FAST ? ga * be_r : ga / be_r) : T(0);
     T al_n = hl ? -k1 * al_l : T(0);
     T ga_n = hr ? -k2 * ga_r : T(0);
     be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
@@ -131,7 +157,7 @@ __device__ __forceinline__ void chunk_solve(T (&a)[CH], T (&b)[CH], T (&c)[CH], 
     al = al_n;
     ga = ga_n;
   }
-  T xs = de / be;
+  T xs = FAST ? de * solve_rcp<T, FAST>(be) : de / be;
   if constexpr (CH == 1) {
     d[0] = xs;
   } else {

@@ -5,13 +5,25 @@
 // systems with a (B,K-1), b (B,K), c (B,K-1), d (B,K) -> x (B,K).
 //
 // One group of P lanes owns one system, CH rows per lane, held in registers
-// for the whole solve (see chunk_solve.cuh); systems longer than 1024 rows
-// run a serial Thomas per thread.  The reference kernels instead
+// for the whole solve (see chunk_solve.cuh).  Bands with 16-byte aligned
+// bases run the bulk-staged kernel (tridiag_bulk.cu: the copy engine fills
+// shared-memory stages); others run tridiag_kernel below, which loads each
+// lane's rows directly; both do the same arithmetic.  Systems longer than
+// 1024 rows run a serial Thomas per thread.  The reference kernels instead
 // run one program per system with a scalar loop over K (Thomas) or stage
 // every PCR stage through global memory.
+#include <atomic>
+
 #include "chunk_solve.cuh"
 
 namespace dgb {
+
+// Bulk-staged solve (tridiag_bulk.cu): DGB_OK when launched, a negative error
+// code, or 1 when it does not apply (unaligned bands, stages too large).
+int tridiag_bulk(int P, int ch, int64_t B, int64_t K, const float* a, const float* b,
+                 const float* c, const float* d, float* x, cudaStream_t st);
+int tridiag_bulk(int P, int ch, int64_t B, int64_t K, const double* a, const double* b,
+                 const double* c, const double* d, double* x, cudaStream_t st);
 
 template <typename T, int CH, int P>
 __global__ void __launch_bounds__(128) tridiag_kernel(int64_t B, int64_t K,
@@ -39,7 +51,7 @@ __global__ void __launch_bounds__(128) tridiag_kernel(int64_t B, int64_t K,
       rb[j] = in ? b[sys * K + i] : T(1);
       rd[j] = in ? d[sys * K + i] : T(0);
     }
-    chunk_solve<T, CH, P>(ra, rb, rc, rd, r);
+    chunk_solve<T, CH, P, kFastRcp<T>>(ra, rb, rc, rd, r);
 #pragma unroll
     for (int j = 0; j < CH; ++j) {
       const int64_t i = (int64_t)r * CH + j;
@@ -49,23 +61,46 @@ __global__ void __launch_bounds__(128) tridiag_kernel(int64_t B, int64_t K,
 }
 
 // Instantiated chunk sizes; a system of K rows uses the smallest CH >= K/P.
-static const int kChunks[] = {1, 2, 3, 4, 5, 6, 7, 8, 10, 12, 13, 16, 24, 32};
+// Odd only: lane r's rows start r*CH words apart, so an odd CH puts the 32
+// lanes of a shared-memory read on 32 different banks (an even CH would
+// serialise them gcd(CH, 32)-fold in the bulk-staged kernel).
+static const int kChunks[] = {1, 3, 5, 7, 9, 11, 13, 15, 17, 21, 25, 33};
+// Longest system on the chunked kernels; longer ones run the serial Thomas.
+constexpr int64_t kMaxChunkedK = 1024;
+
+// Blocks for a grid-stride launch: every resident slot filled once (one wave;
+// an oversubscribed grid would leave a partial last wave idle-tailed).
+// The occupancy query runs once per kernel (no dynamic shared memory, so the
+// answer does not depend on the device's size or the call).
+template <typename K_>
+static int64_t resident_blocks(K_ kern, int threads, int64_t needed, std::atomic<int>& cached) {
+  int per_sm = cached.load(std::memory_order_relaxed);
+  if (per_sm < 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    cached.store(per_sm, std::memory_order_relaxed);
+  }
+  const int64_t cap = (int64_t)device_sm_count() * per_sm;
+  return needed < cap ? needed : cap;
+}
 
 template <typename T, int P>
 static int launch_p(int ch, int64_t B, int64_t K, const T* a, const T* b, const T* c,
                     const T* d, T* x, cudaStream_t st) {
   const int64_t groups = (B + (32 / P) - 1) / (32 / P);
   const int64_t blocks_needed = (groups + 3) / 4;
-  const int64_t max_blocks = (int64_t)device_sm_count() * 16;
-  const int blocks = (int)(blocks_needed < max_blocks ? blocks_needed : max_blocks);
-#define DGB_CASE(CHV)                                                            \
-  case CHV:                                                                      \
-    tridiag_kernel<T, CHV, P><<<blocks, 128, 0, st>>>(B, K, a, b, c, d, x);      \
-    break;
+#define DGB_CASE(CHV)                                                                        \
+  case CHV: {                                                                                \
+    auto kern = tridiag_kernel<T, CHV, P>;                                                   \
+    static std::atomic<int> per_sm{0};                                                       \
+    const int blocks = (int)resident_blocks(kern, 128, blocks_needed, per_sm);              \
+    kern<<<blocks, 128, 0, st>>>(B, K, a, b, c, d, x);                                       \
+  } break;
   switch (ch) {
-    DGB_CASE(1) DGB_CASE(2) DGB_CASE(3) DGB_CASE(4) DGB_CASE(5) DGB_CASE(6)
-    DGB_CASE(7) DGB_CASE(8) DGB_CASE(10) DGB_CASE(12) DGB_CASE(13) DGB_CASE(16)
-    DGB_CASE(24) DGB_CASE(32)
+    DGB_CASE(1) DGB_CASE(3) DGB_CASE(5) DGB_CASE(7) DGB_CASE(9) DGB_CASE(11)
+    DGB_CASE(13) DGB_CASE(15) DGB_CASE(17) DGB_CASE(21) DGB_CASE(25) DGB_CASE(33)
     default:
       set_error("internal: no tridiagonal chunk instantiation for %d", ch);
       return DGB_EINVAL;
@@ -150,6 +185,7 @@ static int chunk_for(int64_t K, int P) {
 template <typename T>
 static int solve_t(int method, int64_t B, int64_t K, const T* a, const T* b, const T* c,
                    const T* d, T* x, cudaStream_t st, int lanes) {
+  if (K > kMaxChunkedK) return thomas_serial<T>(B, K, a, b, c, d, x, st);
   int P = lanes > 0 ? lanes : default_lanes(K, method);
   int ch = chunk_for(K, P);
   if (ch < 0 && P < 32) {
@@ -157,6 +193,9 @@ static int solve_t(int method, int64_t B, int64_t K, const T* a, const T* b, con
     ch = chunk_for(K, P);
   }
   if (ch < 0) return thomas_serial<T>(B, K, a, b, c, d, x, st);
+  // bulk-staged kernel when the bands are 16-byte aligned and its stages fit
+  const int bulk_rc = tridiag_bulk(P, ch, B, K, a, b, c, d, x, st);
+  if (bulk_rc <= 0) return bulk_rc;
   switch (P) {
     case 4: return launch_p<T, 4>(ch, B, K, a, b, c, d, x, st);
     case 8: return launch_p<T, 8>(ch, B, K, a, b, c, d, x, st);

@@ -166,6 +166,15 @@ def pcr_solve_cuda_t(a, b, c, d):
     return tridiag_solve_op(a, b, c, d, _lib.PCR, False)
 
 
+def tridiag_status(device) -> None:
+    """Raise ``DgbTimeout`` if a bounded stage wait inside a bulk-staged
+    tridiagonal solve on ``device`` gave up since the last call (those systems
+    were then not solved).  Synchronises the current stream."""
+    with torch.cuda.device(device):
+        rc = _lib.load().dgb_tridiag_status(_lib.stream_ptr(device))
+    _lib.check(rc, "bulk-staged tridiagonal solve")
+
+
 def tridiag_solve_lanes(a, b, c, d, lanes: int):
     """Forward-only solve with an explicit lanes-per-system split (autotuner)."""
     validate_tridiagonal(a, b, c, d)

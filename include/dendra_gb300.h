@@ -116,6 +116,22 @@ int dgb_tridiag_solve_lanes(int dtype, int64_t B, int64_t K, const void* a,
                             void* x, int32_t lanes, void* stream);
 
 /*
+ * Synchronises the stream and returns DGB_ETIMEOUT if a bounded wait inside a
+ * bulk-staged tridiagonal solve on this device gave up since the last call
+ * (the systems of that CTA were then not solved), else DGB_OK; clears the
+ * flag.  Bands, right-hand sides and solutions whose base addresses are
+ * 16-byte aligned run the bulk-staged kernel (cp.async.bulk copies of each
+ * tile's band slices into shared memory, completed on an mbarrier); others
+ * run the register-direct kernel, with identical arithmetic.
+ */
+int dgb_tridiag_status(void* stream);
+
+/* Diagnostic: polls a bulk-staged tridiagonal CTA spends on each stage wait
+   before it gives up (0 = give up at the first poll; negative restores the
+   default).  A wait that gave up drains its copies at the full limit. */
+int dgb_tridiag_set_wait_limit(int64_t polls);
+
+/*
  * Solve the transposed systems A^T y = g for the same bands (adjoint of
  * dgb_tridiag_solve): the transpose has sub-diagonal c and super-diagonal a.
  * Replaces the transpose solve inside ThomasSolve.backward.
