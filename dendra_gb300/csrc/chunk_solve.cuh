@@ -33,28 +33,6 @@ __device__ __forceinline__ T shfl_down(T v, int delta, int width) {
   return __shfl_down_sync(0xffffffffu, v, delta, width);
 }
 
-// Reciprocal used by the solve.  Exact mode: the correctly rounded 1/x.
-// Fast mode (float only): the hardware approximation rcp.approx.f32 refined by
-// one Newton-Raphson step, r' = r + r (1 - x r), which brings it to within
-// about one ulp of 1/x for normal x with three instructions and no branch.
-// The reference's Triton solves divide with the approximate float division,
-// so the fast mode stays inside its parity tolerances.
-template <typename T, bool FAST>
-__device__ __forceinline__ T solve_rcp(T x) {
-  if constexpr (FAST && sizeof(T) == 4) {
-    float r;
-    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return fmaf(r, fmaf(-x, r, 1.0f), r);
-  } else {
-    return T(1) / x;
-  }
-}
-
-// The tridiagonal drop-ins solve float systems in fast mode, double systems
-// exactly.
-template <typename T>
-constexpr bool kFastRcp = sizeof(T) == 4;
-
 // Solve in place: on return d[j] holds x for the lane's rows.  a, b, c are
 // clobbered.  All 32 lanes of the warp must call this together (groups of P).
 // FAST selects the reciprocal (solve_rcp) and, in the reduction, multiplies

@@ -48,6 +48,28 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 int device_sm_count();
 
+// Reciprocal used by the tridiagonal and tree solves.  Exact mode: the correctly rounded 1/x.
+// Fast mode (float only): the hardware approximation rcp.approx.f32 refined by
+// one Newton-Raphson step, r' = r + r (1 - x r), which brings it to within
+// about one ulp of 1/x for normal x with three instructions and no branch.
+// The reference's Triton solves divide with the approximate float division
+// (div.full.f32), so the fast mode stays inside its parity tolerances.
+template <typename T, bool FAST>
+__device__ __forceinline__ T solve_rcp(T x) {
+  if constexpr (FAST && sizeof(T) == 4) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return fmaf(r, fmaf(-x, r, 1.0f), r);
+  } else {
+    return T(1) / x;
+  }
+}
+
+// The tridiagonal drop-ins and the network's tree solve take float systems in
+// fast mode, double systems exactly.
+template <typename T>
+constexpr bool kFastRcp = sizeof(T) == 4;
+
 // ---------------------------------------------------------------------------
 // dtype-specific HH arithmetic.  Branch thresholds and polynomial degrees
 // follow the reference per dtype:

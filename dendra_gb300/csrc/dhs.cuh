@@ -47,7 +47,9 @@ struct GroupSync {
 
 // sD, sB: shared arrays of K values holding d and b on entry; g: axial
 // conductances of this tree (global or shared).  On return sB holds x.
-template <typename T, typename I, int W = 32, class Sync = WarpSync>
+// FAST (float only): solve_rcp reciprocals, x = (b + g x_p) * rcp(d + g) in
+// the substitution, exactly as the FAST chain schedule below computes them.
+template <typename T, typename I, int W = 32, class Sync = WarpSync, bool FAST = false>
 __device__ __forceinline__ void dhs_eliminate(const TreeTopoT<I>& t, const T* g, T* sD, T* sB,
                                               int lane, Sync sync = Sync()) {
   for (int l = 0; l < t.L; ++l) {
@@ -60,7 +62,7 @@ __device__ __forceinline__ void dhs_eliminate(const TreeTopoT<I>& t, const T* g,
         const int c = t.child_idx[k];
         const T gc = g[c];
         const T Dc = sD[c];
-        const T f = gc * (T(1) / (Dc + gc));
+        const T f = gc * solve_rcp<T, FAST>(Dc + gc);
         D = D + f * Dc;
         Bv = Bv + f * sB[c];
       }
@@ -71,7 +73,7 @@ __device__ __forceinline__ void dhs_eliminate(const TreeTopoT<I>& t, const T* g,
   }
 }
 
-template <typename T, typename I, int W = 32, class Sync = WarpSync>
+template <typename T, typename I, int W = 32, class Sync = WarpSync, bool FAST = false>
 __device__ __forceinline__ void dhs_substitute(const TreeTopoT<I>& t, const T* g, T* sD, T* sB,
                                                int lane, Sync sync = Sync()) {
   for (int l = t.L - 1; l >= 0; --l) {
@@ -81,7 +83,8 @@ __device__ __forceinline__ void dhs_substitute(const TreeTopoT<I>& t, const T* g
       const I p = t.parent[i];
       const T gi = g[i];
       const T xp = has_parent(p) ? sB[p] : T(0);
-      sB[i] = (sB[i] + gi * xp) / (sD[i] + gi);
+      sB[i] = FAST ? (sB[i] + gi * xp) * solve_rcp<T, FAST>(sD[i] + gi)
+                   : (sB[i] + gi * xp) / (sD[i] + gi);
     }
     sync();
   }
@@ -105,8 +108,11 @@ struct ChainTopoT {
   int32_t n_levels;
 };
 
-// lane: index of the thread among the W threads solving this tree.
-template <typename T, typename I, int W = 32, class Sync = WarpSync>
+// lane: index of the thread among the W threads solving this tree.  FAST
+// (float only) takes the reciprocals as solve_rcp's refined approximation and,
+// in the substitution, multiplies by the next node's reciprocal pivot, which
+// is formed one node ahead, off the recurrence's critical path.
+template <typename T, typename I, int W = 32, class Sync = WarpSync, bool FAST = false>
 __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const ChainTopoT<I>& c,
                                                 const T* g, T* sD, T* sB, int lane,
                                                 Sync sync = Sync()) {
@@ -121,7 +127,7 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
         const int cc = t.child_idx[k];
         const T gc = g[cc];
         const T Dc = sD[cc];
-        const T f = gc * (T(1) / (Dc + gc));
+        const T f = gc * solve_rcp<T, FAST>(Dc + gc);
         D = D + f * Dc;
         Bv = Bv + f * sB[cc];
       }
@@ -149,7 +155,7 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
           bn = sB[jn];
           gn = g[jn];
         }
-        const T f = gc * (T(1) / (D + gc));
+        const T f = gc * solve_rcp<T, FAST>(D + gc);
         D = dj + f * D;
         Bv = bj + f * Bv;
         sD[j] = D;
@@ -166,7 +172,7 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
   }
 }
 
-template <typename T, typename I, int W = 32, class Sync = WarpSync>
+template <typename T, typename I, int W = 32, class Sync = WarpSync, bool FAST = false>
 __device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const ChainTopoT<I>& c,
                                                  const T* g, T* sD, T* sB, int lane,
                                                  Sync sync = Sync()) {
@@ -181,6 +187,7 @@ __device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const Ch
       int j = c.nodes[e - 1];
       int jn = e - 2 >= p ? c.nodes[e - 2] : 0;
       T bj = sB[j], dj = sD[j], gj = g[j];
+      T rj = FAST ? solve_rcp<T, FAST>(dj + gj) : T(0);
       for (int q = e - 1; q >= p; --q) {
         const int jnn = q - 2 >= p ? c.nodes[q - 2] : 0;
         T bn = T(0), dn = T(0), gn = T(0);
@@ -189,13 +196,15 @@ __device__ __forceinline__ void chain_substitute(const TreeTopoT<I>& t, const Ch
           dn = sD[jn];
           gn = g[jn];
         }
-        xp = (bj + gj * xp) / (dj + gj);
+        const T rn = FAST ? solve_rcp<T, FAST>(dn + gn) : T(0);
+        xp = FAST ? (bj + gj * xp) * rj : (bj + gj * xp) / (dj + gj);
         sB[j] = xp;
         j = jn;
         jn = jnn;
         bj = bn;
         dj = dn;
         gj = gn;
+        rj = rn;
       }
     }
     sync();

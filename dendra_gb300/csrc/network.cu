@@ -14,7 +14,9 @@
 //   3. state advance: A, B exact decay, soma HH gates by cnexp at v_old;
 //   4. tree system (integrators/tree.py:1202-1357): f = (J - G v) area, axial
 //      flows between child and parent, main = cm/dt + G area; DHS solve
-//      (dhs.cuh); v += dv.
+//      (dhs.cuh; float cells take the chain sweeps' reciprocals in fast mode,
+//      as the reference's Triton tree solve divides with the approximate
+//      float division); v += dv.
 // dgb_net_enqueue then scatters the window's spikes into the delay ring,
 // one thread per target synapse, in connection then step order.
 #include <type_traits>
@@ -245,11 +247,11 @@ __global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetAr
       }
       cell_sync<T, TPC>(group);
       if (chains) {
-        chain_eliminate<T, uint16_t, TPC>(t, ct, sG, sD, sB, lane, sync);
-        chain_substitute<T, uint16_t, TPC>(t, ct, sG, sD, sB, lane, sync);
+        chain_eliminate<T, uint16_t, TPC, Sync, kFastRcp<T>>(t, ct, sG, sD, sB, lane, sync);
+        chain_substitute<T, uint16_t, TPC, Sync, kFastRcp<T>>(t, ct, sG, sD, sB, lane, sync);
       } else {
-        dhs_eliminate<T, uint16_t, TPC>(t, sG, sD, sB, lane, sync);
-        dhs_substitute<T, uint16_t, TPC>(t, sG, sD, sB, lane, sync);
+        dhs_eliminate<T, uint16_t, TPC, Sync, kFastRcp<T>>(t, sG, sD, sB, lane, sync);
+        dhs_substitute<T, uint16_t, TPC, Sync, kFastRcp<T>>(t, sG, sD, sB, lane, sync);
       }
       for (int i = lane; i < K; i += TPC) sV[i] = sV[i] + sB[i];
       cell_sync<T, TPC>(group);
