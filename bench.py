@@ -33,6 +33,26 @@ sys.path.insert(0, ROOT)
 
 METRIC = "compartment-steps/s"
 ALG_BYTES_PER_COMP_STEP = 48  # unfused per-step traffic of one float32 compartment-step
+# persistent config-2 kernel under ncu (4,096 cables x 100 steps, float32 fast
+# math): DRAM bytes per compartment per launch, thread instructions per
+# compartment-step (profiles/ holds the capture's summary)
+C2_NCU_DRAM_BYTES_PER_COMP = 22540800 / 932014
+C2_NCU_THREAD_INSTR_PER_COMP_STEP = 798385556 * 31.61 / 93201400
+
+
+def _issue_bound(instr_per_unit, units, ms, clocks, dev):
+    """The on-chip bound of an issue-bound kernel: the time its instructions
+    take at one instruction per scheduler per cycle on every SM at the timed
+    region's median SM clock, as a fraction of the measured time."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = (clocks.summary() or {}).get("sm_mhz") or 2070.0
+    ceiling_ms = instr_per_unit * units / (sms * 4 * 32 * mhz * 1e6) * 1e3
+    return {"bound": "issue", "thread_instructions_per_unit": instr_per_unit,
+            "ceiling_ms": ceiling_ms, "frac": ceiling_ms / ms, "sm_mhz": mhz,
+            "note": "instructions per compartment-step from the ncu capture; ceiling = "
+                    "all 4 schedulers of every SM issuing every cycle"}
 L2_BYTES = 129 * 1024 * 1024
 
 
@@ -1980,11 +2000,16 @@ def main():
                    "autotune_ms": None if tune_ms is None else
                    {str(k): v for k, v in tune_ms.items()}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": C2_NCU_DRAM_BYTES_PER_COMP * pop.N,
                      "note": (f"achieved = {ALG_BYTES_PER_COMP_STEP} algorithmic B per "
                               f"compartment-step of the unfused update x {comp_steps} "
                               f"compartment-steps / launch time; peak {peak_kind} copy "
-                              "bandwidth; the persistent kernel keeps state on chip")},
+                              "bandwidth; the persistent kernel keeps state on chip, so its "
+                              "DRAM traffic (ncu, 4,096-cable capture, scaled by compartments: "
+                              "it is read once per launch, not per step) is far below the "
+                              "unfused update's")},
+        "onchip": _issue_bound(C2_NCU_THREAD_INSTR_PER_COMP_STEP, comp_steps, ms, clocks, dev),
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
         "gpu_launches": args.steps * (1 if args.no_e2e else 2),
