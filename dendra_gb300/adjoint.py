@@ -37,13 +37,16 @@ class CableGradient:
     per cable (int or per-cable sequence).  The trace has one sample per step,
     (B, n_steps + 1), sample 0 being the initial state.  overlap: recompute
     the next segment on a side stream while the adjoint of the current one
-    runs (two tapes in memory instead of one).  A float32 population built
+    runs (two tapes in memory instead of one).  Off by default: with the
+    bulk-staged adjoint the two kernels compete for shared memory on the SMs,
+    and the serial order measured faster (config 4: 247 vs 308 ms per
+    backward pass).  A float32 population built
     with fast_math runs the forward, the recompute and the adjoint's gate
     partials and solve with the fast-math arithmetic.
     """
 
     def __init__(self, pop: CablePopulation, n_steps: int, rec_idx=0, checkpoint_every=500,
-                 overlap=True):
+                 overlap=False):
         if pop.dt is None:
             raise RuntimeError("Model must be initialized before running.")
         if n_steps < 1 or checkpoint_every < 1:
@@ -165,6 +168,9 @@ class CableGradient:
         rec_done = [torch.cuda.Event() for _ in range(nbuf)]
         adj_done = [torch.cuda.Event() for _ in range(nbuf)]
         used = [False] * nbuf
+        err = torch.zeros(1, dtype=torch.int32, device=dev)
+        scratch = pop._dev["scratch"]
+        side_err = [torch.zeros(1, dtype=torch.int32, device=dev) for _ in range(nbuf)]
 
         def recompute(k):
             b = k % nbuf
@@ -179,6 +185,10 @@ class CableGradient:
                     args.scratch = self._side_scratch.data_ptr()
                 _lib.check(L.dgb_cable_run_taped(args, self._tapes[b].data_ptr(),
                                                  side.cuda_stream), "dgb_cable_run_taped")
+                if nbuf == 2:
+                    side_err[b].copy_(self._side_scratch[1:2])
+                else:
+                    err.bitwise_or_(scratch[1:2])
                 rec_done[b].record(side)
 
         with torch.cuda.device(dev):
@@ -199,10 +209,20 @@ class CableGradient:
                 args = self._args(steps, step0, works[b])
                 _lib.check(L.dgb_cable_adjoint(args, ctypes.byref(adj), main.cuda_stream),
                            "dgb_cable_adjoint")
+                err.bitwise_or_(scratch[1:2])
+                if nbuf == 2:
+                    err.bitwise_or_(side_err[b])
                 adj_done[b].record(main)
                 used[b] = True
             if nbuf == 2:
                 main.wait_stream(side)
+        # a cable the kernels could not process, or a tape-stage wait that gave
+        # up, leaves error bits in the launch's work counter (each launch resets
+        # it): they were gathered after every launch, checked once here
+        bits = int(err.item())
+        if bits:
+            raise RuntimeError(f"dgb_cable_adjoint / dgb_cable_run_taped reported error bits "
+                               f"{bits:#x}")
         # per-compartment results, kept for inspection: adjoint of the initial
         # state (v, m, h, n), dLoss/d(gnabar, gkbar, gl) and the axial term
         self.lam0, self.grad_comp, self.grad_axial = lam, gcomp, gax

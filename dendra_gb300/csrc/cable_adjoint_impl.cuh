@@ -22,6 +22,7 @@
 // ThomasSolve.backward (triton/t_kernel_thomas.py:147-189).
 #pragma once
 #include "adjoint.cuh"
+#include "bulk.cuh"
 #include "cable_common.cuh"
 #include "chunk_solve.cuh"
 
@@ -36,196 +37,140 @@ struct AdjArgsT {
   T *g_gna, *g_gk, *g_gl, *g_ax;
 };
 
-// Planes of one warp in the adjoint: tape state (V and VN swap roles every
-// step), adjoint state, solve scratch, gradient accumulators, and what phase 1
-// keeps for phase 3 (G and the six gate partials).  Geometry, lead field and
-// channel planes follow when they vary along the cable, as in the forward.
+// Error bit of scratch[1]: a tape-stage wait gave up; the warp drained its
+// copies and stopped (the segment's results are then incomplete).
+constexpr int kErrTapeWait = 4;
+constexpr uint32_t kTapeWaitLimit = 1u << 22;  // polls before a stage wait gives up
+
+// Row-interleaved planes of one warp (one cable), as in the forward kernel:
+// element (row j, plane q, lane L) at [(j * NQ + q) * 32 + L], so one row
+// pointer reaches every plane of its row at a compile-time offset and the 32
+// lanes of an access touch 32 consecutive words.  Lane r owns compartments
+// r*ch .. r*ch+ch-1.
+//   LV..LN   adjoint state          MU          transposed solve's solution
+//   AP..DP   elimination scratch    GNA..GAX    gradient accumulators
+//   G        conductance (phase 1 -> 3)  DMM..DNV  gate partials (1 -> 3)
+//   GR..CEL  geometry, lead field, channels (only when they vary, PLANES)
 enum {
-  Q_V0 = 0, Q_V1, Q_M, Q_H, Q_N, Q_LV, Q_LM, Q_LH, Q_LN, Q_MU, Q_AP, Q_CP, Q_DP,
-  Q_GNA, Q_GK, Q_GL, Q_GAX, Q_G, Q_DMM, Q_DMV, Q_DHH, Q_DHV, Q_DNN, Q_DNV, Q_FIXED
+  R_LV = 0, R_LM, R_LH, R_LN, R_MU, R_AP, R_CP, R_DP, R_GNA, R_GK, R_GL, R_GAX, R_G,
+  R_DMM, R_DMV, R_DHH, R_DHV, R_DNN, R_DNV,
+  R_BASE = 19,  // uniform geometry and channels, no lead field
+  R_GR = 19, R_GLF, R_SC, R_FLD, R_CNA, R_CK, R_CL, R_CEL,
+  R_ALL = 27
 };
 
-__host__ __device__ inline PlaneLayout adjoint_layout(bool geo_planes, bool field,
-                                                      bool chan_planes) {
-  PlaneLayout L;
-  int q = Q_FIXED;
-  L.q_geo = geo_planes ? q : -1;
-  q += geo_planes ? 3 : 0;
-  L.q_fld = field ? q : -1;
-  q += field ? 1 : 0;
-  L.q_chan = chan_planes ? q : -1;
-  q += chan_planes ? 4 : 0;
-  L.n_planes = q;
-  return L;
+template <bool PLANES>
+struct AdjNQ {
+  static constexpr int value = PLANES ? R_ALL : R_BASE;
+};
+
+// Tape stages: the 4 tape planes (v, m, h, n) of one step in natural order,
+// brought by cp.async.bulk; plane q of stage b is a region of `cap` elements
+// whose compartment i sits at sh[q] + i (the copy starts at the 16-byte
+// boundary below the plane's first compartment; the last partial 16 bytes
+// come by plain loads).  Then v of the step after the current one (vn, cap
+// elements, natural order).
+template <typename T>
+__host__ __device__ inline int64_t tape_stage_cap(int ch_max) {
+  constexpr int64_t E = 16 / sizeof(T);
+  return ((int64_t)32 * ch_max + E - 1 + E - 1) / E * E;
 }
 
-// Chunked tridiagonal solve of one warp's system held in shared-memory
-// planes: rows i = r*ch + j, coefficients from row(j, a, b, c, d); the
-// solution goes to plane qx.  Same elimination as the forward's fused solve
-// (local sweep per lane, reduced row per lane, PCR across the 32 lanes).
-template <typename T, bool FAST, class Row>
-__device__ __forceinline__ void plane_solve(const Planes<T>& P, int ch, int qx, Row row) {
-  const int r = threadIdx.x & 31;
-  const int last = ch - 1;
-  T As = T(0), Bs = T(1), Cs = T(0), Ds = T(0);
-  T ap = T(0), cp = T(0), dp = T(0);
-  for (int j = 0; j < ch; ++j) {
-    T a, b, c, d;
-    row(j, a, b, c, d);
-    if (j == 0) {
-      As = a;
-      Bs = b;
-      Cs = c;
-      Ds = d;
-    } else if (j == 1) {
-      const T rinv = dv<T, FAST>(T(1), b);
-      ap = a * rinv;
-      cp = c * rinv;
-      dp = d * rinv;
-    } else {
-      const T rinv = dv<T, FAST>(T(1), b - a * cp);
-      ap = -a * ap * rinv;
-      dp = (d - a * dp) * rinv;
-      cp = c * rinv;
-    }
-    if (j >= 1) {
-      P.at(Q_AP, j, r) = ap;
-      P.at(Q_CP, j, r) = cp;
-      P.at(Q_DP, j, r) = dp;
-    }
-  }
-  T al, be, ga, de, Ae = ap, Ce = cp, De = dp;
-  if (ch == 1) {
-    al = As;
-    be = Bs;
-    ga = Cs;
-    de = Ds;
-  } else {
-    T a2 = ap, c2 = cp, d2 = dp;
-    if (ch >= 3) {
-      a2 = P.at(Q_AP, ch - 2, r);
-      c2 = P.at(Q_CP, ch - 2, r);
-      d2 = P.at(Q_DP, ch - 2, r);
-      for (int j = ch - 3; j >= 1; --j) {
-        const T cj = P.at(Q_CP, j, r);
-        d2 = P.at(Q_DP, j, r) - cj * d2;
-        a2 = P.at(Q_AP, j, r) - cj * a2;
-        c2 = -cj * c2;
-        P.at(Q_AP, j, r) = a2;
-        P.at(Q_CP, j, r) = c2;
-        P.at(Q_DP, j, r) = d2;
-      }
-    }
-    T Bs2 = Bs, Cs2 = Cs, Ds2 = Ds;
-    if (ch >= 3) {
-      Bs2 = Bs - Cs * a2;
-      Cs2 = -Cs * c2;
-      Ds2 = Ds - Cs * d2;
-    }
-    T Ae_l = shfl_up<T>(Ae, 1, 32), Ce_l = shfl_up<T>(Ce, 1, 32), De_l = shfl_up<T>(De, 1, 32);
-    if (r == 0) {
-      Ae_l = T(0);
-      Ce_l = T(0);
-      De_l = T(0);
-    }
-    al = -As * Ae_l;
-    be = Bs2 - As * Ce_l - Cs2 * Ae;
-    ga = -Cs2 * Ce;
-    de = Ds2 - As * De_l - Cs2 * De;
-  }
+template <typename T, bool PLANES>
+__host__ __device__ inline size_t adjoint_warp_smem(int ch_max, int nstage) {
+  return ((size_t)AdjNQ<PLANES>::value * ch_max * 32 +
+          (size_t)(4 * nstage + 1) * tape_stage_cap<T>(ch_max)) * sizeof(T);
+}
+
+// Post the copies of tape step s (planes v, m, h, n of compartments
+// [off, off + K)) into stage `st`; lane 0 posts the bulk copies, lanes 0..3
+// load the partial last 16 bytes of planes 0..3.
+template <typename T>
+__device__ __forceinline__ void tape_issue(const T* tape, int64_t N, int64_t off, int K, int s,
+                                           T* st, int64_t cap, uint32_t bar, int lane) {
+  constexpr int64_t E = 16 / sizeof(T);
+  if (lane == 0) {
+    uint32_t bytes = 0;
 #pragma unroll
-  for (int sh = 1; sh < 32; sh <<= 1) {
-    T al_l = shfl_up<T>(al, sh, 32), be_l = shfl_up<T>(be, sh, 32);
-    T ga_l = shfl_up<T>(ga, sh, 32), de_l = shfl_up<T>(de, sh, 32);
-    T al_r = shfl_down<T>(al, sh, 32), be_r = shfl_down<T>(be, sh, 32);
-    T ga_r = shfl_down<T>(ga, sh, 32), de_r = shfl_down<T>(de, sh, 32);
-    const bool hl = r >= sh;
-    const bool hr = r + sh < 32;
-    T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
-    T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
-    T al_n = hl ? -k1 * al_l : T(0);
-    T ga_n = hr ? -k2 * ga_r : T(0);
-    be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
-    de = de - (hl ? k1 * de_l : T(0)) - (hr ? k2 * de_r : T(0));
-    al = al_n;
-    ga = ga_n;
+    for (int q = 0; q < 4; ++q) {
+      const int64_t lo = (int64_t)s * 4 * N + q * N + off;
+      const int64_t lo16 = lo & ~(E - 1), hi16 = (lo + K) & ~(E - 1);
+      if (hi16 > lo16) bytes += (uint32_t)((hi16 - lo16) * (int64_t)sizeof(T));
+    }
+    bulk::bar_expect(bar, bytes);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t lo = (int64_t)s * 4 * N + q * N + off;
+      const int64_t lo16 = lo & ~(E - 1), hi16 = (lo + K) & ~(E - 1);
+      if (hi16 > lo16)
+        bulk::load(bulk::smem_addr(st + q * cap), tape + lo16,
+                   (uint32_t)((hi16 - lo16) * (int64_t)sizeof(T)), bar);
+    }
   }
-  const T xs = dv<T, FAST>(de, be);
-  T xe = xs;
-  if (ch > 1) {
-    T xs_next = shfl_down<T>(xs, 1, 32);
-    if (r == 31) xs_next = T(0);
-    xe = De - Ae * xs - Ce * xs_next;
+  if (lane < 4) {
+    const int64_t lo = (int64_t)s * 4 * N + lane * N + off, hi = lo + K;
+    const int64_t lo16 = lo & ~(E - 1);
+    int64_t e = hi & ~(E - 1);
+    if (e < lo) e = lo;
+    for (; e < hi; ++e) st[lane * cap + (e - lo16)] = tape[e];
   }
-  P.at(qx, 0, r) = xs;
-  for (int j = 1; j < last; ++j)
-    P.at(qx, j, r) = P.at(Q_DP, j, r) - P.at(Q_AP, j, r) * xs - P.at(Q_CP, j, r) * xe;
-  if (ch > 1) P.at(qx, last, r) = xe;
 }
 
-// Value of plane q at row i - 1 / i + 1 of lane r's slot j (0 past the cable).
-template <typename T>
-__device__ __forceinline__ T row_prev(const Planes<T>& P, int q, int j, int r, int last) {
-  return j > 0 ? P.at(q, j - 1, r) : (r > 0 ? P.at(q, last, r - 1) : T(0));
-}
-template <typename T>
-__device__ __forceinline__ T row_next(const Planes<T>& P, int q, int j, int r, int last) {
-  return j < last ? P.at(q, j + 1, r) : (r < 31 ? P.at(q, 0, r + 1) : T(0));
-}
-
-template <typename T, bool FAST>
-__device__ void adjoint_cable(const CableArgsT<T>& A, const AdjArgsT<T>& D, int cable, T* smw,
-                              int ch, const PlaneLayout& lay) {
+template <typename T, bool FAST, bool PLANES>
+__device__ bool adjoint_rows(const CableArgsT<T>& A, const AdjArgsT<T>& D, int cable, T* wsm,
+                             T* stg, int64_t cap, int nstage, int ch, uint32_t* bars,
+                             uint32_t& par) {
+  constexpr int NQ = AdjNQ<PLANES>::value;
+  constexpr int rs = NQ * 32;
+  constexpr int64_t E = 16 / sizeof(T);
   const int r = threadIdx.x & 31;
   const int64_t off = A.cable_ptr[cable];
   const int K = (int)(A.cable_ptr[cable + 1] - off);
   const int64_t N = A.n_comp;
-  Planes<T> P{smw, ch};
-  const bool use_ve = lay.q_fld >= 0;
   const int last = ch - 1;
+  const int row0 = r * ch;
+  T* const p0 = wsm + r;
+  T* const vn = stg + 4 * nstage * cap;  // v after the current step, natural order
+  const bool use_ve = PLANES && A.field != nullptr && A.ve_amp != nullptr;
+  // compartment i of tape plane q sits at stage + q * cap + sh_q + i (4N is a
+  // multiple of 16 bytes, so the shift does not depend on the step)
+  int sh[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) sh[q] = (int)((q * N + off) & (E - 1));
 
-  for (int j = 0; j < ch; ++j) {
-    const int i = r * ch + j;
-    const bool in = i < K;
-    const int64_t g = off + i;
-    P.at(Q_LV, j, r) = in ? D.lam_v[g] : T(0);
-    P.at(Q_LM, j, r) = in ? D.lam_m[g] : T(0);
-    P.at(Q_LH, j, r) = in ? D.lam_h[g] : T(0);
-    P.at(Q_LN, j, r) = in ? D.lam_n[g] : T(0);
-    // the accumulators continue from their values after the later segments
-    P.at(Q_GNA, j, r) = in ? D.g_gna[g] : T(0);
-    P.at(Q_GK, j, r) = in ? D.g_gk[g] : T(0);
-    P.at(Q_GL, j, r) = in ? D.g_gl[g] : T(0);
-    P.at(Q_GAX, j, r) = in ? D.g_ax[g] : T(0);
-    // padding rows keep zero state: their gates stay finite and their
-    // adjoints stay zero (every coupling coefficient is zero there)
-    P.at(Q_V0, j, r) = T(0);
-    P.at(Q_V1, j, r) = T(0);
-    P.at(Q_M, j, r) = T(0);
-    P.at(Q_H, j, r) = T(0);
-    P.at(Q_N, j, r) = T(0);
-    if (lay.q_geo >= 0) {
-      P.at(lay.q_geo + 0, j, r) = in ? A.g_right[g] : T(0);
-      P.at(lay.q_geo + 1, j, r) = in ? A.g_left[g] : T(0);
-      P.at(lay.q_geo + 2, j, r) = in ? A.scale[g] : T(0);
-    }
-    if (use_ve) P.at(lay.q_fld, j, r) = in ? A.field[g] : T(0);
-    if (lay.q_chan >= 0) {
-      P.at(lay.q_chan + 0, j, r) = in ? A.gnabar[g] : T(0);
-      P.at(lay.q_chan + 1, j, r) = in ? A.gkbar[g] : T(0);
-      P.at(lay.q_chan + 2, j, r) = in ? A.gl[g] : T(0);
-      P.at(lay.q_chan + 3, j, r) = in ? A.el[g] : T(0);
+  // ---- state, accumulators and coefficient planes (lane r: its own rows)
+  {
+    T* pr = p0;
+    for (int j = 0; j < ch; ++j, pr += rs) {
+      const int i = row0 + j;
+      const bool in = i < K;
+      const int64_t g = off + i;
+      pr[R_LV * 32] = in ? D.lam_v[g] : T(0);
+      pr[R_LM * 32] = in ? D.lam_m[g] : T(0);
+      pr[R_LH * 32] = in ? D.lam_h[g] : T(0);
+      pr[R_LN * 32] = in ? D.lam_n[g] : T(0);
+      pr[R_GNA * 32] = in ? D.g_gna[g] : T(0);
+      pr[R_GK * 32] = in ? D.g_gk[g] : T(0);
+      pr[R_GL * 32] = in ? D.g_gl[g] : T(0);
+      pr[R_GAX * 32] = in ? D.g_ax[g] : T(0);
+      if constexpr (PLANES) {  // zero past K and at the cable's ends by contract
+        pr[R_GR * 32] = in ? A.g_right[g] : T(0);
+        pr[R_GLF * 32] = in ? A.g_left[g] : T(0);
+        pr[R_SC * 32] = in ? A.scale[g] : T(0);
+        pr[R_FLD * 32] = (in && use_ve) ? A.field[g] : T(0);
+        pr[R_CNA * 32] = in ? A.gnabar[g] : T(0);
+        pr[R_CK * 32] = in ? A.gkbar[g] : T(0);
+        pr[R_CL * 32] = in ? A.gl[g] : T(0);
+        pr[R_CEL * 32] = in ? A.el[g] : T(0);
+      }
     }
   }
-  T gna_c = T(0), gk_c = T(0), gl_c = T(0), el_c = T(0);
-  if (lay.q_chan < 0) {
+  T gna_c = T(0), gk_c = T(0), gl_c = T(0), el_c = T(0), gr_c = T(0), glf_c = T(0), sc_c = T(0);
+  if constexpr (!PLANES) {
     gna_c = A.gnabar[off];
     gk_c = A.gkbar[off];
     gl_c = A.gl[off];
     el_c = A.el[off];
-  }
-  T gr_c = T(0), glf_c = T(0), sc_c = T(0);
-  if (lay.q_geo < 0) {
     gr_c = K > 1 ? A.g_right[off] : T(0);
     glf_c = K > 1 ? A.g_left[off + 1] : T(0);
     sc_c = A.scale[off];
@@ -237,194 +182,360 @@ __device__ void adjoint_cable(const CableArgsT<T>& A, const AdjArgsT<T>& D, int 
     ve_pw = A.ve_pw[cable];
   }
   const int rec_i = (A.rec_idx && D.trace_grad) ? A.rec_idx[cable] : -1;
-  __syncwarp();
   const int S = A.n_steps;
-  int qv = Q_V0, qvn = Q_V1;
   // v after the segment
-  {
-    const T* src = D.tape + (int64_t)S * 4 * N + off;
-    for (RowWalk w(r, ch); w.i < K; w.next()) P.at(qvn, w.j, w.lane) = src[w.i];
-  }
+  for (int i = r; i < K; i += 32) vn[i] = D.tape[(int64_t)S * 4 * N + off + i];
+  __syncwarp();
+  bulk::fence_async_smem();  // earlier generic use of the stages before the copies
+  if (S >= 1) tape_issue<T>(D.tape, N, off, K, S - 1, stg + ((S - 1) & (nstage - 1)) * 4 * cap,
+                            cap, bars[(S - 1) & (nstage - 1)], r);
   const T dt = A.dt, dt_s = A.dt_s, q10 = A.q10, ena = A.ena, ek = A.ek;
-  // per-row coefficients (uniform values or planes)
-  auto geo = [&](int j, T& gr, T& glf, T& scl) {
-    if (lay.q_geo >= 0) {
-      gr = P.at(lay.q_geo, j, r);
-      glf = P.at(lay.q_geo + 1, j, r);
-      scl = P.at(lay.q_geo + 2, j, r);
+
+  // per-row coefficients of row j (compartment i): uniform values or planes
+  auto geo = [&](const T* pr, int i, T& gr, T& glf, T& scl) {
+    if constexpr (PLANES) {
+      gr = pr[R_GR * 32];
+      glf = pr[R_GLF * 32];
+      scl = pr[R_SC * 32];
     } else {
-      const int i = r * ch + j;
       gr = i < K - 1 ? gr_c : T(0);
       glf = (i >= 1 && i < K) ? glf_c : T(0);
       scl = i < K ? sc_c : T(0);
     }
   };
-  // g_right of row i - 1 and g_left of row i + 1 (the transposed couplings)
-  auto gr_prev = [&](int j) -> T {
-    if (lay.q_geo >= 0) return row_prev<T>(P, lay.q_geo, j, r, last);
-    const int i = r * ch + j;
-    return (i >= 1 && i <= K - 1) ? gr_c : T(0);
-  };
-  auto glf_next = [&](int j) -> T {
-    if (lay.q_geo >= 0) return row_next<T>(P, lay.q_geo + 1, j, r, last);
-    const int i = r * ch + j;
-    return (i + 1 < K) ? glf_c : T(0);
-  };
-  for (int s = S - 1; s >= 0; --s) {
-    {
-      const T* src = D.tape + (int64_t)s * 4 * N + off;
-      for (RowWalk w(r, ch); w.i < K; w.next()) {
-        P.at(qv, w.j, w.lane) = src[w.i];
-        P.at(Q_M, w.j, w.lane) = src[N + w.i];
-        P.at(Q_H, w.j, w.lane) = src[2 * N + w.i];
-        P.at(Q_N, w.j, w.lane) = src[3 * N + w.i];
-      }
+  // the transposed couplings: g_right of compartment i - 1, g_left of i + 1
+  // (PLANES: neighbouring rows, across the lane boundary at a chunk's ends)
+  auto gr_prev = [&](const T* pr, int j, int i) -> T {
+    if constexpr (PLANES) {
+      return j > 0 ? pr[-rs + R_GR * 32] : (r > 0 ? wsm[(last * NQ + R_GR) * 32 + r - 1] : T(0));
+    } else {
+      return (i >= 1 && i <= K - 1) ? gr_c : T(0);
     }
+  };
+  auto glf_next = [&](const T* pr, int j, int i) -> T {
+    if constexpr (PLANES) {
+      return j < last ? pr[rs + R_GLF * 32] : (r < 31 ? wsm[R_GLF * 32 + r + 1] : T(0));
+    } else {
+      return (i + 1 < K) ? glf_c : T(0);
+    }
+  };
+
+  for (int s = S - 1; s >= 0; --s) {
+    const int b = s & (nstage - 1);
+    T* const st = stg + b * 4 * cap;
+    if (nstage == 2 && s >= 1) {
+      // prefetch the next (earlier) step into the other stage, which every
+      // lane finished reading at the end of the previous step
+      tape_issue<T>(D.tape, N, off, K, s - 1, stg + ((s - 1) & 1) * 4 * cap, cap,
+                    bars[(s - 1) & 1], r);
+    }
+    // wait for this step's tape (phases alternate per stage use)
+    const uint32_t parity = (par >> b) & 1u;
+    const bool landed = bulk::bar_wait(bars[b], parity, kTapeWaitLimit);
+    if (!__all_sync(0xffffffffu, landed)) {
+      if (r == 0) {
+        atomicOr(A.counter + 1, kErrTapeWait);
+        // drain: this stage, and the prefetch posted into the other one
+        bulk::bar_wait(bars[b], parity, kTapeWaitLimit);
+        if (nstage == 2 && s >= 1)
+          bulk::bar_wait(bars[b ^ 1], (par >> (b ^ 1)) & 1u, kTapeWaitLimit);
+      }
+      __syncwarp();
+      return false;
+    }
+    par ^= 1u << b;
+    __syncwarp();  // the plain tail loads of this stage
+    const T* sv = st + sh[0];
+    T* sm = st + cap + sh[1];
+    T* shh = st + 2 * cap + sh[2];
+    T* sn = st + 3 * cap + sh[3];
     // the trace sample recorded after this step
     const int64_t gstep = A.step0 + s + 1;
     if (rec_i >= 0 && r == rec_i / ch && gstep % A.rec_every == 0 &&
         gstep / A.rec_every < D.trace_len)
-      P.at(Q_LV, rec_i % ch, r) += D.trace_grad[(int64_t)cable * D.trace_len + gstep / A.rec_every];
+      p0[(rec_i % ch) * rs + R_LV * 32] +=
+          D.trace_grad[(int64_t)cable * D.trace_len + gstep / A.rec_every];
     __syncwarp();
     const T t = (T)(A.t0_ms + (double)(A.step0 + s) * A.dt_ms_d);
     const T Ive = use_ve ? rect_pulse<T>(t, ve_amp, ve_delay, ve_pw) : T(0);
     const bool ve_on = Ive != T(0);
 
-    // ---- phase 1: gates with partials at v_old, conductance G
-    for (int j = 0; j < ch; ++j) {
-      const T v = P.at(qv, j, r);
-      T m = P.at(Q_M, j, r), h = P.at(Q_H, j, r), n = P.at(Q_N, j, r);
-      T dmm, dmv, dhh, dhv, dnn, dnv;
-      if constexpr (FAST) {
-        hh_gates_partials_fast(v, q10, dt, m, h, n, dmm, dmv, dhh, dhv, dnn, dnv);
-      } else {
-        hh_gates_partials<T>(v, q10, dt, m, h, n, dmm, dmv, dhh, dhv, dnn, dnv);
+    // ---- phases 1 + 2a: gates with partials at v_old, conductance G, fused
+    // with the forward sweep of the transposed solve M^T mu = lv
+    T As = T(0), Bs = T(1), Cs = T(0), Ds = T(0);
+    T ap = T(0), cp = T(0), dp = T(0);
+    {
+      T* pr = p0;
+      for (int j = 0; j < ch; ++j, pr += rs) {
+        const int i = row0 + j;
+        const bool in = i < K;
+        // padding rows keep zero state: their gates stay finite and their
+        // adjoints stay zero (every coupling coefficient is zero there)
+        const T v = in ? sv[i] : T(0);
+        T m = in ? sm[i] : T(0), h = in ? shh[i] : T(0), n = in ? sn[i] : T(0);
+        T dmm, dmv, dhh, dhv, dnn, dnv;
+        if constexpr (FAST) {
+          hh_gates_partials_fast(v, q10, dt, m, h, n, dmm, dmv, dhh, dhv, dnn, dnv);
+        } else {
+          hh_gates_partials<T>(v, q10, dt, m, h, n, dmm, dmv, dhh, dhv, dnn, dnv);
+        }
+        if (in) {  // the advanced gates replace the tape's in the stage
+          sm[i] = m;
+          shh[i] = h;
+          sn[i] = n;
+        }
+        pr[R_DMM * 32] = dmm;
+        pr[R_DMV * 32] = dmv;
+        pr[R_DHH * 32] = dhh;
+        pr[R_DHV * 32] = dhv;
+        pr[R_DNN * 32] = dnn;
+        pr[R_DNV * 32] = dnv;
+        T gna = gna_c, gk = gk_c, gl = gl_c;
+        if constexpr (PLANES) {
+          gna = pr[R_CNA * 32];
+          gk = pr[R_CK * 32];
+          gl = pr[R_CL * 32];
+        }
+        const T m3 = m * m * m;
+        const T n2 = n * n;
+        const T G = gl + gna * m3 * h + gk * (n2 * n2);
+        pr[R_G * 32] = G;
+        T gr, glf, scl;
+        geo(pr, i, gr, glf, scl);
+        const T bb = T(1) - dt_s * ((-gr + -glf) - mul_rn(G, scl));
+        const T aa = -dt_s * gr_prev(pr, j, i);
+        const T cc = -dt_s * glf_next(pr, j, i);
+        const T dd = pr[R_LV * 32];
+        if (j == 0) {
+          As = aa;
+          Bs = bb;
+          Cs = cc;
+          Ds = dd;
+        } else {
+          if (j == 1) {
+            const T rinv = dv<T, FAST>(T(1), bb);
+            ap = aa * rinv;
+            cp = cc * rinv;
+            dp = dd * rinv;
+          } else {
+            const T rinv = dv<T, FAST>(T(1), bb - aa * cp);
+            ap = -aa * ap * rinv;
+            dp = (dd - aa * dp) * rinv;
+            cp = cc * rinv;
+          }
+          pr[R_AP * 32] = ap;
+          pr[R_CP * 32] = cp;
+          pr[R_DP * 32] = dp;
+        }
       }
-      P.at(Q_M, j, r) = m;
-      P.at(Q_H, j, r) = h;
-      P.at(Q_N, j, r) = n;
-      P.at(Q_DMM, j, r) = dmm;
-      P.at(Q_DMV, j, r) = dmv;
-      P.at(Q_DHH, j, r) = dhh;
-      P.at(Q_DHV, j, r) = dhv;
-      P.at(Q_DNN, j, r) = dnn;
-      P.at(Q_DNV, j, r) = dnv;
-      T gna = gna_c, gk = gk_c, gl = gl_c;
-      if (lay.q_chan >= 0) {
-        gna = P.at(lay.q_chan, j, r);
-        gk = P.at(lay.q_chan + 1, j, r);
-        gl = P.at(lay.q_chan + 2, j, r);
-      }
-      const T m3 = m * m * m;
-      const T n2 = n * n;
-      P.at(Q_G, j, r) = gl + gna * m3 * h + gk * (n2 * n2);
     }
-    // ---- phase 2: M^T mu = lv'
-    plane_solve<T, FAST>(P, ch, Q_MU, [&](int j, T& a, T& b, T& c, T& d) {
-      T gr, glf, scl;
-      geo(j, gr, glf, scl);
-      b = T(1) - dt_s * ((-gr + -glf) - mul_rn(P.at(Q_G, j, r), scl));
-      a = -dt_s * gr_prev(j);
-      c = -dt_s * glf_next(j);
-      d = P.at(Q_LV, j, r);
-    });
+    // ---- phase 2b: backward sweep, reduced row, PCR across the lanes, mu
+    {
+      T al, be, ga, de;
+      const T Ae = ap, Ce = cp, De = dp;
+      if (ch == 1) {
+        al = As;
+        be = Bs;
+        ga = Cs;
+        de = Ds;
+      } else {
+        T a2 = ap, c2 = cp, d2 = dp;
+        if (ch >= 3) {
+          T* q = p0 + (ch - 2) * rs;
+          a2 = q[R_AP * 32];
+          c2 = q[R_CP * 32];
+          d2 = q[R_DP * 32];
+          for (int j = ch - 3; j >= 1; --j) {
+            q -= rs;
+            const T cj = q[R_CP * 32];
+            d2 = q[R_DP * 32] - cj * d2;
+            a2 = q[R_AP * 32] - cj * a2;
+            c2 = -cj * c2;
+            q[R_AP * 32] = a2;
+            q[R_CP * 32] = c2;
+            q[R_DP * 32] = d2;
+          }
+        }
+        T Bs2 = Bs, Cs2 = Cs, Ds2 = Ds;
+        if (ch >= 3) {
+          Bs2 = Bs - Cs * a2;
+          Cs2 = -Cs * c2;
+          Ds2 = Ds - Cs * d2;
+        }
+        T Ae_l = shfl_up<T>(Ae, 1, 32), Ce_l = shfl_up<T>(Ce, 1, 32), De_l = shfl_up<T>(De, 1, 32);
+        if (r == 0) {
+          Ae_l = T(0);
+          Ce_l = T(0);
+          De_l = T(0);
+        }
+        al = -As * Ae_l;
+        be = Bs2 - As * Ce_l - Cs2 * Ae;
+        ga = -Cs2 * Ce;
+        de = Ds2 - As * De_l - Cs2 * De;
+      }
+#pragma unroll
+      for (int sh2 = 1; sh2 < 32; sh2 <<= 1) {
+        T al_l = shfl_up<T>(al, sh2, 32), be_l = shfl_up<T>(be, sh2, 32);
+        T ga_l = shfl_up<T>(ga, sh2, 32), de_l = shfl_up<T>(de, sh2, 32);
+        T al_r = shfl_down<T>(al, sh2, 32), be_r = shfl_down<T>(be, sh2, 32);
+        T ga_r = shfl_down<T>(ga, sh2, 32), de_r = shfl_down<T>(de, sh2, 32);
+        const bool hl = r >= sh2;
+        const bool hr = r + sh2 < 32;
+        T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
+        T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
+        T al_n = hl ? -k1 * al_l : T(0);
+        T ga_n = hr ? -k2 * ga_r : T(0);
+        be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
+        de = de - (hl ? k1 * de_l : T(0)) - (hr ? k2 * de_r : T(0));
+        al = al_n;
+        ga = ga_n;
+      }
+      const T xs = dv<T, FAST>(de, be);
+      T xe = xs;
+      if (ch > 1) {
+        T xs_next = shfl_down<T>(xs, 1, 32);
+        if (r == 31) xs_next = T(0);
+        xe = De - Ae * xs - Ce * xs_next;
+      }
+      p0[R_MU * 32] = xs;
+      T* q = p0;
+      for (int j = 1; j < last; ++j) {
+        q += rs;
+        q[R_MU * 32] = q[R_DP * 32] - q[R_AP * 32] * xs - q[R_CP * 32] * xe;
+      }
+      if (ch > 1) p0[last * rs + R_MU * 32] = xe;
+    }
     __syncwarp();  // mu of the neighbouring rows
 
     // ---- phase 3: adjoints of the state before the step, parameter gradients
-    T f_prev = T(0), fj = T(0);
-    if (ve_on) {
-      f_prev = (r > 0) ? P.at(lay.q_fld, last, r - 1) : T(0);
-      fj = P.at(lay.q_fld, 0, r);
-    }
-    for (int j = 0; j < ch; ++j) {
-      const T mu = P.at(Q_MU, j, r);
-      const T mu_p = row_prev<T>(P, Q_MU, j, r, last);
-      const T mu_n = row_next<T>(P, Q_MU, j, r, last);
-      const T v = P.at(qv, j, r);
-      const T v_p = row_prev<T>(P, qv, j, r, last);
-      const T v_n = row_next<T>(P, qv, j, r, last);
-      const T x = P.at(qvn, j, r) - v;
-      const T x_p = row_prev<T>(P, qvn, j, r, last) - v_p;
-      const T x_n = row_next<T>(P, qvn, j, r, last) - v_n;
-      T gr, glf, scl;
-      geo(j, gr, glf, scl);
-      T dvr = v_n - v, dvl = v - v_p;
-      if (ve_on) {
-        const T f_next = row_next<T>(P, lay.q_fld, j, r, last);
-        const T ve_l = mul_rn(f_prev, Ive), ve_c = mul_rn(fj, Ive), ve_r = mul_rn(f_next, Ive);
-        dvr = dvr + (ve_r - ve_c);
-        dvl = dvl + (ve_c - ve_l);
-        f_prev = fj;
-        fj = f_next;
+    {
+      // sliding windows over compartments i-1, i, i+1: mu (row planes, the
+      // chunk's ends from the neighbouring lanes), v and v_next (natural order)
+      T mu_p = r > 0 ? wsm[(last * NQ + R_MU) * 32 + r - 1] : T(0);
+      T mu_c = p0[R_MU * 32];
+      const T mu_hi = r < 31 ? wsm[R_MU * 32 + r + 1] : T(0);
+      auto vat = [&](const T* a, int i) -> T { return (i >= 0 && i < K) ? a[i] : T(0); };
+      T v_p = vat(sv, row0 - 1), v_c = vat(sv, row0);
+      T x_p = vat(vn, row0 - 1) - v_p, x_c = vat(vn, row0) - v_c;
+      T f_prev = T(0), fj = T(0);
+      if (PLANES && ve_on) {
+        f_prev = r > 0 ? wsm[(last * NQ + R_FLD) * 32 + r - 1] : T(0);
+        fj = p0[R_FLD * 32];
       }
-      const T lfn = dt_s * mu;
-      const T lb = -mu * x;
-      const T la = -mu * x_p;
-      const T lc = -mu * x_n;
-      const T lgr = dt_s * (lb - lc) + dvr * lfn;
-      const T lglf = dt_s * (lb - la) - dvl * lfn;
-      P.at(Q_GAX, j, r) += lgr * gr + lglf * glf;
-      const T G = P.at(Q_G, j, r);
-      const T lG = dt_s * scl * lb - v * scl * lfn;
-      const T lJ = scl * lfn;
-      T gna = gna_c, gk = gk_c, el = el_c;
-      if (lay.q_chan >= 0) {
-        gna = P.at(lay.q_chan, j, r);
-        gk = P.at(lay.q_chan + 1, j, r);
-        el = P.at(lay.q_chan + 3, j, r);
+      T* pr = p0;
+      for (int j = 0; j < ch; ++j, pr += rs) {
+        const int i = row0 + j;
+        const T mu_n = j < last ? pr[rs + R_MU * 32] : mu_hi;
+        const T v_n = vat(sv, i + 1);
+        const T x_n = vat(vn, i + 1) - v_n;
+        const T mu = mu_c, v = v_c, x = x_c;
+        T gr, glf, scl;
+        geo(pr, i, gr, glf, scl);
+        T dvr = v_n - v, dvl = v - v_p;
+        if (PLANES && ve_on) {
+          const T f_next = j < last ? pr[rs + R_FLD * 32] : (r < 31 ? wsm[R_FLD * 32 + r + 1] : T(0));
+          const T ve_l = mul_rn(f_prev, Ive), ve_c = mul_rn(fj, Ive), ve_r = mul_rn(f_next, Ive);
+          dvr = dvr + (ve_r - ve_c);
+          dvl = dvl + (ve_c - ve_l);
+          f_prev = fj;
+          fj = f_next;
+        }
+        const T lfn = dt_s * mu;
+        const T lb = -mu * x;
+        const T la = -mu * x_p;
+        const T lc = -mu * x_n;
+        const T lgr = dt_s * (lb - lc) + dvr * lfn;
+        const T lglf = dt_s * (lb - la) - dvl * lfn;
+        pr[R_GAX * 32] += lgr * gr + lglf * glf;
+        const T G = pr[R_G * 32];
+        const T lG = dt_s * scl * lb - v * scl * lfn;
+        const T lJ = scl * lfn;
+        T gna = gna_c, gk = gk_c, el = el_c;
+        if constexpr (PLANES) {
+          gna = pr[R_CNA * 32];
+          gk = pr[R_CK * 32];
+          el = pr[R_CEL * 32];
+        }
+        const bool in = i < K;
+        const T m = in ? sm[i] : T(0), h = in ? shh[i] : T(0), n = in ? sn[i] : T(0);
+        const T m2 = m * m, n2 = n * n;
+        const T m3 = m2 * m, n3 = n2 * n;
+        const T lgna = lG + ena * lJ;
+        const T lgk = lG + ek * lJ;
+        pr[R_GNA * 32] += m3 * h * lgna;
+        pr[R_GK * 32] += (n2 * n2) * lgk;
+        pr[R_GL * 32] += lG + el * lJ;
+        const T lm = pr[R_LM * 32] + T(3) * gna * m2 * h * lgna;
+        const T lh = pr[R_LH * 32] + gna * m3 * lgna;
+        const T ln = pr[R_LN * 32] + T(4) * gk * n3 * lgk;
+        const T lv = pr[R_LV * 32] - (G * scl + gr + glf) * lfn + gr_prev(pr, j, i) * (dt_s * mu_p) +
+                     glf_next(pr, j, i) * (dt_s * mu_n) + pr[R_DMV * 32] * lm +
+                     pr[R_DHV * 32] * lh + pr[R_DNV * 32] * ln;
+        pr[R_LM * 32] = pr[R_DMM * 32] * lm;
+        pr[R_LH * 32] = pr[R_DHH * 32] * lh;
+        pr[R_LN * 32] = pr[R_DNN * 32] * ln;
+        pr[R_LV * 32] = lv;
+        mu_p = mu;
+        mu_c = mu_n;
+        v_p = v;
+        v_c = v_n;
+        x_p = x;
+        x_c = x_n;
       }
-      const T m = P.at(Q_M, j, r), h = P.at(Q_H, j, r), n = P.at(Q_N, j, r);
-      const T m2 = m * m, n2 = n * n;
-      const T m3 = m2 * m, n3 = n2 * n;
-      const T lgna = lG + ena * lJ;
-      const T lgk = lG + ek * lJ;
-      P.at(Q_GNA, j, r) += m3 * h * lgna;
-      P.at(Q_GK, j, r) += (n2 * n2) * lgk;
-      P.at(Q_GL, j, r) += lG + el * lJ;
-      const T lm = P.at(Q_LM, j, r) + T(3) * gna * m2 * h * lgna;
-      const T lh = P.at(Q_LH, j, r) + gna * m3 * lgna;
-      const T ln = P.at(Q_LN, j, r) + T(4) * gk * n3 * lgk;
-      const T lv = P.at(Q_LV, j, r) - (G * scl + gr + glf) * lfn + gr_prev(j) * (dt_s * mu_p) +
-                   glf_next(j) * (dt_s * mu_n) + P.at(Q_DMV, j, r) * lm +
-                   P.at(Q_DHV, j, r) * lh + P.at(Q_DNV, j, r) * ln;
-      P.at(Q_LM, j, r) = P.at(Q_DMM, j, r) * lm;
-      P.at(Q_LH, j, r) = P.at(Q_DHH, j, r) * lh;
-      P.at(Q_LN, j, r) = P.at(Q_DNN, j, r) * ln;
-      P.at(Q_LV, j, r) = lv;
     }
-    __syncwarp();  // every lane is done with this step's rows before the next load
-    const int tq = qv;
-    qv = qvn;
-    qvn = tq;
+    __syncwarp();  // every lane is done with vn and this stage
+    // v of this step is v_next of the step before it
+    for (int i = r; i < K; i += 32) vn[i] = sv[i];
+    __syncwarp();
+    bulk::fence_async_smem();  // this step's generic accesses before later copies
+    if (nstage == 1 && s >= 1)
+      tape_issue<T>(D.tape, N, off, K, s - 1, stg, cap, bars[0], r);
   }
   // the initial state's trace sample (recorded before the first step)
   if (rec_i >= 0 && A.step0 == 0 && r == rec_i / ch && D.trace_len > 0)
-    P.at(Q_LV, rec_i % ch, r) += D.trace_grad[(int64_t)cable * D.trace_len];
+    p0[(rec_i % ch) * rs + R_LV * 32] += D.trace_grad[(int64_t)cable * D.trace_len];
   __syncwarp();
-  for (int j = 0; j < ch; ++j) {
-    const int i = r * ch + j;
-    if (i < K) {
-      const int64_t g = off + i;
-      D.lam_v[g] = P.at(Q_LV, j, r);
-      D.lam_m[g] = P.at(Q_LM, j, r);
-      D.lam_h[g] = P.at(Q_LH, j, r);
-      D.lam_n[g] = P.at(Q_LN, j, r);
-      D.g_gna[g] = P.at(Q_GNA, j, r);
-      D.g_gk[g] = P.at(Q_GK, j, r);
-      D.g_gl[g] = P.at(Q_GL, j, r);
-      D.g_ax[g] = P.at(Q_GAX, j, r);
+  {
+    const T* pr = p0;
+    for (int j = 0; j < ch; ++j, pr += rs) {
+      const int i = row0 + j;
+      if (i < K) {
+        const int64_t g = off + i;
+        D.lam_v[g] = pr[R_LV * 32];
+        D.lam_m[g] = pr[R_LM * 32];
+        D.lam_h[g] = pr[R_LH * 32];
+        D.lam_n[g] = pr[R_LN * 32];
+        D.g_gna[g] = pr[R_GNA * 32];
+        D.g_gk[g] = pr[R_GK * 32];
+        D.g_gl[g] = pr[R_GL * 32];
+        D.g_ax[g] = pr[R_GAX * 32];
+      }
     }
   }
   __syncwarp();
+  return true;
 }
 
-template <typename T, bool FAST>
+template <typename T, bool FAST, bool PLANES>
 __global__ void __launch_bounds__(kCableMaxWarps * 32)
-    cable_adjoint_kernel(CableArgsT<T> A, AdjArgsT<T> D, int ch_max, PlaneLayout lay) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+    cable_adjoint_kernel(CableArgsT<T> A, AdjArgsT<T> D, int ch_max, int nstage) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars_all[kCableMaxWarps * 2];
   const int warp = threadIdx.x >> 5;
-  T* smw = reinterpret_cast<T*>(smem_raw) + (size_t)warp * lay.n_planes * ch_max * 32;
   const int lane = threadIdx.x & 31;
+  constexpr int NQ = AdjNQ<PLANES>::value;
+  const int64_t cap = tape_stage_cap<T>(ch_max);
+  T* wsm = reinterpret_cast<T*>(smem_raw +
+                                (size_t)warp * adjoint_warp_smem<T, PLANES>(ch_max, nstage));
+  T* stg = wsm + (size_t)NQ * ch_max * 32;
+  uint32_t bars[2] = {bulk::smem_addr(&bars_all[warp * 2]), bulk::smem_addr(&bars_all[warp * 2 + 1])};
+  if (lane == 0) {
+    bulk::bar_init(bars[0], 1);
+    bulk::bar_init(bars[1], 1);
+    bulk::bar_init_fence();
+  }
+  __syncwarp();
+  uint32_t par = 0;  // parity of the next phase of each stage's barrier
   for (;;) {
     int idx = 0;
     if (lane == 0) idx = atomicAdd(A.counter, 1);
@@ -437,23 +548,29 @@ __global__ void __launch_bounds__(kCableMaxWarps * 32)
       if (lane == 0) atomicOr(A.counter + 1, kErrChunk);
       continue;
     }
-    adjoint_cable<T, FAST>(A, D, cable, smw, ch, lay);
+    if (!adjoint_rows<T, FAST, PLANES>(A, D, cable, wsm, stg, cap, nstage, ch, bars, par)) break;
   }
 }
 
-template <typename T, bool FAST>
+template <typename T, bool FAST, bool PLANES>
 static int launch_adjoint(const CableArgsT<T>& A, const AdjArgsT<T>& D, int ch_max,
-                          const PlaneLayout& lay, cudaStream_t st) {
-  const size_t per_warp = (size_t)lay.n_planes * ch_max * 32 * sizeof(T);
-  const int wpb = persistent_wpb(A.wpb, per_warp);
+                          cudaStream_t st) {
+  // two tape stages (the next step's copy overlaps this step) when they fit,
+  // else one (the copy is waited for at once)
+  int nstage = 2;
+  int wpb = persistent_wpb(A.wpb, adjoint_warp_smem<T, PLANES>(ch_max, 2));
+  if (wpb == 0) {
+    nstage = 1;
+    wpb = persistent_wpb(A.wpb, adjoint_warp_smem<T, PLANES>(ch_max, 1));
+  }
   if (wpb == 0) {
     set_error("cable too long for the adjoint's shared memory (%zu bytes per cable, limit %d)",
-              per_warp, 227 * 1024);
+              adjoint_warp_smem<T, PLANES>(ch_max, 1), 227 * 1024);
     return DGB_ERANGE;
   }
   const int threads = wpb * 32;
-  const size_t smem = (size_t)wpb * per_warp;
-  auto kern = cable_adjoint_kernel<T, FAST>;
+  const size_t smem = (size_t)wpb * adjoint_warp_smem<T, PLANES>(ch_max, nstage);
+  auto kern = cable_adjoint_kernel<T, FAST, PLANES>;
   DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   int per_sm = 0;
@@ -464,7 +581,7 @@ static int launch_adjoint(const CableArgsT<T>& A, const AdjArgsT<T>& D, int ch_m
   if (blocks > blocks_needed) blocks = blocks_needed;
   if (blocks < 1) blocks = 1;
   DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, 2 * sizeof(int32_t), st));
-  kern<<<blocks, threads, smem, st>>>(A, D, ch_max, lay);
+  kern<<<blocks, threads, smem, st>>>(A, D, ch_max, nstage);
   DGB_LAUNCH_CHECK();
   return DGB_OK;
 }
@@ -485,14 +602,21 @@ int cable_adjoint_t(const dgb_cable_args* args, const dgb_cable_adjoint_args* ad
   D.g_gk = (T*)adj->grad_gkbar;
   D.g_gl = (T*)adj->grad_gl;
   D.g_ax = (T*)adj->grad_axial;
+  if ((reinterpret_cast<uintptr_t>(adj->tape) & 15u) != 0) {
+    set_error("the adjoint's tape must be 16-byte aligned");
+    return DGB_EINVAL;
+  }
   const bool field = args->field != nullptr && args->ve_amp != nullptr;
   const bool chan_planes = (args->flags & DGB_CABLE_UNIFORM_CHANNELS) == 0;
   const bool geo_planes = (args->flags & DGB_CABLE_UNIFORM_GEOMETRY) == 0;
-  const PlaneLayout lay = adjoint_layout(geo_planes, field, chan_planes);
+  const bool planes = field || chan_planes || geo_planes;
   if constexpr (sizeof(T) == 4) {
-    if (args->flags & DGB_CABLE_FAST_MATH) return launch_adjoint<T, true>(A, D, ch_max, lay, st);
+    if (args->flags & DGB_CABLE_FAST_MATH)
+      return planes ? launch_adjoint<T, true, true>(A, D, ch_max, st)
+                    : launch_adjoint<T, true, false>(A, D, ch_max, st);
   }
-  return launch_adjoint<T, false>(A, D, ch_max, lay, st);
+  return planes ? launch_adjoint<T, false, true>(A, D, ch_max, st)
+                : launch_adjoint<T, false, false>(A, D, ch_max, st);
 }
 
 #define DGB_INSTANTIATE_CABLE_ADJOINT(T)                                                \
