@@ -1747,6 +1747,48 @@ def bench_c5(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+# the other configurations, measured by the default run after config 2 (one
+# child process each, their own JSON lines summarised): workload, extra
+# arguments, time limit in seconds
+OTHER_CONFIGS = (("c1", [], 300), ("c3", [], 600), ("c4", [], 600), ("c5", [], 900),
+                 ("tridiag", [], 300))
+OTHER_KEYS = ("metric", "value", "unit", "ms_per_step", "higher_is_better", "dtype", "config",
+              "e2e", "clocks", "gpu_launches", "accuracy", "fp32_vs_fp64")
+
+
+def _other_configs():
+    """Run every other configuration's bench in a child process (one timed
+    step after 3 warm-up steps, no CPU baseline) and keep each line's
+    measurement, roofline and accuracy keys; a child that fails is recorded
+    with its error."""
+    out = {}
+    for wl, extra, limit in OTHER_CONFIGS:
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", wl, "--steps", "1",
+               "--warmup", "3", "--no-cpu", "--no-configs", *extra]
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=limit,
+                               env=dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0"))
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                tail = (r.stderr or r.stdout).strip().splitlines()[-1:] or [""]
+                out[wl] = {"error": f"exit {r.returncode}: {tail[0][:300]}"}
+                continue
+            d = json.loads(lines[-1])
+            rec = {k: d[k] for k in OTHER_KEYS if k in d}
+            if "roofline" in d:
+                rec["roofline"] = {k: d["roofline"].get(k) for k in
+                                   ("bound", "achieved", "peak", "unit", "frac", "kernel")}
+            for k in d:
+                if k.startswith("speedup") or k in ("threshold_rtol", "spikes_per_run"):
+                    rec[k] = d[k]
+            rec["wall_s"] = time.perf_counter() - t0
+            out[wl] = rec
+        except subprocess.TimeoutExpired:
+            out[wl] = {"error": f"no result within {limit} s"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1757,6 +1799,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="config 2: skip the child runs of the other configurations")
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
     ap.add_argument("--workload", default="c2",
@@ -2041,6 +2085,8 @@ def main():
         line["cpu_baseline"] = cpu
         line["cpu_port"] = port
         line["fp32_vs_fp64"] = _c2_accuracy(gpu_outs)
+    if rank == 0 and world == 1 and not args.no_configs:
+        line["other_configs"] = _other_configs()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if pg is not None:
