@@ -245,8 +245,11 @@ __device__ __forceinline__ void hh_gates_fast(float v, float q10, float dt, floa
 // ---------------------------------------------------------------------------
 // float32 fast-math gate advance for code in which all 32 lanes of a warp
 // call it together (the persistent cable kernel's row loop).  Same formulas
-// as hh_gates_fast with three changes, each tested to the same float64 bound:
-//   * exponentials by __expf (ex2.approx of x log2 e);
+// as hh_gates_fast with four changes, each tested to the same float64 bound:
+//   * exponentials by ex2.approx, with the rates' constant factors folded into
+//     the exponent, and reciprocals by rcp.approx;
+//   * the cnexp step written as x + k (alpha - s x) phi1(z), k = q10 dt,
+//     s = alpha + beta (fewer products per gate);
 //   * the branch of vtrap and of the cnexp step is chosen per warp by vote:
 //     a side no lane needs is not evaluated, and lanes on different sides
 //     both evaluate and select;
@@ -262,61 +265,76 @@ __device__ __forceinline__ float phi1_deg4(float z) {
   return value;
 }
 
+// 2^x and 1/x by the hardware approximations (ex2.approx, rcp.approx).
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ void hh_gates_fast_warp(float v, float q10, float dt, float& m,
                                                    float& h, float& n) {
   constexpr unsigned FULL = 0xffffffffu;
+  constexpr float L2E = 1.4426950408889634f;  // log2 e
   const float xm = -(v + 40.0f), xn = -(v + 55.0f);
-  const float qm = xm * 0.1f, qn = xn * 0.1f;
-  const float e10 = __expf(qm);                 // exp(-(v+40)/10)
-  const float e_n = e10 * 0.22313016014843f;    // exp(-(v+55)/10) = e10 * e^{-1.5}
-  const float e_h = e10 * 1.6487212707001282f;  // exp(-(v+35)/10) = e10 * e^{0.5}
   const float u = -(v + 65.0f);
-  const float e18 = __expf(u * (1.0f / 18.0f));
-  const float e80 = __expf(u * (1.0f / 80.0f));
-  const float e80_2 = e80 * e80;
-  const float e20 = e80_2 * e80_2;
+  // exp(-(v+40)/10); exp(-(v+55)/10) = e10 e^{-1.5} and exp(-(v+35)/10) =
+  // e10 e^{0.5} enter only through e - 1 and e + 1 (one FMA each)
+  const float e10 = ex2_approx(xm * (0.1f * L2E));
+  // the rates' constant factors ride in the exponent: beta_m = 4 exp(u/18),
+  // beta_n = exp(u/80) / 8, alpha_h = 0.07 exp(u/20)
+  const float beta_m = ex2_approx(fmaf(u, L2E / 18.0f, 2.0f));
+  const float beta_n = ex2_approx(fmaf(u, L2E / 80.0f, -3.0f));
+  const float alpha_h = ex2_approx(fmaf(u, L2E / 20.0f, -3.8365012677171206f));  // log2 0.07
+  const float beta_h = rcp_approx(fmaf(e10, 1.6487212707001282f, 1.0f));
   // vtrap(x, 10) = x / (exp(x/10) - 1), local series for |x/10| <= 1
-  const bool sm = fabsf(qm) <= 1.0f, sn = fabsf(qn) <= 1.0f;
-  float vm = __fdividef(xm, e10 - 1.0f), vn = __fdividef(xn, e_n - 1.0f);
+  const bool sm = fabsf(xm) <= 10.0f, sn = fabsf(xn) <= 10.0f;
+  float vm = xm * rcp_approx(e10 - 1.0f);
+  float vn = xn * rcp_approx(fmaf(e10, 0.22313016014843f, -1.0f));
   if (__any_sync(FULL, sm || sn)) {
+    const float qm = xm * 0.1f, qn = xn * 0.1f;
     const float tm = (10.0f - xm * 0.5f) + xm * (qm * Math<float>::even_series(qm));
     const float tn = (10.0f - xn * 0.5f) + xn * (qn * Math<float>::even_series(qn));
     vm = sm ? tm : vm;
     vn = sn ? tn : vn;
   }
-  const float alpha_m = 0.1f * vm;
-  const float beta_m = 4.0f * e18;
-  const float alpha_h = 0.07f * e20;
-  const float beta_h = __fdividef(1.0f, e_h + 1.0f);
-  const float alpha_n = 0.01f * vn;
-  const float beta_n = 0.125f * e80;
-  const float am = q10 * alpha_m, bm = q10 * (alpha_m + beta_m);
-  const float ah = q10 * alpha_h, bh = q10 * (alpha_h + beta_h);
-  const float an = q10 * alpha_n, bn = q10 * (alpha_n + beta_n);
-  const float zm = -bm * dt, zh = -bh * dt, zn = -bn * dt;
+  const float alpha_m = 0.1f * vm, alpha_n = 0.01f * vn;
+  // cnexp with a = q10 alpha, b = q10 (alpha + beta): z = -b dt, the step
+  // x + dt (a - b x) phi1(z) = x + k (alpha - s x) phi1(z) with k = q10 dt,
+  // s = alpha + beta (k is loop-invariant in the caller's row loop)
+  const float k = q10 * dt;
+  const float s_m = alpha_m + beta_m, s_h = alpha_h + beta_h, s_n = alpha_n + beta_n;
+  const float zm = -k * s_m, zh = -k * s_h, zn = -k * s_n;
   const float zmax = fmaxf(fabsf(zm), fmaxf(fabsf(zh), fabsf(zn)));
-  const float rm = am - bm * m, rh = ah - bh * h, rn = an - bn * n;
+  const float rm = k * fmaf(-s_m, m, alpha_m), rh = k * fmaf(-s_h, h, alpha_h),
+              rn = k * fmaf(-s_n, n, alpha_n);
   if (__all_sync(FULL, zmax <= 0.0625f)) {
-    m = m + dt * rm * phi1_deg4(zm);
-    h = h + dt * rh * phi1_deg4(zh);
-    n = n + dt * rn * phi1_deg4(zn);
+    m = fmaf(rm, phi1_deg4(zm), m);
+    h = fmaf(rh, phi1_deg4(zh), h);
+    n = fmaf(rn, phi1_deg4(zn), n);
     return;
   }
-  float mt = m + dt * rm * Math<float>::phi1(zm);
-  float ht = h + dt * rh * Math<float>::phi1(zh);
-  float nt = n + dt * rn * Math<float>::phi1(zn);
+  float mt = fmaf(rm, Math<float>::phi1(zm), m);
+  float ht = fmaf(rh, Math<float>::phi1(zh), h);
+  float nt = fmaf(rn, Math<float>::phi1(zn), n);
   if (__any_sync(FULL, zmax > 0.5f)) {
+    // exact relaxation: x_inf + (x - x_inf) e^z, x_inf = a / b = alpha / s
     if (fabsf(zm) > 0.5f) {
-      const float eq = __fdividef(am, bm);
-      mt = eq + (m - eq) * __expf(zm);
+      const float eq = alpha_m * rcp_approx(s_m);
+      mt = eq + (m - eq) * ex2_approx(zm * L2E);
     }
     if (fabsf(zh) > 0.5f) {
-      const float eq = __fdividef(ah, bh);
-      ht = eq + (h - eq) * __expf(zh);
+      const float eq = alpha_h * rcp_approx(s_h);
+      ht = eq + (h - eq) * ex2_approx(zh * L2E);
     }
     if (fabsf(zn) > 0.5f) {
-      const float eq = __fdividef(an, bn);
-      nt = eq + (n - eq) * __expf(zn);
+      const float eq = alpha_n * rcp_approx(s_n);
+      nt = eq + (n - eq) * ex2_approx(zn * L2E);
     }
   }
   m = mt;
