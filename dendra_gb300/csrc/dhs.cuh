@@ -121,23 +121,9 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
     for (int ch = c.level_ptr[l] + lane; ch < c1; ch += W) {
       const int p = c.chain_ptr[ch], e = c.chain_ptr[ch + 1];
       int i = c.nodes[p];
-      T D = sD[i], Bv = sB[i];
-      const int k1 = t.child_ptr[i + 1];
-      for (int k = t.child_ptr[i]; k < k1; ++k) {
-        const int cc = t.child_idx[k];
-        const T gc = g[cc];
-        const T Dc = sD[cc];
-        const T f = gc * solve_rcp<T, FAST>(Dc + gc);
-        D = D + f * Dc;
-        Bv = Bv + f * sB[cc];
-      }
-      sD[i] = D;
-      sB[i] = Bv;
-      // up the chain (the single child of node j is the node below it); the
-      // next node's values and the index after it are loaded ahead, before
-      // this node's division and stores, so neither load waits on the other
-      // (chains are disjoint: nothing else writes them)
-      T gc = g[i];
+      // the walk's first node j (the bottom's parent) and the index after it,
+      // with j's values, are loaded before the bottom's own work: the bottom
+      // writes only itself, so they do not wait on it (chains are disjoint)
       int q = p + 1;
       int j = q < e ? c.nodes[q] : 0;
       int jn = q + 1 < e ? c.nodes[q + 1] : 0;
@@ -147,6 +133,40 @@ __device__ __forceinline__ void chain_eliminate(const TreeTopoT<I>& t, const Cha
         bj = sB[j];
         gj = g[j];
       }
+      T gc = g[i];
+      T D = sD[i], Bv = sB[i];
+      const int k0 = t.child_ptr[i], k1 = t.child_ptr[i + 1];
+      // the bottom's children (the tops of lower chains): the first two are
+      // loaded together, so their divisions overlap; the sums keep the child
+      // order
+      if (k1 > k0) {
+        const bool two = k1 > k0 + 1;
+        const int ca = t.child_idx[k0];
+        const int cb = two ? t.child_idx[k0 + 1] : ca;
+        const T ga = g[ca], Da = sD[ca], Ba = sB[ca];
+        const T gb = g[cb], Db = sD[cb], Bb = sB[cb];
+        const T fa = ga * solve_rcp<T, FAST>(Da + ga);
+        const T fb = gb * solve_rcp<T, FAST>(Db + gb);
+        D = D + fa * Da;
+        Bv = Bv + fa * Ba;
+        if (two) {
+          D = D + fb * Db;
+          Bv = Bv + fb * Bb;
+        }
+        for (int k = k0 + 2; k < k1; ++k) {
+          const int cc = t.child_idx[k];
+          const T gc = g[cc];
+          const T Dc = sD[cc];
+          const T f = gc * solve_rcp<T, FAST>(Dc + gc);
+          D = D + f * Dc;
+          Bv = Bv + f * sB[cc];
+        }
+      }
+      sD[i] = D;
+      sB[i] = Bv;
+      // up the chain (the single child of node j is the node below it); the
+      // next node's values and the index after it are loaded ahead, before
+      // this node's division and stores, so neither load waits on the other
       for (; q < e; ++q) {
         const int jnn = q + 2 < e ? c.nodes[q + 2] : 0;
         T dn = T(0), bn = T(0), gn = T(0);
