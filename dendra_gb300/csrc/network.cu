@@ -178,17 +178,22 @@ __global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetAr
       const bool ve_on = Ive != T(0);
       // 1. deliver today's events (and clear the row)
       const bool bg = A.bg_bits && ((A.bg_bits[g * A.bg_words + (cell >> 6)] >> (cell & 63)) & 1ull);
+      // (with 3. the synapse decay, in the same pass: A = (A + w factor) decay_A;
+      // the spike detection between them reads only v)
       for (int k = lane; k < S; k += TPC) {
         T w = row[k];
         if (w != T(0)) {
           row[k] = T(0);
         }
         if (bg && k == A.bg_syn) w = w + A.bg_weight;
+        T sa = A.syn_A[s0 + k], sb = A.syn_B[s0 + k];
         if (w != T(0)) {
           const T inc = w * A.syn_factor[s0 + k];
-          A.syn_A[s0 + k] = A.syn_A[s0 + k] + inc;
-          A.syn_B[s0 + k] = A.syn_B[s0 + k] + inc;
+          sa = sa + inc;
+          sb = sb + inc;
         }
+        A.syn_A[s0 + k] = sa * A.syn_decay_A[s0 + k];
+        A.syn_B[s0 + k] = sb * A.syn_decay_B[s0 + k];
       }
       // 2. rising edge at the soma on the previous step's v
       if (lane == 0) {
@@ -199,25 +204,21 @@ __global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetAr
         }
         below = above ? 0 : 1;
       }
-      // 3. state advance: synapse decay, soma gates at v_old
-      for (int k = lane; k < S; k += TPC) {
-        A.syn_A[s0 + k] = A.syn_A[s0 + k] * A.syn_decay_A[s0 + k];
-        A.syn_B[s0 + k] = A.syn_B[s0 + k] * A.syn_decay_B[s0 + k];
-      }
+      // 3. state advance: soma gates at v_old (the synapse decay ran above)
       if (lane == 0) hh_gates<T>(sV[0], A.q10, A.dt, m, h, nn);
       cell_sync<T, TPC>(group);
-      // 4. assemble the tree system into sD (main) and sB (rhs)
-      for (int i = lane; i < K; i += TPC) {
+      // 4. assemble the tree system into sD (main) and sB (rhs); two nodes per
+      // pass, their global loads issued together
+      auto assemble = [&](int i, T gli, T eli, T ar, T cmi, int k0, int k1) {
         const T vi = sV[i];
         T G, J;
         if (i == 0) {
-          hh_affine<T>(m, h, nn, A.gnabar, A.gkbar, gl[0], el[0], A.ena, A.ek, G, J);
+          hh_affine<T>(m, h, nn, A.gnabar, A.gkbar, gli, eli, A.ena, A.ek, G, J);
         } else {
-          G = gl[i];
-          J = mul_rn(gl[i], el[i]);
+          G = gli;
+          J = mul_rn(gli, eli);
         }
-        const T ar = area[i];
-        for (int k = nsp[i]; k < nsp[i + 1]; ++k) {
+        for (int k = k0; k < k1; ++k) {
           // Exp2Syn: g = B - A (uS) -> density g / (1e6 area) (S/cm^2)
           const T gs = (A.syn_B[s0 + k] - A.syn_A[s0 + k]) / (T(1e6) * ar);
           G = G + gs;
@@ -243,7 +244,25 @@ __global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetAr
         }
         if (i == in_i) f = f + Iin;
         sB[i] = f;
-        sD[i] = cmdt[i] + mul_rn(G, ar);
+        sD[i] = cmi + mul_rn(G, ar);
+      };
+      for (int i0 = lane; i0 < K; i0 += 2 * TPC) {
+        const int i1 = i0 + TPC;
+        const bool two = i1 < K;
+        const T gl0 = gl[i0], el0 = el[i0], ar0 = area[i0], cm0 = cmdt[i0];
+        const int a0 = nsp[i0], b0 = nsp[i0 + 1];
+        T gl1 = T(0), el1 = T(0), ar1 = T(1), cm1 = T(0);
+        int a1 = 0, b1 = 0;
+        if (two) {
+          gl1 = gl[i1];
+          el1 = el[i1];
+          ar1 = area[i1];
+          cm1 = cmdt[i1];
+          a1 = nsp[i1];
+          b1 = nsp[i1 + 1];
+        }
+        assemble(i0, gl0, el0, ar0, cm0, a0, b0);
+        if (two) assemble(i1, gl1, el1, ar1, cm1, a1, b1);
       }
       cell_sync<T, TPC>(group);
       if (chains) {
