@@ -776,7 +776,7 @@ def bench_c3(args, world, rank, local):
                      "frac": achieved / peak, "traffic": None,
                      "note": f"{C3_BYTES_PER_COMP_STEP} algorithmic B per compartment-step of the "
                              f"unfused tree step; peak {peak_kind}"},
-        "gpu_launches": args.steps * windows * 2, "spikes_per_run": spikes,
+        "gpu_launches": args.steps * cap.launches, "spikes_per_run": spikes,
         "clocks": clocks.summary(),
     }
     if rank == 0 and not args.no_cpu:

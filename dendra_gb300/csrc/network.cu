@@ -19,6 +19,7 @@
 //      float division); v += dv.
 // dgb_net_enqueue then scatters the window's spikes into the delay ring,
 // one thread per target synapse, in connection then step order.
+#include <stdint.h>
 #include <type_traits>
 
 #include "dhs.cuh"
@@ -65,6 +66,9 @@ struct NetArgsT {
   uint8_t* below;
   unsigned long long* spike_bits;  // [n_cells] for this window
   int32_t* spike_count;
+  // subset of cells (nullptr: all n_cells)
+  const int32_t* cell_list;
+  int32_t n_list;
 };
 
 // Shared memory of one warp (one cell): values sV, sD, sB, sG (axial
@@ -112,9 +116,15 @@ __global__ void __launch_bounds__(TPC > 128 ? TPC : 128) net_window_kernel(NetAr
   uint16_t* sCidx = sCptr + kmax + 1;
   uint16_t* sLptr = sCidx + kmax;      // layer_ptr, or chain_ptr then chain levels
   const bool chains = A.chain_nodes != nullptr;
-  for (int cell = blockIdx.x * cpb + group; cell < A.n_cells; cell += gridDim.x * cpb) {
+  const int n_items = A.cell_list ? A.n_list : A.n_cells;
+  for (int item = blockIdx.x * cpb + group; item < n_items; item += gridDim.x * cpb) {
+    const int cell = A.cell_list ? A.cell_list[item] : item;
     const int64_t base = A.node_ptr[cell];
     const int K = (int)(A.node_ptr[cell + 1] - base);
+    if (K > kmax) {  // the list's size bound was wrong: flag the cell, never overrun
+      if (lane == 0) A.spike_count[cell] = INT32_MIN;
+      continue;
+    }
     const int plan = A.plan_of ? A.plan_of[cell] : cell;
     const int64_t pn = A.plan_node_ptr[plan], pl = A.plan_layer_off[plan];
     const int L = (int)(A.plan_layer_off[plan + 1] - pl - 1);
@@ -377,12 +387,15 @@ static NetArgsT<T> net_typed(const dgb_net_args* a) {
   t.below = a->below;
   t.spike_bits = (unsigned long long*)a->spike_bits;
   t.spike_count = a->spike_count;
+  t.cell_list = a->cell_list;
+  t.n_list = a->n_list;
   return t;
 }
 
 template <typename T>
 static int net_window_t(const dgb_net_args* a, cudaStream_t st) {
-  const int kmax = a->forest.max_k;
+  const int kmax = a->cell_list ? a->list_max_k : a->forest.max_k;
+  const int n_items = a->cell_list ? a->n_list : a->n_cells;
   if (kmax > 65534) {
     set_error("cells of more than 65,534 compartments are not supported (got %d)", kmax);
     return DGB_ERANGE;
@@ -413,7 +426,7 @@ static int net_window_t(const dgb_net_args* a, cudaStream_t st) {
   if (per_sm < 1) per_sm = 1;
   int blocks = device_sm_count() * per_sm;
   const int cpb = threads / tpc;
-  const int need = (a->n_cells + cpb - 1) / cpb;
+  const int need = (n_items + cpb - 1) / cpb;
   if (blocks > need) blocks = need;
   kern<<<blocks, threads, smem, st>>>(net_typed<T>(a), kmax);
   DGB_LAUNCH_CHECK();
@@ -443,6 +456,9 @@ extern "C" int dgb_net_window(const dgb_net_args* a, void* stream) {
               "synapse arrays and ring must be non-null");
   DGB_REQUIRE(a->below && a->spike_bits && a->spike_count, "spike outputs must be non-null");
   DGB_REQUIRE(a->forest.max_k >= 1, "cells must have at least one compartment");
+  DGB_REQUIRE(!a->cell_list || (a->n_list >= 0 && a->list_max_k >= 1),
+              "a cell list needs n_list >= 0 and list_max_k >= 1");
+  if (a->cell_list && a->n_list == 0) return DGB_OK;
   DGB_REQUIRE(!a->ve_field || (a->ve_amp && a->ve_delay && a->ve_pw),
               "ve_field requires ve_amp, ve_delay and ve_pw");
   DGB_REQUIRE(!a->in_node || (a->in_amp && a->in_delay && a->in_pw),

@@ -59,6 +59,7 @@ class NetArgs(ctypes.Structure):
         ("ve_field", ctypes.c_void_p), ("ve_amp", ctypes.c_void_p), ("ve_delay", ctypes.c_void_p),
         ("ve_pw", ctypes.c_void_p), ("in_node", ctypes.c_void_p), ("in_amp", ctypes.c_void_p),
         ("in_delay", ctypes.c_void_p), ("in_pw", ctypes.c_void_p), ("t0_ms", ctypes.c_double),
+        ("cell_list", ctypes.c_void_p), ("n_list", ctypes.c_int32), ("list_max_k", ctypes.c_int32),
     ]
 
 
@@ -129,7 +130,7 @@ class TreeNetwork:
                  dt=0.025, dtype=torch.float32, device="cuda", ra=100.0, cm=1.0, celsius=6.3,
                  v_init=-65.0, g_pas=0.001, e_pas=-70.0, tau1=0.5, tau2=5.0, e_syn=0.0,
                  spk_thr=0.0, bg_steps=None, bg_weight=0.0, window=None, chains=True,
-                 bg_netstim=None, extracellular=None, clamp=None):
+                 bg_netstim=None, extracellular=None, clamp=None, size_classes=False):
         self.dtype = dtype
         self.device = torch.device(device)
         self.dt = float(dt)
@@ -244,6 +245,19 @@ class TreeNetwork:
                               in_delay=per_cell(delay), in_pw=per_cell(pw))
         self._syn_ptr = syn_ptr
         self._node_syn_ptr = node_syn_ptr
+        # size classes (off by default): cells of at most half the largest
+        # cell's compartments are advanced by their own window launch, whose
+        # shared memory per cell is sized for them (about twice as many cells
+        # per SM); same results.  On config 3 the two launches run one after
+        # the other and each ends in a tail: 2.36e10 vs 2.44e10 in one launch.
+        self.classes = None
+        kk = np.diff(node_ptr)
+        half = int(kk.max()) // 2
+        small = np.nonzero(kk <= half)[0]
+        large = np.nonzero(kk > half)[0]
+        if size_classes and small.size and large.size:
+            self.classes = [(torch.as_tensor(ix, dtype=torch.int32, device=dev),
+                             int(kk[ix].max())) for ix in (large, small)]
         self._upload()
 
     @property
@@ -334,8 +348,12 @@ class TreeNetwork:
             a.slot0 = self.slot
             a.spike_bits = masks[w].data_ptr()
             with torch.cuda.device(self.device):
-                rc = L.dgb_net_window(ctypes.byref(a), st)
-                _lib.check(rc, "dgb_net_window")
+                for lst, kmax in self.classes or [(None, 0)]:
+                    a.cell_list = None if lst is None else lst.data_ptr()
+                    a.n_list = 0 if lst is None else lst.numel()
+                    a.list_max_k = kmax
+                    rc = L.dgb_net_window(ctypes.byref(a), st)
+                    _lib.check(rc, "dgb_net_window")
                 rc = L.dgb_net_enqueue(a.dtype, self.ring.data_ptr(), self.depth, self.n_syn,
                                        self.slot, d["csr_ptr"].data_ptr(), self.n_syn, None,
                                        d["csr_pre"].data_ptr(), d["csr_delay"].data_ptr(),
@@ -440,7 +458,7 @@ class CapturedRun:
         self.net, self.graph, self.start = net, graph, start
         self.n_steps, self.windows = n_steps, windows
         self.bg, self.masks = buffers
-        self.launches = 2 * len(windows)
+        self.launches = (1 + len(net.classes or [None])) * len(windows)
 
     def replay(self):
         """Run the captured steps; returns the spike raster like ``run``."""

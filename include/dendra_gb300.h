@@ -533,6 +533,16 @@ typedef struct dgb_net_args {
   const void* in_delay;
   const void* in_pw;
   double t0_ms;
+  /* optional subset of cells advanced by this launch (NULL: every cell):
+     cell_list[0 .. n_list) are cell indices; list_max_k must bound their
+     sizes (it sizes the shared memory per cell in place of forest.max_k).
+     Launching size classes separately (small cells with a small list_max_k,
+     more of them per SM) gives the same results as one launch.  A listed
+     cell larger than list_max_k is not advanced; its spike_count is set to
+     INT32_MIN. */
+  const int32_t* cell_list;
+  int32_t n_list;
+  int32_t list_max_k;
 } dgb_net_args;
 
 /* sizeof(dgb_net_args) as compiled (for foreign-language mirrors). */

@@ -134,3 +134,21 @@ def test_tree_step_drive_matches_oracle(cuda):
     pq = quiet.problem_dict(n_steps)
     oracle.net_run(pq, n_steps)
     assert np.abs(pq["v"] - pd["v"]).max() > 1.0
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_size_classes_give_identical_runs(cuda, dtype):
+    """Cells of at most half the largest size run in their own window launch
+    (smaller shared memory per cell, more cells per SM): the per-cell
+    arithmetic is unchanged, so the run is identical bit for bit."""
+    from dendra_gb300.network import random_network
+
+    out = []
+    for classes in (True, False):
+        net, n = random_network(24, k_range=(60, 900), syn_per_cell=12, seed=21, dtype=dtype,
+                                device=cuda, t_stop_ms=20.0, rate_hz=40.0,
+                                size_classes=classes)
+        assert (net.classes is not None) == classes
+        out.append((net.run(n), net.v.clone(), net.A.clone(), net.spike_count.clone()))
+    assert int(out[0][0].sum()) > 0
+    for a, b in zip(*out):
+        assert torch.equal(a, b)
