@@ -250,9 +250,9 @@ __device__ __forceinline__ void hh_gates_fast(float v, float q10, float dt, floa
 //     the exponent, and reciprocals by rcp.approx;
 //   * the cnexp step written as x + k (alpha - s x) phi1(z), k = q10 dt,
 //     s = alpha + beta (fewer products per gate);
-//   * the branch of vtrap and of the cnexp step is chosen per warp by vote:
-//     a side no lane needs is not evaluated, and lanes on different sides
-//     both evaluate and select;
+//   * vtrap evaluates both forms and selects per lane; the branch of the
+//     cnexp step is chosen per warp by vote (a side no lane needs is not
+//     evaluated, and lanes on different sides both evaluate and select);
 //   * when every lane's |z| = |b dt| <= 1/16, phi1 is its Taylor polynomial
 //     of degree 4 (truncation below 1.3e-9 relative, under float32
 //     rounding) instead of degree 9.
@@ -296,7 +296,9 @@ __device__ __forceinline__ void hh_gates_fast_warp(float v, float q10, float dt,
   const bool sm = fabsf(xm) <= 10.0f, sn = fabsf(xn) <= 10.0f;
   float vm = xm * rcp_approx(e10 - 1.0f);
   float vn = xn * rcp_approx(fmaf(e10, 0.22313016014843f, -1.0f));
-  if (__any_sync(FULL, sm || sn)) {
+  {
+    // both series always: near rest some lane nearly always needs one, and
+    // a warp vote with its branch measured costlier than the ten FMAs
     const float qm = xm * 0.1f, qn = xn * 0.1f;
     const float tm = (10.0f - xm * 0.5f) + xm * (qm * Math<float>::even_series(qm));
     const float tn = (10.0f - xn * 0.5f) + xn * (qn * Math<float>::even_series(qn));
