@@ -36,8 +36,8 @@ ALG_BYTES_PER_COMP_STEP = 48  # unfused per-step traffic of one float32 compartm
 # persistent config-2 kernel under ncu (4,096 cables x 100 steps, float32 fast
 # math): DRAM bytes per compartment per launch, thread instructions per
 # compartment-step (profiles/ holds the capture's summary)
-C2_NCU_DRAM_BYTES_PER_COMP = (22536960 + 256) / 932014
-C2_NCU_THREAD_INSTR_PER_COMP_STEP = 712875715 * 31.56 / 93201400
+C2_NCU_DRAM_BYTES_PER_COMP = 22536960 / 932014
+C2_NCU_THREAD_INSTR_PER_COMP_STEP = 691476115 * 31.55 / 93201400
 
 
 def _issue_bound(instr_per_unit, units, ms, clocks, dev):
