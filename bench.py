@@ -1750,15 +1750,16 @@ def bench_c5(args, world, rank, local):
 # the other configurations, measured by the default run after config 2 (one
 # child process each, their own JSON lines summarised): workload, extra
 # arguments, time limit in seconds
-OTHER_CONFIGS = (("c1", [], 300), ("c3", [], 600), ("c4", [], 600), ("c5", [], 900),
-                 ("tridiag", [], 300))
+OTHER_CONFIGS = (("c1", ["--steps", "3"], 300), ("c3", [], 600), ("c4", ["--steps", "2"], 600),
+                 ("c5", [], 900), ("tridiag", ["--steps", "20"], 300))
 OTHER_KEYS = ("metric", "value", "unit", "ms_per_step", "higher_is_better", "dtype", "config",
               "e2e", "clocks", "gpu_launches", "accuracy", "fp32_vs_fp64")
 
 
 def _other_configs():
-    """Run every other configuration's bench in a child process (one timed
-    step after 3 warm-up steps, no CPU baseline) and keep each line's
+    """Run every other configuration's bench in a child process (3 warm-up
+    steps, then one timed step, or more where a step is short; no CPU
+    baseline) and keep each line's
     measurement, roofline and accuracy keys; a child that fails is recorded
     with its error."""
     out = {}
