@@ -136,8 +136,10 @@ def tune_cable_run(pop, n_steps=50, candidates=CABLE_RUN_CANDIDATES, reps=3, for
         pop.step_index, pop.t = step, t
         pop.run(n_steps)
 
+    # the candidate set is part of the key: a restricted set (e.g. no lane
+    # splits) never inherits a pick from a wider one
     parts = (str(pop.dtype), pop.B, kmax, pop.N, pop.fast_math, "ve" if pop.field is not None
-             else "-")
+             else "-", ";".join(f"{w}/{a}/{b}" for w, a, b in candidates))
     try:
         best, timings = tune("cable_run_split", parts, candidates, run, pop.device, reps, force)
     finally:

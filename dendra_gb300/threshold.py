@@ -98,11 +98,17 @@ class Thresholder:
     (node indices of the myelinated fibre layout) or, for any other cables,
     ``compartments`` (local indices, negative counting from the far end, like
     the reference's ``Active(node_check=...)``).
+
+    tune: pick the trial runs' cables per CTA (1, 2 or 4, every cable on 32
+    lanes) by timing the candidates once per population shape
+    (``autotune.tune_cable_run``, cached per process and in
+    ``DGB_TUNE_CACHE``); the arithmetic, and so every threshold, is the same
+    for each of them.
     """
 
     def __init__(self, pop: CablePopulation, lb, ub, *, rtol=0.01, atol=None,
                  max_tries_bound_fix=10, max_tries_thresh=25, fix_bound_up=2.0,
-                 node_check=(5, -5), thr_mv=0.0, compartments=None):
+                 node_check=(5, -5), thr_mv=0.0, compartments=None, tune=True):
         if rtol is None and atol is None:
             raise ValueError("Either atol or rtol must be provided.")
         self.pop = pop
@@ -123,6 +129,10 @@ class Thresholder:
             self.spk = [torch.where(torch.as_tensor(c) < 0, kk + int(c),
                                     torch.full_like(kk, int(c))) for c in compartments]
         self.thr = thr_mv
+        if tune and pop.device.type == "cuda":
+            from .autotune import tune_cable_run
+
+            tune_cable_run(pop, n_steps=50, candidates=((1, 0, 0), (2, 0, 0), (4, 0, 0)))
         self.state0 = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
         self.trials = 0
         self.fibre_steps = 0
