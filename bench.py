@@ -571,6 +571,8 @@ def bench_c1(args, world, rank, local):
     dev = torch.device("cuda", local)
     dendra_gb300.load()
     pop = cable_population_c1(device=dev)
+    if args.launch:
+        pop.warps_per_block = int(args.launch.split(",")[0])
     state0 = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
 
     def reset():
@@ -648,9 +650,10 @@ def bench_c1(args, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
                      "note": (f"{2 * ALG_BYTES_PER_COMP_STEP} algorithmic B per float64 "
-                              "compartment-step of the unfused update; 64 cables occupy 64 "
-                              f"warps of the GPU: latency bound, not HBM bound ({peak_kind} "
-                              "copy bandwidth)")},
+                              "compartment-step of the unfused update; 64 cables on 64 CTAs "
+                              "of 4 warps (gates split over the SM sub-partitions): bound by "
+                              "the FP64 rate of 64 SMs, not by HBM "
+                              f"({peak_kind} copy bandwidth)")},
         "e2e": {"value": units / (e2e_ms * 1e-3), "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
         "gpu_launches": 2 * args.steps,
@@ -1822,7 +1825,8 @@ def main():
                     help="timesteps of each reference CPU sample (reference arm)")
     ap.add_argument("--ref-child", default="", help=argparse.SUPPRESS)
     ap.add_argument("--launch", default="",
-                    help="c2: fixed 'wpb,k16,k8' instead of autotuning (profiling runs)")
+                    help="c2: fixed 'wpb,k16,k8' instead of autotuning (profiling runs); "
+                         "c1: the first field fixes the cables per CTA")
     args = ap.parse_args()
     if args.ref_child:
         return _ref_child(args.ref_child, args.ref_steps, args.steps, args.warmup)

@@ -23,6 +23,7 @@ CABLE_UNIFORM_CHANNELS = 1
 CABLE_UNIFORM_GEOMETRY = 2
 CABLE_FAST_MATH = 4
 CABLE_STOP_ON_SPIKE = 8
+CABLE_SPLIT_GATES = 16
 
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32

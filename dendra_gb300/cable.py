@@ -184,6 +184,12 @@ class CablePopulation:
         # exceed max(8, those of the longest cable on 32)).  tune_cable_run
         # picks it.
         self.lanes_split = None
+        # True: one cable per CTA of 4 warps, the gate advance of its rows
+        # spread over the SM's four sub-partitions (the same operations:
+        # float32 results bit for bit, float64 up to last-bit contraction).
+        # With warps_per_block 0 and no lanes split the library also chooses
+        # it for a population of at most one cable per SM.
+        self.split_gates = False
         self.field = None
         self.ve = None
         self.intra = None
@@ -344,7 +350,8 @@ class CablePopulation:
         a.max_k = max(self.n_comp)
         a.flags = ((_lib.CABLE_UNIFORM_CHANNELS if self.uniform_channels else 0)
                    | (_lib.CABLE_UNIFORM_GEOMETRY if self.uniform_geometry else 0)
-                   | (_lib.CABLE_FAST_MATH if self.fast_math else 0))
+                   | (_lib.CABLE_FAST_MATH if self.fast_math else 0)
+                   | (_lib.CABLE_SPLIT_GATES if self.split_gates else 0))
         a.n_comp = self.N
         a.comp_cable = d["comp_cable"].data_ptr()
         a.scratch = d["scratch"].data_ptr()

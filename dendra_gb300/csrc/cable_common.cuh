@@ -8,6 +8,9 @@ namespace dgb {
 
 constexpr int kCableWarps = 4;     // default warps (cables in flight) per block
 constexpr int kCableMaxWarps = 4;  // largest accepted warps_per_block
+// warps of one cable in the split-gate run: one per SM sub-partition, each
+// with its own FP32/FP64 pipes
+constexpr int kSplitWarps = 4;
 
 template <typename T>
 struct CableArgsT {
@@ -36,6 +39,7 @@ struct CableArgsT {
   T* tape;         // (n_steps + 1, 4, n_comp) state tape, nullptr = none
   int64_t n_comp;  // total compartments (tape plane stride)
   int wpb;         // requested warps per block (0 = default)
+  int split;       // DGB_CABLE_SPLIT_GATES: one cable per CTA, gates on kSplitWarps warps
   int n_rast, rast_cap;
   const int32_t* rast_idx;
   int32_t *rast_below, *rast_count;
@@ -95,6 +99,7 @@ static CableArgsT<T> typed(const dgb_cable_args* a) {
   t.tape = nullptr;
   t.n_comp = a->n_comp;
   t.wpb = a->warps_per_block;
+  t.split = (a->flags & DGB_CABLE_SPLIT_GATES) ? 1 : 0;
   t.n_rast = a->rast_idx ? a->n_rast : 0;
   t.rast_cap = a->rast_cap;
   t.rast_idx = a->rast_idx;

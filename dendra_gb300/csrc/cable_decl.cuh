@@ -44,7 +44,8 @@ inline int validate_cable_args(const dgb_cable_args* a) {
               "spk_idx2 requires spk_idx and spk_below2");
   DGB_REQUIRE(a->rec_every >= 1, "rec_every must be >= 1");
   DGB_REQUIRE((a->flags & ~(DGB_CABLE_UNIFORM_CHANNELS | DGB_CABLE_UNIFORM_GEOMETRY |
-                             DGB_CABLE_FAST_MATH | DGB_CABLE_STOP_ON_SPIKE)) == 0,
+                             DGB_CABLE_FAST_MATH | DGB_CABLE_STOP_ON_SPIKE |
+                             DGB_CABLE_SPLIT_GATES)) == 0,
               "unknown flags %d", a->flags);
   DGB_REQUIRE(!(a->flags & DGB_CABLE_FAST_MATH) || a->dtype == DGB_F32,
               "DGB_CABLE_FAST_MATH applies to float32 state only");

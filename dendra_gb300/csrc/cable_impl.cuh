@@ -99,6 +99,32 @@ __global__ void __launch_bounds__(kCableMaxWarps * 32) cable_run_kernel(CableArg
   }
 }
 
+// Split-gate run (DGB_CABLE_SPLIT_GATES): one 32-lane cable per CTA of
+// kSplitWarps warps, the gate advance and assembly of its rows spread over
+// the warps (run_rows with GW = kSplitWarps).
+template <typename T, bool FAST, bool TAPE, bool PLANES>
+__global__ void __launch_bounds__(kSplitWarps * 32) cable_run_split_kernel(CableArgsT<T> A,
+                                                                           int ch_alloc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_item;
+  T* smw = reinterpret_cast<T*>(smem_raw);
+  for (;;) {
+    __syncthreads();  // every warp has read the previous item
+    if (threadIdx.x == 0) s_item = atomicAdd(A.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= A.n_cables) break;
+    const int c = A.order ? A.order[item] : item;
+    const int K = (int)(A.cable_ptr[c + 1] - A.cable_ptr[c]);
+    const int ch = (K + 31) / 32;
+    if (ch > ch_alloc) {  // flag, never skip silently
+      if (threadIdx.x == 0) atomicOr(A.counter + 1, kErrChunk);
+      continue;
+    }
+    if (ch > 0) run_rows<T, FAST, TAPE, PLANES, kSplitWarps>(A, item, A.n_cables, 32, ch, smw);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Plain per-step path.
 // ---------------------------------------------------------------------------
@@ -213,12 +239,48 @@ __global__ void __launch_bounds__(128) cable_solve_update_kernel(CableArgsT<T> A
 }
 
 template <typename T, bool FAST, bool TAPE, bool PLANES>
+static int launch_cable_split(CableArgsT<T> A, int ch_max, cudaStream_t st) {
+  DGB_REQUIRE(A.lanes_mode == 0, "DGB_CABLE_SPLIT_GATES needs lanes_mode 0");
+  const size_t smem = (size_t)(RowsNQ<PLANES>::value + 1) * ch_max * 32 * sizeof(T);
+  DGB_REQUIRE(smem <= 227 * 1024, "cable too long for shared memory (%zu bytes per cable)",
+              smem);
+  const int threads = kSplitWarps * 32;
+  auto kern = cable_run_split_kernel<T, FAST, TAPE, PLANES>;
+  DGB_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  int per_sm = 0;
+  DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+  if (per_sm < 1) per_sm = 1;
+  int blocks = device_sm_count() * per_sm;
+  if (blocks > A.n_cables) blocks = A.n_cables;
+  if (blocks < 1) blocks = 1;
+  DGB_CUDA_CHECK(cudaMemsetAsync(A.counter, 0, 2 * sizeof(int32_t), st));
+  kern<<<blocks, threads, smem, st>>>(A, ch_max);
+  DGB_LAUNCH_CHECK();
+  return DGB_OK;
+}
+
+template <typename T, bool FAST, bool TAPE, bool PLANES>
 static int launch_cable_run(CableArgsT<T> A, int ch_max, cudaStream_t st) {
+  // a population with at most one cable per SM: spread each cable's gate
+  // work over the SM's sub-partitions
+  if (A.split || (A.wpb <= 0 && A.lanes_mode == 0 && A.n_cables <= device_sm_count()))
+    return launch_cable_split<T, FAST, TAPE, PLANES>(A, ch_max, st);
   // rows per lane: ch_max at 32 lanes, up to 8 on 16 or 8 lanes when split
   const int ch_alloc = (A.lanes_mode != 0 && ch_max < 8) ? 8 : ch_max;
   const size_t per_warp = (size_t)RowsNQ<PLANES>::value * ch_alloc * 32 * sizeof(T);
-  const int wpb = persistent_wpb(A.wpb, per_warp);
+  int items = A.n_cables;
+  if (A.lanes_mode != 0) {
+    const int n8 = A.n_cables - A.n_lanes32 - A.n_lanes16;
+    items = A.n_lanes32 + (A.n_lanes16 + 1) / 2 + (n8 + 3) / 4;
+  }
+  int wpb = persistent_wpb(A.wpb, per_warp);
   DGB_REQUIRE(wpb > 0, "cable too long for shared memory (%zu bytes per cable)", per_warp);
+  if (A.wpb <= 0) {
+    // default shape: a population with fewer warps of work than the device
+    // has SMs x default CTA width spreads over the SMs, one CTA each
+    while (wpb > 1 && (items + wpb - 1) / wpb < device_sm_count()) wpb >>= 1;
+  }
   const int threads = wpb * 32;
   const size_t smem = (size_t)wpb * per_warp;
   auto kern = cable_run_kernel<T, FAST, TAPE, PLANES>;
@@ -228,11 +290,6 @@ static int launch_cable_run(CableArgsT<T> A, int ch_max, cudaStream_t st) {
   DGB_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
   if (per_sm < 1) per_sm = 1;
   int blocks = device_sm_count() * per_sm;
-  int items = A.n_cables;
-  if (A.lanes_mode != 0) {
-    const int n8 = A.n_cables - A.n_lanes32 - A.n_lanes16;
-    items = A.n_lanes32 + (A.n_lanes16 + 1) / 2 + (n8 + 3) / 4;
-  }
   const int blocks_needed = (items + wpb - 1) / wpb;
   if (blocks > blocks_needed) blocks = blocks_needed;
   if (blocks < 1) blocks = 1;

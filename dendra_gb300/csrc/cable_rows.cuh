@@ -19,6 +19,8 @@
 //   plane  7      extracellular axial term (constant while a pulse is on)
 //   planes 8..10  g_right, g_left, scale   (only when geometry varies)
 //   planes 11..14 gnabar, gkbar, gl, el    (only when channels vary)
+//   one more plane after those with split gates: the assembled diagonal b
+//   (a, c, d go to planes 4..6, which the forward sweep then overwrites)
 // Rows past a cable's end (i >= K, padding of the last lanes) run the same
 // update with the cable's own membrane and axial coefficients but no
 // extracellular or clamp drive: the last real row has exactly zero coupling to
@@ -103,12 +105,21 @@ __device__ __forceinline__ void pulse_steps(const CableArgsT<T>& A, T amp, T del
   if (s1 < s0) s1 = s0;
 }
 
-template <typename T, bool FAST, bool TAPE, bool PLANES>
+// GW > 1 (split gates): the CTA's GW warps share one 32-lane cable.  Warp w
+// advances the gates and assembles rows j = w, w + GW, ... of every lane into
+// planes a -> Q_AP, b -> Q_B, c -> Q_CP, d / dt_s -> Q_DP; after a CTA barrier warp 0
+// runs the forward sweep over those rows (the same operations, in the same
+// order, as the fused sweep) and the rest of the step alone.  Warp 0 also does
+// every global load and store of the cable.
+template <typename T, bool FAST, bool TAPE, bool PLANES, int GW = 1>
 __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int pos_end, int P,
                                          int ch, T* wsm) {
   constexpr unsigned FULL = 0xffffffffu;
-  constexpr int NQ = RowsNQ<PLANES>::value;
+  constexpr int NQ = RowsNQ<PLANES>::value + (GW > 1 ? 1 : 0);
+  constexpr int Q_B = RowsNQ<PLANES>::value;  // split gates: the assembled diagonal
   constexpr int rs = NQ * 32;  // elements from one row to the next
+  const int gw = GW > 1 ? (int)(threadIdx.x >> 5) : 0;
+  const bool solver = gw == 0;
   const int lane = threadIdx.x & 31;
   const int grp = lane / P;
   const int r = lane - grp * P;
@@ -122,20 +133,22 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
   const bool use_ve = A.field != nullptr && A.ve_amp != nullptr;
 
   // ---- load state and coefficients (rows past K start at zero)
-  rows_load<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
-  rows_load<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);
-  rows_load<T>(wsm, NQ, Q_H, ch, lane0, P, r, A.h + off, K);
-  rows_load<T>(wsm, NQ, Q_N, ch, lane0, P, r, A.n + off, K);
-  if constexpr (PLANES) {
-    rows_load<T>(wsm, NQ, Q_GR, ch, lane0, P, r, A.g_right + off, K);
-    rows_load<T>(wsm, NQ, Q_GL, ch, lane0, P, r, A.g_left + off, K);
-    rows_load<T>(wsm, NQ, Q_SC, ch, lane0, P, r, A.scale + off, K);
-    rows_load<T>(wsm, NQ, Q_GNA, ch, lane0, P, r, A.gnabar + off, K);
-    rows_load<T>(wsm, NQ, Q_GK, ch, lane0, P, r, A.gkbar + off, K);
-    rows_load<T>(wsm, NQ, Q_GLK, ch, lane0, P, r, A.gl + off, K);
-    rows_load<T>(wsm, NQ, Q_EL, ch, lane0, P, r, A.el + off, K);
+  if (solver) {
+    rows_load<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
+    rows_load<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);
+    rows_load<T>(wsm, NQ, Q_H, ch, lane0, P, r, A.h + off, K);
+    rows_load<T>(wsm, NQ, Q_N, ch, lane0, P, r, A.n + off, K);
+    if constexpr (PLANES) {
+      rows_load<T>(wsm, NQ, Q_GR, ch, lane0, P, r, A.g_right + off, K);
+      rows_load<T>(wsm, NQ, Q_GL, ch, lane0, P, r, A.g_left + off, K);
+      rows_load<T>(wsm, NQ, Q_SC, ch, lane0, P, r, A.scale + off, K);
+      rows_load<T>(wsm, NQ, Q_GNA, ch, lane0, P, r, A.gnabar + off, K);
+      rows_load<T>(wsm, NQ, Q_GK, ch, lane0, P, r, A.gkbar + off, K);
+      rows_load<T>(wsm, NQ, Q_GLK, ch, lane0, P, r, A.gl + off, K);
+      rows_load<T>(wsm, NQ, Q_EL, ch, lane0, P, r, A.el + off, K);
+    }
+    if (use_ve) rows_load<T>(wsm, NQ, Q_VAX, ch, lane0, P, r, A.field + off, K);
   }
-  if (use_ve) rows_load<T>(wsm, NQ, Q_VAX, ch, lane0, P, r, A.field + off, K);
   __syncwarp();
   // uniform coefficients: the cable's values, identical on every compartment
   // (interior edges for g_right / g_left), so reading them once is exact
@@ -170,12 +183,12 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
   // once with the rounded operations of the per-step form (the field rows are
   // replaced by the term in place, after every lane has read its neighbours)
   T ve_amp = T(0), ve_delay = T(0), ve_pw = T(0);
-  if (use_ve) {
-    if (K > 0) {
-      ve_amp = A.ve_amp[cable];
-      ve_delay = A.ve_delay[cable];
-      ve_pw = A.ve_pw[cable];
-    }
+  if (use_ve && K > 0) {
+    ve_amp = A.ve_amp[cable];
+    ve_delay = A.ve_delay[cable];
+    ve_pw = A.ve_pw[cable];
+  }
+  if (use_ve && solver) {
     T f_prev = r > 0 ? wsm[((ch - 1) * NQ + Q_VAX) * 32 + lane - 1] : T(0);
     T f_hi = r < P - 1 ? wsm[Q_VAX * 32 + lane + 1] : T(0);
     T fj = p0[Q_VAX * 32];
@@ -235,10 +248,10 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
       r_count = A.rast_count[(int64_t)cable * A.n_rast + r];
     }
   }
-  if (rec_i >= 0 && r == 0) A.trace[(int64_t)cable * A.n_rec] = wsm[rec_o];
-  if (A.trace_all) rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.trace_all + off, K);
+  if (solver && rec_i >= 0 && r == 0) A.trace[(int64_t)cable * A.n_rec] = wsm[rec_o];
+  if (solver && A.trace_all) rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.trace_all + off, K);
   if constexpr (TAPE) {
-    if (A.tape) {
+    if (solver && A.tape) {
       T* tp = A.tape + off;
       rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, tp, K);
       rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, tp + A.n_comp, K);
@@ -247,6 +260,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
     }
   }
   __syncwarp();  // the first step rewrites rows other lanes just stored
+  if constexpr (GW > 1) __syncthreads();  // the planes are loaded for every warp
 
   bool live = K > 0;  // this group's cable is still advancing
   int rec_left = A.rec_every, rec_k = 0;  // steps to the next record, records so far
@@ -294,7 +308,14 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
         b = T(1) - dt_s * ((-gr + -glf) - mul_rn(G, scl));
         a = -dt_s * glf;
         c = -dt_s * gr;
-        d = dt_s * fn;
+        // split gates: fn itself, scaled where the sweep uses it, so that the
+        // product dt_s * fn contracts with the sweep's operations exactly as
+        // in the fused sweep
+        if constexpr (GW > 1) {
+          d = fn;
+        } else {
+          d = dt_s * fn;
+        }
       };
       auto sweep = [&](auto ve_tag) {
         T* pr = p0;
@@ -319,155 +340,209 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
           vj = v_next;
         }
       };
-      if (ve_on) {
-        sweep(BoolTag<true>{});
+      if constexpr (GW == 1) {
+        if (ve_on) {
+          sweep(BoolTag<true>{});
+        } else {
+          sweep(BoolTag<false>{});
+        }
       } else {
-        sweep(BoolTag<false>{});
-      }
-    }
-    // ---- backward sweep (rows ch-3 .. 1) and the lane's reduced row
-    T al, be, ga, de;
-    const T Ae = ap, Ce = cp, De = dp;  // row ch-1 (forward form)
-    if (ch == 1) {
-      al = As;
-      be = Bs;
-      ga = Cs;
-      de = Ds;
-    } else {
-      T a2 = ap, c2 = cp, d2 = dp;  // row 1 once the loop below has run
-      if (ch >= 3) {
-        T* q = p0 + (ch - 2) * rs;
-        a2 = q[Q_AP * 32];
-        c2 = q[Q_CP * 32];
-        d2 = q[Q_DP * 32];
-        for (int j = ch - 3; j >= 1; --j) {
-          q -= rs;
-          const T cj = q[Q_CP * 32];
-          d2 = q[Q_DP * 32] - cj * d2;
-          a2 = q[Q_AP * 32] - cj * a2;
-          c2 = -cj * c2;
-          q[Q_AP * 32] = a2;
-          q[Q_CP * 32] = c2;
-          q[Q_DP * 32] = d2;
+        auto rows = [&](auto ve_tag) {
+          for (int j = gw; j < ch; j += GW) {
+            T* pr = p0 + j * rs;
+            const T vj = pr[Q_V * 32];
+            const T v_prev = j > 0 ? pr[Q_V * 32 - rs] : v_lo;
+            const T v_next = j < ch - 1 ? pr[rs + Q_V * 32] : v_hi;
+            T a, b, c, d;
+            assemble(pr, j, v_prev, vj, v_next, ve_tag, a, b, c, d);
+            pr[Q_AP * 32] = a;
+            pr[Q_B * 32] = b;
+            pr[Q_CP * 32] = c;
+            pr[Q_DP * 32] = d;
+          }
+        };
+        if (ve_on) {
+          rows(BoolTag<true>{});
+        } else {
+          rows(BoolTag<false>{});
+        }
+        __syncthreads();  // every row assembled
+        if (solver) {
+          T* pr = p0;
+          As = pr[Q_AP * 32];
+          Bs = pr[Q_B * 32];
+          Cs = pr[Q_CP * 32];
+          Ds = dt_s * pr[Q_DP * 32];
+          for (int j = 1; j < ch; ++j) {
+            pr += rs;
+            const T a = pr[Q_AP * 32], b = pr[Q_B * 32], c = pr[Q_CP * 32];
+            const T d = dt_s * pr[Q_DP * 32];
+            const T rinv = dv<T, FAST>(T(1), b - a * cp);
+            ap = -a * ap * rinv;
+            dp = (d - a * dp) * rinv;
+            cp = c * rinv;
+            pr[Q_AP * 32] = ap;
+            pr[Q_CP * 32] = cp;
+            pr[Q_DP * 32] = dp;
+          }
         }
       }
-      T Bs2 = Bs, Cs2 = Cs, Ds2 = Ds;
-      if (ch >= 3) {
-        Bs2 = Bs - Cs * a2;
-        Cs2 = -Cs * c2;
-        Ds2 = Ds - Cs * d2;
+    }
+    bool done = false;  // stop on spike: no cable of the warp advances further
+    if (solver) {
+      // ---- backward sweep (rows ch-3 .. 1) and the lane's reduced row
+      T al, be, ga, de;
+      const T Ae = ap, Ce = cp, De = dp;  // row ch-1 (forward form)
+      if (ch == 1) {
+        al = As;
+        be = Bs;
+        ga = Cs;
+        de = Ds;
+      } else {
+        T a2 = ap, c2 = cp, d2 = dp;  // row 1 once the loop below has run
+        if (ch >= 3) {
+          T* q = p0 + (ch - 2) * rs;
+          a2 = q[Q_AP * 32];
+          c2 = q[Q_CP * 32];
+          d2 = q[Q_DP * 32];
+          for (int j = ch - 3; j >= 1; --j) {
+            q -= rs;
+            const T cj = q[Q_CP * 32];
+            d2 = q[Q_DP * 32] - cj * d2;
+            a2 = q[Q_AP * 32] - cj * a2;
+            c2 = -cj * c2;
+            q[Q_AP * 32] = a2;
+            q[Q_CP * 32] = c2;
+            q[Q_DP * 32] = d2;
+          }
+        }
+        T Bs2 = Bs, Cs2 = Cs, Ds2 = Ds;
+        if (ch >= 3) {
+          Bs2 = Bs - Cs * a2;
+          Cs2 = -Cs * c2;
+          Ds2 = Ds - Cs * d2;
+        }
+        T Ae_l = shfl_up<T>(Ae, 1, P), Ce_l = shfl_up<T>(Ce, 1, P), De_l = shfl_up<T>(De, 1, P);
+        if (r == 0) {
+          Ae_l = T(0);
+          Ce_l = T(0);
+          De_l = T(0);
+        }
+        al = -As * Ae_l;
+        be = Bs2 - As * Ce_l - Cs2 * Ae;
+        ga = -Cs2 * Ce;
+        de = Ds2 - As * De_l - Cs2 * De;
       }
-      T Ae_l = shfl_up<T>(Ae, 1, P), Ce_l = shfl_up<T>(Ce, 1, P), De_l = shfl_up<T>(De, 1, P);
-      if (r == 0) {
-        Ae_l = T(0);
-        Ce_l = T(0);
-        De_l = T(0);
+      // ---- PCR across the P lanes, then back substitution
+  #pragma unroll
+      for (int sh = 1; sh < 32; sh <<= 1) {
+        if (sh >= P) break;
+        T al_l = shfl_up<T>(al, sh, P), be_l = shfl_up<T>(be, sh, P);
+        T ga_l = shfl_up<T>(ga, sh, P), de_l = shfl_up<T>(de, sh, P);
+        T al_r = shfl_down<T>(al, sh, P), be_r = shfl_down<T>(be, sh, P);
+        T ga_r = shfl_down<T>(ga, sh, P), de_r = shfl_down<T>(de, sh, P);
+        const bool hl = r >= sh;
+        const bool hr = r + sh < P;
+        T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
+        T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
+        T al_n = hl ? -k1 * al_l : T(0);
+        T ga_n = hr ? -k2 * ga_r : T(0);
+        be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
+        de = de - (hl ? k1 * de_l : T(0)) - (hr ? k2 * de_r : T(0));
+        al = al_n;
+        ga = ga_n;
       }
-      al = -As * Ae_l;
-      be = Bs2 - As * Ce_l - Cs2 * Ae;
-      ga = -Cs2 * Ce;
-      de = Ds2 - As * De_l - Cs2 * De;
-    }
-    // ---- PCR across the P lanes, then back substitution
-#pragma unroll
-    for (int sh = 1; sh < 32; sh <<= 1) {
-      if (sh >= P) break;
-      T al_l = shfl_up<T>(al, sh, P), be_l = shfl_up<T>(be, sh, P);
-      T ga_l = shfl_up<T>(ga, sh, P), de_l = shfl_up<T>(de, sh, P);
-      T al_r = shfl_down<T>(al, sh, P), be_r = shfl_down<T>(be, sh, P);
-      T ga_r = shfl_down<T>(ga, sh, P), de_r = shfl_down<T>(de, sh, P);
-      const bool hl = r >= sh;
-      const bool hr = r + sh < P;
-      T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
-      T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
-      T al_n = hl ? -k1 * al_l : T(0);
-      T ga_n = hr ? -k2 * ga_r : T(0);
-      be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
-      de = de - (hl ? k1 * de_l : T(0)) - (hr ? k2 * de_r : T(0));
-      al = al_n;
-      ga = ga_n;
-    }
-    const T xs = dv<T, FAST>(de, be);
-    T xe = xs;
-    if (ch > 1) {
-      T xs_next = shfl_down<T>(xs, 1, P);
-      if (r == P - 1) xs_next = T(0);
-      xe = De - Ae * xs - Ce * xs_next;
-    }
-    __syncwarp();  // every lane has read its neighbours' v for this step
-    p0[Q_V * 32] = p0[Q_V * 32] + xs;
-    {
-      T* q = p0;
-      for (int j = 1; j < ch - 1; ++j) {
-        q += rs;
-        q[Q_V * 32] = q[Q_V * 32] + (q[Q_DP * 32] - q[Q_AP * 32] * xs - q[Q_CP * 32] * xe);
+      const T xs = dv<T, FAST>(de, be);
+      T xe = xs;
+      if (ch > 1) {
+        T xs_next = shfl_down<T>(xs, 1, P);
+        if (r == P - 1) xs_next = T(0);
+        xe = De - Ae * xs - Ce * xs_next;
       }
-    }
-    if (ch > 1) p0[(ch - 1) * rs + Q_V * 32] = p0[(ch - 1) * rs + Q_V * 32] + xe;
-    __syncwarp();  // new v visible to every lane of the group
+      __syncwarp();  // every lane has read its neighbours' v for this step
+      p0[Q_V * 32] = p0[Q_V * 32] + xs;
+      {
+        T* q = p0;
+        for (int j = 1; j < ch - 1; ++j) {
+          q += rs;
+          q[Q_V * 32] = q[Q_V * 32] + (q[Q_DP * 32] - q[Q_AP * 32] * xs - q[Q_CP * 32] * xe);
+        }
+      }
+      if (ch > 1) p0[(ch - 1) * rs + Q_V * 32] = p0[(ch - 1) * rs + Q_V * 32] + xe;
+      __syncwarp();  // new v visible to every lane of the group
 
-    // ---- detection (group lane 0), raster (group lanes < n_rast), recording
-    bool stop_now = false;
-    if (A.spk_idx) {
-      int edge = 0;
-      if (live && spk_i >= 0 && r == 0) {
-        const int above = wsm[spk_o] >= A.spk_thr;
-        edge = above && below;
-        below = !above;
-        if (spk_i2 >= 0) {
-          const int above2 = wsm[spk_o2] >= A.spk_thr;
-          edge = edge || (above2 && below2);
-          below2 = !above2;
+      // ---- detection (group lane 0), raster (group lanes < n_rast), recording
+      bool stop_now = false;
+      if (A.spk_idx) {
+        int edge = 0;
+        if (live && spk_i >= 0 && r == 0) {
+          const int above = wsm[spk_o] >= A.spk_thr;
+          edge = above && below;
+          below = !above;
+          if (spk_i2 >= 0) {
+            const int above2 = wsm[spk_o2] >= A.spk_thr;
+            edge = edge || (above2 && below2);
+            below2 = !above2;
+          }
+          if (edge) {
+            if (count == 0) first = s + 1;
+            count += 1;
+          }
         }
-        if (edge) {
-          if (count == 0) first = s + 1;
-          count += 1;
+        stop_now = A.stop_on_spike && __shfl_sync(FULL, edge, lane0) && live;
+      }
+      if (live && r_idx >= 0) {
+        const int above = wsm[r_o] >= A.spk_thr;
+        if (above && r_latch) {
+          if (r_count < A.rast_cap)
+            A.rast_steps[((int64_t)cable * A.n_rast + r) * A.rast_cap + r_count] = A.step0 + s + 1;
+          r_count += 1;
+        }
+        r_latch = !above;
+      }
+      // record every rec_every steps (a countdown: no division per step)
+      const bool rec_due = --rec_left == 0;
+      if (rec_due) {
+        rec_left = A.rec_every;
+        ++rec_k;
+        if (live && rec_i >= 0 && r == 0) A.trace[(int64_t)cable * A.n_rec + rec_k] = wsm[rec_o];
+        if (A.trace_all)
+          rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.trace_all + (int64_t)rec_k * A.n_comp + off,
+                        live ? K : 0);
+      }
+      if constexpr (TAPE) {
+        if (A.tape) {
+          T* tp = A.tape + (int64_t)(s + 1) * 4 * A.n_comp + off;
+          rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, tp, K);
+          rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, tp + A.n_comp, K);
+          rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, tp + 2 * A.n_comp, K);
+          rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, tp + 3 * A.n_comp, K);
         }
       }
-      stop_now = A.stop_on_spike && __shfl_sync(FULL, edge, lane0) && live;
-    }
-    if (live && r_idx >= 0) {
-      const int above = wsm[r_o] >= A.spk_thr;
-      if (above && r_latch) {
-        if (r_count < A.rast_cap)
-          A.rast_steps[((int64_t)cable * A.n_rast + r) * A.rast_cap + r_count] = A.step0 + s + 1;
-        r_count += 1;
+      if (A.stop_on_spike) {
+        // a cable that fired stops here: its state is written now and frozen
+        if (stop_now) {
+          rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
+          rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);
+          rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, A.h + off, K);
+          rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, A.n + off, K);
+          live = false;
+        }
+        done = !__any_sync(FULL, live);
       }
-      r_latch = !above;
+    }  // solver
+    if constexpr (GW == 1) {
+      if (done) break;
+      __syncwarp();  // the next step rewrites rows other lanes just read
+    } else {
+      __shared__ int s_done;
+      if (threadIdx.x == 0) s_done = done;
+      __syncthreads();  // the new v is visible to every warp
+      if (s_done) break;
     }
-    // record every rec_every steps (a countdown: no division per step)
-    const bool rec_due = --rec_left == 0;
-    if (rec_due) {
-      rec_left = A.rec_every;
-      ++rec_k;
-      if (live && rec_i >= 0 && r == 0) A.trace[(int64_t)cable * A.n_rec + rec_k] = wsm[rec_o];
-      if (A.trace_all)
-        rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.trace_all + (int64_t)rec_k * A.n_comp + off,
-                      live ? K : 0);
-    }
-    if constexpr (TAPE) {
-      if (A.tape) {
-        T* tp = A.tape + (int64_t)(s + 1) * 4 * A.n_comp + off;
-        rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, tp, K);
-        rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, tp + A.n_comp, K);
-        rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, tp + 2 * A.n_comp, K);
-        rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, tp + 3 * A.n_comp, K);
-      }
-    }
-    if (A.stop_on_spike) {
-      // a cable that fired stops here: its state is written now and frozen
-      if (stop_now) {
-        rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
-        rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);
-        rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, A.h + off, K);
-        rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, A.n + off, K);
-        live = false;
-      }
-      if (!__any_sync(FULL, live)) break;
-    }
-    __syncwarp();  // the next step rewrites rows other lanes just read
   }
   // ---- write back the state of cables still advancing, and the counters
+  if (!solver) return;
   if (live) {
     rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, A.v + off, K);
     rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, A.m + off, K);

@@ -315,6 +315,17 @@ typedef struct dgb_cable_args {
    spike is counted (its state then holds that step; the trace is complete up
    to it).  For threshold trials, which only need to know whether a fibre fires. */
 #define DGB_CABLE_STOP_ON_SPIKE 8
+/* SPLIT_GATES (dgb_cable_run, dgb_cable_run_taped; lanes_mode 0): one cable
+   per CTA of 4 warps, one per SM sub-partition.  The gate advance and row
+   assembly of the cable's rows are spread over the 4 warps; the solve,
+   detection and recording stay on the first.  The same operations as the
+   one-warp run: float32 results bit for bit; float64 ones up to the last
+   bits, where the compiler may contract a different multiply-add of the same
+   expression.  For populations with fewer cables than SMs, whose warps would
+   otherwise each be held to one sub-partition's arithmetic rate.  Chosen without the flag
+   when warps_per_block is 0, lanes_mode is 0 and n_cables is at most the
+   device's SM count. */
+#define DGB_CABLE_SPLIT_GATES 16
 
 /*
  * Run n_steps backward-Euler + cnexp steps of every cable in one persistent

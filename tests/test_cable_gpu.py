@@ -229,3 +229,62 @@ def test_config2_spiking_sample_every_compartment_and_spike(cuda, fast_math):
     assert not res.raster.overflow
     np.testing.assert_array_equal(res.raster.count.cpu().numpy(), ref["rast_count"])
     np.testing.assert_array_equal(res.raster.steps.cpu().numpy(), ref["rast_steps"])
+
+
+def _run_all_outputs(pop, steps, stop_on_spike=False):
+    ks = torch.as_tensor(pop.n_comp)
+    rec = (ks - 1).to(torch.int32)
+    res = pop.run(steps, rec_idx=rec, spk_idx=0, spk_idx2=rec // 2, record_all=True,
+                  raster=[0, -1], raster_cap=16, stop_on_spike=stop_on_spike)
+    pop.check_status()
+    outs = [res.trace, res.spk_count, res.spk_first, res.trace_all, res.raster.count,
+            res.raster.steps, res.raster.below]
+    return outs + [getattr(pop, k) for k in ("v", "m", "h", "n")]
+
+
+@pytest.mark.parametrize("dtype,fast_math,compress", [
+    (torch.float64, False, True), (torch.float64, False, False),
+    (torch.float32, False, True), (torch.float32, True, True), (torch.float32, True, False)])
+@pytest.mark.parametrize("stop", [False, True])
+def test_split_gates_equal_fused_run(cuda, dtype, fast_math, compress, stop):
+    """Gate work of one cable spread over 4 warps (DGB_CABLE_SPLIT_GATES) against
+    the one-warp run: ragged K up to 1024 (1 to 32 rows per lane),
+    extracellular and intracellular drive, the full trace, both detection
+    compartments, the raster and stop-on-spike.  float32: every output bit for
+    bit.  float64: spike and raster outputs exactly, voltages and gates within
+    F64_SPLIT (the two kernels' compiled float64 code may contract a different
+    multiply-add of the same expression: last-bit differences, measured at most
+    1.4e-14 mV after 250 steps)."""
+    kw = dict(intra=True, fast_math=fast_math, compress_uniform=compress)
+    runs = []
+    for split in (False, True):
+        pop = synthetic_population(21, 40, 1, 1024, dtype, cuda, **kw)
+        pop.warps_per_block = 2 if not split else 0
+        pop.split_gates = split
+        runs.append(_run_all_outputs(pop, 250, stop_on_spike=stop))
+    assert int(runs[0][1].sum()) > 0  # some cable fires
+    _assert_split_equal(*runs, dtype)
+
+
+# split-gate float64 runs against one-warp runs: last-bit contraction differences
+F64_SPLIT = 1e-11
+
+
+def _assert_split_equal(ra, rb, dtype):
+    for a, b in zip(ra, rb):
+        tol = F64_SPLIT if a.dtype == torch.float64 and dtype == torch.float64 else 0.0
+        torch.testing.assert_close(a, b, rtol=0, atol=tol, equal_nan=True)
+
+
+def test_split_gates_chosen_for_small_populations(cuda):
+    """Default launch shape: the split run for at most one cable per SM, with
+    the same bits as an explicit one-warp-per-cable launch."""
+    a = synthetic_population(22, 24, 51, 401, torch.float32, cuda, intra=True)
+    b = synthetic_population(22, 24, 51, 401, torch.float32, cuda, intra=True)
+    b.warps_per_block = 1
+    ra, rb = _run_all_outputs(a, 200), _run_all_outputs(b, 200)
+    _assert_split_equal(ra, rb, torch.float32)
+    # and the run is the split one: forcing it changes nothing
+    c = synthetic_population(22, 24, 51, 401, torch.float32, cuda, intra=True)
+    c.split_gates = True
+    _assert_split_equal(ra, _run_all_outputs(c, 200), torch.float32)
