@@ -162,6 +162,27 @@ __device__ __forceinline__ T dv(T a, T b) {
   }
 }
 
+// Pivot reciprocal and division of the persistent run's solve: dv's policy in
+// float32; in float64 the Newton-refined reciprocal (rcp_nr64), within about
+// an ulp of the correctly rounded quotient (pivots of the diagonally dominant
+// cable systems are normal and far from zero).
+template <typename T, bool FAST>
+__device__ __forceinline__ T srcp(T b) {
+  if constexpr (sizeof(T) == 8) {
+    return rcp_nr64(b);
+  } else {
+    return dv<T, FAST>(T(1), b);
+  }
+}
+template <typename T, bool FAST>
+__device__ __forceinline__ T sdv(T a, T b) {
+  if constexpr (sizeof(T) == 8) {
+    return a * rcp_nr64(b);
+  } else {
+    return dv<T, FAST>(a, b);
+  }
+}
+
 // Row i of a cable lives in lane i / ch, slot i % ch of the planes.  The
 // tape stores rows contiguously, so lane r visits rows r, r + 32, ... with
 // (lane, slot) advanced incrementally: 32 = (32 / ch) * ch + 32 % ch.

@@ -329,7 +329,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
           v_next = j < ch - 1 ? pr[rs + Q_V * 32] : v_hi;
           T a, b, c, d;
           assemble(pr, j, v_prev, vj, v_next, ve_tag, a, b, c, d);
-          const T rinv = dv<T, FAST>(T(1), b - a * cp);
+          const T rinv = srcp<T, FAST>(b - a * cp);
           ap = -a * ap * rinv;
           dp = (d - a * dp) * rinv;
           cp = c * rinv;
@@ -377,7 +377,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
             pr += rs;
             const T a = pr[Q_AP * 32], b = pr[Q_B * 32], c = pr[Q_CP * 32];
             const T d = dt_s * pr[Q_DP * 32];
-            const T rinv = dv<T, FAST>(T(1), b - a * cp);
+            const T rinv = srcp<T, FAST>(b - a * cp);
             ap = -a * ap * rinv;
             dp = (d - a * dp) * rinv;
             cp = c * rinv;
@@ -434,17 +434,26 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
         de = Ds2 - As * De_l - Cs2 * De;
       }
       // ---- PCR across the P lanes, then back substitution
-  #pragma unroll
+#pragma unroll
       for (int sh = 1; sh < 32; sh <<= 1) {
         if (sh >= P) break;
-        T al_l = shfl_up<T>(al, sh, P), be_l = shfl_up<T>(be, sh, P);
+        // float64: each lane's pivot reciprocal, shuffled to both neighbours
+        T pv = be;
+        if constexpr (sizeof(T) == 8) pv = srcp<T, FAST>(be);
+        T al_l = shfl_up<T>(al, sh, P), pv_l = shfl_up<T>(pv, sh, P);
         T ga_l = shfl_up<T>(ga, sh, P), de_l = shfl_up<T>(de, sh, P);
-        T al_r = shfl_down<T>(al, sh, P), be_r = shfl_down<T>(be, sh, P);
+        T al_r = shfl_down<T>(al, sh, P), pv_r = shfl_down<T>(pv, sh, P);
         T ga_r = shfl_down<T>(ga, sh, P), de_r = shfl_down<T>(de, sh, P);
         const bool hl = r >= sh;
         const bool hr = r + sh < P;
-        T k1 = hl ? dv<T, FAST>(al, be_l) : T(0);
-        T k2 = hr ? dv<T, FAST>(ga, be_r) : T(0);
+        T k1, k2;
+        if constexpr (sizeof(T) == 8) {
+          k1 = hl ? al * pv_l : T(0);
+          k2 = hr ? ga * pv_r : T(0);
+        } else {
+          k1 = hl ? dv<T, FAST>(al, pv_l) : T(0);
+          k2 = hr ? dv<T, FAST>(ga, pv_r) : T(0);
+        }
         T al_n = hl ? -k1 * al_l : T(0);
         T ga_n = hr ? -k2 * ga_r : T(0);
         be = be - (hl ? k1 * ga_l : T(0)) - (hr ? k2 * al_r : T(0));
@@ -452,7 +461,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
         al = al_n;
         ga = ga_n;
       }
-      const T xs = dv<T, FAST>(de, be);
+      const T xs = sdv<T, FAST>(de, be);
       T xe = xs;
       if (ch > 1) {
         T xs_next = shfl_down<T>(xs, 1, P);
