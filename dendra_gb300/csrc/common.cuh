@@ -161,10 +161,32 @@ struct Math<double> {
   }
 };
 
-// x / (exp(x/y) - 1) with the local Bernoulli branch.
+// x / c for a constant integer c whose odd part exceeds 1 (10, 18, 20, 80 in
+// the HH rates).  float32: the division.  float64: q = RN(x rc) with rc =
+// RN(1/c) (folded at compile time), corrected once by the remainder, RN(q +
+// rc RN(x - q c)) with both steps fused multiply-adds (Markstein's
+// correction).  The result is the correctly rounded x / c, bit for bit the
+// division's (up to the sign of a zero quotient), for finite x away from
+// overflow and underflow: x / c is never a rounding midpoint (a midpoint has
+// 54 significant bits and an odd last one, so c times it needs more than 53)
+// and lies at least ulp/(2c) from one, while q + rc (x - q c) is within about
+// 2^-51 ulp of x / c.  Three instructions instead of a division's sequence.
+template <typename T>
+__device__ __forceinline__ T div_c(T x, T c) {
+  if constexpr (sizeof(T) == 8) {
+    const T rc = T(1) / c;
+    const T q = x * rc;
+    return fma(fma(-q, c, x), rc, q);
+  } else {
+    return x / c;
+  }
+}
+
+// x / (exp(x/y) - 1) with the local Bernoulli branch (y: a constant that
+// div_c accepts).
 template <typename T>
 __device__ __forceinline__ T vtrap(T x, T y) {
-  T q = x / y;
+  T q = div_c<T>(x, y);
   if (Math<T>::fabs_(q) <= Math<T>::kVtrapLocal) {
     T even = Math<T>::even_series(q);
     return (y - x / T(2)) + x * (q * even);
@@ -193,11 +215,11 @@ __device__ __forceinline__ T cnexp_step(T x, T a, T b, T dt) {
 template <typename T>
 __device__ __forceinline__ void hh_gates(T v, T q10, T dt, T& m, T& h, T& n) {
   T alpha_m = T(0.1f) * vtrap<T>(-(v + T(40)), T(10));
-  T beta_m = T(4.0) * Math<T>::ex(-(v + T(65)) / T(18));
-  T alpha_h = T(0.07f) * Math<T>::ex(-(v + T(65)) / T(20));
-  T beta_h = T(1.0) / (Math<T>::ex(-(v + T(35)) / T(10)) + T(1));
+  T beta_m = T(4.0) * Math<T>::ex(div_c<T>(-(v + T(65)), T(18)));
+  T alpha_h = T(0.07f) * Math<T>::ex(div_c<T>(-(v + T(65)), T(20)));
+  T beta_h = T(1.0) / (Math<T>::ex(div_c<T>(-(v + T(35)), T(10))) + T(1));
   T alpha_n = T(0.01f) * vtrap<T>(-(v + T(55)), T(10));
-  T beta_n = T(0.125) * Math<T>::ex(-(v + T(65)) / T(80));
+  T beta_n = T(0.125) * Math<T>::ex(div_c<T>(-(v + T(65)), T(80)));
   m = cnexp_step<T>(m, q10 * alpha_m, q10 * (alpha_m + beta_m), dt);
   h = cnexp_step<T>(h, q10 * alpha_h, q10 * (alpha_h + beta_h), dt);
   n = cnexp_step<T>(n, q10 * alpha_n, q10 * (alpha_n + beta_n), dt);
