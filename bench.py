@@ -529,6 +529,17 @@ def _c1_oracle(threads=None):
     return time.perf_counter() - t0, out, oracle.num_threads(), pop.N * C1_STEPS
 
 
+def _apply_launch(pop, launch):
+    """--launch for configs 1 and 4: its first field fixes the cables per CTA
+    of the persistent runs, -1 the split-gate run (one cable on 4 warps);
+    empty keeps the library's default shape."""
+    if not launch:
+        return
+    w = int(launch.split(",")[0])
+    pop.split_gates = w < 0
+    pop.warps_per_block = max(w, 0)
+
+
 def bench_c1(args, world, rank, local):
     """Config 1: 64 HH cables x 101 compartments (L 1000 um, dx 10 um, diam 1 um,
     Ra 100 ohm cm), float64, backward Euler + cnexp at dt 0.025 ms for 2000
@@ -571,8 +582,7 @@ def bench_c1(args, world, rank, local):
     dev = torch.device("cuda", local)
     dendra_gb300.load()
     pop = cable_population_c1(device=dev)
-    if args.launch:
-        pop.warps_per_block = int(args.launch.split(",")[0])
+    _apply_launch(pop, args.launch)
     state0 = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
 
     def reset():
@@ -861,6 +871,7 @@ def bench_c4(args, world, rank, local):
     dev = torch.device("cuda", local)
     pop, spec = cable_population_c4(n_cables, seed=4 + rank, device=dev,
                                     fast_math=not args.exact)
+    _apply_launch(pop, args.launch)
     run = CableGradient(pop, n_ts, rec_idx=0, checkpoint_every=C4_CHECKPOINT)
     names = ("gnabar", "gkbar", "gl", "ra")
     hidden = [torch.as_tensor(spec["hidden"][k], dtype=torch.float32, device=dev) for k in names]
@@ -1826,7 +1837,7 @@ def main():
     ap.add_argument("--ref-child", default="", help=argparse.SUPPRESS)
     ap.add_argument("--launch", default="",
                     help="c2: fixed 'wpb,k16,k8' instead of autotuning (profiling runs); "
-                         "c1: the first field fixes the cables per CTA")
+                         "c1, c4: the first field fixes the cables per CTA (-1: split gates)")
     args = ap.parse_args()
     if args.ref_child:
         return _ref_child(args.ref_child, args.ref_steps, args.steps, args.warmup)
@@ -1875,7 +1886,7 @@ def main():
 
     if args.launch:
         wpb, tune_ms = tuple(int(x) for x in args.launch.split(",")), None
-        pop.warps_per_block = wpb[0]
+        _apply_launch(pop, args.launch)
         pop.lanes_split = None if wpb[1:] == (0, 0) else wpb[1:]
     else:
         wpb, tune_ms = tune_cable_run(pop, n_steps=100)

@@ -42,11 +42,14 @@ class CableGradient:
     and the serial order measured faster (config 4: 247 vs 308 ms per
     backward pass).  A float32 population built
     with fast_math runs the forward, the recompute and the adjoint's gate
-    partials and solve with the fast-math arithmetic.
+    partials and solve with the fast-math arithmetic.  tune: pick the
+    forward and recompute runs' launch shape (cables per CTA or the
+    split-gate run) by timing a short taped recompute, once per population
+    shape (cached); this sets pop.warps_per_block and pop.split_gates.
     """
 
     def __init__(self, pop: CablePopulation, n_steps: int, rec_idx=0, checkpoint_every=500,
-                 overlap=False):
+                 overlap=False, tune=True):
         if pop.dt is None:
             raise RuntimeError("Model must be initialized before running.")
         if n_steps < 1 or checkpoint_every < 1:
@@ -61,6 +64,8 @@ class CableGradient:
             raise ValueError("rec_idx out of range for some cable")
         self.rec = rec.to(dev)
         self.state0 = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
+        if tune:
+            self._tune_launch()
         self.counts = torch.as_tensor(pop.n_comp, device=dev)
         self.comp_cable = pop._dev["comp_cable"].long()
         self.base_axial = (pop._dev["g_right"].clone(), pop._dev["g_left"].clone())
@@ -73,6 +78,37 @@ class CableGradient:
         if self.overlap:
             self._side = torch.cuda.Stream(dev)
             self._side_scratch = torch.zeros(4, dtype=torch.int32, device=dev)
+
+    def _tune_launch(self):
+        """Cables per CTA or the split-gate run for the forward and recompute
+        runs, timed on what dominates them: a taped recompute of
+        min(checkpoint_every, 50) steps from the initial state (cached per
+        population shape)."""
+        from .autotune import CABLE_RUN_SPLIT, tune
+
+        pop = self.pop
+        steps = min(self.seg, 50)
+        tape = torch.empty((steps + 1, 4, pop.N), dtype=pop.dtype, device=pop.device)
+        work = tuple(torch.empty_like(t) for t in self.state0)
+        L = _lib.load()
+
+        def apply(c):
+            pop.warps_per_block = max(int(c[0]), 0)
+            pop.split_gates = int(c[0]) < 0
+
+        def run(c):
+            apply(c)
+            for w, s in zip(work, self.state0):
+                w.copy_(s)
+            _lib.check(L.dgb_cable_run_taped(self._args(steps, 0, work), tape.data_ptr(),
+                                             _lib.stream_ptr(pop.device)), "dgb_cable_run_taped")
+
+        cands = ((2, 0, 0), (4, 0, 0), CABLE_RUN_SPLIT)
+        parts = (str(pop.dtype), pop.B, max(pop.n_comp), pop.N, pop.fast_math,
+                 pop.uniform_geometry and pop.uniform_channels, steps)
+        with torch.cuda.device(pop.device):
+            best, _ = tune("cable_gradient_launch", parts, cands, run, pop.device)
+        apply(best)
 
     # -- parameters -------------------------------------------------------
     def set_params(self, gnabar=None, gkbar=None, gl=None, ra=None):

@@ -104,25 +104,33 @@ def tune(kind, key_parts, candidates, run, device, reps=3, force=False):
 
 
 # (cables per CTA, k16, k8): cables with K <= k8 on 8 lanes, K <= k16 on 16
-# lanes, the rest on 32 ((0, 0): every cable on 32 lanes)
+# lanes, the rest on 32 ((0, 0): every cable on 32 lanes).  Cables per CTA
+# -1: the split-gate run (one cable per CTA of 4 warps, every cable on 32
+# lanes), for populations with few cables per SM.
+CABLE_RUN_SPLIT = (-1, 0, 0)
 CABLE_RUN_CANDIDATES = tuple((w, k16, k8) for w in (2, 4)
-                             for k16, k8 in ((0, 0), (96, 0), (128, 0), (128, 64), (160, 80)))
+                             for k16, k8 in ((0, 0), (96, 0), (128, 0), (128, 64), (160, 80))
+                             ) + (CABLE_RUN_SPLIT,)
 
 
 def tune_cable_run(pop, n_steps=50, candidates=CABLE_RUN_CANDIDATES, reps=3, force=False):
-    """Pick cables per CTA and the lane split for ``pop``'s persistent runs;
-    sets pop.warps_per_block and pop.lanes_split.
+    """Pick cables per CTA (or the split-gate run) and the lane split for
+    ``pop``'s persistent runs; sets pop.warps_per_block, pop.split_gates and
+    pop.lanes_split.
 
     Times ``n_steps`` steps from the population's current state (restored
     after every timing).  Returns ((wpb, k16, k8), {candidate: ms} or None if
     cached)."""
     state = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
     step, t = pop.step_index, pop.t
-    saved = (pop.warps_per_block, pop.lanes_split)
+    saved = (pop.warps_per_block, pop.split_gates, pop.lanes_split)
 
     def apply(c):
         w, k16, k8 = (int(x) for x in c)
-        pop.warps_per_block = w
+        if w < 0 and (k16, k8) != (0, 0):
+            raise ValueError("the split-gate run keeps every cable on 32 lanes")
+        pop.warps_per_block = max(w, 0)
+        pop.split_gates = w < 0
         pop.lanes_split = None if k16 == 0 and k8 == 0 else (k16, k8)
 
     kmax = max(pop.n_comp)
@@ -146,7 +154,7 @@ def tune_cable_run(pop, n_steps=50, candidates=CABLE_RUN_CANDIDATES, reps=3, for
         for dst, src in zip((pop.v, pop.m, pop.h, pop.n), state):
             dst.copy_(src)
         pop.step_index, pop.t = step, t
-        pop.warps_per_block, pop.lanes_split = saved
+        pop.warps_per_block, pop.split_gates, pop.lanes_split = saved
     best = tuple(int(x) for x in best)
     apply(best)
     return best, timings

@@ -72,6 +72,29 @@ __device__ __forceinline__ void rows_store(const T* wsm, int NQ, int q, int ch, 
     dst[i] = wsm[(j * NQ + q) * 32 + L];
   }
 }
+// The per-step state tape: planes v, m, h, n to dst[i], dst[N + i],
+// dst[2N + i], dst[3N + i] in one walk over rows r, r + P, ..., advancing
+// (lane, slot) by (P / ch, P % ch) with one carry (P % ch < ch): two integer
+// divisions per store instead of two per row and plane.
+template <typename T>
+__device__ __forceinline__ void rows_store_state(const T* wsm, int NQ, int ch, int lane0, int P,
+                                                 int r, T* dst, int64_t N, int K) {
+  int L = lane0 + r / ch, j = r % ch;
+  const int dl = P / ch, dj = P % ch;
+  for (int i = r; i < K; i += P) {
+    const T* w = wsm + j * NQ * 32 + L;
+    dst[i] = w[0 * 32];
+    dst[N + i] = w[1 * 32];
+    dst[2 * N + i] = w[2 * 32];
+    dst[3 * N + i] = w[3 * 32];
+    L += dl;
+    j += dj;
+    if (j >= ch) {
+      j -= ch;
+      ++L;
+    }
+  }
+}
 
 // First step s in [0, n_steps] whose stimulus time t(s) = T(t0 + (step0 + s) dt)
 // is >= tb (n_steps when none).  t(s) never decreases with s, so a rectangular
@@ -253,10 +276,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
   if constexpr (TAPE) {
     if (solver && A.tape) {
       T* tp = A.tape + off;
-      rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, tp, K);
-      rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, tp + A.n_comp, K);
-      rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, tp + 2 * A.n_comp, K);
-      rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, tp + 3 * A.n_comp, K);
+      rows_store_state<T>(wsm, NQ, ch, lane0, P, r, tp, A.n_comp, K);
     }
   }
   __syncwarp();  // the first step rewrites rows other lanes just stored
@@ -522,10 +542,7 @@ __device__ __forceinline__ void run_rows(const CableArgsT<T>& A, int pos0, int p
       if constexpr (TAPE) {
         if (A.tape) {
           T* tp = A.tape + (int64_t)(s + 1) * 4 * A.n_comp + off;
-          rows_store<T>(wsm, NQ, Q_V, ch, lane0, P, r, tp, K);
-          rows_store<T>(wsm, NQ, Q_M, ch, lane0, P, r, tp + A.n_comp, K);
-          rows_store<T>(wsm, NQ, Q_H, ch, lane0, P, r, tp + 2 * A.n_comp, K);
-          rows_store<T>(wsm, NQ, Q_N, ch, lane0, P, r, tp + 3 * A.n_comp, K);
+          rows_store_state<T>(wsm, NQ, ch, lane0, P, r, tp, A.n_comp, K);
         }
       }
       if (A.stop_on_spike) {

@@ -20,15 +20,18 @@ def test_cable_run_tuning_picks_a_candidate_and_cta_size_is_result_neutral(cuda)
     pop = synthetic_population(3, 300, 1, 401, torch.float32, cuda, fast_math=True)
     state = tuple(t.clone() for t in (pop.v, pop.m, pop.h, pop.n))
     best, timings = tune_cable_run(pop, n_steps=20, force=True)
-    assert best in CABLE_RUN_CANDIDATES and pop.warps_per_block == best[0]
+    assert best in CABLE_RUN_CANDIDATES and pop.warps_per_block == max(best[0], 0)
+    assert pop.split_gates == (best[0] < 0)
     assert set(timings) == set(CABLE_RUN_CANDIDATES)
     for split in (None, (128, 64)):
         outs = []
-        for wpb in (1, 2, 4):
+        # cables per CTA 1, 2, 4 and (32 lanes only) the split-gate run
+        for wpb in (1, 2, 4) + ((-1,) if split is None else ()):
             for dst, src in zip((pop.v, pop.m, pop.h, pop.n), state):
                 dst.copy_(src)
             pop.step_index = 0
-            pop.warps_per_block = wpb
+            pop.warps_per_block = max(wpb, 0)
+            pop.split_gates = wpb < 0
             pop.lanes_split = split
             res = pop.run(100, rec_idx=0, spk_idx=0)
             pop.check_status()

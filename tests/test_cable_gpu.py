@@ -148,16 +148,19 @@ def test_spike_detection_counts_rising_edges(cuda, golden):
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_uniform_coefficient_compression_is_exact(cuda, dtype):
-    """Per-cable uniform geometry/channels read once give bit-identical runs."""
+    """Per-cable uniform geometry/channels read once give the same runs: the
+    same operations on the same values (float32 bit for bit; float64 within
+    F64_VARIANT, see _assert_variants_equal)."""
     a = synthetic_population(13, 96, 1, 700, dtype, cuda, intra=True)
     b = synthetic_population(13, 96, 1, 700, dtype, cuda, intra=True, compress_uniform=False)
     assert a.uniform_geometry and a.uniform_channels
     assert not b.uniform_geometry and not b.uniform_channels
     ra = a.run(300, rec_idx=0, spk_idx=0)
     rb = b.run(300, rec_idx=0, spk_idx=0)
-    for name in ("v", "m", "h", "n"):
-        torch.testing.assert_close(getattr(a, name), getattr(b, name), rtol=0, atol=0)
-    torch.testing.assert_close(ra.trace, rb.trace, rtol=0, atol=0)
+    _assert_variants_equal([getattr(a, k) for k in ("v", "m", "h", "n")] +
+                           [ra.trace, ra.spk_count, ra.spk_first],
+                           [getattr(b, k) for k in ("v", "m", "h", "n")] +
+                           [rb.trace, rb.spk_count, rb.spk_first], dtype)
 
 
 @pytest.mark.parametrize("fast_math", [False, True])
@@ -252,9 +255,7 @@ def test_split_gates_equal_fused_run(cuda, dtype, fast_math, compress, stop):
     extracellular and intracellular drive, the full trace, both detection
     compartments, the raster and stop-on-spike.  float32: every output bit for
     bit.  float64: spike and raster outputs exactly, voltages and gates within
-    F64_SPLIT (the two kernels' compiled float64 code may contract a different
-    multiply-add of the same expression: last-bit differences, measured at most
-    1.4e-14 mV after 250 steps)."""
+    F64_VARIANT."""
     kw = dict(intra=True, fast_math=fast_math, compress_uniform=compress)
     runs = []
     for split in (False, True):
@@ -263,16 +264,21 @@ def test_split_gates_equal_fused_run(cuda, dtype, fast_math, compress, stop):
         pop.split_gates = split
         runs.append(_run_all_outputs(pop, 250, stop_on_spike=stop))
     assert int(runs[0][1].sum()) > 0  # some cable fires
-    _assert_split_equal(*runs, dtype)
+    _assert_variants_equal(*runs, dtype)
 
 
-# split-gate float64 runs against one-warp runs: last-bit contraction differences
-F64_SPLIT = 1e-11
+# Two compiled kernel variants running the same float64 operations (split vs
+# one-warp run, per-compartment planes vs uniform values) may differ in the
+# last bits: the compiler is free to fuse a different multiply and add of the
+# same expression into an FMA in each, and the choice moves with unrelated
+# code changes (measured: at most 4.2e-14 mV after 300 steps).  float32 runs,
+# integer outputs and spike steps must match exactly.
+F64_VARIANT = 1e-11
 
 
-def _assert_split_equal(ra, rb, dtype):
+def _assert_variants_equal(ra, rb, dtype):
     for a, b in zip(ra, rb):
-        tol = F64_SPLIT if a.dtype == torch.float64 and dtype == torch.float64 else 0.0
+        tol = F64_VARIANT if a.dtype == torch.float64 and dtype == torch.float64 else 0.0
         torch.testing.assert_close(a, b, rtol=0, atol=tol, equal_nan=True)
 
 
@@ -283,8 +289,8 @@ def test_split_gates_chosen_for_small_populations(cuda):
     b = synthetic_population(22, 24, 51, 401, torch.float32, cuda, intra=True)
     b.warps_per_block = 1
     ra, rb = _run_all_outputs(a, 200), _run_all_outputs(b, 200)
-    _assert_split_equal(ra, rb, torch.float32)
+    _assert_variants_equal(ra, rb, torch.float32)
     # and the run is the split one: forcing it changes nothing
     c = synthetic_population(22, 24, 51, 401, torch.float32, cuda, intra=True)
     c.split_gates = True
-    _assert_split_equal(ra, _run_all_outputs(c, 200), torch.float32)
+    _assert_variants_equal(ra, _run_all_outputs(c, 200), torch.float32)
