@@ -64,3 +64,15 @@ def test_reference_arm_of_single_solve_workloads_runs_on_the_host():
         assert line["impl"] == "reference" and line["unit"] == unit
         assert line["value"] > 0 and line["cpu_baseline"]["kind"] == "port"
         assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_launch_override_sets_cables_per_cta_or_split_gates():
+    from types import SimpleNamespace
+
+    pop = SimpleNamespace(warps_per_block=0, split_gates=False)
+    bench._apply_launch(pop, "-1")
+    assert pop.split_gates and pop.warps_per_block == 0
+    bench._apply_launch(pop, "2,0,0")
+    assert not pop.split_gates and pop.warps_per_block == 2
+    bench._apply_launch(pop, "")
+    assert not pop.split_gates and pop.warps_per_block == 2

@@ -176,3 +176,30 @@ def test_block_tree_contract_errors_on_the_host():
     p = 16
     assert L.dgb_dhs_block3_solve(0, 0, 4, p, p, p, p, p, p, 1, p, p, p, 0, None) == -1
     assert L.dgb_dhs_block3_solve(0, 2, 4, p, p, p, p, p, p, 1, p, p, p, 0, None) == -1  # alias
+
+
+def test_cable_flag_constants_match_the_header():
+    text = open(os.path.join(ROOT, "include", "dendra_gb300.h")).read()
+    defined = {m.group(1): int(m.group(2))
+               for m in re.finditer(r"#define DGB_(CABLE_\w+) (\d+)", text)}
+    assert "CABLE_SPLIT_GATES" in defined
+    for name, value in defined.items():
+        assert getattr(_lib, name) == value, name
+
+
+def test_cable_run_flag_checks_on_the_host():
+    """Unknown flag bits and a split-gate run with lane classes are refused
+    before any device work (the pointers are never read)."""
+    L = dendra_gb300.load()
+    a = _lib.CableArgs()
+    a.dtype, a.n_cables, a.n_steps, a.rec_every, a.max_k, a.n_comp = 0, 1, 4, 1, 11, 11
+    for name in ("cable_ptr", "v", "m", "h", "n", "g_right", "g_left", "scale", "cm_inv",
+                 "gnabar", "gkbar", "gl", "el", "scratch"):
+        setattr(a, name, 4096)
+    a.flags = 32
+    assert L.dgb_cable_run(ctypes.byref(a), None) == -1
+    assert b"unknown flags" in L.dgb_last_error()
+    a.flags = _lib.CABLE_SPLIT_GATES
+    a.lanes_mode, a.n_lanes32, a.n_lanes16 = 1, 1, 0
+    assert L.dgb_cable_run(ctypes.byref(a), None) == -1
+    assert b"lanes_mode 0" in L.dgb_last_error()
