@@ -8,8 +8,8 @@ namespace dgb {
 
 constexpr int kCableWarps = 4;     // default warps (cables in flight) per block
 constexpr int kCableMaxWarps = 4;  // largest accepted warps_per_block
-// warps of one cable in the split-gate run: one per SM sub-partition, each
-// with its own FP32/FP64 pipes
+// warps of one cable in the split-gate run: one per SM sub-partition (one
+// warp alone leaves most of an SM's arithmetic rate unused)
 constexpr int kSplitWarps = 4;
 
 template <typename T>

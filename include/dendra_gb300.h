@@ -321,8 +321,9 @@ typedef struct dgb_cable_args {
    detection and recording stay on the first.  The same operations as the
    one-warp run: float32 results bit for bit; float64 ones up to the last
    bits, where the compiler may contract a different multiply-add of the same
-   expression.  For populations with fewer cables than SMs, whose warps would
-   otherwise each be held to one sub-partition's arithmetic rate.  Chosen without the flag
+   expression.  For populations with fewer cables than SMs: one warp per cable
+   leaves most of an SM's arithmetic rate unused (4 float64 cables on one SM ran
+   nearly as fast as 1).  Chosen without the flag
    when warps_per_block is 0, lanes_mode is 0 and n_cables is at most the
    device's SM count. */
 #define DGB_CABLE_SPLIT_GATES 16
