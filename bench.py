@@ -275,7 +275,7 @@ def _c2_gpu_outputs(dev, fast_math, steps=2000, every=10):
 
 
 def _c2_accuracy(gpu_outs, steps=2000, every=10):
-    """float32 GPU vs the float64 oracle judge (float32 pulse grid, same inputs),
+    """float32 GPU vs the float64 oracle (float32 pulse grid, same inputs),
     and the reference's own float32 arithmetic (the oracle in float32) beside it."""
     import oracle
     from dendra_gb300.workloads import cable_population_c2
@@ -298,9 +298,9 @@ def _c2_accuracy(gpu_outs, steps=2000, every=10):
                                           np.array_equal(stp, j["rast_steps"])),
             "crossings": int(j["rast_count"].sum()),
             "cables_firing": int((j["rast_count"].max(axis=1) > 0).sum())}
-    return {"judge": "float64 oracle on the same inputs and float32 pulse grid; every "
-                     "compartment every 10 steps over 2000 steps; crossings at both ends and "
-                     "the middle", "samples": res}
+    return {"reference": "float64 oracle on the same inputs and float32 pulse grid; every "
+                         "compartment every 10 steps over 2000 steps; crossings at both ends "
+                         "and the middle", "samples": res}
 
 
 REF_DIR = os.path.join(ROOT, "baseline", "_ref")
@@ -686,7 +686,7 @@ def bench_c1(args, world, rank, local):
             "max_abs_dv_mv_vs_float64_oracle": float(np.abs(trace - ref["trace_all"]).max()),
             "spike_steps_identical": bool(np.array_equal(rast["count"], ref["rast_count"]) and
                                           np.array_equal(rast["steps"], ref["rast_steps"])),
-            "judge": "float64 CPU oracle of the reference update, same inputs"}
+            "reference": "float64 CPU oracle of the reference update, same inputs"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

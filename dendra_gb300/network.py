@@ -248,7 +248,7 @@ class TreeNetwork:
         # size classes (off by default): cells of at most half the largest
         # cell's compartments are advanced by their own window launch, whose
         # shared memory per cell is sized for them (about twice as many cells
-        # per SM); same results.  On config 3 the two launches run one after
+        # per SM); same results.  On the 4,096-cell network the two launches run one after
         # the other and each ends in a tail: 2.36e10 vs 2.44e10 in one launch.
         self.classes = None
         kk = np.diff(node_ptr)
@@ -476,7 +476,7 @@ class CapturedRun:
 def random_network(n_cells, k_range=(200, 2000), syn_per_cell=100, seed=0, dt=0.025,
                    rate_hz=5.0, t_stop_ms=200.0, bg_weight=0.05, delay_range=(1.0, 5.0),
                    bg="host", **kw):
-    """Config-3-style network: random trees, syn_per_cell Exp2Syn inputs from random
+    """A network like the 4,096-cell benchmark: random trees, syn_per_cell Exp2Syn inputs from random
     pre cells (lognormal(-7, 0.5) uS, delays U[1,5] ms), one background synapse at
     the soma driven by a seeded 5 Hz Poisson process: event times drawn on the
     host (bg="host") or a NetStim per cell on the device (bg="netstim":

@@ -46,7 +46,8 @@ def node_compartment(n):
 
 
 def fibre_params(n, seed=0):
-    """Seeded fibre/stimulus parameters with the config-5 distributions."""
+    """Seeded fibre/stimulus parameters with the distributions of the 65,536-fibre
+    threshold workload (241 compartments per fibre)."""
     rng = np.random.default_rng(seed)
     return dict(D=rng.uniform(2.0, 16.0, n), dist=rng.uniform(200.0, 5000.0, n),
                 offset=rng.uniform(0.0, 1.0, n), pw=rng.uniform(0.05, 1.0, n))

@@ -46,7 +46,8 @@ def c2_spec(n_cables=16384, seed=2024, kmin=51, kmax=401):
 
 def cable_population_c2(n_cables=16384, seed=2024, dtype=torch.float32, device="cuda",
                         subset=None, fast_math=False):
-    """Config-2 population (optionally only the cables listed in ``subset``)."""
+    """The 16,384-cable population (K 51-401, point-source pulse), optionally only
+    the cables listed in ``subset``."""
     s = c2_spec(n_cables, seed)
     idx = np.arange(n_cables) if subset is None else np.asarray(subset)
     ks = s["ks"][idx]
@@ -94,7 +95,8 @@ def c4_spec(n_cables=1024, seed=4):
 
 def cable_population_c4(n_cables=1024, seed=4, dtype=torch.float32, device="cuda",
                         fast_math=False):
-    """Config-4 population at the default parameters (the guesses)."""
+    """The 1,024 × 201 gradient-fit population at the default parameters (the
+    guesses)."""
     s = c4_spec(n_cables, seed)
     pop = CablePopulation([s["K"]] * n_cables, 1.0, 10.0, rhoa=100.0, celsius=6.3,
                           v_init=-65.0, dtype=dtype, device=device, fast_math=fast_math)

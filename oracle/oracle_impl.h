@@ -279,7 +279,7 @@ void F(orc_block3_thomas)(int64_t B, int64_t K, const REAL* lower, const REAL* m
 
 /* Rectangular pulse gate on [delay, delay+pw) at time t (_gates.py:50-65).
    The reference forms the time grid and delay+pw in the state dtype, so a
-   float64 judge of a float32 run evaluates the gate in float32 (gate_f32). */
+   float64 reference run of a float32 run evaluates the gate in float32 (gate_f32). */
 static REAL F(rect)(double t0_ms, int32_t s, double dt_ms, REAL amp, REAL delay, REAL pw,
                     int32_t gate_f32) {
   if (gate_f32) {

@@ -9,7 +9,8 @@ from dendra_gb300.cable import CablePopulation
 
 
 def golden_cable_population(g, dtype, device="cpu", **kw):
-    """The reference's config-1-geometry run recorded in hh_cable_*.npz."""
+    """The reference's run with the 64-cable workload's geometry, recorded in
+    hh_cable_*.npz."""
     B, K = int(g["B"]), int(g["K"])
     pop = CablePopulation([K] * B, float(g["diam"]), float(g["dx"]), rhoa=float(g["rhoa"]),
                           celsius=float(g["celsius"]), v_init=float(g["v_init"]),
@@ -30,15 +31,15 @@ def golden_extra_population(g, dtype, device="cpu", **kw):
 
 
 def as_f64(p):
-    """Widen a problem dict's float arrays to float64 (the float64 judge of a run)."""
+    """Widen a problem dict's float arrays to float64 (the float64 reference of a run)."""
     return {k: (v.astype(np.float64) if isinstance(v, np.ndarray) and v.dtype.kind == "f" else v)
             for k, v in p.items()}
 
 
-def oracle_traces(pop, steps, comps, spk_idx=None, judge64=False):
+def oracle_traces(pop, steps, comps, spk_idx=None, ref64=False):
     """Run the oracle from pop's current state once per recorded compartment.
 
-    judge64: run in float64 on the population's (float32) inputs, with the
+    ref64: run in float64 on the population's (float32) inputs, with the
     pulse gates on the float32 time grid the population itself sees.
     Returns (traces (steps+1, B, len(comps)), final problem dict, spikes).
     """
@@ -47,10 +48,10 @@ def oracle_traces(pop, steps, comps, spk_idx=None, judge64=False):
     out = []
     final = None
     spikes = None
-    gate_f32 = judge64 and pop.dtype == torch.float32
+    gate_f32 = ref64 and pop.dtype == torch.float32
     for c in comps:
         p = pop.problem_dict()
-        if judge64:
+        if ref64:
             p = as_f64(p)
         p["rec_idx"] = np.full(pop.B, int(c), dtype=np.int32)
         if spk_idx is not None:

@@ -6,7 +6,7 @@ pandas/natsort/h5py/dask/matplotlib stand-ins and three torch.library
 compatibility shims) and records its outputs on seeded inputs:
 
   hh_cable_{f64,f32}.npz   Unmyelinated + hh + bwd_euler_ub + somatic mono_rect
-                           (config-1 geometry: diam 1 um, L 1000 um, dx 10 um)
+                           (64-cable workload geometry: diam 1 um, L 1000 um, dx 10 um)
   hh_extra_{f64,f32}.npz   Unmyelinated + hh with extra=(point field, mono_rect)
   tridiag.npz              pcr_solve_t / pcr_solve_parallel_t on random systems
   rates.npz                exprelr, _bounded_phi1, _linear_exact_step, HH rates

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 def test_cable_run_tuning_picks_a_candidate_and_cta_size_is_result_neutral(cuda):
     """The tuner picks one of its (cables per CTA, lane split) candidates; the
     CTA size alone never changes a result (the lane split changes rounding
-    only, within the oracle tolerances tested in test_config1_gpu.py)."""
+    only, within the oracle tolerances tested in test_full_traces_gpu.py)."""
     from dendra_gb300.autotune import CABLE_RUN_CANDIDATES
 
     pop = synthetic_population(3, 300, 1, 401, torch.float32, cuda, fast_math=True)

@@ -15,14 +15,14 @@ from tests._cases import (
 
 pytestmark = pytest.mark.gpu
 
-# float32 state against the float64 judge of the same inputs: at most 1e-3 mV
+# float32 state against the float64 reference run of the same inputs: at most 1e-3 mV
 # anywhere in the trace
 F32_MV = 1e-3
 # ... except through action potentials of strongly driven cables, where the
 # upstroke (hundreds of mV/ms) turns float32 rounding of the state into a
 # voltage difference far above 1e-3 mV: the reference's own float32
-# arithmetic (the oracle in float32) is 1.2e-2 mV from the float64 judge on
-# the spiking config-2 sample below.  Spike steps must still be identical.
+# arithmetic (the oracle in float32) is 1.2e-2 mV from the float64 reference run on
+# the spiking population sample below.  Spike steps must still be identical.
 F32_SPIKING_MV = 2e-2
 
 
@@ -55,25 +55,25 @@ def test_float64_run_matches_reference(cuda, golden, which):
 
 @pytest.mark.parametrize("fast_math", [False, True])
 @pytest.mark.parametrize("which", ["cable", "extra"])
-def test_float32_run_within_tolerance_of_float64_judge(cuda, golden, which, fast_math):
+def test_float32_run_within_tolerance_of_float64_reference(cuda, golden, which, fast_math):
     """float32 GPU run vs the float64 oracle on the same inputs and pulse grid:
-    within 1e-3 mV.  The reference's own float32 run is held to the same judge
+    within 1e-3 mV.  The reference's own float32 run is held to the same reference
     and its error printed beside ours.  Spike steps must equal those of the
     reference's float32 run exactly.
     """
     g32 = golden(f"hh_{which}_f32.npz")
     make = golden_cable_population if which == "cable" else golden_extra_population
     tr, _ = _gpu_traces(make, g32, torch.float32, cuda, g32["trace_comps"], fast_math=fast_math)
-    judge, _, _ = oracle_traces(make(g32, torch.float32), int(g32["steps"]), g32["trace_comps"],
-                                judge64=True)
-    ref_own = np.abs(g32["v_trace"] - judge).max()
-    err = np.abs(tr - judge).max()
-    print(f"{which} fast={fast_math}: gpu f32 vs f64 judge {err:.3e} mV; "
-          f"reference f32 vs judge {ref_own:.3e} mV")
+    ref64, _, _ = oracle_traces(make(g32, torch.float32), int(g32["steps"]), g32["trace_comps"],
+                                ref64=True)
+    ref_own = np.abs(g32["v_trace"] - ref64).max()
+    err = np.abs(tr - ref64).max()
+    print(f"{which} fast={fast_math}: gpu f32 vs f64 reference {err:.3e} mV; "
+          f"reference f32 vs f64 reference {ref_own:.3e} mV")
     assert err <= F32_MV
-    for c in range(judge.shape[2]):
+    for c in range(ref64.shape[2]):
         assert _spike_steps(tr[:, :, c]) == _spike_steps(g32["v_trace"][:, :, c])
-        assert _spike_steps(tr[:, :, c]) == _spike_steps(judge[:, :, c])
+        assert _spike_steps(tr[:, :, c]) == _spike_steps(ref64[:, :, c])
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
@@ -164,8 +164,9 @@ def test_uniform_coefficient_compression_is_exact(cuda, dtype):
 
 
 @pytest.mark.parametrize("fast_math", [False, True])
-def test_config2_sample_within_tolerance(cuda, fast_math):
-    """float32 (exact and fast math) vs the float64 judge on a config-2 subsample."""
+def test_population_sample_within_tolerance(cuda, fast_math):
+    """float32 (exact and fast math) vs the float64 reference run on a subsample of
+    the 16,384-cable population."""
     from dendra_gb300.workloads import cable_population_c2
 
     sub = np.arange(0, 16384, 128)
@@ -182,8 +183,8 @@ def test_config2_sample_within_tolerance(cuda, fast_math):
     err = np.abs(gpu - tr_ref).max()
     own = np.abs(tr32 - tr_ref).max()
     worst = np.unravel_index(np.argmax(np.abs(gpu - tr_ref)), gpu.shape)
-    print(f"c2 sample fast={fast_math}: gpu vs f64 judge {err:.3e} mV at {worst} "
-          f"(v={tr_ref[worst]:.3f}); float32 oracle vs judge {own:.3e}; "
+    print(f"c2 sample fast={fast_math}: gpu vs f64 reference {err:.3e} mV at {worst} "
+          f"(v={tr_ref[worst]:.3f}); float32 oracle vs f64 reference {own:.3e}; "
           f"gpu vs float32 oracle {np.abs(gpu - tr32).max():.3e}")
     assert err <= F32_MV
     np.testing.assert_array_equal(res.spk_count.cpu().numpy(), cnt_ref)
@@ -191,8 +192,9 @@ def test_config2_sample_within_tolerance(cuda, fast_math):
 
 
 def spiking_c2_subset(n=128):
-    """The n config-2 cables with the strongest drive (largest |amp| / distance):
-    about half of them fire (the rest are the thin ones), some repeatedly."""
+    """The n cables of the 16,384-cable population with the strongest drive
+    (largest |amp| / distance): about half of them fire (the rest are the thin
+    ones), some repeatedly."""
     from dendra_gb300.workloads import c2_spec
 
     s = c2_spec()
@@ -201,8 +203,9 @@ def spiking_c2_subset(n=128):
 
 
 @pytest.mark.parametrize("fast_math", [False, True])
-def test_config2_spiking_sample_every_compartment_and_spike(cuda, fast_math):
-    """float32 GPU run of strongly driven config-2 cables vs the float64 judge:
+def test_strongly_driven_sample_every_compartment_and_spike(cuda, fast_math):
+    """float32 GPU run of strongly driven cables of the 16,384-cable population vs
+    the float64 reference run:
     every compartment of every recorded step within 1e-3 mV, and every spike
     step at the two cable ends and the middle identical."""
     from dendra_gb300.workloads import cable_population_c2
@@ -225,7 +228,7 @@ def test_config2_spiking_sample_every_compartment_and_spike(cuda, fast_math):
     own = np.abs(ref32["trace_all"].astype(np.float64) - ref["trace_all"]).max()
     n_fire = int((ref["rast_count"].max(axis=1) > 0).sum())
     print(f"c2 spiking sample fast={fast_math}: {n_fire}/{pop.B} cables fire, "
-          f"{int(ref['rast_count'].sum())} crossings; max |dV| vs f64 judge: GPU {err:.3e} mV, "
+          f"{int(ref['rast_count'].sum())} crossings; max |dV| vs f64 reference: GPU {err:.3e} mV, "
           f"reference float32 arithmetic {own:.3e} mV")
     assert n_fire >= pop.B // 3, checks
     assert err <= F32_SPIKING_MV

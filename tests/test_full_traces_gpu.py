@@ -1,4 +1,4 @@
-"""Config 1 at its stated size and with its stated outputs.
+"""The 64-cable float64 workload at its stated size and with its stated outputs.
 
 64 unbranched HH cables x 101 compartments (L = 1000 um, dx = 10 um, diam
 1 um, Ra 100 ohm cm), float64, backward Euler + cnexp at dt 0.025 ms for
@@ -34,7 +34,7 @@ def _oracle_c1(pop, steps, checks):
     return extra
 
 
-def test_config1_full_traces_and_every_spike_step(cuda):
+def test_64_cable_run_full_traces_and_every_spike_step(cuda):
     pop = cable_population_c1(device=cuda)
     assert pop.B == 64 and set(pop.n_comp) == {101} and pop.dtype == torch.float64
     ref = _oracle_c1(cable_population_c1(device="cpu"), C1_STEPS, CHECKS)
@@ -44,7 +44,7 @@ def test_config1_full_traces_and_every_spike_step(cuda):
     assert tr.shape == (C1_STEPS + 1, 64 * 101)
     assert np.isfinite(tr).all()
     err = np.abs(tr - ref["trace_all"]).max()
-    print(f"config 1: max |dV| GPU vs float64 oracle over all compartments and steps {err:.3e}")
+    print(f"64 cables: max |dV| GPU vs float64 oracle over all compartments and steps {err:.3e}")
     assert err <= F64_MV
     rs = res.raster
     assert not rs.overflow
@@ -108,12 +108,12 @@ def test_lane_split_matches_oracle(cuda, dtype, split):
     pop = synthetic_population(31, 96, 1, 301, dtype, cuda, intra=True)
     pop.lanes_split = split
     p = pop.problem_dict()
-    judge = as_f64(p)
+    ref64 = as_f64(p)
     steps = 400
     kk = np.asarray(pop.n_comp)
     checks = [0, -1]
     idx = np.array([[c % k for c in checks] for k in kk], dtype=np.int32)
-    _, _, _, _, ref = oracle.cable_run(judge, steps, gate_f32=dtype == torch.float32,
+    _, _, _, _, ref = oracle.cable_run(ref64, steps, gate_f32=dtype == torch.float32,
                                        record_all=True, raster=idx, raster_cap=32)
     res = pop.run(steps, record_all=True, raster=checks, raster_cap=32)
     pop.check_status()

@@ -67,7 +67,7 @@ def test_split_runs_continue_identically(cuda):
 
 
 def test_background_rate(cuda):
-    """The config-3 background: 4,096 Poisson generators at 5 Hz over 200 ms."""
+    """The 4,096-cell network's background: 4,096 Poisson generators at 5 Hz over 200 ms."""
     ns = NetStim(4096, interval=200.0, noise=1.0, start=0.0, seed=2024, device=cuda)
     spikes = ns.run(8000, 0.025)
     total = int(spikes.sum())

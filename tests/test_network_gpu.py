@@ -14,11 +14,11 @@ def _raster(r, window=None):
     return r.cpu().numpy()
 
 
-def _judge(dtype, seed, **kw):
+def _ref64(dtype, seed, **kw):
     net, n_steps = random_network(16, k_range=(30, 400), syn_per_cell=12, seed=seed, dtype=dtype,
                                   device="cpu", t_stop_ms=60.0, **kw)
     pd = net.problem_dict(n_steps)
-    if dtype == torch.float32:  # float64 judge on the float32 network's inputs
+    if dtype == torch.float32:  # float64 reference on the float32 network's inputs
         for grp in ("nodes", "syn"):
             pd[grp] = {k: v.astype(np.float64) for k, v in pd[grp].items()}
         for k in ("v", "m", "h", "n", "A", "B", "ring"):
@@ -31,7 +31,7 @@ def _judge(dtype, seed, **kw):
 @pytest.mark.parametrize("seed", [3, 8])
 def test_network_matches_oracle(cuda, dtype, seed):
     kw = dict(bg_weight=0.05)
-    pd, ref_raster, n_steps = _judge(dtype, seed, **kw)
+    pd, ref_raster, n_steps = _ref64(dtype, seed, **kw)
     net, _ = random_network(16, k_range=(30, 400), syn_per_cell=12, seed=seed, dtype=dtype,
                             device=cuda, t_stop_ms=60.0, **kw)
     bits = net.run(n_steps)
@@ -120,8 +120,8 @@ def test_tree_step_drive_matches_oracle(cuda):
     """Extracellular edge currents and the injected current of the tree step
     (integrators/tree.py:1262-1302) against the oracle's restatement."""
     n_steps = 400
-    judge = _driven("cpu")
-    pd = judge.problem_dict(n_steps)
+    ref64 = _driven("cpu")
+    pd = ref64.problem_dict(n_steps)
     ref = oracle.net_run(pd, n_steps)
     net = _driven(cuda)
     raster = net.run(n_steps).cpu().numpy()

@@ -101,7 +101,7 @@ def test_cable_run_with_extracellular_matches_reference(golden, tag):
 
 
 def test_oracle_float32_is_within_tolerance_of_float64(golden):
-    """The float32 reference path and the float64 judge differ by < 1e-3 mV·(scale)."""
+    """The float32 reference path and the float64 reference run differ by < 1e-3 mV·(scale)."""
     g64 = golden("hh_cable_f64.npz")
     g32 = golden("hh_cable_f32.npz")
     assert np.abs(g64["v_trace"] - g32["v_trace"]).max() < 0.05

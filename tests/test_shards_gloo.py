@@ -1,4 +1,4 @@
-"""Multi-rank host logic on CPU: two gloo ranks partition a config-2-like
+"""Multi-rank host logic on CPU: two gloo ranks partition a ragged
 population by compartment count, gather per-cable results back in population
 order, and reduce their timings the way a ``torchrun --nproc-per-node N
 bench.py`` run does on GPUs.
