@@ -1,6 +1,6 @@
 """Benchmark: compartment-steps/s of the batched uneven HH cable population.
 
-Workload (config 2): 16,384 HH cables with odd compartment counts U[51, 401]
+Workload: 16,384 HH cables with odd compartment counts U[51, 401]
 (3.70 M compartments), float32 state, extracellular point-source stimulation
 (cathodic 0.1 ms pulse), dt 0.005 ms for 10 ms = 2000 timesteps.  One bench
 "step" is one full 2000-timestep run of the whole population: a single
@@ -33,7 +33,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "compartment-steps/s"
 ALG_BYTES_PER_COMP_STEP = 48  # unfused per-step traffic of one float32 compartment-step
-# persistent config-2 kernel under ncu (4,096 cables x 100 steps, float32 fast
+# persistent kernel of the 16,384-cable population under ncu (4,096 cables x 100 steps, float32 fast
 # math): DRAM bytes per compartment per launch, thread instructions per
 # compartment-step (profiles/ holds the capture's summary)
 C2_NCU_DRAM_BYTES_PER_COMP = 22536960 / 932014
@@ -227,7 +227,8 @@ def _dist():
 
 
 def cpu_baseline(n_sample: int, steps: int, threads: int | None = None):
-    """Oracle port of the reference CPU cable update on a config-2 subsample."""
+    """Oracle port of the reference CPU cable update on a subsample of the
+    16,384-cable population."""
     import torch
 
     import oracle
@@ -246,7 +247,7 @@ def cpu_baseline(n_sample: int, steps: int, threads: int | None = None):
 
 
 def _c2_samples():
-    """Two config-2 accuracy samples: every 128th cable, and the 128 most
+    """Two accuracy samples of the 16,384-cable population: every 128th cable, and the 128 most
     strongly driven cables (largest |amp| / distance; about half of them fire)."""
     from dendra_gb300.workloads import c2_spec
 
@@ -305,7 +306,7 @@ def _c2_accuracy(gpu_outs, steps=2000, every=10):
 
 REF_DIR = os.path.join(ROOT, "baseline", "_ref")
 REF_SHIM = os.path.join(ROOT, "tests", "golden", "refshim")
-# config-2 cables grouped by compartment count, as the reference needs one
+# cables of the 16,384-cable population grouped by compartment count, as the reference needs one
 # Unmyelinated population per K; the timed sample is these groups
 C2_REF_GROUPS = (51, 225, 401)
 
@@ -428,11 +429,12 @@ def reference_baseline(kind, steps, reps=1, warmup=0):
         return None, r["error"]
     secs = float(np.median(r["times"]))
     if kind == "c2":
-        what = (f"config-2 groups K={list(C2_REF_GROUPS)} ({sum(g[1] for g in r['groups'])} "
-                "cables with their own diameters and electrodes, one Unmyelinated population "
+        n_cab = sum(g[1] for g in r["groups"])
+        what = (f"16,384-cable population groups K={list(C2_REF_GROUPS)} ({n_cab} cables "
+                "with their own diameters and electrodes, one Unmyelinated population "
                 f"per K) x {steps} timesteps, float32")
     else:
-        what = f"config 1 (64 x 101 cables, float64, Recorder(v)) for {steps} of its 2000 steps"
+        what = f"64 x 101 float64 cables with Recorder(v) for {steps} of their 2000 steps"
     return {"value": r["units"] / secs, "unit": METRIC, "cores": r["threads"],
             "kind": "reference",
             "sample": f"{what}; the reference's model.run at JIT=0 (pcr_solve_t), torch "
@@ -440,9 +442,9 @@ def reference_baseline(kind, steps, reps=1, warmup=0):
 
 
 def run_reference(args, world, rank):
-    """Reference arm of config 2: the reference's own PyTorch CPU solver
+    """Reference arm of the 16,384-cable population: the reference's own PyTorch CPU solver
     (baseline/_ref, model.run through its public API) on all host cores, on
-    three of config 2's equal-K groups (their own cables, float32,
+    three of the population's equal-K groups (their own cables, float32,
     extracellular pulse) for --ref-steps timesteps per bench step.  The C port
     of the same update (oracle) is timed beside it and reported as a second
     figure; it becomes the line's value only when the reference cannot run."""
@@ -504,7 +506,7 @@ C1_RASTER = (0, 5, -5)  # soma and the reference Raster's default node_check [5,
 
 
 def _c1_problem():
-    """Config-1 population on the host (float64) with its raster indices."""
+    """The 64 x 101 float64 population on the host with its raster indices."""
     import torch
 
     from dendra_gb300.workloads import cable_population_c1
@@ -515,7 +517,7 @@ def _c1_problem():
 
 
 def _c1_oracle(threads=None):
-    """The float64 oracle on the full config-1 run: (seconds, outputs, cores)."""
+    """The float64 oracle on the full 64-cable run: (seconds, outputs, cores)."""
     import oracle
 
     pop, idx = _c1_problem()
@@ -541,7 +543,7 @@ def _apply_launch(pop, launch):
 
 
 def bench_c1(args, world, rank, local):
-    """Config 1: 64 HH cables x 101 compartments (L 1000 um, dx 10 um, diam 1 um,
+    """64 HH cables x 101 compartments (L 1000 um, dx 10 um, diam 1 um,
     Ra 100 ohm cm), float64, backward Euler + cnexp at dt 0.025 ms for 2000
     steps, a 1 ms somatic clamp at 5 ms of U[0.05, 0.5] nA.  One bench step is
     the whole run with its outputs: the full (2001, 64, 101) voltage trace and
@@ -556,7 +558,7 @@ def bench_c1(args, world, rank, local):
             return
         secs, _, cores, units = _c1_oracle()
         port = {"value": units / secs, "unit": METRIC, "cores": cores, "kind": "port",
-                "sample": "the whole config-1 run (12.9 M compartment-steps, full traces and "
+                "sample": "the whole 64-cable run (12.9 M compartment-steps, full traces and "
                           "raster), the oracle's C restatement"}
         cpu, why = reference_baseline("c1", args.ref_steps * 5, args.steps, args.warmup)
         if cpu is None:
@@ -674,7 +676,7 @@ def bench_c1(args, world, rank, local):
     if rank == 0 and not args.no_cpu:
         secs, ref, cores, _ = _c1_oracle()
         port = {"value": units / secs, "unit": METRIC, "cores": cores, "kind": "port",
-                "sample": "the whole config-1 run, float64 oracle, full traces and raster"}
+                "sample": "the whole 64-cable run, float64 oracle, full traces and raster"}
         cpu, why = reference_baseline("c1", 200)
         if cpu is None:
             cpu = dict(port, note=why)
@@ -695,7 +697,7 @@ C3_BYTES_PER_COMP_STEP = 24  # unfused tree step: v r/w 8 B + main/rhs/axial/par
 
 
 def bench_c3(args, world, rank, local):
-    """Config 3: 4,096 branched cells (200-2,000 compartments, HH soma, passive
+    """4,096 branched cells (200-2,000 compartments, HH soma, passive
     dendrites), 100 Exp2Syn inputs each from random cells (409,600 NetCons,
     lognormal(-7, 0.5) uS, delays U[1, 5] ms), 5 Hz Poisson background, float32,
     dt 0.025 ms for 200 ms (8,000 steps).  One bench step = the whole run."""
@@ -813,7 +815,8 @@ C4_ADJ_BYTES_PER_COMP_STEP = 48
 
 
 def _c4_cpu(n_sample, n_steps, seed=4):
-    """Oracle forward + reverse sweep of the config-4 fit on a sample of cables.
+    """Oracle forward + reverse sweep of the 1,024-cable gradient fit on a sample of
+    cables.
 
     Returns (seconds, compartment-steps, threads)."""
     import torch
@@ -832,7 +835,7 @@ def _c4_cpu(n_sample, n_steps, seed=4):
 
 
 def bench_c4(args, world, rank, local):
-    """Config 4: seconds per gradient iteration (forward with checkpoints every
+    """1,024-cable gradient fit: seconds per gradient iteration (forward with checkpoints every
     500 steps + checkpointed recompute + adjoint) of an MSE fit of somatic
     traces, 1,024 HH cables x 201 compartments, float32, dt 0.025 ms,
     20,000 steps; gradients w.r.t. per-cable gnabar, gkbar, gl and Ra."""
@@ -1382,7 +1385,7 @@ def _delay_bytes(n_edges, width, n_src, depth, steps, elem=4):
 
 
 def _delay_case(n_conn, n_src, depth, seed, dt_ms=0.025):
-    """Config-3 connectivity as a transport rollout: n_conn connections from
+    """The 4,096-cell network's connectivity as a transport rollout: n_conn connections from
     n_src sources, each into its own synapse slot (width n_conn, post slots
     shuffled), delays U[1,5] ms at dt 0.025 ms (positions 40-200 steps),
     lognormal(-7, 0.5) weights."""
@@ -1405,7 +1408,7 @@ def _delay_gates(steps, n_src, seed, rate_hz=5.0, dt_ms=0.025):
 
 
 def bench_delay(args, world, rank, local):
-    """Differentiable event transport (interpolated two-tap delays) at config-3
+    """Differentiable event transport (interpolated two-tap delays) at the 4,096-cell network's
     scale: 409,600 connections from 4,096 sources into a [201][409,600] ring,
     a 2,000-step rollout forward (one launch) and its reverse sweep (one launch
     + the per-source gate reduction) through two_tap_rollout and autograd.
@@ -1614,7 +1617,7 @@ def _c5_cpu(n_fibres, seed=7, lb0=0.0, ub0=0.1, rtol=0.01):
 
 
 def bench_c5(args, world, rank, local):
-    """Config 5: thresholds/s of the learned bracket + confirming bisection vs
+    """65,536-fibre threshold search: thresholds/s of the learned bracket + confirming bisection vs
     plain bisection, 65,536 myelinated-fibre-like cables (241 compartments),
     rtol 1%, dt 0.005 ms, horizon = longest pulse + 4 ms.  The MLP (4 -> 256 ->
     256 -> 256 -> 1, GELU, BF16) is trained on ``--train`` plain-bisection
@@ -1761,7 +1764,7 @@ def bench_c5(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
-# the other configurations, measured by the default run after config 2 (one
+# the other configurations, measured by the default run after the 16,384-cable population (one
 # child process each, their own JSON lines summarised): workload, extra
 # arguments, time limit in seconds
 OTHER_CONFIGS = (("c1", ["--steps", "3"], 300), ("c3", [], 600), ("c4", ["--steps", "2"], 600),
@@ -1815,7 +1818,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
-                    help="config 2: skip the child runs of the other configurations")
+                    help="skip the child runs of the other workloads after the default one")
     ap.add_argument("--exact", action="store_true",
                     help="exact float32 arithmetic instead of the fast-math variant")
     ap.add_argument("--workload", default="c2",
@@ -2028,7 +2031,7 @@ def main():
         reset()
 
     # ---- the reference's own GPU path on the same GPU (Triton Thomas solve +
-    #      eager mechanism kernels per step), on config-2 equal-K groups ----
+    #      eager mechanism kernels per step), on the population's equal-K groups ----
     ref_gpu = None
     if rank == 0 and not args.no_plain:
         r = reference_cpu("c2gpu", 200, reps=3, warmup=1)
@@ -2039,7 +2042,7 @@ def main():
             ref_gpu = {"value": r["units"] / secs, "unit": METRIC, "seconds": secs,
                        "what": (f"the reference's model.run on this GPU at JIT=0 (Triton "
                                 "thomas_solve_cuda_t + eager mechanism kernels per step), "
-                                f"config-2 groups K={list(C2_REF_GROUPS)} "
+                                f"16,384-cable population groups K={list(C2_REF_GROUPS)} "
                                 f"({sum(g[1] for g in r['groups'])} cables, one Unmyelinated "
                                 "population per K) x 200 timesteps, float32")}
 
