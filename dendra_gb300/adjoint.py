@@ -88,9 +88,8 @@ class CableGradient:
 
         pop = self.pop
         steps = min(self.seg, 50)
-        tape = torch.empty((steps + 1, 4, pop.N), dtype=pop.dtype, device=pop.device)
-        work = tuple(torch.empty_like(t) for t in self.state0)
         L = _lib.load()
+        bufs = {}  # tape and work state, made at the first timing (none when cached)
 
         def apply(c):
             pop.warps_per_block = max(int(c[0]), 0)
@@ -98,14 +97,20 @@ class CableGradient:
 
         def run(c):
             apply(c)
-            for w, s in zip(work, self.state0):
+            if not bufs:
+                bufs["tape"] = torch.empty((steps + 1, 4, pop.N), dtype=pop.dtype,
+                                           device=pop.device)
+                bufs["work"] = tuple(torch.empty_like(t) for t in self.state0)
+            for w, s in zip(bufs["work"], self.state0):
                 w.copy_(s)
-            _lib.check(L.dgb_cable_run_taped(self._args(steps, 0, work), tape.data_ptr(),
+            _lib.check(L.dgb_cable_run_taped(self._args(steps, 0, bufs["work"]),
+                                             bufs["tape"].data_ptr(),
                                              _lib.stream_ptr(pop.device)), "dgb_cable_run_taped")
 
         cands = ((2, 0, 0), (4, 0, 0), CABLE_RUN_SPLIT)
         parts = (str(pop.dtype), pop.B, max(pop.n_comp), pop.N, pop.fast_math,
-                 pop.uniform_geometry and pop.uniform_channels, steps)
+                 pop.uniform_geometry and pop.uniform_channels,
+                 "ve" if pop.field is not None else "-", steps)
         with torch.cuda.device(pop.device):
             best, _ = tune("cable_gradient_launch", parts, cands, run, pop.device)
         apply(best)
