@@ -62,7 +62,8 @@ def _div_c(x, c):
 def test_constant_division_is_the_correctly_rounded_quotient(c):
     rng = np.random.default_rng(int(c))
     # the rates divide v + 35, v + 40, v + 55 or v + 65 (mV): voltages from
-    # -200 to 200 mV, plus values near 0, binade edges and odd multiples of c
+    # -200 to 200 mV, plus values near 0, binade edges, multiples of c and the
+    # doubles just above them
     xs = list(rng.uniform(-265.0, 265.0, 4000))
     xs += list(rng.uniform(-1e-3, 1e-3, 500))
     xs += [float(c) * k for k in range(-40, 41)]
