@@ -84,6 +84,7 @@ SIGNATURES = {
     "dgb_tridiag_solve_transpose": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P]),
     "dgb_tridiag_status": (_INT, [_P]),
     "dgb_tridiag_set_wait_limit": (_INT, [_I64]),
+    "dgb_cable_adjoint_set_wait_limit": (_INT, [_I64]),
     "dgb_block3_solve": (_INT, [_INT, _I64, _I64, _P, _P, _P, _P, _P, _P, _I32, _P]),
     "dgb_block3_work_size": (ctypes.c_size_t, [_INT, _I64, _I64]),
     "dgb_cable_run": (_INT, [ctypes.POINTER(CableArgs), _P]),

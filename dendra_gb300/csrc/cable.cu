@@ -85,6 +85,13 @@ extern "C" int dgb_cable_run_taped(const dgb_cable_args* args, void* tape, void*
   return cable_run_launch<float, false, true>(args, tape, ch_max, st);
 }
 
+extern "C" int dgb_cable_adjoint_set_wait_limit(int64_t polls) {
+  clear_error();
+  const int rc = cable_adjoint_wait_limit_t<float>(polls);
+  if (rc) return rc;
+  return cable_adjoint_wait_limit_t<double>(polls);
+}
+
 extern "C" int dgb_cable_adjoint(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj,
                                  void* stream) {
   clear_error();

@@ -41,6 +41,11 @@ struct AdjArgsT {
 // copies and stopped (the segment's results are then incomplete).
 constexpr int kErrTapeWait = 4;
 constexpr uint32_t kTapeWaitLimit = 1u << 22;  // polls before a stage wait gives up
+// Polls of the first wait on a tape stage: kTapeWaitLimit unless the
+// diagnostic dgb_cable_adjoint_set_wait_limit lowered it (the drain after a
+// give-up always uses kTapeWaitLimit).  One copy per dtype's translation
+// unit; the setter writes both.
+static __device__ uint32_t g_tape_wait_limit = kTapeWaitLimit;
 
 // Row-interleaved planes of one warp (one cable), as in the forward kernel:
 // element (row j, plane q, lane L) at [(j * NQ + q) * 32 + L], so one row
@@ -122,6 +127,7 @@ __device__ bool adjoint_rows(const CableArgsT<T>& A, const AdjArgsT<T>& D, int c
                              uint32_t& par) {
   constexpr int NQ = AdjNQ<PLANES>::value;
   constexpr int rs = NQ * 32;
+  const uint32_t wait_limit = g_tape_wait_limit;
   constexpr int64_t E = 16 / sizeof(T);
   const int r = threadIdx.x & 31;
   const int64_t off = A.cable_ptr[cable];
@@ -231,7 +237,7 @@ __device__ bool adjoint_rows(const CableArgsT<T>& A, const AdjArgsT<T>& D, int c
     }
     // wait for this step's tape (phases alternate per stage use)
     const uint32_t parity = (par >> b) & 1u;
-    const bool landed = bulk::bar_wait(bars[b], parity, kTapeWaitLimit);
+    const bool landed = bulk::bar_wait(bars[b], parity, wait_limit);
     if (!__all_sync(0xffffffffu, landed)) {
       if (r == 0) {
         atomicOr(A.counter + 1, kErrTapeWait);
@@ -619,8 +625,18 @@ int cable_adjoint_t(const dgb_cable_args* args, const dgb_cable_adjoint_args* ad
                 : launch_adjoint<T, false, false>(A, D, ch_max, st);
 }
 
+// Sets this translation unit's tape-stage wait limit (polls < 0: the default).
+template <typename T>
+int cable_adjoint_wait_limit_t(int64_t polls) {
+  const uint32_t v = polls < 0 ? kTapeWaitLimit
+                               : (uint32_t)(polls > 0xffffffffll ? 0xffffffffll : polls);
+  DGB_CUDA_CHECK(cudaMemcpyToSymbol(g_tape_wait_limit, &v, sizeof v));
+  return DGB_OK;
+}
+
 #define DGB_INSTANTIATE_CABLE_ADJOINT(T)                                                \
   template int cable_adjoint_t<T>(const dgb_cable_args*, const dgb_cable_adjoint_args*, \
-                                  int, cudaStream_t);
+                                  int, cudaStream_t);                                   \
+  template int cable_adjoint_wait_limit_t<T>(int64_t);
 
 }  // namespace dgb

@@ -19,6 +19,8 @@ template <typename T>
 int cable_adjoint_t(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj, int ch_max,
                     cudaStream_t st);
 template <typename T>
+int cable_adjoint_wait_limit_t(int64_t polls);
+template <typename T>
 int cable_assemble_t(const dgb_cable_args* args, int32_t step, void* lower, void* mainv,
                      void* upper, void* rhs, cudaStream_t st);
 template <typename T>

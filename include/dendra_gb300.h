@@ -413,6 +413,13 @@ typedef struct dgb_cable_adjoint_args {
 int dgb_cable_adjoint(const dgb_cable_args* args, const dgb_cable_adjoint_args* adj,
                       void* stream);
 
+/* Diagnostic: polls a dgb_cable_adjoint warp spends on the first wait for a
+   tape stage before it gives up (0 = give up at the first poll; negative
+   restores the default 2^22).  A warp that gave up drains its posted copies
+   at the full limit, sets error bit 4 in scratch[1] and ends.  Lets a test
+   exercise the timeout path without a fault; no reference counterpart. */
+int dgb_cable_adjoint_set_wait_limit(int64_t polls);
+
 /* sizeof(dgb_cable_adjoint_args) as compiled (for foreign-language mirrors). */
 size_t dgb_cable_adjoint_args_size(void);
 

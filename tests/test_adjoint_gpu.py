@@ -9,7 +9,7 @@ import oracle
 from dendra_gb300.adjoint import CableGradient, cable_traces
 from dendra_gb300.cable import CablePopulation
 from dendra_gb300.workloads import RHOE_OHM_CM
-from tests._cases import golden_adjoint_population, oracle_param_grads
+from tests._cases import golden_adjoint_population, oracle_param_grads, synthetic_population
 
 pytestmark = pytest.mark.gpu
 
@@ -180,3 +180,27 @@ def test_fast_math_float32_adjoint_tracks_the_float64_oracle(cuda):
         v = v.double().cpu().numpy()
         err = np.abs(v - ref[k]).max() / np.abs(ref[k]).max()
         assert err <= 5e-3, (k, err)
+
+
+def test_tape_stage_wait_timeout_surfaces(cuda):
+    """A tape-stage wait limited to zero polls gives up at once: each warp
+    drains its posted copies at the full limit, sets error bit 4 and ends;
+    backward() raises, and with the default restored the same gradient comes
+    out on the same context.  The copies are real, in-bounds bulk loads:
+    nothing faults or hangs."""
+    from dendra_gb300 import _lib
+
+    L = _lib.load()
+    pop = synthetic_population(7, 64, 51, 201, torch.float32, cuda, fast_math=True)
+    run = CableGradient(pop, 200, rec_idx=0, checkpoint_every=100, tune=False)
+    g = torch.ones_like(run.forward())
+    want = run.backward(g)
+    try:
+        assert L.dgb_cable_adjoint_set_wait_limit(0) == 0
+        with pytest.raises(RuntimeError, match="error bits 0x4"):
+            run.backward(g)
+    finally:
+        assert L.dgb_cable_adjoint_set_wait_limit(-1) == 0
+    got = run.backward(g)
+    for k in want:
+        torch.testing.assert_close(got[k], want[k], rtol=0, atol=0)
