@@ -6,7 +6,8 @@ implicit.py:364-440).  Here each knob is a parameter of the C ABI and is
 chosen by timing the candidates on the device:
 
 * cables per CTA of the persistent cable kernels (``dgb_cable_args.
-  warps_per_block``: 1, 2 or 4) and the persistent run's Thomas/PCR split
+  warps_per_block``: 1, 2 or 4), the split-gate run (``DGB_CABLE_SPLIT_GATES``:
+  one cable on 4 warps) and the persistent run's Thomas/PCR split
   (``lanes_mode``/``n_lanes32``/``n_lanes16``: short cables on 8 or 16 lanes,
   i.e. longer sequential chunks and fewer PCR stages) — ``tune_cable_run``;
 * the Thomas-versus-PCR split of the chunked tridiagonal solve (lanes per
