@@ -266,8 +266,11 @@ typedef struct dgb_cable_args {
      [1] error bits after the run (0 = every cable advanced) */
   int32_t* scratch;
   /* launch tuning of the persistent kernels (dgb_cable_run, _taped, _adjoint):
-     cables in flight per CTA, 1, 2 or 4 (0 = 4); halved while the CTA's
-     shared memory would exceed 227 KB.  The autotuner's knob. */
+     cables in flight per CTA, 1, 2 or 4, halved while the CTA's shared
+     memory would exceed 227 KB.  0 = the library's choice: 4, narrowed while
+     the population has fewer CTAs than the device has SMs; for dgb_cable_run
+     and _taped, with lanes_mode 0 and at most one cable per SM, the
+     split-gate run (DGB_CABLE_SPLIT_GATES).  The autotuner's knob. */
   int32_t warps_per_block;
   /* raster (Raster / APCount / threshold_crossing at callbacks.py:2114,
      _threshold_callbacks.py:50-53): n_rast (0..4) checked compartments per
